@@ -1,0 +1,286 @@
+#!/usr/bin/env python
+"""Benchmark: network Fisher matrices per second on one GB300 (and SNR/s).
+
+Workload (default): 10^4 BBH events, IMRPhenomD, network L1 + H1 (fmin 10 Hz) + ET
+triangle at Sardinia (5 Hz wall), Earth rotation on, 2000 log-spaced frequency points
+per event and detector, analytic aLIGO PSD fit.  One step = the network Fisher matrix
+(11x11, summed over detectors and arms) of every event.
+
+value: events / s with the event arrays resident in HBM, CUDA-event timed per step
+(L2 flushed by a 256 MB write before each step, outside the timed interval).
+e2e:   the same through the public API (DetNet.FisherMatr on a host events dict),
+       wall-clock, host->device copy of the parameters and device->host copy of the
+       Fisher matrices included.
+Multi-GPU: one replica per GPU on its own seeded shard (events are independent; no
+collective), value = all ranks' events / max-over-ranks time.
+
+--impl reference: the CPU float64 oracle restatement of gwfast's algorithm (gwfast
+itself needs jax[cpu], which is not installable here) on a bounded sample of the same
+workload, on all host cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_EVENTS = 10000
+RES = 2000
+METRIC = 'network Fisher matrices/s (IMRPhenomD, L1+H1+ETS, Earth rotation, R=2000)'
+
+
+def dist_info():
+    return int(os.environ.get('RANK', 0)), int(os.environ.get('WORLD_SIZE', 1)), int(os.environ.get('LOCAL_RANK', 0))
+
+
+def cpu_sample(n_events, res, threads, seed=1001):
+    """Time the oracle (torch float64 on the CPU) on a sample of the workload's events."""
+    import torch
+    import oracle as O
+    from gwfast_gb300 import synthetic
+    torch.set_num_threads(threads)
+    ev = synthetic.bbh_events(n_events, seed=seed)
+    p = O.to_params(ev)
+    dets = []
+    for name, fmin in synthetic.NETWORK_LHET:
+        spec = synthetic.detector_spec(name, fmin)
+        f, S = spec['psd_path']
+        dets.append(O.Detector(spec['det_lat'], spec['det_long'], spec['det_xax'], spec['detector_shape'],
+                               fmin=fmin, psd_f=f, psd_S=S, earth=True))
+    m = O.Model('PhenomD')
+    t0 = time.perf_counter()
+    O.network_fisher(dets, m, p, res)
+    tf = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.network_snr(dets, m, p, res)
+    ts = time.perf_counter() - t0
+    return n_events / tf, n_events / ts
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    n_sample = args.ref_events
+    vals, svals = [], []
+    for _ in range(args.warmup):
+        cpu_sample(max(1, n_sample // 4), RES, threads)
+    for k in range(args.steps):
+        v, s = cpu_sample(n_sample, RES, threads, seed=1001 + k)
+        vals.append(v)
+        svals.append(s)
+    v = statistics.median(vals)
+    line = {
+        'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': 'Fisher/s', 'n_gpus': 0, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': 1e3 * n_sample / v, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+        'config': {'workload': 'IMRPhenomD BBH, L1+H1+ETS, Earth rotation, R=2000 (sample of %d events per step)'
+                   % n_sample, 'events_per_step': n_sample},
+        'snr_per_s': statistics.median(svals),
+        'cpu_baseline': {'value': v, 'unit': 'Fisher/s', 'cores': threads, 'kind': 'port',
+                         'sample': '%d events per step, all 3 detectors, R=2000' % n_sample},
+        'e2e': {'value': v, 'unit': 'Fisher/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+        'note': 'gwfast needs jax[cpu] (absent from the offline wheelhouse); the timed CPU path is the float64 '
+                'oracle restatement of its algorithm (torch on the host cores)',
+    }
+    print(json.dumps(line))
+
+
+class ClockSampler:
+    def __init__(self, device):
+        self.f = tempfile.NamedTemporaryFile('w+', suffix='.csv', delete=False)
+        q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,'
+             'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+             'clocks_event_reasons.sw_power_cap')
+        try:
+            self.p = subprocess.Popen(['nvidia-smi', '-i', str(device), '--query-gpu=' + q, '--format=csv,noheader,nounits',
+                                       '-lms', '200'], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(',')]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace('.', '').isdigit()]
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith('active')})
+        return {'sm_mhz': statistics.median(sm) if sm else None, 'sm_max_mhz': float(rows[0][2]) if rows else None,
+                'reasons': reasons, 'samples': len(rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as fh:
+            return json.load(fh)
+    except OSError:
+        return {}
+
+
+def fp64_peak(torch, dev):
+    """Dense FP64 throughput of cuBLAS DGEMM (4096^3), best of 5: the FP64 denominator."""
+    a = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    b = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    return 2 * 4096 ** 3 / best / 1e12
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=5)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=('ours', 'reference'))
+    ap.add_argument('--events', type=int, default=N_EVENTS)
+    ap.add_argument('--ref-events', type=int, default=6)
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    args = ap.parse_args()
+    if args.impl == 'reference':
+        return run_reference(args)
+    rank, world, local = dist_info()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl' if torch.cuda.is_available() else 'gloo')
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    from gwfast_gb300 import _build, _lib, synthetic
+    from gwfast_gb300 import waveforms as W
+    from gwfast_gb300.signal import event_array
+    _build.build()
+    N = args.events
+    ev = synthetic.bbh_events(N, seed=1001 + rank)
+    wf = W.IMRPhenomD()
+    net = synthetic.make_network(wf, dets=synthetic.NETWORK_LHET, earth=True, device=local)
+    sigs = list(net.signals.values())
+    ids = [s.det_id for s in sigs]
+    ctx = _lib.context(local)
+    p_host = event_array(ev)
+    p_dev = torch.from_numpy(p_host).to(dev)
+    out = torch.empty((N, 11, 11), dtype=torch.float64, device=dev)
+    snr_out = torch.empty((N,), dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    desc = wf.gpu_desc()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
+
+    def fisher_step(det_ids=ids, o=out):
+        ctx.fisher(det_ids, desc, p_dev, RES, per_arm=False, mem=_lib.MEM_DEVICE, out_net=o, stream=stream.cuda_stream,
+                   ld=N, n=N)
+
+    def snr_step():
+        ctx.snr(ids, desc, p_dev, RES, mem=_lib.MEM_DEVICE, out_net=snr_out, stream=stream.cuda_stream, ld=N, n=N)
+
+    def timed(fn, k):
+        tot = 0.0
+        for _ in range(k):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot / k
+
+    for _ in range(args.warmup):
+        fisher_step()
+        snr_step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(local)
+    ms = timed(fisher_step, args.steps)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms_snr = timed(snr_step, args.steps)
+    # dominant kernel: the ET triangle (2 computed arms) launch alone
+    ms_et = timed(lambda: fisher_step([ids[2]]), args.steps)
+    ms_l1 = timed(lambda: fisher_step([ids[0]]), args.steps)
+    if world > 1:
+        t = torch.tensor([ms, ms_snr], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms, ms_snr = float(t[0]), float(t[1])
+    # end to end through the public API with host buffers
+    for _ in range(max(1, args.warmup // 2)):
+        net.FisherMatr(dict(ev), res=RES)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        F_host = net.FisherMatr(dict(ev), res=RES)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if rank != 0:
+        torch.distributed.destroy_process_group()
+        return
+    ops = json.load(open(os.path.join(ROOT, 'profiles', 'opcounts.json')))['counts']['IMRPhenomD/earth']
+    flop_arm_pt = ops['fisher_per_arm_point']
+    flops_et = N * RES * 3 * flop_arm_pt
+    peak64 = fp64_peak(torch, dev)
+    ach = flops_et / (ms_et / 1e3) / 1e12
+    line = {
+        'metric': METRIC, 'value': world * N / (ms / 1e3), 'unit': 'Fisher/s', 'n_gpus': world, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f64', 'data': 'synthetic (seeded BBH catalogue, analytic aLIGO PSD fit)',
+        'config': {'workload': 'IMRPhenomD BBH 1e4 events, L1+H1+ETS, Earth rotation, R=2000, FP64 kernel',
+                   'events_per_gpu': N, 'res': RES, 'parallelism': 'replicas over event shards' if world > 1 else 'single',
+                   'l2': 'flushed (256 MB write) before every step'},
+        'snr_per_s': world * N / (ms_snr / 1e3),
+        'gpu_launches': 3,
+        'e2e': {'value': world * N / e2e_s, 'unit': 'Fisher/s', 'h2d_bytes_per_step': int(p_host.nbytes),
+                'd2h_bytes_per_step': int(F_host.nbytes)},
+        'roofline': {'bound': 'fp64', 'kernel': 'fisher_kernel<IMRPhenomD, earth, triangle>',
+                     'achieved': ach, 'peak': peak64, 'unit': 'TFLOP/s', 'frac': ach / peak64,
+                     'peak_source': 'cuBLAS DGEMM 4096^3 measured in this run',
+                     'algorithmic_flop_per_launch': flops_et, 'launch_ms': ms_et, 'traffic': None,
+                     'flop_model': 'profiles/opcounts.json IMRPhenomD/earth fisher_per_arm_point x 3 arms x R x N'},
+        'launch_ms': {'L1': ms_l1, 'ETS': ms_et},
+        'clocks': clocks,
+        'hbm_peak_gbs': measured_peaks().get('hbm_gbs'),
+    }
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, _ = cpu_sample(args.ref_events, RES, threads)
+        line['cpu_baseline'] = {'value': v, 'unit': 'Fisher/s', 'cores': threads, 'kind': 'port',
+                                'sample': '%d events, L1+H1+ETS, R=2000, float64 oracle (torch CPU)' % args.ref_events}
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,155 @@
+"""ctypes binding of libgwfast_gb300.so (the C ABI declared in include/gwfast_gb300.h).
+
+The library is built in-tree by ``gwfast_gb300._build.build()``.  There is no CPU
+fallback: if the library or a CUDA device is missing, every call raises.
+"""
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import _build
+
+GWF_OK = 0
+ERRORS = {-1: 'invalid argument', -2: 'CUDA error', -3: 'out of memory', -4: 'timeout', -5: 'unsupported'}
+MODEL_IDS = {'TaylorF2_RestrictedPN': 0, 'IMRPhenomD': 1, 'IMRPhenomHM': 2}
+MEM_HOST, MEM_DEVICE = 0, 1
+
+
+class GWFError(RuntimeError):
+    pass
+
+
+class DetDesc(ctypes.Structure):
+    _fields_ = [('lat_rad', ctypes.c_double), ('long_rad', ctypes.c_double), ('xax_rad', ctypes.c_double),
+                ('shape', ctypes.c_int), ('earth_rotation', ctypes.c_int), ('fmin', ctypes.c_double),
+                ('fmax', ctypes.c_double)]
+
+
+class WfDesc(ctypes.Structure):
+    _fields_ = [('model', ctypes.c_int), ('spin_ho', ctypes.c_int), ('fcut_par', ctypes.c_double)]
+
+
+_P = ctypes.POINTER
+_d = ctypes.c_double
+_i64 = ctypes.c_int64
+_vp = ctypes.c_void_p
+
+SIGNATURES = {
+    'gwf_version': ([], ctypes.c_int),
+    'gwf_last_error': ([], ctypes.c_char_p),
+    'gwf_ctx_create': ([ctypes.c_int, _P(_vp)], ctypes.c_int),
+    'gwf_ctx_destroy': ([_vp], ctypes.c_int),
+    'gwf_set_qnm_table': ([_vp, _vp, _vp, _vp, _i64], ctypes.c_int),
+    'gwf_detector_add': ([_vp, _P(DetDesc), _vp, _vp, _i64, _P(ctypes.c_int)], ctypes.c_int),
+    'gwf_snr': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32, _vp, ctypes.c_int,
+                 ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
+    'gwf_fisher': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32, _vp, ctypes.c_int,
+                    ctypes.c_int, ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
+    'gwf_cov': ([_vp, _vp, _i64, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
+}
+
+_lock = threading.Lock()
+_lib = None
+_ctxs = {}
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load (building first if needed) the CUDA library; raises if it cannot be loaded."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB
+        if not os.path.exists(path) and build_if_missing:
+            _build.build()
+        if not os.path.exists(path):
+            raise GWFError('libgwfast_gb300.so is missing; run gwfast_gb300._build.build()')
+        lib = ctypes.CDLL(path)
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = lib
+        return lib
+
+
+def check(rc):
+    if rc != GWF_OK:
+        msg = load().gwf_last_error().decode(errors='replace')
+        raise GWFError('%s: %s' % (ERRORS.get(rc, rc), msg))
+
+
+def ptr(a):
+    """Address of a numpy array, a torch tensor or an integer device pointer."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, 'data_ptr'):
+        return a.data_ptr()
+    return int(a)
+
+
+def _qnm_table():
+    here = os.path.dirname(os.path.abspath(__file__))
+    return np.ascontiguousarray(np.loadtxt(os.path.join(here, 'data', 'qnm_220.txt')).T)
+
+
+class Context:
+    """One library context (device, PSD tables, staging buffers)."""
+
+    def __init__(self, device=0):
+        lib = load()
+        h = _vp()
+        check(lib.gwf_ctx_create(int(device), ctypes.byref(h)))
+        self.h = h
+        self.device = device
+        q = _qnm_table()
+        check(lib.gwf_set_qnm_table(self.h, ptr(q[0]), ptr(q[1]), ptr(q[2]), q.shape[1]))
+        self._keep = [q]
+
+    def add_detector(self, lat_rad, long_rad, xax_rad, shape, earth, fmin, fmax, psd_f, psd_S):
+        psd_f = np.ascontiguousarray(psd_f, dtype=np.float64)
+        psd_S = np.ascontiguousarray(psd_S, dtype=np.float64)
+        d = DetDesc(lat_rad, long_rad, xax_rad, 0 if shape == 'L' else 1, int(bool(earth)), float(fmin),
+                    -1.0 if fmax is None else float(fmax))
+        out = ctypes.c_int()
+        check(load().gwf_detector_add(self.h, ctypes.byref(d), ptr(psd_f), ptr(psd_S), len(psd_f), ctypes.byref(out)))
+        return out.value
+
+    def snr(self, det_ids, wf, params, res, res_ev=None, spacing=0, mem=MEM_HOST, out_arm=None, out_net=None,
+            stream=None, ld=None, n=None):
+        ids = np.ascontiguousarray(det_ids, dtype=np.int32)
+        n = params.shape[1] if n is None else n
+        ld = (params.shape[1] if ld is None else ld)
+        check(load().gwf_snr(self.h, len(ids), ptr(ids), ctypes.byref(wf), ptr(params), ld, n, int(res),
+                             ptr(res_ev), spacing, mem, ptr(out_arm), ptr(out_net), stream))
+
+    def fisher(self, det_ids, wf, params, res, res_ev=None, spacing=0, per_arm=False, mem=MEM_HOST, out_arm=None,
+               out_net=None, stream=None, ld=None, n=None):
+        ids = np.ascontiguousarray(det_ids, dtype=np.int32)
+        n = params.shape[1] if n is None else n
+        ld = (params.shape[1] if ld is None else ld)
+        check(load().gwf_fisher(self.h, len(ids), ptr(ids), ctypes.byref(wf), ptr(params), ld, n, int(res),
+                                ptr(res_ev), spacing, int(bool(per_arm)), mem, ptr(out_arm), ptr(out_net), stream))
+
+    def cov(self, F, mem=MEM_HOST, cov=None, eps=None, cond=None, n=None, stream=None):
+        n = F.shape[0] if n is None else n
+        check(load().gwf_cov(self.h, ptr(F), n, mem, ptr(cov), ptr(eps), ptr(cond), stream))
+
+
+def context(device=0):
+    """Process-wide context for ``device`` (created on first use)."""
+    with _lock:
+        c = _ctxs.get(device)
+    if c is None:
+        c = Context(device)
+        with _lock:
+            _ctxs[device] = c
+    return c

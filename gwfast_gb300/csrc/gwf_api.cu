@@ -1,0 +1,375 @@
+// C-ABI layer: context, detector tables, staging and launches (see include/gwfast_gb300.h).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gwf_launch.h"
+#include "gwfast_gb300.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define GWF_CK(x)                                                                               \
+  do {                                                                                          \
+    cudaError_t e_ = (x);                                                                       \
+    if (e_ != cudaSuccess) return fail(GWF_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  int ensure(size_t bytes) {
+    if (bytes <= cap) return 0;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return -1;
+    cap = bytes;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+struct HostBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  int ensure(size_t bytes) {
+    if (bytes <= cap) return 0;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) return -1;
+    cap = bytes;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+struct DetRec {
+  gwf_det_desc desc;
+  double* d_f = nullptr;
+  double* d_S = nullptr;
+  int* d_acc = nullptr;
+  int n = 0, nacc = 0;
+  double l0 = 0.0, idl = 0.0;
+};
+
+}  // namespace
+
+struct gwf_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<DetRec> dets;
+  double* d_qnm = nullptr;
+  int nq = 0;
+  DevBuf par, res, oarm, onet, fin, fout, feps, fcond;
+  HostBuf hpar, hout;
+};
+
+namespace {
+
+int check_ctx(gwf_ctx* ctx) {
+  if (!ctx) return fail(GWF_ERR_INVALID_ARG, "null context");
+  GWF_CK(cudaSetDevice(ctx->device));
+  return GWF_OK;
+}
+
+int slots_of(const gwf_ctx* ctx, int n_det, const int* ids) {
+  int s = 0;
+  for (int i = 0; i < n_det; ++i) s += ctx->dets[ids[i]].desc.shape == GWF_SHAPE_T ? 3 : 1;
+  return s;
+}
+
+gwf::DetDev dev_of(const DetRec& r) {
+  gwf::DetDev d;
+  d.lat = r.desc.lat_rad;
+  d.lon = r.desc.long_rad;
+  d.xax = r.desc.xax_rad;
+  d.shape = r.desc.shape;
+  d.sin_zeta = r.desc.shape == GWF_SHAPE_T ? std::sin(M_PI / 3.0) : 1.0;
+  d.fmin = r.desc.fmin;
+  d.fmax = r.desc.fmax;
+  d.earth = r.desc.earth_rotation;
+  d.psd_f = r.d_f;
+  d.psd_S = r.d_S;
+  d.npsd = r.n;
+  d.acc = r.d_acc;
+  d.nacc = r.nacc;
+  d.acc_l0 = r.l0;
+  d.acc_idl = r.idl;
+  return d;
+}
+
+int validate_common(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params,
+                    int64_t ld, int64_t N, int32_t res, const int32_t* res_ev, int spacing, int mem) {
+  if (!det_ids || n_det < 1) return fail(GWF_ERR_INVALID_ARG, "need at least one detector");
+  for (int i = 0; i < n_det; ++i)
+    if (det_ids[i] < 0 || det_ids[i] >= (int)ctx->dets.size()) return fail(GWF_ERR_INVALID_ARG, "unknown detector id");
+  if (!wf || wf->model < 0 || wf->model > 2) return fail(GWF_ERR_INVALID_ARG, "unknown waveform model");
+  if (wf->model == GWF_WF_PHENOMD && ctx->nq < 2) return fail(GWF_ERR_INVALID_ARG, "IMRPhenomD needs the QNM table (gwf_set_qnm_table)");
+  if (!(wf->fcut_par > 0.0)) return fail(GWF_ERR_INVALID_ARG, "fcut_par must be positive");
+  if (N < 0 || (N > 0 && !params)) return fail(GWF_ERR_INVALID_ARG, "bad event array");
+  if (ld < N) return fail(GWF_ERR_INVALID_ARG, "ld must be >= n_events");
+  if (!res_ev && res < 1) return fail(GWF_ERR_INVALID_ARG, "res must be >= 1");
+  if (spacing != GWF_SPACING_GEOM && spacing != GWF_SPACING_LIN) return fail(GWF_ERR_INVALID_ARG, "bad spacing");
+  if (mem != GWF_MEM_HOST && mem != GWF_MEM_DEVICE) return fail(GWF_ERR_INVALID_ARG, "bad memory mode");
+  if (N > (int64_t)1 << 40) return fail(GWF_ERR_INVALID_ARG, "too many events");
+  return GWF_OK;
+}
+
+// stage host inputs into device buffers; returns device pointers
+int stage_inputs(gwf_ctx* ctx, const double* params, int64_t ld, int64_t N, const int32_t* res_ev, int mem,
+                 cudaStream_t st, const double** dp, int64_t* dld, const int** dres) {
+  if (mem == GWF_MEM_DEVICE) {
+    *dp = params;
+    *dld = ld;
+    *dres = res_ev;
+    return GWF_OK;
+  }
+  const size_t pb = (size_t)gwf::NP * (size_t)N * sizeof(double);
+  if (ctx->par.ensure(pb ? pb : 8)) return fail(GWF_ERR_OOM, "device allocation failed (params)");
+  if (N > 0) {
+    if (ld == N) GWF_CK(cudaMemcpyAsync(ctx->par.p, params, pb, cudaMemcpyHostToDevice, st));
+    else GWF_CK(cudaMemcpy2DAsync(ctx->par.p, N * sizeof(double), params, ld * sizeof(double), N * sizeof(double),
+                                  gwf::NP, cudaMemcpyHostToDevice, st));
+  }
+  *dp = (const double*)ctx->par.p;
+  *dld = N;
+  *dres = nullptr;
+  if (res_ev) {
+    if (ctx->res.ensure((size_t)N * sizeof(int) + 4)) return fail(GWF_ERR_OOM, "device allocation failed (res)");
+    GWF_CK(cudaMemcpyAsync(ctx->res.p, res_ev, (size_t)N * sizeof(int), cudaMemcpyHostToDevice, st));
+    *dres = (const int*)ctx->res.p;
+  }
+  return GWF_OK;
+}
+
+int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params,
+        int64_t ld, int64_t N, int32_t res, const int32_t* res_ev, int spacing, int per_arm, int mem,
+        double* out_arm, double* out_net, void* stream) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  rc = validate_common(ctx, n_det, det_ids, wf, params, ld, N, res, res_ev, spacing, mem);
+  if (rc) return rc;
+  if (!out_arm && !out_net) return fail(GWF_ERR_INVALID_ARG, "no output requested");
+  if (fisher && !per_arm) out_arm = nullptr;
+  if (fisher && per_arm && !out_arm) return fail(GWF_ERR_INVALID_ARG, "per_arm needs out_arm");
+  if (N == 0) return GWF_OK;
+  for (int i = 0; i < n_det; ++i)
+    for (int j = 0; j < N && res_ev && mem == GWF_MEM_HOST; ++j)
+      if (res_ev[j] < 1) return fail(GWF_ERR_INVALID_ARG, "res_per_event must be >= 1");
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  const double* dp;
+  int64_t dld;
+  const int* dres;
+  rc = stage_inputs(ctx, params, ld, N, res_ev, mem, st, &dp, &dld, &dres);
+  if (rc) return rc;
+  const int slots = slots_of(ctx, n_det, det_ids);
+  const size_t per = fisher ? (size_t)gwf::NP * gwf::NP : 1;
+  double* darm = nullptr;
+  double* dnet = nullptr;
+  if (mem == GWF_MEM_DEVICE) {
+    darm = out_arm;
+    dnet = out_net;
+  } else {
+    if (out_arm) {
+      if (ctx->oarm.ensure((size_t)slots * N * per * sizeof(double))) return fail(GWF_ERR_OOM, "device allocation failed (out)");
+      darm = (double*)ctx->oarm.p;
+    }
+    if (out_net) {
+      if (ctx->onet.ensure((size_t)N * per * sizeof(double))) return fail(GWF_ERR_OOM, "device allocation failed (out)");
+      dnet = (double*)ctx->onet.p;
+    }
+  }
+  gwf::LaunchArgs a;
+  a.ev.p = dp;
+  a.ev.ld = dld;
+  a.ev.N = N;
+  a.ev.n0 = 0;
+  a.ev.res = res;
+  a.ev.res_ev = dres;
+  a.ev.spacing = spacing;
+  a.wf.model = wf->model;
+  a.wf.spin_ho = wf->spin_ho;
+  a.wf.fcut_par = wf->fcut_par;
+  a.qnm = ctx->d_qnm;
+  a.nq = ctx->nq;
+  a.per_arm = per_arm;
+  a.stream = st;
+  int slot = 0;
+  for (int i = 0; i < n_det; ++i) {
+    const DetRec& r = ctx->dets[det_ids[i]];
+    a.det = dev_of(r);
+    a.out_arm = darm ? darm + (size_t)slot * N * per : nullptr;
+    a.out_det = dnet;
+    a.accum = i > 0;
+    cudaError_t err;
+    if (fisher) err = wf->model == 0 ? gwf::launch_fisher_m0(a) : (wf->model == 1 ? gwf::launch_fisher_m1(a) : gwf::launch_fisher_m2(a));
+    else err = wf->model == 0 ? gwf::launch_snr_m0(a) : (wf->model == 1 ? gwf::launch_snr_m1(a) : gwf::launch_snr_m2(a));
+    if (err != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(err));
+    slot += r.desc.shape == GWF_SHAPE_T ? 3 : 1;
+  }
+  if (mem == GWF_MEM_HOST) {
+    if (out_arm) GWF_CK(cudaMemcpyAsync(out_arm, darm, (size_t)slots * N * per * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (out_net) GWF_CK(cudaMemcpyAsync(out_net, dnet, (size_t)N * per * sizeof(double), cudaMemcpyDeviceToHost, st));
+    GWF_CK(cudaStreamSynchronize(st));
+  }
+  return GWF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gwf_version(void) { return 1; }
+
+const char* gwf_last_error(void) { return g_err.c_str(); }
+
+int gwf_ctx_create(int device, gwf_ctx** out) {
+  if (!out) return fail(GWF_ERR_INVALID_ARG, "null output pointer");
+  int ndev = 0;
+  GWF_CK(cudaGetDeviceCount(&ndev));
+  if (device < 0 || device >= ndev) return fail(GWF_ERR_INVALID_ARG, "no such CUDA device");
+  GWF_CK(cudaSetDevice(device));
+  gwf_ctx* c = new gwf_ctx();
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return fail(GWF_ERR_CUDA, "stream creation failed");
+  }
+  *out = c;
+  return GWF_OK;
+}
+
+int gwf_ctx_destroy(gwf_ctx* ctx) {
+  if (!ctx) return GWF_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& r : ctx->dets) {
+    cudaFree(r.d_f);
+    cudaFree(r.d_S);
+    cudaFree(r.d_acc);
+  }
+  cudaFree(ctx->d_qnm);
+  ctx->par.release(); ctx->res.release(); ctx->oarm.release(); ctx->onet.release();
+  ctx->fin.release(); ctx->fout.release(); ctx->feps.release(); ctx->fcond.release();
+  ctx->hpar.release(); ctx->hout.release();
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return GWF_OK;
+}
+
+int gwf_set_qnm_table(gwf_ctx* ctx, const double* spin, const double* fring, const double* fdamp, int64_t n) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!spin || !fring || !fdamp || n < 2 || n > (1 << 24)) return fail(GWF_ERR_INVALID_ARG, "bad QNM table");
+  for (int64_t i = 1; i < n; ++i)
+    if (!(spin[i] > spin[i - 1])) return fail(GWF_ERR_INVALID_ARG, "QNM spin grid must be strictly increasing");
+  std::vector<double> h(3 * n);
+  std::memcpy(h.data(), spin, n * sizeof(double));
+  std::memcpy(h.data() + n, fring, n * sizeof(double));
+  std::memcpy(h.data() + 2 * n, fdamp, n * sizeof(double));
+  cudaFree(ctx->d_qnm);
+  ctx->d_qnm = nullptr;
+  GWF_CK(cudaMalloc(&ctx->d_qnm, 3 * n * sizeof(double)));
+  GWF_CK(cudaMemcpy(ctx->d_qnm, h.data(), 3 * n * sizeof(double), cudaMemcpyHostToDevice));
+  ctx->nq = (int)n;
+  return GWF_OK;
+}
+
+int gwf_detector_add(gwf_ctx* ctx, const gwf_det_desc* desc, const double* psd_f, const double* psd_S, int64_t n,
+                     int* det_id) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!desc || !psd_f || !psd_S || !det_id) return fail(GWF_ERR_INVALID_ARG, "null argument");
+  if (desc->shape != GWF_SHAPE_L && desc->shape != GWF_SHAPE_T) return fail(GWF_ERR_INVALID_ARG, "Enter valid detector configuration");
+  if (n < 2 || n > (1 << 28)) return fail(GWF_ERR_INVALID_ARG, "PSD table needs at least two rows");
+  if (!(desc->fmin > 0.0)) return fail(GWF_ERR_INVALID_ARG, "fmin must be positive");
+  for (int64_t i = 0; i < n; ++i) {
+    if (!(psd_f[i] > 0.0)) return fail(GWF_ERR_INVALID_ARG, "PSD frequencies must be positive");
+    if (i && !(psd_f[i] > psd_f[i - 1])) return fail(GWF_ERR_INVALID_ARG, "PSD frequencies must be strictly increasing");
+  }
+  DetRec r;
+  r.desc = *desc;
+  r.n = (int)n;
+  r.nacc = 4096;
+  r.l0 = std::log(psd_f[0]);
+  const double l1 = std::log(psd_f[n - 1]);
+  r.idl = r.nacc / (l1 - r.l0);
+  std::vector<int> acc(r.nacc);
+  int64_t j = 0;
+  for (int b = 0; b < r.nacc; ++b) {
+    const double fb = std::exp(r.l0 + b / r.idl);
+    while (j + 1 < n - 1 && psd_f[j + 1] <= fb) ++j;
+    acc[b] = (int)j;
+  }
+  GWF_CK(cudaMalloc(&r.d_f, n * sizeof(double)));
+  GWF_CK(cudaMalloc(&r.d_S, n * sizeof(double)));
+  GWF_CK(cudaMalloc(&r.d_acc, r.nacc * sizeof(int)));
+  GWF_CK(cudaMemcpy(r.d_f, psd_f, n * sizeof(double), cudaMemcpyHostToDevice));
+  GWF_CK(cudaMemcpy(r.d_S, psd_S, n * sizeof(double), cudaMemcpyHostToDevice));
+  GWF_CK(cudaMemcpy(r.d_acc, acc.data(), r.nacc * sizeof(int), cudaMemcpyHostToDevice));
+  ctx->dets.push_back(r);
+  *det_id = (int)ctx->dets.size() - 1;
+  return GWF_OK;
+}
+
+int gwf_snr(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params, int64_t ld,
+            int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int mem, double* out_arm,
+            double* out_net, void* stream) {
+  return run(ctx, false, n_det, det_ids, wf, params, ld, n_events, res, res_per_event, spacing, 0, mem, out_arm,
+             out_net, stream);
+}
+
+int gwf_fisher(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params, int64_t ld,
+               int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int per_arm, int mem,
+               double* out_arm, double* out_net, void* stream) {
+  return run(ctx, true, n_det, det_ids, wf, params, ld, n_events, res, res_per_event, spacing, per_arm, mem, out_arm,
+             out_net, stream);
+}
+
+int gwf_cov(gwf_ctx* ctx, const double* F, int64_t N, int mem, double* cov, double* eps, double* cond, void* stream) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (N < 0 || (N > 0 && (!F || !cov))) return fail(GWF_ERR_INVALID_ARG, "bad covariance arguments");
+  if (mem != GWF_MEM_HOST && mem != GWF_MEM_DEVICE) return fail(GWF_ERR_INVALID_ARG, "bad memory mode");
+  if (N == 0) return GWF_OK;
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  const size_t mb = (size_t)N * 121 * sizeof(double);
+  if (mem == GWF_MEM_DEVICE) {
+    cudaError_t e = gwf::launch_cov(F, N, cov, eps, cond, st);
+    if (e != cudaSuccess) return fail(GWF_ERR_CUDA, cudaGetErrorString(e));
+    return GWF_OK;
+  }
+  if (ctx->fin.ensure(mb) || ctx->fout.ensure(mb) || ctx->feps.ensure(N * sizeof(double)) ||
+      ctx->fcond.ensure(N * sizeof(double)))
+    return fail(GWF_ERR_OOM, "device allocation failed (cov)");
+  GWF_CK(cudaMemcpyAsync(ctx->fin.p, F, mb, cudaMemcpyHostToDevice, st));
+  cudaError_t e = gwf::launch_cov((const double*)ctx->fin.p, N, (double*)ctx->fout.p, (double*)ctx->feps.p,
+                                  (double*)ctx->fcond.p, st);
+  if (e != cudaSuccess) return fail(GWF_ERR_CUDA, cudaGetErrorString(e));
+  GWF_CK(cudaMemcpyAsync(cov, ctx->fout.p, mb, cudaMemcpyDeviceToHost, st));
+  if (eps) GWF_CK(cudaMemcpyAsync(eps, ctx->feps.p, N * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (cond) GWF_CK(cudaMemcpyAsync(cond, ctx->fcond.p, N * sizeof(double), cudaMemcpyDeviceToHost, st));
+  GWF_CK(cudaStreamSynchronize(st));
+  return GWF_OK;
+}
+
+}  // extern "C"

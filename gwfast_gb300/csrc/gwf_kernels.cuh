@@ -1,0 +1,570 @@
+// Fused SNR and Fisher kernels: one CTA per (event, detector).
+//
+// Per frequency point a thread evaluates the waveform and its analytic tangent, the
+// detector projection (with Earth rotation when enabled) and the 11 complex
+// derivatives of the strain; the overall factor exp(i(2 pi f tcoal + phiL - Phicoal))
+// is common to every derivative and cancels in Re<d_a h|d_b h>, so it is never formed.
+// Each warp stages its 32 points' weighted derivatives in shared memory and the lanes
+// accumulate the upper triangle of the 11x11 Gram matrix; the four warps are summed at
+// the end.  Reference: gwfast/signal.py:658-777 (SNR), :782-1098 (Fisher),
+// :1303-1584 (closed-form extrinsic derivatives, which are exact derivatives).
+#pragma once
+#include "gwf_model.cuh"
+
+namespace gwf {
+
+constexpr int kThreads = 128;
+constexpr int kWarps = kThreads / 32;
+constexpr int NP = 11;    // Fisher parameters
+constexpr int NE = 66;    // upper-triangle entries
+// Fisher order: Mc, eta, dL, theta, phi, iota, psi, tcoal, Phicoal, chi1z, chi2z
+enum { I_MC = 0, I_ETA, I_DL, I_TH, I_PH, I_IO, I_PS, I_TC, I_PC, I_C1, I_C2 };
+
+struct DetDev {
+  double lat, lon, xax;  // radians
+  double sin_zeta;       // sine of the angle between the arms
+  double fmin, fmax;     // fmax <= 0 means none
+  int shape;             // 0 = L, 1 = triangle
+  int earth;             // Earth rotation
+  const double* psd_f;
+  const double* psd_S;
+  int npsd;
+  const int* acc;        // log-frequency bin -> table index (accelerates the PSD lookup)
+  int nacc;
+  double acc_l0, acc_idl;
+};
+
+struct EvBatch {
+  const double* p;       // parameters, [11][ld] (Fisher order)
+  long long ld;
+  long long N;
+  long long n0;          // first event of this launch
+  int res;
+  const int* res_ev;     // optional per-event grid length
+  int spacing;           // 0 = geometric, 1 = linear
+};
+
+struct WfDesc {
+  int model;             // 0 = TaylorF2, 1 = IMRPhenomD, 2 = IMRPhenomHM
+  int spin_ho;
+  double fcut_par;       // TaylorF2: fHigh in Hz; IMR: cut in Mf
+};
+
+static __constant__ unsigned char kPairA[NE] = {0,0,0,0,0,0,0,0,0,0,0,1,1,1,1,1,1,1,1,1,1,2,2,2,2,2,2,2,2,2,3,3,3,3,3,3,3,3,4,4,4,4,4,4,4,5,5,5,5,5,5,6,6,6,6,6,7,7,7,7,8,8,8,9,9,10};
+static __constant__ unsigned char kPairB[NE] = {0,1,2,3,4,5,6,7,8,9,10,1,2,3,4,5,6,7,8,9,10,2,3,4,5,6,7,8,9,10,3,4,5,6,7,8,9,10,4,5,6,7,8,9,10,5,6,7,8,9,10,6,7,8,9,10,7,8,9,10,8,9,10,9,10,10};
+
+struct cd { double re, im; };
+__device__ __forceinline__ cd cmul(cd a, cd b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+__device__ __forceinline__ cd cadd(cd a, cd b) { return {a.re + b.re, a.im + b.im}; }
+__device__ __forceinline__ cd cscale(cd a, double s) { return {a.re * s, a.im * s}; }
+__device__ __forceinline__ cd cmuli(cd a) { return {-a.im, a.re}; }  // i * a
+
+// np.interp(f, psd_f, psd_S, left=1, right=1) (gwfast/signal.py:723, :901)
+__device__ __forceinline__ double psd_at(const DetDev& d, double f, double lnf) {
+  const double* xf = d.psd_f;
+  const int n = d.npsd;
+  if (!(f >= xf[0]) || f > xf[n - 1]) return 1.0;
+  int b = (int)((lnf - d.acc_l0) * d.acc_idl);
+  b = b < 0 ? 0 : (b >= d.nacc ? d.nacc - 1 : b);
+  int j = d.acc[b];
+  while (j > 0 && xf[j] > f) --j;
+  while (j < n - 2 && xf[j + 1] <= f) ++j;
+  const double x0 = xf[j], x1 = xf[j + 1];
+  const double y0 = d.psd_S[j], y1 = d.psd_S[j + 1];
+  return y0 + (f - x0) * ((y1 - y0) / (x1 - x0));
+}
+
+// ------------------------------------------------------------------ per-event shared state
+struct GridEv {
+  double fmin, fcut, lnfmin, delta, fac_w, w0, wl;  // geometric: delta = ln step
+  double df;                                         // linear
+  int R;
+  int ok;
+};
+
+// pattern-function constants of one event seen by one detector (gwfast/signal.py:342-387)
+struct ProjEv {
+  double c2p, s2p;               // cos/sin 2 psi
+  double cp, ci, dcp, dci;       // (1+cos^2 i)/2, cos i and d/diota
+  double KA1[3], KA2[2], KB1[2], KB2[2];     // x-harmonic coefficients
+  double dKA1[3], dKA2[2], dKB1[2], dKB2[2]; // their d/d(dec)
+  double s2g[2], c2g[2];         // per computed arm
+  double Rc, cdcl, sdsl, sdcl, cdsl;  // Earth-centre delay pieces
+  double u0;                     // lon - ra (plus 2 pi t added per point)
+  double tc, dL;
+};
+
+// pattern functions and their partial derivatives for one arm
+struct ArmPat {
+  double Fp, Fc;
+  double Fp_x, Fc_x;   // d/dx, x = ra - lon - 2 pi t
+  double Fp_d, Fc_d;   // d/d(dec) at fixed x
+  double Fp_s, Fc_s;   // d/dpsi
+};
+
+struct TimeState {
+  double D, D_th, D_ph, D_t;  // Earth-centre delay (s) and its derivatives (t in days)
+  double x;
+};
+
+__device__ __forceinline__ void proj_setup(ProjEv& pj, const DetDev& d, double theta, double phi, double iota,
+                                           double psi, double tc, double dL) {
+  const double dec = 0.5 * kPi - theta;
+  double sd, cdd, s2d, c2d, s2ps, c2ps, si, ci;
+  sincos(dec, &sd, &cdd);
+  sincos(2.0 * dec, &s2d, &c2d);
+  sincos(2.0 * psi, &s2ps, &c2ps);
+  sincos(iota, &si, &ci);
+  pj.c2p = c2ps; pj.s2p = s2ps;
+  pj.cp = 0.5 * (1.0 + ci * ci); pj.ci = ci;
+  pj.dcp = -ci * si; pj.dci = -si;
+  double sl, cl, s2l, c2l;
+  sincos(d.lat, &sl, &cl);
+  sincos(2.0 * d.lat, &s2l, &c2l);
+  // a = s2g*A1 + c2g*A2 ; b = c2g*B1 + s2g*B2 with
+  // A1 = KA1[0] cos2x + KA1[1] cos x + KA1[2];  A2 = KA2[0] sin2x + KA2[1] sin x
+  // B1 = KB1[0] cos2x + KB1[1] cos x;           B2 = KB2[0] sin2x + KB2[1] sin x
+  pj.KA1[0] = 0.0625 * (3.0 - c2l) * (3.0 - c2d);  pj.dKA1[0] = 0.0625 * (3.0 - c2l) * 2.0 * s2d;
+  pj.KA1[1] = 0.25 * s2l * s2d;                    pj.dKA1[1] = 0.25 * s2l * 2.0 * c2d;
+  pj.KA1[2] = 0.75 * cl * cl * cdd * cdd;          pj.dKA1[2] = -0.75 * cl * cl * s2d;
+  pj.KA2[0] = -0.25 * sl * (3.0 - c2d);            pj.dKA2[0] = -0.25 * sl * 2.0 * s2d;
+  pj.KA2[1] = -0.5 * cl * s2d;                     pj.dKA2[1] = -0.5 * cl * 2.0 * c2d;
+  pj.KB1[0] = sl * sd;                             pj.dKB1[0] = sl * cdd;
+  pj.KB1[1] = cl * cdd;                            pj.dKB1[1] = -cl * sd;
+  pj.KB2[0] = 0.25 * (3.0 - c2l) * sd;             pj.dKB2[0] = 0.25 * (3.0 - c2l) * cdd;
+  pj.KB2[1] = 0.5 * s2l * cdd;                     pj.dKB2[1] = -0.5 * s2l * sd;
+  for (int a = 0; a < 2; ++a) {
+    const double g = d.xax + a * (kPi / 3.0);      // arms rotated by 0 and 60 degrees
+    sincos(2.0 * g, &pj.s2g[a], &pj.c2g[a]);
+  }
+  pj.Rc = kREarth / kClight;
+  pj.cdcl = cdd * cl; pj.sdsl = sd * sl; pj.sdcl = sd * cl; pj.cdsl = cdd * sl;
+  pj.u0 = d.lon - phi;
+  pj.tc = tc;
+  pj.dL = dL;
+}
+
+// Earth-centre delay at time tn (days) and x at the detector time (gwfast/signal.py:401-423, :444-453)
+__device__ __forceinline__ void time_state(const ProjEv& pj, double tn, TimeState& ts) {
+  double su, cu;
+  sincos(pj.u0 + kTwoPi * tn, &su, &cu);  // u = lon + 2 pi t - ra
+  ts.D = -pj.Rc * (pj.cdcl * cu + pj.sdsl);
+  ts.D_th = pj.Rc * (pj.cdsl - pj.sdcl * cu);
+  ts.D_ph = -pj.Rc * pj.cdcl * su;
+  ts.D_t = kTwoPi * pj.Rc * pj.cdcl * su;
+  ts.x = -(pj.u0 + kTwoPi * tn) - kTwoPi * ts.D / kDay;
+}
+
+__device__ __forceinline__ void arm_pattern(const ProjEv& pj, double sz, double x, int arm, ArmPat& ap) {
+  double sx, cx;
+  sincos(x, &sx, &cx);
+  const double s2x = 2.0 * sx * cx, c2x = cx * cx - sx * sx;
+  const double A1 = pj.KA1[0] * c2x + pj.KA1[1] * cx + pj.KA1[2];
+  const double A2 = pj.KA2[0] * s2x + pj.KA2[1] * sx;
+  const double B1 = pj.KB1[0] * c2x + pj.KB1[1] * cx;
+  const double B2 = pj.KB2[0] * s2x + pj.KB2[1] * sx;
+  const double A1x = -2.0 * pj.KA1[0] * s2x - pj.KA1[1] * sx;
+  const double A2x = 2.0 * pj.KA2[0] * c2x + pj.KA2[1] * cx;
+  const double B1x = -2.0 * pj.KB1[0] * s2x - pj.KB1[1] * sx;
+  const double B2x = 2.0 * pj.KB2[0] * c2x + pj.KB2[1] * cx;
+  const double A1d = pj.dKA1[0] * c2x + pj.dKA1[1] * cx + pj.dKA1[2];
+  const double A2d = pj.dKA2[0] * s2x + pj.dKA2[1] * sx;
+  const double B1d = pj.dKB1[0] * c2x + pj.dKB1[1] * cx;
+  const double B2d = pj.dKB2[0] * s2x + pj.dKB2[1] * sx;
+  const double s2g = pj.s2g[arm], c2g = pj.c2g[arm];
+  const double a = s2g * A1 + c2g * A2, b = c2g * B1 + s2g * B2;
+  const double ax = s2g * A1x + c2g * A2x, bx = c2g * B1x + s2g * B2x;
+  const double ad = s2g * A1d + c2g * A2d, bd = c2g * B1d + s2g * B2d;
+  const double c2p = pj.c2p, s2p = pj.s2p;
+  ap.Fp = sz * (a * c2p + b * s2p);    ap.Fc = sz * (b * c2p - a * s2p);
+  ap.Fp_x = sz * (ax * c2p + bx * s2p); ap.Fc_x = sz * (bx * c2p - ax * s2p);
+  ap.Fp_d = sz * (ad * c2p + bd * s2p); ap.Fc_d = sz * (bd * c2p - ad * s2p);
+  ap.Fp_s = 2.0 * sz * (b * c2p - a * s2p); ap.Fc_s = 2.0 * sz * (-b * s2p - a * c2p);
+}
+
+// strain derivatives of one arm, without the common phase factor.
+// hp = P, hc = i C; dP[k], dC[k] are the intrinsic tangents (k = Mc, eta, chi1, chi2),
+// dPi/dCi the iota derivatives; dtn[k] = d t_noloc / d theta_k (days).
+__device__ __forceinline__ void arm_derivs(const ProjEv& pj, const ArmPat& ap, const TimeState& ts, double f,
+                                           cd P, cd C, const cd* dP, const cd* dC, cd dPi, cd dCi,
+                                           const double* dtn, cd* out) {
+  const cd hp = P, hc = cmuli(C);
+  const cd H = cadd(cscale(hp, ap.Fp), cscale(hc, ap.Fc));
+  const cd iH = cmuli(H);
+  const double tpf = kTwoPi * f;
+  const double G = 1.0 + ts.D_t / kDay;                        // d t / d t_noloc
+  // chain through x = ra - lon - 2 pi t and dec = pi/2 - theta
+  const double x_th = -kTwoPi * ts.D_th / kDay;
+  const double x_ph = 1.0 - kTwoPi * ts.D_ph / kDay;
+  const double x_tc = -kTwoPi * G;
+  const cd hx = cadd(cscale(hp, ap.Fp_x), cscale(hc, ap.Fc_x)); // d(h)/dx at fixed waveform
+  const cd hd = cadd(cscale(hp, ap.Fp_d), cscale(hc, ap.Fc_d)); // d(h)/d(dec)
+  const int map[4] = {I_MC, I_ETA, I_C1, I_C2};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    cd v = cadd(cscale(cmuli(dC[k]), ap.Fc), cscale(dP[k], ap.Fp));
+    if (dtn[k] != 0.0) {
+      v = cadd(v, cscale(hx, -kTwoPi * G * dtn[k]));
+      v = cadd(v, cscale(iH, tpf * ts.D_t * dtn[k]));
+    }
+    out[map[k]] = v;
+  }
+  out[I_IO] = cadd(cscale(dPi, ap.Fp), cscale(cmuli(dCi), ap.Fc));
+  out[I_DL] = cscale(H, -1.0 / pj.dL);
+  out[I_TH] = cadd(cadd(cscale(hx, x_th), cscale(hd, -1.0)), cscale(iH, tpf * ts.D_th));
+  out[I_PH] = cadd(cscale(hx, x_ph), cscale(iH, tpf * ts.D_ph));
+  out[I_PS] = cadd(cscale(hp, ap.Fp_s), cscale(hc, ap.Fc_s));
+  out[I_TC] = cscale(cadd(cscale(hx, x_tc), cscale(iH, tpf * (kDay + ts.D_t))), 1.0 / kDay);
+  out[I_PC] = cscale(iH, -1.0);
+}
+
+// ------------------------------------------------------------------ event setup (one thread)
+union EvUnion {
+  TF2Ev tf2;
+  PhdEv phd;
+  HMEv hm;
+};
+
+__device__ inline bool grid_setup(GridEv& g, const DetDev& d, const EvBatch& ev, const WfDesc& wf, long long n,
+                                  double Mc, double eta) {
+  double fcut = (wf.model == 0) ? wf.fcut_par / (Mc / pow(eta, 0.6)) : wf.fcut_par / (Mc * kG3 / pow(eta, 0.6));
+  if (d.fmax > 0.0 && fcut > d.fmax) fcut = d.fmax;
+  const int R = ev.res_ev ? ev.res_ev[n] : ev.res;
+  g.R = R;
+  g.fmin = d.fmin;
+  g.fcut = fcut;
+  g.lnfmin = log(d.fmin);
+  if (R < 2 || !(fcut > 0.0)) { g.ok = 0; return false; }
+  g.ok = 1;
+  if (ev.spacing == 0) {
+    g.delta = (log(fcut) - g.lnfmin) / (R - 1);
+    g.fac_w = sinh(g.delta);
+    g.w0 = 0.5 * expm1(g.delta);
+    g.wl = -0.5 * expm1(-g.delta);
+  } else {
+    g.df = (fcut - d.fmin) / (R - 1);
+  }
+  return true;
+}
+
+// frequency, log-frequency and trapezoid weight of point k (numpy geomspace/linspace + trapz)
+__device__ __forceinline__ void grid_point(const GridEv& g, int spacing, int k, double& f, double& lnf, double& w) {
+  if (spacing == 0) {
+    if (k == g.R - 1) { f = g.fcut; lnf = log(f); w = f * g.wl; }
+    else {
+      lnf = g.lnfmin + k * g.delta;
+      f = (k == 0) ? g.fmin : exp(lnf);
+      w = (k == 0) ? f * g.w0 : f * g.fac_w;
+    }
+  } else {
+    f = (k == g.R - 1) ? g.fcut : g.fmin + k * g.df;
+    lnf = log(f);
+    w = (k == 0 || k == g.R - 1) ? 0.5 * g.df : g.df;
+  }
+}
+
+template <int MODEL>
+__device__ inline void event_setup(EvUnion& E, const DetDev& d, const WfDesc& wf, const double* q, int nq,
+                                   double Mc, double eta, double chi1, double chi2, double dL) {
+  const D4 mc = D4::seed(Mc, P_MC), et = D4::seed(eta, P_ETA), c1 = D4::seed(chi1, P_CHI1), c2 = D4::seed(chi2, P_CHI2);
+  if (MODEL == 0) tf2_setup(E.tf2, mc, et, c1, c2, dL, wf.spin_ho != 0);
+  else if (MODEL == 1) phd_setup(E.phd, mc, et, c1, c2, dL, d.fmin, q, q + nq, q + 2 * nq, nq);
+  else hm_setup_core(E.hm, mc, et, c1, c2, dL, d.fmin);
+}
+
+// waveform at one point: P, C (hp = P, hc = i C) with tangents, iota derivatives, and tau_star tangent.
+template <int MODEL, bool EARTH>
+__device__ __forceinline__ void wave_point_dual(const EvUnion& E, const ProjEv& pj, double f, double lnf,
+                                                cd& P, cd& C, cd* dP, cd* dC, cd& dPi, cd& dCi, D4& tau) {
+  if (MODEL == 2) {
+    Cplx<D4> Pd, Cd;
+    Cplx<double> dPv, dCv;
+    hm_point<D4>(E.hm, f, Pd, Cd, dPv, dCv);
+    P = {Pd.re.v, Pd.im.v}; C = {Cd.re.v, Cd.im.v};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { dP[k] = {Pd.re.d[k], Pd.im.d[k]}; dC[k] = {Cd.re.d[k], Cd.im.d[k]}; }
+    dPi = {dPv.re, dPv.im}; dCi = {dCv.re, dCv.im};
+    if (EARTH) tau = tau_star_point<D4>(E.hm.k.Ms, E.hm.k.vM, E.hm.k.eta, exp(lnf / 3.0));
+  } else {
+    D4 A, Phi;
+    if (MODEL == 0) {
+      const double f13 = exp(lnf / 3.0);
+      tf2_point<D4>(E.tf2, f, f13, lnf, exp(lnf * (-7.0 / 6.0)), A, Phi);
+      if (EARTH) tau = tau_star_point<D4>(E.tf2.Ms, E.tf2.vM, E.tf2.eta, f13);
+    } else {
+      phd_point<D4>(E.phd.k, f, A, Phi);
+      if (EARTH) tau = tau_star_point<D4>(E.phd.k.Ms, E.phd.k.vM, E.phd.k.eta, exp(lnf / 3.0));
+    }
+    // W = A e^{-i Phi} with the common phase dropped: value A, tangent dA - i A dPhi
+    P = {pj.cp * A.v, 0.0};
+    C = {pj.ci * A.v, 0.0};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const cd dW = {A.d[k], -A.v * Phi.d[k]};
+      dP[k] = cscale(dW, pj.cp);
+      dC[k] = cscale(dW, pj.ci);
+    }
+    dPi = {pj.dcp * A.v, 0.0};
+    dCi = {pj.dci * A.v, 0.0};
+  }
+}
+
+// value-only waveform for the SNR: |hp|, |hc| (HM) or A (22-mode)
+template <int MODEL, bool EARTH>
+__device__ __forceinline__ void wave_point_val(const EvUnion& E, const ProjEv& pj, double f, double lnf,
+                                               double& ap, double& ac, double& tau) {
+  if (MODEL == 2) {
+    Cplx<double> Pd, Cd, dPv, dCv;
+    hm_point<double>(E.hm, f, Pd, Cd, dPv, dCv);
+    ap = sqrt(Pd.re * Pd.re + Pd.im * Pd.im);
+    ac = sqrt(Cd.re * Cd.re + Cd.im * Cd.im);
+    if (EARTH) tau = tau_star_point<double>(E.hm.k.Ms, E.hm.k.vM, E.hm.k.eta, exp(lnf / 3.0));
+  } else {
+    double A, Phi;
+    if (MODEL == 0) {
+      const double f13 = exp(lnf / 3.0);
+      tf2_point<double>(E.tf2, f, f13, lnf, exp(lnf * (-7.0 / 6.0)), A, Phi);
+      if (EARTH) tau = tau_star_point<double>(E.tf2.Ms, E.tf2.vM, E.tf2.eta, f13);
+    } else {
+      phd_point<double>(E.phd.k, f, A, Phi);
+      if (EARTH) tau = tau_star_point<double>(E.phd.k.Ms, E.phd.k.vM, E.phd.k.eta, exp(lnf / 3.0));
+    }
+    ap = A * pj.cp;
+    ac = A * pj.ci;
+  }
+}
+
+template <int MODEL>
+__device__ inline void block_setup(EvUnion& E, ProjEv& pj, GridEv& g, const EvBatch& ev, const DetDev& det,
+                                   const WfDesc& wf, const double* qnm, int nq, long long n) {
+  const double* p = ev.p;
+  const long long ld = ev.ld;
+  if (threadIdx.x == 0) {
+    const double Mc = p[0 * ld + n], eta = p[1 * ld + n], dL = p[2 * ld + n];
+    const double th = p[3 * ld + n], ph = p[4 * ld + n], io = p[5 * ld + n], ps = p[6 * ld + n];
+    const double tc = p[7 * ld + n], c1 = p[9 * ld + n], c2 = p[10 * ld + n];
+    if (grid_setup(g, det, ev, wf, n, Mc, eta)) {
+      event_setup<MODEL>(E, det, wf, qnm, nq, Mc, eta, c1, c2, dL);
+    }
+    proj_setup(pj, det, th, ph, io, ps, tc, dL);
+  }
+  if (MODEL == 2) {
+    __syncthreads();
+    if (threadIdx.x < 6 && g.ok) {
+      const double eta = p[1 * ld + n], c1 = p[9 * ld + n], c2 = p[10 * ld + n], io = p[5 * ld + n];
+      hm_setup_mode(E.hm, threadIdx.x, D4::seed(eta, P_ETA), D4::seed(c1, P_CHI1), D4::seed(c2, P_CHI2), io);
+    }
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------ Fisher kernel
+// NG: Gram sets per point. L: 1. Triangle, per arm: 3 (arm1, arm2, -(arm1+arm2)).
+// Triangle, detector total: 2, using G(U)+G(V)+G(U+V) = G(sqrt(3/2)(U+V)) + G(sqrt(1/2)(U-V)).
+template <int MODEL, bool EARTH, int NARM, int NG>
+__global__ void __launch_bounds__(kThreads) fisher_kernel(EvBatch ev, DetDev det, WfDesc wf, const double* qnm, int nq,
+                                                          double* out_arm, double* out_det, int accum) {
+  extern __shared__ __align__(16) unsigned char stage_raw[];
+  cd* stage = reinterpret_cast<cd*>(stage_raw);   // [warp][NG][NP][32]
+  __shared__ EvUnion E;
+  __shared__ ProjEv pj;
+  __shared__ GridEv g;
+  __shared__ ArmPat apc[NARM];
+  __shared__ TimeState tsc;
+  const long long n = ev.n0 + blockIdx.x;
+  if (n >= ev.N) return;
+  block_setup<MODEL>(E, pj, g, ev, det, wf, qnm, nq, n);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (!EARTH) {
+    if (tid == 0) {
+      time_state(pj, pj.tc, tsc);
+      for (int a = 0; a < NARM; ++a) arm_pattern(pj, det.sin_zeta, tsc.x, a, apc[a]);
+    }
+    __syncthreads();
+  }
+  constexpr int NENT = NE * NG;
+  constexpr int EPT = (NENT + 31) / 32;
+  double acc[EPT];
+#pragma unroll
+  for (int i = 0; i < EPT; ++i) acc[i] = 0.0;
+  cd* my = stage + (size_t)warp * NG * NP * 32;
+  const int R = g.ok ? g.R : 0;
+  for (int base = 0; base < R; base += kThreads) {
+    const int k = base + tid;
+    cd D[NARM][NP];
+    double sw = 0.0;
+    if (k < R) {
+      double f, lnf, w;
+      grid_point(g, ev.spacing, k, f, lnf, w);
+      const double S = psd_at(det, f, lnf);
+      sw = sqrt(4.0 * w / S);
+      cd P, C, dP[4], dC[4], dPi, dCi;
+      D4 tau(0.0);
+      wave_point_dual<MODEL, EARTH>(E, pj, f, lnf, P, C, dP, dC, dPi, dCi, tau);
+      double dtn[4] = {0.0, 0.0, 0.0, 0.0};
+      TimeState ts;
+      if (EARTH) {
+        const double tn = pj.tc - tau.v / kDay;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) dtn[q] = -tau.d[q] / kDay;
+        time_state(pj, tn, ts);
+      } else {
+        ts = tsc;
+      }
+#pragma unroll
+      for (int a = 0; a < NARM; ++a) {
+        ArmPat ap;
+        if (EARTH) arm_pattern(pj, det.sin_zeta, ts.x, a, ap);
+        else ap = apc[a];
+        arm_derivs(pj, ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D[a]);
+      }
+    } else {
+#pragma unroll
+      for (int a = 0; a < NARM; ++a)
+#pragma unroll
+        for (int q = 0; q < NP; ++q) D[a][q] = {0.0, 0.0};
+    }
+    // stage weighted derivative vectors of this warp's 32 points
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      if (NG == 1) {
+        my[(0 * NP + q) * 32 + lane] = cscale(D[0][q], sw);
+      } else if (NG == 2) {
+        const cd u = D[0][q], v = D[1][q];
+        my[(0 * NP + q) * 32 + lane] = cscale(cadd(u, v), sw * 1.2247448713915890);   // sqrt(3/2)
+        my[(1 * NP + q) * 32 + lane] = cscale(cadd(u, cscale(v, -1.0)), sw * 0.70710678118654752);
+      } else {
+        const cd u = D[0][q], v = D[1][q];
+        my[(0 * NP + q) * 32 + lane] = cscale(u, sw);
+        my[(1 * NP + q) * 32 + lane] = cscale(v, sw);
+        my[(2 * NP + q) * 32 + lane] = cscale(cadd(u, v), -sw);
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < EPT; ++i) {
+      const int e = lane + 32 * i;
+      if (e < NENT) {
+        const int gs = e / NE, pe = e - gs * NE;
+        const cd* ra = my + (gs * NP + kPairA[pe]) * 32;
+        const cd* rb = my + (gs * NP + kPairB[pe]) * 32;
+        double s = 0.0;
+#pragma unroll 8
+        for (int j = 0; j < 32; ++j) s += ra[j].re * rb[j].re + ra[j].im * rb[j].im;
+        acc[i] += s;
+      }
+    }
+    __syncwarp();
+  }
+  // cross-warp reduction through the (now free) staging area
+  __syncthreads();
+  double* red = reinterpret_cast<double*>(stage_raw);  // [kWarps][NENT]
+#pragma unroll
+  for (int i = 0; i < EPT; ++i) {
+    const int e = lane + 32 * i;
+    if (e < NENT) red[warp * NENT + e] = acc[i];
+  }
+  __syncthreads();
+  const long long N = ev.N;
+  for (int e = tid; e < NENT; e += kThreads) {
+    double s = 0.0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) s += red[w * NENT + e];
+    red[e + kWarps * NENT] = s;
+  }
+  __syncthreads();
+  const double* tot = red + kWarps * NENT;
+  // write full symmetric matrices
+  for (int e = tid; e < NE; e += kThreads) {
+    const int a = kPairA[e], b = kPairB[e];
+    double sdet = 0.0;
+#pragma unroll
+    for (int gs = 0; gs < NG; ++gs) {
+      const double v = tot[gs * NE + e];
+      sdet += v;
+      if (out_arm && (NG == 1 || NG == 3)) {
+        double* o = out_arm + ((size_t)gs * N + n) * (NP * NP);
+        o[a * NP + b] = v;
+        o[b * NP + a] = v;
+      }
+    }
+    if (out_det) {
+      double* o = out_det + (size_t)n * (NP * NP);
+      if (accum) { o[a * NP + b] += sdet; if (a != b) o[b * NP + a] += sdet; }
+      else { o[a * NP + b] = sdet; o[b * NP + a] = sdet; }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ SNR kernel
+// out_arm[a][n] = trapz((Ap^2 + Ac^2)/S) per arm (SNR_arm = 2 sqrt), out_det[n] += 4 sum_arms.
+template <int MODEL, bool EARTH, int NARM>
+__global__ void __launch_bounds__(kThreads) snr_kernel(EvBatch ev, DetDev det, WfDesc wf, const double* qnm, int nq,
+                                                       double* out_arm, double* out_det, int accum) {
+  __shared__ EvUnion E;
+  __shared__ ProjEv pj;
+  __shared__ GridEv g;
+  __shared__ ArmPat apc[NARM];
+  __shared__ double red[kWarps][3];
+  const long long n = ev.n0 + blockIdx.x;
+  if (n >= ev.N) return;
+  block_setup<MODEL>(E, pj, g, ev, det, wf, qnm, nq, n);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (!EARTH) {
+    if (tid == 0) {
+      TimeState ts;
+      time_state(pj, pj.tc, ts);
+      for (int a = 0; a < NARM; ++a) arm_pattern(pj, det.sin_zeta, ts.x, a, apc[a]);
+    }
+    __syncthreads();
+  }
+  double s[3] = {0.0, 0.0, 0.0};
+  const int R = g.ok ? g.R : 0;
+  for (int k = tid; k < R; k += kThreads) {
+    double f, lnf, w;
+    grid_point(g, ev.spacing, k, f, lnf, w);
+    const double S = psd_at(det, f, lnf);
+    double ap, ac, tau = 0.0;
+    wave_point_val<MODEL, EARTH>(E, pj, f, lnf, ap, ac, tau);
+    double Fp[2], Fc[2];
+    if (EARTH) {
+      TimeState ts;
+      time_state(pj, pj.tc - tau / kDay, ts);
+#pragma unroll
+      for (int a = 0; a < NARM; ++a) { ArmPat p; arm_pattern(pj, det.sin_zeta, ts.x, a, p); Fp[a] = p.Fp; Fc[a] = p.Fc; }
+    } else {
+#pragma unroll
+      for (int a = 0; a < NARM; ++a) { Fp[a] = apc[a].Fp; Fc[a] = apc[a].Fc; }
+    }
+    const double ws = w / S;
+    const double p1 = ap * Fp[0], c1 = ac * Fc[0];
+    s[0] += ws * (p1 * p1 + c1 * c1);
+    if (NARM == 2) {
+      const double p2 = ap * Fp[1], c2 = ac * Fc[1];
+      s[1] += ws * (p2 * p2 + c2 * c2);
+      const double p3 = p1 + p2, c3 = c1 + c2;
+      s[2] += ws * (p3 * p3 + c3 * c3);
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    double v = s[a];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp][a] = v;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const int na = (NARM == 2) ? 3 : 1;
+    double tot = 0.0;
+    for (int a = 0; a < na; ++a) {
+      double v = 0.0;
+      for (int w = 0; w < kWarps; ++w) v += red[w][a];
+      if (out_arm) out_arm[(size_t)a * ev.N + n] = v;
+      tot += 4.0 * v;
+    }
+    if (out_det) out_det[n] = accum ? out_det[n] + tot : tot;
+  }
+}
+
+}  // namespace gwf

@@ -1,0 +1,635 @@
+// Waveform models on the device: TaylorF2_RestrictedPN, IMRPhenomD, IMRPhenomHM.
+//
+// Per event, a setup routine evaluates every parameter-dependent coefficient as a
+// Dual<double, 4> (value + d/d{Mc, eta, chi1z, chi2z}); per frequency point the
+// routines below are templated on the scalar S (plain T for the SNR, Dual<T, 4>
+// for the Fisher tangent).  Formulas follow gwfast 1.1.2 (citations per routine);
+// the IMRPhenomD intermediate amplitude is evaluated in Newton-Hermite form (the
+// same quartic that gwfast writes out as delta_0..delta_4).
+#pragma once
+#include "gwf_consts.cuh"
+
+namespace gwf {
+
+using D4 = Dual<double, 4>;
+enum { P_MC = 0, P_ETA = 1, P_CHI1 = 2, P_CHI2 = 3 };
+
+// coefficient access: for S = Dual<T,4> the full dual, for a plain S the value
+template <class S> struct Co;
+template <> struct Co<double> { __device__ __forceinline__ static double get(const D4& c) { return c.v; } };
+template <> struct Co<float> { __device__ __forceinline__ static float get(const D4& c) { return float(c.v); } };
+template <> struct Co<D4> { __device__ __forceinline__ static D4 get(const D4& c) { return c; } };
+template <> struct Co<Dual<float, 4>> {
+  __device__ __forceinline__ static Dual<float, 4> get(const D4& c) {
+    Dual<float, 4> r; r.v = float(c.v);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) r.d[i] = float(c.d[i]);
+    return r;
+  }
+};
+template <class S> __device__ __forceinline__ S co(const D4& c) { return Co<S>::get(c); }
+
+template <class S> struct Real;
+template <> struct Real<double> { typedef double T; };
+template <> struct Real<float> { typedef float T; };
+template <class U, int N> struct Real<Dual<U, N>> { typedef U T; };
+
+__device__ __forceinline__ D4 seta_of(const D4& eta) {
+  // sqrt(1-4 eta) guarded at equal mass (gwfast/waveforms.py:759)
+  return eta.v < 0.25 ? dsqrt(1.0 - 4.0 * eta) : D4(0.0);
+}
+
+// ------------------------------------------------------------------ PN phase coefficients
+struct PNC { D4 A, c2, c3, c4, c5, c5l, c6, c6l, c7; };
+
+// TaylorF2 coefficients, gwfast/waveforms.py:784-812 (QuadMon = 1); drop_ss removes the 3PN
+// spin-spin part as IMRPhenomD does (gwfast/waveforms.py:1077).
+__device__ inline PNC pn_coeffs(const D4& eta, const D4& chi1, const D4& chi2, bool spin_ho, bool drop_ss) {
+  const D4 seta = seta_of(eta);
+  const D4 m1 = 0.5 * (1.0 + seta), m2 = 0.5 * (1.0 - seta);
+  const D4 chis = 0.5 * (chi1 + chi2), chia = 0.5 * (chi1 - chi2);
+  const D4 eta2 = eta * eta;
+  PNC c;
+  c.A = 3.0 / (128.0 * eta);
+  c.c2 = 3715. / 756. + 55. / 9. * eta;
+  c.c3 = -16. * kPi + (113. / 3.) * seta * chia + (113. / 3. - 76. / 3. * eta) * chis;
+  const D4 m1s = m1 * m1 * chi1 * chi1, m2s = m2 * m2 * chi2 * chi2;
+  c.c4 = 5. / 72. * (3058.673 / 7.056 + 5429. / 7. * eta + 617. * eta2) + ((247. - 721.) / 4.8) * eta * chi1 * chi2
+         + ((-720. + 1. + 240. - 7.) / 9.6) * (m1s + m2s);
+  const D4 t5 = (732985. / 2268. - 24260. / 81. * eta - 340. / 9. * eta2) * chis
+                + (732985. / 2268. + 140. / 9. * eta) * seta * chia;
+  c.c5 = 38645. * kPi / 756. - 65. * kPi / 9. * eta - t5;
+  c.c5l = 3.0 * c.c5;
+  D4 six = 11583.231236531 / 4.694215680 - 640. / 3. * kPi * kPi - 684.8 / 2.1 * kEulerGamma
+           + (-15737.765635 / 3.048192 + 225.5 / 1.2 * kPi * kPi) * eta + 76.055 / 1.728 * eta2
+           - 127.825 / 1.296 * eta2 * eta - log(4.0) * (684.8 / 2.1)
+           + kPi * chi1 * m1 * (1490. / 3. + 260. * m1) + kPi * chi2 * m2 * (1490. / 3. + 260. * m2);
+  if (!drop_ss) {
+    const D4 ss1 = (4703.5 / 8.4 - 4108.25 / 6.72) + (2935. / 6. - 108.5 / 1.2) * m1 + (125.5 / 3.6 - 120.) * m1 * m1;
+    const D4 ss2 = (4703.5 / 8.4 - 4108.25 / 6.72) + (2935. / 6. - 108.5 / 1.2) * m2 + (125.5 / 3.6 - 120.) * m2 * m2;
+    six = six + (326.75 / 1.12 + 557.5 / 1.8 * eta) * eta * chi1 * chi2 + ss1 * m1s + ss2 * m2s;
+  }
+  c.c6 = six;
+  c.c6l = D4(-6848. / 21.);
+  D4 sev = 77096675. * kPi / 254016. + 378515. * kPi / 1512. * eta - 74045. * kPi / 756. * eta2;
+  D4 cs = -25150083775. / 3048192. + 10566655595. / 762048. * eta - 1042165. / 3024. * eta2 + 5345. / 36. * eta2 * eta;
+  D4 ca = -25150083775. / 3048192. + 26804935. / 6048. * eta - 1985. / 48. * eta2;
+  if (spin_ho) {
+    cs = cs + (14585. / 8. - 7270. * eta + 80. * eta2) * chia * chia;
+    sev = sev + (14585. / 24. - 475. / 6. * eta + 100. / 3. * eta2) * chis * chis * chis
+          + seta * ((14585. / 24. - 2380. * eta) * chia * chia * chia + (14585. / 8. - 107.5 * eta) * chia * chis * chis);
+  }
+  c.c7 = sev + cs * chis + seta * ca * chia;
+  return c;
+}
+
+// ------------------------------------------------------------------ TaylorF2 (gwfast/waveforms.py:697-953)
+struct TF2Ev {
+  PNC pn;
+  D4 eta;
+  D4 Ms;     // total mass in seconds
+  D4 vM;     // (pi Ms)^(1/3)
+  D4 lnvM;
+  D4 ampK;   // amplitude without f^(-7/6) and without 1/dL dependence in the tangent
+};
+
+__device__ inline void tf2_setup(TF2Ev& e, const D4& Mc, const D4& eta, const D4& chi1, const D4& chi2, double dL, bool spin_ho) {
+  e.pn = pn_coeffs(eta, chi1, chi2, spin_ho, false);
+  e.eta = eta;
+  e.Ms = Mc * kG3 / dpowc(eta, 0.6);
+  e.vM = dcbrt(kPi * e.Ms);
+  e.lnvM = dlog(e.vM);
+  // sqrt(5/24) pi^(-2/3) c/dL (G Mc)^(5/6)  (gwfast/waveforms.py:875)
+  e.ampK = (sqrt(5.0 / 24.0) * pow(kPi, -2.0 / 3.0) * kCGpc / dL) * dpowc(kG3 * Mc, 5.0 / 6.0);
+}
+
+// TF2 phase (without the constant offset, which cancels in every output) and amplitude.
+template <class S>
+__device__ __forceinline__ void tf2_point(const TF2Ev& e, typename Real<S>::T f, typename Real<S>::T f13,
+                                          typename Real<S>::T lnf, typename Real<S>::T fm76, S& amp, S& phase) {
+  typedef typename Real<S>::T T;
+  const S v = co<S>(e.vM) * f13;
+  const S lnv = co<S>(e.lnvM) + lnf * T(1.0 / 3.0);
+  const S v2 = v * v;
+  const S v3 = v2 * v;
+  const S ser = T(1) + co<S>(e.pn.c2) * v2 + co<S>(e.pn.c3) * v3 + co<S>(e.pn.c4) * v2 * v2
+                + (co<S>(e.pn.c5) + co<S>(e.pn.c5l) * lnv) * v2 * v3
+                + (co<S>(e.pn.c6) + co<S>(e.pn.c6l) * lnv) * v3 * v3 + co<S>(e.pn.c7) * v3 * v3 * v;
+  phase = co<S>(e.pn.A) * ser / (v2 * v3);
+  amp = co<S>(e.ampK) * fm76;
+}
+
+// 3.5PN time to coalescence shared by the three models (gwfast/waveforms.py:878-901, :1299-1322, :2712-2735)
+template <class S>
+__device__ __forceinline__ S tau_star_point(const D4& Ms, const D4& vM, const D4& eta_, typename Real<S>::T f13) {
+  typedef typename Real<S>::T T;
+  const S eta = co<S>(eta_);
+  const S v = co<S>(vM) * f13;
+  const S v2 = v * v;
+  const S v4 = v2 * v2;
+  const S eta2 = eta * eta;
+  const S pre = T(5.0 / 256.0) * co<S>(Ms) / (eta * v4 * v4);
+  const S t05 = T(1) + (T(743. / 252.) + T(11. / 3.) * eta) * v2 - T(32. / 5. * kPi) * v2 * v
+                + (T(3058673. / 508032.) + T(5429. / 504.) * eta + T(617. / 72.) * eta2) * v4
+                - (T(7729. / 252.) - T(13. / 3.) * eta) * T(kPi) * v4 * v;
+  const S t6 = (T(-10052469856691. / 23471078400. + 128. / 3. * kPi * kPi + 6848. / 105. * kEulerGamma)
+                + (T(3147553127. / 3048192. - 451. / 12. * kPi * kPi)) * eta - T(15211. / 1728.) * eta2
+                + T(25565. / 1296.) * eta2 * eta + T(3424. / 105.) * dlog(T(16) * v2)) * v4 * v2;
+  const S t7 = (T(-15419335. / 127008.) - T(75703. / 756.) * eta + T(14809. / 378.) * eta2) * T(kPi) * v4 * v2 * v;
+  return pre * (t05 + t6 + t7);
+}
+
+// ------------------------------------------------------------------ IMRPhenomD core
+struct PhdCore {
+  D4 eta, MG, Ms, vM;     // MG = M * G/c^3 (s); Ms = MG; vM = (pi MG)^(1/3) for tau_star
+  D4 fring, fdamp;
+  PNC pn;
+  D4 sig[4], bet[3], alp[5], gam[3];
+  D4 C1Int, C2Int, fMRD, PhiIntTemp, DPhiIntTemp, C1MRD, C2MRD;
+  D4 a23, a1, a43, a53, a2, r1, r2, r3;   // inspiral amplitude
+  D4 fpA;                                 // amplitude peak (gwfast/waveforms.py:1193)
+  D4 f2;                                  // middle collocation node
+  D4 h0, h1, h2, h3, h4;                  // Newton-Hermite coefficients of the intermediate amplitude
+  D4 ampPref;                             // Overallamp * amp0 (model-dependent normalisation)
+  D4 t0;
+  D4 fRef, phiRef;                        // detector-dependent (fRef = M G fmin)
+};
+
+__device__ __forceinline__ D4 fit11(int k, const D4& eta, const D4& xi) {
+  const double* c = kFits[k];
+  const D4 e2 = eta * eta;
+  return c[0] + c[1] * eta + (c[2] + c[3] * eta + c[4] * e2 + (c[5] + c[6] * eta + c[7] * e2) * xi
+                              + (c[8] + c[9] * eta + c[10] * e2) * xi * xi) * xi;
+}
+
+// final spin (gwfast/waveforms.py:1256-1276) and radiated energy (:1278-1297)
+__device__ inline D4 final_spin(const D4& eta, const D4& chi1, const D4& chi2) {
+  const D4 seta = seta_of(eta);
+  const D4 m1 = 0.5 * (1.0 + seta), m2 = 0.5 * (1.0 - seta);
+  const D4 s = m1 * m1 * chi1 + m2 * m2 * chi2;
+  const D4 e2 = eta * eta;
+  return eta * (3.4641016151377544 - 4.399247300629289 * eta + 9.397292189321194 * e2 - 13.180949901606242 * e2 * eta)
+         + eta * (s * ((1.0 / eta - 0.0850917821418767 - 5.837029316602263 * eta) + (0.1014665242971878 - 2.0967746996832157 * eta) * s))
+         + eta * (s * ((-1.3546806617824356 + 4.108962025369336 * eta) * s * s + (-0.8676969352555539 + 2.064046835273906 * eta) * s * s * s));
+}
+__device__ inline D4 radiated_energy(const D4& eta, const D4& chi1, const D4& chi2) {
+  const D4 seta = seta_of(eta);
+  const D4 m1 = 0.5 * (1.0 + seta), m2 = 0.5 * (1.0 - seta);
+  const D4 s = (m1 * m1 * chi1 + m2 * m2 * chi2) / (m1 * m1 + m2 * m2);
+  const D4 e2 = eta * eta;
+  const D4 ens = eta * (0.055974469826360077 + 0.5809510763115132 * eta - 0.9606726679372312 * e2 + 3.352411249771192 * e2 * eta);
+  return ens * (1. + (-0.0030302335878845507 - 2.0066110851351073 * eta + 7.7050567802399215 * e2) * s)
+         / (1. + (-0.6714403054720589 - 1.4756929437702908 * eta + 7.304676214885011 * e2) * s);
+}
+
+// ---- phase pieces (argument x = M f), gwfast/waveforms.py:1079-1153, :2497-2501
+template <class S>
+__device__ __forceinline__ S ins_phase(const PhdCore& k, const S& x) {
+  typedef typename Real<S>::T T;
+  const S xp = T(kPi) * x;
+  const S x13 = dcbrt(xp);
+  const S ix13 = T(1) / x13;
+  const S ix23 = ix13 * ix13;
+  const S lx = dlog(xp) * T(1.0 / 3.0);
+  const S tf2 = ix23 / xp + co<S>(k.pn.c2) / xp + co<S>(k.pn.c3) * ix23 + co<S>(k.pn.c4) * ix13 + co<S>(k.pn.c5)
+                + co<S>(k.pn.c5l) * lx + (co<S>(k.pn.c6) + co<S>(k.pn.c6l) * lx) * x13 + co<S>(k.pn.c7) * x13 * x13;
+  const S m13 = x13 * T(0.68278406325529573);  // x^(1/3) = (pi x)^(1/3) / pi^(1/3)
+  const S eta = co<S>(k.eta);
+  return co<S>(k.pn.A) * tf2 + (co<S>(k.sig[0]) * x + T(0.75) * co<S>(k.sig[1]) * x * m13
+                                + T(0.6) * co<S>(k.sig[2]) * x * m13 * m13 + T(0.5) * co<S>(k.sig[3]) * x * x) / eta;
+}
+
+template <class S>
+__device__ __forceinline__ S int_phase_raw(const PhdCore& k, const S& x) {
+  typedef typename Real<S>::T T;
+  return (co<S>(k.bet[0]) * x - co<S>(k.bet[2]) / (T(3) * x * x * x) + co<S>(k.bet[1]) * dlog(x)) / co<S>(k.eta);
+}
+
+template <class S>
+__device__ __forceinline__ S mrd_phase_raw(const PhdCore& k, const S& x, const S& rho, const S& tau) {
+  typedef typename Real<S>::T T;
+  const S x14 = dsqrt(dsqrt(x));
+  return (-co<S>(k.alp[1]) / x + T(4.0 / 3.0) * co<S>(k.alp[2]) * x14 * x14 * x14 + co<S>(k.alp[0]) * x
+          + co<S>(k.alp[3]) * rho * datan((x - co<S>(k.alp[4]) * co<S>(k.fring)) / (co<S>(k.fdamp) * rho * tau))) / co<S>(k.eta);
+}
+
+// complete phase with the Mf < 0.2 cut (gwfast/waveforms.py:1145, :2499)
+template <class S>
+__device__ __forceinline__ S complete_phase(const PhdCore& k, const S& x, const S& C1, const S& C2, const S& rho, const S& tau) {
+  typedef typename Real<S>::T T;
+  const T xv = val(x);
+  if (xv < T(kPhiFJoin)) return ins_phase(k, x);
+  if (xv < T(val(k.fMRD))) return int_phase_raw(k, x) + co<S>(k.C1Int) + co<S>(k.C2Int) * x;
+  if (xv < T(kMfCut)) return mrd_phase_raw(k, x, rho, tau) + C1 + C2 * x;
+  return S(T(0));
+}
+
+// ---- amplitude pieces, gwfast/waveforms.py:1198-1254
+template <class S>
+__device__ __forceinline__ S ins_amp(const PhdCore& k, const S& x) {
+  typedef typename Real<S>::T T;
+  const S x13 = dcbrt(x);
+  const S x23 = x13 * x13;
+  return T(1) + x23 * co<S>(k.a23) + x * x13 * co<S>(k.a43) + x * x23 * co<S>(k.a53) + x * x * x13 * co<S>(k.r1)
+         + x * x * x23 * co<S>(k.r2) + x * (co<S>(k.a1) + x * co<S>(k.a2) + x * x * co<S>(k.r3));
+}
+
+template <class S>
+__device__ __forceinline__ S mrd_amp(const PhdCore& k, const S& x) {
+  const S fr = co<S>(k.fring), fdg3 = co<S>(k.fdamp) * co<S>(k.gam[2]);
+  const S dx = x - fr;
+  return dexp(-dx * co<S>(k.gam[1]) / fdg3) * (fdg3 * co<S>(k.gam[0])) / (dx * dx + fdg3 * fdg3);
+}
+
+template <class S>
+__device__ __forceinline__ S complete_amp_shape(const PhdCore& k, const S& x) {
+  typedef typename Real<S>::T T;
+  const T xv = val(x);
+  if (xv < T(kAmpFJoin)) return ins_amp(k, x);
+  if (xv < T(val(k.fpA))) {
+    const S u = x - T(kAmpFJoin);
+    return co<S>(k.h0) + u * (co<S>(k.h1) + u * (co<S>(k.h2) + (x - co<S>(k.f2)) * (co<S>(k.h3) + (x - co<S>(k.fpA)) * co<S>(k.h4))));
+  }
+  if (xv < T(kMfCut)) return mrd_amp(k, x);
+  return S(T(0));
+}
+
+// ---- per-event setup of the IMRPhenomD core given fring, fdamp
+__device__ inline void phenom_core_setup(PhdCore& k, const D4& Mc, const D4& eta, const D4& chi1, const D4& chi2,
+                                         const D4& fring, const D4& fdamp) {
+  k.eta = eta;
+  k.MG = Mc * kG3 / dpowc(eta, 0.6);
+  k.Ms = k.MG;
+  k.vM = dcbrt(kPi * k.MG);
+  k.fring = fring;
+  k.fdamp = fdamp;
+  const D4 seta = seta_of(eta);
+  const D4 chis = 0.5 * (chi1 + chi2), chia = 0.5 * (chi1 - chi2);
+  const D4 xi = chis * (1.0 - eta * (76.0 / 113.0)) + seta * chia - 1.0;
+  for (int i = 0; i < 4; ++i) k.sig[i] = fit11(FIT_SIGMA1 + i, eta, xi);
+  for (int i = 0; i < 3; ++i) k.bet[i] = fit11(FIT_BETA1 + i, eta, xi);
+  for (int i = 0; i < 5; ++i) k.alp[i] = fit11(FIT_ALPHA1 + i, eta, xi);
+  for (int i = 0; i < 3; ++i) k.gam[i] = fit11(FIT_GAMMA1 + i, eta, xi);
+  k.pn = pn_coeffs(eta, chi1, chi2, false, true);
+  // inspiral -> intermediate C1 join at Mf = 0.018 (gwfast/waveforms.py:1098-1120)
+  {
+    const double fj = kPhiFJoin;
+    const double x = kPi * fj;
+    const double x13 = cbrt(x);
+    const double lx = log(x) / 3.0;
+    // d/dMf of the inspiral phase
+    const D4 dtf2 = (-5. / 3.) * pow(x, -8. / 3.) - k.pn.c2 / (x * x) - (2. / 3.) * k.pn.c3 * pow(x, -5. / 3.)
+                    - (1. / 3.) * k.pn.c4 * pow(x, -4. / 3.) + k.pn.c5l / (3. * x) + k.pn.c6l * (x13 / (3. * x))
+                    + (k.pn.c6 + k.pn.c6l * lx) * (x13 / (3. * x)) + (2. / 3.) * k.pn.c7 * (x13 * x13 / x);
+    const D4 dins = k.pn.A * dtf2 * kPi + (k.sig[0] + k.sig[1] * cbrt(fj) + k.sig[2] * cbrt(fj) * cbrt(fj) + k.sig[3] * fj) / eta;
+    const D4 dint = (k.bet[0] + k.bet[2] / (fj * fj * fj * fj) + k.bet[1] / fj) / eta;
+    k.C2Int = dins - dint;
+    const D4 xj(fj);
+    const D4 insj = ins_phase<D4>(k, xj);
+    k.C1Int = insj - int_phase_raw<D4>(k, xj) - k.C2Int * fj;
+  }
+  // intermediate -> merger-ringdown at 0.5 fring (gwfast/waveforms.py:1122-1129)
+  k.fMRD = 0.5 * fring;
+  {
+    const D4& fm = k.fMRD;
+    k.PhiIntTemp = int_phase_raw<D4>(k, fm) + k.C1Int + k.C2Int * fm;
+    k.DPhiIntTemp = k.C2Int + (k.bet[0] + k.bet[2] / (fm * fm * fm * fm) + k.bet[1] / fm) / eta;
+    const D4 one(1.0);
+    const D4 u = (fm - k.alp[4] * fring) / fdamp;
+    const D4 dmrd = (k.alp[0] + k.alp[1] / (fm * fm) + k.alp[2] / dsqrt(dsqrt(fm)) + k.alp[3] / (fdamp * (1.0 + u * u))) / eta;
+    k.C2MRD = k.DPhiIntTemp - dmrd;
+    k.C1MRD = k.PhiIntTemp - mrd_phase_raw<D4>(k, fm, one, one) - k.C2MRD * fm;
+  }
+  // amplitude (gwfast/waveforms.py:1189-1245)
+  {
+    const D4 sp1 = 1.0 + seta;
+    const D4 e2 = eta * eta;
+    const D4 c12 = chi1 * chi1, c22 = chi2 * chi2;
+    k.a23 = (-969. + 1804. * eta) * (pow(kPi, 2.0 / 3.0) / 672.);
+    k.a1 = (chi1 * (81. * sp1 - 44. * eta) + chi2 * (81. - 81. * seta - 44. * eta)) * (kPi / 48.);
+    k.a43 = (-27312085.0 - 10287648. * c22 - 10287648. * c12 * sp1 + 10287648. * c22 * seta
+             + 24. * (-1975055. + 857304. * c12 - 994896. * chi1 * chi2 + 857304. * c22) * eta + 35371056. * e2)
+            * (pow(kPi, 4.0 / 3.0) / 8.128512e6);
+    k.a53 = (chi2 * (-285197. * (seta - 1.0) + 4. * (-91902. + 1579. * seta) * eta - 35632. * e2)
+             + chi1 * (285197. * sp1 - 4. * (91902. + 1579. * seta) * eta - 35632. * e2) + 42840. * kPi * (4. * eta - 1.0))
+            * (pow(kPi, 5.0 / 3.0) / 32256.);
+    k.a2 = -(kPi * kPi / 6.0085960704e10) *
+           (-336. * (-3248849057.0 + 2943675504. * c12 - 3339284256. * chi1 * chi2 + 2943675504. * c22) * e2
+            - 324322727232. * e2 * eta
+            - 7. * (-177520268561. + 107414046432. * c22 + 107414046432. * c12 * sp1 - 107414046432. * c22 * seta
+                    + 11087290368. * kPi * (chi1 + chi2 + chi1 * seta - chi2 * seta))
+            + 12. * eta * (-545384828789. - 176491177632. * chi1 * chi2 + 202603761360. * c22
+                           + 77616. * c12 * (2610335. + 995766. * seta) - 77287373856. * c22 * seta
+                           + 5841690624. * kPi * (chi1 + chi2) + 21384760320. * kPi * kPi));
+    k.r1 = fit11(FIT_RHO1, eta, xi);
+    k.r2 = fit11(FIT_RHO2, eta, xi);
+    k.r3 = fit11(FIT_RHO3, eta, xi);
+    const D4& g1 = k.gam[0];
+    const D4& g2 = k.gam[1];
+    const D4& g3 = k.gam[2];
+    k.fpA = (g2.v >= 1.0) ? dabs(fring - fdamp * g3 / g2)
+                          : fring + fdamp * (dsqrt(1.0 - g2 * g2) - 1.0) * g3 / g2;
+    // collocation data: value and slope of the inspiral at f1, value v2 at f2, value and slope of the ringdown at f3
+    const double f1 = kAmpFJoin;
+    const D4 f3 = k.fpA;
+    const D4 f2 = f1 + 0.5 * (f3 - f1);
+    k.f2 = f2;
+    const D4 v1 = ins_amp<D4>(k, D4(f1));
+    const double f113 = cbrt(f1);
+    const D4 d1 = (2. / 3.) * k.a23 / f113 + k.a1 + (4. / 3.) * k.a43 * f113 + (5. / 3.) * k.a53 * f113 * f113 + 2. * k.a2 * f1
+                  + (7. / 3.) * k.r1 * f1 * f113 + (8. / 3.) * k.r2 * f1 * f113 * f113 + 3. * k.r3 * f1 * f1;
+    const D4 v2 = fit11(FIT_V2, eta, xi);
+    const D4 v3 = mrd_amp<D4>(k, f3);
+    const D4 fdg3 = fdamp * g3;
+    const D4 dx3 = f3 - fring;
+    const D4 den3 = dx3 * dx3 + fdg3 * fdg3;
+    const D4 d2 = (-2.0 * fdamp * dx3 * g3 * g1 / den3 - g2 * g1) / (dexp(dx3 * g2 / fdg3) * den3);
+    // divided differences over the nodes (f1, f1, f2, f3, f3)
+    const D4 q12 = (v2 - v1) / (f2 - f1);
+    const D4 q23 = (v3 - v2) / (f3 - f2);
+    const D4 q012 = (q12 - d1) / (f2 - f1);
+    const D4 q123 = (q23 - q12) / (f3 - f1);
+    const D4 q234 = (d2 - q23) / (f3 - f2);
+    const D4 q0123 = (q123 - q012) / (f3 - f1);
+    const D4 q1234 = (q234 - q123) / (f3 - f1);
+    k.h0 = v1;
+    k.h1 = d1;
+    k.h2 = q012;
+    k.h3 = q0123;
+    k.h4 = (q1234 - q0123) / (f3 - f1);
+  }
+}
+
+// t0 and phiRef (detector-dependent through fRef = M G fmin); gwfast/waveforms.py:1131-1147
+__device__ inline void phenom_ref_setup(PhdCore& k, const D4& fpeak, double fmin_hz, const D4& C1, const D4& C2) {
+  const D4 u = (fpeak - k.alp[4] * k.fring) / k.fdamp;
+  k.t0 = (k.alp[0] + k.alp[1] / (fpeak * fpeak) + k.alp[2] / dsqrt(dsqrt(fpeak)) + k.alp[3] / (k.fdamp * (1.0 + u * u))) / k.eta;
+  k.fRef = k.MG * fmin_hz;
+  const D4 one(1.0);
+  k.phiRef = complete_phase<D4>(k, k.fRef, C1, C2, one, one);
+}
+
+struct PhdEv {
+  PhdCore k;
+};
+
+__device__ inline void qnm_lookup(const double* qa, const double* qr, const double* qd, int n, const D4& a,
+                                  D4& fr, D4& fd) {
+  // jnp.interp semantics: segment [j, j+1] with qa[j] <= a < qa[j+1]; slope carries the tangent
+  int lo = 0, hi = n - 1;
+  const double x = a.v;
+  if (x < qa[0]) { lo = 0; }
+  else if (x >= qa[n - 1]) { lo = n - 2; }
+  else {
+    while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (qa[mid] <= x) lo = mid; else hi = mid; }
+  }
+  const double x0 = qa[lo], x1 = qa[lo + 1];
+  fr = qr[lo] + (a - x0) * ((qr[lo + 1] - qr[lo]) / (x1 - x0));
+  fd = qd[lo] + (a - x0) * ((qd[lo + 1] - qd[lo]) / (x1 - x0));
+}
+
+// IMRPhenomD per event (gwfast/waveforms.py:992-1254); fmin_hz sets fRef = min of the grid
+__device__ inline void phd_setup(PhdEv& e, const D4& Mc, const D4& eta, const D4& chi1, const D4& chi2, double dL,
+                                 double fmin_hz, const double* qa, const double* qr, const double* qd, int nq) {
+  PhdCore& k = e.k;
+  const D4 af = final_spin(eta, chi1, chi2);
+  const D4 er = radiated_energy(eta, chi1, chi2);
+  D4 fr, fd;
+  qnm_lookup(qa, qr, qd, nq, af, fr, fd);
+  fr = fr / (1.0 - er);
+  fd = fd / (1.0 - er);
+  phenom_core_setup(k, Mc, eta, chi1, chi2, fr, fd);
+  const D4& g2 = k.gam[1];
+  const D4& g3 = k.gam[2];
+  // phase peak frequency keeps the modulus in both branches (gwfast/waveforms.py:1134)
+  const D4 fpP = (g2.v >= 1.0) ? dabs(fr - fd * g3 / g2) : dabs(fr + fd * (dsqrt(1.0 - g2 * g2) - 1.0) * g3 / g2);
+  phenom_ref_setup(k, fpP, fmin_hz, k.C1MRD, k.C2MRD);
+  // 2 sqrt(5/(64 pi)) M G/c^2[Gpc] M G/c^3 / dL * sqrt(2 eta/3) pi^(-1/6)  (gwfast/waveforms.py:1204, :1248)
+  const D4 M = Mc / dpowc(eta, 0.6);
+  k.ampPref = (2.0 * sqrt(5.0 / (64.0 * kPi)) * kG2Gpc * kG3 / dL * pow(kPi, -1.0 / 6.0)) * M * M * dsqrt(eta * (2.0 / 3.0));
+}
+
+// amplitude A(f) and phase Phi(f) of IMRPhenomD at physical frequency f (Hz)
+template <class S>
+__device__ __forceinline__ void phd_point(const PhdCore& k, typename Real<S>::T f, S& amp, S& phase) {
+  typedef typename Real<S>::T T;
+  const S x = co<S>(k.MG) * f;
+  const T xv = val(x);
+  const S one(T(1));
+  const S shape = complete_amp_shape(k, x);
+  // x^(-7/6)
+  const S xm76 = T(1) / (x * dsqrt(dcbrt(x)));
+  amp = co<S>(k.ampPref) * xm76 * shape;
+  const S ph = complete_phase(k, x, co<S>(k.C1MRD), co<S>(k.C2MRD), one, one);
+  phase = (xv < T(kMfCut)) ? ph - co<S>(k.t0) * (x - co<S>(k.fRef)) - co<S>(k.phiRef) : ph;
+}
+
+// ------------------------------------------------------------------ IMRPhenomHM (gwfast/waveforms.py:2256-2616)
+struct HMMode {
+  D4 rho, tau, C1, C2, frlm;
+  D4 fip, amp_, bmp, PhDB, PhDC, PhDBA, phC;  // phase frequency map and offsets
+  D4 fia, ama, bma;                          // amplitude frequency map
+  D4 hr1, hr2, hr3, hr4, hi4;                // PN amplitude polynomial H(v) = v (hr1 + v (hr2 + v (hr3 + v (hr4 + i hi4))))
+  double yp, yc, dyp, dyc;                   // 0.5(Y +- (-1)^l Y_{l-m}) and d/diota
+  double shift;
+  int l, m;
+};
+
+struct HMEv {
+  PhdCore k;
+  D4 phi0;
+  HMMode md[6];
+};
+
+__device__ inline void rd_fit(int mode, const D4& finmass, const D4& finspin, D4& fr, D4& fd) {
+  const int l = kModeL[mode], m = kModeM[mode];
+  const D4 alpha = dlog(2.0 - finspin) / log(3.0);
+  const double beta = 1.0 / (2.0 + l - (m < 0 ? -m : m));
+  const D4 kap = dpowc(alpha, beta);
+  D4 re(0.0), im(0.0), kp(1.0);
+  for (int j = 0; j < 7; ++j) {
+    double s, c;
+    sincos(kRDPhase[mode][j], &s, &c);
+    re = re + (kRDMod[mode][j] * c) * kp;
+    im = im + (kRDMod[mode][j] * s) * kp;
+    kp = kp * kap;
+  }
+  const D4 den = (2.0 * kPi) * finmass;
+  fr = re / den;
+  fd = im / den;
+}
+
+// spin-weighted harmonics Y_lm, Y_l-m (s = -2, phi = 0) and their iota derivatives, gwfast/waveforms.py:2517-2524
+__device__ inline void sw_harm(int mode, double iota, double& Y, double& Ym, double& dY, double& dYm) {
+  typedef Dual<double, 1> D1;
+  const D1 io = D1::seed(iota, 0);
+  D1 c, s, ch, sh;
+  dsincos(io, &s, &c);
+  dsincos(io * 0.5, &sh, &ch);
+  D1 y, ym;
+  switch (mode) {
+    case 0: y = sqrt(5.0 / (16.0 * kPi)) * s * (1.0 + c); ym = sqrt(5.0 / (16.0 * kPi)) * s * (1.0 - c); break;
+    case 1: y = sqrt(5.0 / (64.0 * kPi)) * (1.0 + c) * (1.0 + c); ym = sqrt(5.0 / (64.0 * kPi)) * (1.0 - c) * (1.0 - c); break;
+    case 2: { const D1 c2 = ch * ch; y = sqrt(7.0 / kPi) * c2 * c2 * (3.0 * c - 2.0) * 0.5;
+              const D1 s2 = sh * sh; ym = sqrt(7.0 / (4.0 * kPi)) * (2.0 + 3.0 * c) * s2 * s2; break; }
+    case 3: { const D1 c2 = ch * ch; const D1 s2 = sh * sh;
+              y = -sqrt(21.0 / (2.0 * kPi)) * c2 * c2 * ch * sh; ym = sqrt(21.0 / (2.0 * kPi)) * ch * s2 * s2 * sh; break; }
+    case 4: { const D1 c2 = ch * ch; const D1 s2 = sh * sh;
+              y = -3.0 * sqrt(7.0 / (2.0 * kPi)) * c2 * c2 * ch * (2.0 * c - 1.0) * sh;
+              ym = 3.0 * sqrt(7.0 / (2.0 * kPi)) * ch * (1.0 + 2.0 * c) * s2 * s2 * sh; break; }
+    default: { const D1 c2 = ch * ch; const D1 s2 = sh * sh;
+               y = 3.0 * sqrt(7.0 / kPi) * c2 * c2 * c2 * s2; ym = 3.0 * sqrt(7.0 / kPi) * c2 * s2 * s2 * s2; break; }
+  }
+  Y = y.v; Ym = ym.v; dY = y.d[0]; dYm = ym.d[0];
+}
+
+__device__ inline void hm_setup_core(HMEv& e, const D4& Mc, const D4& eta, const D4& chi1, const D4& chi2, double dL,
+                                     double fmin_hz) {
+  PhdCore& k = e.k;
+  const D4 af = final_spin(eta, chi1, chi2);
+  const D4 finmass = 1.0 - radiated_energy(eta, chi1, chi2);
+  D4 fr, fd;
+  rd_fit(1, finmass, af, fr, fd);
+  phenom_core_setup(k, Mc, eta, chi1, chi2, fr, fd);
+  // hphc uses the amplitude peak (no modulus in the second branch) for t0 as well (gwfast/waveforms.py:2433, :2527)
+  phenom_ref_setup(k, k.fpA, fmin_hz, k.C1MRD, k.C2MRD);
+  e.phi0 = 0.5 * k.phiRef;
+  const D4 M = Mc / dpowc(eta, 0.6);
+  // M G/c^2[Gpc] M G/c^3 / dL * sqrt(2 eta/3) pi^(-1/6)   (gwfast/waveforms.py:2444, :2489)
+  k.ampPref = (kG2Gpc * kG3 / dL * pow(kPi, -1.0 / 6.0)) * M * M * dsqrt(eta * (2.0 / 3.0));
+}
+
+__device__ inline void hm_setup_mode(HMEv& e, int mode, const D4& eta, const D4& chi1, const D4& chi2, double iota) {
+  PhdCore& k = e.k;
+  HMMode& md = e.md[mode];
+  const int l = kModeL[mode], m = kModeM[mode];
+  md.l = l; md.m = m;
+  const double shifts[5] = {0.0, 0.5 * kPi, 0.0, -0.5 * kPi, kPi};
+  md.shift = shifts[m];
+  const D4 af = final_spin(eta, chi1, chi2);
+  const D4 finmass = 1.0 - radiated_energy(eta, chi1, chi2);
+  D4 frlm, fdlm;
+  rd_fit(mode, finmass, af, frlm, fdlm);
+  md.frlm = frlm;
+  md.rho = k.fring / frlm;
+  md.tau = fdlm / k.fdamp;
+  const D4& rho = md.rho;
+  const D4& tau = md.tau;
+  const D4& fm = k.fMRD;
+  const D4 u = (fm - k.alp[4] * k.fring) / (k.fdamp * rho * tau);
+  const D4 dmrd = (k.alp[0] + k.alp[1] / (fm * fm) + k.alp[2] / dsqrt(dsqrt(fm)) + k.alp[3] / (k.fdamp * tau * (1.0 + u * u))) / k.eta;
+  md.C2 = k.DPhiIntTemp - dmrd;
+  md.C1 = k.PhiIntTemp - mrd_phase_raw<D4>(k, fm, rho, tau) - md.C2 * fm;
+  // phase map (gwfast/waveforms.py:2544-2563, :2587-2597)
+  const double ai = 2.0 / m;
+  md.fip = kPhiFJoin / rho;
+  const D4 Ti = md.fip * ai;
+  md.amp_ = (frlm * rho - Ti) / (frlm - md.fip);
+  md.bmp = Ti - md.fip * md.amp_;
+  md.PhDB = complete_phase<D4>(k, md.amp_ * md.fip + md.bmp, md.C1, md.C2, rho, tau) / md.amp_;
+  md.PhDC = complete_phase<D4>(k, rho * frlm, md.C1, md.C2, rho, tau) / rho;
+  md.PhDBA = complete_phase<D4>(k, md.fip * ai, md.C1, md.C2, rho, tau) / ai;
+  md.phC = md.PhDBA - md.PhDB + complete_phase<D4>(k, md.amp_ * frlm + md.bmp, md.C1, md.C2, rho, tau) / md.amp_;
+  // amplitude map (gwfast/waveforms.py:2546-2568)
+  md.fia = kAmpFJoin / rho;
+  const D4 Tia = md.fia * ai;
+  md.ama = (k.fring - Tia) / (frlm - md.fia);
+  md.bma = Tia - md.fia * md.ama;
+  // PN amplitude H_lm(v) = v (hr1 + v (hr2 + v (hr3 + v (hr4 + i hi4))))  (gwfast/waveforms.py:2511)
+  const D4 seta = seta_of(eta);
+  const D4 chis = 0.5 * (chi1 + chi2), chia = 0.5 * (chi1 - chi2);
+  const D4 z(0.0);
+  md.hr1 = z; md.hr2 = z; md.hr3 = z; md.hr4 = z; md.hi4 = z;
+  switch (mode) {
+    case 0: {
+      const double s = sqrt(2.0) / 3.0;
+      md.hr1 = s * seta;
+      md.hr2 = -1.5 * s * (chia + seta * chis);
+      md.hr3 = s * seta * (335.0 / 672.0 + 117.0 / 56.0 * eta);
+      md.hr4 = s * (chia * (3427.0 / 1344. - 2101.0 / 336. * eta) + seta * chis * (3427.0 / 1344. - 965.0 / 336. * eta) - kPi * seta);
+      md.hi4 = s * seta * (-0.5 - 2.0 * 0.69314718056);
+      break;
+    }
+    case 1: md.hr1 = D4(1.0); break;  // H22 = 1 handled as a constant below
+    case 2: md.hr2 = (sqrt(5.0 / 7.0) / 3.0) * (1.0 - 3.0 * eta); break;
+    case 3: md.hr1 = (0.75 * sqrt(5.0 / 7.0)) * seta; break;
+    case 4: md.hr3 = (0.75 * sqrt(3.0 / 35.0)) * seta * (1.0 - 2.0 * eta); break;
+    default: md.hr2 = (4.0 / 9.0 * sqrt(10.0 / 7.0)) * (1.0 - 3.0 * eta); break;
+  }
+  double Y, Ym, dY, dYm;
+  sw_harm(mode, iota, Y, Ym, dY, dYm);
+  const double sg = (l % 2 == 0) ? 1.0 : -1.0;
+  md.yp = 0.5 * (Y + sg * Ym);
+  md.yc = 0.5 * (Y - sg * Ym);
+  md.dyp = 0.5 * (dY + sg * dYm);
+  md.dyc = 0.5 * (dY - sg * dYm);
+}
+
+// |H_lm(v)| for v = (2 pi x / m)^(1/3)
+template <class S>
+__device__ __forceinline__ S hm_absH(const HMMode& md, int mode, const S& x) {
+  typedef typename Real<S>::T T;
+  if (mode == 1) return S(T(1));
+  const S v = dcbrt(x * T(kTwoPi / md.m));
+  const S re = v * (co<S>(md.hr1) + v * (co<S>(md.hr2) + v * (co<S>(md.hr3) + v * co<S>(md.hr4))));
+  if (mode == 0) {
+    const S v2 = v * v;
+    const S im = v2 * v2 * co<S>(md.hi4);
+    return dsqrt(re * re + im * im);
+  }
+  return dabs(re);
+}
+
+template <class S> struct Cplx { S re, im; };
+
+// hp, hc of IMRPhenomHM without the common factor; returns P, C with hp = P, hc = i C, plus the iota derivatives
+// (dP, dC, value-only).  Point at physical frequency f (Hz).
+template <class S>
+__device__ __forceinline__ void hm_point(const HMEv& e, typename Real<S>::T f, Cplx<S>& P, Cplx<S>& C,
+                                         Cplx<typename Real<S>::T>& dP, Cplx<typename Real<S>::T>& dC) {
+  typedef typename Real<S>::T T;
+  const PhdCore& k = e.k;
+  const S x = co<S>(k.MG) * f;
+  const T xv = val(x);
+  const S zero(T(0));
+  P.re = zero; P.im = zero; C.re = zero; C.im = zero;
+  dP.re = T(0); dP.im = T(0); dC.re = T(0); dC.im = T(0);
+  const S lin = co<S>(k.t0) * (x - co<S>(k.fRef));
+#pragma unroll 1
+  for (int mode = 0; mode < 6; ++mode) {
+    const HMMode& md = e.md[mode];
+    const T ai = T(2.0) / T(md.m);
+    // amplitude
+    S fs;
+    if (xv < T(val(md.fia))) fs = x * ai;
+    else if (xv < T(val(md.frlm))) fs = x * co<S>(md.ama) + co<S>(md.bma);
+    else fs = x - co<S>(md.frlm) + co<S>(k.fring);
+    S amp = co<S>(k.ampPref) * (T(1) / (fs * dsqrt(dcbrt(fs)))) * complete_amp_shape(k, fs);
+    if (mode != 1) {
+      const S h1 = hm_absH(md, mode, x);
+      const S h2 = hm_absH(md, mode, x * ai);
+      const S h3 = hm_absH(md, mode, fs);
+      amp = amp * h1 * h3 / h2;
+      if (!(val(amp) == val(amp))) amp = zero;  // nan_to_num at equal mass (gwfast/waveforms.py:2582)
+    }
+    // phase
+    S ph;
+    const S rho = co<S>(md.rho), tau = co<S>(md.tau), C1 = co<S>(md.C1), C2 = co<S>(md.C2);
+    if (xv < T(val(md.fip))) ph = complete_phase(k, x * ai, C1, C2, rho, tau) / ai;
+    else if (xv < T(val(md.frlm)))
+      ph = co<S>(md.PhDBA) - co<S>(md.PhDB) + complete_phase(k, x * co<S>(md.amp_) + co<S>(md.bmp), C1, C2, rho, tau) / co<S>(md.amp_);
+    else ph = co<S>(md.phC) - co<S>(md.PhDC) + complete_phase(k, x * rho, C1, C2, rho, tau) / rho;
+    ph = ph - lin - T(md.m) * co<S>(e.phi0) + T(md.shift);
+    S sn, cs;
+    dsincos(ph, &sn, &cs);
+    // M = amp e^{-i ph}
+    const S mre = amp * cs, mim = -(amp * sn);
+    const T yp = T(md.yp), yc = T(md.yc);
+    P.re = P.re + yp * mre; P.im = P.im + yp * mim;
+    C.re = C.re + yc * mre; C.im = C.im + yc * mim;
+    dP.re += T(md.dyp) * val(mre); dP.im += T(md.dyp) * val(mim);
+    dC.re += T(md.dyc) * val(mre); dC.im += T(md.dyc) * val(mim);
+  }
+}
+
+}  // namespace gwf

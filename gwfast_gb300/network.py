@@ -1,0 +1,77 @@
+"""DetNet: a network of GWSignal detectors (gwfast/network.py:17-343).
+
+All detectors of the network are evaluated in one library call (one fused kernel
+launch per detector on one stream), and the network Fisher is accumulated on the
+device.
+"""
+import numpy as np
+
+from . import gwfastUtils as utils
+from .signal import fisher_batch, reparametrise, snr_batch
+
+
+class DetNet:
+    """gwfast/network.py:17-31."""
+
+    def __init__(self, signals, verbose=True):
+        self.signals = signals
+        self.verbose = verbose
+
+    def _list(self):
+        return list(self.signals.keys()), list(self.signals.values())
+
+    def _update_all_seeds(self, seeds=[], verbose=True):
+        if seeds == []:
+            seeds = [None for _ in self.signals]
+        for i, d in enumerate(self.signals):
+            self.signals[d]._update_seed(seed=seeds[i])
+
+    def SNR(self, evParams, res=1000, return_all=False):
+        """Network SNR (gwfast/network.py:278-306)."""
+        utils.check_evparams(evParams)
+        names, sigs = self._list()
+        arms = snr_batch(sigs, evParams, res, device=sigs[0].device)
+        snrs = {}
+        for name, s, a in zip(names, sigs, arms):
+            if s.detector_shape == 'T' and return_all:
+                for i in range(3):
+                    snrs['%s_%s' % (name, i)] = a[i]
+            elif s.detector_shape == 'T':
+                snrs[name] = np.sqrt((a ** 2).sum(axis=0))
+            else:
+                snrs[name] = a[0]
+        net = np.sqrt(np.array([snrs[k] ** 2 for k in snrs]).sum(axis=0))
+        if return_all:
+            snrs['net'] = net
+            return snrs
+        return net
+
+    def FisherMatr(self, evParams, return_all=False, return_derivatives=False, return_SNR_derivatives=False, **kwargs):
+        """Network Fisher matrix, (11, 11, N) (gwfast/network.py:309-343)."""
+        if return_derivatives or return_SNR_derivatives:
+            raise NotImplementedError('return_derivatives / return_SNR_derivatives are not implemented on the GPU path')
+        utils.check_evparams(evParams)
+        names, sigs = self._list()
+        res = kwargs.get('res', 1000)
+        if res is None:
+            res = max(s._resolve_res(evParams, None, kwargs.get('df')) for s in sigs)
+        spacing = kwargs.get('spacing', 'geom')
+        use_m1m2 = kwargs.get('use_m1m2', False)
+        use_chi1chi2 = kwargs.get('use_chi1chi2', True)
+        if kwargs.get('computeDerivFinDiff', False):
+            raise NotImplementedError('finite-difference derivatives are not used on the GPU path')
+        if not return_all:
+            F = fisher_batch(sigs, evParams, res, per_arm=False, spacing=spacing, device=sigs[0].device)
+            F = reparametrise(F, evParams, use_m1m2, use_chi1chi2)
+            return np.moveaxis(F, 0, -1)
+        per = fisher_batch(sigs, evParams, res, per_arm=True, spacing=spacing, device=sigs[0].device)
+        allF = {}
+        for name, s, Fa in zip(names, sigs, per):
+            Fa = reparametrise(Fa, evParams, use_m1m2, use_chi1chi2)
+            if s.detector_shape == 'T':
+                for i in range(3):
+                    allF['%s_%s' % (name, i)] = np.moveaxis(Fa[i], 0, -1)
+            else:
+                allF[name] = np.moveaxis(Fa[0], 0, -1)
+        allF['net'] = np.array([allF[k] for k in allF]).sum(axis=0)
+        return allF

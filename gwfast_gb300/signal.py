@@ -1,0 +1,203 @@
+"""GWSignal: one detector, with gwfast's constructor and SNRInteg/FisherMatr signatures.
+
+Replaces gwfast/signal.py:37-1098.  The frequency grid, PSD interpolation, waveform,
+analytic tangent, projection and the PSD-weighted Gram integral all run in one
+fused CUDA kernel per detector (libgwfast_gb300.so); this module only builds the
+event arrays, applies gwfast's host-side conventions (dict mutation, ValueError
+on missing parameters, duty-factor masks, parameter reparametrisations) and
+reshapes the outputs.
+"""
+import numpy as np
+
+from . import _lib
+from . import gwfastUtils as utils
+from .waveforms import PARAMS
+
+DAY = 3600. * 24.
+
+
+def event_array(evParams):
+    """(11, N) float64 array in the Fisher order from the events dict."""
+    cols = [np.atleast_1d(np.asarray(evParams[k], dtype=np.float64)) for k in PARAMS]
+    n = max(len(c) for c in cols)
+    cols = [np.broadcast_to(c, (n,)) if len(c) != n else c for c in cols]
+    return np.ascontiguousarray(np.stack(cols))
+
+
+def _prep(evParams):
+    utils.check_evparams(evParams)
+    utils.fill_spins(evParams)
+    return event_array(evParams)
+
+
+def _arm_slots(signals):
+    return [1 if s.detector_shape == 'L' else 3 for s in signals]
+
+
+def snr_batch(signals, evParams, res=1000, device=0):
+    """Per-arm SNRs of all signals in one library call.  Returns a list (per signal) of (arms, N) arrays."""
+    p = _prep(evParams)
+    wf = signals[0].wf_model
+    if any(type(s.wf_model) is not type(wf) for s in signals):
+        return [s._snr_arms(evParams, res) for s in signals]
+    N = p.shape[1]
+    slots = _arm_slots(signals)
+    out = np.empty((sum(slots), N))
+    ctx = _lib.context(device)
+    ctx.snr([s.det_id for s in signals], wf.gpu_desc(), p, res, out_arm=out)
+    res_l, i = [], 0
+    for s, k in zip(signals, slots):
+        arms = 2. * np.sqrt(out[i:i + k])
+        arms = s._apply_duty(arms, seed=True)
+        res_l.append(arms)
+        i += k
+    return res_l
+
+
+def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', device=0):
+    """Fisher matrices of all signals in one library call.
+
+    per_arm: list (per signal) of (arms, N, 11, 11); otherwise the network total (N, 11, 11).
+    """
+    p = _prep(evParams)
+    wf = signals[0].wf_model
+    N = p.shape[1]
+    slots = _arm_slots(signals)
+    ctx = _lib.context(device)
+    sp = 0 if spacing == 'geom' else 1
+    duty = any(s.DutyFactor is not None for s in signals)
+    if per_arm or duty:
+        out = np.empty((sum(slots), N, 11, 11))
+        ctx.fisher([s.det_id for s in signals], wf.gpu_desc(), p, res, spacing=sp, per_arm=True, out_arm=out)
+        res_l, i = [], 0
+        for s, k in zip(signals, slots):
+            res_l.append(s._apply_duty(out[i:i + k], seed=True))
+            i += k
+        if per_arm:
+            return res_l
+        return sum(r.sum(axis=0) for r in res_l)
+    out = np.empty((N, 11, 11))
+    ctx.fisher([s.det_id for s in signals], wf.gpu_desc(), p, res, spacing=sp, per_arm=False, out_net=out)
+    return out
+
+
+def reparametrise(F, evParams, use_m1m2=False, use_chi1chi2=True):
+    """Chain rule to (m1, m2) and/or (chiS, chiA), F: (..., N, 11, 11) (gwfast/signal.py:818-842)."""
+    if not use_m1m2 and use_chi1chi2:
+        return F
+    N = F.shape[-3]
+    J = np.broadcast_to(np.eye(11), (N, 11, 11)).copy()
+    if use_m1m2:
+        m1, m2 = utils.m1m2_from_Mceta(np.asarray(evParams['Mc']), np.asarray(evParams['eta']))
+        Mc, eta = utils.Mceta_from_m1m2(m1, m2)
+        M = m1 + m2
+        J[:, 0, 0] = Mc * (3. / (5. * m1) - 1. / (5. * M))
+        J[:, 0, 1] = Mc * (3. / (5. * m2) - 1. / (5. * M))
+        J[:, 1, 0] = m2 * (m2 - m1) / M ** 3
+        J[:, 1, 1] = m1 * (m1 - m2) / M ** 3
+    if not use_chi1chi2:
+        J[:, 9, 9] = 1.; J[:, 9, 10] = 1.
+        J[:, 10, 9] = 1.; J[:, 10, 10] = -1.
+    return np.einsum('nai,...nab,nbj->...nij', J, F, J)
+
+
+class GWSignal:
+    """One interferometer (gwfast/signal.py:37-160).
+
+    ``psd_path`` may be a two-column text file (as in gwfast) or a tuple ``(f, S)``
+    of arrays.  ``device`` selects the CUDA device.
+    """
+
+    def __init__(self, wf_model, psd_path=None, detector_shape='T', det_lat=40.44, det_long=9.45, det_xax=0.,
+                 verbose=True, is_ASD=True, useEarthMotion=False, noMotion=False, fmin=2., fmax=None,
+                 IntTablePath=None, DutyFactor=None, compute2arms=True, jitCompileDerivs=False, device=0):
+        if detector_shape not in ('L', 'T'):
+            raise ValueError('Enter valid detector configuration')
+        if psd_path is None:
+            raise ValueError('Enter a valid PSD or ASD path')
+        if noMotion:
+            raise NotImplementedError('noMotion (a check-only mode of gwfast) is not implemented on the GPU path')
+        self.wf_model = wf_model
+        self.verbose = verbose
+        self.detector_shape = detector_shape
+        self.det_lat_rad = det_lat * np.pi / 180.
+        self.det_long_rad = det_long * np.pi / 180.
+        self.det_xax_rad = det_xax * np.pi / 180.
+        self.DutyFactor = DutyFactor
+        self.useEarthMotion = useEarthMotion
+        self.noMotion = noMotion
+        self.fmin = fmin
+        self.fmax = fmax
+        self.compute2arms = compute2arms
+        self.angbtwArms = 0.5 * np.pi if detector_shape == 'L' else np.pi / 3.
+        if isinstance(psd_path, (tuple, list)):
+            f, S = (np.asarray(a, dtype=np.float64) for a in psd_path)
+            self.psd_base_path, self.psd_file_name = '', '<array>'
+        else:
+            noise = np.loadtxt(psd_path, usecols=(0, 1))
+            f, S = noise[:, 0], noise[:, 1]
+            self.psd_base_path = '/'.join(psd_path.split('/')[:-1])
+            self.psd_file_name = psd_path.split('/')[-1]
+        if is_ASD:
+            S = S ** 2
+        self.strainFreq = f
+        self.noiseCurve = S
+        np.random.seed(None)
+        self.seedUse = np.random.randint(2 ** 32 - 1, size=1)
+        self.device = device
+        self.det_id = _lib.context(device).add_detector(self.det_lat_rad, self.det_long_rad, self.det_xax_rad,
+                                                        detector_shape, useEarthMotion, fmin, fmax, f, S)
+
+    def _update_seed(self, seed=None):
+        np.random.seed(None)
+        self.seedUse = np.random.randint(2 ** 32 - 1, size=1) if seed is None else seed
+
+    def _apply_duty(self, arms, seed=True):
+        """Bernoulli duty-cycle masks drawn exactly as gwfast draws them (gwfast/signal.py:672-673, :729-765)."""
+        if self.DutyFactor is None:
+            return arms
+        if seed:
+            np.random.seed(self.seedUse)
+        out = np.array(arms, copy=True)
+        n = out.shape[1]
+        for a in range(out.shape[0]):
+            excl = np.random.choice([0, 1], n, p=[1. - self.DutyFactor, self.DutyFactor])
+            out[a] = out[a] * excl.reshape((n,) + (1,) * (out.ndim - 2))
+        return out
+
+    def _snr_arms(self, evParams, res):
+        return snr_batch([self], evParams, res, self.device)[0]
+
+    def SNRInteg(self, evParams, res=1000, return_all=False):
+        """gwfast/signal.py:658-777."""
+        arms = self._snr_arms(evParams, res)
+        if self.detector_shape == 'T':
+            return arms if return_all else np.sqrt((arms ** 2).sum(axis=0))
+        return arms[0]
+
+    def FisherMatr(self, evParams, res=1000, df=None, spacing='geom', use_m1m2=False, use_chi1chi2=True,
+                   use_prec_ang=True, computeDerivFinDiff=False, computeAnalyticalDeriv=True, return_all=False,
+                   return_derivatives=False, return_SNR_derivatives=False, **kwargs):
+        """gwfast/signal.py:782-1098; returns (11, 11, N), or a list per arm with return_all."""
+        if return_derivatives or return_SNR_derivatives:
+            raise NotImplementedError('return_derivatives / return_SNR_derivatives are not implemented on the GPU path')
+        if computeDerivFinDiff:
+            raise NotImplementedError('finite-difference derivatives are not used on the GPU path')
+        res = self._resolve_res(evParams, res, df)
+        Fa = fisher_batch([self], evParams, res, per_arm=True, spacing=spacing, device=self.device)[0]
+        Fa = reparametrise(Fa, evParams, use_m1m2, use_chi1chi2)
+        arms = [np.moveaxis(F, 0, -1) for F in Fa]
+        if return_all:
+            return arms
+        return arms[0] if self.detector_shape == 'L' else np.sum(arms, axis=0)
+
+    def _resolve_res(self, evParams, res, df):
+        if res is None and df is not None:
+            utils.check_evparams(evParams)
+            fcut = self.wf_model.fcut(**evParams)
+            if self.fmax is not None:
+                fcut = np.where(fcut > self.fmax, self.fmax, fcut)
+            res = np.amax(np.floor(1 + (fcut - self.fmin) / df))
+        elif res is None:
+            raise ValueError('Provide either resolution in frequency or step size.')
+        return int(res)

@@ -1,0 +1,104 @@
+"""Waveform model descriptors with gwfast's interface (gwfast/waveforms.py:49-199, :697, :959, :1838).
+
+The waveforms themselves are evaluated inside the fused CUDA kernels; these
+objects carry what gwfast's callers read from a model (``ParNums``, ``nParams``,
+the ``is_*`` flags, ``objType``, ``fcut``) plus the descriptor the C ABI needs.
+Supported: TaylorF2_RestrictedPN (optionally with the 3.5PN spin-spin terms),
+IMRPhenomD and IMRPhenomHM, aligned spins, no tides or eccentricity.
+"""
+import numpy as np
+
+from . import _lib
+from . import gwfastGlobals as glob
+
+PARAMS = ('Mc', 'eta', 'dL', 'theta', 'phi', 'iota', 'psi', 'tcoal', 'Phicoal', 'chi1z', 'chi2z')
+
+
+class WaveFormModel:
+    """Base class mirroring gwfast's WaveFormModel (gwfast/waveforms.py:49-147)."""
+
+    def __init__(self, objType, fcutPar, is_newtonian=False, is_tidal=False, is_HigherModes=False, is_chi1chi2=True,
+                 is_Precessing=False, is_LAL=False, is_prec_ang=False, is_eccentric=False, is_holomorphic=False,
+                 apply_fcut=True):
+        for flag, name in ((is_newtonian, 'is_newtonian'), (is_tidal, 'is_tidal'), (is_Precessing, 'is_Precessing'),
+                           (is_LAL, 'is_LAL'), (is_eccentric, 'is_eccentric')):
+            if flag:
+                raise NotImplementedError('%s waveforms are not implemented on the GPU path' % name)
+        if not apply_fcut:
+            raise NotImplementedError('apply_fcut=False is not implemented on the GPU path')
+        self.objType = objType
+        self.fcutPar = fcutPar
+        self.is_newtonian = is_newtonian
+        self.is_tidal = is_tidal
+        self.is_HigherModes = is_HigherModes
+        self.is_chi1chi2 = is_chi1chi2
+        self.is_Precessing = is_Precessing
+        self.is_LAL = is_LAL
+        self.is_prec_ang = is_prec_ang
+        self.is_eccentric = is_eccentric
+        self.is_holomorphic = is_holomorphic
+        self.apply_fcut = apply_fcut
+        self.nParams = 11
+        if is_chi1chi2:
+            self.ParNums = {'Mc': 0, 'eta': 1, 'dL': 2, 'theta': 3, 'phi': 4, 'iota': 5, 'psi': 6, 'tcoal': 7,
+                            'Phicoal': 8, 'chi1z': 9, 'chi2z': 10}
+        else:
+            self.ParNums = {'Mc': 0, 'eta': 1, 'dL': 2, 'theta': 3, 'phi': 4, 'iota': 5, 'psi': 6, 'tcoal': 7,
+                            'Phicoal': 8, 'chiS': 9, 'chiA': 10}
+
+    def fcut(self, **kwargs):
+        """Cut frequency in Hz (gwfast/waveforms.py:190-199)."""
+        return self.fcutPar / (np.asarray(kwargs['Mc']) / (np.asarray(kwargs['eta']) ** (3. / 5.)))
+
+    def gpu_desc(self):
+        return _lib.WfDesc(_lib.MODEL_IDS[type(self).__name__], int(getattr(self, 'use_3p5PN_SpinHO', False)),
+                           float(self.fcutPar))
+
+    def _device_only(self, *a, **k):
+        raise NotImplementedError('%s is evaluated inside the fused GPU kernels; use GWSignal / DetNet'
+                                  % type(self).__name__)
+
+    Phi = Ampl = hphc = _device_only
+
+
+class TaylorF2_RestrictedPN(WaveFormModel):
+    """gwfast/waveforms.py:697-953 (fcut: twice the Schwarzschild ISCO by default)."""
+
+    def __init__(self, fHigh=None, is_tidal=False, use_3p5PN_SpinHO=False, phiref_vlso=False, is_eccentric=False,
+                 fRef_ecc=None, which_ISCO='Schw', use_QuadMonTid=False, **kwargs):
+        if fHigh is None:
+            fHigh = 1. / (6. * np.pi * np.sqrt(6.) * glob.GMsun_over_c3)
+        if phiref_vlso or which_ISCO != 'Schw' or use_QuadMonTid:
+            raise NotImplementedError('phiref_vlso, Kerr ISCO and QuadMonTid are not implemented on the GPU path')
+        self.use_3p5PN_SpinHO = use_3p5PN_SpinHO
+        self.phiref_vlso = phiref_vlso
+        self.fRef_ecc = fRef_ecc
+        self.which_ISCO = which_ISCO
+        self.use_QuadMonTid = use_QuadMonTid
+        super().__init__('BNS' if is_tidal else 'BBH', fHigh, is_tidal=is_tidal, is_eccentric=is_eccentric,
+                         is_holomorphic=True, **kwargs)
+
+
+class IMRPhenomD(WaveFormModel):
+    """gwfast/waveforms.py:959-1333 (fRef = lowest grid frequency)."""
+
+    def __init__(self, fRef=None, **kwargs):
+        if fRef is not None:
+            raise NotImplementedError('a fixed fRef is not implemented on the GPU path')
+        self.AMP_fJoin_INS = 0.014
+        self.PHI_fJoin_INS = 0.018
+        self.fRef = fRef
+        super().__init__('BBH', 0.2, **kwargs)
+
+    def fcut(self, **kwargs):
+        """gwfast/waveforms.py:1324-1333."""
+        return self.fcutPar / (np.asarray(kwargs['Mc']) * glob.GMsun_over_c3 / (np.asarray(kwargs['eta']) ** (3. / 5.)))
+
+
+class IMRPhenomHM(IMRPhenomD):
+    """gwfast/waveforms.py:1838-2750 (modes 21, 22, 32, 33, 43, 44)."""
+
+    def __init__(self, fRef=None, **kwargs):
+        kwargs['is_HigherModes'] = True
+        super().__init__(fRef=fRef, **kwargs)
+        self.complShiftm = np.array([0., np.pi * 0.5, 0., -np.pi * 0.5, np.pi, np.pi * 0.5, 0.])

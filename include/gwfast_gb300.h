@@ -1,0 +1,118 @@
+/*
+ * gwfast_gb300 C ABI: SNR and Fisher matrices of gravitational-wave events on one GPU.
+ *
+ * This is the drop-in boundary for the Fisher-forecast hot path of gwfast 1.1.2.
+ * gwfast itself is pure Python; the functions below are what its Python
+ * classes would bind through ctypes to move the hot path onto a GB300.  Every
+ * entry point names the reference interface it replaces.
+ *
+ * Conventions
+ *  - All functions return 0 (GWF_OK) or a negative GWF_ERR_* code; the message of
+ *    the last failure on the calling thread is returned by gwf_last_error().
+ *  - Event parameters are a structure of arrays: params[k * ld + n] holds
+ *    parameter k of event n, k in the Fisher order
+ *      0 Mc [Msun, detector frame], 1 eta, 2 dL [Gpc], 3 theta, 4 phi, 5 iota,
+ *      6 psi [rad], 7 tcoal [GMST days], 8 Phicoal [rad], 9 chi1z, 10 chi2z
+ *    (gwfast/waveforms.py:78, :125-129).
+ *  - mem = GWF_MEM_HOST: params, res_per_event and outputs are host pointers; the
+ *    call copies in, runs, copies out and returns when the outputs are written.
+ *    mem = GWF_MEM_DEVICE: all pointers are device pointers owned by the caller;
+ *    the work is queued on `stream` (NULL = the context's stream) and the call
+ *    returns without waiting.
+ *  - Fisher matrices are written row-major, 11 x 11 per event, tcoal in seconds
+ *    (gwfast/signal.py:918-920).
+ *  - One context per thread; calls on one context are serialised on its stream.
+ */
+#ifndef GWFAST_GB300_H
+#define GWFAST_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GWF_NPARAMS 11
+
+enum {
+  GWF_OK = 0,
+  GWF_ERR_INVALID_ARG = -1,
+  GWF_ERR_CUDA = -2,
+  GWF_ERR_OOM = -3,
+  GWF_ERR_TIMEOUT = -4,
+  GWF_ERR_UNSUPPORTED = -5
+};
+
+enum { GWF_WF_TAYLORF2 = 0, GWF_WF_PHENOMD = 1, GWF_WF_PHENOMHM = 2 };
+enum { GWF_SHAPE_L = 0, GWF_SHAPE_T = 1 };
+enum { GWF_SPACING_GEOM = 0, GWF_SPACING_LIN = 1 };
+enum { GWF_MEM_HOST = 0, GWF_MEM_DEVICE = 1 };
+enum { GWF_PREC_FP64 = 0, GWF_PREC_FP32 = 1 };
+
+typedef struct gwf_ctx gwf_ctx;
+
+/* Detector geometry and band (gwfast/signal.py:68-160, GWSignal.__init__). */
+typedef struct {
+  double lat_rad;      /* latitude */
+  double long_rad;     /* longitude */
+  double xax_rad;      /* bisector of the (first) arms w.r.t. local East */
+  int shape;           /* GWF_SHAPE_L or GWF_SHAPE_T */
+  int earth_rotation;  /* useEarthMotion */
+  double fmin;         /* Hz */
+  double fmax;         /* Hz, <= 0 for none */
+} gwf_det_desc;
+
+/* Waveform model (gwfast/waveforms.py:49-199 WaveFormModel; :697 TaylorF2_RestrictedPN,
+ * :959 IMRPhenomD, :1838 IMRPhenomHM). */
+typedef struct {
+  int model;           /* GWF_WF_* */
+  int spin_ho;         /* TaylorF2 use_3p5PN_SpinHO */
+  double fcut_par;     /* TaylorF2: fHigh [Hz] (default 2 f_ISCO); IMR models: Mf cut (0.2) */
+} gwf_wf_desc;
+
+/* Context: device selection, PSD tables, staging memory.
+ * Replaces the per-process JAX/XLA set-up of gwfast/signal.py:162-214 (_init_jax). */
+int gwf_ctx_create(int device, gwf_ctx** out);
+int gwf_ctx_destroy(gwf_ctx* ctx);
+const char* gwf_last_error(void);
+int gwf_version(void);
+
+/* IMRPhenomD quasi-normal-mode table (spin, fring, fdamp), gwfast/waveforms.py:988-990. */
+int gwf_set_qnm_table(gwf_ctx* ctx, const double* spin, const double* fring, const double* fdamp, int64_t n);
+
+/* Register one detector and its PSD (strictly increasing psd_f, PSD not ASD).
+ * Replaces GWSignal.__init__ geometry and noise-curve loading, gwfast/signal.py:86-147. */
+int gwf_detector_add(gwf_ctx* ctx, const gwf_det_desc* desc, const double* psd_f, const double* psd_S,
+                     int64_t n, int* det_id);
+
+/* Optimal SNR of N events in n_det detectors.
+ * Replaces GWSignal.SNRInteg (gwfast/signal.py:658-777) and DetNet.SNR (gwfast/network.py:278-306).
+ * out_arm (may be NULL): per arm slot (L: 1 slot, triangle: 3 slots, in det_ids order),
+ *   [slots][N] of trapz((A+^2 + Ax^2)/S, f), i.e. (SNR_arm / 2)^2.
+ * out_net (may be NULL): [N] network SNR^2 = sum over arms of 4 * out_arm. */
+int gwf_snr(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params, int64_t ld,
+            int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int mem,
+            double* out_arm, double* out_net, void* stream);
+
+/* Fisher matrices of N events in n_det detectors.
+ * Replaces GWSignal.FisherMatr (gwfast/signal.py:782-1098, default arguments
+ * use_chi1chi2=True, computeAnalyticalDeriv=True) and DetNet.FisherMatr (gwfast/network.py:309-343).
+ * per_arm != 0: out_arm receives [slots][N][11][11] per arm (return_all=True);
+ * out_net (may be NULL): [N][11][11] network total. */
+int gwf_fisher(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params, int64_t ld,
+               int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int per_arm, int mem,
+               double* out_arm, double* out_net, void* stream);
+
+/* Covariance by equilibrated Cholesky inversion, FP64, one 11x11 matrix per event.
+ * Replaces fisherTools.CovMatr 'cho' path (gwfast/fisherTools.py:32-196) together with
+ * compute_inversion_error (:199-212); cond receives the condition number of the
+ * diagonally equilibrated matrix (:81-88).  F, cov: [N][11][11]; eps, cond: [N] (may be NULL).
+ * Events whose equilibrated matrix is not positive definite get NaN covariances. */
+int gwf_cov(gwf_ctx* ctx, const double* F, int64_t n_events, int mem, double* cov, double* eps, double* cond,
+            void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GWFAST_GB300_H */

@@ -1,0 +1,229 @@
+"""Generate golden vectors by running gwfast's own sources (v1.1.2) in this container.
+
+gwfast imports jax, h5py and numdifftools, none of which are installed here.  The
+hot-path code it runs is plain array arithmetic, so this script installs small
+stand-in modules before importing it:
+
+* ``jax.numpy`` is numpy itself (float64, same function names);
+* ``jax.jacrev`` is a 5-point central finite difference (only used for the Fisher
+  golden; the derivative error it leaves is measured and stored beside it);
+* ``jax.vmap`` loops over the leading (event) axis;
+* ``h5py`` / ``numdifftools`` are empty modules (only touched off the hot path).
+
+numpy 2 removed ``trapz`` and scipy removed ``cumtrapz``; aliases to
+``trapezoid``/``cumulative_trapezoid`` are installed for the reference's calls.
+
+The outputs are written to ``tests/golden/*.npz`` and committed; the GPU machine
+never needs the reference.  Run:  python tests/golden/make_golden.py [/root/reference]
+"""
+import os
+import sys
+import types
+
+import numpy as np
+
+REF = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+# ------------------------------------------------------------------ stand-in modules
+def _install_shims():
+    jax = types.ModuleType('jax')
+    jax.numpy = np
+    cfg = types.SimpleNamespace(update=lambda *a, **k: None)
+    jax.config = cfg
+    jax.devices = lambda *a, **k: ['cpu']
+    jax.local_device_count = lambda: 1
+    jax.device_count = lambda: 1
+
+    def vmap(fn):
+        def run(*args):
+            n = len(args[1])
+            outs = [fn(*[a[i] for a in args]) for i in range(n)]
+            if isinstance(outs[0], tuple):
+                return tuple(np.stack([o[j] for o in outs]) for j in range(len(outs[0])))
+            return np.stack(outs)
+        return run
+
+    def jacrev(fn, argnums=0, holomorphic=False):
+        nums = argnums if isinstance(argnums, tuple) else (argnums,)
+
+        def run(*args):
+            res = []
+            for j in nums:
+                x = args[j]
+                xr = np.real(x)
+                h = 1e-7 * max(abs(float(xr)), 1e-1) if j in (1, 2) else 1e-6
+                def at(d):
+                    a = list(args)
+                    a[j] = x + d
+                    return np.asarray(fn(*a))
+                d1 = (-at(2 * h) + 8 * at(h) - 8 * at(-h) + at(-2 * h)) / (12 * h)
+                res.append(d1)
+            return tuple(res) if isinstance(argnums, tuple) else res[0]
+        return run
+
+    jax.vmap = vmap
+    jax.jacrev = jacrev
+    jax.jit = lambda f, **k: f
+    jax.pmap = lambda f, **k: f
+
+    class custom_jvp:
+        def __init__(self, fun, nondiff_argnums=()):
+            self.fun = fun
+
+        def defjvp(self, jvp):
+            return jvp
+
+        def __call__(self, *a, **k):
+            return self.fun(*a, **k)
+    jax.custom_jvp = custom_jvp
+    interp = types.ModuleType('jax.interpreters')
+    interp.xla = types.ModuleType('jax.interpreters.xla')
+    jax.interpreters = interp
+    sys.modules['jax'] = jax
+    sys.modules['jax.numpy'] = np
+    sys.modules['jax.interpreters'] = interp
+    sys.modules['jax.interpreters.xla'] = interp.xla
+    sys.modules['h5py'] = types.ModuleType('h5py')
+    ndt = types.ModuleType('numdifftools')
+    sg = types.ModuleType('numdifftools.step_generators')
+    sg.MaxStepGenerator = lambda **k: None
+    ndt.step_generators = sg
+    sys.modules['numdifftools'] = ndt
+    sys.modules['numdifftools.step_generators'] = sg
+    np.trapz = np.trapezoid
+    import scipy.integrate as igt
+    igt.cumtrapz = igt.cumulative_trapezoid
+
+
+_install_shims()
+sys.path.insert(0, REF)
+import gwfast.gwfastGlobals as glob          # noqa: E402
+import gwfast.waveforms as WF                 # noqa: E402
+import gwfast.signal as SIG                   # noqa: E402
+import gwfast.network as NET                  # noqa: E402
+
+
+def _init_no_jit(self):
+    self._SignalDerivatives_use = self._SignalDerivatives
+
+
+SIG.GWSignal._init_jax = _init_no_jit
+
+
+def aligo_psd(f):
+    x = f / 215.
+    return 1e-49 * (x ** -4.14 - 5. * x ** -2 + 111. * (1. - x * x + 0.5 * x ** 4) / (1. + 0.5 * x * x))
+
+
+def psd_file(fwall, n=2000):
+    f = np.geomspace(fwall, 1e4, n)
+    path = os.path.join('/tmp', 'gwf_psd_%g.txt' % fwall)
+    np.savetxt(path, np.stack([f, aligo_psd(f)], 1))
+    return path
+
+
+def events_bns(rng, n):
+    m = np.sort(rng.uniform(1.1, 2.0, (n, 2)), axis=1)[:, ::-1]
+    m1, m2 = m[:, 0], m[:, 1]
+    Mc = (m1 * m2) ** 0.6 / (m1 + m2) ** 0.2
+    eta = m1 * m2 / (m1 + m2) ** 2
+    return _angles(rng, n, dict(Mc=Mc, eta=eta, chi1z=rng.uniform(-.05, .05, n), chi2z=rng.uniform(-.05, .05, n),
+                                dL=rng.uniform(0.05, 0.5, n)))
+
+
+def events_bbh(rng, n, mmax=80., qmin=0.2, chimax=0.8):
+    u = rng.uniform(0, 1, n)
+    a = -2.3 + 1.
+    m1 = (5. ** a + u * (mmax ** a - 5. ** a)) ** (1. / a)
+    q = rng.uniform(qmin, 1., n)
+    m2 = q * m1
+    Mc = (m1 * m2) ** 0.6 / (m1 + m2) ** 0.2
+    eta = m1 * m2 / (m1 + m2) ** 2
+    return _angles(rng, n, dict(Mc=Mc, eta=eta, chi1z=rng.uniform(-chimax, chimax, n),
+                                chi2z=rng.uniform(-chimax, chimax, n), dL=rng.uniform(0.5, 10., n)))
+
+
+def _angles(rng, n, ev):
+    ev.update(theta=np.arccos(rng.uniform(-1, 1, n)), phi=rng.uniform(0, 2 * np.pi, n),
+              iota=np.arccos(rng.uniform(-1, 1, n)), psi=rng.uniform(0, np.pi, n),
+              tcoal=rng.uniform(0, 1, n), Phicoal=rng.uniform(0, 2 * np.pi, n))
+    return ev
+
+
+KEYS = ('Mc', 'eta', 'dL', 'theta', 'phi', 'iota', 'psi', 'tcoal', 'Phicoal', 'chi1z', 'chi2z')
+
+
+def make_case(name, wf, dets, events, res, fisher=True):
+    out = {'res': np.array(res)}
+    for k in KEYS:
+        out['ev_' + k] = np.asarray(events[k], dtype=np.float64)
+    sigs = {}
+    for dname, (fwall, earth) in dets.items():
+        d = glob.detectors[dname]
+        sigs[dname] = SIG.GWSignal(wf, psd_path=psd_file(fwall), detector_shape=d['shape'], det_lat=d['lat'],
+                                   det_long=d['long'], det_xax=d['xax'], verbose=False, is_ASD=False,
+                                   useEarthMotion=earth, fmin=fwall)
+    net = NET.DetNet(sigs, verbose=False)
+    ev = {k: np.array(v) for k, v in events.items()}
+    snrs = net.SNR(dict(ev), res=res, return_all=True)
+    for k, v in snrs.items():
+        out['snr_' + k] = np.asarray(v)
+    # waveform pieces on the first detector's grid
+    d0 = list(sigs.values())[0]
+    fc = wf.fcut(**ev)
+    fg = np.geomspace(np.full(fc.shape, d0.fmin), fc, num=res)
+    out['fgrid'] = fg
+    out['tau_star'] = wf.tau_star(fg, **ev)
+    out['fcut'] = fc
+    if wf.is_HigherModes:
+        hp, hc = wf.hphc(fg, **ev)
+        out['hp'], out['hc'] = hp, hc
+    else:
+        out['Phi'] = wf.Phi(fg, **ev)
+        out['Ampl'] = wf.Ampl(fg, **ev)
+    for dname, s in sigs.items():
+        rots = (0.,) if s.detector_shape == 'L' else (0., 60.)
+        fc_d = fc if s.fmax is None else np.minimum(fc, s.fmax)
+        fgd = np.geomspace(np.full(fc_d.shape, s.fmin), fc_d, num=res)
+        for r in rots:
+            tag = '%s_r%d' % (dname, int(r))
+            args = [fgd] + [ev[k] for k in ('Mc', 'eta', 'dL', 'theta', 'phi', 'iota', 'psi', 'tcoal', 'Phicoal',
+                                             'chi1z', 'chi2z')]
+            z = np.zeros_like(ev['Mc'])
+            h = s.GWstrain(*args, z, z, z, z, z, z, z, rot=r, is_chi1chi2=True)
+            out['strain_' + tag] = h
+            der = s._AnalyticalDerivatives(*args, z, z, z, z, z, z, z, rot=r, use_chi1chi2=True)
+            for nm, dv in zip(('dL', 'theta', 'phi', 'iota', 'psi', 'tcoal', 'Phicoal'), der):
+                if dv is not None:
+                    out['dana_%s_%s' % (nm, tag)] = np.asarray(dv)
+    if fisher:
+        Fs = net.FisherMatr(dict(ev), res=res, return_all=True)
+        for k, v in Fs.items():
+            out['fisher_' + k] = np.asarray(v)
+    np.savez_compressed(os.path.join(OUT, name + '.npz'), **out)
+    print('wrote', name, sorted(out.keys())[:6], '...')
+
+
+def main():
+    rng = np.random.default_rng(1000)
+    make_case('tf2_L_noearth', WF.TaylorF2_RestrictedPN(), {'Virgo': (10., False)}, events_bns(rng, 4), 400)
+    rng = np.random.default_rng(1001)
+    make_case('tf2_T_earth', WF.TaylorF2_RestrictedPN(use_3p5PN_SpinHO=True), {'ETS': (10., True)},
+              events_bns(rng, 3), 300)
+    rng = np.random.default_rng(1002)
+    make_case('phd_net_earth', WF.IMRPhenomD(), {'L1': (10., True), 'H1': (10., True), 'ETS': (5., True)},
+              events_bbh(rng, 4), 300)
+    rng = np.random.default_rng(1003)
+    make_case('phm_net_earth', WF.IMRPhenomHM(), {'L1': (10., True), 'ETS': (5., True)},
+              events_bbh(rng, 3, mmax=150., qmin=0.1, chimax=0.9), 300)
+    # KAT from the reference tutorial: GW170817-like TF2 Schwarzschild cut frequency 1590.1 Hz
+    z = 0.00980
+    ev = {'Mc': np.array([1.1859 * (1. + z)]), 'eta': np.array([0.24786618323504223])}
+    np.savez_compressed(os.path.join(OUT, 'kat_fcut.npz'), fcut=WF.TaylorF2_RestrictedPN().fcut(**ev),
+                        Mc=ev['Mc'], eta=ev['eta'])
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,127 @@
+"""The oracle against golden vectors produced by gwfast's own sources (tests/golden/make_golden.py)."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden')
+CASES = {
+    'tf2_L_noearth': (O.Model('TF2'), {'Virgo': (10., False)}),
+    'tf2_T_earth': (O.Model('TF2', spin_ho=True), {'ETS': (10., True)}),
+    'phd_net_earth': (O.Model('PhenomD'), {'L1': (10., True), 'H1': (10., True), 'ETS': (5., True)}),
+    'phm_net_earth': (O.Model('PhenomHM'), {'L1': (10., True), 'ETS': (5., True)}),
+}
+
+
+def load(name):
+    g = np.load(os.path.join(GOLD, name + '.npz'))
+    ev = {k: g['ev_' + k] for k in O.PARAMS}
+    return g, O.to_params(ev), int(g['res'])
+
+
+def det_of(name, fw, earth):
+    lat, lon, xax, sh = O.DETECTORS[name]
+    f = np.geomspace(fw, 1e4, 2000)
+    return O.Detector(lat, lon, xax, sh, fmin=fw, psd_f=f, psd_S=O.aligo_psd(f), earth=earth)
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.max(np.abs(a - b)) / np.max(np.abs(b))
+
+
+def test_kat_tf2_fcut():
+    # gwfast new_features_tutorial: TF2 Schwarzschild cut of the GW170817-like event is 1590.1 Hz
+    g = np.load(os.path.join(GOLD, 'kat_fcut.npz'))
+    fc = float(O.tf2_fcut(torch.tensor(g['Mc']), torch.tensor(g['eta']))[0])
+    assert abs(fc - float(g['fcut'][0])) < 1e-9 * fc
+    assert round(fc, 1) == 1590.1
+
+
+@pytest.mark.parametrize('name', list(CASES))
+def test_waveform_values(name):
+    model, _ = CASES[name]
+    g, p, res = load(name)
+    f = torch.as_tensor(g['fgrid'].T.copy())
+    assert rel(model.fcut(p['Mc'], p['eta']).reshape(-1), g['fcut']) < 1e-14
+    assert rel(O.tau_star(f, p['Mc'], p['eta']), g['tau_star'].T) < 1e-13
+    if model.is_hm:
+        hp, hc = model.hphc(f, p)
+        assert rel(hp.numpy(), g['hp'].T) < 1e-10
+        assert rel(hc.numpy(), g['hc'].T) < 1e-10
+    else:
+        assert rel(model.phase(f, p), g['Phi'].T) < 1e-13
+        assert rel(model.ampl(f, p), g['Ampl'].T) < 1e-13
+
+
+@pytest.mark.parametrize('name', list(CASES))
+def test_strain_and_closed_form_derivatives(name):
+    """Oracle AD derivatives equal gwfast's closed-form extrinsic derivatives (gwfast/signal.py:1303-1584).
+
+    For the IMR models the last grid point sits at Mf = 0.2 within an ulp of the cut, where the two
+    implementations can legitimately disagree on which side of the cut it falls; it is excluded.
+    """
+    model, dets = CASES[name]
+    g, p, res = load(name)
+    last = -1 if model.name != 'TF2' else None
+    for dn, (fw, earth) in dets.items():
+        det = det_of(dn, fw, earth)
+        fg, S = O.event_grid(det, model, p, res)
+        for rot in det.rots:
+            tag = '%s_r%d' % (dn, int(rot))
+            h = O.strain(det, model, fg, p, rot).numpy()[:, :last]
+            assert rel(h, g['strain_' + tag].T[:, :last]) < 1e-7
+            J = O.strain_jacobian(det, model, fg, p, rot)
+            for i, nm in enumerate(O.PARAMS):
+                k = 'dana_%s_%s' % (nm, tag)
+                if k in g:
+                    assert rel(J[i].numpy()[:, :last], g[k].T[:, :last]) < 2e-6, (tag, nm)
+
+
+@pytest.mark.parametrize('name', list(CASES))
+def test_snr(name):
+    model, dets = CASES[name]
+    g, p, res = load(name)
+    tol = 1e-12 if not model.is_hm else 1e-10
+    for dn, (fw, earth) in dets.items():
+        det = det_of(dn, fw, earth)
+        arms = O.snr_arms(det, model, p, res)
+        if det.shape == 'L':
+            assert rel(arms[0], g['snr_' + dn]) < tol
+        else:
+            for i in range(3):
+                assert rel(arms[i], g['snr_%s_%d' % (dn, i)]) < tol
+
+
+@pytest.mark.parametrize('name', list(CASES))
+def test_fisher_against_reference_path(name):
+    """Full reference FisherMatr path; its AD derivatives were replaced by 5-point finite differences,
+    whose rounding through the 1e8-rad phase limits that golden to ~1e-4 of sqrt(F_aa F_bb)."""
+    model, dets = CASES[name]
+    g, p, res = load(name)
+    for dn, (fw, earth) in dets.items():
+        det = det_of(dn, fw, earth)
+        Fa = O.fisher_arms(det, model, p, res)
+        names = [dn] if det.shape == 'L' else ['%s_%d' % (dn, i) for i in range(3)]
+        for nm, F in zip(names, Fa):
+            Fr = np.moveaxis(g['fisher_' + nm], -1, 0)
+            d = np.sqrt(np.abs(np.einsum('nii->ni', Fr)))
+            err = np.abs(F.numpy() - Fr) / (d[:, :, None] * d[:, None, :])
+            assert err.max() < 5e-4, (nm, err.max())
+
+
+@pytest.mark.parametrize('name', ['tf2_L_noearth', 'phd_net_earth'])
+def test_identities(name):
+    """F_dLdL = (SNR/dL)^2 and F_PhicPhic = SNR^2 for 22-mode models (gwfast_tutorial cell 15)."""
+    model, dets = CASES[name]
+    g, p, res = load(name)
+    dn, (fw, earth) = next(iter(dets.items()))
+    det = det_of(dn, fw, earth)
+    F = O.fisher(det, model, p, res)
+    snr = O.snr(det, model, p, res)
+    dL = p['dL'].reshape(-1)
+    assert np.allclose(F[:, 2, 2], (snr / dL) ** 2, rtol=1e-12)
+    assert np.allclose(F[:, 8, 8], snr ** 2, rtol=1e-12)
