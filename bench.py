@@ -6,17 +6,20 @@ triangle at Sardinia (5 Hz wall), Earth rotation on, 2000 log-spaced frequency p
 per event and detector, analytic aLIGO PSD fit.  One step = the network Fisher matrix
 (11x11, summed over detectors and arms) of every event.
 
-value: events / s with the event arrays resident in HBM, CUDA-event timed per step
-(L2 flushed by a 256 MB write before each step, outside the timed interval).
-e2e:   the same through the public API (DetNet.FisherMatr on a host events dict),
-       wall-clock, host->device copy of the parameters and device->host copy of the
-       Fisher matrices included.
+value: events/s of the chosen form (FP32 split precision) with the event arrays resident
+       in HBM, CUDA-event timed per step (L2 flushed by a 256 MB write before each step,
+       outside the timed interval).  The plain FP64 kernel is timed the same way
+       (`plain_fp64`), and the chosen form's marginalised 1-sigma errors are compared with
+       the FP64 ones on the workload's events (`sigma_err`).
+e2e:   the chosen form through the public API (DetNet.FisherMatr on a host events dict),
+       wall-clock, host->device copy of the parameters and device->host copy of the Fisher
+       matrices included.
 Multi-GPU: one replica per GPU on its own seeded shard (events are independent; no
-collective), value = all ranks' events / max-over-ranks time.
+collective); value = all ranks' events / max-over-ranks time.
 
---impl reference: the CPU float64 oracle restatement of gwfast's algorithm (gwfast
-itself needs jax[cpu], which is not installable here) on a bounded sample of the same
-workload, on all host cores.
+--impl reference: the CPU float64 oracle restatement of gwfast's algorithm (gwfast itself
+needs jax[cpu], which is not installable here) on a bounded sample of the same workload, on
+all host cores.
 """
 import argparse
 import json
@@ -140,10 +143,11 @@ def measured_peaks():
         return {}
 
 
-def fp64_peak(torch, dev):
-    """Dense FP64 throughput of cuBLAS DGEMM (4096^3), best of 5: the FP64 denominator."""
-    a = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
-    b = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+def gemm_peak(torch, dev, dtype, n):
+    """Dense GEMM throughput (cuBLAS through torch.matmul, TF32 off), best of 5, TFLOP/s."""
+    torch.backends.cuda.matmul.allow_tf32 = False
+    a = torch.randn(n, n, dtype=dtype, device=dev)
+    b = torch.randn(n, n, dtype=dtype, device=dev)
     torch.matmul(a, b)
     torch.cuda.synchronize()
     best = 1e30
@@ -154,7 +158,7 @@ def fp64_peak(torch, dev):
         e1.record()
         torch.cuda.synchronize()
         best = min(best, e0.elapsed_time(e1) / 1e3)
-    return 2 * 4096 ** 3 / best / 1e12
+    return 2 * n ** 3 / best / 1e12
 
 
 def main():
@@ -166,6 +170,8 @@ def main():
     ap.add_argument('--events', type=int, default=N_EVENTS)
     ap.add_argument('--ref-events', type=int, default=6)
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--only-device', action='store_true', help='only the device-resident Fisher steps (for ncu)')
+    ap.add_argument('--precision', default='fp32', choices=('fp32', 'fp64'), help='form used with --only-device')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
@@ -176,7 +182,7 @@ def main():
         dist.init_process_group('nccl' if torch.cuda.is_available() else 'gloo')
     torch.cuda.set_device(local)
     dev = torch.device('cuda', local)
-    from gwfast_gb300 import _build, _lib, synthetic
+    from gwfast_gb300 import _build, _lib, fisherTools, synthetic
     from gwfast_gb300 import waveforms as W
     from gwfast_gb300.signal import event_array
     _build.build()
@@ -190,14 +196,16 @@ def main():
     p_host = event_array(ev)
     p_dev = torch.from_numpy(p_host).to(dev)
     out = torch.empty((N, 11, 11), dtype=torch.float64, device=dev)
+    out64 = torch.empty((N, 11, 11), dtype=torch.float64, device=dev)
     snr_out = torch.empty((N,), dtype=torch.float64, device=dev)
-    stream = torch.cuda.current_stream(dev)
+    stream = torch.cuda.Stream(dev)   # a real stream handle: NULL would mean the library's own stream
+    torch.cuda.set_stream(stream)
     desc = wf.gpu_desc()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
 
-    def fisher_step(det_ids=ids, o=out):
+    def fisher_step(det_ids=ids, o=out, precision='fp32'):
         ctx.fisher(det_ids, desc, p_dev, RES, per_arm=False, mem=_lib.MEM_DEVICE, out_net=o, stream=stream.cuda_stream,
-                   ld=N, n=N)
+                   ld=N, n=N, precision=precision)
 
     def snr_step():
         ctx.snr(ids, desc, p_dev, RES, mem=_lib.MEM_DEVICE, out_net=snr_out, stream=stream.cuda_stream, ld=N, n=N)
@@ -214,8 +222,15 @@ def main():
             tot += e0.elapsed_time(e1)
         return tot / k
 
+    if args.only_device:
+        for _ in range(args.warmup + args.steps):
+            fisher_step(precision=args.precision)
+        torch.cuda.synchronize()
+        print(json.dumps({'only_device': True, 'events': N, 'steps': args.steps, 'precision': args.precision}))
+        return
     for _ in range(args.warmup):
         fisher_step()
+        fisher_step(o=out64, precision='fp64')
         snr_step()
     torch.cuda.synchronize()
     if world > 1:
@@ -228,21 +243,34 @@ def main():
         torch.distributed.barrier()
     torch.cuda.synchronize()
     clocks = clk.stop()
+    ms64 = timed(lambda: fisher_step(o=out64, precision='fp64'), args.steps)
     ms_snr = timed(snr_step, args.steps)
-    # dominant kernel: the ET triangle (2 computed arms) launch alone
+    # per-kernel launches alone: the ET triangle kernel dominates
     ms_et = timed(lambda: fisher_step([ids[2]]), args.steps)
     ms_l1 = timed(lambda: fisher_step([ids[0]]), args.steps)
+    ms_et64 = timed(lambda: fisher_step([ids[2]], precision='fp64'), max(1, args.steps // 2))
     if world > 1:
-        t = torch.tensor([ms, ms_snr], dtype=torch.float64, device=dev)
+        t = torch.tensor([ms, ms64, ms_snr], dtype=torch.float64, device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms, ms_snr = float(t[0]), float(t[1])
+        ms, ms64, ms_snr = (float(x) for x in t)
+    # accuracy of the chosen form on this workload: marginalised 1-sigma errors against FP64
+    fisher_step()
+    fisher_step(o=out64, precision='fp64')
+    torch.cuda.synchronize()
+    nchk = min(N, 4000)
+    F32 = out[:nchk].cpu().numpy()
+    F64 = out64[:nchk].cpu().numpy()
+    c32, _, _ = fisherTools.CovMatr(np.moveaxis(F32, 0, -1), return_cond=True, device=local)
+    c64, _, cond = fisherTools.CovMatr(np.moveaxis(F64, 0, -1), return_cond=True, device=local)
+    s32, s64 = np.sqrt(np.einsum('iin->ni', c32)), np.sqrt(np.einsum('iin->ni', c64))
+    serr = np.nanmax(np.abs(s32 - s64) / s64, axis=1)
     # end to end through the public API with host buffers
     for _ in range(max(1, args.warmup // 2)):
-        net.FisherMatr(dict(ev), res=RES)
+        net.FisherMatr(dict(ev), res=RES, precision='fp32')
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        F_host = net.FisherMatr(dict(ev), res=RES)
+        F_host = net.FisherMatr(dict(ev), res=RES, precision='fp32')
     e2e_s = (time.perf_counter() - t0) / args.steps
     if rank != 0:
         torch.distributed.destroy_process_group()
@@ -250,24 +278,35 @@ def main():
     ops = json.load(open(os.path.join(ROOT, 'profiles', 'opcounts.json')))['counts']['IMRPhenomD/earth']
     flop_arm_pt = ops['fisher_per_arm_point']
     flops_et = N * RES * 3 * flop_arm_pt
-    peak64 = fp64_peak(torch, dev)
+    peak32 = gemm_peak(torch, dev, torch.float32, 8192)
+    peak64 = gemm_peak(torch, dev, torch.float64, 4096)
     ach = flops_et / (ms_et / 1e3) / 1e12
+    ach64 = flops_et / (ms_et64 / 1e3) / 1e12
     line = {
         'metric': METRIC, 'value': world * N / (ms / 1e3), 'unit': 'Fisher/s', 'n_gpus': world, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
-        'dtype': 'f64', 'data': 'synthetic (seeded BBH catalogue, analytic aLIGO PSD fit)',
-        'config': {'workload': 'IMRPhenomD BBH 1e4 events, L1+H1+ETS, Earth rotation, R=2000, FP64 kernel',
+        'dtype': 'f32 per point (f64 per-event set-up, scaling and outputs)',
+        'data': 'synthetic (seeded BBH catalogue, analytic aLIGO PSD fit)',
+        'config': {'workload': 'IMRPhenomD BBH 1e4 events, L1+H1+ETS, Earth rotation, R=2000; FP32 split-precision kernel',
                    'events_per_gpu': N, 'res': RES, 'parallelism': 'replicas over event shards' if world > 1 else 'single',
                    'l2': 'flushed (256 MB write) before every step'},
+        'plain_fp64': {'value': world * N / (ms64 / 1e3), 'unit': 'Fisher/s', 'ms_per_step': ms64},
+        'speedup_vs_plain_fp64': ms64 / ms,
+        'sigma_err': {'events': int(nchk), 'median': float(np.nanmedian(serr)), 'p99': float(np.nanpercentile(serr, 99)),
+                      'max': float(np.nanmax(serr)), 'frac_le_1e-3': float(np.mean(serr <= 1e-3)),
+                      'what': 'max over 11 parameters of |sigma_fp32 - sigma_fp64| / sigma_fp64 per event'},
         'snr_per_s': world * N / (ms_snr / 1e3),
-        'gpu_launches': 3,
+        'gpu_launches': 6,
         'e2e': {'value': world * N / e2e_s, 'unit': 'Fisher/s', 'h2d_bytes_per_step': int(p_host.nbytes),
                 'd2h_bytes_per_step': int(F_host.nbytes)},
-        'roofline': {'bound': 'fp64', 'kernel': 'fisher_kernel<IMRPhenomD, earth, triangle>',
-                     'achieved': ach, 'peak': peak64, 'unit': 'TFLOP/s', 'frac': ach / peak64,
-                     'peak_source': 'cuBLAS DGEMM 4096^3 measured in this run',
+        'roofline': {'bound': 'fp32', 'kernel': 'fisher_kernel_f32<IMRPhenomD, earth, triangle>',
+                     'achieved': ach, 'peak': peak32, 'unit': 'TFLOP/s', 'frac': ach / peak32,
+                     'peak_source': 'cuBLAS SGEMM 8192^3 (TF32 off) measured in this run',
                      'algorithmic_flop_per_launch': flops_et, 'launch_ms': ms_et, 'traffic': None,
                      'flop_model': 'profiles/opcounts.json IMRPhenomD/earth fisher_per_arm_point x 3 arms x R x N'},
+        'roofline_fp64': {'bound': 'fp64', 'kernel': 'fisher_kernel<IMRPhenomD, earth, triangle>', 'achieved': ach64,
+                          'peak': peak64, 'unit': 'TFLOP/s', 'frac': ach64 / peak64, 'launch_ms': ms_et64,
+                          'peak_source': 'cuBLAS DGEMM 4096^3 measured in this run'},
         'launch_ms': {'L1': ms_l1, 'ETS': ms_et},
         'clocks': clocks,
         'hbm_peak_gbs': measured_peaks().get('hbm_gbs'),

@@ -15,6 +15,7 @@ GWF_OK = 0
 ERRORS = {-1: 'invalid argument', -2: 'CUDA error', -3: 'out of memory', -4: 'timeout', -5: 'unsupported'}
 MODEL_IDS = {'TaylorF2_RestrictedPN': 0, 'IMRPhenomD': 1, 'IMRPhenomHM': 2}
 MEM_HOST, MEM_DEVICE = 0, 1
+PRECISION = {'fp64': 0, 'fp32': 1}
 
 
 class GWFError(RuntimeError):
@@ -46,7 +47,7 @@ SIGNATURES = {
     'gwf_snr': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32, _vp, ctypes.c_int,
                  ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
     'gwf_fisher': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32, _vp, ctypes.c_int,
-                    ctypes.c_int, ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
+                    ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
     'gwf_cov': ([_vp, _vp, _i64, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
 }
 
@@ -132,12 +133,13 @@ class Context:
                              ptr(res_ev), spacing, mem, ptr(out_arm), ptr(out_net), stream))
 
     def fisher(self, det_ids, wf, params, res, res_ev=None, spacing=0, per_arm=False, mem=MEM_HOST, out_arm=None,
-               out_net=None, stream=None, ld=None, n=None):
+               out_net=None, stream=None, ld=None, n=None, precision='fp64'):
         ids = np.ascontiguousarray(det_ids, dtype=np.int32)
         n = params.shape[1] if n is None else n
         ld = (params.shape[1] if ld is None else ld)
         check(load().gwf_fisher(self.h, len(ids), ptr(ids), ctypes.byref(wf), ptr(params), ld, n, int(res),
-                                ptr(res_ev), spacing, int(bool(per_arm)), mem, ptr(out_arm), ptr(out_net), stream))
+                                ptr(res_ev), spacing, int(bool(per_arm)), PRECISION[precision], mem, ptr(out_arm),
+                                ptr(out_net), stream))
 
     def cov(self, F, mem=MEM_HOST, cov=None, eps=None, cond=None, n=None, stream=None):
         n = F.shape[0] if n is None else n

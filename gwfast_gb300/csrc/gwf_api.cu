@@ -67,8 +67,10 @@ struct DetRec {
   double* d_f = nullptr;
   double* d_S = nullptr;
   int* d_acc = nullptr;
+  float* d_f32 = nullptr;
+  float* d_s32 = nullptr;
   int n = 0, nacc = 0;
-  double l0 = 0.0, idl = 0.0;
+  double l0 = 0.0, idl = 0.0, scale = 1.0;
 };
 
 }  // namespace
@@ -79,7 +81,8 @@ struct gwf_ctx {
   std::vector<DetRec> dets;
   double* d_qnm = nullptr;
   int nq = 0;
-  DevBuf par, res, oarm, onet, fin, fout, feps, fcond;
+  DevBuf par, res, oarm, onet, fin, fout, feps, fcond, setup;
+  cudaEvent_t scratch_free = nullptr;  // recorded after the last launch that used the set-up scratch
   HostBuf hpar, hout;
 };
 
@@ -114,6 +117,9 @@ gwf::DetDev dev_of(const DetRec& r) {
   d.nacc = r.nacc;
   d.acc_l0 = r.l0;
   d.acc_idl = r.idl;
+  d.psd_f32 = r.d_f32;
+  d.psd_s32 = r.d_s32;
+  d.psd_scale = r.scale;
   return d;
 }
 
@@ -162,13 +168,16 @@ int stage_inputs(gwf_ctx* ctx, const double* params, int64_t ld, int64_t N, cons
 }
 
 int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params,
-        int64_t ld, int64_t N, int32_t res, const int32_t* res_ev, int spacing, int per_arm, int mem,
+        int64_t ld, int64_t N, int32_t res, const int32_t* res_ev, int spacing, int per_arm, int precision, int mem,
         double* out_arm, double* out_net, void* stream) {
   int rc = check_ctx(ctx);
   if (rc) return rc;
   rc = validate_common(ctx, n_det, det_ids, wf, params, ld, N, res, res_ev, spacing, mem);
   if (rc) return rc;
   if (!out_arm && !out_net) return fail(GWF_ERR_INVALID_ARG, "no output requested");
+  if (precision != GWF_PREC_FP64 && precision != GWF_PREC_FP32) return fail(GWF_ERR_INVALID_ARG, "bad precision");
+  if (precision == GWF_PREC_FP32 && (!fisher || wf->model == GWF_WF_PHENOMHM))
+    return fail(GWF_ERR_UNSUPPORTED, "FP32 split precision is implemented for the TaylorF2 and IMRPhenomD Fisher");
   if (fisher && !per_arm) out_arm = nullptr;
   if (fisher && per_arm && !out_arm) return fail(GWF_ERR_INVALID_ARG, "per_arm needs out_arm");
   if (N == 0) return GWF_OK;
@@ -198,7 +207,13 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
       dnet = (double*)ctx->onet.p;
     }
   }
+  const size_t stride = wf->model == 0 ? gwf::setup_stride_m0() : (wf->model == 1 ? gwf::setup_stride_m1() : gwf::setup_stride_m2());
+  const size_t chunk = (size_t)(N < gwf::kChunk ? N : gwf::kChunk);
+  if (ctx->setup.ensure(chunk * stride)) return fail(GWF_ERR_OOM, "device allocation failed (set-up scratch)");
+  // the scratch is shared by every call on this context: order this call after the previous one
+  GWF_CK(cudaStreamWaitEvent(st, ctx->scratch_free, 0));
   gwf::LaunchArgs a;
+  a.scratch = (unsigned char*)ctx->setup.p;
   a.ev.p = dp;
   a.ev.ld = dld;
   a.ev.N = N;
@@ -212,6 +227,7 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
   a.qnm = ctx->d_qnm;
   a.nq = ctx->nq;
   a.per_arm = per_arm;
+  a.precision = precision;
   a.stream = st;
   int slot = 0;
   for (int i = 0; i < n_det; ++i) {
@@ -226,6 +242,7 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
     if (err != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(err));
     slot += r.desc.shape == GWF_SHAPE_T ? 3 : 1;
   }
+  GWF_CK(cudaEventRecord(ctx->scratch_free, st));
   if (mem == GWF_MEM_HOST) {
     if (out_arm) GWF_CK(cudaMemcpyAsync(out_arm, darm, (size_t)slots * N * per * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (out_net) GWF_CK(cudaMemcpyAsync(out_net, dnet, (size_t)N * per * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -250,7 +267,8 @@ int gwf_ctx_create(int device, gwf_ctx** out) {
   GWF_CK(cudaSetDevice(device));
   gwf_ctx* c = new gwf_ctx();
   c->device = device;
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->scratch_free, cudaEventDisableTiming) != cudaSuccess) {
     delete c;
     return fail(GWF_ERR_CUDA, "stream creation failed");
   }
@@ -266,11 +284,14 @@ int gwf_ctx_destroy(gwf_ctx* ctx) {
     cudaFree(r.d_f);
     cudaFree(r.d_S);
     cudaFree(r.d_acc);
+    cudaFree(r.d_f32);
+    cudaFree(r.d_s32);
   }
   cudaFree(ctx->d_qnm);
   ctx->par.release(); ctx->res.release(); ctx->oarm.release(); ctx->onet.release();
-  ctx->fin.release(); ctx->fout.release(); ctx->feps.release(); ctx->fcond.release();
+  ctx->fin.release(); ctx->fout.release(); ctx->feps.release(); ctx->fcond.release(); ctx->setup.release();
   ctx->hpar.release(); ctx->hout.release();
+  cudaEventDestroy(ctx->scratch_free);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return GWF_OK;
@@ -326,6 +347,20 @@ int gwf_detector_add(gwf_ctx* ctx, const gwf_det_desc* desc, const double* psd_f
   GWF_CK(cudaMemcpy(r.d_f, psd_f, n * sizeof(double), cudaMemcpyHostToDevice));
   GWF_CK(cudaMemcpy(r.d_S, psd_S, n * sizeof(double), cudaMemcpyHostToDevice));
   GWF_CK(cudaMemcpy(r.d_acc, acc.data(), r.nacc * sizeof(int), cudaMemcpyHostToDevice));
+  // FP32 copies: frequencies, and the PSD divided by its smallest positive value
+  double smin = INFINITY;
+  for (int64_t i = 0; i < n; ++i)
+    if (psd_S[i] > 0.0 && psd_S[i] < smin) smin = psd_S[i];
+  r.scale = std::isfinite(smin) ? smin : 1.0;
+  std::vector<float> f32(n), s32(n);
+  for (int64_t i = 0; i < n; ++i) {
+    f32[i] = (float)psd_f[i];
+    s32[i] = (float)(psd_S[i] / r.scale);
+  }
+  GWF_CK(cudaMalloc(&r.d_f32, n * sizeof(float)));
+  GWF_CK(cudaMalloc(&r.d_s32, n * sizeof(float)));
+  GWF_CK(cudaMemcpy(r.d_f32, f32.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  GWF_CK(cudaMemcpy(r.d_s32, s32.data(), n * sizeof(float), cudaMemcpyHostToDevice));
   ctx->dets.push_back(r);
   *det_id = (int)ctx->dets.size() - 1;
   return GWF_OK;
@@ -334,15 +369,15 @@ int gwf_detector_add(gwf_ctx* ctx, const gwf_det_desc* desc, const double* psd_f
 int gwf_snr(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params, int64_t ld,
             int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int mem, double* out_arm,
             double* out_net, void* stream) {
-  return run(ctx, false, n_det, det_ids, wf, params, ld, n_events, res, res_per_event, spacing, 0, mem, out_arm,
-             out_net, stream);
+  return run(ctx, false, n_det, det_ids, wf, params, ld, n_events, res, res_per_event, spacing, 0, GWF_PREC_FP64, mem,
+             out_arm, out_net, stream);
 }
 
 int gwf_fisher(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params, int64_t ld,
-               int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int per_arm, int mem,
-               double* out_arm, double* out_net, void* stream) {
-  return run(ctx, true, n_det, det_ids, wf, params, ld, n_events, res, res_per_event, spacing, per_arm, mem, out_arm,
-             out_net, stream);
+               int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int per_arm, int precision,
+               int mem, double* out_arm, double* out_net, void* stream) {
+  return run(ctx, true, n_det, det_ids, wf, params, ld, n_events, res, res_per_event, spacing, per_arm, precision, mem,
+             out_arm, out_net, stream);
 }
 
 int gwf_cov(gwf_ctx* ctx, const double* F, int64_t N, int mem, double* cov, double* eps, double* cond, void* stream) {

@@ -32,6 +32,9 @@ struct DetDev {
   const int* acc;        // log-frequency bin -> table index (accelerates the PSD lookup)
   int nacc;
   double acc_l0, acc_idl;
+  const float* psd_f32;  // FP32 copies for the split-precision kernel: frequencies and PSD / psd_scale
+  const float* psd_s32;
+  double psd_scale;
 };
 
 struct EvBatch {
@@ -334,26 +337,62 @@ __device__ __forceinline__ void wave_point_val(const EvUnion& E, const ProjEv& p
   }
 }
 
+// ------------------------------------------------------------------ per-event set-up records
+// The per-event set-up (FP64 duals) runs in its own kernel, one thread per event, and writes a
+// record per event into a scratch buffer: [GridEv | ProjEv | model coefficients].  The SNR and
+// Fisher kernels copy their event's record into shared memory.
+struct SetupHdr {
+  GridEv g;
+  ProjEv pj;
+};
+
 template <int MODEL>
-__device__ inline void block_setup(EvUnion& E, ProjEv& pj, GridEv& g, const EvBatch& ev, const DetDev& det,
-                                   const WfDesc& wf, const double* qnm, int nq, long long n) {
+__host__ __device__ constexpr size_t wave_bytes() {
+  return MODEL == 0 ? sizeof(TF2Ev) : (MODEL == 1 ? sizeof(PhdEv) : sizeof(HMEv));
+}
+template <int MODEL>
+__host__ __device__ constexpr size_t rec_stride() {
+  return ((sizeof(SetupHdr) + wave_bytes<MODEL>() + 15) / 16) * 16;
+}
+
+template <int MODEL>
+__global__ void __launch_bounds__(64) setup_kernel(EvBatch ev, DetDev det, WfDesc wf, const double* qnm, int nq,
+                                                    unsigned char* scratch, long long count) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = ev.n0 + i;
+  if (i >= count || n >= ev.N) return;
+  unsigned char* rec = scratch + i * rec_stride<MODEL>();
+  SetupHdr& h = *reinterpret_cast<SetupHdr*>(rec);
+  EvUnion& E = *reinterpret_cast<EvUnion*>(rec + sizeof(SetupHdr));
   const double* p = ev.p;
   const long long ld = ev.ld;
-  if (threadIdx.x == 0) {
-    const double Mc = p[0 * ld + n], eta = p[1 * ld + n], dL = p[2 * ld + n];
-    const double th = p[3 * ld + n], ph = p[4 * ld + n], io = p[5 * ld + n], ps = p[6 * ld + n];
-    const double tc = p[7 * ld + n], c1 = p[9 * ld + n], c2 = p[10 * ld + n];
-    if (grid_setup(g, det, ev, wf, n, Mc, eta)) {
-      event_setup<MODEL>(E, det, wf, qnm, nq, Mc, eta, c1, c2, dL);
-    }
-    proj_setup(pj, det, th, ph, io, ps, tc, dL);
+  const double Mc = p[0 * ld + n], eta = p[1 * ld + n], dL = p[2 * ld + n];
+  const double th = p[3 * ld + n], ph = p[4 * ld + n], io = p[5 * ld + n], ps = p[6 * ld + n];
+  const double tc = p[7 * ld + n], c1 = p[9 * ld + n], c2 = p[10 * ld + n];
+  if (grid_setup(h.g, det, ev, wf, n, Mc, eta)) {
+    event_setup<MODEL>(E, det, wf, qnm, nq, Mc, eta, c1, c2, dL);
+    if (MODEL == 2)
+      for (int mode = 0; mode < 6; ++mode)
+        hm_setup_mode(E.hm, mode, D4::seed(eta, P_ETA), D4::seed(c1, P_CHI1), D4::seed(c2, P_CHI2), io);
   }
-  if (MODEL == 2) {
-    __syncthreads();
-    if (threadIdx.x < 6 && g.ok) {
-      const double eta = p[1 * ld + n], c1 = p[9 * ld + n], c2 = p[10 * ld + n], io = p[5 * ld + n];
-      hm_setup_mode(E.hm, threadIdx.x, D4::seed(eta, P_ETA), D4::seed(c1, P_CHI1), D4::seed(c2, P_CHI2), io);
-    }
+  proj_setup(h.pj, det, th, ph, io, ps, tc, dL);
+}
+
+// cooperative copy of one event record into shared memory (all pieces are multiples of 8 bytes)
+template <int MODEL>
+__device__ inline void block_load(EvUnion& E, ProjEv& pj, GridEv& g, const unsigned char* scratch, long long i) {
+  const unsigned char* rec = scratch + i * rec_stride<MODEL>();
+  const unsigned long long* src = reinterpret_cast<const unsigned long long*>(rec);
+  unsigned long long* dg = reinterpret_cast<unsigned long long*>(&g);
+  unsigned long long* dp = reinterpret_cast<unsigned long long*>(&pj);
+  unsigned long long* de = reinterpret_cast<unsigned long long*>(&E);
+  constexpr int ng = sizeof(GridEv) / 8, np = sizeof(ProjEv) / 8, ne = wave_bytes<MODEL>() / 8;
+  static_assert(sizeof(SetupHdr) == sizeof(GridEv) + sizeof(ProjEv), "packed header");
+  for (int w = threadIdx.x; w < ng + np + ne; w += blockDim.x) {
+    const unsigned long long v = src[w];
+    if (w < ng) dg[w] = v;
+    else if (w < ng + np) dp[w - ng] = v;
+    else de[w - ng - np] = v;
   }
   __syncthreads();
 }
@@ -362,7 +401,7 @@ __device__ inline void block_setup(EvUnion& E, ProjEv& pj, GridEv& g, const EvBa
 // NG: Gram sets per point. L: 1. Triangle, per arm: 3 (arm1, arm2, -(arm1+arm2)).
 // Triangle, detector total: 2, using G(U)+G(V)+G(U+V) = G(sqrt(3/2)(U+V)) + G(sqrt(1/2)(U-V)).
 template <int MODEL, bool EARTH, int NARM, int NG>
-__global__ void __launch_bounds__(kThreads) fisher_kernel(EvBatch ev, DetDev det, WfDesc wf, const double* qnm, int nq,
+__global__ void __launch_bounds__(kThreads) fisher_kernel(EvBatch ev, DetDev det, const unsigned char* scratch,
                                                           double* out_arm, double* out_det, int accum) {
   extern __shared__ __align__(16) unsigned char stage_raw[];
   cd* stage = reinterpret_cast<cd*>(stage_raw);   // [warp][NG][NP][32]
@@ -373,7 +412,7 @@ __global__ void __launch_bounds__(kThreads) fisher_kernel(EvBatch ev, DetDev det
   __shared__ TimeState tsc;
   const long long n = ev.n0 + blockIdx.x;
   if (n >= ev.N) return;
-  block_setup<MODEL>(E, pj, g, ev, det, wf, qnm, nq, n);
+  block_load<MODEL>(E, pj, g, scratch, blockIdx.x);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (!EARTH) {
     if (tid == 0) {
@@ -499,7 +538,7 @@ __global__ void __launch_bounds__(kThreads) fisher_kernel(EvBatch ev, DetDev det
 // ------------------------------------------------------------------ SNR kernel
 // out_arm[a][n] = trapz((Ap^2 + Ac^2)/S) per arm (SNR_arm = 2 sqrt), out_det[n] += 4 sum_arms.
 template <int MODEL, bool EARTH, int NARM>
-__global__ void __launch_bounds__(kThreads) snr_kernel(EvBatch ev, DetDev det, WfDesc wf, const double* qnm, int nq,
+__global__ void __launch_bounds__(kThreads) snr_kernel(EvBatch ev, DetDev det, const unsigned char* scratch,
                                                        double* out_arm, double* out_det, int accum) {
   __shared__ EvUnion E;
   __shared__ ProjEv pj;
@@ -508,7 +547,7 @@ __global__ void __launch_bounds__(kThreads) snr_kernel(EvBatch ev, DetDev det, W
   __shared__ double red[kWarps][3];
   const long long n = ev.n0 + blockIdx.x;
   if (n >= ev.N) return;
-  block_setup<MODEL>(E, pj, g, ev, det, wf, qnm, nq, n);
+  block_load<MODEL>(E, pj, g, scratch, blockIdx.x);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (!EARTH) {
     if (tid == 0) {

@@ -1,11 +1,12 @@
 // Launch descriptors shared by the per-model translation units and the C-ABI layer.
 #pragma once
 #include <cuda_runtime.h>
-#include "gwf_kernels.cuh"
+#include "gwf_kernels_f32.cuh"
 
 namespace gwf {
 
-constexpr long long kMaxGrid = 1LL << 30;
+// events per set-up/main launch pair (bounds the set-up scratch: chunk x record stride)
+constexpr long long kChunk = 16384;
 
 struct LaunchArgs {
   EvBatch ev;
@@ -17,6 +18,8 @@ struct LaunchArgs {
   double* out_det;
   int accum;
   int per_arm;
+  int precision;  // 0 = FP64, 1 = FP32 split precision (22-mode models)
+  unsigned char* scratch;  // kChunk x setup_stride(model) bytes
   cudaStream_t stream;
 };
 
@@ -26,6 +29,9 @@ cudaError_t launch_fisher_m2(const LaunchArgs& a);
 cudaError_t launch_snr_m0(const LaunchArgs& a);
 cudaError_t launch_snr_m1(const LaunchArgs& a);
 cudaError_t launch_snr_m2(const LaunchArgs& a);
+size_t setup_stride_m0();
+size_t setup_stride_m1();
+size_t setup_stride_m2();
 cudaError_t launch_cov(const double* F, long long N, double* cov, double* eps, double* cond, cudaStream_t st);
 
 }  // namespace gwf

@@ -14,20 +14,15 @@ namespace gwf {
 using D4 = Dual<double, 4>;
 enum { P_MC = 0, P_ETA = 1, P_CHI1 = 2, P_CHI2 = 3 };
 
-// coefficient access: for S = Dual<T,4> the full dual, for a plain S the value
-template <class S> struct Co;
-template <> struct Co<double> { __device__ __forceinline__ static double get(const D4& c) { return c.v; } };
-template <> struct Co<float> { __device__ __forceinline__ static float get(const D4& c) { return float(c.v); } };
-template <> struct Co<D4> { __device__ __forceinline__ static D4 get(const D4& c) { return c; } };
-template <> struct Co<Dual<float, 4>> {
-  __device__ __forceinline__ static Dual<float, 4> get(const D4& c) {
-    Dual<float, 4> r; r.v = float(c.v);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) r.d[i] = float(c.d[i]);
-    return r;
-  }
-};
-template <class S> __device__ __forceinline__ S co(const D4& c) { return Co<S>::get(c); }
+// coefficient access: per-event coefficients are stored as duals (D4 for FP64, DF4 for FP32);
+// a per-point scalar S of matching precision reads either the full dual or its value.
+using DF4 = Dual<float, 4>;
+template <class S, class C> struct CoT;
+template <> struct CoT<double, D4> { __device__ __forceinline__ static double get(const D4& c) { return c.v; } };
+template <> struct CoT<D4, D4> { __device__ __forceinline__ static D4 get(const D4& c) { return c; } };
+template <> struct CoT<float, DF4> { __device__ __forceinline__ static float get(const DF4& c) { return c.v; } };
+template <> struct CoT<DF4, DF4> { __device__ __forceinline__ static DF4 get(const DF4& c) { return c; } };
+template <class S, class C> __device__ __forceinline__ S co(const C& c) { return CoT<S, C>::get(c); }
 
 template <class S> struct Real;
 template <> struct Real<double> { typedef double T; };
@@ -40,7 +35,8 @@ __device__ __forceinline__ D4 seta_of(const D4& eta) {
 }
 
 // ------------------------------------------------------------------ PN phase coefficients
-struct PNC { D4 A, c2, c3, c4, c5, c5l, c6, c6l, c7; };
+template <class C> struct PNCT { C A, c2, c3, c4, c5, c5l, c6, c6l, c7; };
+using PNC = PNCT<D4>;
 
 // TaylorF2 coefficients, gwfast/waveforms.py:784-812 (QuadMon = 1); drop_ss removes the 3PN
 // spin-spin part as IMRPhenomD does (gwfast/waveforms.py:1077).
@@ -84,14 +80,15 @@ __device__ inline PNC pn_coeffs(const D4& eta, const D4& chi1, const D4& chi2, b
 }
 
 // ------------------------------------------------------------------ TaylorF2 (gwfast/waveforms.py:697-953)
-struct TF2Ev {
-  PNC pn;
-  D4 eta;
-  D4 Ms;     // total mass in seconds
-  D4 vM;     // (pi Ms)^(1/3)
-  D4 lnvM;
-  D4 ampK;   // amplitude without f^(-7/6) and without 1/dL dependence in the tangent
+template <class C> struct TF2EvT {
+  PNCT<C> pn;
+  C eta;
+  C Ms;      // total mass in seconds
+  C vM;      // (pi Ms)^(1/3)
+  C lnvM;
+  C ampK;    // amplitude without f^(-7/6)
 };
+using TF2Ev = TF2EvT<D4>;
 
 __device__ inline void tf2_setup(TF2Ev& e, const D4& Mc, const D4& eta, const D4& chi1, const D4& chi2, double dL, bool spin_ho) {
   e.pn = pn_coeffs(eta, chi1, chi2, spin_ho, false);
@@ -104,8 +101,8 @@ __device__ inline void tf2_setup(TF2Ev& e, const D4& Mc, const D4& eta, const D4
 }
 
 // TF2 phase (without the constant offset, which cancels in every output) and amplitude.
-template <class S>
-__device__ __forceinline__ void tf2_point(const TF2Ev& e, typename Real<S>::T f, typename Real<S>::T f13,
+template <class S, class C>
+__device__ __forceinline__ void tf2_point(const TF2EvT<C>& e, typename Real<S>::T f, typename Real<S>::T f13,
                                           typename Real<S>::T lnf, typename Real<S>::T fm76, S& amp, S& phase) {
   typedef typename Real<S>::T T;
   const S v = co<S>(e.vM) * f13;
@@ -120,8 +117,8 @@ __device__ __forceinline__ void tf2_point(const TF2Ev& e, typename Real<S>::T f,
 }
 
 // 3.5PN time to coalescence shared by the three models (gwfast/waveforms.py:878-901, :1299-1322, :2712-2735)
-template <class S>
-__device__ __forceinline__ S tau_star_point(const D4& Ms, const D4& vM, const D4& eta_, typename Real<S>::T f13) {
+template <class S, class C>
+__device__ __forceinline__ S tau_star_point(const C& Ms, const C& vM, const C& eta_, typename Real<S>::T f13) {
   typedef typename Real<S>::T T;
   const S eta = co<S>(eta_);
   const S v = co<S>(vM) * f13;
@@ -140,20 +137,21 @@ __device__ __forceinline__ S tau_star_point(const D4& Ms, const D4& vM, const D4
 }
 
 // ------------------------------------------------------------------ IMRPhenomD core
-struct PhdCore {
-  D4 eta, MG, Ms, vM;     // MG = M * G/c^3 (s); Ms = MG; vM = (pi MG)^(1/3) for tau_star
-  D4 fring, fdamp;
-  PNC pn;
-  D4 sig[4], bet[3], alp[5], gam[3];
-  D4 C1Int, C2Int, fMRD, PhiIntTemp, DPhiIntTemp, C1MRD, C2MRD;
-  D4 a23, a1, a43, a53, a2, r1, r2, r3;   // inspiral amplitude
-  D4 fpA;                                 // amplitude peak (gwfast/waveforms.py:1193)
-  D4 f2;                                  // middle collocation node
-  D4 h0, h1, h2, h3, h4;                  // Newton-Hermite coefficients of the intermediate amplitude
-  D4 ampPref;                             // Overallamp * amp0 (model-dependent normalisation)
-  D4 t0;
-  D4 fRef, phiRef;                        // detector-dependent (fRef = M G fmin)
+template <class C> struct PhdCoreT {
+  C eta, MG, Ms, vM;      // MG = M * G/c^3 (s); Ms = MG; vM = (pi MG)^(1/3) for tau_star
+  C fring, fdamp;
+  PNCT<C> pn;
+  C sig[4], bet[3], alp[5], gam[3];
+  C C1Int, C2Int, fMRD, PhiIntTemp, DPhiIntTemp, C1MRD, C2MRD;
+  C a23, a1, a43, a53, a2, r1, r2, r3;    // inspiral amplitude
+  C fpA;                                  // amplitude peak (gwfast/waveforms.py:1193)
+  C f2;                                   // middle collocation node
+  C h0, h1, h2, h3, h4;                   // Newton-Hermite coefficients of the intermediate amplitude
+  C ampPref;                              // Overallamp * amp0 (model-dependent normalisation)
+  C t0;
+  C fRef, phiRef;                         // detector-dependent (fRef = M G fmin)
 };
+using PhdCore = PhdCoreT<D4>;
 
 __device__ __forceinline__ D4 fit11(int k, const D4& eta, const D4& xi) {
   const double* c = kFits[k];
@@ -183,8 +181,8 @@ __device__ inline D4 radiated_energy(const D4& eta, const D4& chi1, const D4& ch
 }
 
 // ---- phase pieces (argument x = M f), gwfast/waveforms.py:1079-1153, :2497-2501
-template <class S>
-__device__ __forceinline__ S ins_phase(const PhdCore& k, const S& x) {
+template <class S, class C>
+__device__ __forceinline__ S ins_phase(const PhdCoreT<C>& k, const S& x) {
   typedef typename Real<S>::T T;
   const S xp = T(kPi) * x;
   const S x13 = dcbrt(xp);
@@ -199,14 +197,14 @@ __device__ __forceinline__ S ins_phase(const PhdCore& k, const S& x) {
                                 + T(0.6) * co<S>(k.sig[2]) * x * m13 * m13 + T(0.5) * co<S>(k.sig[3]) * x * x) / eta;
 }
 
-template <class S>
-__device__ __forceinline__ S int_phase_raw(const PhdCore& k, const S& x) {
+template <class S, class C>
+__device__ __forceinline__ S int_phase_raw(const PhdCoreT<C>& k, const S& x) {
   typedef typename Real<S>::T T;
   return (co<S>(k.bet[0]) * x - co<S>(k.bet[2]) / (T(3) * x * x * x) + co<S>(k.bet[1]) * dlog(x)) / co<S>(k.eta);
 }
 
-template <class S>
-__device__ __forceinline__ S mrd_phase_raw(const PhdCore& k, const S& x, const S& rho, const S& tau) {
+template <class S, class C>
+__device__ __forceinline__ S mrd_phase_raw(const PhdCoreT<C>& k, const S& x, const S& rho, const S& tau) {
   typedef typename Real<S>::T T;
   const S x14 = dsqrt(dsqrt(x));
   return (-co<S>(k.alp[1]) / x + T(4.0 / 3.0) * co<S>(k.alp[2]) * x14 * x14 * x14 + co<S>(k.alp[0]) * x
@@ -214,8 +212,8 @@ __device__ __forceinline__ S mrd_phase_raw(const PhdCore& k, const S& x, const S
 }
 
 // complete phase with the Mf < 0.2 cut (gwfast/waveforms.py:1145, :2499)
-template <class S>
-__device__ __forceinline__ S complete_phase(const PhdCore& k, const S& x, const S& C1, const S& C2, const S& rho, const S& tau) {
+template <class S, class C>
+__device__ __forceinline__ S complete_phase(const PhdCoreT<C>& k, const S& x, const S& C1, const S& C2, const S& rho, const S& tau) {
   typedef typename Real<S>::T T;
   const T xv = val(x);
   if (xv < T(kPhiFJoin)) return ins_phase(k, x);
@@ -225,8 +223,8 @@ __device__ __forceinline__ S complete_phase(const PhdCore& k, const S& x, const 
 }
 
 // ---- amplitude pieces, gwfast/waveforms.py:1198-1254
-template <class S>
-__device__ __forceinline__ S ins_amp(const PhdCore& k, const S& x) {
+template <class S, class C>
+__device__ __forceinline__ S ins_amp(const PhdCoreT<C>& k, const S& x) {
   typedef typename Real<S>::T T;
   const S x13 = dcbrt(x);
   const S x23 = x13 * x13;
@@ -234,15 +232,15 @@ __device__ __forceinline__ S ins_amp(const PhdCore& k, const S& x) {
          + x * x * x23 * co<S>(k.r2) + x * (co<S>(k.a1) + x * co<S>(k.a2) + x * x * co<S>(k.r3));
 }
 
-template <class S>
-__device__ __forceinline__ S mrd_amp(const PhdCore& k, const S& x) {
+template <class S, class C>
+__device__ __forceinline__ S mrd_amp(const PhdCoreT<C>& k, const S& x) {
   const S fr = co<S>(k.fring), fdg3 = co<S>(k.fdamp) * co<S>(k.gam[2]);
   const S dx = x - fr;
   return dexp(-dx * co<S>(k.gam[1]) / fdg3) * (fdg3 * co<S>(k.gam[0])) / (dx * dx + fdg3 * fdg3);
 }
 
-template <class S>
-__device__ __forceinline__ S complete_amp_shape(const PhdCore& k, const S& x) {
+template <class S, class C>
+__device__ __forceinline__ S complete_amp_shape(const PhdCoreT<C>& k, const S& x) {
   typedef typename Real<S>::T T;
   const T xv = val(x);
   if (xv < T(kAmpFJoin)) return ins_amp(k, x);
@@ -410,8 +408,8 @@ __device__ inline void phd_setup(PhdEv& e, const D4& Mc, const D4& eta, const D4
 }
 
 // amplitude A(f) and phase Phi(f) of IMRPhenomD at physical frequency f (Hz)
-template <class S>
-__device__ __forceinline__ void phd_point(const PhdCore& k, typename Real<S>::T f, S& amp, S& phase) {
+template <class S, class C>
+__device__ __forceinline__ void phd_point(const PhdCoreT<C>& k, typename Real<S>::T f, S& amp, S& phase) {
   typedef typename Real<S>::T T;
   const S x = co<S>(k.MG) * f;
   const T xv = val(x);
@@ -425,21 +423,23 @@ __device__ __forceinline__ void phd_point(const PhdCore& k, typename Real<S>::T 
 }
 
 // ------------------------------------------------------------------ IMRPhenomHM (gwfast/waveforms.py:2256-2616)
-struct HMMode {
-  D4 rho, tau, C1, C2, frlm;
-  D4 fip, amp_, bmp, PhDB, PhDC, PhDBA, phC;  // phase frequency map and offsets
-  D4 fia, ama, bma;                          // amplitude frequency map
-  D4 hr1, hr2, hr3, hr4, hi4;                // PN amplitude polynomial H(v) = v (hr1 + v (hr2 + v (hr3 + v (hr4 + i hi4))))
-  double yp, yc, dyp, dyc;                   // 0.5(Y +- (-1)^l Y_{l-m}) and d/diota
+template <class C> struct HMModeT {
+  C rho, tau, C1, C2, frlm;
+  C fip, amp_, bmp, PhDB, PhDC, PhDBA, phC;  // phase frequency map and offsets
+  C fia, ama, bma;                          // amplitude frequency map
+  C hr1, hr2, hr3, hr4, hi4;                // PN amplitude polynomial H(v) = v (hr1 + v (hr2 + v (hr3 + v (hr4 + i hi4))))
+  double yp, yc, dyp, dyc;                  // 0.5(Y +- (-1)^l Y_{l-m}) and d/diota
   double shift;
   int l, m;
 };
+using HMMode = HMModeT<D4>;
 
-struct HMEv {
-  PhdCore k;
-  D4 phi0;
-  HMMode md[6];
+template <class C> struct HMEvT {
+  PhdCoreT<C> k;
+  C phi0;
+  HMModeT<C> md[6];
 };
+using HMEv = HMEvT<D4>;
 
 __device__ inline void rd_fit(int mode, const D4& finmass, const D4& finspin, D4& fr, D4& fd) {
   const int l = kModeL[mode], m = kModeM[mode];
@@ -566,8 +566,8 @@ __device__ inline void hm_setup_mode(HMEv& e, int mode, const D4& eta, const D4&
 }
 
 // |H_lm(v)| for v = (2 pi x / m)^(1/3)
-template <class S>
-__device__ __forceinline__ S hm_absH(const HMMode& md, int mode, const S& x) {
+template <class S, class C>
+__device__ __forceinline__ S hm_absH(const HMModeT<C>& md, int mode, const S& x) {
   typedef typename Real<S>::T T;
   if (mode == 1) return S(T(1));
   const S v = dcbrt(x * T(kTwoPi / md.m));
@@ -584,11 +584,11 @@ template <class S> struct Cplx { S re, im; };
 
 // hp, hc of IMRPhenomHM without the common factor; returns P, C with hp = P, hc = i C, plus the iota derivatives
 // (dP, dC, value-only).  Point at physical frequency f (Hz).
-template <class S>
-__device__ __forceinline__ void hm_point(const HMEv& e, typename Real<S>::T f, Cplx<S>& P, Cplx<S>& C,
+template <class S, class K>
+__device__ __forceinline__ void hm_point(const HMEvT<K>& e, typename Real<S>::T f, Cplx<S>& P, Cplx<S>& C,
                                          Cplx<typename Real<S>::T>& dP, Cplx<typename Real<S>::T>& dC) {
   typedef typename Real<S>::T T;
-  const PhdCore& k = e.k;
+  const PhdCoreT<K>& k = e.k;
   const S x = co<S>(k.MG) * f;
   const T xv = val(x);
   const S zero(T(0));
@@ -597,7 +597,7 @@ __device__ __forceinline__ void hm_point(const HMEv& e, typename Real<S>::T f, C
   const S lin = co<S>(k.t0) * (x - co<S>(k.fRef));
 #pragma unroll 1
   for (int mode = 0; mode < 6; ++mode) {
-    const HMMode& md = e.md[mode];
+    const HMModeT<K>& md = e.md[mode];
     const T ai = T(2.0) / T(md.m);
     // amplitude
     S fs;

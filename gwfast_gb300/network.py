@@ -60,11 +60,14 @@ class DetNet:
         use_chi1chi2 = kwargs.get('use_chi1chi2', True)
         if kwargs.get('computeDerivFinDiff', False):
             raise NotImplementedError('finite-difference derivatives are not used on the GPU path')
+        precision = kwargs.get('precision', 'fp64')
         if not return_all:
-            F = fisher_batch(sigs, evParams, res, per_arm=False, spacing=spacing, device=sigs[0].device)
+            F = fisher_batch(sigs, evParams, res, per_arm=False, spacing=spacing, device=sigs[0].device,
+                             precision=precision)
             F = reparametrise(F, evParams, use_m1m2, use_chi1chi2)
             return np.moveaxis(F, 0, -1)
-        per = fisher_batch(sigs, evParams, res, per_arm=True, spacing=spacing, device=sigs[0].device)
+        per = fisher_batch(sigs, evParams, res, per_arm=True, spacing=spacing, device=sigs[0].device,
+                           precision=precision)
         allF = {}
         for name, s, Fa in zip(names, sigs, per):
             Fa = reparametrise(Fa, evParams, use_m1m2, use_chi1chi2)

@@ -54,10 +54,11 @@ def snr_batch(signals, evParams, res=1000, device=0):
     return res_l
 
 
-def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', device=0):
+def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', device=0, precision='fp64'):
     """Fisher matrices of all signals in one library call.
 
     per_arm: list (per signal) of (arms, N, 11, 11); otherwise the network total (N, 11, 11).
+    precision: 'fp64' (the drop-in) or 'fp32' (split precision, TaylorF2 and IMRPhenomD).
     """
     p = _prep(evParams)
     wf = signals[0].wf_model
@@ -68,7 +69,8 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
     duty = any(s.DutyFactor is not None for s in signals)
     if per_arm or duty:
         out = np.empty((sum(slots), N, 11, 11))
-        ctx.fisher([s.det_id for s in signals], wf.gpu_desc(), p, res, spacing=sp, per_arm=True, out_arm=out)
+        ctx.fisher([s.det_id for s in signals], wf.gpu_desc(), p, res, spacing=sp, per_arm=True, out_arm=out,
+                   precision=precision)
         res_l, i = [], 0
         for s, k in zip(signals, slots):
             res_l.append(s._apply_duty(out[i:i + k], seed=True))
@@ -77,7 +79,8 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
             return res_l
         return sum(r.sum(axis=0) for r in res_l)
     out = np.empty((N, 11, 11))
-    ctx.fisher([s.det_id for s in signals], wf.gpu_desc(), p, res, spacing=sp, per_arm=False, out_net=out)
+    ctx.fisher([s.det_id for s in signals], wf.gpu_desc(), p, res, spacing=sp, per_arm=False, out_net=out,
+               precision=precision)
     return out
 
 
@@ -177,14 +180,17 @@ class GWSignal:
 
     def FisherMatr(self, evParams, res=1000, df=None, spacing='geom', use_m1m2=False, use_chi1chi2=True,
                    use_prec_ang=True, computeDerivFinDiff=False, computeAnalyticalDeriv=True, return_all=False,
-                   return_derivatives=False, return_SNR_derivatives=False, **kwargs):
-        """gwfast/signal.py:782-1098; returns (11, 11, N), or a list per arm with return_all."""
+                   return_derivatives=False, return_SNR_derivatives=False, precision='fp64', **kwargs):
+        """gwfast/signal.py:782-1098; returns (11, 11, N), or a list per arm with return_all.
+
+        precision='fp32' selects the split-precision kernel (TaylorF2 and IMRPhenomD)."""
         if return_derivatives or return_SNR_derivatives:
             raise NotImplementedError('return_derivatives / return_SNR_derivatives are not implemented on the GPU path')
         if computeDerivFinDiff:
             raise NotImplementedError('finite-difference derivatives are not used on the GPU path')
         res = self._resolve_res(evParams, res, df)
-        Fa = fisher_batch([self], evParams, res, per_arm=True, spacing=spacing, device=self.device)[0]
+        Fa = fisher_batch([self], evParams, res, per_arm=True, spacing=spacing, device=self.device,
+                          precision=precision)[0]
         Fa = reparametrise(Fa, evParams, use_m1m2, use_chi1chi2)
         arms = [np.moveaxis(F, 0, -1) for F in Fa]
         if return_all:

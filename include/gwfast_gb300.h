@@ -98,10 +98,12 @@ int gwf_snr(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, 
  * Replaces GWSignal.FisherMatr (gwfast/signal.py:782-1098, default arguments
  * use_chi1chi2=True, computeAnalyticalDeriv=True) and DetNet.FisherMatr (gwfast/network.py:309-343).
  * per_arm != 0: out_arm receives [slots][N][11][11] per arm (return_all=True);
- * out_net (may be NULL): [N][11][11] network total. */
+ * out_net (may be NULL): [N][11][11] network total.
+ * precision: GWF_PREC_FP64 (the drop-in) or GWF_PREC_FP32 (split precision: per-event set-up in
+ * FP64, per-point arithmetic in FP32, outputs in FP64; TaylorF2 and IMRPhenomD only). */
 int gwf_fisher(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params, int64_t ld,
-               int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int per_arm, int mem,
-               double* out_arm, double* out_net, void* stream);
+               int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int per_arm, int precision,
+               int mem, double* out_arm, double* out_net, void* stream);
 
 /* Covariance by equilibrated Cholesky inversion, FP64, one 11x11 matrix per event.
  * Replaces fisherTools.CovMatr 'cho' path (gwfast/fisherTools.py:32-196) together with

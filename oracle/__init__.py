@@ -13,3 +13,4 @@ stores their outputs; ``tests/test_oracle_golden.py`` checks this oracle
 against those fixtures.
 """
 from .gwf_oracle import *  # noqa: F401,F403
+from .gwf_oracle import _gram, _trapz  # noqa: F401,E402

@@ -1,0 +1,72 @@
+"""FP32 split-precision Fisher against the FP64 kernel (and so against the oracle).
+
+Error measures: Fisher entries relative to sqrt(F_aa F_bb), and the marginalised 1-sigma
+errors sqrt(diag(Cov)) from the FP64 equilibrated-Cholesky inversion of each.
+"""
+import numpy as np
+import pytest
+
+from gwfast_gb300 import fisherTools, synthetic
+from gwfast_gb300 import waveforms as W
+
+pytestmark = pytest.mark.gpu
+
+
+def entry_err(F, Fr):
+    d = np.sqrt(np.abs(np.einsum('nii->ni', Fr)))
+    return np.abs(F - Fr) / (d[:, :, None] * d[:, None, :])
+
+
+def sigma_err(F32, F64):
+    c32, _, _ = fisherTools.CovMatr(np.moveaxis(F32, 0, -1), return_cond=True)
+    c64, _, cond = fisherTools.CovMatr(np.moveaxis(F64, 0, -1), return_cond=True)
+    s32 = np.sqrt(np.einsum('iin->ni', c32))
+    s64 = np.sqrt(np.einsum('iin->ni', c64))
+    return np.abs(s32 - s64) / s64, cond
+
+
+@pytest.mark.parametrize('earth', [True, False])
+def test_phenomd_network_fp32(gpu_lib, earth):
+    ev = synthetic.bbh_events(512, seed=1001)
+    net = synthetic.make_network(W.IMRPhenomD(), earth=earth)
+    F64 = np.moveaxis(net.FisherMatr(dict(ev), res=2000), -1, 0)
+    F32 = np.moveaxis(net.FisherMatr(dict(ev), res=2000, precision='fp32'), -1, 0)
+    e = entry_err(F32, F64)
+    se, cond = sigma_err(F32, F64)
+    worst = se.max(axis=1)
+    print('PhenomD fp32 entry err max %.2e median %.2e; sigma err median %.2e p95 %.2e max %.2e; frac<=1e-3 %.4f'
+          % (e.max(), np.median(e.max(axis=(1, 2))), np.median(worst), np.percentile(worst, 95), worst.max(),
+             np.mean(worst <= 1e-3)))
+    assert np.median(e.max(axis=(1, 2))) < 1e-5
+    assert np.mean(worst <= 1e-3) >= 0.95
+
+
+@pytest.mark.parametrize('det', [('Virgo', 10.), ('ETS', 5.)])
+def test_taylorf2_fp32(gpu_lib, det):
+    ev = synthetic.bns_events(256, seed=1000)
+    net = synthetic.make_network(W.TaylorF2_RestrictedPN(), dets=(det,), earth=True)
+    F64 = np.moveaxis(net.FisherMatr(dict(ev), res=2000), -1, 0)
+    F32 = np.moveaxis(net.FisherMatr(dict(ev), res=2000, precision='fp32'), -1, 0)
+    e = entry_err(F32, F64)
+    se, cond = sigma_err(F32, F64)
+    worst = se.max(axis=1)
+    print('TF2 %s fp32 entry err max %.2e; sigma err median %.2e p95 %.2e max %.2e; frac<=1e-3 %.4f'
+          % (det[0], e.max(), np.median(worst), np.percentile(worst, 95), worst.max(), np.mean(worst <= 1e-3)))
+    assert np.median(e.max(axis=(1, 2))) < 1e-5
+
+
+def test_fp32_per_arm_sums_to_total(gpu_lib):
+    ev = synthetic.bbh_events(32, seed=17)
+    net = synthetic.make_network(W.IMRPhenomD(), dets=(('ETS', 5.),), earth=True)
+    Fa = net.FisherMatr(dict(ev), res=1000, return_all=True, precision='fp32')
+    Ft = net.FisherMatr(dict(ev), res=1000, precision='fp32')
+    S = Fa['ETS_0'] + Fa['ETS_1'] + Fa['ETS_2']
+    assert entry_err(np.moveaxis(Ft, -1, 0), np.moveaxis(S, -1, 0)).max() < 1e-5
+
+
+def test_fp32_rejected_for_hm(gpu_lib):
+    from gwfast_gb300 import _lib
+    ev = synthetic.bbh_events(2, seed=1)
+    net = synthetic.make_network(W.IMRPhenomHM(), dets=(('L1', 10.),), earth=False)
+    with pytest.raises(_lib.GWFError):
+        net.FisherMatr(dict(ev), res=100, precision='fp32')

@@ -1,0 +1,127 @@
+"""Host-side logic that needs no GPU: parameter handling, reparametrisation, duty cycle, sharding."""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from gwfast_gb300 import gwfastUtils as U
+from gwfast_gb300 import shard, synthetic
+from gwfast_gb300.signal import GWSignal, event_array, reparametrise
+
+
+def test_event_array_order_and_broadcast():
+    ev = synthetic.bbh_events(5, seed=1)
+    ev['tcoal'] = 0.25
+    p = event_array(ev)
+    assert p.shape == (11, 5) and p.flags.c_contiguous
+    assert np.all(p[7] == 0.25)
+    assert np.all(p[0] == ev['Mc']) and np.all(p[10] == ev['chi2z'])
+
+
+def test_check_evparams_mutates_and_raises():
+    ev = {'m1': np.array([30.]), 'm2': np.array([20.]), 'ra': np.array([1.]), 'dec': np.array([0.2]),
+          'thetaJN': np.array([0.4]), 'tcoal': np.array([0.1])}
+    U.check_evparams(ev)
+    Mc, eta = U.Mceta_from_m1m2(30., 20.)
+    assert np.isclose(ev['Mc'][0], Mc) and np.isclose(ev['eta'][0], eta)
+    assert np.isclose(ev['theta'][0], np.pi / 2 - 0.2) and ev['iota'][0] == 0.4
+    with pytest.raises(ValueError):
+        U.check_evparams({'Mc': 1.})
+    with pytest.raises(ValueError):
+        U.fill_spins({})
+    e2 = {'chiS': np.array([0.1]), 'chiA': np.array([0.05])}
+    U.fill_spins(e2)
+    assert np.isclose(e2['chi1z'][0], 0.15) and np.isclose(e2['chi2z'][0], 0.05)
+
+
+def test_mass_conversions_roundtrip():
+    m1, m2 = U.m1m2_from_Mceta(*U.Mceta_from_m1m2(np.array([35.]), np.array([12.])))
+    assert np.allclose([m1[0], m2[0]], [35., 12.])
+
+
+def _oracle_jacobian_new(det, model, f, p, kind):
+    """d h / d(m1, m2) or d(chiS, chiA) by forward AD through the conversion (independent of reparametrise)."""
+    out = []
+    if kind == 'm1m2':
+        m1, m2 = U.m1m2_from_Mceta(p['Mc'].numpy(), p['eta'].numpy())
+        m1, m2 = torch.tensor(m1), torch.tensor(m2)
+        for j in range(2):
+            def fn(x, j=j):
+                a, b = (x, m2) if j == 0 else (m1, x)
+                q = dict(p)
+                q['Mc'] = (a * b) ** 0.6 / (a + b) ** 0.2
+                q['eta'] = a * b / (a + b) ** 2
+                return O.strain_parts(det, model, f, q)
+            prim = (m1 if j == 0 else m2,)
+            _, (re, im) = torch.func.jvp(fn, prim, (torch.ones_like(prim[0]),))
+            out.append(torch.complex(re, im))
+    else:
+        cs, ca = 0.5 * (p['chi1z'] + p['chi2z']), 0.5 * (p['chi1z'] - p['chi2z'])
+        for j in range(2):
+            def fn(x, j=j):
+                s, a = (x, ca) if j == 0 else (cs, x)
+                q = dict(p)
+                q['chi1z'], q['chi2z'] = s + a, s - a
+                return O.strain_parts(det, model, f, q)
+            prim = (cs if j == 0 else ca,)
+            _, (re, im) = torch.func.jvp(fn, prim, (torch.ones_like(prim[0]),))
+            out.append(torch.complex(re, im))
+    return out
+
+
+@pytest.mark.parametrize('kind', ['m1m2', 'chiSchiA'])
+def test_reparametrise_matches_direct_derivatives(kind):
+    ev = synthetic.bbh_events(3, seed=4)
+    p = O.to_params(ev)
+    f0 = np.geomspace(10., 1e4, 500)
+    det = O.Detector(30.563, -90.774, 242.7, 'L', fmin=10., psd_f=f0, psd_S=O.aligo_psd(f0), earth=False)
+    model = O.Model('PhenomD')
+    f, S = O.event_grid(det, model, p, 300)
+    D = O.strain_jacobian(det, model, f, p)
+    D[O.TC_INDEX] /= O.DAY_S
+    F = O._gram(D, S, f).numpy()
+    Fr = reparametrise(F, ev, use_m1m2=(kind == 'm1m2'), use_chi1chi2=(kind == 'm1m2'))
+    new = _oracle_jacobian_new(det, model, f, p, kind)
+    idx = (0, 1) if kind == 'm1m2' else (9, 10)
+    D2 = D.clone()
+    D2[idx[0]], D2[idx[1]] = new
+    Fd = O._gram(D2, S, f).numpy()
+    d = np.sqrt(np.abs(np.einsum('nii->ni', Fd)))
+    assert (np.abs(Fr - Fd) / (d[:, :, None] * d[:, None, :])).max() < 1e-10
+
+
+def test_duty_factor_draws_follow_reference_sequence():
+    """Masks are drawn after np.random.seed(seedUse), one choice([0,1], N) per arm (gwfast/signal.py:729-765)."""
+    s = GWSignal.__new__(GWSignal)
+    s.DutyFactor = 0.7
+    s.seedUse = np.array([12345])
+    arms = np.ones((3, 50))
+    got = s._apply_duty(arms)
+    np.random.seed(s.seedUse)
+    want = np.stack([np.random.choice([0, 1], 50, p=[0.3, 0.7]) for _ in range(3)])
+    assert np.array_equal(got, want)
+    F = np.ones((1, 50, 11, 11))
+    gotF = s._apply_duty(F)
+    np.random.seed(s.seedUse)
+    m = np.random.choice([0, 1], 50, p=[0.3, 0.7])
+    assert np.array_equal(gotF[0, :, 0, 0], m)
+
+
+def test_synthetic_catalogues_are_seeded_and_in_range():
+    a, b = synthetic.bbh_events(1000, seed=1001), synthetic.bbh_events(1000, seed=1001)
+    assert all(np.array_equal(a[k], b[k]) for k in a)
+    m1, m2 = U.m1m2_from_Mceta(a['Mc'], a['eta'])
+    assert m1.min() >= 5. - 1e-9 and m1.max() <= 80. + 1e-9
+    assert np.all(m2 / m1 >= 0.2 - 1e-9) and np.all(a['eta'] <= 0.25)
+    bn = synthetic.bns_events(200, seed=1000)
+    m1, m2 = U.m1m2_from_Mceta(bn['Mc'], bn['eta'])
+    assert np.all(m1 >= m2 - 1e-12) and m2.min() >= 1.1 - 1e-9 and m1.max() <= 2.0 + 1e-9
+
+
+def test_shard_slices_cover_everything():
+    for n in (0, 1, 7, 10, 1001):
+        for w in (1, 2, 3, 8):
+            sl = [shard.shard_slice(n, r, w) for r in range(w)]
+            assert sl[0][0] == 0 and sl[-1][1] == n
+            assert all(sl[i][1] == sl[i + 1][0] for i in range(w - 1))
+            assert max(b - a for a, b in sl) - min(b - a for a, b in sl) <= 1
