@@ -350,9 +350,18 @@ template <int MODEL>
 __host__ __device__ constexpr size_t wave_bytes() {
   return MODEL == 0 ? sizeof(TF2Ev) : (MODEL == 1 ? sizeof(PhdEv) : sizeof(HMEv));
 }
+// the 22-mode models also carry the phase-tangent basis used by the FP32 kernel
+template <int MODEL>
+__host__ __device__ constexpr size_t basis_bytes() {
+  return MODEL < 2 ? sizeof(PhaseBasis) : 0;
+}
 template <int MODEL>
 __host__ __device__ constexpr size_t rec_stride() {
-  return ((sizeof(SetupHdr) + wave_bytes<MODEL>() + 15) / 16) * 16;
+  return ((sizeof(SetupHdr) + wave_bytes<MODEL>() + basis_bytes<MODEL>() + 15) / 16) * 16;
+}
+template <int MODEL>
+__device__ __forceinline__ const PhaseBasis* rec_basis(const unsigned char* scratch, long long i) {
+  return reinterpret_cast<const PhaseBasis*>(scratch + i * rec_stride<MODEL>() + sizeof(SetupHdr) + wave_bytes<MODEL>());
 }
 
 template <int MODEL>
@@ -374,6 +383,9 @@ __global__ void __launch_bounds__(64) setup_kernel(EvBatch ev, DetDev det, WfDes
     if (MODEL == 2)
       for (int mode = 0; mode < 6; ++mode)
         hm_setup_mode(E.hm, mode, D4::seed(eta, P_ETA), D4::seed(c1, P_CHI1), D4::seed(c2, P_CHI2), io);
+    PhaseBasis* pb = reinterpret_cast<PhaseBasis*>(rec + sizeof(SetupHdr) + wave_bytes<MODEL>());
+    if (MODEL == 0) tf2_phase_basis(E.tf2, *pb);
+    if (MODEL == 1) phd_phase_basis(E.phd.k, *pb);
   }
   proj_setup(h.pj, det, th, ph, io, ps, tc, dL);
 }

@@ -8,9 +8,15 @@
 //    FP32 (Dual<float, 4>);
 //  - Earth-rotation angles are formed as FP64 per-event reference angle + small FP32 offset
 //    by angle addition, so no large FP32 argument is ever reduced;
-//  - the PSD is read from an FP32 table normalised by its minimum; the Gram matrix is
-//    accumulated in FP32 per 32-point tile and across tiles with Kahan compensation, then
-//    summed over warps and rescaled (amplitude^2 / PSD scale) in FP64.
+//  - the PSD is read from an FP32 table normalised by its minimum;
+//  - the Gram matrix is accumulated exactly in fixed point: each sqrt(weight)-scaled FP32
+//    derivative vector is rounded to a 22-bit integer on a per-column power-of-two scale (the
+//    running maximum over the warp's tiles), products are formed as int32 x int32 -> int64 and
+//    summed without rounding; sums move to FP64 only when a column scale grows (by an exact
+//    shift) or every kFlushTiles tiles. Rounding each product or partial sum in FP32 instead
+//    adds errors that are not a perturbation of the vectors; with equilibrated condition
+//    numbers of 1e8-1e11 (typical for 11-parameter BBH Fishers) that makes the matrix
+//    indefinite.
 // The overall phase factor cancels in every Gram entry and is never formed (as in FP64).
 #pragma once
 #include "gwf_kernels.cuh"
@@ -147,6 +153,73 @@ union EvUnionF {
   PhdCoreT<DF4> phd;
 };
 
+// FP32 copy of the phase-tangent basis: each FP64 coefficient derivative as a (hi, lo) float pair
+struct PBF {
+  float hi[22][4], lo[22][4];   // inspiral 0..12, intermediate 13..16, merger-ringdown 17..21
+  float du1[4], du0[4];
+  float u1, u0, k4, mg, fmrd;
+};
+
+__device__ inline void pbf_load(const PhaseBasis* src, PBF& b) {
+  for (int i = threadIdx.x; i < 22 * 4; i += blockDim.x) {
+    const int c = i >> 2, q = i & 3;
+    const D4& d = c < 13 ? src->ins[c] : (c < 17 ? src->itm[c - 13] : src->mrd[c - 17]);
+    const double v = d.d[q];
+    const float h = (float)v;
+    b.hi[c][q] = h;
+    b.lo[c][q] = (float)(v - (double)h);
+  }
+  if (threadIdx.x < 4) {
+    b.du1[threadIdx.x] = (float)src->U1.d[threadIdx.x];
+    b.du0[threadIdx.x] = (float)src->U0.d[threadIdx.x];
+  }
+  if (threadIdx.x == 0) {
+    b.u1 = (float)src->U1.v; b.u0 = (float)src->U0.v; b.k4 = (float)src->mrd[4].v;
+    b.mg = (float)src->MG.v; b.fmrd = (float)src->fMRD;
+  }
+}
+
+// d Phi / d(Mc, eta, chi1z, chi2z) at frequency f from the basis (see PhaseBasis)
+__device__ __forceinline__ void phase_tangent_f(const PBF& b, float f, float lnf, float* dphi) {
+  const float x = b.mg * f;
+  float bas[13];
+  int off, nb;
+  float datn = 0.0f;
+  if (x < (float)kPhiFJoin) {
+    const float f13 = cbrtf(f);
+    const float i13 = 1.0f / f13;
+    const float i23 = i13 * i13;
+    bas[0] = i23 * i23 * i13; bas[1] = 1.0f / f; bas[2] = i23; bas[3] = i13;
+    bas[4] = 1.0f; bas[5] = lnf; bas[6] = f13; bas[7] = f13 * lnf; bas[8] = f13 * f13;
+    bas[9] = f; bas[10] = f * f13; bas[11] = f * f13 * f13; bas[12] = f * f;
+    off = 0; nb = 13;
+  } else if (x < b.fmrd) {
+    const float inv = 1.0f / f;
+    bas[0] = f; bas[1] = inv * inv * inv; bas[2] = lnf; bas[3] = 1.0f;
+    off = 13; nb = 4;
+  } else if (x < (float)kMfCut) {
+    const float u = b.u1 * f - b.u0;
+    datn = 1.0f / (1.0f + u * u);
+    const float f14 = sqrtf(sqrtf(f));
+    bas[0] = 1.0f / f; bas[1] = f14 * f14 * f14; bas[2] = f; bas[3] = 1.0f; bas[4] = atanf(u);
+    off = 17; nb = 5;
+  } else {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) dphi[q] = 0.0f;
+    return;
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    float sh = 0.0f, sl = 0.0f;
+    for (int j = 0; j < nb; ++j) {
+      sh = fmaf(b.hi[off + j][q], bas[j], sh);
+      sl = fmaf(b.lo[off + j][q], bas[j], sl);
+    }
+    if (off == 17) sl = fmaf(b.k4 * datn, fmaf(b.du1[q], f, -b.du0[q]), sl);
+    dphi[q] = sh + sl;
+  }
+}
+
 // round a struct of FP64 duals to its FP32 twin, all threads of the block; the dual at `amp_member`
 // is divided by `amp` first (so the FP32 amplitude is O(1)); ends with a block barrier
 template <class SRC, class DST>
@@ -165,12 +238,44 @@ __device__ inline void round_struct_par(const SRC& s, DST& d, const D4* amp_memb
 static __constant__ unsigned char kBlkR[16] = {0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2, 3, 3, 4, 4, 5};
 static __constant__ unsigned char kBlkC[16] = {0, 1, 2, 3, 0, 1, 2, 3, 1, 2, 3, 2, 3, 2, 3, 3};
 
+// fixed-point Gram accumulation
+constexpr int kQBits = 22;                    // quantised |value| <= 2^22
+constexpr int kQMinExp = -100;                // floor of the running column exponents
+constexpr float kRoundMagic = 12582912.0f;    // 1.5 * 2^23: fmaf(x, s, magic) = magic + rint(x s) for |x s| < 2^22
+constexpr int kRoundMagicBits = 0x4B400000;   // bit pattern of kRoundMagic
+constexpr int kFlushTiles = 4096;             // 4096 tiles x 2^50 per tile < 2^63
+
+// add the integer sums (at scale 2^-(M_r + M_c - 2 (kQBits - 1))) to the FP64 Gram of this warp
+template <int NG, int NQ, int BPL, int NB>
+__device__ __forceinline__ void flush_fixed(long long (&acc)[BPL][6], const int* M, double* fl, int lane) {
+#pragma unroll
+  for (int i = 0; i < BPL; ++i) {
+    const int bl = (NG == 1 ? (lane & 15) : lane + 32 * i);
+    if (bl < NB) {
+      const int gs = bl >> 4, bi = bl & 15;
+      const int r0 = 2 * kBlkR[bi], c0 = 3 * kBlkC[bi];
+      const int* m = M + gs * NQ;
+#pragma unroll
+      for (int e = 0; e < 6; ++e) {
+        const int r = r0 + e / 3, c = c0 + e % 3;
+        // exact power of two: the exponent lies in [2 kQMinExp - 42, 254 - 42], inside the normal range
+        const double p2 = __longlong_as_double((long long)(1023 + m[r] + m[c] - 2 * (kQBits - 1)) << 52);
+        atomicAdd(&fl[(gs * NQ + r) * NQ + c], (double)acc[i][e] * p2);
+        acc[i][e] = 0ll;
+      }
+    }
+  }
+}
+
 template <int MODEL, bool EARTH, int NARM, int NG>
 __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, DetDev det, const unsigned char* scratch,
                                                                  double* out_arm, double* out_det, int accum) {
   constexpr int NQ = 12;  // padded parameter count
   extern __shared__ __align__(16) unsigned char stage_raw[];
-  cf* stage = reinterpret_cast<cf*>(stage_raw);   // [warp][NG][NQ][32]
+  int2* stage = reinterpret_cast<int2*>(stage_raw);   // [warp][NG][NQ][32] quantised (re, im)
+  __shared__ int colM[2][kWarps][NG * NQ];             // running column exponents, double-buffered
+  __shared__ double fl[kWarps][NG][NQ][NQ];            // FP64 Gram per warp and set
+  __shared__ int badw[kWarps];
   __shared__ EvUnion E;
   __shared__ EvUnionF EF;
   __shared__ ProjEv pj;
@@ -180,6 +285,7 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
   __shared__ ArmF apc[NARM];
   __shared__ TimeF tsc;
   __shared__ double scale;
+  __shared__ PBF pbf;
   const long long n = ev.n0 + blockIdx.x;
   if (n >= ev.N) return;
   block_load<MODEL>(E, pj, g, scratch, blockIdx.x);
@@ -187,6 +293,7 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
   // amplitude prefactor divided out before rounding the coefficients to FP32
   const double amp = g.ok ? (MODEL == 0 ? E.tf2.ampK.v : E.phd.k.ampPref.v) : 1.0;
   if (g.ok) {
+    pbf_load(rec_basis<MODEL>(scratch, blockIdx.x), pbf);
     if (MODEL == 0) round_struct_par(E.tf2, EF.tf2, &E.tf2.ampK, amp);
     else round_struct_par(E.phd.k, EF.phd, &E.phd.k.ampPref, amp);
   }
@@ -203,26 +310,39 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
   __syncthreads();
   constexpr int NB = 16 * NG;
   constexpr int BPL = (NB + 31) / 32;
-  float acc[BPL][6], cmp[BPL][6];
+  long long acc[BPL][6];
 #pragma unroll
   for (int i = 0; i < BPL; ++i)
 #pragma unroll
-    for (int e = 0; e < 6; ++e) { acc[i][e] = 0.0f; cmp[i][e] = 0.0f; }
-  cf* my = stage + (size_t)warp * NG * NQ * 32;
-  // zero padding row (parameter 11) once
-  for (int gs = 0; gs < NG; ++gs) my[(gs * NQ + 11) * 32 + lane] = {0.0f, 0.0f};
+    for (int e = 0; e < 6; ++e) acc[i][e] = 0ll;
+  int2* my = stage + (size_t)warp * NG * NQ * 32;
+  // zero padding row (parameter 11) once; running column exponents start below any value
+  for (int gs = 0; gs < NG; ++gs) my[(gs * NQ + 11) * 32 + lane] = make_int2(0, 0);
+  for (int i = lane; i < 2 * NG * NQ; i += 32) (&colM[i / (NG * NQ)][warp][0])[i % (NG * NQ)] = kQMinExp;
+  for (int i = lane; i < NG * NQ * NQ; i += 32) (&fl[warp][0][0][0])[i] = 0.0;
+  if (lane == 0) badw[warp] = 0;
+  int par = 0, tiles = 0;
+  bool moved = false, bad = false;
+  __syncwarp();
   const int R = gf.R;
   for (int base = 0; base < R; base += kThreads) {
     const int k = base + tid;
     cf D[NARM][NP];
     float sw = 0.0f;
+    // geometric grid: f_k = f_tile * exp(lane * delta), with the tile's first frequency formed in FP64
+    float ftile = 0.0f;
+    if (ev.spacing == 0) {
+      double ft = 0.0;
+      if (lane == 0) ft = exp(g.lnfmin + (double)(base + warp * 32) * g.delta);
+      ftile = (float)__shfl_sync(0xffffffffu, ft, 0);
+    }
     if (k < R) {
       float f, lnf, w;
       if (ev.spacing == 0) {
-        lnf = gf.lnfmin + (float)k * gf.delta;
+        lnf = (float)(g.lnfmin + (double)k * g.delta);
         if (k == R - 1) { f = gf.fcut; w = f * gf.wl; }
         else if (k == 0) { f = gf.fmin; w = f * gf.w0; }
-        else { f = expf(lnf); w = f * gf.fac_w; }
+        else { f = ftile * expf((float)lane * gf.delta); w = f * gf.fac_w; }
       } else {
         f = (k == R - 1) ? gf.fcut : gf.fmin + (float)k * gf.df;
         lnf = logf(f);
@@ -230,12 +350,14 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
       }
       const float S = psd_at_f(det, f, lnf);
       sw = sqrtf(4.0f * w / S);
-      DF4 A, Phi;
+      DF4 A;
+      float dphi[4];
       float dtn[4] = {0.f, 0.f, 0.f, 0.f};
       TimeF ts;
+      phase_tangent_f(pbf, f, lnf, dphi);
       if (MODEL == 0) {
-        const float f13 = expf(lnf * (1.0f / 3.0f));
-        tf2_point<DF4>(EF.tf2, f, f13, lnf, expf(lnf * (-7.0f / 6.0f)), A, Phi);
+        const float f13 = cbrtf(f);
+        A = EF.tf2.ampK * (1.0f / (f * sqrtf(f13)));
         if (EARTH) {
           const DF4 tau = tau_star_point<DF4>(EF.tf2.Ms, EF.tf2.vM, EF.tf2.eta, f13);
 #pragma unroll
@@ -243,9 +365,9 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
           time_f(pf, -tau.v * (1.0f / 86400.0f), ts);
         }
       } else {
-        phd_point<DF4>(EF.phd, f, A, Phi);
+        A = phd_amp_point<DF4>(EF.phd, f);
         if (EARTH) {
-          const DF4 tau = tau_star_point<DF4>(EF.phd.Ms, EF.phd.vM, EF.phd.eta, expf(lnf * (1.0f / 3.0f)));
+          const DF4 tau = tau_star_point<DF4>(EF.phd.Ms, EF.phd.vM, EF.phd.eta, cbrtf(f));
 #pragma unroll
           for (int q = 0; q < 4; ++q) dtn[q] = -tau.d[q] * (1.0f / 86400.0f);
           time_f(pf, -tau.v * (1.0f / 86400.0f), ts);
@@ -256,7 +378,7 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
       cf dP[4], dC[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        const cf dW = {A.d[q], -A.v * Phi.d[q]};
+        const cf dW = {A.d[q], -A.v * dphi[q]};
         dP[q] = fscale(dW, pf.cp);
         dC[q] = fscale(dW, pf.ci);
       }
@@ -274,71 +396,85 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
 #pragma unroll
         for (int q = 0; q < NP; ++q) D[a][q] = {0.0f, 0.0f};
     }
+    // Quantise the sqrt(weight)-scaled derivative vectors to integers, |q| < 2^(kQBits-1+1),
+    // on a per-column power-of-two scale that follows the largest magnitude this warp has seen.
+    // The rounding is a perturbation of the vectors themselves, so the accumulated Gram matrix
+    // stays an exact Gram matrix of slightly perturbed vectors (positive semidefinite).
+    const int* Mo = &colM[par][warp][0];
+    int* Mn = &colM[par ^ 1][warp][0];
 #pragma unroll
-    for (int q = 0; q < NP; ++q) {
-      if (NG == 1) {
-        my[(0 * NQ + q) * 32 + lane] = fscale(D[0][q], sw);
-      } else if (NG == 2) {
-        const cf u = D[0][q], v = D[1][q];
-        my[(0 * NQ + q) * 32 + lane] = fscale(fadd(u, v), sw * 1.2247448713915890f);
-        my[(1 * NQ + q) * 32 + lane] = fscale(fadd(u, fscale(v, -1.0f)), sw * 0.70710678118654752f);
-      } else {
-        const cf u = D[0][q], v = D[1][q];
-        my[(0 * NQ + q) * 32 + lane] = fscale(u, sw);
-        my[(1 * NQ + q) * 32 + lane] = fscale(v, sw);
-        my[(2 * NQ + q) * 32 + lane] = fscale(fadd(u, v), -sw);
+    for (int gs = 0; gs < NG; ++gs)
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        cf u;
+        if (NG == 1) u = fscale(D[0][q], sw);
+        else if (NG == 2) u = gs == 0 ? fscale(fadd(D[0][q], D[1][q]), sw * 1.2247448713915890f)
+                                      : fscale(fadd(D[0][q], fscale(D[1][q], -1.0f)), sw * 0.70710678118654752f);
+        else u = gs == 0 ? fscale(D[0][q], sw) : gs == 1 ? fscale(D[1][q], sw) : fscale(fadd(D[0][q], D[1][q]), -sw);
+        const int mold = Mo[gs * NQ + q];
+        const unsigned bits = max(__float_as_uint(fabsf(u.re)), __float_as_uint(fabsf(u.im)));
+        const int e = (int)(__reduce_max_sync(0xffffffffu, bits) >> 23) - 127;
+        bad |= e > 127;                                   // Inf or NaN somewhere in the tile
+        const int mnew = min(max(mold, e), 127);
+        moved |= mnew != mold;
+        if (lane == 0) Mn[gs * NQ + q] = mnew;
+        const float s = __int_as_float((127 + kQBits - 1 - mnew) << 23);   // 2^(kQBits-1-mnew)
+        const int qr = __float_as_int(fmaf(u.re, s, kRoundMagic)) - kRoundMagicBits;
+        const int qi = __float_as_int(fmaf(u.im, s, kRoundMagic)) - kRoundMagicBits;
+        my[(gs * NQ + q) * 32 + lane] = make_int2(qr, qi);
       }
-    }
     __syncwarp();
 #pragma unroll
     for (int i = 0; i < BPL; ++i) {
-      const int bl = lane + 32 * i;
+      const int bl = (NG == 1 ? (lane & 15) : lane + 32 * i);
       if (bl < NB) {
         const int gs = bl >> 4, bi = bl & 15;
         const int r0 = 2 * kBlkR[bi], c0 = 3 * kBlkC[bi];
-        const cf* base_g = my + gs * NQ * 32;
-        float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll 4
-        for (int j = 0; j < 32; ++j) {
-          const cf a0 = base_g[(r0 + 0) * 32 + j], a1 = base_g[(r0 + 1) * 32 + j];
-          const cf b0 = base_g[(c0 + 0) * 32 + j], b1 = base_g[(c0 + 1) * 32 + j], b2 = base_g[(c0 + 2) * 32 + j];
-          s[0] += a0.re * b0.re + a0.im * b0.im;
-          s[1] += a0.re * b1.re + a0.im * b1.im;
-          s[2] += a0.re * b2.re + a0.im * b2.im;
-          s[3] += a1.re * b0.re + a1.im * b0.im;
-          s[4] += a1.re * b1.re + a1.im * b1.im;
-          s[5] += a1.re * b2.re + a1.im * b2.im;
-        }
+        const int2* base_g = my + gs * NQ * 32;
+        if (moved) {   // rescale the running sums to the new column scales
+          const int* mo = Mo + gs * NQ;
+          const int* mn = Mn + gs * NQ;
 #pragma unroll
-        for (int e = 0; e < 6; ++e) {  // Kahan-compensated accumulation across tiles
-          const float y = s[e] - cmp[i][e];
-          const float t = acc[i][e] + y;
-          cmp[i][e] = (t - acc[i][e]) - y;
-          acc[i][e] = t;
+          for (int e = 0; e < 6; ++e) {
+            const int r = r0 + e / 3, c = c0 + e % 3;
+            const int sh = (mn[r] - mo[r]) + (mn[c] - mo[c]);
+            acc[i][e] = sh >= 63 ? 0ll : (acc[i][e] >> sh);
+          }
+        }
+        const int j0 = NG == 1 ? 16 * (lane >> 4) : 0;
+        constexpr int NJ = NG == 1 ? 16 : 32;
+#pragma unroll 4
+        for (int jj = 0; jj < NJ; ++jj) {
+          const int j = j0 + jj;
+          const int2 a0 = base_g[(r0 + 0) * 32 + j], a1 = base_g[(r0 + 1) * 32 + j];
+          const int2 b0 = base_g[(c0 + 0) * 32 + j], b1 = base_g[(c0 + 1) * 32 + j], b2 = base_g[(c0 + 2) * 32 + j];
+          acc[i][0] += (long long)a0.x * b0.x + (long long)a0.y * b0.y;
+          acc[i][1] += (long long)a0.x * b1.x + (long long)a0.y * b1.y;
+          acc[i][2] += (long long)a0.x * b2.x + (long long)a0.y * b2.y;
+          acc[i][3] += (long long)a1.x * b0.x + (long long)a1.y * b0.y;
+          acc[i][4] += (long long)a1.x * b1.x + (long long)a1.y * b1.y;
+          acc[i][5] += (long long)a1.x * b2.x + (long long)a1.y * b2.y;
         }
       }
     }
+    par ^= 1;
+    moved = false;
+    if (++tiles == kFlushTiles) {   // keep |sum| < 2^63: move the integer sums into FP64
+      flush_fixed<NG, NQ, BPL, NB>(acc, &colM[par][warp][0], &fl[warp][0][0][0], lane);
+      tiles = 0;
+    }
     __syncwarp();
   }
-  // cross-warp reduction in FP64
+  flush_fixed<NG, NQ, BPL, NB>(acc, &colM[par][warp][0], &fl[warp][0][0][0], lane);
+  if (lane == 0 && bad) badw[warp] = 1;
   __syncthreads();
-  double* red = reinterpret_cast<double*>(stage_raw);  // [kWarps][NG][NQ][NQ]
-  for (int i = tid; i < kWarps * NG * NQ * NQ; i += kThreads) red[i] = 0.0;
-  __syncthreads();
-#pragma unroll
-  for (int i = 0; i < BPL; ++i) {
-    const int bl = lane + 32 * i;
-    if (bl < NB) {
-      const int gs = bl >> 4, bi = bl & 15;
-      const int r0 = 2 * kBlkR[bi], c0 = 3 * kBlkC[bi];
-      double* o = red + ((size_t)(warp * NG + gs) * NQ) * NQ;
-#pragma unroll
-      for (int e = 0; e < 6; ++e) o[(r0 + e / 3) * NQ + c0 + e % 3] = (double)acc[i][e] - (double)cmp[i][e];
-    }
-  }
-  __syncthreads();
+  // sum over warps in FP64
+  const double* red = &fl[0][0][0][0];  // [kWarps][NG][NQ][NQ]
   const long long N = ev.N;
-  const double sc = scale;
+  int anybad = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; ++w) anybad |= badw[w];
+  const double sc = anybad ? __longlong_as_double(0x7ff8000000000000ll) : scale;
   for (int e = tid; e < NE; e += kThreads) {
     const int a = kPairA[e], b = kPairB[e];
     double sdet = 0.0;

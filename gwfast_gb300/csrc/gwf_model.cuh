@@ -422,6 +422,103 @@ __device__ __forceinline__ void phd_point(const PhdCoreT<C>& k, typename Real<S>
   phase = (xv < T(kMfCut)) ? ph - co<S>(k.t0) * (x - co<S>(k.fRef)) - co<S>(k.phiRef) : ph;
 }
 
+// IMRPhenomD amplitude only
+template <class S, class C>
+__device__ __forceinline__ S phd_amp_point(const PhdCoreT<C>& k, typename Real<S>::T f) {
+  typedef typename Real<S>::T T;
+  const S x = co<S>(k.MG) * f;
+  return co<S>(k.ampPref) * (T(1) / (x * dsqrt(dcbrt(x)))) * complete_amp_shape(k, x);
+}
+
+// ------------------------------------------------------------------ phase tangent in a frequency basis
+// Within each region the phase is a fixed linear combination of basis functions of the physical
+// frequency f with parameter-dependent coefficients:
+//   inspiral (Mf < 0.018), 13 terms: f^-5/3 f^-1 f^-2/3 f^-1/3 1 ln f f^1/3 f^1/3 ln f f^2/3 f f^4/3 f^5/3 f^2
+//   intermediate (Mf < fring/2), 4 terms: f f^-3 ln f 1
+//   merger-ringdown (Mf < 0.2), 5 terms: f^-1 f^3/4 f 1 atan((U1 f - U0))
+// (expanding (pi M f)^q = (pi M)^q f^q and folding -t0 (Mf - MfRef) - phiRef into the f and 1
+// coefficients).  Their d/d(Mc, eta, chi1z, chi2z) are formed here in FP64; large terms that
+// cancel in the tangent (the eta-independence of the Newtonian term at fixed Mc, the t0 shift
+// against the merger slope, the reference-phase subtraction) therefore cancel in FP64, once
+// per event, and the per-point FP32 work is a short, well-conditioned sum.
+struct PhaseBasis {
+  D4 ins[13];
+  D4 itm[4];
+  D4 mrd[5];
+  D4 U1, U0;
+  D4 MG;          // region boundaries are tested on MG f
+  double fMRD;    // intermediate/merger join in Mf
+  double pad;
+};
+
+__device__ inline void tf2_phase_basis(const TF2Ev& e, PhaseBasis& b) {
+  // Phi = A (pi Ms f)^(-5/3) [1 + c2 v^2 + ... ] with v = (pi Ms f)^(1/3)  (gwfast/waveforms.py:860)
+  const D4 lpm = dlog(kPi * e.Ms);
+  const D4 pm13 = dexp(lpm * (1.0 / 3.0));
+  const D4 pm_53 = dexp(lpm * (-5.0 / 3.0));
+  const D4 pm13_2 = pm13 * pm13;
+  const PNC& c = e.pn;
+  for (int i = 0; i < 13; ++i) b.ins[i] = D4(0.0);
+  b.ins[0] = c.A * pm_53;
+  b.ins[1] = c.A * c.c2 * pm_53 * pm13_2;
+  b.ins[2] = c.A * c.c3 * pm_53 * pm13_2 * pm13;
+  b.ins[3] = c.A * c.c4 * pm_53 * pm13_2 * pm13_2;
+  b.ins[4] = c.A * (c.c5 + c.c5l * lpm * (1.0 / 3.0));
+  b.ins[5] = c.A * c.c5l * (1.0 / 3.0);
+  b.ins[6] = c.A * (c.c6 + c.c6l * lpm * (1.0 / 3.0)) * pm13;
+  b.ins[7] = c.A * c.c6l * (1.0 / 3.0) * pm13;
+  b.ins[8] = c.A * c.c7 * pm13_2;
+  for (int i = 0; i < 4; ++i) b.itm[i] = D4(0.0);
+  for (int i = 0; i < 5; ++i) b.mrd[i] = D4(0.0);
+  b.U1 = D4(0.0); b.U0 = D4(0.0);
+  b.MG = D4(0.0);  // every point is in the inspiral form
+  b.fMRD = 1e30;
+  b.pad = 0.0;
+}
+
+__device__ inline void phd_phase_basis(const PhdCore& k, PhaseBasis& b) {
+  const D4& MG = k.MG;
+  const D4 eta = k.eta;
+  const D4 lpm = dlog(kPi * MG);
+  const D4 pm13 = dexp(lpm * (1.0 / 3.0));
+  const D4 pm_53 = dexp(lpm * (-5.0 / 3.0));
+  const D4 pm13_2 = pm13 * pm13;
+  const PNC& c = k.pn;
+  const D4 lin = k.t0 * k.fRef - k.phiRef;           // constant part of -t0 (Mf - MfRef) - phiRef
+  const D4 m13 = dexp(dlog(MG) * (1.0 / 3.0));
+  // inspiral (gwfast/waveforms.py:1145)
+  b.ins[0] = c.A * pm_53;
+  b.ins[1] = c.A * c.c2 * pm_53 * pm13_2;
+  b.ins[2] = c.A * c.c3 * pm_53 * pm13_2 * pm13;
+  b.ins[3] = c.A * c.c4 * pm_53 * pm13_2 * pm13_2;
+  b.ins[4] = c.A * (c.c5 + c.c5l * lpm * (1.0 / 3.0)) + lin;
+  b.ins[5] = c.A * c.c5l * (1.0 / 3.0);
+  b.ins[6] = c.A * (c.c6 + c.c6l * lpm * (1.0 / 3.0)) * pm13;
+  b.ins[7] = c.A * c.c6l * (1.0 / 3.0) * pm13;
+  b.ins[8] = c.A * c.c7 * pm13_2;
+  b.ins[9] = (k.sig[0] / eta - k.t0) * MG;
+  b.ins[10] = (0.75 * k.sig[1] / eta) * MG * m13;
+  b.ins[11] = (0.6 * k.sig[2] / eta) * MG * m13 * m13;
+  b.ins[12] = (0.5 * k.sig[3] / eta) * MG * MG;
+  // intermediate: (b1 x - b3/(3 x^3) + b2 ln x)/eta + C1Int + C2Int x
+  b.itm[0] = (k.bet[0] / eta + k.C2Int - k.t0) * MG;
+  b.itm[1] = -k.bet[2] / (3.0 * eta * MG * MG * MG);
+  b.itm[2] = k.bet[1] / eta;
+  b.itm[3] = k.bet[1] / eta * dlog(MG) + k.C1Int + lin;
+  // merger-ringdown: (-a2/x + 4/3 a3 x^3/4 + a1 x + a4 atan((x - a5 fring)/fdamp))/eta + C1MRD + C2MRD x
+  const D4 m14 = dsqrt(dsqrt(MG));
+  b.mrd[0] = -k.alp[1] / (eta * MG);
+  b.mrd[1] = (4.0 / 3.0) * k.alp[2] / eta * m14 * m14 * m14;
+  b.mrd[2] = (k.alp[0] / eta + k.C2MRD - k.t0) * MG;
+  b.mrd[3] = k.C1MRD + lin;
+  b.mrd[4] = k.alp[3] / eta;
+  b.U1 = MG / k.fdamp;
+  b.U0 = k.alp[4] * k.fring / k.fdamp;
+  b.MG = MG;
+  b.fMRD = k.fMRD.v;
+  b.pad = 0.0;
+}
+
 // ------------------------------------------------------------------ IMRPhenomHM (gwfast/waveforms.py:2256-2616)
 template <class C> struct HMModeT {
   C rho, tau, C1, C2, frlm;

@@ -33,7 +33,7 @@ cudaError_t fisher_one(const LaunchArgs& a) {
 template <bool EARTH, int NARM, int NG>
 cudaError_t fisher_one_f32(const LaunchArgs& a) {
   auto k = fisher_kernel_f32<1, EARTH, NARM, NG>;
-  const int smem = kWarps * NG * 12 * 32 * (int)sizeof(cf);
+  const int smem = kWarps * NG * 12 * 32 * (int)sizeof(int2);
   cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (err != cudaSuccess) return err;
   return chunked(a, [&](const EvBatch& ev, long long cnt) {
