@@ -49,6 +49,8 @@ SIGNATURES = {
     'gwf_fisher': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32, _vp, ctypes.c_int,
                     ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
     'gwf_cov': ([_vp, _vp, _i64, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
+    'gwf_fisher_noalloc': ([_P(DetDesc), _vp, _vp, _i64, _P(WfDesc), _vp, _vp, _vp, _i64, _vp, _i64, _i64,
+                            ctypes.c_int32, ctypes.c_int, _vp, _vp], ctypes.c_int),
 }
 
 _lock = threading.Lock()

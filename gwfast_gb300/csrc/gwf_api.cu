@@ -75,6 +75,11 @@ struct DetRec {
 
 }  // namespace
 
+namespace gwf {
+// error text for gwf_last_error from the other translation units
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace gwf
+
 struct gwf_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;

@@ -113,6 +113,36 @@ int gwf_fisher(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* w
 int gwf_cov(gwf_ctx* ctx, const double* F, int64_t n_events, int mem, double* cov, double* eps, double* cond,
             void* stream);
 
+/* Limits of gwf_fisher_noalloc: its scratch is one fixed array of GWF_NOALLOC_SCRATCH_MIB MiB
+ * per GPU that loads the library, held until the process exits. */
+#define GWF_NOALLOC_SCRATCH_MIB 24
+#define GWF_NOALLOC_MAX_PSD 16384 /* PSD table rows */
+#define GWF_NOALLOC_MAX_QNM 2048  /* QNM table rows */
+
+/* FP64 Fisher matrices of one detector, with no device memory allocated by the library.
+ *
+ * No counterpart in the reference: this entry point exists for callers that cannot call
+ * cudaMalloc — programs whose device memory belongs to their own pool allocator (a framework
+ * that reserves the GPU at start-up, where a library's cudaMalloc fails or fragments the
+ * pool), or loops that cannot take the device synchronisation of cudaMalloc/cudaFree. It needs
+ * no context. The caller passes the detector, its PSD table and (IMRPhenomD only) the QNM table
+ * in host memory, as gwf_detector_add and gwf_set_qnm_table take them, and params ([11][ld],
+ * Fisher order, float64) and out ([n_events][11][11], float64) in DEVICE memory. accumulate != 0
+ * adds into out, so a network is the sum of calls over its detectors. Geometric frequency
+ * grid with res points per event; detector total over the arms of a triangle.
+ *
+ * Scratch (the PSD table and its index, the QNM table and the per-event set-up records) lives
+ * in a file-scope __device__ array of GWF_NOALLOC_SCRATCH_MIB MiB; events run in passes that fit
+ * it. PSD tables longer than GWF_NOALLOC_MAX_PSD rows or QNM tables longer than
+ * GWF_NOALLOC_MAX_QNM rows are rejected with GWF_ERR_INVALID_ARG. The first call on a device
+ * (with that device current) looks the array's address up; make that first call before any
+ * stream capture. Every call shares the array and rewrites what it reads; calls whose GPU work
+ * overlaps (unordered streams) race on it. stream NULL = the default stream. */
+int gwf_fisher_noalloc(const gwf_det_desc* det, const double* psd_f, const double* psd_S, int64_t n_psd,
+                       const gwf_wf_desc* wf, const double* qnm_spin, const double* qnm_fring, const double* qnm_fdamp,
+                       int64_t n_qnm, const double* params, int64_t ld, int64_t n_events, int32_t res, int accumulate,
+                       double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
