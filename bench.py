@@ -6,11 +6,14 @@ triangle at Sardinia (5 Hz wall), Earth rotation on, 2000 log-spaced frequency p
 per event and detector, analytic aLIGO PSD fit.  One step = the network Fisher matrix
 (11x11, summed over detectors and arms) of every event.
 
-value: events/s of the chosen form (FP32 split precision) with the event arrays resident
-       in HBM, CUDA-event timed per step (L2 flushed by a 256 MB write before each step,
-       outside the timed interval).  The plain FP64 kernel is timed the same way
-       (`plain_fp64`), and the chosen form's marginalised 1-sigma errors are compared with
-       the FP64 ones on the workload's events (`sigma_err`).
+value: events/s of the chosen form with the event arrays resident in HBM, CUDA-event timed
+       per step (L2 flushed by a 256 MB write before each step, outside the timed interval).
+       The chosen form is 'mixed': the FP32 split-precision kernel for every event, the
+       condition number of every network Fisher, and the FP64 kernel again for the events
+       above 3e11 (gathered, recomputed, scattered back), all inside the step.  The plain FP64
+       kernel and the FP32 form alone are timed the same way (`plain_fp64`, `fp32_only`), and
+       the marginalised 1-sigma errors of both reduced forms are compared with the FP64 ones
+       on the workload's events (`sigma_err`, `sigma_err_fp32_only`).
 e2e:   the chosen form through the public API (DetNet.FisherMatr on a host events dict),
        wall-clock, host->device copy of the parameters and device->host copy of the Fisher
        matrices included.
@@ -171,7 +174,8 @@ def main():
     ap.add_argument('--ref-events', type=int, default=6)
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--only-device', action='store_true', help='only the device-resident Fisher steps (for ncu)')
-    ap.add_argument('--precision', default='fp32', choices=('fp32', 'fp64'), help='form used with --only-device')
+    ap.add_argument('--precision', default='fp32', choices=('fp32', 'fp64', 'mixed'), help='form used with --only-device')
+    ap.add_argument('--refine-cond', type=float, default=3e11, help='condition-number threshold of the mixed form')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
@@ -203,7 +207,10 @@ def main():
     desc = wf.gpu_desc()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
 
-    def fisher_step(det_ids=ids, o=out, precision='fp32'):
+    ctx.set_refine_cond(args.refine_cond)
+    out32 = torch.empty((N, 11, 11), dtype=torch.float64, device=dev)
+
+    def fisher_step(det_ids=ids, o=out, precision='mixed'):
         ctx.fisher(det_ids, desc, p_dev, RES, per_arm=False, mem=_lib.MEM_DEVICE, out_net=o, stream=stream.cuda_stream,
                    ld=N, n=N, precision=precision)
 
@@ -230,6 +237,7 @@ def main():
         return
     for _ in range(args.warmup):
         fisher_step()
+        fisher_step(o=out32, precision='fp32')
         fisher_step(o=out64, precision='fp64')
         snr_step()
     torch.cuda.synchronize()
@@ -244,33 +252,44 @@ def main():
     torch.cuda.synchronize()
     clocks = clk.stop()
     ms64 = timed(lambda: fisher_step(o=out64, precision='fp64'), args.steps)
+    ms32 = timed(lambda: fisher_step(o=out32, precision='fp32'), args.steps)
     ms_snr = timed(snr_step, args.steps)
     # per-kernel launches alone: the ET triangle kernel dominates
-    ms_et = timed(lambda: fisher_step([ids[2]]), args.steps)
-    ms_l1 = timed(lambda: fisher_step([ids[0]]), args.steps)
+    ms_et = timed(lambda: fisher_step([ids[2]], o=out32, precision='fp32'), args.steps)
+    ms_l1 = timed(lambda: fisher_step([ids[0]], o=out32, precision='fp32'), args.steps)
     ms_et64 = timed(lambda: fisher_step([ids[2]], precision='fp64'), max(1, args.steps // 2))
     if world > 1:
-        t = torch.tensor([ms, ms64, ms_snr], dtype=torch.float64, device=dev)
+        t = torch.tensor([ms, ms64, ms32, ms_snr], dtype=torch.float64, device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms, ms64, ms_snr = (float(x) for x in t)
-    # accuracy of the chosen form on this workload: marginalised 1-sigma errors against FP64
+        ms, ms64, ms32, ms_snr = (float(x) for x in t)
+    # accuracy of the reduced forms on this workload: marginalised 1-sigma errors against FP64
     fisher_step()
+    fisher_step(o=out32, precision='fp32')
     fisher_step(o=out64, precision='fp64')
     torch.cuda.synchronize()
+    Fm_all = out.cpu().numpy()
+    F64_all = out64.cpu().numpy()
+    refined = float(np.mean(np.all(Fm_all == F64_all, axis=(1, 2))))
     nchk = min(N, 4000)
-    F32 = out[:nchk].cpu().numpy()
-    F64 = out64[:nchk].cpu().numpy()
-    c32, _, _ = fisherTools.CovMatr(np.moveaxis(F32, 0, -1), return_cond=True, device=local)
-    c64, _, cond = fisherTools.CovMatr(np.moveaxis(F64, 0, -1), return_cond=True, device=local)
-    s32, s64 = np.sqrt(np.einsum('iin->ni', c32)), np.sqrt(np.einsum('iin->ni', c64))
-    serr = np.nanmax(np.abs(s32 - s64) / s64, axis=1)
+    c64, _, cond = fisherTools.CovMatr(np.moveaxis(F64_all[:nchk], 0, -1), return_cond=True, device=local)
+    s64 = np.sqrt(np.einsum('iin->ni', c64))
+
+    def sig_err(F):
+        c, _, _ = fisherTools.CovMatr(np.moveaxis(F[:nchk], 0, -1), return_cond=True, device=local)
+        e = np.nanmax(np.abs(np.sqrt(np.einsum('iin->ni', c)) - s64) / s64, axis=1)
+        return {'events': int(nchk), 'median': float(np.nanmedian(e)), 'p99': float(np.nanpercentile(e, 99)),
+                'max': float(np.nanmax(e)), 'frac_le_1e-3': float(np.mean(e <= 1e-3)),
+                'what': 'max over 11 parameters of |sigma - sigma_fp64| / sigma_fp64 per event'}
+
+    serr_mixed = sig_err(Fm_all)
+    serr_fp32 = sig_err(out32.cpu().numpy())
     # end to end through the public API with host buffers
     for _ in range(max(1, args.warmup // 2)):
-        net.FisherMatr(dict(ev), res=RES, precision='fp32')
+        net.FisherMatr(dict(ev), res=RES, precision='mixed', refine_cond=args.refine_cond)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        F_host = net.FisherMatr(dict(ev), res=RES, precision='fp32')
+        F_host = net.FisherMatr(dict(ev), res=RES, precision='mixed', refine_cond=args.refine_cond)
     e2e_s = (time.perf_counter() - t0) / args.steps
     if rank != 0:
         torch.distributed.destroy_process_group()
@@ -285,18 +304,21 @@ def main():
     line = {
         'metric': METRIC, 'value': world * N / (ms / 1e3), 'unit': 'Fisher/s', 'n_gpus': world, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
-        'dtype': 'f32 per point (f64 per-event set-up, scaling and outputs)',
+        'dtype': 'f32 per point (f64 per-event set-up, scaling, outputs, and f64 throughout for events with cond > %.0e)'
+                 % args.refine_cond,
         'data': 'synthetic (seeded BBH catalogue, analytic aLIGO PSD fit)',
-        'config': {'workload': 'IMRPhenomD BBH 1e4 events, L1+H1+ETS, Earth rotation, R=2000; FP32 split-precision kernel',
+        'config': {'workload': 'IMRPhenomD BBH 1e4 events, L1+H1+ETS, Earth rotation, R=2000; mixed form (FP32 '
+                               'split precision, FP64 for equilibrated cond > %.0e)' % args.refine_cond,
                    'events_per_gpu': N, 'res': RES, 'parallelism': 'replicas over event shards' if world > 1 else 'single',
                    'l2': 'flushed (256 MB write) before every step'},
         'plain_fp64': {'value': world * N / (ms64 / 1e3), 'unit': 'Fisher/s', 'ms_per_step': ms64},
         'speedup_vs_plain_fp64': ms64 / ms,
-        'sigma_err': {'events': int(nchk), 'median': float(np.nanmedian(serr)), 'p99': float(np.nanpercentile(serr, 99)),
-                      'max': float(np.nanmax(serr)), 'frac_le_1e-3': float(np.mean(serr <= 1e-3)),
-                      'what': 'max over 11 parameters of |sigma_fp32 - sigma_fp64| / sigma_fp64 per event'},
+        'fp32_only': {'value': world * N / (ms32 / 1e3), 'unit': 'Fisher/s', 'ms_per_step': ms32},
+        'refined_fraction': refined,
+        'sigma_err': serr_mixed,
+        'sigma_err_fp32_only': serr_fp32,
         'snr_per_s': world * N / (ms_snr / 1e3),
-        'gpu_launches': 6,
+        'gpu_launches': 6 + 2 + (8 if refined > 0 else 0),
         'e2e': {'value': world * N / e2e_s, 'unit': 'Fisher/s', 'h2d_bytes_per_step': int(p_host.nbytes),
                 'd2h_bytes_per_step': int(F_host.nbytes)},
         'roofline': {'bound': 'fp32', 'kernel': 'fisher_kernel_f32<IMRPhenomD, earth, triangle>',

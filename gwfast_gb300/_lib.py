@@ -15,7 +15,7 @@ GWF_OK = 0
 ERRORS = {-1: 'invalid argument', -2: 'CUDA error', -3: 'out of memory', -4: 'timeout', -5: 'unsupported'}
 MODEL_IDS = {'TaylorF2_RestrictedPN': 0, 'IMRPhenomD': 1, 'IMRPhenomHM': 2}
 MEM_HOST, MEM_DEVICE = 0, 1
-PRECISION = {'fp64': 0, 'fp32': 1}
+PRECISION = {'fp64': 0, 'fp32': 1, 'mixed': 2}
 
 
 class GWFError(RuntimeError):
@@ -49,6 +49,7 @@ SIGNATURES = {
     'gwf_fisher': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32, _vp, ctypes.c_int,
                     ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
     'gwf_cov': ([_vp, _vp, _i64, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
+    'gwf_set_refine_cond': ([_vp, _d], ctypes.c_int),
     'gwf_fisher_noalloc': ([_P(DetDesc), _vp, _vp, _i64, _P(WfDesc), _vp, _vp, _vp, _i64, _vp, _i64, _i64,
                             ctypes.c_int32, ctypes.c_int, _vp, _vp], ctypes.c_int),
 }
@@ -142,6 +143,10 @@ class Context:
         check(load().gwf_fisher(self.h, len(ids), ptr(ids), ctypes.byref(wf), ptr(params), ld, n, int(res),
                                 ptr(res_ev), spacing, int(bool(per_arm)), PRECISION[precision], mem, ptr(out_arm),
                                 ptr(out_net), stream))
+
+    def set_refine_cond(self, kappa):
+        """Condition-number threshold above which the 'mixed' form recomputes an event in FP64."""
+        check(load().gwf_set_refine_cond(self.h, float(kappa)))
 
     def cov(self, F, mem=MEM_HOST, cov=None, eps=None, cond=None, n=None, stream=None):
         n = F.shape[0] if n is None else n

@@ -87,6 +87,8 @@ struct gwf_ctx {
   double* d_qnm = nullptr;
   int nq = 0;
   DevBuf par, res, oarm, onet, fin, fout, feps, fcond, setup;
+  DevBuf mix_idx, mix_cnt, mix_par, mix_res, mix_net, mix_arm;  // FP64 recomputation of GWF_PREC_MIXED
+  double refine_cond = 3e11;
   cudaEvent_t scratch_free = nullptr;  // recorded after the last launch that used the set-up scratch
   HostBuf hpar, hout;
 };
@@ -172,6 +174,56 @@ int stage_inputs(gwf_ctx* ctx, const double* params, int64_t ld, int64_t N, cons
   return GWF_OK;
 }
 
+// GWF_PREC_MIXED, second stage: condition numbers of the FP32 network Fishers, then the FP64
+// Fisher of the events above the threshold, computed as a compact batch and scattered back
+int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const double* dp, int64_t dld,
+           const int* dres, int64_t N, int slots, double* darm, double* dnet, cudaStream_t st) {
+  const size_t per = (size_t)gwf::NP * gwf::NP;
+  if (ctx->fout.ensure((size_t)N * per * sizeof(double)) || ctx->fcond.ensure((size_t)N * sizeof(double)) ||
+      ctx->mix_idx.ensure((size_t)N * sizeof(long long)) || ctx->mix_cnt.ensure(sizeof(unsigned long long)))
+    return fail(GWF_ERR_OOM, "device allocation failed (mixed precision)");
+  long long* idx = (long long*)ctx->mix_idx.p;
+  cudaError_t e = gwf::launch_cov(dnet, N, (double*)ctx->fout.p, nullptr, (double*)ctx->fcond.p, st);
+  if (e == cudaSuccess)
+    e = gwf::launch_select((const double*)ctx->fcond.p, N, ctx->refine_cond, idx, (unsigned long long*)ctx->mix_cnt.p, st);
+  unsigned long long M = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&M, ctx->mix_cnt.p, sizeof(M), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("mixed precision: ") + cudaGetErrorString(e));
+  if (M == 0) return GWF_OK;
+  if (ctx->mix_par.ensure(M * gwf::NP * sizeof(double)) || ctx->mix_net.ensure(M * per * sizeof(double)) ||
+      (dres && ctx->mix_res.ensure(M * sizeof(int))) || (darm && ctx->mix_arm.ensure((size_t)slots * M * per * sizeof(double))))
+    return fail(GWF_ERR_OOM, "device allocation failed (mixed precision)");
+  double* cpar = (double*)ctx->mix_par.p;
+  double* cnet = (double*)ctx->mix_net.p;
+  double* carm = darm ? (double*)ctx->mix_arm.p : nullptr;
+  int* cres = dres ? (int*)ctx->mix_res.p : nullptr;
+  e = gwf::launch_gather(dp, dld, dres, idx, (long long)M, cpar, cres, st);
+  if (e != cudaSuccess) return fail(GWF_ERR_CUDA, cudaGetErrorString(e));
+  a.ev.p = cpar;
+  a.ev.ld = (long long)M;
+  a.ev.N = (long long)M;
+  a.ev.res_ev = cres;
+  a.precision = GWF_PREC_FP64;
+  int slot = 0;
+  for (int i = 0; i < n_det; ++i) {
+    const DetRec& r = ctx->dets[det_ids[i]];
+    a.det = dev_of(r);
+    a.out_arm = carm ? carm + (size_t)slot * M * per : nullptr;
+    a.out_det = cnet;
+    a.accum = i > 0;
+    const int model = a.wf.model;
+    e = model == 0 ? gwf::launch_fisher_m0(a) : gwf::launch_fisher_m1(a);
+    if (e != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    slot += r.desc.shape == GWF_SHAPE_T ? 3 : 1;
+  }
+  e = gwf::launch_scatter(cnet, idx, (long long)M, (int)per, dnet, st);
+  for (int s = 0; carm && s < slots && e == cudaSuccess; ++s)
+    e = gwf::launch_scatter(carm + (size_t)s * M * per, idx, (long long)M, (int)per, darm + (size_t)s * N * per, st);
+  if (e != cudaSuccess) return fail(GWF_ERR_CUDA, cudaGetErrorString(e));
+  return GWF_OK;
+}
+
 int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params,
         int64_t ld, int64_t N, int32_t res, const int32_t* res_ev, int spacing, int per_arm, int precision, int mem,
         double* out_arm, double* out_net, void* stream) {
@@ -180,8 +232,9 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
   rc = validate_common(ctx, n_det, det_ids, wf, params, ld, N, res, res_ev, spacing, mem);
   if (rc) return rc;
   if (!out_arm && !out_net) return fail(GWF_ERR_INVALID_ARG, "no output requested");
-  if (precision != GWF_PREC_FP64 && precision != GWF_PREC_FP32) return fail(GWF_ERR_INVALID_ARG, "bad precision");
-  if (precision == GWF_PREC_FP32 && (!fisher || wf->model == GWF_WF_PHENOMHM))
+  if (precision != GWF_PREC_FP64 && precision != GWF_PREC_FP32 && precision != GWF_PREC_MIXED)
+    return fail(GWF_ERR_INVALID_ARG, "bad precision");
+  if (precision != GWF_PREC_FP64 && (!fisher || wf->model == GWF_WF_PHENOMHM))
     return fail(GWF_ERR_UNSUPPORTED, "FP32 split precision is implemented for the TaylorF2 and IMRPhenomD Fisher");
   if (fisher && !per_arm) out_arm = nullptr;
   if (fisher && per_arm && !out_arm) return fail(GWF_ERR_INVALID_ARG, "per_arm needs out_arm");
@@ -212,6 +265,11 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
       dnet = (double*)ctx->onet.p;
     }
   }
+  // the mixed form needs the network total to decide which events get FP64
+  if (precision == GWF_PREC_MIXED && !dnet) {
+    if (ctx->onet.ensure((size_t)N * per * sizeof(double))) return fail(GWF_ERR_OOM, "device allocation failed (out)");
+    dnet = (double*)ctx->onet.p;
+  }
   const size_t stride = wf->model == 0 ? gwf::setup_stride_m0() : (wf->model == 1 ? gwf::setup_stride_m1() : gwf::setup_stride_m2());
   const size_t chunk = (size_t)(N < gwf::kChunk ? N : gwf::kChunk);
   if (ctx->setup.ensure(chunk * stride)) return fail(GWF_ERR_OOM, "device allocation failed (set-up scratch)");
@@ -232,7 +290,7 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
   a.qnm = ctx->d_qnm;
   a.nq = ctx->nq;
   a.per_arm = per_arm;
-  a.precision = precision;
+  a.precision = precision == GWF_PREC_FP64 ? GWF_PREC_FP64 : GWF_PREC_FP32;
   a.stream = st;
   int slot = 0;
   for (int i = 0; i < n_det; ++i) {
@@ -246,6 +304,10 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
     else err = wf->model == 0 ? gwf::launch_snr_m0(a) : (wf->model == 1 ? gwf::launch_snr_m1(a) : gwf::launch_snr_m2(a));
     if (err != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(err));
     slot += r.desc.shape == GWF_SHAPE_T ? 3 : 1;
+  }
+  if (precision == GWF_PREC_MIXED) {
+    rc = refine(ctx, n_det, det_ids, a, dp, dld, dres, N, slots, darm, dnet, st);
+    if (rc) return rc;
   }
   GWF_CK(cudaEventRecord(ctx->scratch_free, st));
   if (mem == GWF_MEM_HOST) {
@@ -295,6 +357,8 @@ int gwf_ctx_destroy(gwf_ctx* ctx) {
   cudaFree(ctx->d_qnm);
   ctx->par.release(); ctx->res.release(); ctx->oarm.release(); ctx->onet.release();
   ctx->fin.release(); ctx->fout.release(); ctx->feps.release(); ctx->fcond.release(); ctx->setup.release();
+  ctx->mix_idx.release(); ctx->mix_cnt.release(); ctx->mix_par.release(); ctx->mix_res.release();
+  ctx->mix_net.release(); ctx->mix_arm.release();
   ctx->hpar.release(); ctx->hout.release();
   cudaEventDestroy(ctx->scratch_free);
   cudaStreamDestroy(ctx->stream);
@@ -383,6 +447,13 @@ int gwf_fisher(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* w
                int mem, double* out_arm, double* out_net, void* stream) {
   return run(ctx, true, n_det, det_ids, wf, params, ld, n_events, res, res_per_event, spacing, per_arm, precision, mem,
              out_arm, out_net, stream);
+}
+
+int gwf_set_refine_cond(gwf_ctx* ctx, double kappa) {
+  if (!ctx) return fail(GWF_ERR_INVALID_ARG, "null context");
+  if (!(kappa > 0.0)) return fail(GWF_ERR_INVALID_ARG, "refinement threshold must be positive");
+  ctx->refine_cond = kappa;
+  return GWF_OK;
 }
 
 int gwf_cov(gwf_ctx* ctx, const double* F, int64_t N, int mem, double* cov, double* eps, double* cond, void* stream) {

@@ -10,10 +10,11 @@
 //    by angle addition, so no large FP32 argument is ever reduced;
 //  - the PSD is read from an FP32 table normalised by its minimum;
 //  - the Gram matrix is accumulated exactly in fixed point: each sqrt(weight)-scaled FP32
-//    derivative vector is rounded to a 22-bit integer on a per-column power-of-two scale (the
-//    running maximum over the warp's tiles), products are formed as int32 x int32 -> int64 and
-//    summed without rounding; sums move to FP64 only when a column scale grows (by an exact
-//    shift) or every kFlushTiles tiles. Rounding each product or partial sum in FP32 instead
+//    derivative vector is rounded to an integer of at most 26 bits on a per-column power-of-two
+//    scale (the running maximum over the warp's tiles, so the largest values keep all their
+//    bits), products are formed as int32 x int32 -> int64 and summed without rounding; a growing
+//    column scale shifts the sums that involve it, and the sums move to FP64 every kFlushTiles
+//    tiles. Rounding each product or partial sum in FP32 instead
 //    adds errors that are not a perturbation of the vectors; with equilibrated condition
 //    numbers of 1e8-1e11 (typical for 11-parameter BBH Fishers) that makes the matrix
 //    indefinite.
@@ -36,11 +37,12 @@ struct ProjF {
   float Rc, cdcl, sdsl, sdcl, cdsl;
   float sU0, cU0;   // sin, cos of (lon - ra + 2 pi tcoal), formed in FP64
   float idL, sz;
+  float dcs, sgn;   // (1 - |cos i|)^2 / 2 and the sign of cos i (psi column, see point_f32)
 };
 
 struct TimeF { float D, D_th, D_ph, D_t, sx, cx; };
 struct ArmF { float Fp, Fc, Fp_x, Fc_x, Fp_d, Fc_d, Fp_s, Fc_s; };
-struct GridF { float lnfmin, delta, fac_w, w0, wl, fmin, fcut, df; int R; };
+struct GridF { float lnfmin, delta, fac_w, w0, wl, fmin, fcut, df, acc_l0, acc_idl; int R; };
 
 __device__ inline void projf_setup(ProjF& q, const ProjEv& p, double sz) {
   q.c2p = (float)p.c2p; q.s2p = (float)p.s2p; q.cp = (float)p.cp; q.ci = (float)p.ci;
@@ -58,6 +60,9 @@ __device__ inline void projf_setup(ProjF& q, const ProjEv& p, double sz) {
   q.sU0 = (float)s; q.cU0 = (float)c;
   q.idL = (float)(1.0 / p.dL);
   q.sz = (float)sz;
+  const double ac = 1.0 - fabs(p.ci);
+  q.dcs = (float)(0.5 * ac * ac);
+  q.sgn = p.ci >= 0.0 ? 1.0f : -1.0f;
 }
 
 // delay and sin/cos x at t_noloc = tcoal + delta (days); x = ra - lon - 2 pi t (gwfast/signal.py:401-423)
@@ -134,11 +139,11 @@ __device__ __forceinline__ void arm_derivs_f(const ProjF& q, const ArmF& ap, con
 
 // np.interp on the FP32 table normalised by its minimum; outside the table the reference PSD of 1
 // gives weights ~1e-46 of in-band ones, represented here as exactly zero.
-__device__ __forceinline__ float psd_at_f(const DetDev& d, float f, float lnf) {
+__device__ __forceinline__ float psd_at_f(const DetDev& d, float f, float lnf, float acc_l0, float acc_idl) {
   const float* xf = d.psd_f32;
   const int n = d.npsd;
   if (!(f >= xf[0]) || f > xf[n - 1]) return INFINITY;
-  int b = (int)((lnf - (float)d.acc_l0) * (float)d.acc_idl);
+  int b = (int)((lnf - acc_l0) * acc_idl);
   b = b < 0 ? 0 : (b >= d.nacc ? d.nacc - 1 : b);
   int j = d.acc[b];
   while (j > 0 && xf[j] > f) --j;
@@ -179,45 +184,59 @@ __device__ inline void pbf_load(const PhaseBasis* src, PBF& b) {
   }
 }
 
+// compensated sum of NB basis terms: each product hi * basis is split exactly into p + e (FMA), p
+// is added to the running sum with an exact two-sum, and every rounding error goes to the low-order
+// sum. The terms cancel strongly (the result can be far smaller than the largest term), so a plain
+// FP32 sum would carry an error of an ulp of the largest partial sum.
+template <int NB>
+__device__ __forceinline__ void phase_terms(const PBF& b, int off, const float (&bas)[NB], float* sh, float* sl) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    float h_ = 0.0f, l_ = 0.0f;
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+      const float h = b.hi[off + j][q];
+      const float p = h * bas[j];
+      const float e = fmaf(h, bas[j], -p);
+      const float t = h_ + p, bp = t - h_;
+      l_ += ((h_ - (t - bp)) + (p - bp)) + e;
+      h_ = t;
+      l_ = fmaf(b.lo[off + j][q], bas[j], l_);
+    }
+    sh[q] = h_;
+    sl[q] = l_;
+  }
+}
+
 // d Phi / d(Mc, eta, chi1z, chi2z) at frequency f from the basis (see PhaseBasis)
 __device__ __forceinline__ void phase_tangent_f(const PBF& b, float f, float lnf, float* dphi) {
   const float x = b.mg * f;
-  float bas[13];
-  int off, nb;
-  float datn = 0.0f;
+  float sh[4], sl[4];
   if (x < (float)kPhiFJoin) {
     const float f13 = cbrtf(f);
     const float i13 = 1.0f / f13;
     const float i23 = i13 * i13;
-    bas[0] = i23 * i23 * i13; bas[1] = 1.0f / f; bas[2] = i23; bas[3] = i13;
-    bas[4] = 1.0f; bas[5] = lnf; bas[6] = f13; bas[7] = f13 * lnf; bas[8] = f13 * f13;
-    bas[9] = f; bas[10] = f * f13; bas[11] = f * f13 * f13; bas[12] = f * f;
-    off = 0; nb = 13;
+    const float bas[13] = {i23 * i23 * i13, 1.0f / f, i23, i13, 1.0f, lnf, f13, f13 * lnf, f13 * f13,
+                           f, f * f13, f * f13 * f13, f * f};
+    phase_terms<13>(b, 0, bas, sh, sl);
   } else if (x < b.fmrd) {
     const float inv = 1.0f / f;
-    bas[0] = f; bas[1] = inv * inv * inv; bas[2] = lnf; bas[3] = 1.0f;
-    off = 13; nb = 4;
+    const float bas[4] = {f, inv * inv * inv, lnf, 1.0f};
+    phase_terms<4>(b, 13, bas, sh, sl);
   } else if (x < (float)kMfCut) {
     const float u = b.u1 * f - b.u0;
-    datn = 1.0f / (1.0f + u * u);
+    const float datn = 1.0f / (1.0f + u * u);
     const float f14 = sqrtf(sqrtf(f));
-    bas[0] = 1.0f / f; bas[1] = f14 * f14 * f14; bas[2] = f; bas[3] = 1.0f; bas[4] = atanf(u);
-    off = 17; nb = 5;
+    const float bas[5] = {1.0f / f, f14 * f14 * f14, f, 1.0f, atanf(u)};
+    phase_terms<5>(b, 17, bas, sh, sl);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) sl[q] = fmaf(b.k4 * datn, fmaf(b.du1[q], f, -b.du0[q]), sl[q]);
   } else {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) dphi[q] = 0.0f;
-    return;
+    for (int q = 0; q < 4; ++q) { sh[q] = 0.0f; sl[q] = 0.0f; }
   }
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    float sh = 0.0f, sl = 0.0f;
-    for (int j = 0; j < nb; ++j) {
-      sh = fmaf(b.hi[off + j][q], bas[j], sh);
-      sl = fmaf(b.lo[off + j][q], bas[j], sl);
-    }
-    if (off == 17) sl = fmaf(b.k4 * datn, fmaf(b.du1[q], f, -b.du0[q]), sl);
-    dphi[q] = sh + sl;
-  }
+  for (int q = 0; q < 4; ++q) dphi[q] = sh[q] + sl[q];
 }
 
 // round a struct of FP64 duals to its FP32 twin, all threads of the block; the dual at `amp_member`
@@ -234,18 +253,76 @@ __device__ inline void round_struct_par(const SRC& s, DST& d, const D4* amp_memb
   __syncthreads();
 }
 
+// derivative vectors d h / d theta (11 parameters, every arm) at one frequency point, FP32 form;
+// the amplitude prefactor is divided out (restored with the Gram scale).
+// The psi slot holds Delta = dh/dpsi - 2 s dh/dPhicoal (s = sign cos i) instead of dh/dpsi: with
+// hp = cp A, hx = i ci A, dh/dpsi = 2A (cp Fx - i ci F+) and dh/dPhicoal = A (ci Fx - i cp F+), so
+// Delta = 2 A (cp - s ci)(Fx + i s F+), where cp - s ci = (1 - |cos i|)^2 / 2. Near face-on and
+// face-off dh/dpsi is almost exactly 2 s dh/dPhicoal; forming the small difference directly keeps
+// its FP32 relative accuracy (the Gram of the original columns is restored in FP64 at the end).
+template <int MODEL, bool EARTH, int NARM>
+__device__ __forceinline__ void point_f32(const EvUnionF& EF, const PBF& pbf, const ProjF& pf, const ArmF* apc,
+                                          const TimeF& tsc, float f, float lnf, cf (&D)[NARM][NP]) {
+  DF4 A;
+  float dphi[4];
+  float dtn[4] = {0.f, 0.f, 0.f, 0.f};
+  TimeF ts;
+  phase_tangent_f(pbf, f, lnf, dphi);
+  if (MODEL == 0) {
+    const float f13 = cbrtf(f);
+    A = EF.tf2.ampK * (1.0f / (f * sqrtf(f13)));
+    if (EARTH) {
+      const DF4 tau = tau_star_point<DF4>(EF.tf2.Ms, EF.tf2.vM, EF.tf2.eta, f13);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dtn[q] = -tau.d[q] * (1.0f / 86400.0f);
+      time_f(pf, -tau.v * (1.0f / 86400.0f), ts);
+    }
+  } else {
+    A = phd_amp_point<DF4>(EF.phd, f);
+    if (EARTH) {
+      const DF4 tau = tau_star_point<DF4>(EF.phd.Ms, EF.phd.vM, EF.phd.eta, cbrtf(f));
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dtn[q] = -tau.d[q] * (1.0f / 86400.0f);
+      time_f(pf, -tau.v * (1.0f / 86400.0f), ts);
+    }
+  }
+  if (!EARTH) ts = tsc;
+  const cf P = {pf.cp * A.v, 0.0f}, C = {pf.ci * A.v, 0.0f};
+  cf dP[4], dC[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const cf dW = {A.d[q], -A.v * dphi[q]};
+    dP[q] = fscale(dW, pf.cp);
+    dC[q] = fscale(dW, pf.ci);
+  }
+  const cf dPi = {pf.dcp * A.v, 0.0f}, dCi = {pf.dci * A.v, 0.0f};
+#pragma unroll
+  for (int a = 0; a < NARM; ++a) {
+    ArmF ap;
+    if (EARTH) arm_f(pf, ts, a, ap);
+    else ap = apc[a];
+    arm_derivs_f(pf, ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D[a]);
+    const float k = 2.0f * A.v * pf.dcs;
+    D[a][I_PS] = {k * ap.Fc, k * pf.sgn * ap.Fp};
+  }
+}
+
 // 2x3 register blocks covering the upper triangle of the padded 12x12 Gram matrix
 static __constant__ unsigned char kBlkR[16] = {0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2, 3, 3, 4, 4, 5};
 static __constant__ unsigned char kBlkC[16] = {0, 1, 2, 3, 0, 1, 2, 3, 1, 2, 3, 2, 3, 2, 3, 3};
 
 // fixed-point Gram accumulation
-constexpr int kQBits = 22;                    // quantised |value| <= 2^22
-constexpr int kQMinExp = -100;                // floor of the running column exponents
-constexpr float kRoundMagic = 12582912.0f;    // 1.5 * 2^23: fmaf(x, s, magic) = magic + rint(x s) for |x s| < 2^22
-constexpr int kRoundMagicBits = 0x4B400000;   // bit pattern of kRoundMagic
-constexpr int kFlushTiles = 4096;             // 4096 tiles x 2^50 per tile < 2^63
+constexpr int kQBits = 25;        // quantised |value| <= 2^25: the largest values of a column keep all 24 FP32 bits
+constexpr int kQMinExp = -100;    // floor of the running column exponents
+constexpr int kFlushTiles = 64;   // per tile |sum| <= 32 x 2 x 2^50 = 2^56, so 64 tiles stay below 2^62
 
-// add the integer sums (at scale 2^-(M_r + M_c - 2 (kQBits - 1))) to the FP64 Gram of this warp
+// Gram slots per warp: one per Gram set, or, for a single set, one per half-warp (the two halves
+// of a warp split each tile's points between them)
+template <int NG>
+__host__ __device__ constexpr int gram_slots() { return NG == 1 ? 2 : NG; }
+
+// add the integer sums (at scale 2^-(M_r + M_c - 2 (kQBits - 1))) to the FP64 Gram of this warp;
+// every (slot, entry) has exactly one owning lane
 template <int NG, int NQ, int BPL, int NB>
 __device__ __forceinline__ void flush_fixed(long long (&acc)[BPL][6], const int* M, double* fl, int lane) {
 #pragma unroll
@@ -253,14 +330,15 @@ __device__ __forceinline__ void flush_fixed(long long (&acc)[BPL][6], const int*
     const int bl = (NG == 1 ? (lane & 15) : lane + 32 * i);
     if (bl < NB) {
       const int gs = bl >> 4, bi = bl & 15;
+      const int slot = NG == 1 ? (lane >> 4) : gs;
       const int r0 = 2 * kBlkR[bi], c0 = 3 * kBlkC[bi];
       const int* m = M + gs * NQ;
 #pragma unroll
       for (int e = 0; e < 6; ++e) {
         const int r = r0 + e / 3, c = c0 + e % 3;
-        // exact power of two: the exponent lies in [2 kQMinExp - 42, 254 - 42], inside the normal range
+        // exact power of two: the exponent lies in [2 kQMinExp - 48, 254 - 48], inside the normal range
         const double p2 = __longlong_as_double((long long)(1023 + m[r] + m[c] - 2 * (kQBits - 1)) << 52);
-        atomicAdd(&fl[(gs * NQ + r) * NQ + c], (double)acc[i][e] * p2);
+        fl[(slot * NQ + r) * NQ + c] += (double)acc[i][e] * p2;
         acc[i][e] = 0ll;
       }
     }
@@ -274,8 +352,9 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
   extern __shared__ __align__(16) unsigned char stage_raw[];
   int2* stage = reinterpret_cast<int2*>(stage_raw);   // [warp][NG][NQ][32] quantised (re, im)
   __shared__ int colM[2][kWarps][NG * NQ];             // running column exponents, double-buffered
-  __shared__ double fl[kWarps][NG][NQ][NQ];            // FP64 Gram per warp and set
+  __shared__ double fl[kWarps][gram_slots<NG>()][NQ][NQ];  // FP64 Gram per warp and slot
   __shared__ int badw[kWarps];
+  __shared__ double gsum[NG][NP][NP];                  // Gram per set, summed over warps
   __shared__ EvUnion E;
   __shared__ EvUnionF EF;
   __shared__ ProjEv pj;
@@ -302,6 +381,7 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
     projf_setup(pf, pj, det.sin_zeta);
     gf.lnfmin = (float)g.lnfmin; gf.delta = (float)g.delta; gf.fac_w = (float)g.fac_w; gf.w0 = (float)g.w0;
     gf.wl = (float)g.wl; gf.fmin = (float)g.fmin; gf.fcut = (float)g.fcut; gf.df = (float)g.df; gf.R = g.ok ? g.R : 0;
+    gf.acc_l0 = (float)det.acc_l0; gf.acc_idl = (float)det.acc_idl;
     if (!EARTH) {
       time_f(pf, 0.0f, tsc);
       for (int a = 0; a < NARM; ++a) arm_f(pf, tsc, a, apc[a]);
@@ -319,9 +399,10 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
   // zero padding row (parameter 11) once; running column exponents start below any value
   for (int gs = 0; gs < NG; ++gs) my[(gs * NQ + 11) * 32 + lane] = make_int2(0, 0);
   for (int i = lane; i < 2 * NG * NQ; i += 32) (&colM[i / (NG * NQ)][warp][0])[i % (NG * NQ)] = kQMinExp;
-  for (int i = lane; i < NG * NQ * NQ; i += 32) (&fl[warp][0][0][0])[i] = 0.0;
+  for (int i = lane; i < gram_slots<NG>() * NQ * NQ; i += 32) (&fl[warp][0][0][0])[i] = 0.0;
   if (lane == 0) badw[warp] = 0;
   int par = 0, tiles = 0;
+  float anc_f = 0.0f, anc_l = 0.0f;
   bool moved = false, bad = false;
   __syncwarp();
   const int R = gf.R;
@@ -329,17 +410,20 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
     const int k = base + tid;
     cf D[NARM][NP];
     float sw = 0.0f;
-    // geometric grid: f_k = f_tile * exp(lane * delta), with the tile's first frequency formed in FP64
-    float ftile = 0.0f;
-    if (ev.spacing == 0) {
-      double ft = 0.0;
-      if (lane == 0) ft = exp(g.lnfmin + (double)(base + warp * 32) * g.delta);
-      ftile = (float)__shfl_sync(0xffffffffu, ft, 0);
+    // geometric grid: f_k = f_tile * exp(lane * delta), ln f_k = ln f_tile + lane * delta, with the
+    // tile anchors formed in FP64: each lane computes the anchor of one of the warp's next 32 tiles
+    const int it = base / kThreads;
+    if (ev.spacing == 0 && (it & 31) == 0) {
+      const double l = g.lnfmin + (double)(((long long)(it + lane) * kWarps + warp) * 32) * g.delta;
+      anc_f = (float)exp(l);
+      anc_l = (float)l;
     }
+    const float ftile = __shfl_sync(0xffffffffu, anc_f, it & 31);
+    const float ltile = __shfl_sync(0xffffffffu, anc_l, it & 31);
     if (k < R) {
       float f, lnf, w;
       if (ev.spacing == 0) {
-        lnf = (float)(g.lnfmin + (double)k * g.delta);
+        lnf = fmaf((float)lane, gf.delta, ltile);
         if (k == R - 1) { f = gf.fcut; w = f * gf.wl; }
         else if (k == 0) { f = gf.fmin; w = f * gf.w0; }
         else { f = ftile * expf((float)lane * gf.delta); w = f * gf.fac_w; }
@@ -348,55 +432,16 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
         lnf = logf(f);
         w = (k == 0 || k == R - 1) ? 0.5f * gf.df : gf.df;
       }
-      const float S = psd_at_f(det, f, lnf);
+      const float S = psd_at_f(det, f, lnf, gf.acc_l0, gf.acc_idl);
       sw = sqrtf(4.0f * w / S);
-      DF4 A;
-      float dphi[4];
-      float dtn[4] = {0.f, 0.f, 0.f, 0.f};
-      TimeF ts;
-      phase_tangent_f(pbf, f, lnf, dphi);
-      if (MODEL == 0) {
-        const float f13 = cbrtf(f);
-        A = EF.tf2.ampK * (1.0f / (f * sqrtf(f13)));
-        if (EARTH) {
-          const DF4 tau = tau_star_point<DF4>(EF.tf2.Ms, EF.tf2.vM, EF.tf2.eta, f13);
-#pragma unroll
-          for (int q = 0; q < 4; ++q) dtn[q] = -tau.d[q] * (1.0f / 86400.0f);
-          time_f(pf, -tau.v * (1.0f / 86400.0f), ts);
-        }
-      } else {
-        A = phd_amp_point<DF4>(EF.phd, f);
-        if (EARTH) {
-          const DF4 tau = tau_star_point<DF4>(EF.phd.Ms, EF.phd.vM, EF.phd.eta, cbrtf(f));
-#pragma unroll
-          for (int q = 0; q < 4; ++q) dtn[q] = -tau.d[q] * (1.0f / 86400.0f);
-          time_f(pf, -tau.v * (1.0f / 86400.0f), ts);
-        }
-      }
-      if (!EARTH) ts = tsc;
-      const cf P = {pf.cp * A.v, 0.0f}, C = {pf.ci * A.v, 0.0f};
-      cf dP[4], dC[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const cf dW = {A.d[q], -A.v * dphi[q]};
-        dP[q] = fscale(dW, pf.cp);
-        dC[q] = fscale(dW, pf.ci);
-      }
-      const cf dPi = {pf.dcp * A.v, 0.0f}, dCi = {pf.dci * A.v, 0.0f};
-#pragma unroll
-      for (int a = 0; a < NARM; ++a) {
-        ArmF ap;
-        if (EARTH) arm_f(pf, ts, a, ap);
-        else ap = apc[a];
-        arm_derivs_f(pf, ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D[a]);
-      }
+      point_f32<MODEL, EARTH, NARM>(EF, pbf, pf, apc, tsc, f, lnf, D);
     } else {
 #pragma unroll
       for (int a = 0; a < NARM; ++a)
 #pragma unroll
         for (int q = 0; q < NP; ++q) D[a][q] = {0.0f, 0.0f};
     }
-    // Quantise the sqrt(weight)-scaled derivative vectors to integers, |q| < 2^(kQBits-1+1),
+    // Quantise the sqrt(weight)-scaled derivative vectors to integers, |q| <= 2^kQBits,
     // on a per-column power-of-two scale that follows the largest magnitude this warp has seen.
     // The rounding is a perturbation of the vectors themselves, so the accumulated Gram matrix
     // stays an exact Gram matrix of slightly perturbed vectors (positive semidefinite).
@@ -418,9 +463,9 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
         const int mnew = min(max(mold, e), 127);
         moved |= mnew != mold;
         if (lane == 0) Mn[gs * NQ + q] = mnew;
-        const float s = __int_as_float((127 + kQBits - 1 - mnew) << 23);   // 2^(kQBits-1-mnew)
-        const int qr = __float_as_int(fmaf(u.re, s, kRoundMagic)) - kRoundMagicBits;
-        const int qi = __float_as_int(fmaf(u.im, s, kRoundMagic)) - kRoundMagicBits;
+        const float s = __int_as_float((127 + kQBits - 1 - mnew) << 23);   // 2^(kQBits-1-mnew), exact scaling
+        const int qr = __float2int_rn(u.re * s);
+        const int qi = __float2int_rn(u.im * s);
         my[(gs * NQ + q) * 32 + lane] = make_int2(qr, qi);
       }
     __syncwarp();
@@ -468,21 +513,38 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
   flush_fixed<NG, NQ, BPL, NB>(acc, &colM[par][warp][0], &fl[warp][0][0][0], lane);
   if (lane == 0 && bad) badw[warp] = 1;
   __syncthreads();
-  // sum over warps in FP64
-  const double* red = &fl[0][0][0][0];  // [kWarps][NG][NQ][NQ]
+  // sum over warps in FP64, per Gram set
+  const double* red = &fl[0][0][0][0];  // [kWarps][gram_slots][NQ][NQ]
+  constexpr int NS = gram_slots<NG>();
+  for (int e = tid; e < NG * NE; e += kThreads) {
+    const int gs = e / NE, a = kPairA[e % NE], b = kPairB[e % NE];
+    double v = 0.0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+      v += red[((size_t)(w * NS + gs) * NQ + a) * NQ + b];
+      if (NG == 1) v += red[((size_t)(w * NS + 1) * NQ + a) * NQ + b];
+    }
+    gsum[gs][a][b] = v;
+    gsum[gs][b][a] = v;
+  }
+  __syncthreads();
   const long long N = ev.N;
   int anybad = 0;
 #pragma unroll
   for (int w = 0; w < kWarps; ++w) anybad |= badw[w];
   const double sc = anybad ? __longlong_as_double(0x7ff8000000000000ll) : scale;
+  // back to the psi column: dh/dpsi = Delta + 2 s dh/dPhicoal
+  const double s2 = 2.0 * (double)pf.sgn;
   for (int e = tid; e < NE; e += kThreads) {
     const int a = kPairA[e], b = kPairB[e];
     double sdet = 0.0;
 #pragma unroll
     for (int gs = 0; gs < NG; ++gs) {
-      double v = 0.0;
-#pragma unroll
-      for (int w = 0; w < kWarps; ++w) v += red[((size_t)(w * NG + gs) * NQ + a) * NQ + b];
+      const double (*G)[NP] = gsum[gs];
+      double v = G[a][b];
+      if (a == I_PS && b == I_PS) v += 2.0 * s2 * G[I_PS][I_PC] + s2 * s2 * G[I_PC][I_PC];
+      else if (a == I_PS) v += s2 * G[I_PC][b];
+      else if (b == I_PS) v += s2 * G[a][I_PC];
       v *= sc;
       sdet += v;
       if (out_arm && (NG == 1 || NG == 3)) {

@@ -18,7 +18,7 @@ struct LaunchArgs {
   double* out_det;
   int accum;
   int per_arm;
-  int precision;  // 0 = FP64, 1 = FP32 split precision (22-mode models)
+  int precision;  // 0 = FP64, 1 = FP32 split precision (22-mode models); the launchers see no other value
   unsigned char* scratch;  // kChunk x setup_stride(model) bytes
   cudaStream_t stream;
 };
@@ -33,5 +33,11 @@ size_t setup_stride_m0();
 size_t setup_stride_m1();
 size_t setup_stride_m2();
 cudaError_t launch_cov(const double* F, long long N, double* cov, double* eps, double* cond, cudaStream_t st);
+// mixed precision (gwf_mixed.cu)
+cudaError_t launch_select(const double* cond, long long N, double thresh, long long* idx, unsigned long long* count,
+                          cudaStream_t st);
+cudaError_t launch_gather(const double* p, long long ld, const int* res, const long long* idx, long long M, double* out,
+                          int* res_out, cudaStream_t st);
+cudaError_t launch_scatter(const double* src, const long long* idx, long long M, int per, double* dst, cudaStream_t st);
 
 }  // namespace gwf

@@ -54,17 +54,22 @@ def snr_batch(signals, evParams, res=1000, device=0):
     return res_l
 
 
-def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', device=0, precision='fp64'):
+def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', device=0, precision='fp64',
+                 refine_cond=None):
     """Fisher matrices of all signals in one library call.
 
     per_arm: list (per signal) of (arms, N, 11, 11); otherwise the network total (N, 11, 11).
-    precision: 'fp64' (the drop-in) or 'fp32' (split precision, TaylorF2 and IMRPhenomD).
+    precision: 'fp64' (the drop-in), 'fp32' (split precision, TaylorF2 and IMRPhenomD), or
+    'mixed' ('fp32', then FP64 for the events whose network Fisher has an equilibrated condition
+    number above refine_cond, default 3e11).
     """
     p = _prep(evParams)
     wf = signals[0].wf_model
     N = p.shape[1]
     slots = _arm_slots(signals)
     ctx = _lib.context(device)
+    if precision == 'mixed':
+        ctx.set_refine_cond(3e11 if refine_cond is None else refine_cond)
     sp = 0 if spacing == 'geom' else 1
     duty = any(s.DutyFactor is not None for s in signals)
     if per_arm or duty:
@@ -183,14 +188,15 @@ class GWSignal:
                    return_derivatives=False, return_SNR_derivatives=False, precision='fp64', **kwargs):
         """gwfast/signal.py:782-1098; returns (11, 11, N), or a list per arm with return_all.
 
-        precision='fp32' selects the split-precision kernel (TaylorF2 and IMRPhenomD)."""
+        precision='fp32' selects the split-precision kernel (TaylorF2 and IMRPhenomD), 'mixed' the
+        split-precision kernel with FP64 recomputation of ill-conditioned events (refine_cond)."""
         if return_derivatives or return_SNR_derivatives:
             raise NotImplementedError('return_derivatives / return_SNR_derivatives are not implemented on the GPU path')
         if computeDerivFinDiff:
             raise NotImplementedError('finite-difference derivatives are not used on the GPU path')
         res = self._resolve_res(evParams, res, df)
         Fa = fisher_batch([self], evParams, res, per_arm=True, spacing=spacing, device=self.device,
-                          precision=precision)[0]
+                          precision=precision, refine_cond=kwargs.get('refine_cond'))[0]
         Fa = reparametrise(Fa, evParams, use_m1m2, use_chi1chi2)
         arms = [np.moveaxis(F, 0, -1) for F in Fa]
         if return_all:

@@ -47,7 +47,7 @@ enum { GWF_WF_TAYLORF2 = 0, GWF_WF_PHENOMD = 1, GWF_WF_PHENOMHM = 2 };
 enum { GWF_SHAPE_L = 0, GWF_SHAPE_T = 1 };
 enum { GWF_SPACING_GEOM = 0, GWF_SPACING_LIN = 1 };
 enum { GWF_MEM_HOST = 0, GWF_MEM_DEVICE = 1 };
-enum { GWF_PREC_FP64 = 0, GWF_PREC_FP32 = 1 };
+enum { GWF_PREC_FP64 = 0, GWF_PREC_FP32 = 1, GWF_PREC_MIXED = 2 };
 
 typedef struct gwf_ctx gwf_ctx;
 
@@ -100,10 +100,18 @@ int gwf_snr(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, 
  * per_arm != 0: out_arm receives [slots][N][11][11] per arm (return_all=True);
  * out_net (may be NULL): [N][11][11] network total.
  * precision: GWF_PREC_FP64 (the drop-in) or GWF_PREC_FP32 (split precision: per-event set-up in
- * FP64, per-point arithmetic in FP32, outputs in FP64; TaylorF2 and IMRPhenomD only). */
+ * FP64, per-point arithmetic in FP32, outputs in FP64; TaylorF2 and IMRPhenomD only), or
+ * GWF_PREC_MIXED: GWF_PREC_FP32 for all events, then the events whose network Fisher has an
+ * equilibrated condition number above the context's threshold (gwf_set_refine_cond, default
+ * 3e11) or a non-finite one are recomputed in FP64 (all outputs). With mem = GWF_MEM_DEVICE,
+ * GWF_PREC_MIXED waits on the stream once, to read how many events need FP64. */
 int gwf_fisher(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params, int64_t ld,
                int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int per_arm, int precision,
                int mem, double* out_arm, double* out_net, void* stream);
+
+/* Condition-number threshold of GWF_PREC_MIXED (no counterpart in gwfast: a property of the
+ * reduced-precision form). kappa > 0; events with equilibrated condition number above it get FP64. */
+int gwf_set_refine_cond(gwf_ctx* ctx, double kappa);
 
 /* Covariance by equilibrated Cholesky inversion, FP64, one 11x11 matrix per event.
  * Replaces fisherTools.CovMatr 'cho' path (gwfast/fisherTools.py:32-196) together with

@@ -70,3 +70,30 @@ def test_fp32_rejected_for_hm(gpu_lib):
     net = synthetic.make_network(W.IMRPhenomHM(), dets=(('L1', 10.),), earth=False)
     with pytest.raises(_lib.GWFError):
         net.FisherMatr(dict(ev), res=100, precision='fp32')
+
+
+def test_phenomd_network_mixed(gpu_lib):
+    """FP32 form plus FP64 for events above the condition-number threshold: sigma within 1e-3."""
+    ev = synthetic.bbh_events(512, seed=1001)
+    net = synthetic.make_network(W.IMRPhenomD(), earth=True)
+    F64 = np.moveaxis(net.FisherMatr(dict(ev), res=2000), -1, 0)
+    Fm = np.moveaxis(net.FisherMatr(dict(ev), res=2000, precision="mixed", refine_cond=3e11), -1, 0)
+    se, cond = sigma_err(Fm, F64)
+    worst = se.max(axis=1)
+    exact = np.all(Fm == F64, axis=(1, 2))
+    print('PhenomD mixed: FP64 events %.3f, cond of those >= %.2e; sigma err median %.2e max %.2e; frac<=1e-3 %.4f'
+          % (exact.mean(), cond[exact].min() if exact.any() else np.nan, np.median(worst), worst.max(),
+             np.mean(worst <= 1e-3)))
+    assert np.all(cond[~exact] <= 3.03e11)     # every event above the threshold went to FP64
+    assert np.mean(worst <= 1e-3) >= 0.998
+
+
+def test_mixed_all_refined_is_fp64(gpu_lib):
+    """With a threshold below every condition number, the mixed form returns the FP64 matrices
+    bit for bit (gather, FP64 recomputation and scatter of every event), per arm as well."""
+    ev = synthetic.bbh_events(200, seed=5)
+    net = synthetic.make_network(W.IMRPhenomD(), earth=True)
+    F64 = net.FisherMatr(dict(ev), res=1000, return_all=True)
+    Fm = net.FisherMatr(dict(ev), res=1000, return_all=True, precision='mixed', refine_cond=1.0)
+    for k in F64:
+        assert np.array_equal(Fm[k], F64[k]), k
