@@ -88,7 +88,7 @@ struct gwf_ctx {
   int nq = 0;
   DevBuf par, res, oarm, onet, fin, fout, feps, fcond, setup;
   DevBuf mix_idx, mix_cnt, mix_par, mix_res, mix_net, mix_arm;  // FP64 recomputation of GWF_PREC_MIXED
-  double refine_cond = 3e11;
+  double refine_cond = 1e11;
   cudaEvent_t scratch_free = nullptr;  // recorded after the last launch that used the set-up scratch
   HostBuf hpar, hout;
 };
@@ -179,11 +179,11 @@ int stage_inputs(gwf_ctx* ctx, const double* params, int64_t ld, int64_t N, cons
 int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const double* dp, int64_t dld,
            const int* dres, int64_t N, int slots, double* darm, double* dnet, cudaStream_t st) {
   const size_t per = (size_t)gwf::NP * gwf::NP;
-  if (ctx->fout.ensure((size_t)N * per * sizeof(double)) || ctx->fcond.ensure((size_t)N * sizeof(double)) ||
-      ctx->mix_idx.ensure((size_t)N * sizeof(long long)) || ctx->mix_cnt.ensure(sizeof(unsigned long long)))
+  if (ctx->fcond.ensure((size_t)N * sizeof(double)) || ctx->mix_idx.ensure((size_t)N * sizeof(long long)) ||
+      ctx->mix_cnt.ensure(sizeof(unsigned long long)))
     return fail(GWF_ERR_OOM, "device allocation failed (mixed precision)");
   long long* idx = (long long*)ctx->mix_idx.p;
-  cudaError_t e = gwf::launch_cov(dnet, N, (double*)ctx->fout.p, nullptr, (double*)ctx->fcond.p, st);
+  cudaError_t e = gwf::launch_cond(dnet, N, (double*)ctx->fcond.p, st);
   if (e == cudaSuccess)
     e = gwf::launch_select((const double*)ctx->fcond.p, N, ctx->refine_cond, idx, (unsigned long long*)ctx->mix_cnt.p, st);
   unsigned long long M = 0;

@@ -34,6 +34,7 @@ size_t setup_stride_m1();
 size_t setup_stride_m2();
 cudaError_t launch_cov(const double* F, long long N, double* cov, double* eps, double* cond, cudaStream_t st);
 // mixed precision (gwf_mixed.cu)
+cudaError_t launch_cond(const double* F, long long N, double* cond, cudaStream_t st);
 cudaError_t launch_select(const double* cond, long long N, double thresh, long long* idx, unsigned long long* count,
                           cudaStream_t st);
 cudaError_t launch_gather(const double* p, long long ld, const int* res, const long long* idx, long long M, double* out,

@@ -2,12 +2,90 @@
 // whose FP32 network Fisher is ill-conditioned. These kernels pick those events, gather their
 // parameters into a compact batch and scatter the FP64 results back.
 #include <cuda_runtime.h>
+#include <math.h>
 
 #include "gwf_launch.h"
 
 namespace gwf {
 
 namespace {
+
+// Condition-number estimate of the diagonally equilibrated Fisher (the quantity fisherTools
+// reports), one thread per event: Cholesky factor, then power iteration for the largest
+// eigenvalue and inverse iteration (two triangular solves per step) for the smallest, each
+// closed by a Rayleigh quotient. Not positive definite -> infinity. Far cheaper than the Jacobi
+// eigen-decomposition of the covariance kernel; only used to pick events for FP64.
+__global__ void cond_kernel(const double* __restrict__ F, long long N, double* __restrict__ cond) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  constexpr int K = NP;
+  const double* f = F + n * K * K;
+  double w[K], L[K * K];
+  for (int i = 0; i < K; ++i) {
+    const double d = f[i * K + i];
+    if (!(d > 0.0)) { cond[n] = INFINITY; return; }
+    w[i] = 1.0 / sqrt(d);
+  }
+  // Cholesky of A = diag(w) F diag(w), lower triangle of L
+  for (int j = 0; j < K; ++j) {
+    double s = f[j * K + j] * w[j] * w[j];
+    for (int k = 0; k < j; ++k) s -= L[j * K + k] * L[j * K + k];
+    if (!(s > 0.0)) { cond[n] = INFINITY; return; }
+    const double ljj = sqrt(s);
+    L[j * K + j] = ljj;
+    for (int i = j + 1; i < K; ++i) {
+      double t = f[i * K + j] * w[i] * w[j];
+      for (int k = 0; k < j; ++k) t -= L[i * K + k] * L[j * K + k];
+      L[i * K + j] = t / ljj;
+    }
+  }
+  double x[K], y[K];
+  // largest eigenvalue: power iteration on A = L L^T
+  for (int i = 0; i < K; ++i) x[i] = 1.0 + 0.1 * i;
+  double lmax = 0.0;
+  for (int it = 0; it < 30; ++it) {
+    double nx = 0.0;
+    for (int i = 0; i < K; ++i) nx += x[i] * x[i];
+    nx = 1.0 / sqrt(nx);
+    for (int i = 0; i < K; ++i) x[i] *= nx;
+    for (int i = 0; i < K; ++i) {   // y = L^T x
+      double s = 0.0;
+      for (int k = i; k < K; ++k) s += L[k * K + i] * x[k];
+      y[i] = s;
+    }
+    double q = 0.0;
+    for (int i = 0; i < K; ++i) {   // x = L y, Rayleigh quotient |L^T x|^2
+      q += y[i] * y[i];
+      double s = 0.0;
+      for (int k = 0; k <= i; ++k) s += L[i * K + k] * y[k];
+      x[i] = s;
+    }
+    lmax = q;
+  }
+  // smallest eigenvalue: inverse iteration, x <- A^{-1} x by forward and back substitution
+  for (int i = 0; i < K; ++i) x[i] = (i & 1) ? -1.0 : 1.0 + 0.05 * i;
+  double lmin = INFINITY;
+  for (int it = 0; it < 16; ++it) {
+    double nx = 0.0;
+    for (int i = 0; i < K; ++i) nx += x[i] * x[i];
+    nx = 1.0 / sqrt(nx);
+    for (int i = 0; i < K; ++i) x[i] *= nx;
+    for (int i = 0; i < K; ++i) {   // L y = x
+      double s = x[i];
+      for (int k = 0; k < i; ++k) s -= L[i * K + k] * y[k];
+      y[i] = s / L[i * K + i];
+    }
+    double q = 0.0;                 // x^T A^{-1} x = |y|^2
+    for (int i = 0; i < K; ++i) q += y[i] * y[i];
+    for (int i = K - 1; i >= 0; --i) {   // L^T x = y
+      double s = y[i];
+      for (int k = i + 1; k < K; ++k) s -= L[k * K + i] * x[k];
+      x[i] = s / L[i * K + i];
+    }
+    lmin = 1.0 / q;
+  }
+  cond[n] = lmax / lmin;
+}
 
 // events with condition number above thresh (or not finite) -> idx[0..count)
 __global__ void select_kernel(const double* __restrict__ cond, long long N, double thresh, long long* __restrict__ idx,
@@ -42,6 +120,12 @@ __global__ void scatter_kernel(const double* __restrict__ src, const long long* 
 unsigned blocks(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 }  // namespace
+
+cudaError_t launch_cond(const double* F, long long N, double* cond, cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  cond_kernel<<<blocks(N, 64), 64, 0, st>>>(F, N, cond);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_select(const double* cond, long long N, double thresh, long long* idx, unsigned long long* count,
                           cudaStream_t st) {

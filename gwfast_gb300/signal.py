@@ -61,7 +61,7 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
     per_arm: list (per signal) of (arms, N, 11, 11); otherwise the network total (N, 11, 11).
     precision: 'fp64' (the drop-in), 'fp32' (split precision, TaylorF2 and IMRPhenomD), or
     'mixed' ('fp32', then FP64 for the events whose network Fisher has an equilibrated condition
-    number above refine_cond, default 3e11).
+    number above refine_cond, default 1e11).
     """
     p = _prep(evParams)
     wf = signals[0].wf_model
@@ -69,7 +69,7 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
     slots = _arm_slots(signals)
     ctx = _lib.context(device)
     if precision == 'mixed':
-        ctx.set_refine_cond(3e11 if refine_cond is None else refine_cond)
+        ctx.set_refine_cond(1e11 if refine_cond is None else refine_cond)
     sp = 0 if spacing == 'geom' else 1
     duty = any(s.DutyFactor is not None for s in signals)
     if per_arm or duty:
