@@ -269,7 +269,8 @@ def main():
     torch.cuda.synchronize()
     Fm_all = out.cpu().numpy()
     F64_all = out64.cpu().numpy()
-    refined = float(np.mean(np.all(Fm_all == F64_all, axis=(1, 2))))
+    dg = np.sqrt(np.abs(np.einsum('nii->ni', F64_all)))
+    refined = float(np.mean((np.abs(Fm_all - F64_all) / (dg[:, :, None] * dg[:, None, :])).max(axis=(1, 2)) < 1e-11))
     nchk = min(N, 4000)
     c64, _, cond = fisherTools.CovMatr(np.moveaxis(F64_all[:nchk], 0, -1), return_cond=True, device=local)
     s64 = np.sqrt(np.einsum('iin->ni', c64))

@@ -50,6 +50,9 @@ SIGNATURES = {
                     ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
     'gwf_cov': ([_vp, _vp, _i64, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     'gwf_set_refine_cond': ([_vp, _d], ctypes.c_int),
+    'gwf_set_segments': ([_vp, ctypes.c_int], ctypes.c_int),
+    'gwf_autotune_segments': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32, _vp, ctypes.c_int,
+                               ctypes.c_int, ctypes.c_int, _P(ctypes.c_int)], ctypes.c_int),
     'gwf_fisher_noalloc': ([_P(DetDesc), _vp, _vp, _i64, _P(WfDesc), _vp, _vp, _vp, _i64, _vp, _i64, _i64,
                             ctypes.c_int32, ctypes.c_int, _vp, _vp], ctypes.c_int),
 }
@@ -143,6 +146,21 @@ class Context:
         check(load().gwf_fisher(self.h, len(ids), ptr(ids), ctypes.byref(wf), ptr(params), ld, n, int(res),
                                 ptr(res_ev), spacing, int(bool(per_arm)), PRECISION[precision], mem, ptr(out_arm),
                                 ptr(out_net), stream))
+
+    def set_segments(self, points):
+        """0: one CTA per event; > 0: persistent launches over frequency segments of this many points."""
+        check(load().gwf_set_segments(self.h, int(points)))
+
+    def autotune_segments(self, det_ids, wf, params, res, res_ev=None, spacing=0, precision='fp64', mem=MEM_HOST,
+                          ld=None, n=None):
+        """Time the candidate segment lengths on this workload, keep and return the fastest."""
+        ids = np.ascontiguousarray(det_ids, dtype=np.int32)
+        n = params.shape[1] if n is None else n
+        ld = params.shape[1] if ld is None else ld
+        best = ctypes.c_int()
+        check(load().gwf_autotune_segments(self.h, len(ids), ptr(ids), ctypes.byref(wf), ptr(params), ld, n, int(res),
+                                           ptr(res_ev), spacing, PRECISION[precision], mem, ctypes.byref(best)))
+        return best.value
 
     def set_refine_cond(self, kappa):
         """Condition-number threshold above which the 'mixed' form recomputes an event in FP64."""

@@ -89,6 +89,9 @@ struct gwf_ctx {
   DevBuf par, res, oarm, onet, fin, fout, feps, fcond, setup;
   DevBuf mix_idx, mix_cnt, mix_par, mix_res, mix_net, mix_arm;  // FP64 recomputation of GWF_PREC_MIXED
   double refine_cond = 1e11;
+  int seg_points = 0;      // Fisher launches: 0 = one CTA per event, > 0 = persistent, segments of this many points
+  int refine_seg = 256;    // segment length of the FP64 recomputation of GWF_PREC_MIXED
+  DevBuf seg_off, seg_ctr, seg_part, seg_ovf, tune_out;
   cudaEvent_t scratch_free = nullptr;  // recorded after the last launch that used the set-up scratch
   HostBuf hpar, hout;
 };
@@ -174,6 +177,39 @@ int stage_inputs(gwf_ctx* ctx, const double* params, int64_t ld, int64_t N, cons
   return GWF_OK;
 }
 
+// largest per-event resolution of a call (bounds the number of segments per event)
+int max_res(int32_t res, const int32_t* res_ev, int64_t N, int mem, int64_t* out) {
+  if (!res_ev) { *out = res; return GWF_OK; }
+  int64_t m = 1;
+  if (mem == GWF_MEM_HOST) {
+    for (int64_t i = 0; i < N; ++i) m = res_ev[i] > m ? res_ev[i] : m;
+  } else {
+    std::vector<int32_t> h((size_t)N);
+    GWF_CK(cudaMemcpy(h.data(), res_ev, (size_t)N * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < N; ++i) m = h[i] > m ? h[i] : m;
+  }
+  *out = m;
+  return GWF_OK;
+}
+
+// buffers of the segmented launches for chunks of up to `chunk` events with at most rmax points
+int seg_setup(gwf_ctx* ctx, gwf::LaunchArgs& a, int seg, int64_t chunk, int64_t rmax, cudaStream_t st) {
+  const long long per_ev = (long long)((rmax + seg - 1) / seg);
+  const long long cap = (long long)chunk * (per_ev > 0 ? per_ev : 1);
+  if (ctx->seg_off.ensure((size_t)(gwf::kChunk + 1) * sizeof(long long)) ||
+      ctx->seg_ctr.ensure(sizeof(unsigned long long)) || ctx->seg_ovf.ensure(sizeof(int)) ||
+      ctx->seg_part.ensure((size_t)cap * 3 * gwf::NE * sizeof(double)))
+    return fail(GWF_ERR_OOM, "device allocation failed (segments)");
+  GWF_CK(cudaMemsetAsync(ctx->seg_ovf.p, 0, sizeof(int), st));
+  a.seg = seg;
+  a.seg_off = (long long*)ctx->seg_off.p;
+  a.seg_ctr = (unsigned long long*)ctx->seg_ctr.p;
+  a.seg_part = (double*)ctx->seg_part.p;
+  a.seg_cap = cap;
+  a.seg_ovf = (int*)ctx->seg_ovf.p;
+  return GWF_OK;
+}
+
 // GWF_PREC_MIXED, second stage: condition numbers of the FP32 network Fishers, then the FP64
 // Fisher of the events above the threshold, computed as a compact batch and scattered back
 int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const double* dp, int64_t dld,
@@ -205,6 +241,17 @@ int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const
   a.ev.N = (long long)M;
   a.ev.res_ev = cres;
   a.precision = GWF_PREC_FP64;
+  // few events: split each into frequency segments so that they fill the GPU
+  int64_t rmax = a.ev.res;
+  if (dres) {
+    int rc = max_res(a.ev.res, dres, N, GWF_MEM_DEVICE, &rmax);
+    if (rc) return rc;
+  }
+  {
+    const int64_t chunk = (int64_t)M < gwf::kChunk ? (int64_t)M : gwf::kChunk;
+    int rc = seg_setup(ctx, a, ctx->refine_seg, chunk, rmax, st);
+    if (rc) return rc;
+  }
   int slot = 0;
   for (int i = 0; i < n_det; ++i) {
     const DetRec& r = ctx->dets[det_ids[i]];
@@ -277,6 +324,13 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
   GWF_CK(cudaStreamWaitEvent(st, ctx->scratch_free, 0));
   gwf::LaunchArgs a;
   a.scratch = (unsigned char*)ctx->setup.p;
+  a.cap_events = (long long)chunk;
+  if (fisher && ctx->seg_points > 0) {
+    int64_t rmax = 0;
+    rc = max_res(res, res_ev, N, mem, &rmax);
+    if (!rc) rc = seg_setup(ctx, a, ctx->seg_points, (int64_t)chunk, rmax, st);
+    if (rc) return rc;
+  }
   a.ev.p = dp;
   a.ev.ld = dld;
   a.ev.N = N;
@@ -313,7 +367,11 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
   if (mem == GWF_MEM_HOST) {
     if (out_arm) GWF_CK(cudaMemcpyAsync(out_arm, darm, (size_t)slots * N * per * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (out_net) GWF_CK(cudaMemcpyAsync(out_net, dnet, (size_t)N * per * sizeof(double), cudaMemcpyDeviceToHost, st));
+    int ovf = 0;
+    if (fisher && (a.seg > 0 || precision == GWF_PREC_MIXED) && ctx->seg_ovf.p)
+      GWF_CK(cudaMemcpyAsync(&ovf, ctx->seg_ovf.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     GWF_CK(cudaStreamSynchronize(st));
+    if (ovf) return fail(GWF_ERR_CUDA, "segment buffer overflow (internal error)");
   }
   return GWF_OK;
 }
@@ -359,6 +417,8 @@ int gwf_ctx_destroy(gwf_ctx* ctx) {
   ctx->fin.release(); ctx->fout.release(); ctx->feps.release(); ctx->fcond.release(); ctx->setup.release();
   ctx->mix_idx.release(); ctx->mix_cnt.release(); ctx->mix_par.release(); ctx->mix_res.release();
   ctx->mix_net.release(); ctx->mix_arm.release();
+  ctx->seg_off.release(); ctx->seg_ctr.release(); ctx->seg_part.release(); ctx->seg_ovf.release();
+  ctx->tune_out.release();
   ctx->hpar.release(); ctx->hout.release();
   cudaEventDestroy(ctx->scratch_free);
   cudaStreamDestroy(ctx->stream);
@@ -454,6 +514,72 @@ int gwf_set_refine_cond(gwf_ctx* ctx, double kappa) {
   if (!(kappa > 0.0)) return fail(GWF_ERR_INVALID_ARG, "refinement threshold must be positive");
   ctx->refine_cond = kappa;
   return GWF_OK;
+}
+
+int gwf_set_segments(gwf_ctx* ctx, int points) {
+  if (!ctx) return fail(GWF_ERR_INVALID_ARG, "null context");
+  if (points < 0 || points % gwf::kThreads) return fail(GWF_ERR_INVALID_ARG, "segment length must be 0 or a multiple of 128");
+  ctx->seg_points = points;
+  return GWF_OK;
+}
+
+int gwf_autotune_segments(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params,
+                          int64_t ld, int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing,
+                          int precision, int mem, int* best) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  rc = validate_common(ctx, n_det, det_ids, wf, params, ld, n_events, res, res_per_event, spacing, mem);
+  if (rc) return rc;
+  if (n_events < 1) return fail(GWF_ERR_INVALID_ARG, "autotuning needs events");
+  cudaStream_t st = ctx->stream;
+  const double* dp;
+  int64_t dld;
+  const int* dres;
+  rc = stage_inputs(ctx, params, ld, n_events, res_per_event, mem, st, &dp, &dld, &dres);
+  if (rc) return rc;
+  // keep staged inputs: later runs reuse ctx->par / ctx->res, so copy them aside
+  DevBuf tp, tr;
+  if (mem == GWF_MEM_HOST) {
+    if (tp.ensure((size_t)gwf::NP * n_events * sizeof(double)) || (dres && tr.ensure((size_t)n_events * sizeof(int))))
+      return fail(GWF_ERR_OOM, "device allocation failed (autotune)");
+    GWF_CK(cudaMemcpyAsync(tp.p, dp, (size_t)gwf::NP * n_events * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    if (dres) GWF_CK(cudaMemcpyAsync(tr.p, dres, (size_t)n_events * sizeof(int), cudaMemcpyDeviceToDevice, st));
+    dp = (const double*)tp.p;
+    dres = dres ? (const int*)tr.p : nullptr;
+    dld = n_events;
+  }
+  if (ctx->tune_out.ensure((size_t)n_events * gwf::NP * gwf::NP * sizeof(double)))
+    return fail(GWF_ERR_OOM, "device allocation failed (autotune)");
+  const int cands[] = {0, 256, 512, 1024, 2048};
+  const int saved = ctx->seg_points;
+  cudaEvent_t e0, e1;
+  GWF_CK(cudaEventCreate(&e0));
+  GWF_CK(cudaEventCreate(&e1));
+  float best_ms = 1e30f;
+  int best_seg = saved;
+  for (int c : cands) {
+    ctx->seg_points = c;
+    float tot = 0.0f;
+    for (int rep = 0; rep < 3 && rc == GWF_OK; ++rep) {   // first run warms up
+      cudaEventRecord(e0, st);
+      rc = run(ctx, true, n_det, det_ids, wf, dp, dld, n_events, res, dres, spacing, 0, precision, GWF_MEM_DEVICE,
+               nullptr, (double*)ctx->tune_out.p, st);
+      cudaEventRecord(e1, st);
+      cudaEventSynchronize(e1);
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep) tot += ms;
+    }
+    if (rc) break;
+    if (tot < best_ms) { best_ms = tot; best_seg = c; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  tp.release();
+  tr.release();
+  ctx->seg_points = rc ? saved : best_seg;
+  if (best) *best = ctx->seg_points;
+  return rc;
 }
 
 int gwf_cov(gwf_ctx* ctx, const double* F, int64_t N, int mem, double* cov, double* eps, double* cond, void* stream) {

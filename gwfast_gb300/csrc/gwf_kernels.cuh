@@ -409,65 +409,115 @@ __device__ inline void block_load(EvUnion& E, ProjEv& pj, GridEv& g, const unsig
   __syncthreads();
 }
 
-// ------------------------------------------------------------------ Fisher kernel
-// NG: Gram sets per point. L: 1. Triangle, per arm: 3 (arm1, arm2, -(arm1+arm2)).
-// Triangle, detector total: 2, using G(U)+G(V)+G(U+V) = G(sqrt(3/2)(U+V)) + G(sqrt(1/2)(U-V)).
-template <int MODEL, bool EARTH, int NARM, int NG>
-__global__ void __launch_bounds__(kThreads) fisher_kernel(EvBatch ev, DetDev det, const unsigned char* scratch,
-                                                          double* out_arm, double* out_det, int accum) {
-  extern __shared__ __align__(16) unsigned char stage_raw[];
-  cd* stage = reinterpret_cast<cd*>(stage_raw);   // [warp][NG][NP][32]
-  __shared__ EvUnion E;
-  __shared__ ProjEv pj;
-  __shared__ GridEv g;
-  __shared__ ArmPat apc[NARM];
-  __shared__ TimeState tsc;
-  const long long n = ev.n0 + blockIdx.x;
-  if (n >= ev.N) return;
-  block_load<MODEL>(E, pj, g, scratch, blockIdx.x);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (!EARTH) {
-    if (tid == 0) {
-      time_state(pj, pj.tc, tsc);
-      for (int a = 0; a < NARM; ++a) arm_pattern(pj, det.sin_zeta, tsc.x, a, apc[a]);
+// ------------------------------------------------------------------ Fisher kernels
+// Work unit: an item = (event, frequency segment [k0, k1)). The classic kernels run one item per
+// event (k0 = 0, k1 = R) and write the event's matrices; the segmented kernels are persistent,
+// take items from an atomic counter (work stealing), and write one partial Gram per item, which
+// gram_reduce_kernel sums per event in segment order (deterministic).
+//
+// Gram layout in shared memory and in the partials: [set][upper-triangle entry], entry index
+// pidx(a, b) for a <= b (kPairA / kPairB order).
+__host__ __device__ constexpr int pidx(int a, int b) { return a * NP - a * (a - 1) / 2 + (b - a); }
+
+// write the event's matrices from gsum[NG][NE]: scale, and (FP32 form) the psi column restored
+// from Delta = dh/dpsi - 2 s dh/dPhicoal, i.e. F_psi,psi = G_DD + 4 s G_DPc + 4 G_PcPc and
+// F_psi,j = G_Dj + 2 s G_Pcj (psi_sgn = s = +-1; 0: the psi column is dh/dpsi itself)
+template <int NG>
+__device__ void write_gram(const double* gsum, double scale, double psi_sgn, long long n, long long N,
+                           double* out_arm, double* out_det, int accum) {
+  const double s2 = 2.0 * psi_sgn;
+  for (int e = threadIdx.x; e < NE; e += blockDim.x) {
+    const int a = kPairA[e], b = kPairB[e];
+    double sdet = 0.0;
+#pragma unroll
+    for (int gs = 0; gs < NG; ++gs) {
+      const double* G = gsum + gs * NE;
+      double v = G[e];
+      if (psi_sgn != 0.0) {
+        auto at = [&](int x, int y) { return x <= y ? G[pidx(x, y)] : G[pidx(y, x)]; };
+        if (a == I_PS && b == I_PS) v += 2.0 * s2 * at(I_PS, I_PC) + s2 * s2 * at(I_PC, I_PC);
+        else if (a == I_PS) v += s2 * at(I_PC, b);
+        else if (b == I_PS) v += s2 * at(a, I_PC);
+      }
+      v *= scale;
+      sdet += v;
+      if (out_arm && (NG == 1 || NG == 3)) {
+        double* o = out_arm + ((size_t)gs * N + n) * (NP * NP);
+        o[a * NP + b] = v;
+        o[b * NP + a] = v;
+      }
     }
-    __syncthreads();
+    if (out_det) {
+      double* o = out_det + (size_t)n * (NP * NP);
+      if (accum) { o[a * NP + b] += sdet; if (a != b) o[b * NP + a] += sdet; }
+      else { o[a * NP + b] = sdet; o[b * NP + a] = sdet; }
+    }
   }
+}
+
+// per-event state of the FP64 kernels (shared memory)
+template <int NARM, int NG>
+struct F64State {
+  EvUnion E;
+  ProjEv pj;
+  GridEv g;
+  ArmPat apc[NARM];
+  TimeState tsc;
+  double gsum[NG * NE];
+  long long rec;
+};
+
+template <int MODEL, bool EARTH, int NARM, int NG>
+__device__ inline void f64_prepare(const DetDev& det, const unsigned char* scratch, long long rec, F64State<NARM, NG>& S) {
+  block_load<MODEL>(S.E, S.pj, S.g, scratch, rec);
+  if (!EARTH) {
+    if (threadIdx.x == 0) {
+      time_state(S.pj, S.pj.tc, S.tsc);
+      for (int a = 0; a < NARM; ++a) arm_pattern(S.pj, det.sin_zeta, S.tsc.x, a, S.apc[a]);
+    }
+  }
+  if (threadIdx.x == 0) S.rec = rec;
+  __syncthreads();
+}
+
+// Gram of points [k0, k1) into S.gsum (summed over warps); stage: [warp][NG][NP][32] complex
+template <int MODEL, bool EARTH, int NARM, int NG>
+__device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<NARM, NG>& S, cd* stage, int k0, int k1) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NENT = NE * NG;
   constexpr int EPT = (NENT + 31) / 32;
   double acc[EPT];
 #pragma unroll
   for (int i = 0; i < EPT; ++i) acc[i] = 0.0;
   cd* my = stage + (size_t)warp * NG * NP * 32;
-  const int R = g.ok ? g.R : 0;
-  for (int base = 0; base < R; base += kThreads) {
+  for (int base = k0; base < k1; base += kThreads) {
     const int k = base + tid;
     cd D[NARM][NP];
     double sw = 0.0;
-    if (k < R) {
+    if (k < k1) {
       double f, lnf, w;
-      grid_point(g, ev.spacing, k, f, lnf, w);
-      const double S = psd_at(det, f, lnf);
-      sw = sqrt(4.0 * w / S);
+      grid_point(S.g, ev.spacing, k, f, lnf, w);
+      const double Sn = psd_at(det, f, lnf);
+      sw = sqrt(4.0 * w / Sn);
       cd P, C, dP[4], dC[4], dPi, dCi;
       D4 tau(0.0);
-      wave_point_dual<MODEL, EARTH>(E, pj, f, lnf, P, C, dP, dC, dPi, dCi, tau);
+      wave_point_dual<MODEL, EARTH>(S.E, S.pj, f, lnf, P, C, dP, dC, dPi, dCi, tau);
       double dtn[4] = {0.0, 0.0, 0.0, 0.0};
       TimeState ts;
       if (EARTH) {
-        const double tn = pj.tc - tau.v / kDay;
+        const double tn = S.pj.tc - tau.v / kDay;
 #pragma unroll
         for (int q = 0; q < 4; ++q) dtn[q] = -tau.d[q] / kDay;
-        time_state(pj, tn, ts);
+        time_state(S.pj, tn, ts);
       } else {
-        ts = tsc;
+        ts = S.tsc;
       }
 #pragma unroll
       for (int a = 0; a < NARM; ++a) {
         ArmPat ap;
-        if (EARTH) arm_pattern(pj, det.sin_zeta, ts.x, a, ap);
-        else ap = apc[a];
-        arm_derivs(pj, ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D[a]);
+        if (EARTH) arm_pattern(S.pj, det.sin_zeta, ts.x, a, ap);
+        else ap = S.apc[a];
+        arm_derivs(S.pj, ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D[a]);
       }
     } else {
 #pragma unroll
@@ -507,44 +557,152 @@ __global__ void __launch_bounds__(kThreads) fisher_kernel(EvBatch ev, DetDev det
     }
     __syncwarp();
   }
-  // cross-warp reduction through the (now free) staging area
+  // cross-warp reduction through the staging area
   __syncthreads();
-  double* red = reinterpret_cast<double*>(stage_raw);  // [kWarps][NENT]
+  double* red = reinterpret_cast<double*>(stage);  // [kWarps][NENT]
 #pragma unroll
   for (int i = 0; i < EPT; ++i) {
     const int e = lane + 32 * i;
     if (e < NENT) red[warp * NENT + e] = acc[i];
   }
   __syncthreads();
-  const long long N = ev.N;
   for (int e = tid; e < NENT; e += kThreads) {
     double s = 0.0;
 #pragma unroll
     for (int w = 0; w < kWarps; ++w) s += red[w * NENT + e];
-    red[e + kWarps * NENT] = s;
+    S.gsum[e] = s;
   }
   __syncthreads();
-  const double* tot = red + kWarps * NENT;
-  // write full symmetric matrices
-  for (int e = tid; e < NE; e += kThreads) {
-    const int a = kPairA[e], b = kPairB[e];
-    double sdet = 0.0;
-#pragma unroll
-    for (int gs = 0; gs < NG; ++gs) {
-      const double v = tot[gs * NE + e];
-      sdet += v;
-      if (out_arm && (NG == 1 || NG == 3)) {
-        double* o = out_arm + ((size_t)gs * N + n) * (NP * NP);
-        o[a * NP + b] = v;
-        o[b * NP + a] = v;
-      }
-    }
-    if (out_det) {
-      double* o = out_det + (size_t)n * (NP * NP);
-      if (accum) { o[a * NP + b] += sdet; if (a != b) o[b * NP + a] += sdet; }
-      else { o[a * NP + b] = sdet; o[b * NP + a] = sdet; }
-    }
+}
+
+// NG: Gram sets per point. L: 1. Triangle, per arm: 3 (arm1, arm2, -(arm1+arm2)).
+// Triangle, detector total: 2, using G(U)+G(V)+G(U+V) = G(sqrt(3/2)(U+V)) + G(sqrt(1/2)(U-V)).
+template <int MODEL, bool EARTH, int NARM, int NG>
+__global__ void __launch_bounds__(kThreads) fisher_kernel(EvBatch ev, DetDev det, const unsigned char* scratch,
+                                                          double* out_arm, double* out_det, int accum) {
+  extern __shared__ __align__(16) unsigned char stage_raw[];
+  __shared__ F64State<NARM, NG> S;
+  const long long n = ev.n0 + blockIdx.x;
+  if (n >= ev.N) return;
+  f64_prepare<MODEL, EARTH, NARM, NG>(det, scratch, blockIdx.x, S);
+  f64_item<MODEL, EARTH, NARM, NG>(ev, det, S, reinterpret_cast<cd*>(stage_raw), 0, S.g.ok ? S.g.R : 0);
+  write_gram<NG>(S.gsum, 1.0, 0.0, n, ev.N, out_arm, out_det, accum);
+}
+
+// ------------------------------------------------------------------ segmented (persistent) launches
+// Segment bookkeeping of one chunk: off[i] = first item of record i, off[count] = total items.
+struct SegInfo {
+  const long long* off;
+  unsigned long long* counter;   // next item to take
+  double* partial;               // [item][NG * NE]
+  long long cap;                 // items the partial buffer holds
+  int seg;                       // points per segment (multiple of kThreads)
+  int* overflow;                 // set when the items exceed cap (never expected: cap is an upper bound)
+};
+
+// items per record: ceil(R / seg); exclusive scan over the chunk in one block of 1024 threads
+template <int MODEL>
+__global__ void __launch_bounds__(1024) seg_scan_kernel(const unsigned char* scratch, long long count, int seg,
+                                                        long long* off) {
+  __shared__ long long part[1024];
+  const int t = threadIdx.x;
+  const long long per = (count + 1023) / 1024;
+  const long long lo = t * per, hi = lo + per < count ? lo + per : count;
+  long long s = 0;
+  for (long long i = lo; i < hi; ++i) {
+    const GridEv& g = reinterpret_cast<const SetupHdr*>(scratch + i * rec_stride<MODEL>())->g;
+    const long long R = g.ok ? g.R : 0;
+    s += (R + seg - 1) / seg;
   }
+  part[t] = s;
+  __syncthreads();
+  for (int d = 1; d < 1024; d <<= 1) {   // inclusive scan (Hillis-Steele)
+    const long long v = t >= d ? part[t - d] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  long long run = t ? part[t - 1] : 0;
+  for (long long i = lo; i < hi; ++i) {
+    off[i] = run;
+    const GridEv& g = reinterpret_cast<const SetupHdr*>(scratch + i * rec_stride<MODEL>())->g;
+    const long long R = g.ok ? g.R : 0;
+    run += (R + seg - 1) / seg;
+  }
+  if (t == 1023) off[count] = part[1023];
+}
+
+// take the next item; returns false when none is left. Thread 0 takes it and finds its record by
+// binary search in off[]; everything is broadcast through shared memory.
+__device__ inline bool next_item(const SegInfo& si, long long count, long long& item, long long& rec, int& k0) {
+  __shared__ long long sh_item, sh_rec;
+  if (threadIdx.x == 0) {
+    const long long total = si.off[count];
+    long long it = (long long)atomicAdd(si.counter, 1ull);
+    if (it >= total) it = -1;
+    else if (it >= si.cap) { atomicExch(si.overflow, 1); it = -1; }
+    long long r = -1;
+    if (it >= 0) {
+      long long a = 0, b = count;   // largest r with off[r] <= it
+      while (b - a > 1) {
+        const long long m = (a + b) >> 1;
+        if (si.off[m] <= it) a = m; else b = m;
+      }
+      r = a;
+    }
+    sh_item = it;
+    sh_rec = r;
+  }
+  __syncthreads();
+  item = sh_item;
+  rec = sh_rec;
+  __syncthreads();
+  if (item < 0) return false;
+  k0 = (int)((item - si.off[rec]) * si.seg);
+  return true;
+}
+
+template <int MODEL, bool EARTH, int NARM, int NG>
+__global__ void __launch_bounds__(kThreads) fisher_seg_kernel(EvBatch ev, DetDev det, const unsigned char* scratch,
+                                                              long long count, SegInfo si) {
+  extern __shared__ __align__(16) unsigned char stage_raw[];
+  __shared__ F64State<NARM, NG> S;
+  if (threadIdx.x == 0) S.rec = -1;
+  __syncthreads();
+  long long item, rec;
+  int k0;
+  while (next_item(si, count, item, rec, k0)) {
+    if (S.rec != rec) f64_prepare<MODEL, EARTH, NARM, NG>(det, scratch, rec, S);
+    const int R = S.g.ok ? S.g.R : 0;
+    const int k1 = k0 + si.seg < R ? k0 + si.seg : R;
+    f64_item<MODEL, EARTH, NARM, NG>(ev, det, S, reinterpret_cast<cd*>(stage_raw), k0, k1);
+    double* o = si.partial + item * (NG * NE);
+    for (int e = threadIdx.x; e < NG * NE; e += blockDim.x) o[e] = S.gsum[e];
+  }
+}
+
+// per event: sum of its items' partial Grams in segment order, then the event's matrices.
+// scale_of / psi_of give the Gram scale and the psi-column sign of record i (FP32 form) or 1 / 0.
+template <int NG>
+__global__ void __launch_bounds__(kThreads) gram_reduce_kernel(long long n0, long long N, long long count, SegInfo si,
+                                                               const double* scale_of, const double* psi_of,
+                                                               long long rec_stride_d, double* out_arm,
+                                                               double* out_det, int accum) {
+  __shared__ double gsum[NG * NE];
+  const long long i = blockIdx.x;
+  if (i >= count) return;
+  const long long a = si.off[i];
+  long long b = si.off[i + 1];
+  if (b > si.cap) b = si.cap;   // items beyond the buffer were never written (overflow is flagged)
+  for (int e = threadIdx.x; e < NG * NE; e += blockDim.x) {
+    double s = 0.0;
+    for (long long it = a; it < b; ++it) s += si.partial[it * (NG * NE) + e];
+    gsum[e] = s;
+  }
+  __syncthreads();
+  const double scale = scale_of ? scale_of[i * rec_stride_d] : 1.0;
+  const double psi = psi_of ? psi_of[i * rec_stride_d] : 0.0;
+  write_gram<NG>(gsum, scale, psi, n0 + i, N, out_arm, out_det, accum);
 }
 
 // ------------------------------------------------------------------ SNR kernel

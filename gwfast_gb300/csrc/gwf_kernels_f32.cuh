@@ -165,23 +165,21 @@ struct PBF {
   float u1, u0, k4, mg, fmrd;
 };
 
-__device__ inline void pbf_load(const PhaseBasis* src, PBF& b) {
-  for (int i = threadIdx.x; i < 22 * 4; i += blockDim.x) {
+__device__ inline void pbf_fill(const PhaseBasis& src, PBF& b) {
+  for (int i = 0; i < 22 * 4; ++i) {
     const int c = i >> 2, q = i & 3;
-    const D4& d = c < 13 ? src->ins[c] : (c < 17 ? src->itm[c - 13] : src->mrd[c - 17]);
+    const D4& d = c < 13 ? src.ins[c] : (c < 17 ? src.itm[c - 13] : src.mrd[c - 17]);
     const double v = d.d[q];
     const float h = (float)v;
     b.hi[c][q] = h;
     b.lo[c][q] = (float)(v - (double)h);
   }
-  if (threadIdx.x < 4) {
-    b.du1[threadIdx.x] = (float)src->U1.d[threadIdx.x];
-    b.du0[threadIdx.x] = (float)src->U0.d[threadIdx.x];
+  for (int q = 0; q < 4; ++q) {
+    b.du1[q] = (float)src.U1.d[q];
+    b.du0[q] = (float)src.U0.d[q];
   }
-  if (threadIdx.x == 0) {
-    b.u1 = (float)src->U1.v; b.u0 = (float)src->U0.v; b.k4 = (float)src->mrd[4].v;
-    b.mg = (float)src->MG.v; b.fmrd = (float)src->fMRD;
-  }
+  b.u1 = (float)src.U1.v; b.u0 = (float)src.U0.v; b.k4 = (float)src.mrd[4].v;
+  b.mg = (float)src.MG.v; b.fmrd = (float)src.fMRD;
 }
 
 // compensated sum of NB basis terms: each product hi * basis is split exactly into p + e (FMA), p
@@ -239,18 +237,17 @@ __device__ __forceinline__ void phase_tangent_f(const PBF& b, float f, float lnf
   for (int q = 0; q < 4; ++q) dphi[q] = sh[q] + sl[q];
 }
 
-// round a struct of FP64 duals to its FP32 twin, all threads of the block; the dual at `amp_member`
-// is divided by `amp` first (so the FP32 amplitude is O(1)); ends with a block barrier
+// round a struct of FP64 duals to its FP32 twin (one thread); the dual at `amp_member` is divided
+// by `amp` first, so the FP32 amplitude is O(1)
 template <class SRC, class DST>
-__device__ inline void round_struct_par(const SRC& s, DST& d, const D4* amp_member, double amp) {
+__device__ inline void round_struct(const SRC& s, DST& d, const D4* amp_member, double amp) {
   static_assert(sizeof(SRC) == 2 * sizeof(DST), "dual structs must hold only duals");
   const double* a = reinterpret_cast<const double*>(&s);
   float* b = reinterpret_cast<float*>(&d);
   const int lo = (int)(reinterpret_cast<const double*>(amp_member) - a);
   const double inv = 1.0 / amp;
-  for (int i = threadIdx.x; i < (int)(sizeof(DST) / sizeof(float)); i += blockDim.x)
+  for (int i = 0; i < (int)(sizeof(DST) / sizeof(float)); ++i)
     b[i] = (float)((i >= lo && i < lo + 5) ? a[i] * inv : a[i]);
-  __syncthreads();
 }
 
 // derivative vectors d h / d theta (11 parameters, every arm) at one frequency point, FP32 form;
@@ -345,49 +342,81 @@ __device__ __forceinline__ void flush_fixed(long long (&acc)[BPL][6], const int*
   }
 }
 
-template <int MODEL, bool EARTH, int NARM, int NG>
-__global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, DetDev det, const unsigned char* scratch,
-                                                                 double* out_arm, double* out_det, int accum) {
-  constexpr int NQ = 12;  // padded parameter count
-  extern __shared__ __align__(16) unsigned char stage_raw[];
-  int2* stage = reinterpret_cast<int2*>(stage_raw);   // [warp][NG][NQ][32] quantised (re, im)
-  __shared__ int colM[2][kWarps][NG * NQ];             // running column exponents, double-buffered
-  __shared__ double fl[kWarps][gram_slots<NG>()][NQ][NQ];  // FP64 Gram per warp and slot
-  __shared__ int badw[kWarps];
-  __shared__ double gsum[NG][NP][NP];                  // Gram per set, summed over warps
-  __shared__ EvUnion E;
-  __shared__ EvUnionF EF;
-  __shared__ ProjEv pj;
-  __shared__ ProjF pf;
-  __shared__ GridEv g;
-  __shared__ GridF gf;
-  __shared__ ArmF apc[NARM];
-  __shared__ TimeF tsc;
-  __shared__ double scale;
-  __shared__ PBF pbf;
-  const long long n = ev.n0 + blockIdx.x;
-  if (n >= ev.N) return;
-  block_load<MODEL>(E, pj, g, scratch, blockIdx.x);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // amplitude prefactor divided out before rounding the coefficients to FP32
+// FP32 form of one event record: everything the per-point loop reads, rounded once per event by
+// setup_f32_kernel (one thread per event) from the FP64 record
+template <int MODEL>
+struct __align__(16) F32Rec {
+  double scale;     // Gram scale amp^2 / psd_scale (first: the segment reduction reads it)
+  double psi_sgn;   // sign of cos(iota): the psi column is Delta (see point_f32)
+  double lnfmin, delta;
+  EvUnionF ef;
+  PBF pbf;
+  ProjF pf;
+  ArmF apc[2];
+  TimeF tsc;
+  GridF gf;
+};
+template <int MODEL>
+__host__ __device__ constexpr size_t f32_stride() { return ((sizeof(F32Rec<MODEL>) + 15) / 16) * 16; }
+
+template <int MODEL>
+__global__ void __launch_bounds__(64) setup_f32_kernel(DetDev det, const unsigned char* scratch, unsigned char* scratch32,
+                                                       long long count, int narm, int earth) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const unsigned char* rec = scratch + i * rec_stride<MODEL>();
+  const SetupHdr& h = *reinterpret_cast<const SetupHdr*>(rec);
+  const EvUnion& E = *reinterpret_cast<const EvUnion*>(rec + sizeof(SetupHdr));
+  F32Rec<MODEL>& r = *reinterpret_cast<F32Rec<MODEL>*>(scratch32 + i * f32_stride<MODEL>());
+  const GridEv& g = h.g;
   const double amp = g.ok ? (MODEL == 0 ? E.tf2.ampK.v : E.phd.k.ampPref.v) : 1.0;
   if (g.ok) {
-    pbf_load(rec_basis<MODEL>(scratch, blockIdx.x), pbf);
-    if (MODEL == 0) round_struct_par(E.tf2, EF.tf2, &E.tf2.ampK, amp);
-    else round_struct_par(E.phd.k, EF.phd, &E.phd.k.ampPref, amp);
+    pbf_fill(*rec_basis<MODEL>(scratch, i), r.pbf);
+    if (MODEL == 0) round_struct(E.tf2, r.ef.tf2, &E.tf2.ampK, amp);
+    else round_struct(E.phd.k, r.ef.phd, &E.phd.k.ampPref, amp);
   }
-  if (tid == 0) {
-    scale = amp * amp / det.psd_scale;
-    projf_setup(pf, pj, det.sin_zeta);
-    gf.lnfmin = (float)g.lnfmin; gf.delta = (float)g.delta; gf.fac_w = (float)g.fac_w; gf.w0 = (float)g.w0;
-    gf.wl = (float)g.wl; gf.fmin = (float)g.fmin; gf.fcut = (float)g.fcut; gf.df = (float)g.df; gf.R = g.ok ? g.R : 0;
-    gf.acc_l0 = (float)det.acc_l0; gf.acc_idl = (float)det.acc_idl;
-    if (!EARTH) {
-      time_f(pf, 0.0f, tsc);
-      for (int a = 0; a < NARM; ++a) arm_f(pf, tsc, a, apc[a]);
-    }
+  r.scale = amp * amp / det.psd_scale;
+  projf_setup(r.pf, h.pj, det.sin_zeta);
+  r.psi_sgn = r.pf.sgn;
+  GridF& gf = r.gf;
+  gf.lnfmin = (float)g.lnfmin; gf.delta = (float)g.delta; gf.fac_w = (float)g.fac_w; gf.w0 = (float)g.w0;
+  gf.wl = (float)g.wl; gf.fmin = (float)g.fmin; gf.fcut = (float)g.fcut; gf.df = (float)g.df; gf.R = g.ok ? g.R : 0;
+  gf.acc_l0 = (float)det.acc_l0; gf.acc_idl = (float)det.acc_idl;
+  r.lnfmin = g.lnfmin;
+  r.delta = g.delta;
+  if (!earth) {
+    time_f(r.pf, 0.0f, r.tsc);
+    for (int a = 0; a < narm; ++a) arm_f(r.pf, r.tsc, a, r.apc[a]);
   }
+}
+
+// per-block state of the FP32 kernels (shared memory); the staging area is dynamic shared memory
+template <int MODEL, int NG>
+struct F32State {
+  F32Rec<MODEL> r;
+  int colM[2][kWarps][NG * 12];                      // running column exponents, double-buffered
+  double fl[kWarps][gram_slots<NG>()][12][12];       // FP64 Gram per warp and slot
+  double gsum[NG * NE];                              // Gram per set, summed over warps
+  int badw[kWarps];
+  long long rec;
+};
+
+template <int MODEL, int NG>
+__device__ inline void f32_prepare(const unsigned char* scratch32, long long rec, F32State<MODEL, NG>& S) {
+  const uint4* src = reinterpret_cast<const uint4*>(scratch32 + rec * f32_stride<MODEL>());
+  uint4* dst = reinterpret_cast<uint4*>(&S.r);
+  for (int i = threadIdx.x; i < (int)(sizeof(F32Rec<MODEL>) / 16); i += blockDim.x) dst[i] = src[i];
+  if (threadIdx.x == 0) S.rec = rec;
   __syncthreads();
+}
+
+// Gram of points [k0, k1) (k0 a multiple of kThreads) into S.gsum, summed over warps
+template <int MODEL, bool EARTH, int NARM, int NG>
+__device__ inline void f32_item(const EvBatch& ev, const DetDev& det, F32State<MODEL, NG>& S, int2* stage, int k0, int k1) {
+  constexpr int NQ = 12;  // padded parameter count
+  const F32Rec<MODEL>& r = S.r;
+  const GridF& gf = r.gf;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NB = 16 * NG;
   constexpr int BPL = (NB + 31) / 32;
   long long acc[BPL][6];
@@ -396,31 +425,35 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
 #pragma unroll
     for (int e = 0; e < 6; ++e) acc[i][e] = 0ll;
   int2* my = stage + (size_t)warp * NG * NQ * 32;
+  auto& colM = S.colM;
+  auto& fl = S.fl;
   // zero padding row (parameter 11) once; running column exponents start below any value
   for (int gs = 0; gs < NG; ++gs) my[(gs * NQ + 11) * 32 + lane] = make_int2(0, 0);
   for (int i = lane; i < 2 * NG * NQ; i += 32) (&colM[i / (NG * NQ)][warp][0])[i % (NG * NQ)] = kQMinExp;
   for (int i = lane; i < gram_slots<NG>() * NQ * NQ; i += 32) (&fl[warp][0][0][0])[i] = 0.0;
-  if (lane == 0) badw[warp] = 0;
+  if (lane == 0) S.badw[warp] = 0;
   int par = 0, tiles = 0;
   float anc_f = 0.0f, anc_l = 0.0f;
+  int it0 = -1000000;
   bool moved = false, bad = false;
   __syncwarp();
   const int R = gf.R;
-  for (int base = 0; base < R; base += kThreads) {
+  for (int base = k0; base < k1; base += kThreads) {
     const int k = base + tid;
     cf D[NARM][NP];
     float sw = 0.0f;
     // geometric grid: f_k = f_tile * exp(lane * delta), ln f_k = ln f_tile + lane * delta, with the
     // tile anchors formed in FP64: each lane computes the anchor of one of the warp's next 32 tiles
     const int it = base / kThreads;
-    if (ev.spacing == 0 && (it & 31) == 0) {
-      const double l = g.lnfmin + (double)(((long long)(it + lane) * kWarps + warp) * 32) * g.delta;
+    if (ev.spacing == 0 && it - it0 >= 32) {
+      it0 = it;
+      const double l = r.lnfmin + (double)(((long long)(it + lane) * kWarps + warp) * 32) * r.delta;
       anc_f = (float)exp(l);
       anc_l = (float)l;
     }
-    const float ftile = __shfl_sync(0xffffffffu, anc_f, it & 31);
-    const float ltile = __shfl_sync(0xffffffffu, anc_l, it & 31);
-    if (k < R) {
+    const float ftile = __shfl_sync(0xffffffffu, anc_f, (it - it0) & 31);
+    const float ltile = __shfl_sync(0xffffffffu, anc_l, (it - it0) & 31);
+    if (k < k1) {
       float f, lnf, w;
       if (ev.spacing == 0) {
         lnf = fmaf((float)lane, gf.delta, ltile);
@@ -432,9 +465,9 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
         lnf = logf(f);
         w = (k == 0 || k == R - 1) ? 0.5f * gf.df : gf.df;
       }
-      const float S = psd_at_f(det, f, lnf, gf.acc_l0, gf.acc_idl);
-      sw = sqrtf(4.0f * w / S);
-      point_f32<MODEL, EARTH, NARM>(EF, pbf, pf, apc, tsc, f, lnf, D);
+      const float Sn = psd_at_f(det, f, lnf, gf.acc_l0, gf.acc_idl);
+      sw = sqrtf(4.0f * w / Sn);
+      point_f32<MODEL, EARTH, NARM>(r.ef, r.pbf, r.pf, r.apc, r.tsc, f, lnf, D);
     } else {
 #pragma unroll
       for (int a = 0; a < NARM; ++a)
@@ -511,9 +544,12 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
     __syncwarp();
   }
   flush_fixed<NG, NQ, BPL, NB>(acc, &colM[par][warp][0], &fl[warp][0][0][0], lane);
-  if (lane == 0 && bad) badw[warp] = 1;
+  if (lane == 0 && bad) S.badw[warp] = 1;
   __syncthreads();
-  // sum over warps in FP64, per Gram set
+  // sum over warps in FP64, per Gram set; NaN if any tile held Inf or NaN
+  int anybad = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; ++w) anybad |= S.badw[w];
   const double* red = &fl[0][0][0][0];  // [kWarps][gram_slots][NQ][NQ]
   constexpr int NS = gram_slots<NG>();
   for (int e = tid; e < NG * NE; e += kThreads) {
@@ -524,40 +560,39 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
       v += red[((size_t)(w * NS + gs) * NQ + a) * NQ + b];
       if (NG == 1) v += red[((size_t)(w * NS + 1) * NQ + a) * NQ + b];
     }
-    gsum[gs][a][b] = v;
-    gsum[gs][b][a] = v;
+    S.gsum[e] = anybad ? __longlong_as_double(0x7ff8000000000000ll) : v;
   }
   __syncthreads();
-  const long long N = ev.N;
-  int anybad = 0;
-#pragma unroll
-  for (int w = 0; w < kWarps; ++w) anybad |= badw[w];
-  const double sc = anybad ? __longlong_as_double(0x7ff8000000000000ll) : scale;
-  // back to the psi column: dh/dpsi = Delta + 2 s dh/dPhicoal
-  const double s2 = 2.0 * (double)pf.sgn;
-  for (int e = tid; e < NE; e += kThreads) {
-    const int a = kPairA[e], b = kPairB[e];
-    double sdet = 0.0;
-#pragma unroll
-    for (int gs = 0; gs < NG; ++gs) {
-      const double (*G)[NP] = gsum[gs];
-      double v = G[a][b];
-      if (a == I_PS && b == I_PS) v += 2.0 * s2 * G[I_PS][I_PC] + s2 * s2 * G[I_PC][I_PC];
-      else if (a == I_PS) v += s2 * G[I_PC][b];
-      else if (b == I_PS) v += s2 * G[a][I_PC];
-      v *= sc;
-      sdet += v;
-      if (out_arm && (NG == 1 || NG == 3)) {
-        double* o = out_arm + ((size_t)gs * N + n) * (NP * NP);
-        o[a * NP + b] = v;
-        o[b * NP + a] = v;
-      }
-    }
-    if (out_det) {
-      double* o = out_det + (size_t)n * (NP * NP);
-      if (accum) { o[a * NP + b] += sdet; if (a != b) o[b * NP + a] += sdet; }
-      else { o[a * NP + b] = sdet; o[b * NP + a] = sdet; }
-    }
+}
+
+template <int MODEL, bool EARTH, int NARM, int NG>
+__global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, DetDev det, const unsigned char* scratch32,
+                                                                 double* out_arm, double* out_det, int accum) {
+  extern __shared__ __align__(16) unsigned char stage_raw[];
+  __shared__ F32State<MODEL, NG> S;
+  const long long n = ev.n0 + blockIdx.x;
+  if (n >= ev.N) return;
+  f32_prepare<MODEL, NG>(scratch32, blockIdx.x, S);
+  f32_item<MODEL, EARTH, NARM, NG>(ev, det, S, reinterpret_cast<int2*>(stage_raw), 0, S.r.gf.R);
+  write_gram<NG>(S.gsum, S.r.scale, S.r.psi_sgn, n, ev.N, out_arm, out_det, accum);
+}
+
+template <int MODEL, bool EARTH, int NARM, int NG>
+__global__ void __launch_bounds__(kThreads, 4) fisher_seg_kernel_f32(EvBatch ev, DetDev det, const unsigned char* scratch32,
+                                                                     long long count, SegInfo si) {
+  extern __shared__ __align__(16) unsigned char stage_raw[];
+  __shared__ F32State<MODEL, NG> S;
+  if (threadIdx.x == 0) S.rec = -1;
+  __syncthreads();
+  long long item, rec;
+  int k0;
+  while (next_item(si, count, item, rec, k0)) {
+    if (S.rec != rec) f32_prepare<MODEL, NG>(scratch32, rec, S);
+    const int R = S.r.gf.R;
+    const int k1 = k0 + si.seg < R ? k0 + si.seg : R;
+    f32_item<MODEL, EARTH, NARM, NG>(ev, det, S, reinterpret_cast<int2*>(stage_raw), k0, k1);
+    double* o = si.partial + item * (NG * NE);
+    for (int e = threadIdx.x; e < NG * NE; e += blockDim.x) o[e] = S.gsum[e];
   }
 }
 

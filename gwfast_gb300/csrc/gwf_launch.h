@@ -19,8 +19,16 @@ struct LaunchArgs {
   int accum;
   int per_arm;
   int precision;  // 0 = FP64, 1 = FP32 split precision (22-mode models); the launchers see no other value
-  unsigned char* scratch;  // kChunk x setup_stride(model) bytes
+  unsigned char* scratch;  // cap_events x setup_stride(model) bytes: FP64 records, then FP32 records
+  long long cap_events;    // events the scratch holds (locates the FP32 records)
   cudaStream_t stream;
+  // segmented persistent launches (seg > 0: points per segment, a multiple of kThreads)
+  int seg = 0;
+  long long* seg_off = nullptr;            // kChunk + 1
+  unsigned long long* seg_ctr = nullptr;   // item counter
+  double* seg_part = nullptr;              // seg_cap x 3 x 66 partial Grams
+  long long seg_cap = 0;
+  int* seg_ovf = nullptr;                  // set if the items exceed seg_cap
 };
 
 cudaError_t launch_fisher_m0(const LaunchArgs& a);

@@ -166,6 +166,7 @@ extern "C" int gwf_fisher_noalloc(const gwf_det_desc* det, const double* psd_f, 
   const size_t stride = wf->model == 0 ? gwf::setup_stride_m0() : (wf->model == 1 ? gwf::setup_stride_m1() : gwf::setup_stride_m2());
   long long per_pass = (long long)((kScratchBytes - kOffRec) / stride);
   if (per_pass > gwf::kChunk) per_pass = gwf::kChunk;
+  a.cap_events = per_pass;
   // events are processed in passes that fit the set-up records into the scratch
   for (long long s0 = 0; s0 < n_events; s0 += per_pass) {
     const long long cnt = (n_events - s0) < per_pass ? (n_events - s0) : per_pass;

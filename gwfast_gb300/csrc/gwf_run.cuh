@@ -1,0 +1,167 @@
+// Launch sequences of one waveform model. Each of gwf_run_tf2.cu, gwf_run_phd.cu and
+// gwf_run_phm.cu defines GWF_MODEL and includes this file, so the three models compile as
+// separate translation units in parallel.
+//
+// Per chunk of events: the per-event set-up kernel (FP64 records), for the FP32 form the FP32
+// record kernel, then either the classic Fisher/SNR kernel (one CTA per event) or, when the
+// launch asks for segments, the segment scan, the persistent work-stealing Fisher kernel and the
+// per-event reduction of the segment partials.
+#include "gwf_launch.h"
+
+namespace gwf {
+
+namespace {
+
+constexpr int M = GWF_MODEL;
+
+unsigned char* scratch32_of(const LaunchArgs& a) { return a.scratch + (size_t)a.cap_events * rec_stride<M>(); }
+
+int sm_count() {
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n > 0 ? n : 1;
+}
+
+template <class MAIN>
+cudaError_t chunked(const LaunchArgs& a, bool f32, MAIN main) {
+  for (long long n0 = 0; n0 < a.ev.N; n0 += kChunk) {
+    EvBatch ev = a.ev;
+    ev.n0 = n0;
+    const long long cnt = (a.ev.N - n0) < kChunk ? (a.ev.N - n0) : kChunk;
+    const unsigned nb = (unsigned)((cnt + 63) / 64);
+    setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, a.det, a.wf, a.qnm, a.nq, a.scratch, cnt);
+#if GWF_MODEL < 2
+    if (f32) setup_f32_kernel<M><<<nb, 64, 0, a.stream>>>(a.det, a.scratch, scratch32_of(a), cnt,
+                                                          a.det.shape == 1 ? 2 : 1, a.det.earth);
+#endif
+    const cudaError_t e = main(ev, cnt);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaGetLastError();
+}
+
+SegInfo seg_info(const LaunchArgs& a) {
+  SegInfo si;
+  si.off = a.seg_off;
+  si.counter = a.seg_ctr;
+  si.partial = a.seg_part;
+  si.cap = a.seg_cap;
+  si.seg = a.seg;
+  si.overflow = a.seg_ovf;
+  return si;
+}
+
+// segmented launch of one chunk: scan, persistent kernel, reduction
+template <int NG, class KSEG>
+cudaError_t seg_chunk(const LaunchArgs& a, const EvBatch& ev, long long cnt, KSEG ks, const unsigned char* kscratch,
+                      int smem, int grid, const double* scale_of, const double* psi_of, long long stride_d) {
+  seg_scan_kernel<M><<<1, 1024, 0, a.stream>>>(a.scratch, cnt, a.seg, a.seg_off);
+  cudaError_t e = cudaMemsetAsync(a.seg_ctr, 0, sizeof(unsigned long long), a.stream);
+  if (e != cudaSuccess) return e;
+  const SegInfo si = seg_info(a);
+  ks<<<grid, kThreads, smem, a.stream>>>(ev, a.det, kscratch, cnt, si);
+  gram_reduce_kernel<NG><<<(unsigned)cnt, kThreads, 0, a.stream>>>(ev.n0, ev.N, cnt, si, scale_of, psi_of, stride_d,
+                                                                   a.out_arm, a.out_det, a.accum);
+  return cudaGetLastError();
+}
+
+template <class K>
+cudaError_t persist_grid(K k, int smem, int* grid) {
+  int occ = 0;
+  const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kThreads, smem);
+  if (e != cudaSuccess) return e;
+  *grid = (occ > 0 ? occ : 1) * sm_count();
+  return cudaSuccess;
+}
+
+template <bool EARTH, int NARM, int NG>
+cudaError_t fisher_one(const LaunchArgs& a) {
+  const int smem = kWarps * NG * NP * 32 * (int)sizeof(cd);
+  if (a.seg <= 0) {
+    auto k = fisher_kernel<M, EARTH, NARM, NG>;
+    cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (err != cudaSuccess) return err;
+    return chunked(a, false, [&](const EvBatch& ev, long long cnt) {
+      k<<<(unsigned)cnt, kThreads, smem, a.stream>>>(ev, a.det, a.scratch, a.out_arm, a.out_det, a.accum);
+      return cudaSuccess;
+    });
+  }
+  auto ks = fisher_seg_kernel<M, EARTH, NARM, NG>;
+  cudaError_t err = cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  int grid = 0;
+  if (err == cudaSuccess) err = persist_grid(ks, smem, &grid);
+  if (err != cudaSuccess) return err;
+  return chunked(a, false, [&](const EvBatch& ev, long long cnt) {
+    return seg_chunk<NG>(a, ev, cnt, ks, a.scratch, smem, grid, nullptr, nullptr, 0);
+  });
+}
+
+#if GWF_MODEL < 2
+template <bool EARTH, int NARM, int NG>
+cudaError_t fisher_one_f32(const LaunchArgs& a) {
+  const int smem = kWarps * NG * 12 * 32 * (int)sizeof(int2);
+  unsigned char* s32 = scratch32_of(a);
+  if (a.seg <= 0) {
+    auto k = fisher_kernel_f32<M, EARTH, NARM, NG>;
+    cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (err != cudaSuccess) return err;
+    return chunked(a, true, [&](const EvBatch& ev, long long cnt) {
+      k<<<(unsigned)cnt, kThreads, smem, a.stream>>>(ev, a.det, s32, a.out_arm, a.out_det, a.accum);
+      return cudaSuccess;
+    });
+  }
+  auto ks = fisher_seg_kernel_f32<M, EARTH, NARM, NG>;
+  cudaError_t err = cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  int grid = 0;
+  if (err == cudaSuccess) err = persist_grid(ks, smem, &grid);
+  if (err != cudaSuccess) return err;
+  // Gram scale and psi-column sign lead each FP32 record
+  const double* rec0 = reinterpret_cast<const double*>(s32);
+  const long long stride_d = (long long)(f32_stride<M>() / sizeof(double));
+  return chunked(a, true, [&](const EvBatch& ev, long long cnt) {
+    return seg_chunk<NG>(a, ev, cnt, ks, s32, smem, grid, rec0, rec0 + 1, stride_d);
+  });
+}
+#endif
+
+template <bool EARTH, int NARM>
+cudaError_t snr_one(const LaunchArgs& a) {
+  return chunked(a, false, [&](const EvBatch& ev, long long cnt) {
+    snr_kernel<M, EARTH, NARM><<<(unsigned)cnt, kThreads, 0, a.stream>>>(ev, a.det, a.scratch, a.out_arm, a.out_det,
+                                                                          a.accum);
+    return cudaSuccess;
+  });
+}
+
+cudaError_t fisher_dispatch(const LaunchArgs& a) {
+  const bool tri = a.det.shape == 1;
+  if (a.precision == 1) {
+#if GWF_MODEL < 2
+    if (a.det.earth) {
+      if (!tri) return fisher_one_f32<true, 1, 1>(a);
+      return a.per_arm ? fisher_one_f32<true, 2, 3>(a) : fisher_one_f32<true, 2, 2>(a);
+    }
+    if (!tri) return fisher_one_f32<false, 1, 1>(a);
+    return a.per_arm ? fisher_one_f32<false, 2, 3>(a) : fisher_one_f32<false, 2, 2>(a);
+#else
+    return cudaErrorNotSupported;
+#endif
+  }
+  if (a.det.earth) {
+    if (!tri) return fisher_one<true, 1, 1>(a);
+    return a.per_arm ? fisher_one<true, 2, 3>(a) : fisher_one<true, 2, 2>(a);
+  }
+  if (!tri) return fisher_one<false, 1, 1>(a);
+  return a.per_arm ? fisher_one<false, 2, 3>(a) : fisher_one<false, 2, 2>(a);
+}
+
+cudaError_t snr_dispatch(const LaunchArgs& a) {
+  const bool tri = a.det.shape == 1;
+  if (a.det.earth) return tri ? snr_one<true, 2>(a) : snr_one<true, 1>(a);
+  return tri ? snr_one<false, 2>(a) : snr_one<false, 1>(a);
+}
+
+}  // namespace
+
+}  // namespace gwf

@@ -63,11 +63,13 @@ class DetNet:
         precision = kwargs.get('precision', 'fp64')
         if not return_all:
             F = fisher_batch(sigs, evParams, res, per_arm=False, spacing=spacing, device=sigs[0].device,
-                             precision=precision, refine_cond=kwargs.get('refine_cond'))
+                             precision=precision, refine_cond=kwargs.get('refine_cond'),
+                             res_per_event=kwargs.get('res_per_event'))
             F = reparametrise(F, evParams, use_m1m2, use_chi1chi2)
             return np.moveaxis(F, 0, -1)
         per = fisher_batch(sigs, evParams, res, per_arm=True, spacing=spacing, device=sigs[0].device,
-                           precision=precision, refine_cond=kwargs.get('refine_cond'))
+                           precision=precision, refine_cond=kwargs.get('refine_cond'),
+                           res_per_event=kwargs.get('res_per_event'))
         allF = {}
         for name, s, Fa in zip(names, sigs, per):
             Fa = reparametrise(Fa, evParams, use_m1m2, use_chi1chi2)

@@ -55,10 +55,11 @@ def snr_batch(signals, evParams, res=1000, device=0):
 
 
 def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', device=0, precision='fp64',
-                 refine_cond=None):
+                 refine_cond=None, res_per_event=None):
     """Fisher matrices of all signals in one library call.
 
     per_arm: list (per signal) of (arms, N, 11, 11); otherwise the network total (N, 11, 11).
+    res_per_event: optional (N,) grid lengths, one per event (an extension: gwfast uses one res).
     precision: 'fp64' (the drop-in), 'fp32' (split precision, TaylorF2 and IMRPhenomD), or
     'mixed' ('fp32', then FP64 for the events whose network Fisher has an equilibrated condition
     number above refine_cond, default 1e11).
@@ -71,11 +72,12 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
     if precision == 'mixed':
         ctx.set_refine_cond(1e11 if refine_cond is None else refine_cond)
     sp = 0 if spacing == 'geom' else 1
+    rev = None if res_per_event is None else np.ascontiguousarray(np.broadcast_to(res_per_event, (N,)), dtype=np.int32)
     duty = any(s.DutyFactor is not None for s in signals)
     if per_arm or duty:
         out = np.empty((sum(slots), N, 11, 11))
-        ctx.fisher([s.det_id for s in signals], wf.gpu_desc(), p, res, spacing=sp, per_arm=True, out_arm=out,
-                   precision=precision)
+        ctx.fisher([s.det_id for s in signals], wf.gpu_desc(), p, res, res_ev=rev, spacing=sp, per_arm=True,
+                   out_arm=out, precision=precision)
         res_l, i = [], 0
         for s, k in zip(signals, slots):
             res_l.append(s._apply_duty(out[i:i + k], seed=True))
@@ -84,8 +86,8 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
             return res_l
         return sum(r.sum(axis=0) for r in res_l)
     out = np.empty((N, 11, 11))
-    ctx.fisher([s.det_id for s in signals], wf.gpu_desc(), p, res, spacing=sp, per_arm=False, out_net=out,
-               precision=precision)
+    ctx.fisher([s.det_id for s in signals], wf.gpu_desc(), p, res, res_ev=rev, spacing=sp, per_arm=False,
+               out_net=out, precision=precision)
     return out
 
 

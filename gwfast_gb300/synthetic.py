@@ -44,9 +44,31 @@ def bbh_events(n, seed=1001, mmin=5., mmax=80., alpha=-2.3, qmin=0.2, chimax=0.8
     return _angles(rng, n, ev)
 
 
+def mixed_events(n, seed=1002, bns_fraction=0.5):
+    """Mixed catalogue: the first round(n * bns_fraction) events BNS (bns_events distributions), the
+    rest BBH (bbh_events distributions), each part from its own stream of the seed."""
+    nb = int(round(n * bns_fraction))
+    a, b = bns_events(nb, seed=seed), bbh_events(n - nb, seed=seed + 1)
+    return {k: np.concatenate([np.asarray(a[k]), np.asarray(b[k])]) for k in a}
+
+
+def chirp_time(Mc, f):
+    """Leading-order time to coalescence from frequency f [Hz] for chirp mass Mc [Msun], seconds."""
+    tM = np.asarray(Mc) * glob.GMsun_over_c3
+    return 5. / 256. * (np.pi * f) ** (-8. / 3.) * tM ** (-5. / 3.)
+
+
+def res_from_chirp_time(Mc, fmin, lo=200, hi=40000, tau0=100., power=0.8):
+    """Per-event grid length growing with the chirp time from fmin: lo * (tau / tau0)^power, clipped
+    to [lo, hi] (200 points for heavy BBH, 40000 for BNS from 2 Hz)."""
+    r = lo * (chirp_time(Mc, fmin) / tau0) ** power
+    return np.clip(np.rint(r), lo, hi).astype(np.int32)
+
+
 # detector networks: name -> (low-frequency wall / fmin in Hz)
 NETWORK_LHET = (('L1', 10.), ('H1', 10.), ('ETS', 5.))
 NETWORK_ET_CE = (('ETS', 5.), ('CE1Id', 5.), ('CE2NM', 5.))
+NETWORK_LHET2 = (('L1', 10.), ('H1', 10.), ('ETS', 2.))   # mixed catalogue: ET wall at 2 Hz
 
 
 def detector_spec(name, fmin):

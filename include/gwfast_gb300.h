@@ -113,6 +113,22 @@ int gwf_fisher(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* w
  * reduced-precision form). kappa > 0; events with equilibrated condition number above it get FP64. */
 int gwf_set_refine_cond(gwf_ctx* ctx, double kappa);
 
+/* Work decomposition of gwf_fisher (no counterpart in gwfast: a launch-shape choice).
+ * points = 0: one CTA per (event, detector), the default. points > 0 (a multiple of 128): every
+ * event is cut into frequency segments of that many points; persistent CTAs take segments from
+ * an atomic counter (work stealing), and a second kernel sums each event's segment Grams in
+ * order (deterministic). Catalogues whose events have very different grid lengths
+ * (res_per_event) keep every SM busy this way. */
+int gwf_set_segments(gwf_ctx* ctx, int points);
+
+/* Autotuner for gwf_set_segments: runs the given workload (typically a sample of the catalogue)
+ * as gwf_fisher would, with each candidate segment length (0 = per event, 256, 512, 1024, 2048),
+ * times each with CUDA events (one warm-up and two timed runs), keeps the fastest in the context
+ * and returns it in *best. Arguments as gwf_fisher. */
+int gwf_autotune_segments(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params,
+                          int64_t ld, int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing,
+                          int precision, int mem, int* best);
+
 /* Covariance by equilibrated Cholesky inversion, FP64, one 11x11 matrix per event.
  * Replaces fisherTools.CovMatr 'cho' path (gwfast/fisherTools.py:32-196) together with
  * compute_inversion_error (:199-212); cond receives the condition number of the

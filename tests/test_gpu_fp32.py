@@ -80,7 +80,7 @@ def test_phenomd_network_mixed(gpu_lib):
     Fm = np.moveaxis(net.FisherMatr(dict(ev), res=2000, precision="mixed", refine_cond=3e11), -1, 0)
     se, cond = sigma_err(Fm, F64)
     worst = se.max(axis=1)
-    exact = np.all(Fm == F64, axis=(1, 2))
+    exact = entry_err(Fm, F64).max(axis=(1, 2)) < 1e-11   # recomputed in FP64 (segmented: rounding-level)
     print('PhenomD mixed: FP64 events %.3f, cond of those >= %.2e; sigma err median %.2e max %.2e; frac<=1e-3 %.4f'
           % (exact.mean(), cond[exact].min() if exact.any() else np.nan, np.median(worst), worst.max(),
              np.mean(worst <= 1e-3)))
@@ -93,13 +93,14 @@ def test_phenomd_network_mixed(gpu_lib):
 
 def test_mixed_all_refined_is_fp64(gpu_lib):
     """With a threshold below every condition number, the mixed form returns the FP64 matrices
-    bit for bit (gather, FP64 recomputation and scatter of every event), per arm as well."""
+    (gather, FP64 recomputation in frequency segments and scatter of every event), per arm as well;
+    the segment sums differ from the per-event kernel only in summation order."""
     ev = synthetic.bbh_events(200, seed=5)
     net = synthetic.make_network(W.IMRPhenomD(), earth=True)
     F64 = net.FisherMatr(dict(ev), res=1000, return_all=True)
     Fm = net.FisherMatr(dict(ev), res=1000, return_all=True, precision='mixed', refine_cond=1.0)
     for k in F64:
-        assert np.array_equal(Fm[k], F64[k]), k
+        assert entry_err(np.moveaxis(Fm[k], -1, 0), np.moveaxis(F64[k], -1, 0)).max() < 1e-12, k
 
 
 def test_mixed_condition_estimate(gpu_lib):
@@ -111,6 +112,6 @@ def test_mixed_condition_estimate(gpu_lib):
     for kappa in np.percentile(cond, [10, 50, 90]):
         # every event whose mixed result is FP64 had an estimated condition number above kappa
         Fm = np.moveaxis(net.FisherMatr(dict(ev), res=1000, precision='mixed', refine_cond=kappa), -1, 0)
-        refined = np.all(Fm == F, axis=(1, 2))
+        refined = entry_err(Fm, F).max(axis=(1, 2)) < 1e-11
         assert np.all(cond[refined] >= kappa / 1.05)
         assert np.all(cond[~refined] <= kappa * 1.05)
