@@ -176,6 +176,7 @@ def main():
     ap.add_argument('--only-device', action='store_true', help='only the device-resident Fisher steps (for ncu)')
     ap.add_argument('--precision', default='fp32', choices=('fp32', 'fp64', 'mixed'), help='form used with --only-device')
     ap.add_argument('--refine-cond', type=float, default=1e11, help='condition-number threshold of the mixed form')
+    ap.add_argument('--no-autotune', action='store_true', help='per-event launches, no segment autotuning')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
@@ -209,6 +210,11 @@ def main():
 
     ctx.set_refine_cond(args.refine_cond)
     out32 = torch.empty((N, 11, 11), dtype=torch.float64, device=dev)
+    # launch shape: per-event CTAs or persistent segments, chosen by the library's autotuner on a sample
+    seg = 0
+    if not args.no_autotune:
+        ns = min(N, 2000)
+        seg = ctx.autotune_segments(ids, desc, p_dev, RES, precision='fp32', mem=_lib.MEM_DEVICE, ld=N, n=ns)
 
     def fisher_step(det_ids=ids, o=out, precision='mixed'):
         ctx.fisher(det_ids, desc, p_dev, RES, per_arm=False, mem=_lib.MEM_DEVICE, out_net=o, stream=stream.cuda_stream,
@@ -275,12 +281,19 @@ def main():
     c64, _, cond = fisherTools.CovMatr(np.moveaxis(F64_all[:nchk], 0, -1), return_cond=True, device=local)
     s64 = np.sqrt(np.einsum('iin->ni', c64))
 
+    # above equilibrated cond ~1e13 the FP64 sigmas themselves change with the summation order
+    # (two FP64 runs that sum in a different order disagree there), so those events are counted apart
+    stable = cond < 1e13
+
     def sig_err(F):
         c, _, _ = fisherTools.CovMatr(np.moveaxis(F[:nchk], 0, -1), return_cond=True, device=local)
         e = np.nanmax(np.abs(np.sqrt(np.einsum('iin->ni', c)) - s64) / s64, axis=1)
-        return {'events': int(nchk), 'median': float(np.nanmedian(e)), 'p99': float(np.nanpercentile(e, 99)),
-                'max': float(np.nanmax(e)), 'frac_le_1e-3': float(np.mean(e <= 1e-3)),
-                'what': 'max over 11 parameters of |sigma - sigma_fp64| / sigma_fp64 per event'}
+        es = e[stable]
+        return {'events': int(stable.sum()), 'median': float(np.nanmedian(es)), 'p99': float(np.nanpercentile(es, 99)),
+                'max': float(np.nanmax(es)), 'frac_le_1e-3': float(np.mean(es <= 1e-3)),
+                'events_cond_ge_1e13': int((~stable).sum()), 'frac_le_1e-3_all_events': float(np.mean(e <= 1e-3)),
+                'what': 'max over 11 parameters of |sigma - sigma_fp64| / sigma_fp64 per event, events with '
+                        'equilibrated cond < 1e13 (FP64 sigmas stable under summation order)'}
 
     serr_mixed = sig_err(Fm_all)
     serr_fp32 = sig_err(out32.cpu().numpy())
@@ -311,7 +324,8 @@ def main():
         'config': {'workload': 'IMRPhenomD BBH 1e4 events, L1+H1+ETS, Earth rotation, R=2000; mixed form (FP32 '
                                'split precision, FP64 for equilibrated cond > %.0e)' % args.refine_cond,
                    'events_per_gpu': N, 'res': RES, 'parallelism': 'replicas over event shards' if world > 1 else 'single',
-                   'l2': 'flushed (256 MB write) before every step'},
+                   'l2': 'flushed (256 MB write) before every step',
+                   'segments': seg if seg else 'per-event launches (autotuned)' if not args.no_autotune else 'per-event launches'},
         'plain_fp64': {'value': world * N / (ms64 / 1e3), 'unit': 'Fisher/s', 'ms_per_step': ms64},
         'speedup_vs_plain_fp64': ms64 / ms,
         'fp32_only': {'value': world * N / (ms32 / 1e3), 'unit': 'Fisher/s', 'ms_per_step': ms32},

@@ -51,6 +51,7 @@ SIGNATURES = {
     'gwf_cov': ([_vp, _vp, _i64, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     'gwf_set_refine_cond': ([_vp, _d], ctypes.c_int),
     'gwf_set_segments': ([_vp, ctypes.c_int], ctypes.c_int),
+    'gwf_set_graphs': ([_vp, ctypes.c_int], ctypes.c_int),
     'gwf_autotune_segments': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32, _vp, ctypes.c_int,
                                ctypes.c_int, ctypes.c_int, _P(ctypes.c_int)], ctypes.c_int),
     'gwf_fisher_noalloc': ([_P(DetDesc), _vp, _vp, _i64, _P(WfDesc), _vp, _vp, _vp, _i64, _vp, _i64, _i64,
@@ -146,6 +147,10 @@ class Context:
         check(load().gwf_fisher(self.h, len(ids), ptr(ids), ctypes.byref(wf), ptr(params), ld, n, int(res),
                                 ptr(res_ev), spacing, int(bool(per_arm)), PRECISION[precision], mem, ptr(out_arm),
                                 ptr(out_net), stream))
+
+    def set_graphs(self, on):
+        """Capture repeated device-resident Fisher calls in CUDA graphs and replay them."""
+        check(load().gwf_set_graphs(self.h, int(bool(on))))
 
     def set_segments(self, points):
         """0: one CTA per event; > 0: persistent launches over frequency segments of this many points."""

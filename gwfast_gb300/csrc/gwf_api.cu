@@ -3,6 +3,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -73,6 +74,11 @@ struct DetRec {
   double l0 = 0.0, idl = 0.0, scale = 1.0;
 };
 
+struct GraphEntry {
+  cudaGraphExec_t exec;
+  std::string bufs;   // buffer_sig at capture time
+};
+
 }  // namespace
 
 namespace gwf {
@@ -92,6 +98,10 @@ struct gwf_ctx {
   int seg_points = 0;      // Fisher launches: 0 = one CTA per event, > 0 = persistent, segments of this many points
   int refine_seg = 256;    // segment length of the FP64 recomputation of GWF_PREC_MIXED
   DevBuf seg_off, seg_ctr, seg_part, seg_ovf, tune_out;
+  int graphs = 0;                                  // capture device-resident Fisher calls in CUDA graphs
+  std::map<std::string, GraphEntry> graph_cache;   // call identity -> instantiated graph
+  std::string graph_pending;                       // identity of the last uncaptured call
+  int64_t graph_rmax = 0;
   cudaEvent_t scratch_free = nullptr;  // recorded after the last launch that used the set-up scratch
   HostBuf hpar, hout;
 };
@@ -271,6 +281,33 @@ int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const
   return GWF_OK;
 }
 
+int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params,
+             int64_t ld, int64_t N, int32_t res, const int32_t* res_ev, int spacing, int per_arm, int precision,
+             int mem, double* out_arm, double* out_net, cudaStream_t st, bool capturing);
+
+// a call's identity for the graph cache: every argument, pointers included
+std::string graph_key(int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params, int64_t ld,
+                      int64_t N, int32_t res, const int32_t* res_ev, int spacing, int per_arm, int precision,
+                      const double* out_arm, const double* out_net, cudaStream_t st) {
+  std::string k;
+  auto add = [&](const void* p, size_t n) { k.append(reinterpret_cast<const char*>(p), n); };
+  add(&n_det, sizeof n_det);
+  add(det_ids, sizeof(int) * (size_t)n_det);
+  add(wf, sizeof(*wf));
+  add(&params, sizeof params); add(&ld, sizeof ld); add(&N, sizeof N); add(&res, sizeof res); add(&res_ev, sizeof res_ev);
+  add(&spacing, sizeof spacing); add(&per_arm, sizeof per_arm); add(&precision, sizeof precision);
+  add(&out_arm, sizeof out_arm); add(&out_net, sizeof out_net); add(&st, sizeof st);
+  return k;
+}
+
+// the context buffers a captured graph refers to
+std::string buffer_sig(const gwf_ctx* ctx) {
+  const void* p[] = {ctx->setup.p, ctx->seg_off.p, ctx->seg_ctr.p, ctx->seg_part.p, ctx->seg_ovf.p};
+  std::string k(reinterpret_cast<const char*>(p), sizeof p);
+  k.append(reinterpret_cast<const char*>(&ctx->seg_points), sizeof ctx->seg_points);
+  return k;
+}
+
 int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params,
         int64_t ld, int64_t N, int32_t res, const int32_t* res_ev, int spacing, int per_arm, int precision, int mem,
         double* out_arm, double* out_net, void* stream) {
@@ -286,10 +323,61 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
   if (fisher && !per_arm) out_arm = nullptr;
   if (fisher && per_arm && !out_arm) return fail(GWF_ERR_INVALID_ARG, "per_arm needs out_arm");
   if (N == 0) return GWF_OK;
-  for (int i = 0; i < n_det; ++i)
-    for (int j = 0; j < N && res_ev && mem == GWF_MEM_HOST; ++j)
-      if (res_ev[j] < 1) return fail(GWF_ERR_INVALID_ARG, "res_per_event must be >= 1");
+  for (int j = 0; j < N && res_ev && mem == GWF_MEM_HOST; ++j)
+    if (res_ev[j] < 1) return fail(GWF_ERR_INVALID_ARG, "res_per_event must be >= 1");
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  // CUDA graphs: device-resident Fisher calls without a host round trip are captured on their
+  // second identical call and replayed afterwards
+  if (ctx->graphs && fisher && mem == GWF_MEM_DEVICE && precision != GWF_PREC_MIXED) {
+    std::string key = graph_key(n_det, det_ids, wf, params, ld, N, res, res_ev, spacing, per_arm, precision,
+                                out_arm, out_net, st);
+    const std::string bufs = buffer_sig(ctx);
+    auto it = ctx->graph_cache.find(key);
+    if (it != ctx->graph_cache.end() && it->second.bufs == bufs) {
+      GWF_CK(cudaStreamWaitEvent(st, ctx->scratch_free, 0));
+      GWF_CK(cudaGraphLaunch(it->second.exec, st));
+      GWF_CK(cudaEventRecord(ctx->scratch_free, st));
+      return GWF_OK;
+    }
+    if (it != ctx->graph_cache.end()) {   // buffers were reallocated since the capture
+      cudaGraphExecDestroy(it->second.exec);
+      ctx->graph_cache.erase(it);
+    }
+    if (key == ctx->graph_pending) {
+      GWF_CK(cudaStreamWaitEvent(st, ctx->scratch_free, 0));
+      cudaGraph_t graph = nullptr;
+      GWF_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+      rc = run_body(ctx, fisher, n_det, det_ids, wf, params, ld, N, res, res_ev, spacing, per_arm, precision, mem,
+                    out_arm, out_net, st, true);
+      const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+      if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+      if (ce != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+      cudaGraphExec_t exec = nullptr;
+      const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ie != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+      if (ctx->graph_cache.size() >= 16) {
+        cudaGraphExecDestroy(ctx->graph_cache.begin()->second.exec);
+        ctx->graph_cache.erase(ctx->graph_cache.begin());
+      }
+      ctx->graph_cache[key] = GraphEntry{exec, buffer_sig(ctx)};
+      ctx->graph_pending.clear();
+      GWF_CK(cudaGraphLaunch(exec, st));
+      GWF_CK(cudaEventRecord(ctx->scratch_free, st));
+      return GWF_OK;
+    }
+    ctx->graph_pending = key;
+  }
+  return run_body(ctx, fisher, n_det, det_ids, wf, params, ld, N, res, res_ev, spacing, per_arm, precision, mem,
+                  out_arm, out_net, st, false);
+}
+
+// the launches of one call; capturing: inside a stream capture (no host round trips, no
+// ordering events: the caller orders the graph launch)
+int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params,
+             int64_t ld, int64_t N, int32_t res, const int32_t* res_ev, int spacing, int per_arm, int precision,
+             int mem, double* out_arm, double* out_net, cudaStream_t st, bool capturing) {
+  int rc = GWF_OK;
   const double* dp;
   int64_t dld;
   const int* dres;
@@ -321,13 +409,15 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
   const size_t chunk = (size_t)(N < gwf::kChunk ? N : gwf::kChunk);
   if (ctx->setup.ensure(chunk * stride)) return fail(GWF_ERR_OOM, "device allocation failed (set-up scratch)");
   // the scratch is shared by every call on this context: order this call after the previous one
-  GWF_CK(cudaStreamWaitEvent(st, ctx->scratch_free, 0));
+  if (!capturing) GWF_CK(cudaStreamWaitEvent(st, ctx->scratch_free, 0));
   gwf::LaunchArgs a;
   a.scratch = (unsigned char*)ctx->setup.p;
   a.cap_events = (long long)chunk;
   if (fisher && ctx->seg_points > 0) {
     int64_t rmax = 0;
-    rc = max_res(res, res_ev, N, mem, &rmax);
+    if (capturing && res_ev) rmax = ctx->graph_rmax;   // from the uncaptured run of the same call
+    else rc = max_res(res, res_ev, N, mem, &rmax);
+    ctx->graph_rmax = rmax;
     if (!rc) rc = seg_setup(ctx, a, ctx->seg_points, (int64_t)chunk, rmax, st);
     if (rc) return rc;
   }
@@ -363,7 +453,7 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
     rc = refine(ctx, n_det, det_ids, a, dp, dld, dres, N, slots, darm, dnet, st);
     if (rc) return rc;
   }
-  GWF_CK(cudaEventRecord(ctx->scratch_free, st));
+  if (!capturing) GWF_CK(cudaEventRecord(ctx->scratch_free, st));
   if (mem == GWF_MEM_HOST) {
     if (out_arm) GWF_CK(cudaMemcpyAsync(out_arm, darm, (size_t)slots * N * per * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (out_net) GWF_CK(cudaMemcpyAsync(out_net, dnet, (size_t)N * per * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -419,6 +509,8 @@ int gwf_ctx_destroy(gwf_ctx* ctx) {
   ctx->mix_net.release(); ctx->mix_arm.release();
   ctx->seg_off.release(); ctx->seg_ctr.release(); ctx->seg_part.release(); ctx->seg_ovf.release();
   ctx->tune_out.release();
+  for (auto& g : ctx->graph_cache) cudaGraphExecDestroy(g.second.exec);
+  ctx->graph_cache.clear();
   ctx->hpar.release(); ctx->hout.release();
   cudaEventDestroy(ctx->scratch_free);
   cudaStreamDestroy(ctx->stream);
@@ -513,6 +605,18 @@ int gwf_set_refine_cond(gwf_ctx* ctx, double kappa) {
   if (!ctx) return fail(GWF_ERR_INVALID_ARG, "null context");
   if (!(kappa > 0.0)) return fail(GWF_ERR_INVALID_ARG, "refinement threshold must be positive");
   ctx->refine_cond = kappa;
+  return GWF_OK;
+}
+
+int gwf_set_graphs(gwf_ctx* ctx, int on) {
+  if (!ctx) return fail(GWF_ERR_INVALID_ARG, "null context");
+  GWF_CK(cudaSetDevice(ctx->device));
+  ctx->graphs = on ? 1 : 0;
+  if (!on) {
+    for (auto& g : ctx->graph_cache) cudaGraphExecDestroy(g.second.exec);
+    ctx->graph_cache.clear();
+    ctx->graph_pending.clear();
+  }
   return GWF_OK;
 }
 

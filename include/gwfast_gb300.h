@@ -121,6 +121,15 @@ int gwf_set_refine_cond(gwf_ctx* ctx, double kappa);
  * (res_per_event) keep every SM busy this way. */
 int gwf_set_segments(gwf_ctx* ctx, int points);
 
+/* CUDA graphs for device-resident calls (no counterpart in gwfast). on != 0: a gwf_fisher call with
+ * mem = GWF_MEM_DEVICE and precision FP64 or FP32 is captured into a CUDA graph the second time the
+ * same call (same arguments, pointers and stream included) is made, and later identical calls
+ * replay the graph: one launch instead of the per-chunk set-up, scan, persistent and reduction
+ * launches of every detector. The inputs behind the pointers may change between calls. A graph
+ * is dropped when the context's buffers are reallocated. GWF_PREC_MIXED calls read a count back
+ * to the host and are never captured. */
+int gwf_set_graphs(gwf_ctx* ctx, int on);
+
 /* Autotuner for gwf_set_segments: runs the given workload (typically a sample of the catalogue)
  * as gwf_fisher would, with each candidate segment length (0 = per event, 256, 512, 1024, 2048),
  * times each with CUDA events (one warm-up and two timed runs), keeps the fastest in the context

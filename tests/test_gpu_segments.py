@@ -111,3 +111,38 @@ def test_autotune_segments(gpu_lib):
     F0 = np.moveaxis(net.FisherMatr(dict(ev), res=int(res.max()), res_per_event=res), -1, 0)
     print('autotuned segment length', best)
     assert norm_err(F1, F0).max() < 1e-12
+
+
+@pytest.mark.parametrize('seg', [0, 512])
+def test_graph_capture_and_replay(gpu_lib, seg):
+    """Device-resident calls: the second identical call is captured into a CUDA graph, later ones
+    replay it; new parameter values in the same buffers must show up in the replayed results."""
+    torch = pytest.importorskip('torch')
+    from gwfast_gb300.signal import event_array
+    net = synthetic.make_network(W.IMRPhenomD(), earth=True)
+    ids = [s.det_id for s in net.signals.values()]
+    desc = W.IMRPhenomD().gpu_desc()
+    n = 128
+    ctx = _lib.context(0)
+    st = torch.cuda.Stream()
+    p_dev = torch.empty((11, n), dtype=torch.float64, device='cuda')
+    out = torch.empty((n, 11, 11), dtype=torch.float64, device='cuda')
+    ref = torch.empty((n, 11, 11), dtype=torch.float64, device='cuda')
+    ctx.set_segments(seg)
+    try:
+        for call, seed in enumerate((101, 102, 103, 104)):
+            p_dev.copy_(torch.from_numpy(event_array(synthetic.bbh_events(n, seed=seed))))
+            for prec in ('fp64', 'fp32'):
+                ctx.set_graphs(False)
+                ctx.fisher(ids, desc, p_dev, 1000, mem=_lib.MEM_DEVICE, out_net=ref, stream=st.cuda_stream, ld=n, n=n,
+                           precision=prec)
+                ctx.set_graphs(True)
+                for _ in range(3):   # plain run, capture, replay
+                    ctx.fisher(ids, desc, p_dev, 1000, mem=_lib.MEM_DEVICE, out_net=out, stream=st.cuda_stream,
+                               ld=n, n=n, precision=prec)
+                st.synchronize()
+                err = norm_err(out.cpu().numpy(), ref.cpu().numpy()).max()
+                assert err < 1e-12, (call, prec, err)
+    finally:
+        ctx.set_graphs(False)
+        ctx.set_segments(0)
