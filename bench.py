@@ -40,6 +40,7 @@ sys.path.insert(0, ROOT)
 
 N_EVENTS = 10000
 RES = 2000
+SNR_TH = 12.
 METRIC = 'network Fisher matrices/s (IMRPhenomD, L1+H1+ETS, Earth rotation, R=2000)'
 
 
@@ -164,6 +165,85 @@ def gemm_peak(torch, dev, dtype, n):
     return 2 * n ** 3 / best / 1e12
 
 
+def run_mixed_catalogue(args):
+    """Batching workload: 50 % BNS + 50 % BBH, per-event grid lengths from the chirp time at 2 Hz
+    (200 to 40000 points), L1 + H1 (10 Hz) + ET triangle (2 Hz wall), IMRPhenomD, Earth rotation.
+    Times the per-event launches against the autotuned persistent segmented launches (CUDA-graph
+    replay for the device-resident FP64 and FP32 forms) and the mixed form."""
+    import torch
+    from gwfast_gb300 import _build, _lib, synthetic
+    from gwfast_gb300 import waveforms as W
+    from gwfast_gb300.signal import event_array
+    _build.build()
+    dev = torch.device('cuda', 0)
+    N = args.events
+    ev = synthetic.mixed_events(N, seed=1002)
+    res_ev = synthetic.res_from_chirp_time(ev['Mc'], 2.)
+    rmax = int(res_ev.max())
+    wf = W.IMRPhenomD()
+    net = synthetic.make_network(wf, dets=synthetic.NETWORK_LHET2, earth=True)
+    ids = [s.det_id for s in net.signals.values()]
+    ctx = _lib.context(0)
+    p_dev = torch.from_numpy(event_array(ev)).to(dev)
+    r_dev = torch.from_numpy(np.ascontiguousarray(res_ev, dtype=np.int32)).to(dev)
+    out = torch.empty((N, 11, 11), dtype=torch.float64, device=dev)
+    snr_out = torch.empty((N,), dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    desc = wf.gpu_desc()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+
+    def step(precision):
+        ctx.fisher(ids, desc, p_dev, rmax, res_ev=r_dev, per_arm=False, mem=_lib.MEM_DEVICE, out_net=out,
+                   stream=stream.cuda_stream, ld=N, n=N, precision=precision)
+
+    def timed(fn, k, warm):
+        for _ in range(warm):
+            fn()
+        tot = 0.0
+        for _ in range(k):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot / k
+
+    forms = {}
+    ctx.set_graphs(False)
+    for prec in ('fp64', 'fp32'):
+        ctx.set_segments(0)
+        forms[prec + '_per_event'] = timed(lambda: step(prec), args.steps, args.warmup)
+        ns = min(N, 2000)
+        seg = ctx.autotune_segments(ids, desc, p_dev, rmax, res_ev=r_dev, precision=prec, mem=_lib.MEM_DEVICE,
+                                    ld=N, n=ns)
+        ctx.set_graphs(True)
+        forms[prec + '_segmented_graph'] = timed(lambda: step(prec), args.steps, args.warmup)
+        forms[prec + '_segment_points'] = seg
+        ctx.set_graphs(False)
+    forms['mixed_segmented'] = timed(lambda: step('mixed'), args.steps, args.warmup)
+    ctx.set_segments(0)
+    ms_snr = timed(lambda: ctx.snr(ids, desc, p_dev, rmax, res_ev=r_dev, mem=_lib.MEM_DEVICE, out_net=snr_out,
+                                   stream=stream.cuda_stream, ld=N, n=N), args.steps, args.warmup)
+    line = {
+        'metric': 'network Fisher matrices/s, mixed BNS+BBH catalogue (per-event grids 200-40000 points)',
+        'value': N / (forms['mixed_segmented'] / 1e3), 'unit': 'Fisher/s', 'n_gpus': 1, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': forms['mixed_segmented'], 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f32 per point, f64 for events with cond > %.0e' % args.refine_cond,
+        'data': 'synthetic (seeded mixed catalogue)',
+        'config': {'workload': 'IMRPhenomD, %d events (50%% BNS, 50%% BBH), L1+H1 (10 Hz) + ETS (2 Hz), Earth rotation, '
+                               'per-event res from chirp time' % N, 'res_min': int(res_ev.min()), 'res_max': rmax,
+                   'points_total': int(res_ev.sum()), 'l2': 'flushed (256 MB write) before every step'},
+        'forms_ms_per_step': forms,
+        'fisher_per_s': {k: N / (v / 1e3) for k, v in forms.items() if not k.endswith('points')},
+        'speedup_vs_fp64_per_event': forms['fp64_per_event'] / forms['mixed_segmented'],
+        'snr_per_s': N / (ms_snr / 1e3),
+    }
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -177,9 +257,13 @@ def main():
     ap.add_argument('--precision', default='fp32', choices=('fp32', 'fp64', 'mixed'), help='form used with --only-device')
     ap.add_argument('--refine-cond', type=float, default=1e11, help='condition-number threshold of the mixed form')
     ap.add_argument('--no-autotune', action='store_true', help='per-event launches, no segment autotuning')
+    ap.add_argument('--workload', default='lhet', choices=('lhet', 'mixed-catalogue'),
+                    help='lhet: the headline workload; mixed-catalogue: the batching workload (separate line)')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
+    if args.workload == 'mixed-catalogue':
+        return run_mixed_catalogue(args)
     rank, world, local = dist_info()
     import torch
     if world > 1:
@@ -297,7 +381,7 @@ def main():
 
     serr_mixed = sig_err(Fm_all)
     serr_fp32 = sig_err(out32.cpu().numpy())
-    # end to end through the public API with host buffers
+    # end to end through the public API with host buffers: DetNet.FisherMatr (mixed form) on every event
     for _ in range(max(1, args.warmup // 2)):
         net.FisherMatr(dict(ev), res=RES, precision='mixed', refine_cond=args.refine_cond)
     torch.cuda.synchronize()
@@ -305,6 +389,21 @@ def main():
     for _ in range(args.steps):
         F_host = net.FisherMatr(dict(ev), res=RES, precision='mixed', refine_cond=args.refine_cond)
     e2e_s = (time.perf_counter() - t0) / args.steps
+    # the forecast pipeline: SNR pass (FP32) on every event, threshold SNR > 12, network Fisher of the
+    # detected events (mixed form), covariances; Fisher/s = detected events / wall time of SNR + Fisher
+    from gwfast_gb300 import pipeline
+    for _ in range(max(1, args.warmup // 2)):
+        pipeline.compute_errs(net, dict(ev), snr_th=SNR_TH, res=RES, precision='mixed', refine_cond=args.refine_cond)
+    torch.cuda.synchronize()
+    pipe_t, cov_t, ndet = 0.0, 0.0, 0
+    for _ in range(args.steps):
+        tm = {}
+        r = pipeline.compute_errs(net, dict(ev), snr_th=SNR_TH, res=RES, precision='mixed',
+                                  refine_cond=args.refine_cond, timings=tm)
+        pipe_t += tm['snr'] + tm['fisher']
+        cov_t += tm['cov']
+        ndet = int(r['detected'].sum())
+    pipe_s = pipe_t / args.steps
     if rank != 0:
         torch.distributed.destroy_process_group()
         return
@@ -335,7 +434,14 @@ def main():
         'snr_per_s': world * N / (ms_snr / 1e3),
         'gpu_launches': 6 + 2 + (8 if refined > 0 else 0),
         'e2e': {'value': world * N / e2e_s, 'unit': 'Fisher/s', 'h2d_bytes_per_step': int(p_host.nbytes),
-                'd2h_bytes_per_step': int(F_host.nbytes)},
+                'd2h_bytes_per_step': int(F_host.nbytes),
+                'what': 'DetNet.FisherMatr(precision=mixed) on a host events dict, host (11, 11, N) out, wall clock'},
+        'forecast_pipeline': {'value': world * ndet / pipe_s, 'unit': 'Fisher/s', 'detected': ndet, 'events': N,
+                              'snr_plus_fisher_s': pipe_s, 'covariance_s': cov_t / args.steps,
+                              'what': 'pipeline.compute_errs: DetNet.SNR (FP32) on every event, threshold SNR > %g, '
+                                      'DetNet.FisherMatr (mixed) on the detected ones; Fisher/s = detected / wall '
+                                      'time of SNR + Fisher (host dict in, host arrays out)' % SNR_TH,
+                              'h2d_bytes': int(8 * 11 * (N + ndet)), 'd2h_bytes': int(8 * (5 * N + 121 * ndet))},
         'roofline': {'bound': 'fp32', 'kernel': 'fisher_kernel_f32<IMRPhenomD, earth, triangle>',
                      'achieved': ach, 'peak': peak32, 'unit': 'TFLOP/s', 'frac': ach / peak32,
                      'peak_source': 'cuBLAS SGEMM 8192^3 (TF32 off) measured in this run',

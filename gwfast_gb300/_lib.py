@@ -45,7 +45,7 @@ SIGNATURES = {
     'gwf_set_qnm_table': ([_vp, _vp, _vp, _vp, _i64], ctypes.c_int),
     'gwf_detector_add': ([_vp, _P(DetDesc), _vp, _vp, _i64, _P(ctypes.c_int)], ctypes.c_int),
     'gwf_snr': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32, _vp, ctypes.c_int,
-                 ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
+                 ctypes.c_int, ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
     'gwf_fisher': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32, _vp, ctypes.c_int,
                     ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
     'gwf_cov': ([_vp, _vp, _i64, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
@@ -132,12 +132,12 @@ class Context:
         return out.value
 
     def snr(self, det_ids, wf, params, res, res_ev=None, spacing=0, mem=MEM_HOST, out_arm=None, out_net=None,
-            stream=None, ld=None, n=None):
+            stream=None, ld=None, n=None, precision='fp64'):
         ids = np.ascontiguousarray(det_ids, dtype=np.int32)
         n = params.shape[1] if n is None else n
         ld = (params.shape[1] if ld is None else ld)
         check(load().gwf_snr(self.h, len(ids), ptr(ids), ctypes.byref(wf), ptr(params), ld, n, int(res),
-                             ptr(res_ev), spacing, mem, ptr(out_arm), ptr(out_net), stream))
+                             ptr(res_ev), spacing, PRECISION[precision], mem, ptr(out_arm), ptr(out_net), stream))
 
     def fisher(self, det_ids, wf, params, res, res_ev=None, spacing=0, per_arm=False, mem=MEM_HOST, out_arm=None,
                out_net=None, stream=None, ld=None, n=None, precision='fp64'):

@@ -318,8 +318,9 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
   if (!out_arm && !out_net) return fail(GWF_ERR_INVALID_ARG, "no output requested");
   if (precision != GWF_PREC_FP64 && precision != GWF_PREC_FP32 && precision != GWF_PREC_MIXED)
     return fail(GWF_ERR_INVALID_ARG, "bad precision");
-  if (precision != GWF_PREC_FP64 && (!fisher || wf->model == GWF_WF_PHENOMHM))
-    return fail(GWF_ERR_UNSUPPORTED, "FP32 split precision is implemented for the TaylorF2 and IMRPhenomD Fisher");
+  if (precision != GWF_PREC_FP64 && wf->model == GWF_WF_PHENOMHM)
+    return fail(GWF_ERR_UNSUPPORTED, "FP32 split precision is implemented for TaylorF2 and IMRPhenomD");
+  if (precision == GWF_PREC_MIXED && !fisher) return fail(GWF_ERR_INVALID_ARG, "the mixed form is a Fisher form");
   if (fisher && !per_arm) out_arm = nullptr;
   if (fisher && per_arm && !out_arm) return fail(GWF_ERR_INVALID_ARG, "per_arm needs out_arm");
   if (N == 0) return GWF_OK;
@@ -588,9 +589,9 @@ int gwf_detector_add(gwf_ctx* ctx, const gwf_det_desc* desc, const double* psd_f
 }
 
 int gwf_snr(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params, int64_t ld,
-            int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int mem, double* out_arm,
-            double* out_net, void* stream) {
-  return run(ctx, false, n_det, det_ids, wf, params, ld, n_events, res, res_per_event, spacing, 0, GWF_PREC_FP64, mem,
+            int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int precision, int mem,
+            double* out_arm, double* out_net, void* stream) {
+  return run(ctx, false, n_det, det_ids, wf, params, ld, n_events, res, res_per_event, spacing, 0, precision, mem,
              out_arm, out_net, stream);
 }
 

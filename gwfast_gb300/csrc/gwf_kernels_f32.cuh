@@ -410,6 +410,45 @@ __device__ inline void f32_prepare(const unsigned char* scratch32, long long rec
   __syncthreads();
 }
 
+// FP32 frequency grid of one event, traversed by a block of kThreads in steps of kThreads points
+// (warp w takes points base + 32 w + lane). Geometric grid: f_k = f_tile exp(lane delta),
+// ln f_k = ln f_tile + lane delta, with the tile anchors formed in FP64; each lane computes the
+// anchor of one of the warp's next 32 tiles, and the tiles read them by shuffle.
+struct GridIterF {
+  float anc_f = 0.0f, anc_l = 0.0f;
+  int it0 = -1000000;
+  // call once per step, by all lanes of the warp; returns the point's f, ln f and trapezoid weight
+  template <int MODEL>
+  __device__ __forceinline__ void step(const F32Rec<MODEL>& r, int spacing, int base, int lane, int warp) {
+    const int it = base / kThreads;
+    if (spacing == 0 && it - it0 >= 32) {
+      it0 = it;
+      const double l = r.lnfmin + (double)(((long long)(it + lane) * kWarps + warp) * 32) * r.delta;
+      anc_f = (float)exp(l);
+      anc_l = (float)l;
+    }
+    ftile = __shfl_sync(0xffffffffu, anc_f, (it - it0) & 31);
+    ltile = __shfl_sync(0xffffffffu, anc_l, (it - it0) & 31);
+  }
+  template <int MODEL>
+  __device__ __forceinline__ void point(const F32Rec<MODEL>& r, int spacing, int k, int lane, float& f, float& lnf,
+                                        float& w) const {
+    const GridF& gf = r.gf;
+    const int R = gf.R;
+    if (spacing == 0) {
+      lnf = fmaf((float)lane, gf.delta, ltile);
+      if (k == R - 1) { f = gf.fcut; w = f * gf.wl; }
+      else if (k == 0) { f = gf.fmin; w = f * gf.w0; }
+      else { f = ftile * expf((float)lane * gf.delta); w = f * gf.fac_w; }
+    } else {
+      f = (k == R - 1) ? gf.fcut : gf.fmin + (float)k * gf.df;
+      lnf = logf(f);
+      w = (k == 0 || k == R - 1) ? 0.5f * gf.df : gf.df;
+    }
+  }
+  float ftile = 0.0f, ltile = 0.0f;
+};
+
 // Gram of points [k0, k1) (k0 a multiple of kThreads) into S.gsum, summed over warps
 template <int MODEL, bool EARTH, int NARM, int NG>
 __device__ inline void f32_item(const EvBatch& ev, const DetDev& det, F32State<MODEL, NG>& S, int2* stage, int k0, int k1) {
@@ -433,38 +472,17 @@ __device__ inline void f32_item(const EvBatch& ev, const DetDev& det, F32State<M
   for (int i = lane; i < gram_slots<NG>() * NQ * NQ; i += 32) (&fl[warp][0][0][0])[i] = 0.0;
   if (lane == 0) S.badw[warp] = 0;
   int par = 0, tiles = 0;
-  float anc_f = 0.0f, anc_l = 0.0f;
-  int it0 = -1000000;
+  GridIterF grid;
   bool moved = false, bad = false;
   __syncwarp();
-  const int R = gf.R;
   for (int base = k0; base < k1; base += kThreads) {
     const int k = base + tid;
     cf D[NARM][NP];
     float sw = 0.0f;
-    // geometric grid: f_k = f_tile * exp(lane * delta), ln f_k = ln f_tile + lane * delta, with the
-    // tile anchors formed in FP64: each lane computes the anchor of one of the warp's next 32 tiles
-    const int it = base / kThreads;
-    if (ev.spacing == 0 && it - it0 >= 32) {
-      it0 = it;
-      const double l = r.lnfmin + (double)(((long long)(it + lane) * kWarps + warp) * 32) * r.delta;
-      anc_f = (float)exp(l);
-      anc_l = (float)l;
-    }
-    const float ftile = __shfl_sync(0xffffffffu, anc_f, (it - it0) & 31);
-    const float ltile = __shfl_sync(0xffffffffu, anc_l, (it - it0) & 31);
+    grid.step(r, ev.spacing, base, lane, warp);
     if (k < k1) {
       float f, lnf, w;
-      if (ev.spacing == 0) {
-        lnf = fmaf((float)lane, gf.delta, ltile);
-        if (k == R - 1) { f = gf.fcut; w = f * gf.wl; }
-        else if (k == 0) { f = gf.fmin; w = f * gf.w0; }
-        else { f = ftile * expf((float)lane * gf.delta); w = f * gf.fac_w; }
-      } else {
-        f = (k == R - 1) ? gf.fcut : gf.fmin + (float)k * gf.df;
-        lnf = logf(f);
-        w = (k == 0 || k == R - 1) ? 0.5f * gf.df : gf.df;
-      }
+      grid.point(r, ev.spacing, k, lane, f, lnf, w);
       const float Sn = psd_at_f(det, f, lnf, gf.acc_l0, gf.acc_idl);
       sw = sqrtf(4.0f * w / Sn);
       point_f32<MODEL, EARTH, NARM>(r.ef, r.pbf, r.pf, r.apc, r.tsc, f, lnf, D);
@@ -593,6 +611,93 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_seg_kernel_f32(EvBatch ev,
     f32_item<MODEL, EARTH, NARM, NG>(ev, det, S, reinterpret_cast<int2*>(stage_raw), k0, k1);
     double* o = si.partial + item * (NG * NE);
     for (int e = threadIdx.x; e < NG * NE; e += blockDim.x) o[e] = S.gsum[e];
+  }
+}
+
+// ------------------------------------------------------------------ FP32 SNR
+// Per arm: scale * sum_k w_k / S_k * A_k^2 ((cp F+)^2 + (ci Fx)^2) with A, the pattern functions and
+// the Earth-rotation time in FP32; each thread sums its points with Kahan compensation, the block
+// sums in FP64. Outputs as snr_kernel.
+template <int MODEL, bool EARTH, int NARM>
+__global__ void __launch_bounds__(kThreads) snr_kernel_f32(EvBatch ev, DetDev det, const unsigned char* scratch32,
+                                                           double* out_arm, double* out_det, int accum) {
+  __shared__ F32Rec<MODEL> r;
+  __shared__ double red[kWarps][3];
+  const long long n = ev.n0 + blockIdx.x;
+  if (n >= ev.N) return;
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(scratch32 + (size_t)blockIdx.x * f32_stride<MODEL>());
+    uint4* dst = reinterpret_cast<uint4*>(&r);
+    for (int i = threadIdx.x; i < (int)(sizeof(F32Rec<MODEL>) / 16); i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int NA = NARM == 2 ? 3 : 1;
+  float sum[NA], cmp[NA];
+#pragma unroll
+  for (int a = 0; a < NA; ++a) { sum[a] = 0.0f; cmp[a] = 0.0f; }
+  const int R = r.gf.R;
+  GridIterF grid;
+  for (int base = 0; base < R; base += kThreads) {
+    const int k = base + tid;
+    grid.step(r, ev.spacing, base, lane, warp);
+    if (k >= R) continue;
+    float f, lnf, w;
+    grid.point(r, ev.spacing, k, lane, f, lnf, w);
+    const float ws = w / psd_at_f(det, f, lnf, r.gf.acc_l0, r.gf.acc_idl);
+    float A;
+    TimeF ts;
+    if (MODEL == 0) {
+      const float f13 = cbrtf(f);
+      A = r.ef.tf2.ampK.v * (1.0f / (f * sqrtf(f13)));
+      if (EARTH) time_f(r.pf, -tau_star_point<float>(r.ef.tf2.Ms, r.ef.tf2.vM, r.ef.tf2.eta, f13) * (1.0f / 86400.0f), ts);
+    } else {
+      A = phd_amp_point<float>(r.ef.phd, f);
+      if (EARTH) time_f(r.pf, -tau_star_point<float>(r.ef.phd.Ms, r.ef.phd.vM, r.ef.phd.eta, cbrtf(f)) * (1.0f / 86400.0f), ts);
+    }
+    const float ap = A * r.pf.cp, ac = A * r.pf.ci;
+    float p[2], c[2];
+#pragma unroll
+    for (int a = 0; a < NARM; ++a) {
+      ArmF pat;
+      if (EARTH) arm_f(r.pf, ts, a, pat);
+      else pat = r.apc[a];
+      p[a] = ap * pat.Fp;
+      c[a] = ac * pat.Fc;
+    }
+    float term[NA];
+    term[0] = ws * (p[0] * p[0] + c[0] * c[0]);
+    if (NARM == 2) {
+      term[1] = ws * (p[1] * p[1] + c[1] * c[1]);
+      const float p3 = p[0] + p[1], c3 = c[0] + c[1];
+      term[2] = ws * (p3 * p3 + c3 * c3);
+    }
+#pragma unroll
+    for (int a = 0; a < NA; ++a) {   // Kahan
+      const float y = term[a] - cmp[a];
+      const float t = sum[a] + y;
+      cmp[a] = (t - sum[a]) - y;
+      sum[a] = t;
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < NA; ++a) {
+    double v = (double)sum[a] - (double)cmp[a];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp][a] = v;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double tot = 0.0;
+    for (int a = 0; a < NA; ++a) {
+      double v = 0.0;
+      for (int w = 0; w < kWarps; ++w) v += red[w][a];
+      v *= r.scale;
+      if (out_arm) out_arm[(size_t)a * ev.N + n] = v;
+      tot += 4.0 * v;
+    }
+    if (out_det) out_det[n] = accum ? out_det[n] + tot : tot;
   }
 }
 

@@ -156,8 +156,28 @@ cudaError_t fisher_dispatch(const LaunchArgs& a) {
   return a.per_arm ? fisher_one<false, 2, 3>(a) : fisher_one<false, 2, 2>(a);
 }
 
+#if GWF_MODEL < 2
+template <bool EARTH, int NARM>
+cudaError_t snr_one_f32(const LaunchArgs& a) {
+  unsigned char* s32 = scratch32_of(a);
+  return chunked(a, true, [&](const EvBatch& ev, long long cnt) {
+    snr_kernel_f32<M, EARTH, NARM><<<(unsigned)cnt, kThreads, 0, a.stream>>>(ev, a.det, s32, a.out_arm, a.out_det,
+                                                                              a.accum);
+    return cudaSuccess;
+  });
+}
+#endif
+
 cudaError_t snr_dispatch(const LaunchArgs& a) {
   const bool tri = a.det.shape == 1;
+  if (a.precision == 1) {
+#if GWF_MODEL < 2
+    if (a.det.earth) return tri ? snr_one_f32<true, 2>(a) : snr_one_f32<true, 1>(a);
+    return tri ? snr_one_f32<false, 2>(a) : snr_one_f32<false, 1>(a);
+#else
+    return cudaErrorNotSupported;
+#endif
+  }
   if (a.det.earth) return tri ? snr_one<true, 2>(a) : snr_one<true, 1>(a);
   return tri ? snr_one<false, 2>(a) : snr_one<false, 1>(a);
 }

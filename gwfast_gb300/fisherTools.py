@@ -20,14 +20,23 @@ def CovMatr(FisherMatrix, invMethodIn='cho', condNumbMax=1e50, truncate=False, s
     if truncate:
         raise NotImplementedError('singular-value truncation is not implemented on the GPU path')
     F = np.ascontiguousarray(np.moveaxis(np.asarray(FisherMatrix, dtype=np.float64), -1, 0))
-    if F.shape[1:] != (11, 11):
-        raise NotImplementedError('the GPU inversion handles 11x11 matrices')
+    P = F.shape[1]
+    if F.shape[1:] != (P, P) or P > 11:
+        raise NotImplementedError('the GPU inversion handles up to 11x11 matrices')
+    if P < 11:
+        # block-diagonal embedding with an identity block (e.g. after fixParams): the inverse of
+        # the leading block is the leading block of the inverse; an equilibrated matrix has
+        # eigenvalues on both sides of 1, so the condition number is unchanged, and the identity
+        # block adds no inversion error
+        Fp = np.broadcast_to(np.eye(11), (F.shape[0], 11, 11)).copy()
+        Fp[:, :P, :P] = F
+        F = Fp
     N = F.shape[0]
     cov = np.empty_like(F)
     eps = np.empty(N)
     cond = np.empty(N)
     _lib.context(device).cov(F, cov=cov, eps=eps, cond=cond)
-    out = np.moveaxis(cov, 0, -1)
+    out = np.moveaxis(np.ascontiguousarray(cov[:, :P, :P]), 0, -1)
     if return_cond:
         return out, eps, cond
     return out, eps
@@ -47,3 +56,28 @@ def CheckFisher(FisherM, condNumbMax=1.0e15, use_mpmath=True, verbose=False):
     if verbose and np.any(cond > condNumbMax):
         print('WARNING: the condition number is too large at positions %s' % np.where(cond > condNumbMax)[0])
     return evals, evecs, cond
+
+
+def fixParams(MatrIn, ParNums_inp, ParMarg):
+    """Drop the rows and columns of the fixed parameters (gwfast/fisherTools.py:340-375).
+
+    MatrIn: (P, P, N). Returns the reduced (P', P', N) matrices and the renumbered ParNums."""
+    drop = sorted(ParNums_inp[p] for p in ParMarg)
+    out = np.delete(np.delete(np.asarray(MatrIn), drop, axis=0), drop, axis=1)
+    keep = sorted((i, k) for k, i in ParNums_inp.items() if k not in ParMarg)
+    return out, {k: j for j, (_, k) in enumerate(keep)}
+
+
+def compute_localization_region(Cov, parNum, thFid, perc_level=90, units='SqDeg'):
+    """Sky area of the perc_level credible ellipse from the (theta, phi) covariance block
+    (gwfast/fisherTools.py:830-866; Barack & Cutler, PRD 69, 082005, 2004):
+    dOmega = -2 pi |sin theta| sqrt(C_thth C_phph - C_thph^2) ln(1 - perc_level / 100)."""
+    cth = Cov[parNum['theta'], parNum['theta']]
+    cph = Cov[parNum['phi'], parNum['phi']]
+    cx = Cov[parNum['phi'], parNum['theta']]
+    area = -2. * np.pi * np.sqrt(cth * cph - cx ** 2) * np.abs(np.sin(thFid)) * np.log(1. - perc_level / 100.)
+    if units == 'Sterad':
+        return area
+    if units == 'SqDeg':
+        return (180. / np.pi) ** 2 * area
+    raise ValueError("units must be 'SqDeg' or 'Sterad'")

@@ -26,11 +26,11 @@ class DetNet:
         for i, d in enumerate(self.signals):
             self.signals[d]._update_seed(seed=seeds[i])
 
-    def SNR(self, evParams, res=1000, return_all=False):
-        """Network SNR (gwfast/network.py:278-306)."""
+    def SNR(self, evParams, res=1000, return_all=False, precision='fp64', res_per_event=None):
+        """Network SNR (gwfast/network.py:278-306); precision='fp32' selects the FP32 SNR kernel."""
         utils.check_evparams(evParams)
         names, sigs = self._list()
-        arms = snr_batch(sigs, evParams, res, device=sigs[0].device)
+        arms = snr_batch(sigs, evParams, res, device=sigs[0].device, precision=precision, res_per_event=res_per_event)
         snrs = {}
         for name, s, a in zip(names, sigs, arms):
             if s.detector_shape == 'T' and return_all:

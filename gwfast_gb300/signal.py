@@ -34,17 +34,20 @@ def _arm_slots(signals):
     return [1 if s.detector_shape == 'L' else 3 for s in signals]
 
 
-def snr_batch(signals, evParams, res=1000, device=0):
-    """Per-arm SNRs of all signals in one library call.  Returns a list (per signal) of (arms, N) arrays."""
+def snr_batch(signals, evParams, res=1000, device=0, precision='fp64', res_per_event=None):
+    """Per-arm SNRs of all signals in one library call.  Returns a list (per signal) of (arms, N) arrays.
+
+    precision: 'fp64' or 'fp32' (TaylorF2 and IMRPhenomD); res_per_event as in fisher_batch."""
     p = _prep(evParams)
     wf = signals[0].wf_model
     if any(type(s.wf_model) is not type(wf) for s in signals):
-        return [s._snr_arms(evParams, res) for s in signals]
+        return [s._snr_arms(evParams, res, precision) for s in signals]
     N = p.shape[1]
     slots = _arm_slots(signals)
     out = np.empty((sum(slots), N))
     ctx = _lib.context(device)
-    ctx.snr([s.det_id for s in signals], wf.gpu_desc(), p, res, out_arm=out)
+    rev = None if res_per_event is None else np.ascontiguousarray(np.broadcast_to(res_per_event, (N,)), dtype=np.int32)
+    ctx.snr([s.det_id for s in signals], wf.gpu_desc(), p, res, res_ev=rev, out_arm=out, precision=precision)
     res_l, i = [], 0
     for s, k in zip(signals, slots):
         arms = 2. * np.sqrt(out[i:i + k])
@@ -175,12 +178,12 @@ class GWSignal:
             out[a] = out[a] * excl.reshape((n,) + (1,) * (out.ndim - 2))
         return out
 
-    def _snr_arms(self, evParams, res):
-        return snr_batch([self], evParams, res, self.device)[0]
+    def _snr_arms(self, evParams, res, precision='fp64'):
+        return snr_batch([self], evParams, res, self.device, precision=precision)[0]
 
-    def SNRInteg(self, evParams, res=1000, return_all=False):
-        """gwfast/signal.py:658-777."""
-        arms = self._snr_arms(evParams, res)
+    def SNRInteg(self, evParams, res=1000, return_all=False, precision='fp64'):
+        """gwfast/signal.py:658-777; precision='fp32' selects the FP32 SNR kernel."""
+        arms = self._snr_arms(evParams, res, precision)
         if self.detector_shape == 'T':
             return arms if return_all else np.sqrt((arms ** 2).sum(axis=0))
         return arms[0]

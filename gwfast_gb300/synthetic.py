@@ -58,10 +58,13 @@ def chirp_time(Mc, f):
     return 5. / 256. * (np.pi * f) ** (-8. / 3.) * tM ** (-5. / 3.)
 
 
-def res_from_chirp_time(Mc, fmin, lo=200, hi=40000, tau0=100., power=0.8):
-    """Per-event grid length growing with the chirp time from fmin: lo * (tau / tau0)^power, clipped
-    to [lo, hi] (200 points for heavy BBH, 40000 for BNS from 2 Hz)."""
-    r = lo * (chirp_time(Mc, fmin) / tau0) ** power
+def res_from_chirp_time(Mc, fmin, lo=200, hi=40000, mc_ref=None):
+    """Per-event grid length R = clip(round(k sqrt(tau)), lo, hi) with tau the Newtonian chirp time
+    from fmin; k puts the lightest BNS of the bns_events distribution (m1 = m2 = 1.1 Msun) at hi."""
+    if mc_ref is None:
+        mc_ref = Mceta_from_m1m2(np.array([1.1]), np.array([1.1]))[0][0]
+    k = hi / np.sqrt(chirp_time(mc_ref, fmin))
+    r = k * np.sqrt(chirp_time(Mc, fmin))
     return np.clip(np.rint(r), lo, hi).astype(np.int32)
 
 

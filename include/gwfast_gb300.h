@@ -89,9 +89,11 @@ int gwf_detector_add(gwf_ctx* ctx, const gwf_det_desc* desc, const double* psd_f
  * Replaces GWSignal.SNRInteg (gwfast/signal.py:658-777) and DetNet.SNR (gwfast/network.py:278-306).
  * out_arm (may be NULL): per arm slot (L: 1 slot, triangle: 3 slots, in det_ids order),
  *   [slots][N] of trapz((A+^2 + Ax^2)/S, f), i.e. (SNR_arm / 2)^2.
- * out_net (may be NULL): [N] network SNR^2 = sum over arms of 4 * out_arm. */
+ * out_net (may be NULL): [N] network SNR^2 = sum over arms of 4 * out_arm.
+ * precision: GWF_PREC_FP64, or GWF_PREC_FP32 (TaylorF2 and IMRPhenomD: per-point amplitude, pattern
+ * functions and Earth-rotation time in FP32, per-thread compensated sums, FP64 block sums). */
 int gwf_snr(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params, int64_t ld,
-            int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int mem,
+            int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int precision, int mem,
             double* out_arm, double* out_net, void* stream);
 
 /* Fisher matrices of N events in n_det detectors.

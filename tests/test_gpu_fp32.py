@@ -115,3 +115,20 @@ def test_mixed_condition_estimate(gpu_lib):
         refined = entry_err(Fm, F).max(axis=(1, 2)) < 1e-11
         assert np.all(cond[refined] >= kappa / 1.05)
         assert np.all(cond[~refined] <= kappa * 1.05)
+
+
+@pytest.mark.parametrize('model,dets,maker', [
+    ('IMRPhenomD', synthetic.NETWORK_LHET, synthetic.bbh_events),
+    ('TaylorF2_RestrictedPN', (('ETS', 5.), ('Virgo', 10.)), synthetic.bns_events)])
+def test_snr_fp32(gpu_lib, model, dets, maker):
+    """FP32 SNR kernel against the FP64 one: network SNR relative error <= 1e-6; single arms (whose
+    pattern functions can nearly vanish, so their FP32 values lose relative accuracy) <= 1e-5."""
+    ev = maker(512, seed=71)
+    net = synthetic.make_network(getattr(W, model)(), dets=dets, earth=True)
+    s64 = net.SNR(dict(ev), res=2000, return_all=True)
+    s32 = net.SNR(dict(ev), res=2000, return_all=True, precision='fp32')
+    worst_net = np.max(np.abs(s32['net'] - s64['net']) / s64['net'])
+    worst_arm = max(np.max(np.abs(s32[k] - s64[k]) / s64[k]) for k in s64)
+    print('%s fp32 SNR max rel err: network %.2e, single arms %.2e' % (model, worst_net, worst_arm))
+    assert worst_net <= 1e-6
+    assert worst_arm <= 1e-5

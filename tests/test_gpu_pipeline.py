@@ -1,0 +1,44 @@
+"""Batch forecast pipeline (SNR -> threshold -> Fisher -> covariance -> errors, sky areas)."""
+import numpy as np
+import pytest
+
+from gwfast_gb300 import fisherTools, pipeline, synthetic
+from gwfast_gb300 import waveforms as W
+
+pytestmark = pytest.mark.gpu
+
+
+def test_compute_errs_forms_agree(gpu_lib):
+    ev = synthetic.bbh_events(400, seed=81)
+    ev['dL'] = ev['dL'] * 3.0          # push part of the catalogue below threshold
+    net = synthetic.make_network(W.IMRPhenomD(), earth=True)
+    r64 = pipeline.compute_errs(net, dict(ev), snr_th=12., res=2000, precision='fp64', snr_precision='fp64')
+    rm = pipeline.compute_errs(net, dict(ev), snr_th=12., res=2000, precision='mixed', snr_precision='fp32')
+    assert 0 < r64['detected'].sum() < len(r64['detected'])
+    assert np.array_equal(r64['detected'], rm['detected'])
+    assert np.max(np.abs(rm['snr'] - r64['snr']) / r64['snr']) < 1e-6
+    ok = r64['cond'] < 1e13
+    e = np.max(np.abs(rm['errors'] - r64['errors']) / r64['errors'], axis=0)
+    print('detected %d of %d; mixed vs fp64 sigma err median %.2e max %.2e (cond < 1e13)'
+          % (r64['detected'].sum(), len(r64['detected']), np.median(e[ok]), e[ok].max()))
+    assert np.all(e[ok] <= 1e-3)
+    a = r64['sky_area_90']
+    assert np.all(np.isfinite(a[ok])) and np.all(a[ok] > 0)
+    # the sky area is the one of the returned covariance
+    ref = fisherTools.compute_localization_region(r64['cov'], r64['par_nums'], ev['theta'][r64['detected']])
+    assert np.allclose(a, ref, equal_nan=True)
+
+
+def test_compute_errs_fixed_params(gpu_lib):
+    ev = synthetic.bbh_events(64, seed=82)
+    net = synthetic.make_network(W.IMRPhenomD(), earth=True)
+    full = pipeline.compute_errs(net, dict(ev), snr_th=0., res=1000, precision='fp64', snr_precision='fp64')
+    fx = pipeline.compute_errs(net, dict(ev), snr_th=0., res=1000, precision='fp64', snr_precision='fp64',
+                               params_fix=('psi', 'Phicoal'))
+    assert fx['cov'].shape == (9, 9, 64)
+    keep = [0, 1, 2, 3, 4, 5, 7, 9, 10]
+    F = full['fisher'][np.ix_(keep, keep)]
+    C = np.moveaxis(np.linalg.inv(np.moveaxis(F, -1, 0)), 0, -1)
+    ok = full['cond'] < 1e12
+    rel = np.abs(np.sqrt(np.einsum('iin->in', C)) - fx['errors']) / fx['errors']
+    assert np.max(rel[:, ok]) < 1e-6

@@ -125,3 +125,22 @@ def test_shard_slices_cover_everything():
             assert sl[0][0] == 0 and sl[-1][1] == n
             assert all(sl[i][1] == sl[i + 1][0] for i in range(w - 1))
             assert max(b - a for a, b in sl) - min(b - a for a, b in sl) <= 1
+
+
+def test_fix_params_and_sky_area():
+    from gwfast_gb300 import fisherTools
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((5, 11, 11))
+    F = np.moveaxis(A @ np.swapaxes(A, 1, 2) + 11 * np.eye(11), 0, -1)
+    pn = {'Mc': 0, 'eta': 1, 'dL': 2, 'theta': 3, 'phi': 4, 'iota': 5, 'psi': 6, 'tcoal': 7, 'Phicoal': 8,
+          'chi1z': 9, 'chi2z': 10}
+    Fr, pr = fisherTools.fixParams(F, pn, ['psi', 'Phicoal'])
+    assert Fr.shape == (9, 9, 5)
+    assert pr == {'Mc': 0, 'eta': 1, 'dL': 2, 'theta': 3, 'phi': 4, 'iota': 5, 'tcoal': 6, 'chi1z': 7, 'chi2z': 8}
+    keep = [0, 1, 2, 3, 4, 5, 7, 9, 10]
+    assert np.array_equal(Fr, F[np.ix_(keep, keep)])
+    # sky area from a diagonal (theta, phi) block: 2 pi sqrt(det) |sin theta| (-ln 0.1) sr
+    C = np.zeros((11, 11, 1))
+    C[3, 3], C[4, 4] = 1e-4, 4e-4
+    a = fisherTools.compute_localization_region(C, pn, np.array([np.pi / 2]), units='Sterad')
+    assert np.isclose(a[0], 2 * np.pi * 2e-4 * np.log(10.))
