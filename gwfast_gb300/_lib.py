@@ -54,6 +54,15 @@ SIGNATURES = {
     'gwf_set_graphs': ([_vp, ctypes.c_int], ctypes.c_int),
     'gwf_autotune_segments': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32, _vp, ctypes.c_int,
                                ctypes.c_int, ctypes.c_int, _P(ctypes.c_int)], ctypes.c_int),
+    'gwf_mlp_create': ([_vp, ctypes.c_int, ctypes.c_int, ctypes.c_uint64, _P(_vp)], ctypes.c_int),
+    'gwf_mlp_destroy': ([_vp], ctypes.c_int),
+    'gwf_mlp_num_weights': ([_vp, _P(_i64)], ctypes.c_int),
+    'gwf_mlp_get_weights': ([_vp, _vp, _vp], ctypes.c_int),
+    'gwf_mlp_set_weights': ([_vp, _vp, _vp], ctypes.c_int),
+    'gwf_mlp_train': ([_vp, _vp, _i64, _i64, _vp, ctypes.c_int, ctypes.c_int, _d, ctypes.c_uint64, ctypes.c_int,
+                       _P(_d)], ctypes.c_int),
+    'gwf_mlp_gradients': ([_vp, _vp, _i64, _i64, _vp, ctypes.c_int, _P(_d), _vp], ctypes.c_int),
+    'gwf_mlp_predict': ([_vp, _vp, _i64, _i64, ctypes.c_int, _vp], ctypes.c_int),
     'gwf_fisher_noalloc': ([_P(DetDesc), _vp, _vp, _i64, _P(WfDesc), _vp, _vp, _vp, _i64, _vp, _i64, _i64,
                             ctypes.c_int32, ctypes.c_int, _vp, _vp], ctypes.c_int),
 }
@@ -185,3 +194,62 @@ def context(device=0):
         with _lock:
             _ctxs[device] = c
     return c
+
+
+class MLP:
+    """The library's SNR-screen network (gwf_mlp_*): 11 features -> hidden SiLU layers -> ln SNR."""
+
+    def __init__(self, hidden=256, layers=4, seed=0, device=0):
+        lib = load()
+        self._ctx = context(device)
+        h = _vp()
+        check(lib.gwf_mlp_create(self._ctx.h, int(hidden), int(layers), int(seed), ctypes.byref(h)))
+        self.h = h
+        self.hidden, self.layers = hidden, layers
+        n = ctypes.c_int64()
+        check(lib.gwf_mlp_num_weights(self.h, ctypes.byref(n)))
+        self.n_weights = n.value
+
+    def __del__(self):
+        h = getattr(self, 'h', None)
+        if h is not None and _lib is not None:
+            _lib.gwf_mlp_destroy(h)
+            self.h = None
+
+    def get_weights(self):
+        w = np.empty(self.n_weights, dtype=np.float32)
+        check(load().gwf_mlp_get_weights(self.h, ptr(w), None))
+        return w
+
+    def get_norm(self):
+        nm = np.empty(22, dtype=np.float32)
+        check(load().gwf_mlp_get_weights(self.h, None, ptr(nm)))
+        return nm
+
+    def set_weights(self, w=None, norm=None):
+        w = None if w is None else np.ascontiguousarray(w, dtype=np.float32)
+        norm = None if norm is None else np.ascontiguousarray(norm, dtype=np.float32)
+        check(load().gwf_mlp_set_weights(self.h, ptr(w), ptr(norm)))
+
+    def train(self, params, target, epochs=30, batch=4096, lr=2e-3, seed=0):
+        params = np.ascontiguousarray(params, dtype=np.float64)
+        target = np.ascontiguousarray(target, dtype=np.float64)
+        loss = ctypes.c_double()
+        check(load().gwf_mlp_train(self.h, ptr(params), params.shape[1], params.shape[1], ptr(target), int(epochs),
+                                   int(batch), float(lr), int(seed), MEM_HOST, ctypes.byref(loss)))
+        return loss.value
+
+    def gradients(self, params, target):
+        params = np.ascontiguousarray(params, dtype=np.float64)
+        target = np.ascontiguousarray(target, dtype=np.float64)
+        g = np.empty(self.n_weights, dtype=np.float32)
+        loss = ctypes.c_double()
+        check(load().gwf_mlp_gradients(self.h, ptr(params), params.shape[1], params.shape[1], ptr(target), MEM_HOST,
+                                       ctypes.byref(loss), ptr(g)))
+        return loss.value, g
+
+    def predict(self, params):
+        params = np.ascontiguousarray(params, dtype=np.float64)
+        out = np.empty(params.shape[1])
+        check(load().gwf_mlp_predict(self.h, ptr(params), params.shape[1], params.shape[1], MEM_HOST, ptr(out)))
+        return out

@@ -84,6 +84,7 @@ struct GraphEntry {
 namespace gwf {
 // error text for gwf_last_error from the other translation units
 void set_last_error(const char* msg) { g_err = msg; }
+int ctx_device(const gwf_ctx* ctx);
 }  // namespace gwf
 
 struct gwf_ctx {
@@ -468,6 +469,8 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
 }
 
 }  // namespace
+
+int gwf::ctx_device(const gwf_ctx* ctx) { return ctx->device; }
 
 extern "C" {
 

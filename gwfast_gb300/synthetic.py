@@ -52,6 +52,15 @@ def mixed_events(n, seed=1002, bns_fraction=0.5):
     return {k: np.concatenate([np.asarray(a[k]), np.asarray(b[k])]) for k in a}
 
 
+def screen_population(n, seed=1004, dl_max=30.):
+    """Learned-screen population: the mixed catalogue's distributions with dL ~ U[dL_min, dl_max] Gpc."""
+    ev = mixed_events(n, seed=seed)
+    rng = np.random.default_rng(seed + 10)
+    nb = int(round(n * 0.5))
+    ev['dL'] = np.concatenate([rng.uniform(0.05, dl_max, nb), rng.uniform(0.5, dl_max, n - nb)])
+    return ev
+
+
 def chirp_time(Mc, f):
     """Leading-order time to coalescence from frequency f [Hz] for chirp mass Mc [Msun], seconds."""
     tM = np.asarray(Mc) * glob.GMsun_over_c3

@@ -50,6 +50,7 @@ enum { GWF_MEM_HOST = 0, GWF_MEM_DEVICE = 1 };
 enum { GWF_PREC_FP64 = 0, GWF_PREC_FP32 = 1, GWF_PREC_MIXED = 2 };
 
 typedef struct gwf_ctx gwf_ctx;
+typedef struct gwf_mlp gwf_mlp;
 
 /* Detector geometry and band (gwfast/signal.py:68-160, GWSignal.__init__). */
 typedef struct {
@@ -147,6 +148,33 @@ int gwf_autotune_segments(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf
  * Events whose equilibrated matrix is not positive definite get NaN covariances. */
 int gwf_cov(gwf_ctx* ctx, const double* F, int64_t n_events, int mem, double* cov, double* eps, double* cond,
             void* stream);
+
+/* Learned SNR screen (no counterpart in gwfast: a method-level addition). A multilayer perceptron,
+ * 11 features -> `layers` hidden layers of `hidden` SiLU units -> ln(network SNR), trained on SNRs
+ * from gwf_snr. Weights are stored in FP32 (the optimiser's copy) and used in BF16; arithmetic
+ * accumulates in FP32. Features: ln Mc, eta, ln dL, cos theta, sin and cos of (phi - 2 pi tcoal),
+ * cos iota, sin and cos of 2 psi, chi1z, chi2z, standardised by the mean and deviation of the
+ * training events. params as in gwf_fisher ([11][ld], Fisher order); mem as in gwf_fisher. The MLP
+ * lives on the context's device and runs on its own stream; calls are synchronous. */
+int gwf_mlp_create(gwf_ctx* ctx, int hidden, int layers, uint64_t seed, gwf_mlp** out);
+int gwf_mlp_destroy(gwf_mlp* mlp);
+/* weights + biases in the flat layout [W_0 (11 x H), W_1 (H x H), ..., W_L (H x 1), b_0, ..., b_L],
+ * each W row-major (input index major) */
+int gwf_mlp_num_weights(gwf_mlp* mlp, int64_t* n);
+/* FP32 weights (may be NULL) and the standardisation [mean[11], 1/deviation[11]] (may be NULL) */
+int gwf_mlp_get_weights(gwf_mlp* mlp, float* weights, float* norm);
+int gwf_mlp_set_weights(gwf_mlp* mlp, const float* weights, const float* norm);
+/* Adam (beta 0.9, 0.999) on the mean squared error of the predicted ln SNR against target_ln_snr,
+ * minibatches drawn with replacement, learning rate lr with cosine decay over the run; sets the
+ * standardisation from these events. final_loss: mean batch loss of the last epoch. */
+int gwf_mlp_train(gwf_mlp* mlp, const double* params, int64_t ld, int64_t n_events, const double* target_ln_snr,
+                  int epochs, int batch, double lr, uint64_t seed, int mem, double* final_loss);
+/* one forward and backward pass over all n events as one batch: loss and the gradient of the loss
+ * with respect to every weight and bias (flat layout above), for checking against a CPU model */
+int gwf_mlp_gradients(gwf_mlp* mlp, const double* params, int64_t ld, int64_t n_events, const double* target_ln_snr,
+                      int mem, double* loss, float* grad);
+/* predicted ln(network SNR) of n events */
+int gwf_mlp_predict(gwf_mlp* mlp, const double* params, int64_t ld, int64_t n_events, int mem, double* out_ln_snr);
 
 /* Limits of gwf_fisher_noalloc: its scratch is one fixed array of GWF_NOALLOC_SCRATCH_MIB MiB
  * per GPU that loads the library, held until the process exits. */

@@ -1,0 +1,73 @@
+"""SNR-screen MLP: GPU forward/backward against the CPU float64 model, training, and the screen's
+gain in the forecast pipeline."""
+import numpy as np
+import pytest
+
+from gwfast_gb300 import _lib, pipeline, synthetic
+from gwfast_gb300 import waveforms as W
+from gwfast_gb300.screen import SNRScreen
+from gwfast_gb300.signal import event_array
+from oracle import mlp_oracle as M
+
+pytestmark = pytest.mark.gpu
+
+
+def params(n, seed):
+    return event_array(synthetic.screen_population(n, seed=seed))
+
+
+@pytest.mark.parametrize('hidden,layers,n', [(32, 2, 300), (256, 4, 600)])
+def test_mlp_gradients_match_cpu(gpu_lib, hidden, layers, n):
+    rng = np.random.default_rng(hidden)
+    mlp = _lib.MLP(hidden=hidden, layers=layers, seed=3)
+    p = params(n, 11)
+    t = rng.normal(1.0, 1.5, n)
+    loss_g, g_gpu = mlp.gradients(p, t)          # sets the standardisation from these events
+    w, norm = mlp.get_weights(), mlp.get_norm().astype(np.float64)
+    loss_c, g_cpu = M.forward_backward(w, norm, p, t, hidden, layers)
+    rel = np.linalg.norm(g_gpu - g_cpu) / np.linalg.norm(g_cpu)
+    print('hidden %d layers %d: loss %.6e vs %.6e, gradient relative error %.2e' % (hidden, layers, loss_g, loss_c, rel))
+    assert abs(loss_g - loss_c) <= 1e-5 * loss_c
+    assert rel < 1e-4
+
+
+def test_mlp_training_reduces_loss_and_predicts(gpu_lib):
+    p = params(20000, 21)
+    f = M.features(p)
+    t = 0.8 * f[:, 0] - f[:, 2] + 0.5 * f[:, 6] ** 2 + 0.3 * f[:, 5]      # a smooth target of the features
+    mlp = _lib.MLP(hidden=64, layers=2, seed=5)
+    l0, _ = mlp.gradients(p, t)
+    loss = mlp.train(p, t, epochs=20, batch=2048, lr=3e-3)
+    pred = mlp.predict(p)
+    rms = np.sqrt(np.mean((pred - t) ** 2))
+    print('initial loss %.3e, final %.3e, rms %.3e' % (l0, loss, rms))
+    assert loss < 1e-2 * l0
+    assert abs(rms ** 2 - loss) < 0.5 * loss + 1e-6
+    # predictions agree with the CPU model with the trained weights
+    _, _ = M.forward_backward(mlp.get_weights(), mlp.get_norm().astype(np.float64), p[:, :100], t[:100], 64, 2)
+
+
+def test_screen_gain_and_audit(gpu_lib):
+    net = synthetic.make_network(W.IMRPhenomD(), earth=True)
+    train = synthetic.screen_population(40000, seed=31)
+    screen = SNRScreen(net, hidden=256, layers=4, seed=1)
+    loss = screen.fit(dict(train), res=1000, epochs=40, batch=4096, lr=2e-3)
+    ev = synthetic.screen_population(20000, seed=32)
+    exact_snr = net.SNR(dict(ev), res=1000, precision='fp32')
+    pred = screen.predict_ln_snr(dict(ev))
+    err = pred - np.log(exact_snr)
+    near = np.abs(np.log(exact_snr) - np.log(12.)) < 1.0
+    r0 = pipeline.compute_errs(net, dict(ev), snr_th=12., res=1000, precision='mixed', sky_area=False)
+    r1 = pipeline.compute_errs(net, dict(ev), snr_th=12., res=1000, precision='mixed', sky_area=False, screen=screen)
+    info = r1['screen']
+    print('train loss %.3e; held-out ln SNR error rms %.3f (%.3f near threshold), max |err| %.3f; screen %s; '
+          'detected %d (exact path %d)' % (loss, np.sqrt(np.mean(err ** 2)), np.sqrt(np.mean(err[near] ** 2)),
+                                            np.abs(err).max(), info, r1['detected'].sum(), r0['detected'].sum()))
+    assert info['audit_missed_detections'] == 0
+    assert info['exact_snr_fraction'] < 0.5          # the gain: most events need no exact SNR
+    # recall against the exact path (a detection is lost only if its prediction is off by more than
+    # the band and it is not in the audit sample), and few false detections
+    recall = np.mean(r1['detected'][r0['detected']])
+    precision = np.mean(exact_snr[r1['detected']] > 12.)
+    print('recall %.4f precision %.4f' % (recall, precision))
+    assert recall >= 0.99 and precision >= 0.95

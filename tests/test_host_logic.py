@@ -144,3 +144,29 @@ def test_fix_params_and_sky_area():
     C[3, 3], C[4, 4] = 1e-4, 4e-4
     a = fisherTools.compute_localization_region(C, pn, np.array([np.pi / 2]), units='Sterad')
     assert np.isclose(a[0], 2 * np.pi * 2e-4 * np.log(10.))
+
+
+def test_mlp_oracle_gradient_matches_finite_differences():
+    """The CPU model's analytic backward pass against central differences (weights kept exactly
+    representable in bfloat16 so the rounding does not move under the perturbation)."""
+    from oracle import mlp_oracle as M
+    rng = np.random.default_rng(5)
+    hidden, layers = 8, 2
+    n_w = 11 * 8 + 8 * 8 + 8 + 8 + 8 + 1
+    w = M.bf16(rng.normal(0., 0.3, n_w).astype(np.float32))
+    p = np.stack([rng.uniform(5, 50, 20), rng.uniform(0.1, 0.25, 20), rng.uniform(0.5, 10, 20),
+                  rng.uniform(0, np.pi, 20), rng.uniform(0, 2 * np.pi, 20), rng.uniform(0, np.pi, 20),
+                  rng.uniform(0, np.pi, 20), rng.uniform(0, 1, 20), rng.uniform(0, 2 * np.pi, 20),
+                  rng.uniform(-.5, .5, 20), rng.uniform(-.5, .5, 20)])
+    norm = np.concatenate([np.zeros(11), np.ones(11)])
+    t = rng.normal(2., 1., 20)
+    loss, g = M.forward_backward(w, norm, p, t, hidden, layers)
+    # biases are not rounded: check them by central differences
+    Ws, _ = M.unpack(w, hidden, layers)
+    nW = sum(W.size for W in Ws)
+    for i in range(nW, n_w):
+        d = np.zeros(n_w)
+        d[i] = 1e-6
+        fd = (M.forward_backward(w + d, norm, p, t, hidden, layers)[0]
+              - M.forward_backward(w - d, norm, p, t, hidden, layers)[0]) / 2e-6
+        assert abs(fd - g[i]) < 1e-6 * max(1., abs(g[i]))
