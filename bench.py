@@ -357,7 +357,7 @@ def main():
     out32 = torch.empty((N, 11, 11), dtype=torch.float64, device=dev)
     # launch shape: per-event CTAs or persistent segments, chosen by the library's autotuner on a sample
     seg = 0
-    if not args.no_autotune:
+    if not args.no_autotune and not args.only_device:
         ns = min(N, 2000)
         seg = ctx.autotune_segments(ids, desc, p_dev, RES, precision='fp32', mem=_lib.MEM_DEVICE, ld=N, n=ns)
 
@@ -365,8 +365,9 @@ def main():
         ctx.fisher(det_ids, desc, p_dev, RES, per_arm=False, mem=_lib.MEM_DEVICE, out_net=o, stream=stream.cuda_stream,
                    ld=N, n=N, precision=precision)
 
-    def snr_step():
-        ctx.snr(ids, desc, p_dev, RES, mem=_lib.MEM_DEVICE, out_net=snr_out, stream=stream.cuda_stream, ld=N, n=N)
+    def snr_step(precision='fp64'):
+        ctx.snr(ids, desc, p_dev, RES, mem=_lib.MEM_DEVICE, out_net=snr_out, stream=stream.cuda_stream, ld=N, n=N,
+                precision=precision)
 
     def timed(fn, k):
         tot = 0.0
@@ -405,6 +406,8 @@ def main():
     ms64 = timed(lambda: fisher_step(o=out64, precision='fp64'), args.steps)
     ms32 = timed(lambda: fisher_step(o=out32, precision='fp32'), args.steps)
     ms_snr = timed(snr_step, args.steps)
+    snr_step('fp32')
+    ms_snr32 = timed(lambda: snr_step('fp32'), args.steps)
     # per-kernel launches alone: the ET triangle kernel dominates
     ms_et = timed(lambda: fisher_step([ids[2]], o=out32, precision='fp32'), args.steps)
     ms_l1 = timed(lambda: fisher_step([ids[0]], o=out32, precision='fp32'), args.steps)
@@ -493,6 +496,7 @@ def main():
         'sigma_err': serr_mixed,
         'sigma_err_fp32_only': serr_fp32,
         'snr_per_s': world * N / (ms_snr / 1e3),
+        'snr_per_s_fp32': world * N / (ms_snr32 / 1e3),
         'gpu_launches': 6 + 2 + (8 if refined > 0 else 0),
         'e2e': {'value': world * N / e2e_s, 'unit': 'Fisher/s', 'h2d_bytes_per_step': int(p_host.nbytes),
                 'd2h_bytes_per_step': int(F_host.nbytes),

@@ -584,7 +584,7 @@ __device__ inline void f32_item(const EvBatch& ev, const DetDev& det, F32State<M
 }
 
 template <int MODEL, bool EARTH, int NARM, int NG>
-__global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, DetDev det, const unsigned char* scratch32,
+__global__ void __launch_bounds__(kThreads, 5) fisher_kernel_f32(EvBatch ev, DetDev det, const unsigned char* scratch32,
                                                                  double* out_arm, double* out_det, int accum) {
   extern __shared__ __align__(16) unsigned char stage_raw[];
   __shared__ F32State<MODEL, NG> S;
@@ -596,7 +596,7 @@ __global__ void __launch_bounds__(kThreads, 4) fisher_kernel_f32(EvBatch ev, Det
 }
 
 template <int MODEL, bool EARTH, int NARM, int NG>
-__global__ void __launch_bounds__(kThreads, 4) fisher_seg_kernel_f32(EvBatch ev, DetDev det, const unsigned char* scratch32,
+__global__ void __launch_bounds__(kThreads, 5) fisher_seg_kernel_f32(EvBatch ev, DetDev det, const unsigned char* scratch32,
                                                                      long long count, SegInfo si) {
   extern __shared__ __align__(16) unsigned char stage_raw[];
   __shared__ F32State<MODEL, NG> S;
