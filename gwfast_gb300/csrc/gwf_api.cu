@@ -95,7 +95,7 @@ struct gwf_ctx {
   int nq = 0;
   DevBuf par, res, oarm, onet, fin, fout, feps, fcond, setup;
   DevBuf mix_idx, mix_cnt, mix_par, mix_res, mix_net, mix_arm;  // FP64 recomputation of GWF_PREC_MIXED
-  double refine_cond = 1e11;
+  double refine_cond = 1e12;
   int seg_points = 0;      // Fisher launches: 0 = one CTA per event, > 0 = persistent, segments of this many points
   int refine_seg = 256;    // segment length of the FP64 recomputation of GWF_PREC_MIXED
   DevBuf seg_off, seg_ctr, seg_part, seg_ovf, tune_out;

@@ -419,26 +419,38 @@ __device__ inline void block_load(EvUnion& E, ProjEv& pj, GridEv& g, const unsig
 // pidx(a, b) for a <= b (kPairA / kPairB order).
 __host__ __device__ constexpr int pidx(int a, int b) { return a * NP - a * (a - 1) / 2 + (b - a); }
 
-// write the event's matrices from gsum[NG][NE]: scale, and (FP32 form) the psi column restored
-// from Delta = dh/dpsi - 2 s dh/dPhicoal, i.e. F_psi,psi = G_DD + 4 s G_DPc + 4 G_PcPc and
-// F_psi,j = G_Dj + 2 s G_Pcj (psi_sgn = s = +-1; 0: the psi column is dh/dpsi itself)
+// Column changes of the FP32 form, undone here in FP64. The FP32 kernel accumulates the Gram G of
+// modified columns D' and the original columns are D_a = D'_a + k_a D'_{c(a)}:
+//   psi:    D_psi  = Delta + 2 s D_Phicoal   (psi_sgn = s = +-1; 0: no change)
+//   chi1z:  D_chi1 = D'_chi1 + alpha D_chi2  (chi_alpha = alpha; 0: no change)
+// so F_ab = G_ab + k_a G_{c(a) b} + k_b G_{a c(b)} + k_a k_b G_{c(a) c(b)}.
+struct ColMix {
+  double psi2, alpha;
+  __device__ __forceinline__ int partner(int a, double& k) const {
+    if (a == I_PS && psi2 != 0.0) { k = psi2; return I_PC; }
+    if (a == I_C1 && alpha != 0.0) { k = alpha; return I_C2; }
+    k = 0.0;
+    return -1;
+  }
+};
+
+// write the event's matrices from gsum[NG][NE] (upper triangles): column changes undone, scaled
 template <int NG>
-__device__ void write_gram(const double* gsum, double scale, double psi_sgn, long long n, long long N,
-                           double* out_arm, double* out_det, int accum) {
-  const double s2 = 2.0 * psi_sgn;
+__device__ void write_gram(const double* gsum, double scale, ColMix mix, long long n, long long N, double* out_arm,
+                           double* out_det, int accum) {
   for (int e = threadIdx.x; e < NE; e += blockDim.x) {
     const int a = kPairA[e], b = kPairB[e];
+    double ka, kb;
+    const int ca = mix.partner(a, ka), cb = mix.partner(b, kb);
     double sdet = 0.0;
 #pragma unroll
     for (int gs = 0; gs < NG; ++gs) {
       const double* G = gsum + gs * NE;
+      auto at = [&](int x, int y) { return x <= y ? G[pidx(x, y)] : G[pidx(y, x)]; };
       double v = G[e];
-      if (psi_sgn != 0.0) {
-        auto at = [&](int x, int y) { return x <= y ? G[pidx(x, y)] : G[pidx(y, x)]; };
-        if (a == I_PS && b == I_PS) v += 2.0 * s2 * at(I_PS, I_PC) + s2 * s2 * at(I_PC, I_PC);
-        else if (a == I_PS) v += s2 * at(I_PC, b);
-        else if (b == I_PS) v += s2 * at(a, I_PC);
-      }
+      if (ca >= 0) v += ka * at(ca, b);
+      if (cb >= 0) v += kb * at(a, cb);
+      if (ca >= 0 && cb >= 0) v += ka * kb * at(ca, cb);
       v *= scale;
       sdet += v;
       if (out_arm && (NG == 1 || NG == 3)) {
@@ -586,7 +598,7 @@ __global__ void __launch_bounds__(kThreads) fisher_kernel(EvBatch ev, DetDev det
   if (n >= ev.N) return;
   f64_prepare<MODEL, EARTH, NARM, NG>(det, scratch, blockIdx.x, S);
   f64_item<MODEL, EARTH, NARM, NG>(ev, det, S, reinterpret_cast<cd*>(stage_raw), 0, S.g.ok ? S.g.R : 0);
-  write_gram<NG>(S.gsum, 1.0, 0.0, n, ev.N, out_arm, out_det, accum);
+  write_gram<NG>(S.gsum, 1.0, ColMix{0.0, 0.0}, n, ev.N, out_arm, out_det, accum);
 }
 
 // ------------------------------------------------------------------ segmented (persistent) launches
@@ -682,12 +694,12 @@ __global__ void __launch_bounds__(kThreads) fisher_seg_kernel(EvBatch ev, DetDev
 }
 
 // per event: sum of its items' partial Grams in segment order, then the event's matrices.
-// scale_of / psi_of give the Gram scale and the psi-column sign of record i (FP32 form) or 1 / 0.
+// rec (FP32 form) points at the first record's [scale, psi_sgn, chi_alpha] (stride rec_stride_d
+// doubles); null: scale 1, no column changes.
 template <int NG>
 __global__ void __launch_bounds__(kThreads) gram_reduce_kernel(long long n0, long long N, long long count, SegInfo si,
-                                                               const double* scale_of, const double* psi_of,
-                                                               long long rec_stride_d, double* out_arm,
-                                                               double* out_det, int accum) {
+                                                               const double* rec, long long rec_stride_d,
+                                                               double* out_arm, double* out_det, int accum) {
   __shared__ double gsum[NG * NE];
   const long long i = blockIdx.x;
   if (i >= count) return;
@@ -700,9 +712,10 @@ __global__ void __launch_bounds__(kThreads) gram_reduce_kernel(long long n0, lon
     gsum[e] = s;
   }
   __syncthreads();
-  const double scale = scale_of ? scale_of[i * rec_stride_d] : 1.0;
-  const double psi = psi_of ? psi_of[i * rec_stride_d] : 0.0;
-  write_gram<NG>(gsum, scale, psi, n0 + i, N, out_arm, out_det, accum);
+  const double* r = rec ? rec + i * rec_stride_d : nullptr;
+  const double scale = r ? r[0] : 1.0;
+  const ColMix mix{r ? 2.0 * r[1] : 0.0, r ? r[2] : 0.0};
+  write_gram<NG>(gsum, scale, mix, n0 + i, N, out_arm, out_det, accum);
 }
 
 // ------------------------------------------------------------------ SNR kernel

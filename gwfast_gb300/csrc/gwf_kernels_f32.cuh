@@ -165,18 +165,19 @@ struct PBF {
   float u1, u0, k4, mg, fmrd;
 };
 
-__device__ inline void pbf_fill(const PhaseBasis& src, PBF& b) {
+__device__ inline void pbf_fill(const PhaseBasis& src, PBF& b, double alpha) {
+  auto tan = [&](const D4& d, int q) { return q == P_CHI1 ? d.d[P_CHI1] - alpha * d.d[P_CHI2] : d.d[q]; };
   for (int i = 0; i < 22 * 4; ++i) {
     const int c = i >> 2, q = i & 3;
     const D4& d = c < 13 ? src.ins[c] : (c < 17 ? src.itm[c - 13] : src.mrd[c - 17]);
-    const double v = d.d[q];
+    const double v = tan(d, q);
     const float h = (float)v;
     b.hi[c][q] = h;
     b.lo[c][q] = (float)(v - (double)h);
   }
   for (int q = 0; q < 4; ++q) {
-    b.du1[q] = (float)src.U1.d[q];
-    b.du0[q] = (float)src.U0.d[q];
+    b.du1[q] = (float)tan(src.U1, q);
+    b.du0[q] = (float)tan(src.U0, q);
   }
   b.u1 = (float)src.U1.v; b.u0 = (float)src.U0.v; b.k4 = (float)src.mrd[4].v;
   b.mg = (float)src.MG.v; b.fmrd = (float)src.fMRD;
@@ -239,15 +240,21 @@ __device__ __forceinline__ void phase_tangent_f(const PBF& b, float f, float lnf
 
 // round a struct of FP64 duals to its FP32 twin (one thread); the dual at `amp_member` is divided
 // by `amp` first, so the FP32 amplitude is O(1)
+// (tangent slots: value, d/dMc, d/deta, d/dchi1, d/dchi2 per dual; the chi1 slot becomes
+// d/dchi1 - alpha d/dchi2 before rounding)
 template <class SRC, class DST>
-__device__ inline void round_struct(const SRC& s, DST& d, const D4* amp_member, double amp) {
+__device__ inline void round_struct(const SRC& s, DST& d, const D4* amp_member, double amp, double alpha) {
   static_assert(sizeof(SRC) == 2 * sizeof(DST), "dual structs must hold only duals");
+  static_assert(sizeof(D4) == 5 * sizeof(double) && sizeof(SRC) % sizeof(D4) == 0, "dual layout");
   const double* a = reinterpret_cast<const double*>(&s);
   float* b = reinterpret_cast<float*>(&d);
   const int lo = (int)(reinterpret_cast<const double*>(amp_member) - a);
   const double inv = 1.0 / amp;
-  for (int i = 0; i < (int)(sizeof(DST) / sizeof(float)); ++i)
-    b[i] = (float)((i >= lo && i < lo + 5) ? a[i] * inv : a[i]);
+  for (int i = 0; i < (int)(sizeof(DST) / sizeof(float)); ++i) {
+    double v = a[i];
+    if (i % 5 == 1 + P_CHI1) v -= alpha * a[i + 1];
+    b[i] = (float)((i >= lo && i < lo + 5) ? v * inv : v);
+  }
 }
 
 // derivative vectors d h / d theta (11 parameters, every arm) at one frequency point, FP32 form;
@@ -346,8 +353,9 @@ __device__ __forceinline__ void flush_fixed(long long (&acc)[BPL][6], const int*
 // setup_f32_kernel (one thread per event) from the FP64 record
 template <int MODEL>
 struct __align__(16) F32Rec {
-  double scale;     // Gram scale amp^2 / psd_scale (first: the segment reduction reads it)
+  double scale;     // Gram scale amp^2 / psd_scale (first three: the segment reduction reads them)
   double psi_sgn;   // sign of cos(iota): the psi column is Delta (see point_f32)
+  double chi_alpha; // the chi1z tangent is d/dchi1 - alpha d/dchi2 (see setup_f32_kernel)
   double lnfmin, delta;
   EvUnionF ef;
   PBF pbf;
@@ -370,11 +378,20 @@ __global__ void __launch_bounds__(64) setup_f32_kernel(DetDev det, const unsigne
   F32Rec<MODEL>& r = *reinterpret_cast<F32Rec<MODEL>*>(scratch32 + i * f32_stride<MODEL>());
   const GridEv& g = h.g;
   const double amp = g.ok ? (MODEL == 0 ? E.tf2.ampK.v : E.phd.k.ampPref.v) : 1.0;
+  // chi1z and chi2z enter the phase almost only through one combination, so d/dchi1 and d/dchi2
+  // are nearly parallel and their information sits in a small difference. The FP32 form carries
+  // d/dchi1 - alpha d/dchi2 instead, alpha from the spin-orbit (f^-2/3) term of the phase basis,
+  // which that combination cancels in FP64; write_gram restores d/dchi1 in FP64.
+  double alpha = 0.0;
+  const PhaseBasis& pb = *rec_basis<MODEL>(scratch, i);
   if (g.ok) {
-    pbf_fill(*rec_basis<MODEL>(scratch, i), r.pbf);
-    if (MODEL == 0) round_struct(E.tf2, r.ef.tf2, &E.tf2.ampK, amp);
-    else round_struct(E.phd.k, r.ef.phd, &E.phd.k.ampPref, amp);
+    const double c1 = pb.ins[2].d[P_CHI1], c2 = pb.ins[2].d[P_CHI2];
+    if (fabs(c2) > 1e-300 && isfinite(c1 / c2)) alpha = c1 / c2;
+    pbf_fill(pb, r.pbf, alpha);
+    if (MODEL == 0) round_struct(E.tf2, r.ef.tf2, &E.tf2.ampK, amp, alpha);
+    else round_struct(E.phd.k, r.ef.phd, &E.phd.k.ampPref, amp, alpha);
   }
+  r.chi_alpha = alpha;
   r.scale = amp * amp / det.psd_scale;
   projf_setup(r.pf, h.pj, det.sin_zeta);
   r.psi_sgn = r.pf.sgn;
@@ -592,7 +609,7 @@ __global__ void __launch_bounds__(kThreads, 5) fisher_kernel_f32(EvBatch ev, Det
   if (n >= ev.N) return;
   f32_prepare<MODEL, NG>(scratch32, blockIdx.x, S);
   f32_item<MODEL, EARTH, NARM, NG>(ev, det, S, reinterpret_cast<int2*>(stage_raw), 0, S.r.gf.R);
-  write_gram<NG>(S.gsum, S.r.scale, S.r.psi_sgn, n, ev.N, out_arm, out_det, accum);
+  write_gram<NG>(S.gsum, S.r.scale, ColMix{2.0 * S.r.psi_sgn, S.r.chi_alpha}, n, ev.N, out_arm, out_det, accum);
 }
 
 template <int MODEL, bool EARTH, int NARM, int NG>

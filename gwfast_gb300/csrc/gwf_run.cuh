@@ -55,13 +55,13 @@ SegInfo seg_info(const LaunchArgs& a) {
 // segmented launch of one chunk: scan, persistent kernel, reduction
 template <int NG, class KSEG>
 cudaError_t seg_chunk(const LaunchArgs& a, const EvBatch& ev, long long cnt, KSEG ks, const unsigned char* kscratch,
-                      int smem, int grid, const double* scale_of, const double* psi_of, long long stride_d) {
+                      int smem, int grid, const double* rec, long long stride_d) {
   seg_scan_kernel<M><<<1, 1024, 0, a.stream>>>(a.scratch, cnt, a.seg, a.seg_off);
   cudaError_t e = cudaMemsetAsync(a.seg_ctr, 0, sizeof(unsigned long long), a.stream);
   if (e != cudaSuccess) return e;
   const SegInfo si = seg_info(a);
   ks<<<grid, kThreads, smem, a.stream>>>(ev, a.det, kscratch, cnt, si);
-  gram_reduce_kernel<NG><<<(unsigned)cnt, kThreads, 0, a.stream>>>(ev.n0, ev.N, cnt, si, scale_of, psi_of, stride_d,
+  gram_reduce_kernel<NG><<<(unsigned)cnt, kThreads, 0, a.stream>>>(ev.n0, ev.N, cnt, si, rec, stride_d,
                                                                    a.out_arm, a.out_det, a.accum);
   return cudaGetLastError();
 }
@@ -93,7 +93,7 @@ cudaError_t fisher_one(const LaunchArgs& a) {
   if (err == cudaSuccess) err = persist_grid(ks, smem, &grid);
   if (err != cudaSuccess) return err;
   return chunked(a, false, [&](const EvBatch& ev, long long cnt) {
-    return seg_chunk<NG>(a, ev, cnt, ks, a.scratch, smem, grid, nullptr, nullptr, 0);
+    return seg_chunk<NG>(a, ev, cnt, ks, a.scratch, smem, grid, nullptr, 0);
   });
 }
 
@@ -116,11 +116,11 @@ cudaError_t fisher_one_f32(const LaunchArgs& a) {
   int grid = 0;
   if (err == cudaSuccess) err = persist_grid(ks, smem, &grid);
   if (err != cudaSuccess) return err;
-  // Gram scale and psi-column sign lead each FP32 record
+  // Gram scale, psi-column sign and chi1 column coefficient lead each FP32 record
   const double* rec0 = reinterpret_cast<const double*>(s32);
   const long long stride_d = (long long)(f32_stride<M>() / sizeof(double));
   return chunked(a, true, [&](const EvBatch& ev, long long cnt) {
-    return seg_chunk<NG>(a, ev, cnt, ks, s32, smem, grid, rec0, rec0 + 1, stride_d);
+    return seg_chunk<NG>(a, ev, cnt, ks, s32, smem, grid, rec0, stride_d);
   });
 }
 #endif

@@ -65,7 +65,7 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
     res_per_event: optional (N,) grid lengths, one per event (an extension: gwfast uses one res).
     precision: 'fp64' (the drop-in), 'fp32' (split precision, TaylorF2 and IMRPhenomD), or
     'mixed' ('fp32', then FP64 for the events whose network Fisher has an equilibrated condition
-    number above refine_cond, default 1e11).
+    number above refine_cond, default 1e12).
     """
     p = _prep(evParams)
     wf = signals[0].wf_model
@@ -73,7 +73,7 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
     slots = _arm_slots(signals)
     ctx = _lib.context(device)
     if precision == 'mixed':
-        ctx.set_refine_cond(1e11 if refine_cond is None else refine_cond)
+        ctx.set_refine_cond(1e12 if refine_cond is None else refine_cond)
     sp = 0 if spacing == 'geom' else 1
     rev = None if res_per_event is None else np.ascontiguousarray(np.broadcast_to(res_per_event, (N,)), dtype=np.int32)
     duty = any(s.DutyFactor is not None for s in signals)
