@@ -48,6 +48,8 @@ SIGNATURES = {
                  ctypes.c_int, ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
     'gwf_fisher': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32, _vp, ctypes.c_int,
                     ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
+    'gwf_fisher_ex': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32, _vp, ctypes.c_int,
+                       ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
     'gwf_cov': ([_vp, _vp, _i64, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     'gwf_set_refine_cond': ([_vp, _d], ctypes.c_int),
     'gwf_set_segments': ([_vp, ctypes.c_int], ctypes.c_int),
@@ -149,13 +151,18 @@ class Context:
                              ptr(res_ev), spacing, PRECISION[precision], mem, ptr(out_arm), ptr(out_net), stream))
 
     def fisher(self, det_ids, wf, params, res, res_ev=None, spacing=0, per_arm=False, mem=MEM_HOST, out_arm=None,
-               out_net=None, stream=None, ld=None, n=None, precision='fp64'):
+               out_net=None, stream=None, ld=None, n=None, precision='fp64', out_sd_arm=None, out_sd_net=None):
         ids = np.ascontiguousarray(det_ids, dtype=np.int32)
         n = params.shape[1] if n is None else n
         ld = (params.shape[1] if ld is None else ld)
-        check(load().gwf_fisher(self.h, len(ids), ptr(ids), ctypes.byref(wf), ptr(params), ld, n, int(res),
-                                ptr(res_ev), spacing, int(bool(per_arm)), PRECISION[precision], mem, ptr(out_arm),
-                                ptr(out_net), stream))
+        if out_sd_arm is None and out_sd_net is None:
+            check(load().gwf_fisher(self.h, len(ids), ptr(ids), ctypes.byref(wf), ptr(params), ld, n, int(res),
+                                    ptr(res_ev), spacing, int(bool(per_arm)), PRECISION[precision], mem, ptr(out_arm),
+                                    ptr(out_net), stream))
+        else:
+            check(load().gwf_fisher_ex(self.h, len(ids), ptr(ids), ctypes.byref(wf), ptr(params), ld, n, int(res),
+                                       ptr(res_ev), spacing, int(bool(per_arm)), PRECISION[precision], mem,
+                                       ptr(out_arm), ptr(out_net), ptr(out_sd_arm), ptr(out_sd_net), stream))
 
     def set_graphs(self, on):
         """Capture repeated device-resident Fisher calls in CUDA graphs and replay them."""

@@ -99,6 +99,10 @@ struct gwf_ctx {
   int seg_points = 0;      // Fisher launches: 0 = one CTA per event, > 0 = persistent, segments of this many points
   int refine_seg = 256;    // segment length of the FP64 recomputation of GWF_PREC_MIXED
   DevBuf seg_off, seg_ctr, seg_part, seg_ovf, tune_out;
+  // SNR-derivative outputs of the current gwf_fisher_ex call (host or device pointers, as mem says)
+  double* call_sd_arm = nullptr;
+  double* call_sd_net = nullptr;
+  DevBuf osda, osdn, mix_sda, mix_sdn;
   int graphs = 0;                                  // capture device-resident Fisher calls in CUDA graphs
   std::map<std::string, GraphEntry> graph_cache;   // call identity -> instantiated graph
   std::string graph_pending;                       // identity of the last uncaptured call
@@ -209,7 +213,7 @@ int seg_setup(gwf_ctx* ctx, gwf::LaunchArgs& a, int seg, int64_t chunk, int64_t 
   const long long cap = (long long)chunk * (per_ev > 0 ? per_ev : 1);
   if (ctx->seg_off.ensure((size_t)(gwf::kChunk + 1) * sizeof(long long)) ||
       ctx->seg_ctr.ensure(sizeof(unsigned long long)) || ctx->seg_ovf.ensure(sizeof(int)) ||
-      ctx->seg_part.ensure((size_t)cap * 3 * gwf::NE * sizeof(double)))
+      ctx->seg_part.ensure((size_t)cap * 3 * gwf::NEX * sizeof(double)))
     return fail(GWF_ERR_OOM, "device allocation failed (segments)");
   GWF_CK(cudaMemsetAsync(ctx->seg_ovf.p, 0, sizeof(int), st));
   a.seg = seg;
@@ -224,7 +228,8 @@ int seg_setup(gwf_ctx* ctx, gwf::LaunchArgs& a, int seg, int64_t chunk, int64_t 
 // GWF_PREC_MIXED, second stage: condition numbers of the FP32 network Fishers, then the FP64
 // Fisher of the events above the threshold, computed as a compact batch and scattered back
 int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const double* dp, int64_t dld,
-           const int* dres, int64_t N, int slots, double* darm, double* dnet, cudaStream_t st) {
+           const int* dres, int64_t N, int slots, double* darm, double* dnet, double* dsda, double* dsdn,
+           cudaStream_t st) {
   const size_t per = (size_t)gwf::NP * gwf::NP;
   if (ctx->fcond.ensure((size_t)N * sizeof(double)) || ctx->mix_idx.ensure((size_t)N * sizeof(long long)) ||
       ctx->mix_cnt.ensure(sizeof(unsigned long long)))
@@ -245,6 +250,11 @@ int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const
   double* cnet = (double*)ctx->mix_net.p;
   double* carm = darm ? (double*)ctx->mix_arm.p : nullptr;
   int* cres = dres ? (int*)ctx->mix_res.p : nullptr;
+  if ((dsda && ctx->mix_sda.ensure((size_t)slots * M * gwf::NP * sizeof(double))) ||
+      (dsdn && ctx->mix_sdn.ensure((size_t)M * gwf::NP * sizeof(double))))
+    return fail(GWF_ERR_OOM, "device allocation failed (mixed precision)");
+  double* csda = dsda ? (double*)ctx->mix_sda.p : nullptr;
+  double* csdn = dsdn ? (double*)ctx->mix_sdn.p : nullptr;
   e = gwf::launch_gather(dp, dld, dres, idx, (long long)M, cpar, cres, st);
   if (e != cudaSuccess) return fail(GWF_ERR_CUDA, cudaGetErrorString(e));
   a.ev.p = cpar;
@@ -269,6 +279,8 @@ int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const
     a.det = dev_of(r);
     a.out_arm = carm ? carm + (size_t)slot * M * per : nullptr;
     a.out_det = cnet;
+    a.out_sd_arm = csda ? csda + (size_t)slot * M * gwf::NP : nullptr;
+    a.out_sd_det = csdn;
     a.accum = i > 0;
     const int model = a.wf.model;
     e = model == 0 ? gwf::launch_fisher_m0(a) : gwf::launch_fisher_m1(a);
@@ -278,6 +290,10 @@ int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const
   e = gwf::launch_scatter(cnet, idx, (long long)M, (int)per, dnet, st);
   for (int s = 0; carm && s < slots && e == cudaSuccess; ++s)
     e = gwf::launch_scatter(carm + (size_t)s * M * per, idx, (long long)M, (int)per, darm + (size_t)s * N * per, st);
+  if (csdn && e == cudaSuccess) e = gwf::launch_scatter(csdn, idx, (long long)M, gwf::NP, dsdn, st);
+  for (int s = 0; csda && s < slots && e == cudaSuccess; ++s)
+    e = gwf::launch_scatter(csda + (size_t)s * M * gwf::NP, idx, (long long)M, gwf::NP,
+                            dsda + (size_t)s * N * gwf::NP, st);
   if (e != cudaSuccess) return fail(GWF_ERR_CUDA, cudaGetErrorString(e));
   return GWF_OK;
 }
@@ -289,7 +305,8 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
 // a call's identity for the graph cache: every argument, pointers included
 std::string graph_key(int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params, int64_t ld,
                       int64_t N, int32_t res, const int32_t* res_ev, int spacing, int per_arm, int precision,
-                      const double* out_arm, const double* out_net, cudaStream_t st) {
+                      const double* out_arm, const double* out_net, cudaStream_t st, const double* sd_arm,
+                      const double* sd_net) {
   std::string k;
   auto add = [&](const void* p, size_t n) { k.append(reinterpret_cast<const char*>(p), n); };
   add(&n_det, sizeof n_det);
@@ -298,6 +315,7 @@ std::string graph_key(int n_det, const int* det_ids, const gwf_wf_desc* wf, cons
   add(&params, sizeof params); add(&ld, sizeof ld); add(&N, sizeof N); add(&res, sizeof res); add(&res_ev, sizeof res_ev);
   add(&spacing, sizeof spacing); add(&per_arm, sizeof per_arm); add(&precision, sizeof precision);
   add(&out_arm, sizeof out_arm); add(&out_net, sizeof out_net); add(&st, sizeof st);
+  add(&sd_arm, sizeof sd_arm); add(&sd_net, sizeof sd_net);
   return k;
 }
 
@@ -324,6 +342,7 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
   if (precision == GWF_PREC_MIXED && !fisher) return fail(GWF_ERR_INVALID_ARG, "the mixed form is a Fisher form");
   if (fisher && !per_arm) out_arm = nullptr;
   if (fisher && per_arm && !out_arm) return fail(GWF_ERR_INVALID_ARG, "per_arm needs out_arm");
+  if (!fisher && (ctx->call_sd_arm || ctx->call_sd_net)) return fail(GWF_ERR_INVALID_ARG, "SNR derivatives come with the Fisher");
   if (N == 0) return GWF_OK;
   for (int j = 0; j < N && res_ev && mem == GWF_MEM_HOST; ++j)
     if (res_ev[j] < 1) return fail(GWF_ERR_INVALID_ARG, "res_per_event must be >= 1");
@@ -332,7 +351,7 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
   // second identical call and replayed afterwards
   if (ctx->graphs && fisher && mem == GWF_MEM_DEVICE && precision != GWF_PREC_MIXED) {
     std::string key = graph_key(n_det, det_ids, wf, params, ld, N, res, res_ev, spacing, per_arm, precision,
-                                out_arm, out_net, st);
+                                out_arm, out_net, st, ctx->call_sd_arm, ctx->call_sd_net);
     const std::string bufs = buffer_sig(ctx);
     auto it = ctx->graph_cache.find(key);
     if (it != ctx->graph_cache.end() && it->second.bufs == bufs) {
@@ -402,6 +421,24 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
       dnet = (double*)ctx->onet.p;
     }
   }
+  // SNR-derivative outputs (Fisher calls through gwf_fisher_ex)
+  double* sd_arm = fisher ? ctx->call_sd_arm : nullptr;
+  double* sd_net = fisher ? ctx->call_sd_net : nullptr;
+  double* dsda = nullptr;
+  double* dsdn = nullptr;
+  if (mem == GWF_MEM_DEVICE) {
+    dsda = sd_arm;
+    dsdn = sd_net;
+  } else {
+    if (sd_arm) {
+      if (ctx->osda.ensure((size_t)slots * N * gwf::NP * sizeof(double))) return fail(GWF_ERR_OOM, "device allocation failed (out)");
+      dsda = (double*)ctx->osda.p;
+    }
+    if (sd_net) {
+      if (ctx->osdn.ensure((size_t)N * gwf::NP * sizeof(double))) return fail(GWF_ERR_OOM, "device allocation failed (out)");
+      dsdn = (double*)ctx->osdn.p;
+    }
+  }
   // the mixed form needs the network total to decide which events get FP64
   if (precision == GWF_PREC_MIXED && !dnet) {
     if (ctx->onet.ensure((size_t)N * per * sizeof(double))) return fail(GWF_ERR_OOM, "device allocation failed (out)");
@@ -435,7 +472,7 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   a.wf.fcut_par = wf->fcut_par;
   a.qnm = ctx->d_qnm;
   a.nq = ctx->nq;
-  a.per_arm = per_arm;
+  a.per_arm = per_arm || dsda;   // per-arm SNR derivatives need the per-arm Gram sets
   a.precision = precision == GWF_PREC_FP64 ? GWF_PREC_FP64 : GWF_PREC_FP32;
   a.stream = st;
   int slot = 0;
@@ -444,6 +481,8 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
     a.det = dev_of(r);
     a.out_arm = darm ? darm + (size_t)slot * N * per : nullptr;
     a.out_det = dnet;
+    a.out_sd_arm = dsda ? dsda + (size_t)slot * N * gwf::NP : nullptr;
+    a.out_sd_det = dsdn;
     a.accum = i > 0;
     cudaError_t err;
     if (fisher) err = wf->model == 0 ? gwf::launch_fisher_m0(a) : (wf->model == 1 ? gwf::launch_fisher_m1(a) : gwf::launch_fisher_m2(a));
@@ -452,13 +491,15 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
     slot += r.desc.shape == GWF_SHAPE_T ? 3 : 1;
   }
   if (precision == GWF_PREC_MIXED) {
-    rc = refine(ctx, n_det, det_ids, a, dp, dld, dres, N, slots, darm, dnet, st);
+    rc = refine(ctx, n_det, det_ids, a, dp, dld, dres, N, slots, darm, dnet, dsda, dsdn, st);
     if (rc) return rc;
   }
   if (!capturing) GWF_CK(cudaEventRecord(ctx->scratch_free, st));
   if (mem == GWF_MEM_HOST) {
     if (out_arm) GWF_CK(cudaMemcpyAsync(out_arm, darm, (size_t)slots * N * per * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (out_net) GWF_CK(cudaMemcpyAsync(out_net, dnet, (size_t)N * per * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (sd_arm) GWF_CK(cudaMemcpyAsync(sd_arm, dsda, (size_t)slots * N * gwf::NP * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (sd_net) GWF_CK(cudaMemcpyAsync(sd_net, dsdn, (size_t)N * gwf::NP * sizeof(double), cudaMemcpyDeviceToHost, st));
     int ovf = 0;
     if (fisher && (a.seg > 0 || precision == GWF_PREC_MIXED) && ctx->seg_ovf.p)
       GWF_CK(cudaMemcpyAsync(&ovf, ctx->seg_ovf.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -513,6 +554,7 @@ int gwf_ctx_destroy(gwf_ctx* ctx) {
   ctx->mix_net.release(); ctx->mix_arm.release();
   ctx->seg_off.release(); ctx->seg_ctr.release(); ctx->seg_part.release(); ctx->seg_ovf.release();
   ctx->tune_out.release();
+  ctx->osda.release(); ctx->osdn.release(); ctx->mix_sda.release(); ctx->mix_sdn.release();
   for (auto& g : ctx->graph_cache) cudaGraphExecDestroy(g.second.exec);
   ctx->graph_cache.clear();
   ctx->hpar.release(); ctx->hout.release();
@@ -687,6 +729,33 @@ int gwf_autotune_segments(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf
   tr.release();
   ctx->seg_points = rc ? saved : best_seg;
   if (best) *best = ctx->seg_points;
+  return rc;
+}
+
+int gwf_fisher_ex(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params, int64_t ld,
+                  int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int per_arm, int precision,
+                  int mem, double* out_arm, double* out_net, double* out_snr_der_arm, double* out_snr_der_net,
+                  void* stream) {
+  if (!ctx) return fail(GWF_ERR_INVALID_ARG, "null context");
+  ctx->call_sd_arm = out_snr_der_arm;
+  ctx->call_sd_net = out_snr_der_net;
+  if (!out_arm && !out_net && (out_snr_der_arm || out_snr_der_net)) {   // derivatives only: a throw-away total
+    if (ctx->tune_out.ensure((size_t)(n_events > 0 ? n_events : 1) * gwf::NP * gwf::NP * sizeof(double))) {
+      ctx->call_sd_arm = ctx->call_sd_net = nullptr;
+      return fail(GWF_ERR_OOM, "device allocation failed");
+    }
+  }
+  const bool tmp_net = !out_arm && !out_net && (out_snr_der_arm || out_snr_der_net);
+  double* host_tmp = nullptr;
+  std::vector<double> htmp;
+  if (tmp_net && mem == GWF_MEM_HOST) {
+    htmp.resize((size_t)(n_events > 0 ? n_events : 1) * gwf::NP * gwf::NP);
+    host_tmp = htmp.data();
+  }
+  const int rc = run(ctx, true, n_det, det_ids, wf, params, ld, n_events, res, res_per_event, spacing, per_arm,
+                     precision, mem, out_arm, tmp_net ? (mem == GWF_MEM_HOST ? host_tmp : (double*)ctx->tune_out.p)
+                                                      : out_net, stream);
+  ctx->call_sd_arm = ctx->call_sd_net = nullptr;
   return rc;
 }
 

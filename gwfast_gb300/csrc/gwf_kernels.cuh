@@ -418,6 +418,9 @@ __device__ inline void block_load(EvUnion& E, ProjEv& pj, GridEv& g, const unsig
 // Gram layout in shared memory and in the partials: [set][upper-triangle entry], entry index
 // pidx(a, b) for a <= b (kPairA / kPairB order).
 __host__ __device__ constexpr int pidx(int a, int b) { return a * NP - a * (a - 1) / 2 + (b - a); }
+// per Gram set: the NE upper-triangle entries, then the NP products Re<dh/dtheta_a | h> with the
+// strain itself (for the SNR derivatives; zero unless asked for)
+constexpr int NEX = NE + NP;
 
 // Column changes of the FP32 form, undone here in FP64. The FP32 kernel accumulates the Gram G of
 // modified columns D' and the original columns are D_a = D'_a + k_a D'_{c(a)}:
@@ -437,7 +440,7 @@ struct ColMix {
 // write the event's matrices from gsum[NG][NE] (upper triangles): column changes undone, scaled
 template <int NG>
 __device__ void write_gram(const double* gsum, double scale, ColMix mix, long long n, long long N, double* out_arm,
-                           double* out_det, int accum) {
+                           double* out_det, double* out_sd_arm, double* out_sd_det, int accum) {
   for (int e = threadIdx.x; e < NE; e += blockDim.x) {
     const int a = kPairA[e], b = kPairB[e];
     double ka, kb;
@@ -445,7 +448,7 @@ __device__ void write_gram(const double* gsum, double scale, ColMix mix, long lo
     double sdet = 0.0;
 #pragma unroll
     for (int gs = 0; gs < NG; ++gs) {
-      const double* G = gsum + gs * NE;
+      const double* G = gsum + gs * NEX;
       auto at = [&](int x, int y) { return x <= y ? G[pidx(x, y)] : G[pidx(y, x)]; };
       double v = G[e];
       if (ca >= 0) v += ka * at(ca, b);
@@ -465,6 +468,26 @@ __device__ void write_gram(const double* gsum, double scale, ColMix mix, long lo
       else { o[a * NP + b] = sdet; o[b * NP + a] = sdet; }
     }
   }
+  if (out_sd_arm || out_sd_det) {   // Re<dh/dtheta_a | h>, the same column changes undone
+    for (int a = threadIdx.x; a < NP; a += blockDim.x) {
+      double k;
+      const int c = mix.partner(a, k);
+      double sdet = 0.0;
+#pragma unroll
+      for (int gs = 0; gs < NG; ++gs) {
+        const double* H = gsum + gs * NEX + NE;
+        double v = H[a];
+        if (c >= 0) v += k * H[c];
+        v *= scale;
+        sdet += v;
+        if (out_sd_arm && (NG == 1 || NG == 3)) out_sd_arm[((size_t)gs * N + n) * NP + a] = v;
+      }
+      if (out_sd_det) {
+        double* o = out_sd_det + (size_t)n * NP + a;
+        *o = accum ? *o + sdet : sdet;
+      }
+    }
+  }
 }
 
 // per-event state of the FP64 kernels (shared memory)
@@ -475,7 +498,7 @@ struct F64State {
   GridEv g;
   ArmPat apc[NARM];
   TimeState tsc;
-  double gsum[NG * NE];
+  double gsum[NG * NEX];
   long long rec;
 };
 
@@ -492,19 +515,22 @@ __device__ inline void f64_prepare(const DetDev& det, const unsigned char* scrat
   __syncthreads();
 }
 
-// Gram of points [k0, k1) into S.gsum (summed over warps); stage: [warp][NG][NP][32] complex
+// Gram of points [k0, k1) into S.gsum (summed over warps); stage: [warp][NG][NP + 1][32] complex,
+// column NP holding the strain itself when sd (SNR derivatives) is set
 template <int MODEL, bool EARTH, int NARM, int NG>
-__device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<NARM, NG>& S, cd* stage, int k0, int k1) {
+__device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<NARM, NG>& S, cd* stage, int k0, int k1,
+                                bool sd) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  constexpr int NENT = NE * NG;
+  constexpr int NPS = NP + 1;
+  constexpr int NENT = NEX * NG;
   constexpr int EPT = (NENT + 31) / 32;
   double acc[EPT];
 #pragma unroll
   for (int i = 0; i < EPT; ++i) acc[i] = 0.0;
-  cd* my = stage + (size_t)warp * NG * NP * 32;
+  cd* my = stage + (size_t)warp * NG * NPS * 32;
   for (int base = k0; base < k1; base += kThreads) {
     const int k = base + tid;
-    cd D[NARM][NP];
+    cd D[NARM][NPS];
     double sw = 0.0;
     if (k < k1) {
       double f, lnf, w;
@@ -530,27 +556,28 @@ __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<N
         if (EARTH) arm_pattern(S.pj, det.sin_zeta, ts.x, a, ap);
         else ap = S.apc[a];
         arm_derivs(S.pj, ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D[a]);
+        D[a][NP] = sd ? cadd(cscale(P, ap.Fp), cscale(cmuli(C), ap.Fc)) : cd{0.0, 0.0};
       }
     } else {
 #pragma unroll
       for (int a = 0; a < NARM; ++a)
 #pragma unroll
-        for (int q = 0; q < NP; ++q) D[a][q] = {0.0, 0.0};
+        for (int q = 0; q < NPS; ++q) D[a][q] = {0.0, 0.0};
     }
     // stage weighted derivative vectors of this warp's 32 points
 #pragma unroll
-    for (int q = 0; q < NP; ++q) {
+    for (int q = 0; q < NPS; ++q) {
       if (NG == 1) {
-        my[(0 * NP + q) * 32 + lane] = cscale(D[0][q], sw);
+        my[(0 * NPS + q) * 32 + lane] = cscale(D[0][q], sw);
       } else if (NG == 2) {
         const cd u = D[0][q], v = D[1][q];
-        my[(0 * NP + q) * 32 + lane] = cscale(cadd(u, v), sw * 1.2247448713915890);   // sqrt(3/2)
-        my[(1 * NP + q) * 32 + lane] = cscale(cadd(u, cscale(v, -1.0)), sw * 0.70710678118654752);
+        my[(0 * NPS + q) * 32 + lane] = cscale(cadd(u, v), sw * 1.2247448713915890);   // sqrt(3/2)
+        my[(1 * NPS + q) * 32 + lane] = cscale(cadd(u, cscale(v, -1.0)), sw * 0.70710678118654752);
       } else {
         const cd u = D[0][q], v = D[1][q];
-        my[(0 * NP + q) * 32 + lane] = cscale(u, sw);
-        my[(1 * NP + q) * 32 + lane] = cscale(v, sw);
-        my[(2 * NP + q) * 32 + lane] = cscale(cadd(u, v), -sw);
+        my[(0 * NPS + q) * 32 + lane] = cscale(u, sw);
+        my[(1 * NPS + q) * 32 + lane] = cscale(v, sw);
+        my[(2 * NPS + q) * 32 + lane] = cscale(cadd(u, v), -sw);
       }
     }
     __syncwarp();
@@ -558,9 +585,11 @@ __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<N
     for (int i = 0; i < EPT; ++i) {
       const int e = lane + 32 * i;
       if (e < NENT) {
-        const int gs = e / NE, pe = e - gs * NE;
-        const cd* ra = my + (gs * NP + kPairA[pe]) * 32;
-        const cd* rb = my + (gs * NP + kPairB[pe]) * 32;
+        const int gs = e / NEX, pe = e - gs * NEX;
+        if (pe >= NE && !sd) continue;
+        const int a = pe < NE ? kPairA[pe] : pe - NE, b = pe < NE ? kPairB[pe] : NP;
+        const cd* ra = my + (gs * NPS + a) * 32;
+        const cd* rb = my + (gs * NPS + b) * 32;
         double s = 0.0;
 #pragma unroll 8
         for (int j = 0; j < 32; ++j) s += ra[j].re * rb[j].re + ra[j].im * rb[j].im;
@@ -591,14 +620,16 @@ __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<N
 // Triangle, detector total: 2, using G(U)+G(V)+G(U+V) = G(sqrt(3/2)(U+V)) + G(sqrt(1/2)(U-V)).
 template <int MODEL, bool EARTH, int NARM, int NG>
 __global__ void __launch_bounds__(kThreads) fisher_kernel(EvBatch ev, DetDev det, const unsigned char* scratch,
-                                                          double* out_arm, double* out_det, int accum) {
+                                                          double* out_arm, double* out_det, double* out_sd_arm,
+                                                          double* out_sd_det, int accum) {
   extern __shared__ __align__(16) unsigned char stage_raw[];
   __shared__ F64State<NARM, NG> S;
   const long long n = ev.n0 + blockIdx.x;
   if (n >= ev.N) return;
   f64_prepare<MODEL, EARTH, NARM, NG>(det, scratch, blockIdx.x, S);
-  f64_item<MODEL, EARTH, NARM, NG>(ev, det, S, reinterpret_cast<cd*>(stage_raw), 0, S.g.ok ? S.g.R : 0);
-  write_gram<NG>(S.gsum, 1.0, ColMix{0.0, 0.0}, n, ev.N, out_arm, out_det, accum);
+  f64_item<MODEL, EARTH, NARM, NG>(ev, det, S, reinterpret_cast<cd*>(stage_raw), 0, S.g.ok ? S.g.R : 0,
+                                   out_sd_arm || out_sd_det);
+  write_gram<NG>(S.gsum, 1.0, ColMix{0.0, 0.0}, n, ev.N, out_arm, out_det, out_sd_arm, out_sd_det, accum);
 }
 
 // ------------------------------------------------------------------ segmented (persistent) launches
@@ -606,7 +637,7 @@ __global__ void __launch_bounds__(kThreads) fisher_kernel(EvBatch ev, DetDev det
 struct SegInfo {
   const long long* off;
   unsigned long long* counter;   // next item to take
-  double* partial;               // [item][NG * NE]
+  double* partial;               // [item][NG * NEX]
   long long cap;                 // items the partial buffer holds
   int seg;                       // points per segment (multiple of kThreads)
   int* overflow;                 // set when the items exceed cap (never expected: cap is an upper bound)
@@ -676,7 +707,7 @@ __device__ inline bool next_item(const SegInfo& si, long long count, long long& 
 
 template <int MODEL, bool EARTH, int NARM, int NG>
 __global__ void __launch_bounds__(kThreads) fisher_seg_kernel(EvBatch ev, DetDev det, const unsigned char* scratch,
-                                                              long long count, SegInfo si) {
+                                                              long long count, SegInfo si, int sd) {
   extern __shared__ __align__(16) unsigned char stage_raw[];
   __shared__ F64State<NARM, NG> S;
   if (threadIdx.x == 0) S.rec = -1;
@@ -687,9 +718,9 @@ __global__ void __launch_bounds__(kThreads) fisher_seg_kernel(EvBatch ev, DetDev
     if (S.rec != rec) f64_prepare<MODEL, EARTH, NARM, NG>(det, scratch, rec, S);
     const int R = S.g.ok ? S.g.R : 0;
     const int k1 = k0 + si.seg < R ? k0 + si.seg : R;
-    f64_item<MODEL, EARTH, NARM, NG>(ev, det, S, reinterpret_cast<cd*>(stage_raw), k0, k1);
-    double* o = si.partial + item * (NG * NE);
-    for (int e = threadIdx.x; e < NG * NE; e += blockDim.x) o[e] = S.gsum[e];
+    f64_item<MODEL, EARTH, NARM, NG>(ev, det, S, reinterpret_cast<cd*>(stage_raw), k0, k1, sd != 0);
+    double* o = si.partial + item * (NG * NEX);
+    for (int e = threadIdx.x; e < NG * NEX; e += blockDim.x) o[e] = S.gsum[e];
   }
 }
 
@@ -699,23 +730,24 @@ __global__ void __launch_bounds__(kThreads) fisher_seg_kernel(EvBatch ev, DetDev
 template <int NG>
 __global__ void __launch_bounds__(kThreads) gram_reduce_kernel(long long n0, long long N, long long count, SegInfo si,
                                                                const double* rec, long long rec_stride_d,
-                                                               double* out_arm, double* out_det, int accum) {
-  __shared__ double gsum[NG * NE];
+                                                               double* out_arm, double* out_det, double* out_sd_arm,
+                                                               double* out_sd_det, int accum) {
+  __shared__ double gsum[NG * NEX];
   const long long i = blockIdx.x;
   if (i >= count) return;
   const long long a = si.off[i];
   long long b = si.off[i + 1];
   if (b > si.cap) b = si.cap;   // items beyond the buffer were never written (overflow is flagged)
-  for (int e = threadIdx.x; e < NG * NE; e += blockDim.x) {
+  for (int e = threadIdx.x; e < NG * NEX; e += blockDim.x) {
     double s = 0.0;
-    for (long long it = a; it < b; ++it) s += si.partial[it * (NG * NE) + e];
+    for (long long it = a; it < b; ++it) s += si.partial[it * (NG * NEX) + e];
     gsum[e] = s;
   }
   __syncthreads();
   const double* r = rec ? rec + i * rec_stride_d : nullptr;
   const double scale = r ? r[0] : 1.0;
   const ColMix mix{r ? 2.0 * r[1] : 0.0, r ? r[2] : 0.0};
-  write_gram<NG>(gsum, scale, mix, n0 + i, N, out_arm, out_det, accum);
+  write_gram<NG>(gsum, scale, mix, n0 + i, N, out_arm, out_det, out_sd_arm, out_sd_det, accum);
 }
 
 // ------------------------------------------------------------------ SNR kernel

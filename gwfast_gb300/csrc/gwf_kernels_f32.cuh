@@ -266,7 +266,7 @@ __device__ inline void round_struct(const SRC& s, DST& d, const D4* amp_member, 
 // its FP32 relative accuracy (the Gram of the original columns is restored in FP64 at the end).
 template <int MODEL, bool EARTH, int NARM>
 __device__ __forceinline__ void point_f32(const EvUnionF& EF, const PBF& pbf, const ProjF& pf, const ArmF* apc,
-                                          const TimeF& tsc, float f, float lnf, cf (&D)[NARM][NP]) {
+                                          const TimeF& tsc, float f, float lnf, cf (&D)[NARM][NP], cf (&H)[NARM]) {
   DF4 A;
   float dphi[4];
   float dtn[4] = {0.f, 0.f, 0.f, 0.f};
@@ -308,6 +308,7 @@ __device__ __forceinline__ void point_f32(const EvUnionF& EF, const PBF& pbf, co
     arm_derivs_f(pf, ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D[a]);
     const float k = 2.0f * A.v * pf.dcs;
     D[a][I_PS] = {k * ap.Fc, k * pf.sgn * ap.Fp};
+    H[a] = fadd(fscale(P, ap.Fp), fscale(fmuli(C), ap.Fc));   // the strain (common phase dropped)
   }
 }
 
@@ -413,7 +414,7 @@ struct F32State {
   F32Rec<MODEL> r;
   int colM[2][kWarps][NG * 12];                      // running column exponents, double-buffered
   double fl[kWarps][gram_slots<NG>()][12][12];       // FP64 Gram per warp and slot
-  double gsum[NG * NE];                              // Gram per set, summed over warps
+  double gsum[NG * NEX];                             // Gram per set (and strain products), summed over warps
   int badw[kWarps];
   long long rec;
 };
@@ -468,7 +469,8 @@ struct GridIterF {
 
 // Gram of points [k0, k1) (k0 a multiple of kThreads) into S.gsum, summed over warps
 template <int MODEL, bool EARTH, int NARM, int NG>
-__device__ inline void f32_item(const EvBatch& ev, const DetDev& det, F32State<MODEL, NG>& S, int2* stage, int k0, int k1) {
+__device__ inline void f32_item(const EvBatch& ev, const DetDev& det, F32State<MODEL, NG>& S, int2* stage, int k0, int k1,
+                                bool sd) {
   constexpr int NQ = 12;  // padded parameter count
   const F32Rec<MODEL>& r = S.r;
   const GridF& gf = r.gf;
@@ -494,7 +496,7 @@ __device__ inline void f32_item(const EvBatch& ev, const DetDev& det, F32State<M
   __syncwarp();
   for (int base = k0; base < k1; base += kThreads) {
     const int k = base + tid;
-    cf D[NARM][NP];
+    cf D[NARM][NP], Hs[NARM];
     float sw = 0.0f;
     grid.step(r, ev.spacing, base, lane, warp);
     if (k < k1) {
@@ -502,12 +504,14 @@ __device__ inline void f32_item(const EvBatch& ev, const DetDev& det, F32State<M
       grid.point(r, ev.spacing, k, lane, f, lnf, w);
       const float Sn = psd_at_f(det, f, lnf, gf.acc_l0, gf.acc_idl);
       sw = sqrtf(4.0f * w / Sn);
-      point_f32<MODEL, EARTH, NARM>(r.ef, r.pbf, r.pf, r.apc, r.tsc, f, lnf, D);
+      point_f32<MODEL, EARTH, NARM>(r.ef, r.pbf, r.pf, r.apc, r.tsc, f, lnf, D, Hs);
     } else {
 #pragma unroll
-      for (int a = 0; a < NARM; ++a)
+      for (int a = 0; a < NARM; ++a) {
 #pragma unroll
         for (int q = 0; q < NP; ++q) D[a][q] = {0.0f, 0.0f};
+        Hs[a] = {0.0f, 0.0f};
+      }
     }
     // Quantise the sqrt(weight)-scaled derivative vectors to integers, |q| <= 2^kQBits,
     // on a per-column power-of-two scale that follows the largest magnitude this warp has seen.
@@ -518,12 +522,14 @@ __device__ inline void f32_item(const EvBatch& ev, const DetDev& det, F32State<M
 #pragma unroll
     for (int gs = 0; gs < NG; ++gs)
 #pragma unroll
-      for (int q = 0; q < NP; ++q) {
+      for (int q = 0; q <= NP; ++q) {   // column NP: the strain itself, staged only for SNR derivatives
+        if (q == NP && !sd) break;
+        const cf d0 = q < NP ? D[0][q] : Hs[0], d1 = q < NP ? D[NARM - 1][q] : Hs[NARM - 1];
         cf u;
-        if (NG == 1) u = fscale(D[0][q], sw);
-        else if (NG == 2) u = gs == 0 ? fscale(fadd(D[0][q], D[1][q]), sw * 1.2247448713915890f)
-                                      : fscale(fadd(D[0][q], fscale(D[1][q], -1.0f)), sw * 0.70710678118654752f);
-        else u = gs == 0 ? fscale(D[0][q], sw) : gs == 1 ? fscale(D[1][q], sw) : fscale(fadd(D[0][q], D[1][q]), -sw);
+        if (NG == 1) u = fscale(d0, sw);
+        else if (NG == 2) u = gs == 0 ? fscale(fadd(d0, d1), sw * 1.2247448713915890f)
+                                      : fscale(fadd(d0, fscale(d1, -1.0f)), sw * 0.70710678118654752f);
+        else u = gs == 0 ? fscale(d0, sw) : gs == 1 ? fscale(d1, sw) : fscale(fadd(d0, d1), -sw);
         const int mold = Mo[gs * NQ + q];
         const unsigned bits = max(__float_as_uint(fabsf(u.re)), __float_as_uint(fabsf(u.im)));
         const int e = (int)(__reduce_max_sync(0xffffffffu, bits) >> 23) - 127;
@@ -587,34 +593,37 @@ __device__ inline void f32_item(const EvBatch& ev, const DetDev& det, F32State<M
   for (int w = 0; w < kWarps; ++w) anybad |= S.badw[w];
   const double* red = &fl[0][0][0][0];  // [kWarps][gram_slots][NQ][NQ]
   constexpr int NS = gram_slots<NG>();
-  for (int e = tid; e < NG * NE; e += kThreads) {
-    const int gs = e / NE, a = kPairA[e % NE], b = kPairB[e % NE];
+  for (int e = tid; e < NG * NEX; e += kThreads) {
+    const int gs = e / NEX, pe = e % NEX;
+    const int a = pe < NE ? kPairA[pe] : pe - NE, b = pe < NE ? kPairB[pe] : NP;   // (a, NP): strain products
     double v = 0.0;
 #pragma unroll
     for (int w = 0; w < kWarps; ++w) {
       v += red[((size_t)(w * NS + gs) * NQ + a) * NQ + b];
       if (NG == 1) v += red[((size_t)(w * NS + 1) * NQ + a) * NQ + b];
     }
-    S.gsum[e] = anybad ? __longlong_as_double(0x7ff8000000000000ll) : v;
+    S.gsum[e] = anybad ? __longlong_as_double(0x7ff8000000000000ll) : (pe >= NE && !sd ? 0.0 : v);
   }
   __syncthreads();
 }
 
 template <int MODEL, bool EARTH, int NARM, int NG>
 __global__ void __launch_bounds__(kThreads, 5) fisher_kernel_f32(EvBatch ev, DetDev det, const unsigned char* scratch32,
-                                                                 double* out_arm, double* out_det, int accum) {
+                                                                 double* out_arm, double* out_det, double* out_sd_arm,
+                                                                 double* out_sd_det, int accum) {
   extern __shared__ __align__(16) unsigned char stage_raw[];
   __shared__ F32State<MODEL, NG> S;
   const long long n = ev.n0 + blockIdx.x;
   if (n >= ev.N) return;
   f32_prepare<MODEL, NG>(scratch32, blockIdx.x, S);
-  f32_item<MODEL, EARTH, NARM, NG>(ev, det, S, reinterpret_cast<int2*>(stage_raw), 0, S.r.gf.R);
-  write_gram<NG>(S.gsum, S.r.scale, ColMix{2.0 * S.r.psi_sgn, S.r.chi_alpha}, n, ev.N, out_arm, out_det, accum);
+  f32_item<MODEL, EARTH, NARM, NG>(ev, det, S, reinterpret_cast<int2*>(stage_raw), 0, S.r.gf.R, out_sd_arm || out_sd_det);
+  write_gram<NG>(S.gsum, S.r.scale, ColMix{2.0 * S.r.psi_sgn, S.r.chi_alpha}, n, ev.N, out_arm, out_det, out_sd_arm,
+                 out_sd_det, accum);
 }
 
 template <int MODEL, bool EARTH, int NARM, int NG>
 __global__ void __launch_bounds__(kThreads, 5) fisher_seg_kernel_f32(EvBatch ev, DetDev det, const unsigned char* scratch32,
-                                                                     long long count, SegInfo si) {
+                                                                     long long count, SegInfo si, int sd) {
   extern __shared__ __align__(16) unsigned char stage_raw[];
   __shared__ F32State<MODEL, NG> S;
   if (threadIdx.x == 0) S.rec = -1;
@@ -625,9 +634,9 @@ __global__ void __launch_bounds__(kThreads, 5) fisher_seg_kernel_f32(EvBatch ev,
     if (S.rec != rec) f32_prepare<MODEL, NG>(scratch32, rec, S);
     const int R = S.r.gf.R;
     const int k1 = k0 + si.seg < R ? k0 + si.seg : R;
-    f32_item<MODEL, EARTH, NARM, NG>(ev, det, S, reinterpret_cast<int2*>(stage_raw), k0, k1);
-    double* o = si.partial + item * (NG * NE);
-    for (int e = threadIdx.x; e < NG * NE; e += blockDim.x) o[e] = S.gsum[e];
+    f32_item<MODEL, EARTH, NARM, NG>(ev, det, S, reinterpret_cast<int2*>(stage_raw), k0, k1, sd != 0);
+    double* o = si.partial + item * (NG * NEX);
+    for (int e = threadIdx.x; e < NG * NEX; e += blockDim.x) o[e] = S.gsum[e];
   }
 }
 

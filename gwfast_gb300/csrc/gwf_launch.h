@@ -16,6 +16,8 @@ struct LaunchArgs {
   int nq;
   double* out_arm;
   double* out_det;
+  double* out_sd_arm = nullptr;   // Re<dh/dtheta | h> per arm slot [slots][N][11] (SNR derivatives), or null
+  double* out_sd_det = nullptr;   // the same summed over the detector's arms [N][11] (+= when accum)
   int accum;
   int per_arm;
   int precision;  // 0 = FP64, 1 = FP32 split precision (22-mode models); the launchers see no other value
@@ -26,7 +28,7 @@ struct LaunchArgs {
   int seg = 0;
   long long* seg_off = nullptr;            // kChunk + 1
   unsigned long long* seg_ctr = nullptr;   // item counter
-  double* seg_part = nullptr;              // seg_cap x 3 x 66 partial Grams
+  double* seg_part = nullptr;              // seg_cap x 3 x 77 partial Grams
   long long seg_cap = 0;
   int* seg_ovf = nullptr;                  // set if the items exceed seg_cap
 };

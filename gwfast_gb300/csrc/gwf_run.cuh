@@ -60,9 +60,9 @@ cudaError_t seg_chunk(const LaunchArgs& a, const EvBatch& ev, long long cnt, KSE
   cudaError_t e = cudaMemsetAsync(a.seg_ctr, 0, sizeof(unsigned long long), a.stream);
   if (e != cudaSuccess) return e;
   const SegInfo si = seg_info(a);
-  ks<<<grid, kThreads, smem, a.stream>>>(ev, a.det, kscratch, cnt, si);
-  gram_reduce_kernel<NG><<<(unsigned)cnt, kThreads, 0, a.stream>>>(ev.n0, ev.N, cnt, si, rec, stride_d,
-                                                                   a.out_arm, a.out_det, a.accum);
+  ks<<<grid, kThreads, smem, a.stream>>>(ev, a.det, kscratch, cnt, si, (a.out_sd_arm || a.out_sd_det) ? 1 : 0);
+  gram_reduce_kernel<NG><<<(unsigned)cnt, kThreads, 0, a.stream>>>(ev.n0, ev.N, cnt, si, rec, stride_d, a.out_arm,
+                                                                   a.out_det, a.out_sd_arm, a.out_sd_det, a.accum);
   return cudaGetLastError();
 }
 
@@ -77,13 +77,14 @@ cudaError_t persist_grid(K k, int smem, int* grid) {
 
 template <bool EARTH, int NARM, int NG>
 cudaError_t fisher_one(const LaunchArgs& a) {
-  const int smem = kWarps * NG * NP * 32 * (int)sizeof(cd);
+  const int smem = kWarps * NG * (NP + 1) * 32 * (int)sizeof(cd);
   if (a.seg <= 0) {
     auto k = fisher_kernel<M, EARTH, NARM, NG>;
     cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (err != cudaSuccess) return err;
     return chunked(a, false, [&](const EvBatch& ev, long long cnt) {
-      k<<<(unsigned)cnt, kThreads, smem, a.stream>>>(ev, a.det, a.scratch, a.out_arm, a.out_det, a.accum);
+      k<<<(unsigned)cnt, kThreads, smem, a.stream>>>(ev, a.det, a.scratch, a.out_arm, a.out_det, a.out_sd_arm,
+                                                     a.out_sd_det, a.accum);
       return cudaSuccess;
     });
   }
@@ -107,7 +108,8 @@ cudaError_t fisher_one_f32(const LaunchArgs& a) {
     cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (err != cudaSuccess) return err;
     return chunked(a, true, [&](const EvBatch& ev, long long cnt) {
-      k<<<(unsigned)cnt, kThreads, smem, a.stream>>>(ev, a.det, s32, a.out_arm, a.out_det, a.accum);
+      k<<<(unsigned)cnt, kThreads, smem, a.stream>>>(ev, a.det, s32, a.out_arm, a.out_det, a.out_sd_arm, a.out_sd_det,
+                                                     a.accum);
       return cudaSuccess;
     });
   }

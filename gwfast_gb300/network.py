@@ -7,7 +7,7 @@ device.
 import numpy as np
 
 from . import gwfastUtils as utils
-from .signal import fisher_batch, reparametrise, snr_batch
+from .signal import fisher_batch, reparametrise, reparametrise_vec, snr_batch
 
 
 class DetNet:
@@ -47,9 +47,14 @@ class DetNet:
         return net
 
     def FisherMatr(self, evParams, return_all=False, return_derivatives=False, return_SNR_derivatives=False, **kwargs):
-        """Network Fisher matrix, (11, 11, N) (gwfast/network.py:309-343)."""
-        if return_derivatives or return_SNR_derivatives:
-            raise NotImplementedError('return_derivatives / return_SNR_derivatives are not implemented on the GPU path')
+        """Network Fisher matrix, (11, 11, N) (gwfast/network.py:309-377).
+
+        return_SNR_derivatives=True returns (allF, allDer) as gwfast: per-arm Fisher matrices and
+        per-arm SNR-derivative integrals (11, N) keyed by detector (name_0..2 for triangles), plus
+        'net': the Fisher total and dSNR/dtheta = sum of the integrals / network SNR (SNRs from
+        kwargs['SNRs'] if given)."""
+        if return_derivatives:
+            raise NotImplementedError('return_derivatives (the (P, N, R) derivative arrays) is not implemented on the GPU path')
         utils.check_evparams(evParams)
         names, sigs = self._list()
         res = kwargs.get('res', 1000)
@@ -61,6 +66,23 @@ class DetNet:
         if kwargs.get('computeDerivFinDiff', False):
             raise NotImplementedError('finite-difference derivatives are not used on the GPU path')
         precision = kwargs.get('precision', 'fp64')
+        if return_SNR_derivatives:
+            per, der = fisher_batch(sigs, evParams, res, per_arm=True, spacing=spacing, device=sigs[0].device,
+                                    precision=precision, refine_cond=kwargs.get('refine_cond'),
+                                    res_per_event=kwargs.get('res_per_event'), snr_derivs=True)
+            allF, allDer = {}, {}
+            for name, s, Fa, Da in zip(names, sigs, per, der):
+                Fa = reparametrise(Fa, evParams, use_m1m2, use_chi1chi2)
+                Da = reparametrise_vec(Da, evParams, use_m1m2, use_chi1chi2)
+                keys = ['%s_%s' % (name, i) for i in range(3)] if s.detector_shape == 'T' else [name]
+                for i, k in enumerate(keys):
+                    allF[k] = np.moveaxis(Fa[i], 0, -1)
+                    allDer[k] = np.moveaxis(Da[i], 0, -1)
+            snrs = kwargs['SNRs'] if 'SNRs' in kwargs else self.SNR(evParams, res=res, precision='fp64' if precision ==
+                                                                    'fp64' else 'fp32')
+            allF['net'] = np.array([allF[k] for k in allF]).sum(axis=0)
+            allDer['net'] = np.array([allDer[k] for k in allDer]).sum(axis=0) / snrs
+            return allF, allDer
         if not return_all:
             F = fisher_batch(sigs, evParams, res, per_arm=False, spacing=spacing, device=sigs[0].device,
                              precision=precision, refine_cond=kwargs.get('refine_cond'),

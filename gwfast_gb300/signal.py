@@ -58,11 +58,14 @@ def snr_batch(signals, evParams, res=1000, device=0, precision='fp64', res_per_e
 
 
 def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', device=0, precision='fp64',
-                 refine_cond=None, res_per_event=None):
+                 refine_cond=None, res_per_event=None, snr_derivs=False):
     """Fisher matrices of all signals in one library call.
 
     per_arm: list (per signal) of (arms, N, 11, 11); otherwise the network total (N, 11, 11).
     res_per_event: optional (N,) grid lengths, one per event (an extension: gwfast uses one res).
+    snr_derivs: also return, per signal, (arms, N, 11) of 4 trapz(Re(h conj(dh/dtheta)) / S) (the
+    per-arm SNR-derivative integrals of gwfast's return_SNR_derivatives); the Fisher part is then
+    per arm.
     precision: 'fp64' (the drop-in), 'fp32' (split precision, TaylorF2 and IMRPhenomD), or
     'mixed' ('fp32', then FP64 for the events whose network Fisher has an equilibrated condition
     number above refine_cond, default 1e12).
@@ -77,14 +80,19 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
     sp = 0 if spacing == 'geom' else 1
     rev = None if res_per_event is None else np.ascontiguousarray(np.broadcast_to(res_per_event, (N,)), dtype=np.int32)
     duty = any(s.DutyFactor is not None for s in signals)
-    if per_arm or duty:
+    if per_arm or duty or snr_derivs:
         out = np.empty((sum(slots), N, 11, 11))
+        sd = np.empty((sum(slots), N, 11)) if snr_derivs else None
         ctx.fisher([s.det_id for s in signals], wf.gpu_desc(), p, res, res_ev=rev, spacing=sp, per_arm=True,
-                   out_arm=out, precision=precision)
-        res_l, i = [], 0
+                   out_arm=out, precision=precision, out_sd_arm=sd)
+        res_l, sd_l, i = [], [], 0
         for s, k in zip(signals, slots):
             res_l.append(s._apply_duty(out[i:i + k], seed=True))
+            if snr_derivs:
+                sd_l.append(s._apply_duty(sd[i:i + k], seed=True))
             i += k
+        if snr_derivs:
+            return res_l, sd_l
         if per_arm:
             return res_l
         return sum(r.sum(axis=0) for r in res_l)
@@ -94,11 +102,7 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
     return out
 
 
-def reparametrise(F, evParams, use_m1m2=False, use_chi1chi2=True):
-    """Chain rule to (m1, m2) and/or (chiS, chiA), F: (..., N, 11, 11) (gwfast/signal.py:818-842)."""
-    if not use_m1m2 and use_chi1chi2:
-        return F
-    N = F.shape[-3]
+def _jacobian(evParams, N, use_m1m2, use_chi1chi2):
     J = np.broadcast_to(np.eye(11), (N, 11, 11)).copy()
     if use_m1m2:
         m1, m2 = utils.m1m2_from_Mceta(np.asarray(evParams['Mc']), np.asarray(evParams['eta']))
@@ -111,7 +115,23 @@ def reparametrise(F, evParams, use_m1m2=False, use_chi1chi2=True):
     if not use_chi1chi2:
         J[:, 9, 9] = 1.; J[:, 9, 10] = 1.
         J[:, 10, 9] = 1.; J[:, 10, 10] = -1.
+    return J
+
+
+def reparametrise(F, evParams, use_m1m2=False, use_chi1chi2=True):
+    """Chain rule to (m1, m2) and/or (chiS, chiA), F: (..., N, 11, 11) (gwfast/signal.py:818-842)."""
+    if not use_m1m2 and use_chi1chi2:
+        return F
+    J = _jacobian(evParams, F.shape[-3], use_m1m2, use_chi1chi2)
     return np.einsum('nai,...nab,nbj->...nij', J, F, J)
+
+
+def reparametrise_vec(v, evParams, use_m1m2=False, use_chi1chi2=True):
+    """The same chain rule for derivative vectors, v: (..., N, 11)."""
+    if not use_m1m2 and use_chi1chi2:
+        return v
+    J = _jacobian(evParams, v.shape[-2], use_m1m2, use_chi1chi2)
+    return np.einsum('nai,...na->...ni', J, v)
 
 
 class GWSignal:
@@ -195,11 +215,18 @@ class GWSignal:
 
         precision='fp32' selects the split-precision kernel (TaylorF2 and IMRPhenomD), 'mixed' the
         split-precision kernel with FP64 recomputation of ill-conditioned events (refine_cond)."""
-        if return_derivatives or return_SNR_derivatives:
-            raise NotImplementedError('return_derivatives / return_SNR_derivatives are not implemented on the GPU path')
+        if return_derivatives:
+            raise NotImplementedError('return_derivatives (the (P, N, R) derivative arrays) is not implemented on the GPU path')
         if computeDerivFinDiff:
             raise NotImplementedError('finite-difference derivatives are not used on the GPU path')
         res = self._resolve_res(evParams, res, df)
+        if return_SNR_derivatives:
+            # as gwfast: per-arm Fisher matrices and per-arm (P, N) SNR-derivative integrals
+            Fa, Da = fisher_batch([self], evParams, res, per_arm=True, spacing=spacing, device=self.device,
+                                  precision=precision, refine_cond=kwargs.get('refine_cond'), snr_derivs=True)
+            Fa = reparametrise(Fa[0], evParams, use_m1m2, use_chi1chi2)
+            Da = reparametrise_vec(Da[0], evParams, use_m1m2, use_chi1chi2)
+            return [np.moveaxis(F, 0, -1) for F in Fa], [np.moveaxis(D, 0, -1) for D in Da]
         Fa = fisher_batch([self], evParams, res, per_arm=True, spacing=spacing, device=self.device,
                           precision=precision, refine_cond=kwargs.get('refine_cond'))[0]
         Fa = reparametrise(Fa, evParams, use_m1m2, use_chi1chi2)

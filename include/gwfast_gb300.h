@@ -112,6 +112,17 @@ int gwf_fisher(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* w
                int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int per_arm, int precision,
                int mem, double* out_arm, double* out_net, void* stream);
 
+/* gwf_fisher plus the SNR derivatives (GWSignal.FisherMatr / DetNet.FisherMatr with
+ * return_SNR_derivatives=True, gwfast/signal.py:938-945, :1016-1022, :1090-1094; gwfast/network.py:139-145):
+ * out_snr_der_arm (may be NULL): [slots][N][11] per arm, 4 trapz(Re(h conj(dh/dtheta)) / S, f)
+ * (tcoal in seconds); out_snr_der_net (may be NULL): [N][11] the same summed over all arms.
+ * Divided by the network SNR, the sum is d SNR / d theta. Same precision forms; the column changes
+ * of the FP32 form are undone as for the Fisher. out_arm / out_net may both be NULL. */
+int gwf_fisher_ex(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params, int64_t ld,
+                  int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int per_arm, int precision,
+                  int mem, double* out_arm, double* out_net, double* out_snr_der_arm, double* out_snr_der_net,
+                  void* stream);
+
 /* Condition-number threshold of GWF_PREC_MIXED (no counterpart in gwfast: a property of the
  * reduced-precision form). kappa > 0; events with equilibrated condition number above it get FP64. */
 int gwf_set_refine_cond(gwf_ctx* ctx, double kappa);

@@ -860,3 +860,19 @@ def aligo_psd(f):
     """S(f) = 1e-49 [x^-4.14 - 5 x^-2 + 111 (1 - x^2 + x^4/2)/(1 + x^2/2)], x = f/215 Hz."""
     x = np.asarray(f, dtype=np.float64) / 215.
     return 1e-49 * (x ** -4.14 - 5. * x ** -2 + 111. * (1. - x * x + 0.5 * x ** 4) / (1. + 0.5 * x * x))
+
+
+def snr_derivs_arms(det, model, p, res=1000):
+    """Per-arm 4 trapz(Re(h conj(dh/dtheta)) / S, f), (11, N) each, tcoal in seconds
+    (gwfast/signal.py:938-945, :1016-1022, :1090-1094)."""
+    f, S = event_grid(det, model, p, res)
+    hs, Ds = [], []
+    for rot in det.rots:
+        D = strain_jacobian(det, model, f, p, rot)
+        D[TC_INDEX] = D[TC_INDEX] / DAY_S
+        Ds.append(D)
+        hs.append(strain(det, model, f, p, rot))
+    if det.shape == 'T':
+        Ds.append(-(Ds[0] + Ds[1]))
+        hs.append(-(hs[0] + hs[1]))
+    return [4. * _trapz((h[None] * D.conj()).real / S[None], f[None]) for h, D in zip(hs, Ds)]

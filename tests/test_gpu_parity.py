@@ -165,3 +165,45 @@ def test_errors_are_reported(gpu_lib):
         ctx.snr([999], W.IMRPhenomD().gpu_desc(), np.zeros((11, 2)), 100, out_net=np.empty(2))
     with pytest.raises(_lib.GWFError):
         ctx.add_detector(0., 0., 0., 'L', False, 10., None, np.array([2., 1.]), np.array([1., 1.]))
+
+
+@pytest.mark.parametrize('model', ['TF2', 'PhenomD', 'PhenomHM'])
+def test_snr_derivatives(gpu_lib, model):
+    """return_SNR_derivatives: per-arm 4 trapz(Re(h conj(dh/dtheta)) / S) against the oracle, and the
+    identities sum_arms 4 trapz(Re(h conj(dh/ddL)) / S) = -dL F_dLdL and the Phicoal one = 0 (the
+    network entry is divided by DetNet.SNR, which for IMRPhenomHM is gwfast's SNR without the
+    h+ hx cross term, so the identity is checked on the undivided sum)."""
+    mk, om, kind = MODELS[model]
+    ev = events(kind, 4, seed=17)
+    res = 300
+    dets = (('L1', 10.), ('ETS', 5.))
+    net = synthetic.make_network(mk(), dets=dets, earth=True)
+    allF, allDer = net.FisherMatr(dict(ev), res=res, return_SNR_derivatives=True)
+    p = O.to_params(ev)
+    worst = 0.0
+    for name, fmin in dets:
+        od = oracle_det(name, fmin, True)
+        ref = O.snr_derivs_arms(od, om, p, res)
+        snr = O.snr_arms(od, om, p, res)
+        keys = [name] if od.shape == 'L' else ['%s_%d' % (name, i) for i in range(3)]
+        for k, r, sn in zip(keys, ref, snr):
+            Fd = np.sqrt(np.abs(np.einsum('iin->in', allF[k])))
+            scale = sn.numpy()[None] / 2. * Fd          # Cauchy-Schwarz bound of each entry
+            worst = max(worst, np.max(np.abs(allDer[k] - r.numpy()) / scale))
+    print('%s SNR derivatives: max normalised error %.2e' % (model, worst))
+    assert worst < (F_TOL_HM if model == 'PhenomHM' else F_TOL)
+    snr_net = net.SNR(dict(ev), res=res)
+    d = allDer['net']
+    assert np.allclose(d[2] * snr_net, -ev['dL'] * allF['net'][2, 2], rtol=1e-9)
+    assert np.all(np.abs(d[8]) < 1e-9 * np.sqrt(np.einsum('iin->in', allF['net'])[8]))
+
+
+def test_snr_derivatives_fp32(gpu_lib):
+    ev = synthetic.bbh_events(256, seed=19)
+    net = synthetic.make_network(W.IMRPhenomD(), earth=True)
+    F64, D64 = net.FisherMatr(dict(ev), res=1000, return_SNR_derivatives=True)
+    F32, D32 = net.FisherMatr(dict(ev), res=1000, return_SNR_derivatives=True, precision='fp32')
+    Fd = np.sqrt(np.abs(np.einsum('iin->in', F64['net'])))
+    err = np.max(np.abs(D32['net'] - D64['net']) / Fd)
+    print('fp32 dSNR/dtheta max error relative to sqrt(F_aa): %.2e' % err)
+    assert err < 1e-5
