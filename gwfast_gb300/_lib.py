@@ -50,6 +50,10 @@ SIGNATURES = {
                     ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp], ctypes.c_int),
     'gwf_fisher_ex': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32, _vp, ctypes.c_int,
                        ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
+    'gwf_strain_derivs': ([_vp, ctypes.c_int, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32, ctypes.c_int, ctypes.c_int,
+                           _vp, _vp], ctypes.c_int),
+    'gwf_overlap': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32,
+                     ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     'gwf_cov': ([_vp, _vp, _i64, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     'gwf_set_refine_cond': ([_vp, _d], ctypes.c_int),
     'gwf_set_segments': ([_vp, ctypes.c_int], ctypes.c_int),
@@ -163,6 +167,23 @@ class Context:
             check(load().gwf_fisher_ex(self.h, len(ids), ptr(ids), ctypes.byref(wf), ptr(params), ld, n, int(res),
                                        ptr(res_ev), spacing, int(bool(per_arm)), PRECISION[precision], mem,
                                        ptr(out_arm), ptr(out_net), ptr(out_sd_arm), ptr(out_sd_net), stream))
+
+    def strain_derivs(self, det_id, wf, params, res, spacing=0, mem=MEM_HOST, out=None, stream=None, ld=None,
+                      n=None):
+        """d h / d theta on each event's grid: out complex128 [arms][11][N][res] (arms 1 or 3)."""
+        n = params.shape[1] if n is None else n
+        ld = params.shape[1] if ld is None else ld
+        check(load().gwf_strain_derivs(self.h, int(det_id), ctypes.byref(wf), ptr(params), ld, n, int(res), spacing,
+                                       mem, ptr(out), stream))
+
+    def overlap(self, det_ids, wf1, params1, wf2, params2, res, mem=MEM_HOST, out_ov=None, out_n1=None, out_n2=None,
+                stream=None, n=None):
+        """Per-detector 4 trapz(Re(h1 conj h2)/S), 4 trapz(|h1|^2/S), 4 trapz(|h2|^2/S), each [n_det][N]."""
+        ids = np.ascontiguousarray(det_ids, dtype=np.int32)
+        n = params1.shape[1] if n is None else n
+        check(load().gwf_overlap(self.h, len(ids), ptr(ids), ctypes.byref(wf1), ptr(params1), params1.shape[1],
+                                 ctypes.byref(wf2), ptr(params2), params2.shape[1], n, int(res), mem, ptr(out_ov),
+                                 ptr(out_n1), ptr(out_n2), stream))
 
     def set_graphs(self, on):
         """Capture repeated device-resident Fisher calls in CUDA graphs and replay them."""

@@ -1,6 +1,7 @@
 // C-ABI layer: context, detector tables, staging and launches (see include/gwfast_gb300.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -109,6 +110,7 @@ struct gwf_ctx {
   int64_t graph_rmax = 0;
   cudaEvent_t scratch_free = nullptr;  // recorded after the last launch that used the set-up scratch
   HostBuf hpar, hout;
+  DevBuf wbuf, par2, fcutb, ovb;   // strain-tangent and overlap outputs
 };
 
 namespace {
@@ -165,9 +167,17 @@ int validate_common(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_de
   return GWF_OK;
 }
 
+int stage_inputs_to(gwf_ctx* ctx, DevBuf& par, const double* params, int64_t ld, int64_t N, const int32_t* res_ev,
+                    int mem, cudaStream_t st, const double** dp, int64_t* dld, const int** dres);
+
 // stage host inputs into device buffers; returns device pointers
 int stage_inputs(gwf_ctx* ctx, const double* params, int64_t ld, int64_t N, const int32_t* res_ev, int mem,
                  cudaStream_t st, const double** dp, int64_t* dld, const int** dres) {
+  return stage_inputs_to(ctx, ctx->par, params, ld, N, res_ev, mem, st, dp, dld, dres);
+}
+
+int stage_inputs_to(gwf_ctx* ctx, DevBuf& par, const double* params, int64_t ld, int64_t N, const int32_t* res_ev,
+                    int mem, cudaStream_t st, const double** dp, int64_t* dld, const int** dres) {
   if (mem == GWF_MEM_DEVICE) {
     *dp = params;
     *dld = ld;
@@ -175,13 +185,13 @@ int stage_inputs(gwf_ctx* ctx, const double* params, int64_t ld, int64_t N, cons
     return GWF_OK;
   }
   const size_t pb = (size_t)gwf::NP * (size_t)N * sizeof(double);
-  if (ctx->par.ensure(pb ? pb : 8)) return fail(GWF_ERR_OOM, "device allocation failed (params)");
+  if (par.ensure(pb ? pb : 8)) return fail(GWF_ERR_OOM, "device allocation failed (params)");
   if (N > 0) {
-    if (ld == N) GWF_CK(cudaMemcpyAsync(ctx->par.p, params, pb, cudaMemcpyHostToDevice, st));
-    else GWF_CK(cudaMemcpy2DAsync(ctx->par.p, N * sizeof(double), params, ld * sizeof(double), N * sizeof(double),
+    if (ld == N) GWF_CK(cudaMemcpyAsync(par.p, params, pb, cudaMemcpyHostToDevice, st));
+    else GWF_CK(cudaMemcpy2DAsync(par.p, N * sizeof(double), params, ld * sizeof(double), N * sizeof(double),
                                   gwf::NP, cudaMemcpyHostToDevice, st));
   }
-  *dp = (const double*)ctx->par.p;
+  *dp = (const double*)par.p;
   *dld = N;
   *dres = nullptr;
   if (res_ev) {
@@ -509,6 +519,43 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   return GWF_OK;
 }
 
+// WFOverlap grid: upper frequency max(fcut_1, fcut_2) per event; with a detector fmax, gwfast
+// takes fmax where that maximum exceeds it and the first waveform's cut elsewhere
+// (gwfast/signal.py:1861-1867, reproduced as written)
+__global__ void fcut_pair_kernel(const double* p1, long long ld1, gwf::WfDesc w1, const double* p2, long long ld2,
+                                 gwf::WfDesc w2, double fmax, long long N, double* out) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const double f1 = gwf::model_fcut(w1, p1[n], p1[ld1 + n]);
+  const double f2 = gwf::model_fcut(w2, p2[n], p2[ld2 + n]);
+  double fu = f1 > f2 ? f1 : f2;
+  if (fmax > 0.0) fu = fu > fmax ? fmax : f1;
+  out[n] = fu;
+}
+
+gwf::WfDesc wf_dev(const gwf_wf_desc* wf) {
+  gwf::WfDesc w;
+  w.model = wf->model;
+  w.spin_ho = wf->spin_ho;
+  w.fcut_par = wf->fcut_par;
+  return w;
+}
+
+size_t stride_of(int model) {
+  return model == 0 ? gwf::setup_stride_m0() : (model == 1 ? gwf::setup_stride_m1() : gwf::setup_stride_m2());
+}
+
+cudaError_t launch_wave(const gwf::LaunchArgs& a, const gwf::WaveOut& o) {
+  return a.wf.model == 0 ? gwf::launch_wave_m0(a, o) : (a.wf.model == 1 ? gwf::launch_wave_m1(a, o) : gwf::launch_wave_m2(a, o));
+}
+
+// events per output launch so that a staging buffer of per_event bytes each stays near 1 GiB
+int64_t wave_chunk(size_t per_event) {
+  int64_t c = (int64_t)(((size_t)1 << 30) / (per_event ? per_event : 1));
+  if (c < 1) c = 1;
+  return c < gwf::kChunk ? c : gwf::kChunk;
+}
+
 }  // namespace
 
 int gwf::ctx_device(const gwf_ctx* ctx) { return ctx->device; }
@@ -555,6 +602,7 @@ int gwf_ctx_destroy(gwf_ctx* ctx) {
   ctx->seg_off.release(); ctx->seg_ctr.release(); ctx->seg_part.release(); ctx->seg_ovf.release();
   ctx->tune_out.release();
   ctx->osda.release(); ctx->osdn.release(); ctx->mix_sda.release(); ctx->mix_sdn.release();
+  ctx->wbuf.release(); ctx->par2.release(); ctx->fcutb.release(); ctx->ovb.release();
   for (auto& g : ctx->graph_cache) cudaGraphExecDestroy(g.second.exec);
   ctx->graph_cache.clear();
   ctx->hpar.release(); ctx->hout.release();
@@ -757,6 +805,165 @@ int gwf_fisher_ex(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc
                                                       : out_net, stream);
   ctx->call_sd_arm = ctx->call_sd_net = nullptr;
   return rc;
+}
+
+int gwf_strain_derivs(gwf_ctx* ctx, int det_id, const gwf_wf_desc* wf, const double* params, int64_t ld,
+                      int64_t n_events, int32_t res, int spacing, int mem, double* out, void* stream) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  rc = validate_common(ctx, 1, &det_id, wf, params, ld, n_events, res, nullptr, spacing, mem);
+  if (rc) return rc;
+  if (!out) return fail(GWF_ERR_INVALID_ARG, "no output requested");
+  const int64_t N = n_events;
+  if (N == 0) return GWF_OK;
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  const double* dp;
+  int64_t dld;
+  const int* dres;
+  rc = stage_inputs(ctx, params, ld, N, nullptr, mem, st, &dp, &dld, &dres);
+  if (rc) return rc;
+  const DetRec& r = ctx->dets[det_id];
+  const int NA = r.desc.shape == GWF_SHAPE_T ? 3 : 1;
+  const size_t per_ev = (size_t)NA * gwf::NP * (size_t)res * 2 * sizeof(double);
+  const int64_t chunk = mem == GWF_MEM_DEVICE ? (N < gwf::kChunk ? N : gwf::kChunk) : wave_chunk(per_ev);
+  const int64_t cap = chunk < N ? chunk : N;
+  if (ctx->setup.ensure((size_t)cap * stride_of(wf->model))) return fail(GWF_ERR_OOM, "device allocation failed (set-up scratch)");
+  if (mem == GWF_MEM_HOST && ctx->wbuf.ensure((size_t)cap * per_ev)) return fail(GWF_ERR_OOM, "device allocation failed (derivatives)");
+  GWF_CK(cudaStreamWaitEvent(st, ctx->scratch_free, 0));
+  gwf::LaunchArgs a;
+  a.ev.p = dp;
+  a.ev.ld = dld;
+  a.ev.N = N;
+  a.ev.n0 = 0;
+  a.ev.res = res;
+  a.ev.res_ev = nullptr;
+  a.ev.spacing = spacing;
+  a.det = dev_of(r);
+  a.wf = wf_dev(wf);
+  a.qnm = ctx->d_qnm;
+  a.nq = ctx->nq;
+  a.out_arm = a.out_det = nullptr;
+  a.accum = 0;
+  a.per_arm = 0;
+  a.precision = GWF_PREC_FP64;
+  a.scratch = (unsigned char*)ctx->setup.p;
+  a.cap_events = cap;
+  a.stream = st;
+  for (int64_t n0 = 0; n0 < N; n0 += chunk) {
+    const int64_t cnt = (N - n0) < chunk ? (N - n0) : chunk;
+    gwf::WaveOut o{};
+    o.mode = gwf::WAVE_DERIVS;
+    o.n0 = n0;
+    o.cnt = cnt;
+    o.R_out = res;
+    if (mem == GWF_MEM_DEVICE) {
+      o.out = reinterpret_cast<gwf::cd*>(out);
+      o.out_n = N;
+      o.out_base = 0;
+    } else {
+      o.out = reinterpret_cast<gwf::cd*>(ctx->wbuf.p);
+      o.out_n = cnt;
+      o.out_base = n0;
+    }
+    cudaError_t e = launch_wave(a, o);
+    if (e != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    if (mem == GWF_MEM_HOST) {   // rows [n0, n0 + cnt) of each (arm, parameter) block
+      const size_t row = (size_t)res * 2 * sizeof(double);
+      GWF_CK(cudaMemcpy2DAsync(out + (size_t)n0 * res * 2, (size_t)N * row, ctx->wbuf.p, (size_t)cnt * row,
+                               (size_t)cnt * row, (size_t)NA * gwf::NP, cudaMemcpyDeviceToHost, st));
+    }
+  }
+  GWF_CK(cudaEventRecord(ctx->scratch_free, st));
+  if (mem == GWF_MEM_HOST) GWF_CK(cudaStreamSynchronize(st));
+  return GWF_OK;
+}
+
+int gwf_overlap(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf1, const double* params1,
+                int64_t ld1, const gwf_wf_desc* wf2, const double* params2, int64_t ld2, int64_t n_events, int32_t res,
+                int mem, double* out_ov, double* out_n1, double* out_n2, void* stream) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  rc = validate_common(ctx, n_det, det_ids, wf1, params1, ld1, n_events, res, nullptr, GWF_SPACING_GEOM, mem);
+  if (!rc) rc = validate_common(ctx, n_det, det_ids, wf2, params2, ld2, n_events, res, nullptr, GWF_SPACING_GEOM, mem);
+  if (rc) return rc;
+  if (!out_ov || !out_n1 || !out_n2) return fail(GWF_ERR_INVALID_ARG, "overlap needs all three outputs");
+  const int64_t N = n_events;
+  if (N == 0) return GWF_OK;
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  const double *dp1, *dp2;
+  int64_t dld1, dld2;
+  const int* dres;
+  rc = stage_inputs(ctx, params1, ld1, N, nullptr, mem, st, &dp1, &dld1, &dres);
+  if (!rc) rc = stage_inputs_to(ctx, ctx->par2, params2, ld2, N, nullptr, mem, st, &dp2, &dld2, &dres);
+  if (rc) return rc;
+  const size_t per_ev = (size_t)2 * res * 2 * sizeof(double);   // at most two computed arms
+  const int64_t chunk = wave_chunk(per_ev);
+  const int64_t cap = chunk < N ? chunk : N;
+  const size_t stride = std::max(stride_of(wf1->model), stride_of(wf2->model));
+  if (ctx->setup.ensure((size_t)cap * stride) || ctx->wbuf.ensure((size_t)cap * per_ev) ||
+      ctx->fcutb.ensure((size_t)N * sizeof(double)) ||
+      (mem == GWF_MEM_HOST && ctx->ovb.ensure((size_t)3 * n_det * N * sizeof(double))))
+    return fail(GWF_ERR_OOM, "device allocation failed (overlap)");
+  double* dov = mem == GWF_MEM_DEVICE ? out_ov : (double*)ctx->ovb.p;
+  double* dn1 = mem == GWF_MEM_DEVICE ? out_n1 : dov + (size_t)n_det * N;
+  double* dn2 = mem == GWF_MEM_DEVICE ? out_n2 : dov + (size_t)2 * n_det * N;
+  GWF_CK(cudaStreamWaitEvent(st, ctx->scratch_free, 0));
+  gwf::LaunchArgs a;
+  a.ev.N = N;
+  a.ev.n0 = 0;
+  a.ev.res = res;
+  a.ev.res_ev = nullptr;
+  a.ev.spacing = GWF_SPACING_GEOM;
+  a.ev.fcut_ev = (const double*)ctx->fcutb.p;
+  a.qnm = ctx->d_qnm;
+  a.nq = ctx->nq;
+  a.out_arm = a.out_det = nullptr;
+  a.accum = 0;
+  a.per_arm = 0;
+  a.precision = GWF_PREC_FP64;
+  a.scratch = (unsigned char*)ctx->setup.p;
+  a.cap_events = cap;
+  a.stream = st;
+  for (int i = 0; i < n_det; ++i) {
+    const DetRec& r = ctx->dets[det_ids[i]];
+    a.det = dev_of(r);
+    fcut_pair_kernel<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(dp1, dld1, wf_dev(wf1), dp2, dld2, wf_dev(wf2),
+                                                                 r.desc.fmax, N, (double*)ctx->fcutb.p);
+    GWF_CK(cudaGetLastError());
+    for (int64_t n0 = 0; n0 < N; n0 += chunk) {
+      const int64_t cnt = (N - n0) < chunk ? (N - n0) : chunk;
+      gwf::WaveOut o{};
+      o.n0 = n0;
+      o.cnt = cnt;
+      o.out = reinterpret_cast<gwf::cd*>(ctx->wbuf.p);
+      o.out_n = cnt;
+      o.out_base = n0;
+      o.R_out = res;
+      o.ov = dov + (size_t)i * N;
+      o.n1 = dn1 + (size_t)i * N;
+      o.n2 = dn2 + (size_t)i * N;
+      o.mode = gwf::WAVE_STORE;
+      a.ev.p = dp1;
+      a.ev.ld = dld1;
+      a.wf = wf_dev(wf1);
+      cudaError_t e = launch_wave(a, o);
+      o.mode = gwf::WAVE_OVERLAP;
+      a.ev.p = dp2;
+      a.ev.ld = dld2;
+      a.wf = wf_dev(wf2);
+      if (e == cudaSuccess) e = launch_wave(a, o);
+      if (e != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    }
+  }
+  GWF_CK(cudaEventRecord(ctx->scratch_free, st));
+  if (mem == GWF_MEM_HOST) {
+    const size_t b = (size_t)n_det * N * sizeof(double);
+    GWF_CK(cudaMemcpyAsync(out_ov, dov, b, cudaMemcpyDeviceToHost, st));
+    GWF_CK(cudaMemcpyAsync(out_n1, dn1, b, cudaMemcpyDeviceToHost, st));
+    GWF_CK(cudaMemcpyAsync(out_n2, dn2, b, cudaMemcpyDeviceToHost, st));
+    GWF_CK(cudaStreamSynchronize(st));
+  }
+  return GWF_OK;
 }
 
 int gwf_cov(gwf_ctx* ctx, const double* F, int64_t N, int mem, double* cov, double* eps, double* cond, void* stream) {

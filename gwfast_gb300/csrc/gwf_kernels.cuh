@@ -45,6 +45,7 @@ struct EvBatch {
   int res;
   const int* res_ev;     // optional per-event grid length
   int spacing;           // 0 = geometric, 1 = linear
+  const double* fcut_ev = nullptr;   // optional per-event upper grid frequency (replaces the model cut and fmax)
 };
 
 struct WfDesc {
@@ -228,10 +229,16 @@ union EvUnion {
   HMEv hm;
 };
 
+// upper grid frequency of the model (gwfast/waveforms.py:903-920, :1324-1333, :2737-2750)
+__host__ __device__ inline double model_fcut(const WfDesc& wf, double Mc, double eta) {
+  return (wf.model == 0) ? wf.fcut_par / (Mc / pow(eta, 0.6)) : wf.fcut_par / (Mc * kG3 / pow(eta, 0.6));
+}
+
 __device__ inline bool grid_setup(GridEv& g, const DetDev& d, const EvBatch& ev, const WfDesc& wf, long long n,
                                   double Mc, double eta) {
-  double fcut = (wf.model == 0) ? wf.fcut_par / (Mc / pow(eta, 0.6)) : wf.fcut_par / (Mc * kG3 / pow(eta, 0.6));
+  double fcut = model_fcut(wf, Mc, eta);
   if (d.fmax > 0.0 && fcut > d.fmax) fcut = d.fmax;
+  if (ev.fcut_ev) fcut = ev.fcut_ev[n];
   const int R = ev.res_ev ? ev.res_ev[n] : ev.res;
   g.R = R;
   g.fmin = d.fmin;
@@ -275,10 +282,16 @@ __device__ inline void event_setup(EvUnion& E, const DetDev& d, const WfDesc& wf
   else hm_setup_core(E.hm, mc, et, c1, c2, dL, d.fmin);
 }
 
+// constant pi - pi/4 of the TaylorF2 phase (gwfast/waveforms.py:802, :862), left out of tf2_point
+constexpr double kTF2PhaseConst = 0.75 * kPi;
+
 // waveform at one point: P, C (hp = P, hc = i C) with tangents, iota derivatives, and tau_star tangent.
+// phi0: the waveform phase left out of P and C (22-mode models: Phi(f); HM: 0, the mode phases are in P, C)
 template <int MODEL, bool EARTH>
 __device__ __forceinline__ void wave_point_dual(const EvUnion& E, const ProjEv& pj, double f, double lnf,
-                                                cd& P, cd& C, cd* dP, cd* dC, cd& dPi, cd& dCi, D4& tau) {
+                                                cd& P, cd& C, cd* dP, cd* dC, cd& dPi, cd& dCi, D4& tau,
+                                                double& phi0) {
+  phi0 = 0.0;
   if (MODEL == 2) {
     Cplx<D4> Pd, Cd;
     Cplx<double> dPv, dCv;
@@ -299,6 +312,7 @@ __device__ __forceinline__ void wave_point_dual(const EvUnion& E, const ProjEv& 
       if (EARTH) tau = tau_star_point<D4>(E.phd.k.Ms, E.phd.k.vM, E.phd.k.eta, exp(lnf / 3.0));
     }
     // W = A e^{-i Phi} with the common phase dropped: value A, tangent dA - i A dPhi
+    phi0 = Phi.v + (MODEL == 0 ? kTF2PhaseConst : 0.0);
     P = {pj.cp * A.v, 0.0};
     C = {pj.ci * A.v, 0.0};
 #pragma unroll
@@ -309,6 +323,33 @@ __device__ __forceinline__ void wave_point_dual(const EvUnion& E, const ProjEv& 
     }
     dPi = {pj.dcp * A.v, 0.0};
     dCi = {pj.dci * A.v, 0.0};
+  }
+}
+
+// value-only waveform with its phase: P, C (hp = P, hc = i C) and phi0 as in wave_point_dual
+template <int MODEL, bool EARTH>
+__device__ __forceinline__ void wave_point_full(const EvUnion& E, const ProjEv& pj, double f, double lnf,
+                                                cd& P, cd& C, double& phi0, double& tau) {
+  if (MODEL == 2) {
+    Cplx<double> Pd, Cd, dPv, dCv;
+    hm_point<double>(E.hm, f, Pd, Cd, dPv, dCv);
+    P = {Pd.re, Pd.im};
+    C = {Cd.re, Cd.im};
+    phi0 = 0.0;
+    if (EARTH) tau = tau_star_point<double>(E.hm.k.Ms, E.hm.k.vM, E.hm.k.eta, exp(lnf / 3.0));
+  } else {
+    double A, Phi;
+    if (MODEL == 0) {
+      const double f13 = exp(lnf / 3.0);
+      tf2_point<double>(E.tf2, f, f13, lnf, exp(lnf * (-7.0 / 6.0)), A, Phi);
+      if (EARTH) tau = tau_star_point<double>(E.tf2.Ms, E.tf2.vM, E.tf2.eta, f13);
+    } else {
+      phd_point<double>(E.phd.k, f, A, Phi);
+      if (EARTH) tau = tau_star_point<double>(E.phd.k.Ms, E.phd.k.vM, E.phd.k.eta, exp(lnf / 3.0));
+    }
+    P = {pj.cp * A, 0.0};
+    C = {pj.ci * A, 0.0};
+    phi0 = Phi + (MODEL == 0 ? kTF2PhaseConst : 0.0);
   }
 }
 
@@ -539,7 +580,8 @@ __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<N
       sw = sqrt(4.0 * w / Sn);
       cd P, C, dP[4], dC[4], dPi, dCi;
       D4 tau(0.0);
-      wave_point_dual<MODEL, EARTH>(S.E, S.pj, f, lnf, P, C, dP, dC, dPi, dCi, tau);
+      double phi0;
+      wave_point_dual<MODEL, EARTH>(S.E, S.pj, f, lnf, P, C, dP, dC, dPi, dCi, tau, phi0);
       double dtn[4] = {0.0, 0.0, 0.0, 0.0};
       TimeState ts;
       if (EARTH) {

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include "gwf_kernels_f32.cuh"
+#include "gwf_wave_out.cuh"
 
 namespace gwf {
 
@@ -39,6 +40,11 @@ cudaError_t launch_fisher_m2(const LaunchArgs& a);
 cudaError_t launch_snr_m0(const LaunchArgs& a);
 cudaError_t launch_snr_m1(const LaunchArgs& a);
 cudaError_t launch_snr_m2(const LaunchArgs& a);
+// strain tangent / strain / overlap outputs (gwf_wave_out.cuh): set-up and output launch for
+// events [o.n0, o.n0 + o.cnt) of a.ev; a.scratch holds at least o.cnt records
+cudaError_t launch_wave_m0(const LaunchArgs& a, const WaveOut& o);
+cudaError_t launch_wave_m1(const LaunchArgs& a, const WaveOut& o);
+cudaError_t launch_wave_m2(const LaunchArgs& a, const WaveOut& o);
 size_t setup_stride_m0();
 size_t setup_stride_m1();
 size_t setup_stride_m2();

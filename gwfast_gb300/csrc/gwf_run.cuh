@@ -184,6 +184,23 @@ cudaError_t snr_dispatch(const LaunchArgs& a) {
   return tri ? snr_one<false, 2>(a) : snr_one<false, 1>(a);
 }
 
+template <bool EARTH, int NARM>
+cudaError_t wave_one(const LaunchArgs& a, const WaveOut& o) {
+  EvBatch ev = a.ev;
+  ev.n0 = o.n0;
+  const unsigned nb = (unsigned)((o.cnt + 63) / 64);
+  setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, a.det, a.wf, a.qnm, a.nq, a.scratch, o.cnt);
+  wave_out_kernel<M, EARTH, NARM><<<(unsigned)o.cnt, kThreads, 0, a.stream>>>(ev, a.det, a.scratch, o);
+  return cudaGetLastError();
+}
+
+cudaError_t wave_dispatch(const LaunchArgs& a, const WaveOut& o) {
+  if (o.cnt <= 0) return cudaSuccess;
+  const bool tri = a.det.shape == 1;
+  if (a.det.earth) return tri ? wave_one<true, 2>(a, o) : wave_one<true, 1>(a, o);
+  return tri ? wave_one<false, 2>(a, o) : wave_one<false, 1>(a, o);
+}
+
 }  // namespace
 
 }  // namespace gwf

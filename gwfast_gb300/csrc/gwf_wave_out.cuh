@@ -1,0 +1,163 @@
+// Strain and strain tangent written out on the event grids, and the overlap integrals of two
+// waveforms. Same per-event set-up records and per-point code as the Fisher kernels; the common
+// phase factor that the Fisher kernels leave out (it cancels in Re(conj(a) b)) is restored:
+//   h = (F+ hp + Fx hc) e^{i Psi},  Psi = 2 pi f (tcoal + Delta t_loc) - Phi_c - Phi(f)
+// (gwfast/signal.py:485-655; IMRPhenomHM: the mode phases are inside hp, hc and Phi(f) = 0).
+#pragma once
+#include "gwf_kernels.cuh"
+
+namespace gwf {
+
+enum { WAVE_DERIVS = 0, WAVE_STORE = 1, WAVE_OVERLAP = 2 };
+
+// One launch of wave_out_kernel over events [n0, n0 + cnt) of the batch.
+//  WAVE_DERIVS:  out[((arm * NP + p) * out_n + n - out_base) * R_out + k] = d h_arm / d theta_p at
+//                point k (tcoal in seconds; triangle: 3 arms, the third minus the sum of the first
+//                two), the layout of gwfast's return_derivatives per arm (signal.py:938-939).
+//  WAVE_STORE:   out[(arm * out_n + n - out_base) * R_out + k] = h_arm sqrt(4 w_k / S_k), computed
+//                arms only (1 or 2).
+//  WAVE_OVERLAP: reads the WAVE_STORE output of the first waveform at the same place and writes,
+//                summed over the arms (triangle: 3), ov[n] = sum Re(u1 conj u2), n1[n] = sum |u1|^2,
+//                n2[n] = sum |u2|^2: the trapezoid integrals 4 int Re(h1 conj h2) / S df etc.
+struct WaveOut {
+  int mode;
+  long long n0, cnt;
+  cd* out;
+  long long out_n, out_base;
+  int R_out;
+  double* ov;
+  double* n1;
+  double* n2;
+};
+
+// e^{i Psi} with Psi = 2 pi f (tc [days] + D [s]) - phi: the large tc term (up to ~1e9 rad) is
+// rotated separately, so that two waveforms with the same tcoal on the same grid share its
+// rounding exactly and their relative phase keeps full precision
+__device__ __forceinline__ cd common_phase(double f, double tc, double D, double phi) {
+  const double tpf = kTwoPi * f;
+  double s1, c1, s2, c2;
+  sincos(tpf * (tc * kDay), &s1, &c1);
+  sincos(tpf * D - phi, &s2, &c2);
+  return cmul(cd{c1, s1}, cd{c2, s2});
+}
+
+template <int MODEL, bool EARTH, int NARM>
+__global__ void __launch_bounds__(kThreads) wave_out_kernel(EvBatch ev, DetDev det, const unsigned char* scratch,
+                                                            WaveOut o) {
+  __shared__ EvUnion E;
+  __shared__ ProjEv pj;
+  __shared__ GridEv g;
+  __shared__ ArmPat apc[NARM];
+  __shared__ TimeState tsc;
+  __shared__ double red[kWarps][3];
+  const long long n = ev.n0 + blockIdx.x;
+  if (n >= ev.N) return;
+  block_load<MODEL>(E, pj, g, scratch, blockIdx.x);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (!EARTH) {
+    if (tid == 0) {
+      time_state(pj, pj.tc, tsc);
+      for (int a = 0; a < NARM; ++a) arm_pattern(pj, det.sin_zeta, tsc.x, a, apc[a]);
+    }
+    __syncthreads();
+  }
+  constexpr int NA = NARM == 2 ? 3 : 1;
+  const double phic = ev.p[8 * ev.ld + n];
+  const int R = g.ok ? g.R : 0;
+  const long long row = n - o.out_base;
+  double s[3] = {0.0, 0.0, 0.0};
+  for (int k = tid; k < o.R_out; k += kThreads) {
+    if (k >= R) {   // no valid grid for this event: zeros
+      if (o.mode == WAVE_DERIVS)
+        for (int a = 0; a < NA; ++a)
+          for (int p = 0; p < NP; ++p) o.out[((long long)(a * NP + p) * o.out_n + row) * o.R_out + k] = {0.0, 0.0};
+      else if (o.mode == WAVE_STORE)
+        for (int a = 0; a < NARM; ++a) o.out[((long long)a * o.out_n + row) * o.R_out + k] = {0.0, 0.0};
+      continue;
+    }
+    double f, lnf, w;
+    grid_point(g, ev.spacing, k, f, lnf, w);
+    if (o.mode == WAVE_DERIVS) {
+      cd P, C, dP[4], dC[4], dPi, dCi;
+      D4 tau(0.0);
+      double phi0;
+      wave_point_dual<MODEL, EARTH>(E, pj, f, lnf, P, C, dP, dC, dPi, dCi, tau, phi0);
+      double dtn[4] = {0.0, 0.0, 0.0, 0.0};
+      TimeState ts;
+      if (EARTH) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) dtn[q] = -tau.d[q] / kDay;
+        time_state(pj, pj.tc - tau.v / kDay, ts);
+      } else {
+        ts = tsc;
+      }
+      const cd ph = common_phase(f, pj.tc, ts.D, phic + phi0);
+      cd D[NARM][NP];
+#pragma unroll
+      for (int a = 0; a < NARM; ++a) {
+        ArmPat ap;
+        if (EARTH) arm_pattern(pj, det.sin_zeta, ts.x, a, ap);
+        else ap = apc[a];
+        arm_derivs(pj, ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D[a]);
+      }
+#pragma unroll
+      for (int a = 0; a < NA; ++a)
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          const cd v = a < NARM ? D[a][p] : cscale(cadd(D[0][p], D[NARM - 1][p]), -1.0);
+          o.out[((long long)(a * NP + p) * o.out_n + row) * o.R_out + k] = cmul(v, ph);
+        }
+    } else {
+      cd P, C;
+      double phi0, tau = 0.0;
+      wave_point_full<MODEL, EARTH>(E, pj, f, lnf, P, C, phi0, tau);
+      TimeState ts;
+      if (EARTH) time_state(pj, pj.tc - tau / kDay, ts);
+      else ts = tsc;
+      const double sw = sqrt(4.0 * w / psd_at(det, f, lnf));
+      const cd ph = cscale(common_phase(f, pj.tc, ts.D, phic + phi0), sw);
+      cd u[NARM];
+#pragma unroll
+      for (int a = 0; a < NARM; ++a) {
+        ArmPat ap;
+        if (EARTH) arm_pattern(pj, det.sin_zeta, ts.x, a, ap);
+        else ap = apc[a];
+        u[a] = cmul(cadd(cscale(P, ap.Fp), cscale(cmuli(C), ap.Fc)), ph);
+      }
+      if (o.mode == WAVE_STORE) {
+#pragma unroll
+        for (int a = 0; a < NARM; ++a) o.out[((long long)a * o.out_n + row) * o.R_out + k] = u[a];
+      } else {
+        cd v[NARM];
+#pragma unroll
+        for (int a = 0; a < NARM; ++a) v[a] = o.out[((long long)a * o.out_n + row) * o.R_out + k];
+#pragma unroll
+        for (int a = 0; a < NA; ++a) {
+          const cd x = a < NARM ? v[a] : cscale(cadd(v[0], v[NARM - 1]), -1.0);
+          const cd y = a < NARM ? u[a] : cscale(cadd(u[0], u[NARM - 1]), -1.0);
+          s[0] += x.re * y.re + x.im * y.im;
+          s[1] += x.re * x.re + x.im * x.im;
+          s[2] += y.re * y.re + y.im * y.im;
+        }
+      }
+    }
+  }
+  if (o.mode != WAVE_OVERLAP) return;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    double v = s[j];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if (lane == 0) red[warp][j] = v;
+  }
+  __syncthreads();
+  if (tid < 3) {
+    double v = 0.0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) v += red[w][tid];
+    double* dst = tid == 0 ? o.ov : (tid == 1 ? o.n1 : o.n2);
+    dst[n] = v;
+  }
+}
+
+}  // namespace gwf

@@ -7,7 +7,8 @@ device.
 import numpy as np
 
 from . import gwfastUtils as utils
-from .signal import fisher_batch, reparametrise, reparametrise_vec, snr_batch
+from .signal import (fisher_batch, overlap_batch, reparametrise, reparametrise_derivs, reparametrise_vec, snr_batch,
+                     strain_derivs_batch)
 
 
 class DetNet:
@@ -53,8 +54,6 @@ class DetNet:
         per-arm SNR-derivative integrals (11, N) keyed by detector (name_0..2 for triangles), plus
         'net': the Fisher total and dSNR/dtheta = sum of the integrals / network SNR (SNRs from
         kwargs['SNRs'] if given)."""
-        if return_derivatives:
-            raise NotImplementedError('return_derivatives (the (P, N, R) derivative arrays) is not implemented on the GPU path')
         utils.check_evparams(evParams)
         names, sigs = self._list()
         res = kwargs.get('res', 1000)
@@ -66,6 +65,19 @@ class DetNet:
         if kwargs.get('computeDerivFinDiff', False):
             raise NotImplementedError('finite-difference derivatives are not used on the GPU path')
         precision = kwargs.get('precision', 'fp64')
+        if return_derivatives and not return_SNR_derivatives:
+            # gwfast/network.py:126-137: per-arm Fisher matrices plus 'net', per-arm (P, N, R) derivatives
+            allF, allDer = {}, {}
+            for name, s in zip(names, sigs):
+                Fa, Da = s.FisherMatr(evParams, res=res, spacing=spacing, use_m1m2=use_m1m2, use_chi1chi2=use_chi1chi2,
+                                      return_derivatives=True, precision=precision,
+                                      refine_cond=kwargs.get('refine_cond'))
+                keys = ['%s_%s' % (name, i) for i in range(3)] if s.detector_shape == 'T' else [name]
+                for i, k in enumerate(keys):
+                    allF[k] = Fa[i]
+                    allDer[k] = Da[i]
+            allF['net'] = np.array([allF[k] for k in allF]).sum(axis=0)
+            return allF, allDer
         if return_SNR_derivatives:
             per, der = fisher_batch(sigs, evParams, res, per_arm=True, spacing=spacing, device=sigs[0].device,
                                     precision=precision, refine_cond=kwargs.get('refine_cond'),
@@ -102,3 +114,10 @@ class DetNet:
                 allF[name] = np.moveaxis(Fa[0], 0, -1)
         allF['net'] = np.array([allF[k] for k in allF]).sum(axis=0)
         return allF
+
+    def WFOverlap(self, WF1, WF2, evParams1, evParams2, res=1000, **kwargs):
+        """Network overlap of two waveforms on two parameter sets (gwfast/network.py:198-227):
+        sum_d (h1|h2)_d / sqrt(sum_d SNR1_d^2 sum_d SNR2_d^2)."""
+        names, sigs = self._list()
+        ov, n1, n2 = overlap_batch(sigs, WF1, WF2, evParams1, evParams2, res)
+        return ov.sum(axis=0) / np.sqrt(n1.sum(axis=0) * n2.sum(axis=0))

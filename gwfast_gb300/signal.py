@@ -102,6 +102,32 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
     return out
 
 
+def strain_derivs_batch(signal, evParams, res=1000, spacing='geom'):
+    """d h / d theta on each event's grid for one detector: complex128 (arms, 11, N, res), tcoal
+    row in 1/s (the per-arm arrays of gwfast's return_derivatives, gwfast/signal.py:938-939)."""
+    p = _prep(evParams)
+    N = p.shape[1]
+    arms = 1 if signal.detector_shape == 'L' else 3
+    out = np.empty((arms, 11, N, int(res)), dtype=np.complex128)
+    _lib.context(signal.device).strain_derivs(signal.det_id, signal.wf_model.gpu_desc(), p, res,
+                                              spacing=0 if spacing == 'geom' else 1, out=out)
+    return out
+
+
+def overlap_batch(signals, WF1, WF2, evParams1, evParams2, res=1000):
+    """Per detector (n_det, N) arrays (4 trapz(Re(h1 conj h2)/S), 4 trapz(|h1|^2/S), 4 trapz(|h2|^2/S)),
+    summed over each detector's arms (gwfast/signal.py:1759-1921)."""
+    p1 = _prep(evParams1)
+    p2 = _prep(evParams2)
+    if p1.shape != p2.shape:
+        raise ValueError('the two parameter sets must hold the same number of events')
+    N = p1.shape[1]
+    ov, n1, n2 = (np.empty((len(signals), N)) for _ in range(3))
+    _lib.context(signals[0].device).overlap([s.det_id for s in signals], WF1.gpu_desc(), p1, WF2.gpu_desc(), p2, res,
+                                            out_ov=ov, out_n1=n1, out_n2=n2)
+    return ov, n1, n2
+
+
 def _jacobian(evParams, N, use_m1m2, use_chi1chi2):
     J = np.broadcast_to(np.eye(11), (N, 11, 11)).copy()
     if use_m1m2:
@@ -124,6 +150,14 @@ def reparametrise(F, evParams, use_m1m2=False, use_chi1chi2=True):
         return F
     J = _jacobian(evParams, F.shape[-3], use_m1m2, use_chi1chi2)
     return np.einsum('nai,...nab,nbj->...nij', J, F, J)
+
+
+def reparametrise_derivs(D, evParams, use_m1m2=False, use_chi1chi2=True):
+    """The chain rule for strain derivatives, D: (arms, 11, N, R)."""
+    if not use_m1m2 and use_chi1chi2:
+        return D
+    J = _jacobian(evParams, D.shape[2], use_m1m2, use_chi1chi2)
+    return np.einsum('naj,xanr->xjnr', J, D)
 
 
 def reparametrise_vec(v, evParams, use_m1m2=False, use_chi1chi2=True):
@@ -185,17 +219,22 @@ class GWSignal:
         np.random.seed(None)
         self.seedUse = np.random.randint(2 ** 32 - 1, size=1) if seed is None else seed
 
-    def _apply_duty(self, arms, seed=True):
-        """Bernoulli duty-cycle masks drawn exactly as gwfast draws them (gwfast/signal.py:672-673, :729-765)."""
-        if self.DutyFactor is None:
-            return arms
+    def _duty_masks(self, n_arms, n, seed=True):
+        """Bernoulli duty-cycle masks, one per arm, drawn exactly as gwfast draws them
+        (gwfast/signal.py:672-673, :729-765, :809-810, :932-937)."""
         if seed:
             np.random.seed(self.seedUse)
+        return [np.random.choice([0, 1], n, p=[1. - self.DutyFactor, self.DutyFactor]) for _ in range(n_arms)]
+
+    def _apply_duty(self, arms, seed=True, masks=None):
+        """arms: (arms, N, ...) with the duty-cycle mask of each arm applied."""
+        if self.DutyFactor is None:
+            return arms
         out = np.array(arms, copy=True)
         n = out.shape[1]
+        masks = self._duty_masks(out.shape[0], n, seed) if masks is None else masks
         for a in range(out.shape[0]):
-            excl = np.random.choice([0, 1], n, p=[1. - self.DutyFactor, self.DutyFactor])
-            out[a] = out[a] * excl.reshape((n,) + (1,) * (out.ndim - 2))
+            out[a] = out[a] * masks[a].reshape((n,) + (1,) * (out.ndim - 2))
         return out
 
     def _snr_arms(self, evParams, res, precision='fp64'):
@@ -215,11 +254,23 @@ class GWSignal:
 
         precision='fp32' selects the split-precision kernel (TaylorF2 and IMRPhenomD), 'mixed' the
         split-precision kernel with FP64 recomputation of ill-conditioned events (refine_cond)."""
-        if return_derivatives:
-            raise NotImplementedError('return_derivatives (the (P, N, R) derivative arrays) is not implemented on the GPU path')
         if computeDerivFinDiff:
             raise NotImplementedError('finite-difference derivatives are not used on the GPU path')
         res = self._resolve_res(evParams, res, df)
+        if return_derivatives and not return_SNR_derivatives:
+            # as gwfast: per-arm Fisher matrices and per-arm (P, N, R) strain derivatives, the same
+            # duty-cycle mask on both
+            Fa = fisher_batch([self], evParams, res, per_arm=True, spacing=spacing, device=self.device,
+                              precision=precision, refine_cond=kwargs.get('refine_cond'))
+            Fa = np.asarray(Fa[0])
+            D = strain_derivs_batch(self, evParams, res, spacing)
+            if self.DutyFactor is not None:
+                # fisher_batch applied the masks drawn from the seed; draw the same ones for D
+                masks = self._duty_masks(D.shape[0], D.shape[2])
+                D = D * np.stack(masks)[:, None, :, None]
+            Fa = reparametrise(Fa, evParams, use_m1m2, use_chi1chi2)
+            D = reparametrise_derivs(D, evParams, use_m1m2, use_chi1chi2)
+            return [np.moveaxis(F, 0, -1) for F in Fa], [D[i] for i in range(D.shape[0])]
         if return_SNR_derivatives:
             # as gwfast: per-arm Fisher matrices and per-arm (P, N) SNR-derivative integrals
             Fa, Da = fisher_batch([self], evParams, res, per_arm=True, spacing=spacing, device=self.device,
@@ -234,6 +285,14 @@ class GWSignal:
         if return_all:
             return arms
         return arms[0] if self.detector_shape == 'L' else np.sum(arms, axis=0)
+
+    def WFOverlap(self, WF1, WF2, evParams1, evParams2, res=1000, return_separate=False, **kwargs):
+        """Overlap of two waveforms on two parameter sets in this detector (gwfast/signal.py:1759-1921).
+        return_separate: (4 trapz(Re(h1 conj h2)/S), SNR_1, SNR_2) instead of the overlap."""
+        ov, n1, n2 = overlap_batch([self], WF1, WF2, evParams1, evParams2, res)
+        if return_separate:
+            return ov[0], np.sqrt(n1[0]), np.sqrt(n2[0])
+        return ov[0] / np.sqrt(n1[0] * n2[0])
 
     def _resolve_res(self, evParams, res, df):
         if res is None and df is not None:

@@ -123,6 +123,27 @@ int gwf_fisher_ex(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc
                   int mem, double* out_arm, double* out_net, double* out_snr_der_arm, double* out_snr_der_net,
                   void* stream);
 
+/* Strain derivatives on the frequency grid of each event, one detector (GWSignal.FisherMatr with
+ * return_derivatives=True, gwfast/signal.py:938-939, :974-975, :1014-1015, :1048-1049, :1078-1079;
+ * gwfast/network.py:130-137). out: complex128 as interleaved (re, im) doubles,
+ * [arms][11][N][res], arms = 1 (L) or 3 (triangle; the third arm is minus the sum of the first
+ * two); d h / d theta in the Fisher parameter order with the tcoal row in 1/s. FP64, one res for
+ * all events (as gwfast). With mem = GWF_MEM_HOST the output is staged through a device buffer of
+ * about 1 GiB per launch. */
+int gwf_strain_derivs(gwf_ctx* ctx, int det_id, const gwf_wf_desc* wf, const double* params, int64_t ld,
+                      int64_t n_events, int32_t res, int spacing, int mem, double* out, void* stream);
+
+/* Overlap integrals of two waveforms on two parameter sets (GWSignal.WFOverlap with
+ * return_separate=True, gwfast/signal.py:1759-1921; DetNet.WFOverlap, gwfast/network.py:198-227).
+ * Per detector i and event n, on the geometric grid from fmin to max(fcut_1, fcut_2) (with a
+ * detector fmax: fmax where that maximum exceeds it, else fcut_1, as gwfast), summed over the
+ * detector's arms: out_ov[i][n] = 4 trapz(Re(h1 conj h2) / S), out_n1[i][n] = 4 trapz(|h1|^2 / S),
+ * out_n2[i][n] = 4 trapz(|h2|^2 / S). The overlap is out_ov / sqrt(out_n1 out_n2) after summing
+ * each over detectors. FP64. */
+int gwf_overlap(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf1, const double* params1,
+                int64_t ld1, const gwf_wf_desc* wf2, const double* params2, int64_t ld2, int64_t n_events, int32_t res,
+                int mem, double* out_ov, double* out_n1, double* out_n2, void* stream);
+
 /* Condition-number threshold of GWF_PREC_MIXED (no counterpart in gwfast: a property of the
  * reduced-precision form). kappa > 0; events with equilibrated condition number above it get FP64. */
 int gwf_set_refine_cond(gwf_ctx* ctx, double kappa);

@@ -876,3 +876,41 @@ def snr_derivs_arms(det, model, p, res=1000):
         Ds.append(-(Ds[0] + Ds[1]))
         hs.append(-(hs[0] + hs[1]))
     return [4. * _trapz((h[None] * D.conj()).real / S[None], f[None]) for h, D in zip(hs, Ds)]
+
+
+def strain_derivs_arms(det, model, p, res=1000, spacing='geom'):
+    """Per-arm d h / d theta on the event grids, (11, N, R) complex each, tcoal row in 1/s
+    (gwfast/signal.py:913-916, :938-939; triangle arms: 0, 60 degrees and minus their sum, :1057)."""
+    f, _ = event_grid(det, model, p, res, spacing)
+    Ds = []
+    for rot in det.rots:
+        D = strain_jacobian(det, model, f, p, rot)
+        D[TC_INDEX] = D[TC_INDEX] / DAY_S
+        Ds.append(D)
+    if det.shape == 'T':
+        Ds.append(-(Ds[0] + Ds[1]))
+    return Ds
+
+
+def overlap_parts(det, model1, p1, model2, p2, res=1000):
+    """One detector of WFOverlap (gwfast/signal.py:1759-1921): (h1|h2), SNR_1^2, SNR_2^2 summed over
+    the arms, on the geometric grid from fmin to max(fcut_1, fcut_2) (with fmax: fmax where that
+    maximum exceeds it, else fcut_1, as :1865-1866 reads)."""
+    fc1 = model1.fcut(p1['Mc'], p1['eta']).reshape(-1).detach().numpy()
+    fc2 = model2.fcut(p2['Mc'], p2['eta']).reshape(-1).detach().numpy()
+    fu = np.where(fc1 > fc2, fc1, fc2)
+    if det.fmax is not None:
+        fu = np.where(fu > det.fmax, det.fmax, fc1)
+    fn = freq_grid(det.fmin, fu, res)
+    S = psd_on_grid(det, fn)
+    f = torch.as_tensor(fn, dtype=DT)
+    h1 = [strain(det, model1, f, p1, rot) for rot in det.rots]
+    h2 = [strain(det, model2, f, p2, rot) for rot in det.rots]
+    if det.shape == 'T':
+        h1.append(-(h1[0] + h1[1]))
+        h2.append(-(h2[0] + h2[1]))
+    ov = sum(4. * _trapz((a * b.conj()).real / S, f) for a, b in zip(h1, h2))
+    n1 = sum(4. * _trapz((a * a.conj()).real / S, f) for a in h1)
+    n2 = sum(4. * _trapz((b * b.conj()).real / S, f) for b in h2)
+    return ov, n1, n2
+
