@@ -293,7 +293,7 @@ int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const
     a.out_sd_det = csdn;
     a.accum = i > 0;
     const int model = a.wf.model;
-    e = model == 0 ? gwf::launch_fisher_m0(a) : gwf::launch_fisher_m1(a);
+    e = model == 0 ? gwf::launch_fisher_m0(a) : (model == 1 ? gwf::launch_fisher_m1(a) : gwf::launch_fisher_m2(a));
     if (e != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
     slot += r.desc.shape == GWF_SHAPE_T ? 3 : 1;
   }
@@ -347,8 +347,8 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
   if (!out_arm && !out_net) return fail(GWF_ERR_INVALID_ARG, "no output requested");
   if (precision != GWF_PREC_FP64 && precision != GWF_PREC_FP32 && precision != GWF_PREC_MIXED)
     return fail(GWF_ERR_INVALID_ARG, "bad precision");
-  if (precision != GWF_PREC_FP64 && wf->model == GWF_WF_PHENOMHM)
-    return fail(GWF_ERR_UNSUPPORTED, "FP32 split precision is implemented for TaylorF2 and IMRPhenomD");
+  if (precision != GWF_PREC_FP64 && wf->model == GWF_WF_PHENOMHM && !fisher)
+    return fail(GWF_ERR_UNSUPPORTED, "the FP32 SNR is implemented for TaylorF2 and IMRPhenomD");
   if (precision == GWF_PREC_MIXED && !fisher) return fail(GWF_ERR_INVALID_ARG, "the mixed form is a Fisher form");
   if (fisher && !per_arm) out_arm = nullptr;
   if (fisher && per_arm && !out_arm) return fail(GWF_ERR_INVALID_ARG, "per_arm needs out_arm");

@@ -1,4 +1,4 @@
-// FP32 split-precision Fisher kernel for the 22-mode models (TaylorF2, IMRPhenomD).
+// FP32 split-precision Fisher kernel (TaylorF2, IMRPhenomD; IMRPhenomHM with FP64 mode phases).
 //
 // Precision split:
 //  - per event, everything parameter-dependent is evaluated in FP64 duals (the same set-up
@@ -20,6 +20,9 @@
 //    indefinite.
 // The overall phase factor cancels in every Gram entry and is never formed (as in FP64).
 #pragma once
+#include <cstddef>
+#include <type_traits>
+
 #include "gwf_kernels.cuh"
 
 namespace gwf {
@@ -312,6 +315,160 @@ __device__ __forceinline__ void point_f32(const EvUnionF& EF, const PBF& pbf, co
   }
 }
 
+// ------------------------------------------------------------------ IMRPhenomHM, split precision
+// Per event the model record exists twice: FP64 values (for the mode phases) and FP32 duals (for
+// amplitudes and tangents, the amplitude prefactor divided out as for the 22-mode models). Per
+// point every mode phase is evaluated in FP64 and reduced modulo 2 pi before it reaches FP32: the
+// phases reach 1e4-1e5 rad at low frequency, and their differences between modes set the
+// interference in the mode sum, so FP32 could not carry them to the ~1e-7 rad the sum needs.
+// Amplitudes, phase tangents, harmonics and the mode sums run in FP32 duals.
+struct HMF32 {
+  HMEvT<DF4> e32;
+  HMEvT<double> e64;
+};
+struct NoRec {};
+
+// FP64 dual -> FP32 dual, with the chi1 tangent replaced by d/dchi1 - alpha d/dchi2 (see
+// setup_f32_kernel) and value and tangents multiplied by scale
+__device__ inline DF4 to_df4(const D4& d, double alpha, double scale) {
+  DF4 r;
+  r.v = (float)(d.v * scale);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const double t = q == P_CHI1 ? d.d[P_CHI1] - alpha * d.d[P_CHI2] : d.d[q];
+    r.d[q] = (float)(t * scale);
+  }
+  return r;
+}
+
+constexpr int kHMModeDuals = 20;   // leading dual members of HMModeT (rho ... hi4)
+
+__device__ inline void hm_round(const HMEv& s, HMF32& d, double amp, double alpha) {
+  static_assert(sizeof(PhdCoreT<D4>) % sizeof(D4) == 0, "core holds only duals");
+  static_assert(sizeof(PhdCoreT<D4>) / sizeof(D4) == sizeof(PhdCoreT<DF4>) / sizeof(DF4) &&
+                sizeof(PhdCoreT<D4>) / sizeof(D4) == sizeof(PhdCoreT<double>) / sizeof(double), "core layouts");
+  static_assert(offsetof(HMModeT<D4>, yp) == kHMModeDuals * sizeof(D4) &&
+                offsetof(HMModeT<DF4>, yp) >= kHMModeDuals * sizeof(DF4) &&
+                offsetof(HMModeT<double>, yp) == kHMModeDuals * sizeof(double), "mode layouts");
+  const int n = (int)(sizeof(PhdCoreT<D4>) / sizeof(D4));
+  const D4* a = reinterpret_cast<const D4*>(&s.k);
+  DF4* b = reinterpret_cast<DF4*>(&d.e32.k);
+  double* c = reinterpret_cast<double*>(&d.e64.k);
+  const D4* ampm = &s.k.ampPref;
+  for (int i = 0; i < n; ++i) {
+    b[i] = to_df4(a[i], alpha, a + i == ampm ? 1.0 / amp : 1.0);
+    c[i] = a[i].v;
+  }
+  d.e32.phi0 = to_df4(s.phi0, alpha, 1.0);
+  d.e64.phi0 = s.phi0.v;
+  for (int m = 0; m < 6; ++m) {
+    const HMMode& sm = s.md[m];
+    HMModeT<DF4>& fm = d.e32.md[m];
+    HMModeT<double>& vm = d.e64.md[m];
+    const D4* sa = reinterpret_cast<const D4*>(&sm);
+    DF4* fa = reinterpret_cast<DF4*>(&fm);
+    double* va = reinterpret_cast<double*>(&vm);
+    for (int i = 0; i < kHMModeDuals; ++i) {
+      fa[i] = to_df4(sa[i], alpha, 1.0);
+      va[i] = sa[i].v;
+    }
+    fm.yp = vm.yp = sm.yp; fm.yc = vm.yc = sm.yc; fm.dyp = vm.dyp = sm.dyp; fm.dyc = vm.dyc = sm.dyc;
+    fm.ysp = vm.ysp = sm.ysp; fm.ysm = vm.ysm = sm.ysm; fm.shift = vm.shift = sm.shift;
+    fm.l = vm.l = sm.l; fm.m = vm.m = sm.m;
+  }
+}
+
+// derivative vectors of IMRPhenomHM at one point, FP32 form (as point_f32; the psi slot holds
+// Delta = dh/dpsi - 2 s dh/dPhicoal = 2 (P - s C)(Fx + i s F+), with P - s C summed over the modes
+// from the harmonic differences yp - s yc formed in FP64, so it keeps FP32 relative accuracy near
+// face-on and face-off)
+template <bool EARTH, int NARM>
+__device__ __forceinline__ void point_f32_hm(const HMF32& H, const ProjF& pf, const ArmF* apc, const TimeF& tsc,
+                                             float f, cf (&D)[NARM][NP], cf (&Hs)[NARM]) {
+  const HMEvT<DF4>& e = H.e32;
+  const HMEvT<double>& v = H.e64;
+  const double x64 = v.k.MG * (double)f;
+  const DF4 x = e.k.MG * f;
+  const double lin64 = v.k.t0 * (x64 - v.k.fRef);
+  const DF4 lin = e.k.t0 * (x - e.k.fRef);
+  const bool spos = pf.sgn > 0.0f;
+  cf P = {0.0f, 0.0f}, C = {0.0f, 0.0f}, dPi = {0.0f, 0.0f}, dCi = {0.0f, 0.0f}, Q = {0.0f, 0.0f};
+  cf dP[4], dC[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) { dP[q] = {0.0f, 0.0f}; dC[q] = {0.0f, 0.0f}; }
+#pragma unroll 1
+  for (int mode = 0; mode < 6; ++mode) {
+    const HMModeT<DF4>& m = e.md[mode];
+    const HMModeT<double>& mv = v.md[mode];
+    const double ai64 = 2.0 / mv.m;
+    const float ai = 2.0f / (float)m.m;
+    // amplitude: frequency map chosen on the FP64 argument, as the FP64 kernel does
+    DF4 fs;
+    if (x64 < mv.fia) fs = x * ai;
+    else if (x64 < mv.frlm) fs = x * m.ama + m.bma;
+    else fs = x - m.frlm + e.k.fring;
+    DF4 amp = e.k.ampPref * (1.0f / (fs * dsqrt(dcbrt(fs)))) * complete_amp_shape(e.k, fs);
+    if (mode != 1) {
+      amp = amp * hm_absH(m, mode, x) * hm_absH(m, mode, fs) / hm_absH(m, mode, x * ai);
+      if (!(amp.v == amp.v)) amp = DF4(0.0f);   // nan_to_num at equal mass (gwfast/waveforms.py:2582)
+    }
+    // phase: value in FP64, tangent in FP32
+    double ph64;
+    DF4 ph;
+    if (x64 < mv.fip) {
+      ph64 = complete_phase<double>(v.k, x64 * ai64, mv.C1, mv.C2, mv.rho, mv.tau) / ai64;
+      ph = complete_phase<DF4>(e.k, x * ai, m.C1, m.C2, m.rho, m.tau) / ai;
+    } else if (x64 < mv.frlm) {
+      ph64 = mv.PhDBA - mv.PhDB + complete_phase<double>(v.k, x64 * mv.amp_ + mv.bmp, mv.C1, mv.C2, mv.rho, mv.tau) / mv.amp_;
+      ph = m.PhDBA - m.PhDB + complete_phase<DF4>(e.k, x * m.amp_ + m.bmp, m.C1, m.C2, m.rho, m.tau) / m.amp_;
+    } else {
+      ph64 = mv.phC - mv.PhDC + complete_phase<double>(v.k, x64 * mv.rho, mv.C1, mv.C2, mv.rho, mv.tau) / mv.rho;
+      ph = m.phC - m.PhDC + complete_phase<DF4>(e.k, x * m.rho, m.C1, m.C2, m.rho, m.tau) / m.rho;
+    }
+    ph64 = ph64 - lin64 - (double)mv.m * v.phi0 + mv.shift;
+    ph = ph - lin - (float)m.m * e.phi0;   // its value is not used
+    const double red = ph64 - kTwoPi * rint(ph64 * (1.0 / kTwoPi));
+    float sn, cs;
+    sincosf((float)red, &sn, &cs);
+    // mode term amp e^{-i phase} and its tangent (d amp - i amp d phase) e^{-i phase}
+    const float a = amp.v;
+    const cf M = {a * cs, -a * sn};
+    const float yp = (float)m.yp, yc = (float)m.yc;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float re0 = amp.d[q], im0 = -a * ph.d[q];
+      const cf dM = {re0 * cs + im0 * sn, im0 * cs - re0 * sn};
+      dP[q] = fadd(dP[q], fscale(dM, yp));
+      dC[q] = fadd(dC[q], fscale(dM, yc));
+    }
+    P = fadd(P, fscale(M, yp));
+    C = fadd(C, fscale(M, yc));
+    dPi = fadd(dPi, fscale(M, (float)m.dyp));
+    dCi = fadd(dCi, fscale(M, (float)m.dyc));
+    Q = fadd(Q, fscale(M, (float)(spos ? m.ysp : m.ysm)));
+  }
+  float dtn[4] = {0.f, 0.f, 0.f, 0.f};
+  TimeF ts;
+  if (EARTH) {
+    const DF4 tau = tau_star_point<DF4>(e.k.Ms, e.k.vM, e.k.eta, cbrtf(f));
+#pragma unroll
+    for (int q = 0; q < 4; ++q) dtn[q] = -tau.d[q] * (1.0f / 86400.0f);
+    time_f(pf, -tau.v * (1.0f / 86400.0f), ts);
+  } else {
+    ts = tsc;
+  }
+#pragma unroll
+  for (int a = 0; a < NARM; ++a) {
+    ArmF ap;
+    if (EARTH) arm_f(pf, ts, a, ap);
+    else ap = apc[a];
+    arm_derivs_f(pf, ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D[a]);
+    const float wr = ap.Fc, wi = pf.sgn * ap.Fp;
+    D[a][I_PS] = {2.0f * (Q.re * wr - Q.im * wi), 2.0f * (Q.re * wi + Q.im * wr)};
+    Hs[a] = fadd(fscale(P, ap.Fp), fscale(fmuli(C), ap.Fc));
+  }
+}
+
 // 2x3 register blocks covering the upper triangle of the padded 12x12 Gram matrix
 static __constant__ unsigned char kBlkR[16] = {0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2, 3, 3, 4, 4, 5};
 static __constant__ unsigned char kBlkC[16] = {0, 1, 2, 3, 0, 1, 2, 3, 1, 2, 3, 2, 3, 2, 3, 3};
@@ -358,8 +515,8 @@ struct __align__(16) F32Rec {
   double psi_sgn;   // sign of cos(iota): the psi column is Delta (see point_f32)
   double chi_alpha; // the chi1z tangent is d/dchi1 - alpha d/dchi2 (see setup_f32_kernel)
   double lnfmin, delta;
-  EvUnionF ef;
-  PBF pbf;
+  typename std::conditional<MODEL == 2, HMF32, EvUnionF>::type ef;
+  typename std::conditional<MODEL == 2, NoRec, PBF>::type pbf;
   ProjF pf;
   ArmF apc[2];
   TimeF tsc;
@@ -378,19 +535,28 @@ __global__ void __launch_bounds__(64) setup_f32_kernel(DetDev det, const unsigne
   const EvUnion& E = *reinterpret_cast<const EvUnion*>(rec + sizeof(SetupHdr));
   F32Rec<MODEL>& r = *reinterpret_cast<F32Rec<MODEL>*>(scratch32 + i * f32_stride<MODEL>());
   const GridEv& g = h.g;
-  const double amp = g.ok ? (MODEL == 0 ? E.tf2.ampK.v : E.phd.k.ampPref.v) : 1.0;
   // chi1z and chi2z enter the phase almost only through one combination, so d/dchi1 and d/dchi2
   // are nearly parallel and their information sits in a small difference. The FP32 form carries
-  // d/dchi1 - alpha d/dchi2 instead, alpha from the spin-orbit (f^-2/3) term of the phase basis,
+  // d/dchi1 - alpha d/dchi2 instead, alpha from the spin-orbit (f^-2/3) phase coefficient,
   // which that combination cancels in FP64; write_gram restores d/dchi1 in FP64.
-  double alpha = 0.0;
-  const PhaseBasis& pb = *rec_basis<MODEL>(scratch, i);
-  if (g.ok) {
-    const double c1 = pb.ins[2].d[P_CHI1], c2 = pb.ins[2].d[P_CHI2];
-    if (fabs(c2) > 1e-300 && isfinite(c1 / c2)) alpha = c1 / c2;
-    pbf_fill(pb, r.pbf, alpha);
-    if (MODEL == 0) round_struct(E.tf2, r.ef.tf2, &E.tf2.ampK, amp, alpha);
-    else round_struct(E.phd.k, r.ef.phd, &E.phd.k.ampPref, amp, alpha);
+  double alpha = 0.0, amp = 1.0;
+  if constexpr (MODEL == 2) {
+    if (g.ok) {
+      amp = E.hm.k.ampPref.v;
+      const double c1 = E.hm.k.pn.c3.d[P_CHI1], c2 = E.hm.k.pn.c3.d[P_CHI2];
+      if (fabs(c2) > 1e-300 && isfinite(c1 / c2)) alpha = c1 / c2;
+      hm_round(E.hm, r.ef, amp, alpha);
+    }
+  } else {
+    const PhaseBasis& pb = *rec_basis<MODEL>(scratch, i);
+    if (g.ok) {
+      amp = MODEL == 0 ? E.tf2.ampK.v : E.phd.k.ampPref.v;
+      const double c1 = pb.ins[2].d[P_CHI1], c2 = pb.ins[2].d[P_CHI2];
+      if (fabs(c2) > 1e-300 && isfinite(c1 / c2)) alpha = c1 / c2;
+      pbf_fill(pb, r.pbf, alpha);
+      if (MODEL == 0) round_struct(E.tf2, r.ef.tf2, &E.tf2.ampK, amp, alpha);
+      else round_struct(E.phd.k, r.ef.phd, &E.phd.k.ampPref, amp, alpha);
+    }
   }
   r.chi_alpha = alpha;
   r.scale = amp * amp / det.psd_scale;
@@ -504,7 +670,8 @@ __device__ inline void f32_item(const EvBatch& ev, const DetDev& det, F32State<M
       grid.point(r, ev.spacing, k, lane, f, lnf, w);
       const float Sn = psd_at_f(det, f, lnf, gf.acc_l0, gf.acc_idl);
       sw = sqrtf(4.0f * w / Sn);
-      point_f32<MODEL, EARTH, NARM>(r.ef, r.pbf, r.pf, r.apc, r.tsc, f, lnf, D, Hs);
+      if constexpr (MODEL == 2) point_f32_hm<EARTH, NARM>(r.ef, r.pf, r.apc, r.tsc, f, D, Hs);
+      else point_f32<MODEL, EARTH, NARM>(r.ef, r.pbf, r.pf, r.apc, r.tsc, f, lnf, D, Hs);
     } else {
 #pragma unroll
       for (int a = 0; a < NARM; ++a) {

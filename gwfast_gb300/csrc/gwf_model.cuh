@@ -19,6 +19,7 @@ enum { P_MC = 0, P_ETA = 1, P_CHI1 = 2, P_CHI2 = 3 };
 using DF4 = Dual<float, 4>;
 template <class S, class C> struct CoT;
 template <> struct CoT<double, D4> { __device__ __forceinline__ static double get(const D4& c) { return c.v; } };
+template <> struct CoT<double, double> { __device__ __forceinline__ static double get(double c) { return c; } };
 template <> struct CoT<D4, D4> { __device__ __forceinline__ static D4 get(const D4& c) { return c; } };
 template <> struct CoT<float, DF4> { __device__ __forceinline__ static float get(const DF4& c) { return c.v; } };
 template <> struct CoT<DF4, DF4> { __device__ __forceinline__ static DF4 get(const DF4& c) { return c; } };
@@ -526,6 +527,7 @@ template <class C> struct HMModeT {
   C fia, ama, bma;                          // amplitude frequency map
   C hr1, hr2, hr3, hr4, hi4;                // PN amplitude polynomial H(v) = v (hr1 + v (hr2 + v (hr3 + v (hr4 + i hi4))))
   double yp, yc, dyp, dyc;                  // 0.5(Y +- (-1)^l Y_{l-m}) and d/diota
+  double ysp, ysm;                          // yp - yc = (-1)^l Y_{l-m} and yp + yc = Y, formed directly
   double shift;
   int l, m;
 };
@@ -660,6 +662,8 @@ __device__ inline void hm_setup_mode(HMEv& e, int mode, const D4& eta, const D4&
   md.yc = 0.5 * (Y - sg * Ym);
   md.dyp = 0.5 * (dY + sg * dYm);
   md.dyc = 0.5 * (dY - sg * dYm);
+  md.ysp = sg * Ym;
+  md.ysm = Y;
 }
 
 // |H_lm(v)| for v = (2 pi x / m)^(1/3)

@@ -31,10 +31,8 @@ cudaError_t chunked(const LaunchArgs& a, bool f32, MAIN main) {
     const long long cnt = (a.ev.N - n0) < kChunk ? (a.ev.N - n0) : kChunk;
     const unsigned nb = (unsigned)((cnt + 63) / 64);
     setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, a.det, a.wf, a.qnm, a.nq, a.scratch, cnt);
-#if GWF_MODEL < 2
     if (f32) setup_f32_kernel<M><<<nb, 64, 0, a.stream>>>(a.det, a.scratch, scratch32_of(a), cnt,
                                                           a.det.shape == 1 ? 2 : 1, a.det.earth);
-#endif
     const cudaError_t e = main(ev, cnt);
     if (e != cudaSuccess) return e;
   }
@@ -98,7 +96,6 @@ cudaError_t fisher_one(const LaunchArgs& a) {
   });
 }
 
-#if GWF_MODEL < 2
 template <bool EARTH, int NARM, int NG>
 cudaError_t fisher_one_f32(const LaunchArgs& a) {
   const int smem = kWarps * NG * 12 * 32 * (int)sizeof(int2);
@@ -125,7 +122,6 @@ cudaError_t fisher_one_f32(const LaunchArgs& a) {
     return seg_chunk<NG>(a, ev, cnt, ks, s32, smem, grid, rec0, stride_d);
   });
 }
-#endif
 
 template <bool EARTH, int NARM>
 cudaError_t snr_one(const LaunchArgs& a) {
@@ -139,16 +135,12 @@ cudaError_t snr_one(const LaunchArgs& a) {
 cudaError_t fisher_dispatch(const LaunchArgs& a) {
   const bool tri = a.det.shape == 1;
   if (a.precision == 1) {
-#if GWF_MODEL < 2
     if (a.det.earth) {
       if (!tri) return fisher_one_f32<true, 1, 1>(a);
       return a.per_arm ? fisher_one_f32<true, 2, 3>(a) : fisher_one_f32<true, 2, 2>(a);
     }
     if (!tri) return fisher_one_f32<false, 1, 1>(a);
     return a.per_arm ? fisher_one_f32<false, 2, 3>(a) : fisher_one_f32<false, 2, 2>(a);
-#else
-    return cudaErrorNotSupported;
-#endif
   }
   if (a.det.earth) {
     if (!tri) return fisher_one<true, 1, 1>(a);

@@ -4,7 +4,7 @@
 
 namespace gwf {
 
-size_t setup_stride_m2() { return rec_stride<2>() + (GWF_MODEL < 2 ? f32_stride<2>() : 0); }
+size_t setup_stride_m2() { return rec_stride<2>() + f32_stride<2>(); }
 cudaError_t launch_fisher_m2(const LaunchArgs& a) { return fisher_dispatch(a); }
 cudaError_t launch_snr_m2(const LaunchArgs& a) { return snr_dispatch(a); }
 cudaError_t launch_wave_m2(const LaunchArgs& a, const WaveOut& o) { return wave_dispatch(a, o); }

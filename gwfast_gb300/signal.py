@@ -66,7 +66,7 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
     snr_derivs: also return, per signal, (arms, N, 11) of 4 trapz(Re(h conj(dh/dtheta)) / S) (the
     per-arm SNR-derivative integrals of gwfast's return_SNR_derivatives); the Fisher part is then
     per arm.
-    precision: 'fp64' (the drop-in), 'fp32' (split precision, TaylorF2 and IMRPhenomD), or
+    precision: 'fp64' (the drop-in), 'fp32' (split precision; IMRPhenomHM with FP64 mode phases), or
     'mixed' ('fp32', then FP64 for the events whose network Fisher has an equilibrated condition
     number above refine_cond, default 1e12).
     """
@@ -252,7 +252,7 @@ class GWSignal:
                    return_derivatives=False, return_SNR_derivatives=False, precision='fp64', **kwargs):
         """gwfast/signal.py:782-1098; returns (11, 11, N), or a list per arm with return_all.
 
-        precision='fp32' selects the split-precision kernel (TaylorF2 and IMRPhenomD), 'mixed' the
+        precision='fp32' selects the split-precision kernel (all three models), 'mixed' the
         split-precision kernel with FP64 recomputation of ill-conditioned events (refine_cond)."""
         if computeDerivFinDiff:
             raise NotImplementedError('finite-difference derivatives are not used on the GPU path')

@@ -64,12 +64,50 @@ def test_fp32_per_arm_sums_to_total(gpu_lib):
     assert entry_err(np.moveaxis(Ft, -1, 0), np.moveaxis(S, -1, 0)).max() < 1e-5
 
 
-def test_fp32_rejected_for_hm(gpu_lib):
+def hm_events(n, seed):
+    """IMRPhenomHM catalogue distributions: m1 power law on [5, 150], q ~ U[0.1, 1], chi ~ U[-0.9, 0.9]."""
+    return synthetic.bbh_events(n, seed=seed, mmax=150., qmin=0.1, chimax=0.9, dl=(0.5, 20.))
+
+
+@pytest.mark.parametrize('earth', [True, False])
+def test_phenomhm_network_fp32(gpu_lib, earth):
+    """IMRPhenomHM split precision (FP64 mode phases, FP32 amplitudes, tangents and mode sums)."""
+    ev = hm_events(256, seed=1003)
+    net = synthetic.make_network(W.IMRPhenomHM(), dets=synthetic.NETWORK_ET_CE, earth=earth)
+    F64 = np.moveaxis(net.FisherMatr(dict(ev), res=1000), -1, 0)
+    F32 = np.moveaxis(net.FisherMatr(dict(ev), res=1000, precision='fp32'), -1, 0)
+    e = entry_err(F32, F64)
+    se, cond = sigma_err(F32, F64)
+    worst = se.max(axis=1)
+    ok = cond < 1e12
+    print('PhenomHM fp32 entry err max %.2e median %.2e; sigma err median %.2e p95 %.2e max %.2e; frac<=1e-3 %.4f;'
+          ' cond<1e12: %d events, max %.2e'
+          % (e.max(), np.median(e.max(axis=(1, 2))), np.median(worst), np.percentile(worst, 95), worst.max(),
+             np.mean(worst <= 1e-3), ok.sum(), worst[ok].max()))
+    assert np.median(e.max(axis=(1, 2))) < 1e-4
+    assert np.mean(worst <= 1e-3) >= 0.95
+
+
+def test_phenomhm_mixed(gpu_lib):
+    """IMRPhenomHM mixed form: sigma within 1e-3 of the FP64 kernel on every event with cond < 1e13."""
+    ev = hm_events(256, seed=1004)
+    net = synthetic.make_network(W.IMRPhenomHM(), dets=synthetic.NETWORK_ET_CE, earth=True)
+    F64 = np.moveaxis(net.FisherMatr(dict(ev), res=1000), -1, 0)
+    Fm = np.moveaxis(net.FisherMatr(dict(ev), res=1000, precision='mixed', refine_cond=1e11), -1, 0)
+    se, cond = sigma_err(Fm, F64)
+    worst = se.max(axis=1)
+    ok = cond < 1e13
+    print('PhenomHM mixed: sigma err median %.2e max (cond<1e13, %d events) %.2e'
+          % (np.median(worst), ok.sum(), worst[ok].max()))
+    assert worst[ok].max() <= 1e-3
+
+
+def test_fp32_snr_rejected_for_hm(gpu_lib):
     from gwfast_gb300 import _lib
     ev = synthetic.bbh_events(2, seed=1)
     net = synthetic.make_network(W.IMRPhenomHM(), dets=(('L1', 10.),), earth=False)
     with pytest.raises(_lib.GWFError):
-        net.FisherMatr(dict(ev), res=100, precision='fp32')
+        net.SNR(dict(ev), res=100, precision='fp32')
 
 
 def test_phenomd_network_mixed(gpu_lib):
