@@ -300,6 +300,98 @@ def run_screen(args):
     print(json.dumps(line))
 
 
+def run_hm(args):
+    """Higher-mode workload: IMRPhenomHM (modes 21, 22, 32, 33, 43, 44) aligned-spin BBH, m1 power law
+    on [5, 150] Msun, q ~ U[0.1, 1], chi ~ U[-0.9, 0.9], dL ~ U[0.5, 20] Gpc; ET triangle + CE1Id +
+    CE2NM (5 Hz walls), Earth rotation, R = 4000. Device-resident events; the FP32 split-precision
+    form (FP64 mode phases) and the mixed form over all events, the FP64 kernel over the first
+    10^4 (i.i.d. events, so the per-event rate carries over); sigma errors of both forms against the
+    FP64 kernel on the first 4096 events."""
+    import torch
+    from gwfast_gb300 import _build, _lib, fisherTools, synthetic
+    from gwfast_gb300 import waveforms as W
+    from gwfast_gb300.signal import event_array
+    _build.build()
+    dev = torch.device('cuda', 0)
+    N = args.events if args.events != N_EVENTS else 100000
+    R = 4000
+    ev = synthetic.bbh_events(N, seed=1003, mmax=150., qmin=0.1, chimax=0.9, dl=(0.5, 20.))
+    wf = W.IMRPhenomHM()
+    net = synthetic.make_network(wf, dets=synthetic.NETWORK_ET_CE, earth=True)
+    ids = [s.det_id for s in net.signals.values()]
+    ctx = _lib.context(0)
+    ctx.set_refine_cond(args.refine_cond)
+    p_dev = torch.from_numpy(event_array(ev)).to(dev)
+    out = torch.empty((N, 11, 11), dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    desc = wf.gpu_desc()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+
+    def step(precision, n, o=out):
+        ctx.fisher(ids, desc, p_dev, R, per_arm=False, mem=_lib.MEM_DEVICE, out_net=o, stream=stream.cuda_stream,
+                   ld=N, n=n, precision=precision)
+
+    def timed(fn, k, warm):
+        for _ in range(warm):
+            fn()
+        tot = 0.0
+        for _ in range(k):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot / k
+
+    n64 = min(N, 10000)
+    clk = ClockSampler(0)
+    ms32 = timed(lambda: step('fp32', N), args.steps, args.warmup)
+    msmix = timed(lambda: step('mixed', N), args.steps, args.warmup)
+    ms64 = timed(lambda: step('fp64', n64), max(1, args.steps // 2), 1)
+    clocks = clk.stop()
+    ns = min(N, 4096)
+    F = {}
+    for prec in ('fp64', 'fp32', 'mixed'):
+        o = torch.empty((ns, 11, 11), dtype=torch.float64, device=dev)
+        step(prec, ns, o)
+        torch.cuda.synchronize()
+        F[prec] = o.cpu().numpy()
+
+    def sigmas(Fx):
+        c, _, cond = fisherTools.CovMatr(np.moveaxis(Fx, 0, -1), return_cond=True)
+        return np.sqrt(np.abs(np.einsum('iin->ni', c))), cond
+
+    s64, cond = sigmas(F['fp64'])
+    stable = cond < 1e13
+    errs = {}
+    for prec in ('fp32', 'mixed'):
+        sx, _ = sigmas(F[prec])
+        w = (np.abs(sx - s64) / s64).max(axis=1)
+        errs[prec] = {'median': float(np.median(w)), 'p99': float(np.percentile(w, 99)),
+                      'max_cond_lt_1e13': float(w[stable].max()), 'events_cond_lt_1e13': int(stable.sum()),
+                      'events': int(ns), 'frac_le_1e-3': float(np.mean(w <= 1e-3))}
+    rate64 = n64 / (ms64 / 1e3)
+    line = {
+        'metric': 'network Fisher matrices/s, IMRPhenomHM on ET + 2 CE (mixed form vs plain FP64 kernel)',
+        'value': N / (msmix / 1e3), 'unit': 'Fisher/s', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': msmix, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f64 mode phases, f32 amplitudes/tangents/mode sums, f64 for events with cond > %.0e'
+                 % args.refine_cond,
+        'data': 'synthetic (seeded BBH catalogue)',
+        'config': {'workload': 'IMRPhenomHM, %d BBH, ETS + CE1Id + CE2NM (5 Hz), Earth rotation, R=%d' % (N, R),
+                   'l2': 'flushed (256 MB write) before every step'},
+        'fisher_per_s': {'mixed': N / (msmix / 1e3), 'fp32': N / (ms32 / 1e3), 'fp64': rate64},
+        'fp64_timed_on_events': n64,
+        'speedup_mixed_vs_fp64': (N / (msmix / 1e3)) / rate64,
+        'sigma_err_vs_fp64': errs,
+        'clocks': clocks,
+    }
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -313,9 +405,9 @@ def main():
     ap.add_argument('--precision', default='fp32', choices=('fp32', 'fp64', 'mixed'), help='form used with --only-device')
     ap.add_argument('--refine-cond', type=float, default=1e12, help='condition-number threshold of the mixed form')
     ap.add_argument('--no-autotune', action='store_true', help='per-event launches, no segment autotuning')
-    ap.add_argument('--workload', default='lhet', choices=('lhet', 'mixed-catalogue', 'screen'),
+    ap.add_argument('--workload', default='lhet', choices=('lhet', 'mixed-catalogue', 'screen', 'hm'),
                     help='lhet: the headline workload; mixed-catalogue: the batching workload; screen: the learned '
-                         'SNR screen on a 10^6-event population (separate lines)')
+                         'SNR screen on a 10^6-event population; hm: IMRPhenomHM on ET + CE (separate lines)')
     ap.add_argument('--train-events', type=int, default=200000)
     ap.add_argument('--train-epochs', type=int, default=40)
     args = ap.parse_args()
@@ -325,6 +417,8 @@ def main():
         return run_mixed_catalogue(args)
     if args.workload == 'screen':
         return run_screen(args)
+    if args.workload == 'hm':
+        return run_hm(args)
     rank, world, local = dist_info()
     import torch
     if world > 1:
