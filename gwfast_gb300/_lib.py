@@ -57,6 +57,7 @@ SIGNATURES = {
     'gwf_cov': ([_vp, _vp, _i64, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     'gwf_set_refine_cond': ([_vp, _d], ctypes.c_int),
     'gwf_set_segments': ([_vp, ctypes.c_int], ctypes.c_int),
+    'gwf_set_detector_groups': ([_vp, ctypes.c_int], ctypes.c_int),
     'gwf_set_graphs': ([_vp, ctypes.c_int], ctypes.c_int),
     'gwf_autotune_segments': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32, _vp, ctypes.c_int,
                                ctypes.c_int, ctypes.c_int, _P(ctypes.c_int)], ctypes.c_int),
@@ -188,6 +189,10 @@ class Context:
     def set_graphs(self, on):
         """Capture repeated device-resident Fisher calls in CUDA graphs and replay them."""
         check(load().gwf_set_graphs(self.h, int(bool(on))))
+
+    def set_detector_groups(self, on):
+        """FP32 network totals: evaluate detectors that share the grid in one launch (default on)."""
+        check(load().gwf_set_detector_groups(self.h, int(bool(on))))
 
     def set_segments(self, points):
         """0: one CTA per event; > 0: persistent launches over frequency segments of this many points."""

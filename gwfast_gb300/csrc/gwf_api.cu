@@ -111,6 +111,8 @@ struct gwf_ctx {
   cudaEvent_t scratch_free = nullptr;  // recorded after the last launch that used the set-up scratch
   HostBuf hpar, hout;
   DevBuf wbuf, par2, fcutb, ovb;   // strain-tangent and overlap outputs
+  DevBuf core;                     // source-dependent model records, shared by the detectors of a call
+  int groups = 1;                  // FP32 network totals: detectors sharing the grid in one launch
 };
 
 namespace {
@@ -239,7 +241,7 @@ int seg_setup(gwf_ctx* ctx, gwf::LaunchArgs& a, int seg, int64_t chunk, int64_t 
 // Fisher of the events above the threshold, computed as a compact batch and scattered back
 int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const double* dp, int64_t dld,
            const int* dres, int64_t N, int slots, double* darm, double* dnet, double* dsda, double* dsdn,
-           cudaStream_t st) {
+           bool core_filled, cudaStream_t st) {
   const size_t per = (size_t)gwf::NP * gwf::NP;
   if (ctx->fcond.ensure((size_t)N * sizeof(double)) || ctx->mix_idx.ensure((size_t)N * sizeof(long long)) ||
       ctx->mix_cnt.ensure(sizeof(unsigned long long)))
@@ -272,6 +274,10 @@ int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const
   a.ev.N = (long long)M;
   a.ev.res_ev = cres;
   a.precision = GWF_PREC_FP64;
+  // the source records of these events are in the cache when the first pass filled it
+  a.core = core_filled ? (unsigned char*)ctx->core.p : nullptr;
+  a.core_mode = core_filled ? 2 : 0;
+  a.core_idx = core_filled ? idx : nullptr;
   // few events: split each into frequency segments so that they fill the GPU
   int64_t rmax = a.ev.res;
   if (dres) {
@@ -331,7 +337,7 @@ std::string graph_key(int n_det, const int* det_ids, const gwf_wf_desc* wf, cons
 
 // the context buffers a captured graph refers to
 std::string buffer_sig(const gwf_ctx* ctx) {
-  const void* p[] = {ctx->setup.p, ctx->seg_off.p, ctx->seg_ctr.p, ctx->seg_part.p, ctx->seg_ovf.p};
+  const void* p[] = {ctx->setup.p, ctx->seg_off.p, ctx->seg_ctr.p, ctx->seg_part.p, ctx->seg_ovf.p, ctx->core.p};
   std::string k(reinterpret_cast<const char*>(p), sizeof p);
   k.append(reinterpret_cast<const char*>(&ctx->seg_points), sizeof ctx->seg_points);
   return k;
@@ -456,7 +462,31 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   }
   const size_t stride = wf->model == 0 ? gwf::setup_stride_m0() : (wf->model == 1 ? gwf::setup_stride_m1() : gwf::setup_stride_m2());
   const size_t chunk = (size_t)(N < gwf::kChunk ? N : gwf::kChunk);
-  if (ctx->setup.ensure(chunk * stride)) return fail(GWF_ERR_OOM, "device allocation failed (set-up scratch)");
+  // FP32 network totals: detectors with the same grid (fmin, fmax, Earth rotation) form groups
+  // that one launch evaluates together (the waveform once per point for the whole group)
+  std::vector<std::vector<int>> groups;
+  const bool grouping = fisher && ctx->groups && precision != GWF_PREC_FP64 && !darm && !dsda && !dsdn &&
+                        ctx->seg_points == 0;
+  for (int i = 0; i < n_det; ++i) {
+    const gwf_det_desc& di = ctx->dets[det_ids[i]].desc;
+    bool placed = false;
+    for (auto& g : groups) {
+      const gwf_det_desc& d0 = ctx->dets[det_ids[g[0]]].desc;
+      if (grouping && (int)g.size() < gwf::kMaxGroup && d0.fmin == di.fmin && d0.fmax == di.fmax &&
+          d0.earth_rotation == di.earth_rotation) {
+        g.push_back(i);
+        placed = true;
+        break;
+      }
+    }
+    if (!placed) groups.push_back({i});
+  }
+  size_t gmax = 1;
+  for (auto& g : groups) gmax = g.size() > gmax ? g.size() : gmax;
+  if (ctx->setup.ensure(gmax * chunk * stride)) return fail(GWF_ERR_OOM, "device allocation failed (set-up scratch)");
+  // a network shares the source-dependent part of the per-event set-up between its detectors
+  const size_t core_b = wf->model == 0 ? gwf::core_bytes_m0() : (wf->model == 1 ? gwf::core_bytes_m1() : gwf::core_bytes_m2());
+  const bool share = n_det > 1 && ctx->core.ensure((size_t)N * core_b) == 0;
   // the scratch is shared by every call on this context: order this call after the previous one
   if (!capturing) GWF_CK(cudaStreamWaitEvent(st, ctx->scratch_free, 0));
   gwf::LaunchArgs a;
@@ -486,22 +516,42 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   a.precision = precision == GWF_PREC_FP64 ? GWF_PREC_FP64 : GWF_PREC_FP32;
   a.stream = st;
   int slot = 0;
-  for (int i = 0; i < n_det; ++i) {
-    const DetRec& r = ctx->dets[det_ids[i]];
+  bool first = true;
+  for (auto& grp : groups) {
+    a.core = share ? (unsigned char*)ctx->core.p : nullptr;
+    a.core_mode = share ? (first ? 1 : 2) : 0;
+    a.accum = !first;
+    a.out_det = dnet;
+    first = false;
+    cudaError_t err;
+    if (grp.size() > 1) {   // (grouping implies: FP32 Fisher, network total only)
+      gwf::GroupDev g;
+      g.nd = (int)grp.size();
+      for (int d = 0; d < g.nd; ++d) {
+        g.det[d] = dev_of(ctx->dets[det_ids[grp[d]]]);
+        g.wr[d] = (float)std::sqrt(g.det[0].psd_scale / g.det[d].psd_scale);
+      }
+      g.slice = 0;
+      a.det = g.det[0];
+      a.out_arm = nullptr;
+      a.out_sd_arm = nullptr;
+      a.out_sd_det = nullptr;
+      err = wf->model == 0 ? gwf::launch_group_m0(a, g) : (wf->model == 1 ? gwf::launch_group_m1(a, g) : gwf::launch_group_m2(a, g));
+      if (err != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(err));
+      continue;
+    }
+    const DetRec& r = ctx->dets[det_ids[grp[0]]];
     a.det = dev_of(r);
     a.out_arm = darm ? darm + (size_t)slot * N * per : nullptr;
-    a.out_det = dnet;
     a.out_sd_arm = dsda ? dsda + (size_t)slot * N * gwf::NP : nullptr;
     a.out_sd_det = dsdn;
-    a.accum = i > 0;
-    cudaError_t err;
     if (fisher) err = wf->model == 0 ? gwf::launch_fisher_m0(a) : (wf->model == 1 ? gwf::launch_fisher_m1(a) : gwf::launch_fisher_m2(a));
     else err = wf->model == 0 ? gwf::launch_snr_m0(a) : (wf->model == 1 ? gwf::launch_snr_m1(a) : gwf::launch_snr_m2(a));
     if (err != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(err));
     slot += r.desc.shape == GWF_SHAPE_T ? 3 : 1;
   }
   if (precision == GWF_PREC_MIXED) {
-    rc = refine(ctx, n_det, det_ids, a, dp, dld, dres, N, slots, darm, dnet, dsda, dsdn, st);
+    rc = refine(ctx, n_det, det_ids, a, dp, dld, dres, N, slots, darm, dnet, dsda, dsdn, share, st);
     if (rc) return rc;
   }
   if (!capturing) GWF_CK(cudaEventRecord(ctx->scratch_free, st));
@@ -603,6 +653,7 @@ int gwf_ctx_destroy(gwf_ctx* ctx) {
   ctx->tune_out.release();
   ctx->osda.release(); ctx->osdn.release(); ctx->mix_sda.release(); ctx->mix_sdn.release();
   ctx->wbuf.release(); ctx->par2.release(); ctx->fcutb.release(); ctx->ovb.release();
+  ctx->core.release();
   for (auto& g : ctx->graph_cache) cudaGraphExecDestroy(g.second.exec);
   ctx->graph_cache.clear();
   ctx->hpar.release(); ctx->hout.release();
@@ -711,6 +762,12 @@ int gwf_set_graphs(gwf_ctx* ctx, int on) {
     ctx->graph_cache.clear();
     ctx->graph_pending.clear();
   }
+  return GWF_OK;
+}
+
+int gwf_set_detector_groups(gwf_ctx* ctx, int on) {
+  if (!ctx) return fail(GWF_ERR_INVALID_ARG, "null context");
+  ctx->groups = on ? 1 : 0;
   return GWF_OK;
 }
 

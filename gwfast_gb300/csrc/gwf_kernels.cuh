@@ -405,9 +405,14 @@ __device__ __forceinline__ const PhaseBasis* rec_basis(const unsigned char* scra
   return reinterpret_cast<const PhaseBasis*>(scratch + i * rec_stride<MODEL>() + sizeof(SetupHdr) + wave_bytes<MODEL>());
 }
 
+// core: optional per-call cache of the source-dependent model record, indexed by event (or by
+// core_idx[event] for a gathered batch); core_mode 1 computes the record and stores it there, 2 loads
+// it and recomputes only the detector-dependent part (the per-event set-up is FP64-bound, and a
+// network evaluates it once per detector)
 template <int MODEL>
 __global__ void __launch_bounds__(64) setup_kernel(EvBatch ev, DetDev det, WfDesc wf, const double* qnm, int nq,
-                                                    unsigned char* scratch, long long count) {
+                                                    unsigned char* scratch, long long count, unsigned char* core,
+                                                    int core_mode, const long long* core_idx) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long n = ev.n0 + i;
   if (i >= count || n >= ev.N) return;
@@ -420,10 +425,22 @@ __global__ void __launch_bounds__(64) setup_kernel(EvBatch ev, DetDev det, WfDes
   const double th = p[3 * ld + n], ph = p[4 * ld + n], io = p[5 * ld + n], ps = p[6 * ld + n];
   const double tc = p[7 * ld + n], c1 = p[9 * ld + n], c2 = p[10 * ld + n];
   if (grid_setup(h.g, det, ev, wf, n, Mc, eta)) {
-    event_setup<MODEL>(E, det, wf, qnm, nq, Mc, eta, c1, c2, dL);
-    if (MODEL == 2)
-      for (int mode = 0; mode < 6; ++mode)
-        hm_setup_mode(E.hm, mode, D4::seed(eta, P_ETA), D4::seed(c1, P_CHI1), D4::seed(c2, P_CHI2), io);
+    constexpr int nw = (int)(wave_bytes<MODEL>() / 8);
+    const long long crow = core_idx ? core_idx[n] : n;   // a gathered batch reads the rows of its events
+    unsigned long long* cw = core ? reinterpret_cast<unsigned long long*>(core + (size_t)crow * wave_bytes<MODEL>()) : nullptr;
+    unsigned long long* ew = reinterpret_cast<unsigned long long*>(&E);
+    if (core_mode == 2 && cw) {
+      for (int w = 0; w < nw; ++w) ew[w] = cw[w];
+      if (MODEL == 1) phd_ref(E.phd, det.fmin);
+      if (MODEL == 2) hm_ref(E.hm, det.fmin);
+    } else {
+      event_setup<MODEL>(E, det, wf, qnm, nq, Mc, eta, c1, c2, dL);
+      if (MODEL == 2)
+        for (int mode = 0; mode < 6; ++mode)
+          hm_setup_mode(E.hm, mode, D4::seed(eta, P_ETA), D4::seed(c1, P_CHI1), D4::seed(c2, P_CHI2), io);
+      if (core_mode == 1 && cw)
+        for (int w = 0; w < nw; ++w) cw[w] = ew[w];
+    }
     PhaseBasis* pb = reinterpret_cast<PhaseBasis*>(rec + sizeof(SetupHdr) + wave_bytes<MODEL>());
     if (MODEL == 0) tf2_phase_basis(E.tf2, *pb);
     if (MODEL == 1) phd_phase_basis(E.phd.k, *pb);

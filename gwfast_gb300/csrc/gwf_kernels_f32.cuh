@@ -260,59 +260,86 @@ __device__ inline void round_struct(const SRC& s, DST& d, const D4* amp_member, 
   }
 }
 
-// derivative vectors d h / d theta (11 parameters, every arm) at one frequency point, FP32 form;
-// the amplitude prefactor is divided out (restored with the Gram scale).
-// The psi slot holds Delta = dh/dpsi - 2 s dh/dPhicoal (s = sign cos i) instead of dh/dpsi: with
-// hp = cp A, hx = i ci A, dh/dpsi = 2A (cp Fx - i ci F+) and dh/dPhicoal = A (ci Fx - i cp F+), so
-// Delta = 2 A (cp - s ci)(Fx + i s F+), where cp - s ci = (1 - |cos i|)^2 / 2. Near face-on and
-// face-off dh/dpsi is almost exactly 2 s dh/dPhicoal; forming the small difference directly keeps
-// its FP32 relative accuracy (the Gram of the original columns is restored in FP64 at the end).
-template <int MODEL, bool EARTH, int NARM>
-__device__ __forceinline__ void point_f32(const EvUnionF& EF, const PBF& pbf, const ProjF& pf, const ArmF* apc,
-                                          const TimeF& tsc, float f, float lnf, cf (&D)[NARM][NP], cf (&H)[NARM]) {
+// The detector-independent part of one frequency point: hp = P, hc = i C without the common phase,
+// their tangents in (Mc, eta, chi1z, chi2z), the iota derivatives, Q = P - s C (s = sign cos iota, see
+// project_f32) and, with Earth rotation, tau_star and its tangent. The amplitude prefactor is
+// divided out (restored with the Gram scale).
+struct WaveF {
+  cf P, C, dP[4], dC[4], dPi, dCi, Q;
+  float tau;      // tau_star (s)
+  float dtn[4];   // d t_noloc / d theta_k (days)
+};
+
+template <int MODEL, bool EARTH>
+__device__ __forceinline__ void wave_f32(const EvUnionF& EF, const PBF& pbf, const ProjF& pf, float f, float lnf,
+                                         WaveF& w) {
   DF4 A;
   float dphi[4];
-  float dtn[4] = {0.f, 0.f, 0.f, 0.f};
-  TimeF ts;
   phase_tangent_f(pbf, f, lnf, dphi);
+  w.tau = 0.0f;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) w.dtn[q] = 0.0f;
   if (MODEL == 0) {
     const float f13 = cbrtf(f);
     A = EF.tf2.ampK * (1.0f / (f * sqrtf(f13)));
     if (EARTH) {
       const DF4 tau = tau_star_point<DF4>(EF.tf2.Ms, EF.tf2.vM, EF.tf2.eta, f13);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) dtn[q] = -tau.d[q] * (1.0f / 86400.0f);
-      time_f(pf, -tau.v * (1.0f / 86400.0f), ts);
+      for (int q = 0; q < 4; ++q) w.dtn[q] = -tau.d[q] * (1.0f / 86400.0f);
+      w.tau = tau.v;
     }
   } else {
     A = phd_amp_point<DF4>(EF.phd, f);
     if (EARTH) {
       const DF4 tau = tau_star_point<DF4>(EF.phd.Ms, EF.phd.vM, EF.phd.eta, cbrtf(f));
 #pragma unroll
-      for (int q = 0; q < 4; ++q) dtn[q] = -tau.d[q] * (1.0f / 86400.0f);
-      time_f(pf, -tau.v * (1.0f / 86400.0f), ts);
+      for (int q = 0; q < 4; ++q) w.dtn[q] = -tau.d[q] * (1.0f / 86400.0f);
+      w.tau = tau.v;
     }
   }
-  if (!EARTH) ts = tsc;
-  const cf P = {pf.cp * A.v, 0.0f}, C = {pf.ci * A.v, 0.0f};
-  cf dP[4], dC[4];
+  w.P = {pf.cp * A.v, 0.0f};
+  w.C = {pf.ci * A.v, 0.0f};
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const cf dW = {A.d[q], -A.v * dphi[q]};
-    dP[q] = fscale(dW, pf.cp);
-    dC[q] = fscale(dW, pf.ci);
+    w.dP[q] = fscale(dW, pf.cp);
+    w.dC[q] = fscale(dW, pf.ci);
   }
-  const cf dPi = {pf.dcp * A.v, 0.0f}, dCi = {pf.dci * A.v, 0.0f};
+  w.dPi = {pf.dcp * A.v, 0.0f};
+  w.dCi = {pf.dci * A.v, 0.0f};
+  w.Q = {A.v * pf.dcs, 0.0f};   // P - s C = A (cp - s ci) = A (1 - |cos i|)^2 / 2
+}
+
+// The detector part: derivative vectors d h / d theta of every arm (11 parameters) and the strain.
+// The psi slot holds Delta = dh/dpsi - 2 s dh/dPhicoal instead of dh/dpsi: with dh/dpsi =
+// 2 (Fx P - i F+ C) and dh/dPhicoal = -i (F+ P + i Fx C), Delta = 2 (P - s C)(Fx + i s F+). Near
+// face-on and face-off dh/dpsi is almost exactly 2 s dh/dPhicoal; forming the small difference
+// directly keeps its FP32 relative accuracy (the Gram of the original columns is restored in FP64
+// at the end).
+template <bool EARTH, int NARM>
+__device__ __forceinline__ void project_f32(const WaveF& w, const ProjF& pf, const ArmF* apc, const TimeF& tsc, float f,
+                                            cf (&D)[NARM][NP], cf (&H)[NARM]) {
+  TimeF ts;
+  if (EARTH) time_f(pf, -w.tau * (1.0f / 86400.0f), ts);
+  else ts = tsc;
 #pragma unroll
   for (int a = 0; a < NARM; ++a) {
     ArmF ap;
     if (EARTH) arm_f(pf, ts, a, ap);
     else ap = apc[a];
-    arm_derivs_f(pf, ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D[a]);
-    const float k = 2.0f * A.v * pf.dcs;
-    D[a][I_PS] = {k * ap.Fc, k * pf.sgn * ap.Fp};
-    H[a] = fadd(fscale(P, ap.Fp), fscale(fmuli(C), ap.Fc));   // the strain (common phase dropped)
+    arm_derivs_f(pf, ap, ts, f, w.P, w.C, w.dP, w.dC, w.dPi, w.dCi, w.dtn, D[a]);
+    const float wr = ap.Fc, wi = pf.sgn * ap.Fp;
+    D[a][I_PS] = {2.0f * (w.Q.re * wr - w.Q.im * wi), 2.0f * (w.Q.re * wi + w.Q.im * wr)};
+    H[a] = fadd(fscale(w.P, ap.Fp), fscale(fmuli(w.C), ap.Fc));   // the strain (common phase dropped)
   }
+}
+
+template <int MODEL, bool EARTH, int NARM>
+__device__ __forceinline__ void point_f32(const EvUnionF& EF, const PBF& pbf, const ProjF& pf, const ArmF* apc,
+                                          const TimeF& tsc, float f, float lnf, cf (&D)[NARM][NP], cf (&H)[NARM]) {
+  WaveF w;
+  wave_f32<MODEL, EARTH>(EF, pbf, pf, f, lnf, w);
+  project_f32<EARTH, NARM>(w, pf, apc, tsc, f, D, H);
 }
 
 // ------------------------------------------------------------------ IMRPhenomHM, split precision
@@ -378,13 +405,11 @@ __device__ inline void hm_round(const HMEv& s, HMF32& d, double amp, double alph
   }
 }
 
-// derivative vectors of IMRPhenomHM at one point, FP32 form (as point_f32; the psi slot holds
-// Delta = dh/dpsi - 2 s dh/dPhicoal = 2 (P - s C)(Fx + i s F+), with P - s C summed over the modes
-// from the harmonic differences yp - s yc formed in FP64, so it keeps FP32 relative accuracy near
-// face-on and face-off)
-template <bool EARTH, int NARM>
-__device__ __forceinline__ void point_f32_hm(const HMF32& H, const ProjF& pf, const ArmF* apc, const TimeF& tsc,
-                                             float f, cf (&D)[NARM][NP], cf (&Hs)[NARM]) {
+// IMRPhenomHM at one point, FP32 form: the detector-independent part (as wave_f32). Q = P - s C is
+// summed over the modes from the harmonic differences yp - s yc formed in FP64, so it keeps FP32
+// relative accuracy near face-on and face-off.
+template <bool EARTH>
+__device__ __forceinline__ void wave_f32_hm(const HMF32& H, const ProjF& pf, float f, WaveF& w) {
   const HMEvT<DF4>& e = H.e32;
   const HMEvT<double>& v = H.e64;
   const double x64 = v.k.MG * (double)f;
@@ -393,7 +418,8 @@ __device__ __forceinline__ void point_f32_hm(const HMF32& H, const ProjF& pf, co
   const DF4 lin = e.k.t0 * (x - e.k.fRef);
   const bool spos = pf.sgn > 0.0f;
   cf P = {0.0f, 0.0f}, C = {0.0f, 0.0f}, dPi = {0.0f, 0.0f}, dCi = {0.0f, 0.0f}, Q = {0.0f, 0.0f};
-  cf dP[4], dC[4];
+  cf (&dP)[4] = w.dP;
+  cf (&dC)[4] = w.dC;
 #pragma unroll
   for (int q = 0; q < 4; ++q) { dP[q] = {0.0f, 0.0f}; dC[q] = {0.0f, 0.0f}; }
 #pragma unroll 1
@@ -447,26 +473,24 @@ __device__ __forceinline__ void point_f32_hm(const HMF32& H, const ProjF& pf, co
     dCi = fadd(dCi, fscale(M, (float)m.dyc));
     Q = fadd(Q, fscale(M, (float)(spos ? m.ysp : m.ysm)));
   }
-  float dtn[4] = {0.f, 0.f, 0.f, 0.f};
-  TimeF ts;
+  w.P = P; w.C = C; w.dPi = dPi; w.dCi = dCi; w.Q = Q;
+  w.tau = 0.0f;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) w.dtn[q] = 0.0f;
   if (EARTH) {
     const DF4 tau = tau_star_point<DF4>(e.k.Ms, e.k.vM, e.k.eta, cbrtf(f));
 #pragma unroll
-    for (int q = 0; q < 4; ++q) dtn[q] = -tau.d[q] * (1.0f / 86400.0f);
-    time_f(pf, -tau.v * (1.0f / 86400.0f), ts);
-  } else {
-    ts = tsc;
+    for (int q = 0; q < 4; ++q) w.dtn[q] = -tau.d[q] * (1.0f / 86400.0f);
+    w.tau = tau.v;
   }
-#pragma unroll
-  for (int a = 0; a < NARM; ++a) {
-    ArmF ap;
-    if (EARTH) arm_f(pf, ts, a, ap);
-    else ap = apc[a];
-    arm_derivs_f(pf, ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D[a]);
-    const float wr = ap.Fc, wi = pf.sgn * ap.Fp;
-    D[a][I_PS] = {2.0f * (Q.re * wr - Q.im * wi), 2.0f * (Q.re * wi + Q.im * wr)};
-    Hs[a] = fadd(fscale(P, ap.Fp), fscale(fmuli(C), ap.Fc));
-  }
+}
+
+template <bool EARTH, int NARM>
+__device__ __forceinline__ void point_f32_hm(const HMF32& H, const ProjF& pf, const ArmF* apc, const TimeF& tsc,
+                                             float f, cf (&D)[NARM][NP], cf (&Hs)[NARM]) {
+  WaveF w;
+  wave_f32_hm<EARTH>(H, pf, f, w);
+  project_f32<EARTH, NARM>(w, pf, apc, tsc, f, D, Hs);
 }
 
 // 2x3 register blocks covering the upper triangle of the padded 12x12 Gram matrix
@@ -805,6 +829,179 @@ __global__ void __launch_bounds__(kThreads, 5) fisher_seg_kernel_f32(EvBatch ev,
     double* o = si.partial + item * (NG * NEX);
     for (int e = threadIdx.x; e < NG * NEX; e += blockDim.x) o[e] = S.gsum[e];
   }
+}
+
+// ------------------------------------------------------------------ detector groups
+// Detectors that share the frequency grid (same fmin, fmax, Earth-rotation flag) share the
+// waveform at every point: hp, hc and their tangents do not depend on the detector. For the network
+// total, one block per event evaluates the waveform once per point and projects it onto every
+// detector of the group; all their derivative vectors are accumulated into one exact Gram (the
+// network Gram is the Gram of all detectors' vectors together), so the waveform cost is paid once
+// per group instead of once per detector.
+constexpr int kMaxGroup = 4;
+
+struct GroupDev {
+  DetDev det[kMaxGroup];
+  float wr[kMaxGroup];   // sqrt(psd_scale of detector 0 / psd_scale of detector d): common Gram scale
+  int nd;
+  long long slice;       // bytes between the FP32 record areas of consecutive detectors
+};
+
+struct GroupProj {
+  ProjF pf[kMaxGroup];
+  ArmF apc[kMaxGroup][2];
+  TimeF tsc[kMaxGroup];
+};
+
+template <int MODEL, bool EARTH>
+__device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32State<MODEL, 1>& S, const GroupProj& gp,
+                                      int2* stage, int k1) {
+  constexpr int NQ = 12;
+  const F32Rec<MODEL>& r = S.r;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  long long acc[1][6];
+#pragma unroll
+  for (int e = 0; e < 6; ++e) acc[0][e] = 0ll;
+  int2* my = stage + (size_t)warp * NQ * 32;
+  auto& colM = S.colM;
+  auto& fl = S.fl;
+  my[11 * 32 + lane] = make_int2(0, 0);   // padding row (no strain column here)
+  for (int i = lane; i < 2 * NQ; i += 32) colM[i / NQ][warp][i % NQ] = kQMinExp;
+  for (int i = lane; i < gram_slots<1>() * NQ * NQ; i += 32) (&fl[warp][0][0][0])[i] = 0.0;
+  if (lane == 0) S.badw[warp] = 0;
+  int par = 0, tiles = 0;
+  bool moved = false, bad = false;
+  const int bi = lane & 15;
+  const int r0 = 2 * kBlkR[bi], c0 = 3 * kBlkC[bi];
+  const int j0 = 16 * (lane >> 4);
+  __syncwarp();
+  // one vector per lane (the lane's point) into the Gram: quantise, stage, accumulate (as f32_item,
+  // one Gram set, the two half-warps taking 16 points each)
+  auto add = [&](const cf (&u)[NP]) {
+    const int* Mo = &colM[par][warp][0];
+    int* Mn = &colM[par ^ 1][warp][0];
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      const int mold = Mo[q];
+      const unsigned bits = max(__float_as_uint(fabsf(u[q].re)), __float_as_uint(fabsf(u[q].im)));
+      const int e = (int)(__reduce_max_sync(0xffffffffu, bits) >> 23) - 127;
+      bad |= e > 127;
+      const int mnew = min(max(mold, e), 127);
+      moved |= mnew != mold;
+      if (lane == 0) Mn[q] = mnew;
+      const float sc = __int_as_float((127 + kQBits - 1 - mnew) << 23);
+      my[q * 32 + lane] = make_int2(__float2int_rn(u[q].re * sc), __float2int_rn(u[q].im * sc));
+    }
+    __syncwarp();
+    if (moved) {
+#pragma unroll
+      for (int e = 0; e < 6; ++e) {
+        const int rr = r0 + e / 3, cc = c0 + e % 3;
+        const int sh = (Mn[rr] - Mo[rr]) + (Mn[cc] - Mo[cc]);
+        acc[0][e] = sh >= 63 ? 0ll : (acc[0][e] >> sh);
+      }
+    }
+#pragma unroll 4
+    for (int jj = 0; jj < 16; ++jj) {
+      const int j = j0 + jj;
+      const int2 a0 = my[(r0 + 0) * 32 + j], a1 = my[(r0 + 1) * 32 + j];
+      const int2 b0 = my[(c0 + 0) * 32 + j], b1 = my[(c0 + 1) * 32 + j], b2 = my[(c0 + 2) * 32 + j];
+      acc[0][0] += (long long)a0.x * b0.x + (long long)a0.y * b0.y;
+      acc[0][1] += (long long)a0.x * b1.x + (long long)a0.y * b1.y;
+      acc[0][2] += (long long)a0.x * b2.x + (long long)a0.y * b2.y;
+      acc[0][3] += (long long)a1.x * b0.x + (long long)a1.y * b0.y;
+      acc[0][4] += (long long)a1.x * b1.x + (long long)a1.y * b1.y;
+      acc[0][5] += (long long)a1.x * b2.x + (long long)a1.y * b2.y;
+    }
+    par ^= 1;
+    moved = false;
+    if (++tiles == kFlushTiles) {
+      flush_fixed<1, NQ, 1, 16>(acc, &colM[par][warp][0], &fl[warp][0][0][0], lane);
+      tiles = 0;
+    }
+    __syncwarp();
+  };
+  GridIterF grid;
+  const int nd = g.nd;
+  for (int base = 0; base < k1; base += kThreads) {
+    const int k = base + tid;
+    grid.step(r, ev.spacing, base, lane, warp);
+    const bool valid = k < k1;
+    float f = 0.0f, lnf = 0.0f, w = 0.0f;
+    WaveF wv;
+    if (valid) {
+      grid.point(r, ev.spacing, k, lane, f, lnf, w);
+      if constexpr (MODEL == 2) wave_f32_hm<EARTH>(r.ef, r.pf, f, wv);
+      else wave_f32<MODEL, EARTH>(r.ef, r.pbf, r.pf, f, lnf, wv);
+    }
+    for (int d = 0; d < nd; ++d) {
+      const DetDev& det = g.det[d];
+      float sw = 0.0f;
+      if (valid) sw = sqrtf(4.0f * w / psd_at_f(det, f, lnf, (float)det.acc_l0, (float)det.acc_idl)) * g.wr[d];
+      cf u[NP];
+      if (det.shape == 0) {
+        cf D[1][NP], Hs[1];
+        if (valid) project_f32<EARTH, 1>(wv, gp.pf[d], gp.apc[d], gp.tsc[d], f, D, Hs);
+#pragma unroll
+        for (int q = 0; q < NP; ++q) u[q] = valid ? fscale(D[0][q], sw) : cf{0.0f, 0.0f};
+        add(u);
+      } else {
+        // triangle total: G(U) + G(V) + G(U+V) = G(sqrt(3/2)(U+V)) + G(sqrt(1/2)(U-V))
+        cf D[2][NP], Hs[2];
+        if (valid) project_f32<EARTH, 2>(wv, gp.pf[d], gp.apc[d], gp.tsc[d], f, D, Hs);
+#pragma unroll
+        for (int q = 0; q < NP; ++q) u[q] = valid ? fscale(fadd(D[0][q], D[1][q]), sw * 1.2247448713915890f) : cf{0.0f, 0.0f};
+        add(u);
+#pragma unroll
+        for (int q = 0; q < NP; ++q)
+          u[q] = valid ? fscale(fadd(D[0][q], fscale(D[1][q], -1.0f)), sw * 0.70710678118654752f) : cf{0.0f, 0.0f};
+        add(u);
+      }
+    }
+  }
+  flush_fixed<1, NQ, 1, 16>(acc, &colM[par][warp][0], &fl[warp][0][0][0], lane);
+  if (lane == 0 && bad) S.badw[warp] = 1;
+  __syncthreads();
+  int anybad = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; ++w) anybad |= S.badw[w];
+  const double* red = &fl[0][0][0][0];
+  constexpr int NS = gram_slots<1>();
+  for (int e = tid; e < NEX; e += kThreads) {
+    double v = 0.0;
+    if (e < NE) {
+      const int a = kPairA[e], b = kPairB[e];
+#pragma unroll
+      for (int w = 0; w < kWarps; ++w)
+        v += red[((size_t)(w * NS) * NQ + a) * NQ + b] + red[((size_t)(w * NS + 1) * NQ + a) * NQ + b];
+    }
+    S.gsum[e] = anybad ? __longlong_as_double(0x7ff8000000000000ll) : v;
+  }
+  __syncthreads();
+}
+
+template <int MODEL, bool EARTH>
+__global__ void __launch_bounds__(kThreads, 4) fisher_group_kernel_f32(EvBatch ev, GroupDev g,
+                                                                       const unsigned char* scratch32, double* out_det,
+                                                                       int accum) {
+  extern __shared__ __align__(16) unsigned char stage_raw[];
+  __shared__ F32State<MODEL, 1> S;
+  __shared__ GroupProj gp;
+  const long long n = ev.n0 + blockIdx.x;
+  if (n >= ev.N) return;
+  if ((int)threadIdx.x < g.nd) {   // the projection pieces of every detector of the group
+    const int d = threadIdx.x;
+    const F32Rec<MODEL>& rd =
+        *reinterpret_cast<const F32Rec<MODEL>*>(scratch32 + d * g.slice + (size_t)blockIdx.x * f32_stride<MODEL>());
+    gp.pf[d] = rd.pf;
+    gp.apc[d][0] = rd.apc[0];
+    gp.apc[d][1] = rd.apc[1];
+    gp.tsc[d] = rd.tsc;
+  }
+  f32_prepare<MODEL, 1>(scratch32, blockIdx.x, S);
+  f32_item_group<MODEL, EARTH>(ev, g, S, gp, reinterpret_cast<int2*>(stage_raw), S.r.gf.R);
+  write_gram<1>(S.gsum, S.r.scale, ColMix{2.0 * S.r.psi_sgn, S.r.chi_alpha}, n, ev.N, nullptr, out_det, nullptr, nullptr,
+                accum);
 }
 
 // ------------------------------------------------------------------ FP32 SNR

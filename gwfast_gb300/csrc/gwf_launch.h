@@ -32,6 +32,10 @@ struct LaunchArgs {
   double* seg_part = nullptr;              // seg_cap x 3 x 77 partial Grams
   long long seg_cap = 0;
   int* seg_ovf = nullptr;                  // set if the items exceed seg_cap
+  // cache of the source-dependent model records across the detectors of one call (see setup_kernel)
+  unsigned char* core = nullptr;           // N x core_bytes(model)
+  int core_mode = 0;                       // 0: none, 1: compute and store, 2: load
+  const long long* core_idx = nullptr;     // cache row of each event of a gathered batch
 };
 
 cudaError_t launch_fisher_m0(const LaunchArgs& a);
@@ -45,7 +49,15 @@ cudaError_t launch_snr_m2(const LaunchArgs& a);
 cudaError_t launch_wave_m0(const LaunchArgs& a, const WaveOut& o);
 cudaError_t launch_wave_m1(const LaunchArgs& a, const WaveOut& o);
 cudaError_t launch_wave_m2(const LaunchArgs& a, const WaveOut& o);
+// FP32 network total of a group of detectors sharing the grid (gwf_kernels_f32.cuh); a.det is the
+// group's first detector, a.scratch holds g.nd slices of a.cap_events set-up records
+cudaError_t launch_group_m0(const LaunchArgs& a, const GroupDev& g);
+cudaError_t launch_group_m1(const LaunchArgs& a, const GroupDev& g);
+cudaError_t launch_group_m2(const LaunchArgs& a, const GroupDev& g);
 size_t setup_stride_m0();
+size_t core_bytes_m0();
+size_t core_bytes_m1();
+size_t core_bytes_m2();
 size_t setup_stride_m1();
 size_t setup_stride_m2();
 cudaError_t launch_cov(const double* F, long long N, double* cov, double* eps, double* cond, cudaStream_t st);

@@ -387,6 +387,19 @@ __device__ inline void qnm_lookup(const double* qa, const double* qr, const doub
   fd = qd[lo] + (a - x0) * ((qd[lo + 1] - qd[lo]) / (x1 - x0));
 }
 
+// the detector-dependent part of the IMRPhenomD record: fRef = M G fmin and the phase there
+// (the rest of the record depends on the source alone)
+__device__ inline void phd_ref(PhdEv& e, double fmin_hz) {
+  PhdCore& k = e.k;
+  const D4& g2 = k.gam[1];
+  const D4& g3 = k.gam[2];
+  const D4& fr = k.fring;
+  const D4& fd = k.fdamp;
+  // phase peak frequency keeps the modulus in both branches (gwfast/waveforms.py:1134)
+  const D4 fpP = (g2.v >= 1.0) ? dabs(fr - fd * g3 / g2) : dabs(fr + fd * (dsqrt(1.0 - g2 * g2) - 1.0) * g3 / g2);
+  phenom_ref_setup(k, fpP, fmin_hz, k.C1MRD, k.C2MRD);
+}
+
 // IMRPhenomD per event (gwfast/waveforms.py:992-1254); fmin_hz sets fRef = min of the grid
 __device__ inline void phd_setup(PhdEv& e, const D4& Mc, const D4& eta, const D4& chi1, const D4& chi2, double dL,
                                  double fmin_hz, const double* qa, const double* qr, const double* qd, int nq) {
@@ -398,11 +411,7 @@ __device__ inline void phd_setup(PhdEv& e, const D4& Mc, const D4& eta, const D4
   fr = fr / (1.0 - er);
   fd = fd / (1.0 - er);
   phenom_core_setup(k, Mc, eta, chi1, chi2, fr, fd);
-  const D4& g2 = k.gam[1];
-  const D4& g3 = k.gam[2];
-  // phase peak frequency keeps the modulus in both branches (gwfast/waveforms.py:1134)
-  const D4 fpP = (g2.v >= 1.0) ? dabs(fr - fd * g3 / g2) : dabs(fr + fd * (dsqrt(1.0 - g2 * g2) - 1.0) * g3 / g2);
-  phenom_ref_setup(k, fpP, fmin_hz, k.C1MRD, k.C2MRD);
+  phd_ref(e, fmin_hz);
   // 2 sqrt(5/(64 pi)) M G/c^2[Gpc] M G/c^3 / dL * sqrt(2 eta/3) pi^(-1/6)  (gwfast/waveforms.py:1204, :1248)
   const D4 M = Mc / dpowc(eta, 0.6);
   k.ampPref = (2.0 * sqrt(5.0 / (64.0 * kPi)) * kG2Gpc * kG3 / dL * pow(kPi, -1.0 / 6.0)) * M * M * dsqrt(eta * (2.0 / 3.0));
@@ -582,6 +591,13 @@ __device__ inline void sw_harm(int mode, double iota, double& Y, double& Ym, dou
   Y = y.v; Ym = ym.v; dY = y.d[0]; dYm = ym.d[0];
 }
 
+// the detector-dependent part of the IMRPhenomHM record (the modes depend on the source alone);
+// hphc uses the amplitude peak (no modulus in the second branch) for t0 as well (gwfast/waveforms.py:2433, :2527)
+__device__ inline void hm_ref(HMEv& e, double fmin_hz) {
+  phenom_ref_setup(e.k, e.k.fpA, fmin_hz, e.k.C1MRD, e.k.C2MRD);
+  e.phi0 = 0.5 * e.k.phiRef;
+}
+
 __device__ inline void hm_setup_core(HMEv& e, const D4& Mc, const D4& eta, const D4& chi1, const D4& chi2, double dL,
                                      double fmin_hz) {
   PhdCore& k = e.k;
@@ -590,9 +606,7 @@ __device__ inline void hm_setup_core(HMEv& e, const D4& Mc, const D4& eta, const
   D4 fr, fd;
   rd_fit(1, finmass, af, fr, fd);
   phenom_core_setup(k, Mc, eta, chi1, chi2, fr, fd);
-  // hphc uses the amplitude peak (no modulus in the second branch) for t0 as well (gwfast/waveforms.py:2433, :2527)
-  phenom_ref_setup(k, k.fpA, fmin_hz, k.C1MRD, k.C2MRD);
-  e.phi0 = 0.5 * k.phiRef;
+  hm_ref(e, fmin_hz);
   const D4 M = Mc / dpowc(eta, 0.6);
   // M G/c^2[Gpc] M G/c^3 / dL * sqrt(2 eta/3) pi^(-1/6)   (gwfast/waveforms.py:2444, :2489)
   k.ampPref = (kG2Gpc * kG3 / dL * pow(kPi, -1.0 / 6.0)) * M * M * dsqrt(eta * (2.0 / 3.0));

@@ -30,7 +30,7 @@ cudaError_t chunked(const LaunchArgs& a, bool f32, MAIN main) {
     ev.n0 = n0;
     const long long cnt = (a.ev.N - n0) < kChunk ? (a.ev.N - n0) : kChunk;
     const unsigned nb = (unsigned)((cnt + 63) / 64);
-    setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, a.det, a.wf, a.qnm, a.nq, a.scratch, cnt);
+    setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, a.det, a.wf, a.qnm, a.nq, a.scratch, cnt, a.core, a.core_mode, a.core_idx);
     if (f32) setup_f32_kernel<M><<<nb, 64, 0, a.stream>>>(a.det, a.scratch, scratch32_of(a), cnt,
                                                           a.det.shape == 1 ? 2 : 1, a.det.earth);
     const cudaError_t e = main(ev, cnt);
@@ -176,12 +176,46 @@ cudaError_t snr_dispatch(const LaunchArgs& a) {
   return tri ? snr_one<false, 2>(a) : snr_one<false, 1>(a);
 }
 
+// a group of detectors sharing the grid (network total, FP32 form): per chunk, the set-up of each
+// detector into its own scratch slice, then one launch over all of them
+template <bool EARTH>
+cudaError_t group_one(const LaunchArgs& a, GroupDev g) {
+  const int smem = kWarps * 12 * 32 * (int)sizeof(int2);
+  auto k = fisher_group_kernel_f32<M, EARTH>;
+  cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (err != cudaSuccess) return err;
+  const long long chunk = a.cap_events;
+  const size_t stride = rec_stride<M>() + f32_stride<M>();
+  g.slice = (long long)(chunk * stride);
+  for (long long n0 = 0; n0 < a.ev.N; n0 += chunk) {
+    EvBatch ev = a.ev;
+    ev.n0 = n0;
+    const long long cnt = (a.ev.N - n0) < chunk ? (a.ev.N - n0) : chunk;
+    const unsigned nb = (unsigned)((cnt + 63) / 64);
+    for (int d = 0; d < g.nd; ++d) {
+      unsigned char* sc = a.scratch + (size_t)d * chunk * stride;
+      const int mode = d == 0 ? a.core_mode : (a.core ? 2 : 0);
+      setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, g.det[d], a.wf, a.qnm, a.nq, sc, cnt, a.core, mode, nullptr);
+      setup_f32_kernel<M><<<nb, 64, 0, a.stream>>>(g.det[d], sc, sc + (size_t)chunk * rec_stride<M>(), cnt,
+                                                   g.det[d].shape == 1 ? 2 : 1, g.det[d].earth);
+    }
+    k<<<(unsigned)cnt, kThreads, smem, a.stream>>>(ev, g, a.scratch + (size_t)chunk * rec_stride<M>(), a.out_det, a.accum);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t group_dispatch(const LaunchArgs& a, const GroupDev& g) {
+  return a.det.earth ? group_one<true>(a, g) : group_one<false>(a, g);
+}
+
 template <bool EARTH, int NARM>
 cudaError_t wave_one(const LaunchArgs& a, const WaveOut& o) {
   EvBatch ev = a.ev;
   ev.n0 = o.n0;
   const unsigned nb = (unsigned)((o.cnt + 63) / 64);
-  setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, a.det, a.wf, a.qnm, a.nq, a.scratch, o.cnt);
+  setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, a.det, a.wf, a.qnm, a.nq, a.scratch, o.cnt, nullptr, 0, nullptr);
   wave_out_kernel<M, EARTH, NARM><<<(unsigned)o.cnt, kThreads, 0, a.stream>>>(ev, a.det, a.scratch, o);
   return cudaGetLastError();
 }

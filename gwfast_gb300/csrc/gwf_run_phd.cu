@@ -5,8 +5,10 @@
 namespace gwf {
 
 size_t setup_stride_m1() { return rec_stride<1>() + f32_stride<1>(); }
+size_t core_bytes_m1() { return wave_bytes<1>(); }
 cudaError_t launch_fisher_m1(const LaunchArgs& a) { return fisher_dispatch(a); }
 cudaError_t launch_snr_m1(const LaunchArgs& a) { return snr_dispatch(a); }
 cudaError_t launch_wave_m1(const LaunchArgs& a, const WaveOut& o) { return wave_dispatch(a, o); }
+cudaError_t launch_group_m1(const LaunchArgs& a, const GroupDev& g) { return group_dispatch(a, g); }
 
 }  // namespace gwf

@@ -5,8 +5,10 @@
 namespace gwf {
 
 size_t setup_stride_m2() { return rec_stride<2>() + f32_stride<2>(); }
+size_t core_bytes_m2() { return wave_bytes<2>(); }
 cudaError_t launch_fisher_m2(const LaunchArgs& a) { return fisher_dispatch(a); }
 cudaError_t launch_snr_m2(const LaunchArgs& a) { return snr_dispatch(a); }
 cudaError_t launch_wave_m2(const LaunchArgs& a, const WaveOut& o) { return wave_dispatch(a, o); }
+cudaError_t launch_group_m2(const LaunchArgs& a, const GroupDev& g) { return group_dispatch(a, g); }
 
 }  // namespace gwf

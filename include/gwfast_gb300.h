@@ -103,7 +103,7 @@ int gwf_snr(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, 
  * per_arm != 0: out_arm receives [slots][N][11][11] per arm (return_all=True);
  * out_net (may be NULL): [N][11][11] network total.
  * precision: GWF_PREC_FP64 (the drop-in) or GWF_PREC_FP32 (split precision: per-event set-up in
- * FP64, per-point arithmetic in FP32, outputs in FP64; TaylorF2 and IMRPhenomD only), or
+ * FP64, per-point arithmetic in FP32, outputs in FP64; IMRPhenomHM with its mode phases in FP64), or
  * GWF_PREC_MIXED: GWF_PREC_FP32 for all events, then the events whose network Fisher has an
  * equilibrated condition number above the context's threshold (gwf_set_refine_cond, default
  * 1e12) or a non-finite one are recomputed in FP64 (all outputs). With mem = GWF_MEM_DEVICE,
@@ -143,6 +143,13 @@ int gwf_strain_derivs(gwf_ctx* ctx, int det_id, const gwf_wf_desc* wf, const dou
 int gwf_overlap(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf1, const double* params1,
                 int64_t ld1, const gwf_wf_desc* wf2, const double* params2, int64_t ld2, int64_t n_events, int32_t res,
                 int mem, double* out_ov, double* out_n1, double* out_n2, void* stream);
+
+/* Detector groups for FP32 network totals (no counterpart in gwfast: a launch-shape choice). on != 0
+ * (the default): in gwf_fisher with precision GWF_PREC_FP32 or GWF_PREC_MIXED, per_arm = 0, no
+ * SNR derivatives and no segments, detectors with the same fmin, fmax and Earth-rotation flag (up to
+ * four) are evaluated by one launch that computes the waveform and its tangent once per frequency
+ * point and accumulates all their derivative vectors into one Gram. on = 0: one launch per detector. */
+int gwf_set_detector_groups(gwf_ctx* ctx, int on);
 
 /* Condition-number threshold of GWF_PREC_MIXED (no counterpart in gwfast: a property of the
  * reduced-precision form). kappa > 0; events with equilibrated condition number above it get FP64. */
