@@ -591,7 +591,10 @@ def main():
         'sigma_err_fp32_only': serr_fp32,
         'snr_per_s': world * N / (ms_snr / 1e3),
         'snr_per_s_fp32': world * N / (ms_snr32 / 1e3),
-        'gpu_launches': 6 + 2 + (8 if refined > 0 else 0),
+        # first pass: 3 set-up + 3 FP32-record launches, the L1+H1 group kernel and the ET kernel; the
+        # condition estimate and selection; with refined events: gather, 3 x (set-up, segment scan,
+        # segmented FP64 kernel, reduction) and scatter
+        'gpu_launches': 8 + 2 + (14 if refined > 0 else 0),
         'e2e': {'value': world * N / e2e_s, 'unit': 'Fisher/s', 'h2d_bytes_per_step': int(p_host.nbytes),
                 'd2h_bytes_per_step': int(F_host.nbytes),
                 'what': 'DetNet.FisherMatr(precision=mixed) on a host events dict, host (11, 11, N) out, wall clock'},
