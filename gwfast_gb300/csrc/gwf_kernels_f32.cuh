@@ -405,6 +405,31 @@ __device__ inline void hm_round(const HMEv& s, HMF32& d, double amp, double alph
   }
 }
 
+// FP64 inspiral phase of the IMRPhenomD core at x' = x * ai (as ins_phase in gwf_model.cuh), from the
+// per-point values cbrt(pi x), 1 / cbrt(pi x), log(pi x) and 1 / (pi x) shared by all modes: the mode
+// phases of the inspiral region differ only by the scale ai = 2 / m of their argument, so
+// cbrt(pi x ai) = cbrt(pi x) cbrt(ai) and log(pi x ai) = log(pi x) + log(ai), and each mode costs a
+// short polynomial instead of its own cube root and logarithm.
+struct InsShared { double x13, ix13, lx, ixp; };
+
+__device__ __forceinline__ double ins_phase_scaled(const PhdCoreT<double>& k, const InsShared& b, double x, int m) {
+  // cbrt(ai), 1 / cbrt(ai), log(ai) for ai = 2 / m, m = 1..4
+  constexpr double kCb[5] = {0.0, 1.2599210498948731648, 1.0, 0.87358046473629886905, 0.79370052598409973738};
+  constexpr double kICb[5] = {0.0, 0.79370052598409973738, 1.0, 1.1447142425533318678, 1.2599210498948731648};
+  constexpr double kLg[5] = {0.0, 0.69314718055994530942, 0.0, -0.40546510810816438198, -0.69314718055994530942};
+  const double ai = 2.0 / m;
+  const double x13 = b.x13 * kCb[m];
+  const double ix13 = b.ix13 * kICb[m];
+  const double ix23 = ix13 * ix13;
+  const double ixp = b.ixp / ai;
+  const double lx = (b.lx + kLg[m]) * (1.0 / 3.0);
+  const double tf2 = ix23 * ixp + k.pn.c2 * ixp + k.pn.c3 * ix23 + k.pn.c4 * ix13 + k.pn.c5 + k.pn.c5l * lx
+                     + (k.pn.c6 + k.pn.c6l * lx) * x13 + k.pn.c7 * x13 * x13;
+  const double m13 = x13 * 0.68278406325529573;
+  return k.pn.A * tf2 + (k.sig[0] * x + 0.75 * k.sig[1] * x * m13 + 0.6 * k.sig[2] * x * m13 * m13
+                         + 0.5 * k.sig[3] * x * x) / k.eta;
+}
+
 // IMRPhenomHM at one point, FP32 form: the detector-independent part (as wave_f32). Q = P - s C is
 // summed over the modes from the harmonic differences yp - s yc formed in FP64, so it keeps FP32
 // relative accuracy near face-on and face-off.
@@ -417,6 +442,14 @@ __device__ __forceinline__ void wave_f32_hm(const HMF32& H, const ProjF& pf, flo
   const double lin64 = v.k.t0 * (x64 - v.k.fRef);
   const DF4 lin = e.k.t0 * (x - e.k.fRef);
   const bool spos = pf.sgn > 0.0f;
+  InsShared ins;
+  if (x64 < 2.0 * kPhiFJoin) {   // some mode argument x * 2 / m lies in the inspiral region
+    const double xp = kPi * x64;
+    ins.x13 = cbrt(xp);
+    ins.ix13 = 1.0 / ins.x13;
+    ins.lx = log(xp);
+    ins.ixp = 1.0 / xp;
+  }
   cf P = {0.0f, 0.0f}, C = {0.0f, 0.0f}, dPi = {0.0f, 0.0f}, dCi = {0.0f, 0.0f}, Q = {0.0f, 0.0f};
   cf (&dP)[4] = w.dP;
   cf (&dC)[4] = w.dC;
@@ -442,7 +475,9 @@ __device__ __forceinline__ void wave_f32_hm(const HMF32& H, const ProjF& pf, flo
     double ph64;
     DF4 ph;
     if (x64 < mv.fip) {
-      ph64 = complete_phase<double>(v.k, x64 * ai64, mv.C1, mv.C2, mv.rho, mv.tau) / ai64;
+      const double xa = x64 * ai64;
+      ph64 = (xa < kPhiFJoin ? ins_phase_scaled(v.k, ins, xa, mv.m)
+                             : complete_phase<double>(v.k, xa, mv.C1, mv.C2, mv.rho, mv.tau)) / ai64;
       ph = complete_phase<DF4>(e.k, x * ai, m.C1, m.C2, m.rho, m.tau) / ai;
     } else if (x64 < mv.frlm) {
       ph64 = mv.PhDBA - mv.PhDB + complete_phase<double>(v.k, x64 * mv.amp_ + mv.bmp, mv.C1, mv.C2, mv.rho, mv.tau) / mv.amp_;
