@@ -1016,7 +1016,7 @@ __device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32S
 }
 
 template <int MODEL, bool EARTH>
-__global__ void __launch_bounds__(kThreads, 4) fisher_group_kernel_f32(EvBatch ev, GroupDev g,
+__global__ void __launch_bounds__(kThreads, 5) fisher_group_kernel_f32(EvBatch ev, GroupDev g,
                                                                        const unsigned char* scratch32, double* out_det,
                                                                        int accum) {
   extern __shared__ __align__(16) unsigned char stage_raw[];
