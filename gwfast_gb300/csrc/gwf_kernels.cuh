@@ -573,7 +573,11 @@ __device__ inline void f64_prepare(const DetDev& det, const unsigned char* scrat
   __syncthreads();
 }
 
-// Gram of points [k0, k1) into S.gsum (summed over warps); stage: [warp][NG][NP + 1][32] complex,
+// staging row stride (complex values): lanes of a quarter-warp read different rows at the same
+// point; with an odd stride those rows fall in different banks (32 gives 8-way conflicts)
+constexpr int kSR64 = 33;
+
+// Gram of points [k0, k1) into S.gsum (summed over warps); stage: [warp][NG][NP + 1][kSR64] complex,
 // column NP holding the strain itself when sd (SNR derivatives) is set
 template <int MODEL, bool EARTH, int NARM, int NG>
 __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<NARM, NG>& S, cd* stage, int k0, int k1,
@@ -585,7 +589,7 @@ __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<N
   double acc[EPT];
 #pragma unroll
   for (int i = 0; i < EPT; ++i) acc[i] = 0.0;
-  cd* my = stage + (size_t)warp * NG * NPS * 32;
+  cd* my = stage + (size_t)warp * NG * NPS * kSR64;
   for (int base = k0; base < k1; base += kThreads) {
     const int k = base + tid;
     cd D[NARM][NPS];
@@ -627,16 +631,16 @@ __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<N
 #pragma unroll
     for (int q = 0; q < NPS; ++q) {
       if (NG == 1) {
-        my[(0 * NPS + q) * 32 + lane] = cscale(D[0][q], sw);
+        my[(0 * NPS + q) * kSR64 + lane] = cscale(D[0][q], sw);
       } else if (NG == 2) {
         const cd u = D[0][q], v = D[1][q];
-        my[(0 * NPS + q) * 32 + lane] = cscale(cadd(u, v), sw * 1.2247448713915890);   // sqrt(3/2)
-        my[(1 * NPS + q) * 32 + lane] = cscale(cadd(u, cscale(v, -1.0)), sw * 0.70710678118654752);
+        my[(0 * NPS + q) * kSR64 + lane] = cscale(cadd(u, v), sw * 1.2247448713915890);   // sqrt(3/2)
+        my[(1 * NPS + q) * kSR64 + lane] = cscale(cadd(u, cscale(v, -1.0)), sw * 0.70710678118654752);
       } else {
         const cd u = D[0][q], v = D[1][q];
-        my[(0 * NPS + q) * 32 + lane] = cscale(u, sw);
-        my[(1 * NPS + q) * 32 + lane] = cscale(v, sw);
-        my[(2 * NPS + q) * 32 + lane] = cscale(cadd(u, v), -sw);
+        my[(0 * NPS + q) * kSR64 + lane] = cscale(u, sw);
+        my[(1 * NPS + q) * kSR64 + lane] = cscale(v, sw);
+        my[(2 * NPS + q) * kSR64 + lane] = cscale(cadd(u, v), -sw);
       }
     }
     __syncwarp();
@@ -647,8 +651,8 @@ __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<N
         const int gs = e / NEX, pe = e - gs * NEX;
         if (pe >= NE && !sd) continue;
         const int a = pe < NE ? kPairA[pe] : pe - NE, b = pe < NE ? kPairB[pe] : NP;
-        const cd* ra = my + (gs * NPS + a) * 32;
-        const cd* rb = my + (gs * NPS + b) * 32;
+        const cd* ra = my + (gs * NPS + a) * kSR64;
+        const cd* rb = my + (gs * NPS + b) * kSR64;
         double s = 0.0;
 #pragma unroll 8
         for (int j = 0; j < 32; ++j) s += ra[j].re * rb[j].re + ra[j].im * rb[j].im;

@@ -536,6 +536,10 @@ static __constant__ unsigned char kBlkC[16] = {0, 1, 2, 3, 0, 1, 2, 3, 1, 2, 3, 
 constexpr int kQBits = 25;        // quantised |value| <= 2^25: the largest values of a column keep all 24 FP32 bits
 constexpr int kQMinExp = -100;    // floor of the running column exponents
 constexpr int kFlushTiles = 64;   // per tile |sum| <= 32 x 2 x 2^50 = 2^56, so 64 tiles stay below 2^62
+// staging row stride in int2: a lane of the Gram loop reads row r0 (or c0) at column j while the
+// other lanes of its half-warp read other rows at the same column; with 33 (odd) those rows fall
+// in different banks (32 would put all of them in one bank: 6-way conflicts)
+constexpr int kSR = 33;
 
 // Gram slots per warp: one per Gram set, or, for a single set, one per half-warp (the two halves
 // of a warp split each tile's points between them)
@@ -707,11 +711,11 @@ __device__ inline void f32_item(const EvBatch& ev, const DetDev& det, F32State<M
   for (int i = 0; i < BPL; ++i)
 #pragma unroll
     for (int e = 0; e < 6; ++e) acc[i][e] = 0ll;
-  int2* my = stage + (size_t)warp * NG * NQ * 32;
+  int2* my = stage + (size_t)warp * NG * NQ * kSR;
   auto& colM = S.colM;
   auto& fl = S.fl;
   // zero padding row (parameter 11) once; running column exponents start below any value
-  for (int gs = 0; gs < NG; ++gs) my[(gs * NQ + 11) * 32 + lane] = make_int2(0, 0);
+  for (int gs = 0; gs < NG; ++gs) my[(gs * NQ + 11) * kSR + lane] = make_int2(0, 0);
   for (int i = lane; i < 2 * NG * NQ; i += 32) (&colM[i / (NG * NQ)][warp][0])[i % (NG * NQ)] = kQMinExp;
   for (int i = lane; i < gram_slots<NG>() * NQ * NQ; i += 32) (&fl[warp][0][0][0])[i] = 0.0;
   if (lane == 0) S.badw[warp] = 0;
@@ -766,7 +770,7 @@ __device__ inline void f32_item(const EvBatch& ev, const DetDev& det, F32State<M
         const float s = __int_as_float((127 + kQBits - 1 - mnew) << 23);   // 2^(kQBits-1-mnew), exact scaling
         const int qr = __float2int_rn(u.re * s);
         const int qi = __float2int_rn(u.im * s);
-        my[(gs * NQ + q) * 32 + lane] = make_int2(qr, qi);
+        my[(gs * NQ + q) * kSR + lane] = make_int2(qr, qi);
       }
     __syncwarp();
 #pragma unroll
@@ -775,7 +779,7 @@ __device__ inline void f32_item(const EvBatch& ev, const DetDev& det, F32State<M
       if (bl < NB) {
         const int gs = bl >> 4, bi = bl & 15;
         const int r0 = 2 * kBlkR[bi], c0 = 3 * kBlkC[bi];
-        const int2* base_g = my + gs * NQ * 32;
+        const int2* base_g = my + gs * NQ * kSR;
         if (moved) {   // rescale the running sums to the new column scales
           const int* mo = Mo + gs * NQ;
           const int* mn = Mn + gs * NQ;
@@ -791,8 +795,8 @@ __device__ inline void f32_item(const EvBatch& ev, const DetDev& det, F32State<M
 #pragma unroll 4
         for (int jj = 0; jj < NJ; ++jj) {
           const int j = j0 + jj;
-          const int2 a0 = base_g[(r0 + 0) * 32 + j], a1 = base_g[(r0 + 1) * 32 + j];
-          const int2 b0 = base_g[(c0 + 0) * 32 + j], b1 = base_g[(c0 + 1) * 32 + j], b2 = base_g[(c0 + 2) * 32 + j];
+          const int2 a0 = base_g[(r0 + 0) * kSR + j], a1 = base_g[(r0 + 1) * kSR + j];
+          const int2 b0 = base_g[(c0 + 0) * kSR + j], b1 = base_g[(c0 + 1) * kSR + j], b2 = base_g[(c0 + 2) * kSR + j];
           acc[i][0] += (long long)a0.x * b0.x + (long long)a0.y * b0.y;
           acc[i][1] += (long long)a0.x * b1.x + (long long)a0.y * b1.y;
           acc[i][2] += (long long)a0.x * b2.x + (long long)a0.y * b2.y;
@@ -897,10 +901,10 @@ __device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32S
   long long acc[1][6];
 #pragma unroll
   for (int e = 0; e < 6; ++e) acc[0][e] = 0ll;
-  int2* my = stage + (size_t)warp * NQ * 32;
+  int2* my = stage + (size_t)warp * NQ * kSR;
   auto& colM = S.colM;
   auto& fl = S.fl;
-  my[11 * 32 + lane] = make_int2(0, 0);   // padding row (no strain column here)
+  my[11 * kSR + lane] = make_int2(0, 0);   // padding row (no strain column here)
   for (int i = lane; i < 2 * NQ; i += 32) colM[i / NQ][warp][i % NQ] = kQMinExp;
   for (int i = lane; i < gram_slots<1>() * NQ * NQ; i += 32) (&fl[warp][0][0][0])[i] = 0.0;
   if (lane == 0) S.badw[warp] = 0;
@@ -925,7 +929,7 @@ __device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32S
       moved |= mnew != mold;
       if (lane == 0) Mn[q] = mnew;
       const float sc = __int_as_float((127 + kQBits - 1 - mnew) << 23);
-      my[q * 32 + lane] = make_int2(__float2int_rn(u[q].re * sc), __float2int_rn(u[q].im * sc));
+      my[q * kSR + lane] = make_int2(__float2int_rn(u[q].re * sc), __float2int_rn(u[q].im * sc));
     }
     __syncwarp();
     if (moved) {
@@ -939,8 +943,8 @@ __device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32S
 #pragma unroll 4
     for (int jj = 0; jj < 16; ++jj) {
       const int j = j0 + jj;
-      const int2 a0 = my[(r0 + 0) * 32 + j], a1 = my[(r0 + 1) * 32 + j];
-      const int2 b0 = my[(c0 + 0) * 32 + j], b1 = my[(c0 + 1) * 32 + j], b2 = my[(c0 + 2) * 32 + j];
+      const int2 a0 = my[(r0 + 0) * kSR + j], a1 = my[(r0 + 1) * kSR + j];
+      const int2 b0 = my[(c0 + 0) * kSR + j], b1 = my[(c0 + 1) * kSR + j], b2 = my[(c0 + 2) * kSR + j];
       acc[0][0] += (long long)a0.x * b0.x + (long long)a0.y * b0.y;
       acc[0][1] += (long long)a0.x * b1.x + (long long)a0.y * b1.y;
       acc[0][2] += (long long)a0.x * b2.x + (long long)a0.y * b2.y;

@@ -75,7 +75,7 @@ cudaError_t persist_grid(K k, int smem, int* grid) {
 
 template <bool EARTH, int NARM, int NG>
 cudaError_t fisher_one(const LaunchArgs& a) {
-  const int smem = kWarps * NG * (NP + 1) * 32 * (int)sizeof(cd);
+  const int smem = kWarps * NG * (NP + 1) * kSR64 * (int)sizeof(cd);
   if (a.seg <= 0) {
     auto k = fisher_kernel<M, EARTH, NARM, NG>;
     cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -98,7 +98,7 @@ cudaError_t fisher_one(const LaunchArgs& a) {
 
 template <bool EARTH, int NARM, int NG>
 cudaError_t fisher_one_f32(const LaunchArgs& a) {
-  const int smem = kWarps * NG * 12 * 32 * (int)sizeof(int2);
+  const int smem = kWarps * NG * 12 * kSR * (int)sizeof(int2);
   unsigned char* s32 = scratch32_of(a);
   if (a.seg <= 0) {
     auto k = fisher_kernel_f32<M, EARTH, NARM, NG>;
@@ -180,7 +180,7 @@ cudaError_t snr_dispatch(const LaunchArgs& a) {
 // detector into its own scratch slice, then one launch over all of them
 template <bool EARTH>
 cudaError_t group_one(const LaunchArgs& a, GroupDev g) {
-  const int smem = kWarps * 12 * 32 * (int)sizeof(int2);
+  const int smem = kWarps * 12 * kSR * (int)sizeof(int2);
   auto k = fisher_group_kernel_f32<M, EARTH>;
   cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (err != cudaSuccess) return err;
