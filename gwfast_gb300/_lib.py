@@ -14,6 +14,7 @@ from . import _build
 GWF_OK = 0
 ERRORS = {-1: 'invalid argument', -2: 'CUDA error', -3: 'out of memory', -4: 'timeout', -5: 'unsupported'}
 MODEL_IDS = {'TaylorF2_RestrictedPN': 0, 'IMRPhenomD': 1, 'IMRPhenomHM': 2}
+MODEL_TF2_TIDAL = 3
 MEM_HOST, MEM_DEVICE = 0, 1
 PRECISION = {'fp64': 0, 'fp32': 1, 'mixed': 2}
 
@@ -55,6 +56,7 @@ SIGNATURES = {
     'gwf_overlap': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32,
                      ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     'gwf_cov': ([_vp, _vp, _i64, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
+    'gwf_cov_n': ([_vp, _vp, _i64, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     'gwf_set_refine_cond': ([_vp, _d], ctypes.c_int),
     'gwf_set_segments': ([_vp, ctypes.c_int], ctypes.c_int),
     'gwf_set_detector_groups': ([_vp, ctypes.c_int], ctypes.c_int),
@@ -213,9 +215,9 @@ class Context:
         """Condition-number threshold above which the 'mixed' form recomputes an event in FP64."""
         check(load().gwf_set_refine_cond(self.h, float(kappa)))
 
-    def cov(self, F, mem=MEM_HOST, cov=None, eps=None, cond=None, n=None, stream=None):
+    def cov(self, F, mem=MEM_HOST, cov=None, eps=None, cond=None, n=None, stream=None, n_params=11):
         n = F.shape[0] if n is None else n
-        check(load().gwf_cov(self.h, ptr(F), n, mem, ptr(cov), ptr(eps), ptr(cond), stream))
+        check(load().gwf_cov_n(self.h, ptr(F), n, int(n_params), mem, ptr(cov), ptr(eps), ptr(cond), stream))
 
 
 def context(device=0):

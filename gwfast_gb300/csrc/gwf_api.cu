@@ -117,6 +117,9 @@ struct gwf_ctx {
 
 namespace {
 
+// Fisher parameters of a waveform model: 11, or 13 for the tidal TaylorF2 (LambdaTilde, deltaLambda)
+int npar_of(int model) { return model == GWF_WF_TAYLORF2_TIDAL ? 13 : 11; }
+
 int check_ctx(gwf_ctx* ctx) {
   if (!ctx) return fail(GWF_ERR_INVALID_ARG, "null context");
   GWF_CK(cudaSetDevice(ctx->device));
@@ -157,7 +160,7 @@ int validate_common(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_de
   if (!det_ids || n_det < 1) return fail(GWF_ERR_INVALID_ARG, "need at least one detector");
   for (int i = 0; i < n_det; ++i)
     if (det_ids[i] < 0 || det_ids[i] >= (int)ctx->dets.size()) return fail(GWF_ERR_INVALID_ARG, "unknown detector id");
-  if (!wf || wf->model < 0 || wf->model > 2) return fail(GWF_ERR_INVALID_ARG, "unknown waveform model");
+  if (!wf || wf->model < 0 || wf->model > 3) return fail(GWF_ERR_INVALID_ARG, "unknown waveform model");
   if (wf->model == GWF_WF_PHENOMD && ctx->nq < 2) return fail(GWF_ERR_INVALID_ARG, "IMRPhenomD needs the QNM table (gwf_set_qnm_table)");
   if (!(wf->fcut_par > 0.0)) return fail(GWF_ERR_INVALID_ARG, "fcut_par must be positive");
   if (N < 0 || (N > 0 && !params)) return fail(GWF_ERR_INVALID_ARG, "bad event array");
@@ -170,28 +173,28 @@ int validate_common(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_de
 }
 
 int stage_inputs_to(gwf_ctx* ctx, DevBuf& par, const double* params, int64_t ld, int64_t N, const int32_t* res_ev,
-                    int mem, cudaStream_t st, const double** dp, int64_t* dld, const int** dres);
+                    int mem, cudaStream_t st, const double** dp, int64_t* dld, const int** dres, int npar = gwf::NP);
 
 // stage host inputs into device buffers; returns device pointers
 int stage_inputs(gwf_ctx* ctx, const double* params, int64_t ld, int64_t N, const int32_t* res_ev, int mem,
-                 cudaStream_t st, const double** dp, int64_t* dld, const int** dres) {
-  return stage_inputs_to(ctx, ctx->par, params, ld, N, res_ev, mem, st, dp, dld, dres);
+                 cudaStream_t st, const double** dp, int64_t* dld, const int** dres, int npar = gwf::NP) {
+  return stage_inputs_to(ctx, ctx->par, params, ld, N, res_ev, mem, st, dp, dld, dres, npar);
 }
 
 int stage_inputs_to(gwf_ctx* ctx, DevBuf& par, const double* params, int64_t ld, int64_t N, const int32_t* res_ev,
-                    int mem, cudaStream_t st, const double** dp, int64_t* dld, const int** dres) {
+                    int mem, cudaStream_t st, const double** dp, int64_t* dld, const int** dres, int npar) {
   if (mem == GWF_MEM_DEVICE) {
     *dp = params;
     *dld = ld;
     *dres = res_ev;
     return GWF_OK;
   }
-  const size_t pb = (size_t)gwf::NP * (size_t)N * sizeof(double);
+  const size_t pb = (size_t)npar * (size_t)N * sizeof(double);
   if (par.ensure(pb ? pb : 8)) return fail(GWF_ERR_OOM, "device allocation failed (params)");
   if (N > 0) {
     if (ld == N) GWF_CK(cudaMemcpyAsync(par.p, params, pb, cudaMemcpyHostToDevice, st));
     else GWF_CK(cudaMemcpy2DAsync(par.p, N * sizeof(double), params, ld * sizeof(double), N * sizeof(double),
-                                  gwf::NP, cudaMemcpyHostToDevice, st));
+                                  npar, cudaMemcpyHostToDevice, st));
   }
   *dp = (const double*)par.p;
   *dld = N;
@@ -355,6 +358,8 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
     return fail(GWF_ERR_INVALID_ARG, "bad precision");
   if (precision != GWF_PREC_FP64 && wf->model == GWF_WF_PHENOMHM && !fisher)
     return fail(GWF_ERR_UNSUPPORTED, "the FP32 SNR is implemented for TaylorF2 and IMRPhenomD");
+  if (precision != GWF_PREC_FP64 && wf->model == GWF_WF_TAYLORF2_TIDAL)
+    return fail(GWF_ERR_UNSUPPORTED, "the tidal TaylorF2 is implemented in FP64");
   if (precision == GWF_PREC_MIXED && !fisher) return fail(GWF_ERR_INVALID_ARG, "the mixed form is a Fisher form");
   if (fisher && !per_arm) out_arm = nullptr;
   if (fisher && per_arm && !out_arm) return fail(GWF_ERR_INVALID_ARG, "per_arm needs out_arm");
@@ -418,10 +423,11 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   const double* dp;
   int64_t dld;
   const int* dres;
-  rc = stage_inputs(ctx, params, ld, N, res_ev, mem, st, &dp, &dld, &dres);
+  const int npar = npar_of(wf->model);
+  rc = stage_inputs(ctx, params, ld, N, res_ev, mem, st, &dp, &dld, &dres, npar);
   if (rc) return rc;
   const int slots = slots_of(ctx, n_det, det_ids);
-  const size_t per = fisher ? (size_t)gwf::NP * gwf::NP : 1;
+  const size_t per = fisher ? (size_t)npar * npar : 1;
   double* darm = nullptr;
   double* dnet = nullptr;
   if (mem == GWF_MEM_DEVICE) {
@@ -447,11 +453,11 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
     dsdn = sd_net;
   } else {
     if (sd_arm) {
-      if (ctx->osda.ensure((size_t)slots * N * gwf::NP * sizeof(double))) return fail(GWF_ERR_OOM, "device allocation failed (out)");
+      if (ctx->osda.ensure((size_t)slots * N * npar * sizeof(double))) return fail(GWF_ERR_OOM, "device allocation failed (out)");
       dsda = (double*)ctx->osda.p;
     }
     if (sd_net) {
-      if (ctx->osdn.ensure((size_t)N * gwf::NP * sizeof(double))) return fail(GWF_ERR_OOM, "device allocation failed (out)");
+      if (ctx->osdn.ensure((size_t)N * npar * sizeof(double))) return fail(GWF_ERR_OOM, "device allocation failed (out)");
       dsdn = (double*)ctx->osdn.p;
     }
   }
@@ -460,7 +466,9 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
     if (ctx->onet.ensure((size_t)N * per * sizeof(double))) return fail(GWF_ERR_OOM, "device allocation failed (out)");
     dnet = (double*)ctx->onet.p;
   }
-  const size_t stride = wf->model == 0 ? gwf::setup_stride_m0() : (wf->model == 1 ? gwf::setup_stride_m1() : gwf::setup_stride_m2());
+  const size_t stride = wf->model == 0 ? gwf::setup_stride_m0()
+                        : (wf->model == 1 ? gwf::setup_stride_m1()
+                                          : (wf->model == 2 ? gwf::setup_stride_m2() : gwf::setup_stride_m3()));
   const size_t chunk = (size_t)(N < gwf::kChunk ? N : gwf::kChunk);
   // FP32 network totals: detectors with the same grid (fmin, fmax, Earth rotation) form groups
   // that one launch evaluates together (the waveform once per point for the whole group)
@@ -485,14 +493,16 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   for (auto& g : groups) gmax = g.size() > gmax ? g.size() : gmax;
   if (ctx->setup.ensure(gmax * chunk * stride)) return fail(GWF_ERR_OOM, "device allocation failed (set-up scratch)");
   // a network shares the source-dependent part of the per-event set-up between its detectors
-  const size_t core_b = wf->model == 0 ? gwf::core_bytes_m0() : (wf->model == 1 ? gwf::core_bytes_m1() : gwf::core_bytes_m2());
+  const size_t core_b = wf->model == 0 ? gwf::core_bytes_m0()
+                        : (wf->model == 1 ? gwf::core_bytes_m1()
+                                          : (wf->model == 2 ? gwf::core_bytes_m2() : gwf::core_bytes_m3()));
   const bool share = n_det > 1 && ctx->core.ensure((size_t)N * core_b) == 0;
   // the scratch is shared by every call on this context: order this call after the previous one
   if (!capturing) GWF_CK(cudaStreamWaitEvent(st, ctx->scratch_free, 0));
   gwf::LaunchArgs a;
   a.scratch = (unsigned char*)ctx->setup.p;
   a.cap_events = (long long)chunk;
-  if (fisher && ctx->seg_points > 0) {
+  if (fisher && ctx->seg_points > 0 && wf->model != GWF_WF_TAYLORF2_TIDAL) {
     int64_t rmax = 0;
     if (capturing && res_ev) rmax = ctx->graph_rmax;   // from the uncaptured run of the same call
     else rc = max_res(res, res_ev, N, mem, &rmax);
@@ -543,10 +553,14 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
     const DetRec& r = ctx->dets[det_ids[grp[0]]];
     a.det = dev_of(r);
     a.out_arm = darm ? darm + (size_t)slot * N * per : nullptr;
-    a.out_sd_arm = dsda ? dsda + (size_t)slot * N * gwf::NP : nullptr;
+    a.out_sd_arm = dsda ? dsda + (size_t)slot * N * npar : nullptr;
     a.out_sd_det = dsdn;
-    if (fisher) err = wf->model == 0 ? gwf::launch_fisher_m0(a) : (wf->model == 1 ? gwf::launch_fisher_m1(a) : gwf::launch_fisher_m2(a));
-    else err = wf->model == 0 ? gwf::launch_snr_m0(a) : (wf->model == 1 ? gwf::launch_snr_m1(a) : gwf::launch_snr_m2(a));
+    if (fisher)
+      err = wf->model == 0 ? gwf::launch_fisher_m0(a)
+            : (wf->model == 1 ? gwf::launch_fisher_m1(a) : (wf->model == 2 ? gwf::launch_fisher_m2(a) : gwf::launch_fisher_m3(a)));
+    else
+      err = wf->model == 0 ? gwf::launch_snr_m0(a)
+            : (wf->model == 1 ? gwf::launch_snr_m1(a) : (wf->model == 2 ? gwf::launch_snr_m2(a) : gwf::launch_snr_m3(a)));
     if (err != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(err));
     slot += r.desc.shape == GWF_SHAPE_T ? 3 : 1;
   }
@@ -558,8 +572,8 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   if (mem == GWF_MEM_HOST) {
     if (out_arm) GWF_CK(cudaMemcpyAsync(out_arm, darm, (size_t)slots * N * per * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (out_net) GWF_CK(cudaMemcpyAsync(out_net, dnet, (size_t)N * per * sizeof(double), cudaMemcpyDeviceToHost, st));
-    if (sd_arm) GWF_CK(cudaMemcpyAsync(sd_arm, dsda, (size_t)slots * N * gwf::NP * sizeof(double), cudaMemcpyDeviceToHost, st));
-    if (sd_net) GWF_CK(cudaMemcpyAsync(sd_net, dsdn, (size_t)N * gwf::NP * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (sd_arm) GWF_CK(cudaMemcpyAsync(sd_arm, dsda, (size_t)slots * N * npar * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (sd_net) GWF_CK(cudaMemcpyAsync(sd_net, dsdn, (size_t)N * npar * sizeof(double), cudaMemcpyDeviceToHost, st));
     int ovf = 0;
     if (fisher && (a.seg > 0 || precision == GWF_PREC_MIXED) && ctx->seg_ovf.p)
       GWF_CK(cudaMemcpyAsync(&ovf, ctx->seg_ovf.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -790,20 +804,21 @@ int gwf_autotune_segments(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf
   const double* dp;
   int64_t dld;
   const int* dres;
-  rc = stage_inputs(ctx, params, ld, n_events, res_per_event, mem, st, &dp, &dld, &dres);
+  const int npar = npar_of(wf->model);
+  rc = stage_inputs(ctx, params, ld, n_events, res_per_event, mem, st, &dp, &dld, &dres, npar);
   if (rc) return rc;
   // keep staged inputs: later runs reuse ctx->par / ctx->res, so copy them aside
   DevBuf tp, tr;
   if (mem == GWF_MEM_HOST) {
-    if (tp.ensure((size_t)gwf::NP * n_events * sizeof(double)) || (dres && tr.ensure((size_t)n_events * sizeof(int))))
+    if (tp.ensure((size_t)npar * n_events * sizeof(double)) || (dres && tr.ensure((size_t)n_events * sizeof(int))))
       return fail(GWF_ERR_OOM, "device allocation failed (autotune)");
-    GWF_CK(cudaMemcpyAsync(tp.p, dp, (size_t)gwf::NP * n_events * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    GWF_CK(cudaMemcpyAsync(tp.p, dp, (size_t)npar * n_events * sizeof(double), cudaMemcpyDeviceToDevice, st));
     if (dres) GWF_CK(cudaMemcpyAsync(tr.p, dres, (size_t)n_events * sizeof(int), cudaMemcpyDeviceToDevice, st));
     dp = (const double*)tp.p;
     dres = dres ? (const int*)tr.p : nullptr;
     dld = n_events;
   }
-  if (ctx->tune_out.ensure((size_t)n_events * gwf::NP * gwf::NP * sizeof(double)))
+  if (ctx->tune_out.ensure((size_t)n_events * npar * npar * sizeof(double)))
     return fail(GWF_ERR_OOM, "device allocation failed (autotune)");
   const int cands[] = {0, 256, 512, 1024, 2048};
   const int saved = ctx->seg_points;
@@ -845,7 +860,8 @@ int gwf_fisher_ex(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc
   ctx->call_sd_arm = out_snr_der_arm;
   ctx->call_sd_net = out_snr_der_net;
   if (!out_arm && !out_net && (out_snr_der_arm || out_snr_der_net)) {   // derivatives only: a throw-away total
-    if (ctx->tune_out.ensure((size_t)(n_events > 0 ? n_events : 1) * gwf::NP * gwf::NP * sizeof(double))) {
+    const int npar = wf ? npar_of(wf->model) : gwf::NP;
+    if (ctx->tune_out.ensure((size_t)(n_events > 0 ? n_events : 1) * npar * npar * sizeof(double))) {
       ctx->call_sd_arm = ctx->call_sd_net = nullptr;
       return fail(GWF_ERR_OOM, "device allocation failed");
     }
@@ -854,7 +870,7 @@ int gwf_fisher_ex(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc
   double* host_tmp = nullptr;
   std::vector<double> htmp;
   if (tmp_net && mem == GWF_MEM_HOST) {
-    htmp.resize((size_t)(n_events > 0 ? n_events : 1) * gwf::NP * gwf::NP);
+    htmp.resize((size_t)(n_events > 0 ? n_events : 1) * (wf ? npar_of(wf->model) : gwf::NP) * (wf ? npar_of(wf->model) : gwf::NP));
     host_tmp = htmp.data();
   }
   const int rc = run(ctx, true, n_det, det_ids, wf, params, ld, n_events, res, res_per_event, spacing, per_arm,
@@ -871,6 +887,7 @@ int gwf_strain_derivs(gwf_ctx* ctx, int det_id, const gwf_wf_desc* wf, const dou
   rc = validate_common(ctx, 1, &det_id, wf, params, ld, n_events, res, nullptr, spacing, mem);
   if (rc) return rc;
   if (!out) return fail(GWF_ERR_INVALID_ARG, "no output requested");
+  if (wf->model == GWF_WF_TAYLORF2_TIDAL) return fail(GWF_ERR_UNSUPPORTED, "strain derivatives are implemented for the 11-parameter models");
   const int64_t N = n_events;
   if (N == 0) return GWF_OK;
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
@@ -944,6 +961,8 @@ int gwf_overlap(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* 
   if (!rc) rc = validate_common(ctx, n_det, det_ids, wf2, params2, ld2, n_events, res, nullptr, GWF_SPACING_GEOM, mem);
   if (rc) return rc;
   if (!out_ov || !out_n1 || !out_n2) return fail(GWF_ERR_INVALID_ARG, "overlap needs all three outputs");
+  if (wf1->model == GWF_WF_TAYLORF2_TIDAL || wf2->model == GWF_WF_TAYLORF2_TIDAL)
+    return fail(GWF_ERR_UNSUPPORTED, "the overlap is implemented for the 11-parameter models");
   const int64_t N = n_events;
   if (N == 0) return GWF_OK;
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
@@ -1023,16 +1042,18 @@ int gwf_overlap(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* 
   return GWF_OK;
 }
 
-int gwf_cov(gwf_ctx* ctx, const double* F, int64_t N, int mem, double* cov, double* eps, double* cond, void* stream) {
+int gwf_cov_n(gwf_ctx* ctx, const double* F, int64_t N, int n_params, int mem, double* cov, double* eps, double* cond,
+              void* stream) {
   int rc = check_ctx(ctx);
   if (rc) return rc;
+  if (n_params != 11 && n_params != 13) return fail(GWF_ERR_INVALID_ARG, "n_params must be 11 or 13");
   if (N < 0 || (N > 0 && (!F || !cov))) return fail(GWF_ERR_INVALID_ARG, "bad covariance arguments");
   if (mem != GWF_MEM_HOST && mem != GWF_MEM_DEVICE) return fail(GWF_ERR_INVALID_ARG, "bad memory mode");
   if (N == 0) return GWF_OK;
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
-  const size_t mb = (size_t)N * 121 * sizeof(double);
+  const size_t mb = (size_t)N * n_params * n_params * sizeof(double);
   if (mem == GWF_MEM_DEVICE) {
-    cudaError_t e = gwf::launch_cov(F, N, cov, eps, cond, st);
+    cudaError_t e = gwf::launch_cov(F, N, cov, eps, cond, st, n_params);
     if (e != cudaSuccess) return fail(GWF_ERR_CUDA, cudaGetErrorString(e));
     return GWF_OK;
   }
@@ -1041,13 +1062,17 @@ int gwf_cov(gwf_ctx* ctx, const double* F, int64_t N, int mem, double* cov, doub
     return fail(GWF_ERR_OOM, "device allocation failed (cov)");
   GWF_CK(cudaMemcpyAsync(ctx->fin.p, F, mb, cudaMemcpyHostToDevice, st));
   cudaError_t e = gwf::launch_cov((const double*)ctx->fin.p, N, (double*)ctx->fout.p, (double*)ctx->feps.p,
-                                  (double*)ctx->fcond.p, st);
+                                  (double*)ctx->fcond.p, st, n_params);
   if (e != cudaSuccess) return fail(GWF_ERR_CUDA, cudaGetErrorString(e));
   GWF_CK(cudaMemcpyAsync(cov, ctx->fout.p, mb, cudaMemcpyDeviceToHost, st));
   if (eps) GWF_CK(cudaMemcpyAsync(eps, ctx->feps.p, N * sizeof(double), cudaMemcpyDeviceToHost, st));
   if (cond) GWF_CK(cudaMemcpyAsync(cond, ctx->fcond.p, N * sizeof(double), cudaMemcpyDeviceToHost, st));
   GWF_CK(cudaStreamSynchronize(st));
   return GWF_OK;
+}
+
+int gwf_cov(gwf_ctx* ctx, const double* F, int64_t N, int mem, double* cov, double* eps, double* cond, void* stream) {
+  return gwf_cov_n(ctx, F, N, 11, mem, cov, eps, cond, stream);
 }
 
 }  // extern "C"

@@ -1,4 +1,5 @@
-// Batched FP64 covariance: equilibrated Cholesky inverse of 11x11 Fisher matrices.
+// Batched FP64 covariance: equilibrated Cholesky inverse of NC x NC Fisher matrices (NC = 11, or 13
+// for the tidal model).
 //
 // One thread per event.  Steps (gwfast/fisherTools.py:32-212, 'cho' path):
 //  w_i = 1/sqrt(F_ii);  F' = diag(w) F diag(w)
@@ -13,8 +14,7 @@
 
 namespace gwf {
 
-constexpr int NC = 11;
-
+template <int NC>
 __global__ void cov_kernel(const double* __restrict__ F, long long N, double* __restrict__ cov,
                            double* __restrict__ eps, double* __restrict__ cond) {
   const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -142,11 +142,13 @@ __global__ void cov_kernel(const double* __restrict__ F, long long N, double* __
   }
 }
 
-cudaError_t launch_cov(const double* F, long long N, double* cov, double* eps, double* cond, cudaStream_t st) {
+cudaError_t launch_cov(const double* F, long long N, double* cov, double* eps, double* cond, cudaStream_t st, int np) {
   if (N <= 0) return cudaSuccess;
   const int bs = 64;
   const long long nb = (N + bs - 1) / bs;
-  cov_kernel<<<(unsigned)nb, bs, 0, st>>>(F, N, cov, eps, cond);
+  if (np == 13) cov_kernel<13><<<(unsigned)nb, bs, 0, st>>>(F, N, cov, eps, cond);
+  else if (np == 11) cov_kernel<11><<<(unsigned)nb, bs, 0, st>>>(F, N, cov, eps, cond);
+  else return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 

@@ -18,7 +18,20 @@ constexpr int kWarps = kThreads / 32;
 constexpr int NP = 11;    // Fisher parameters
 constexpr int NE = 66;    // upper-triangle entries
 // Fisher order: Mc, eta, dL, theta, phi, iota, psi, tcoal, Phicoal, chi1z, chi2z
-enum { I_MC = 0, I_ETA, I_DL, I_TH, I_PH, I_IO, I_PS, I_TC, I_PC, I_C1, I_C2 };
+// (the tidal TaylorF2, model 3, appends LambdaTilde, deltaLambda)
+enum { I_MC = 0, I_ETA, I_DL, I_TH, I_PH, I_IO, I_PS, I_TC, I_PC, I_C1, I_C2, I_LT, I_DLT };
+
+// Fisher parameters of a model, upper-triangle entries, entries plus strain products, entry index
+template <int MODEL> __host__ __device__ constexpr int np_of() { return MODEL == 3 ? 13 : 11; }
+__host__ __device__ constexpr int ne_of(int npr) { return npr * (npr + 1) / 2; }
+__host__ __device__ constexpr int nex_of(int npr) { return ne_of(npr) + npr; }
+__host__ __device__ constexpr int pidx_n(int npr, int a, int b) { return a * npr - a * (a - 1) / 2 + (b - a); }
+// (a, b), a <= b, of upper-triangle entry e
+__host__ __device__ inline void pair_n(int npr, int e, int& a, int& b) {
+  a = 0;
+  while (e >= npr - a) { e -= npr - a; ++a; }
+  b = a + e;
+}
 
 struct DetDev {
   double lat, lon, xax;  // radians
@@ -227,11 +240,13 @@ union EvUnion {
   TF2Ev tf2;
   PhdEv phd;
   HMEv hm;
+  TF2TEv tf2t;
 };
 
 // upper grid frequency of the model (gwfast/waveforms.py:903-920, :1324-1333, :2737-2750)
 __host__ __device__ inline double model_fcut(const WfDesc& wf, double Mc, double eta) {
-  return (wf.model == 0) ? wf.fcut_par / (Mc / pow(eta, 0.6)) : wf.fcut_par / (Mc * kG3 / pow(eta, 0.6));
+  // TaylorF2 (models 0 and 3): fcut_par is fHigh in Hz Msun; the IMR models: a cut in M f
+  return (wf.model == 0 || wf.model == 3) ? wf.fcut_par / (Mc / pow(eta, 0.6)) : wf.fcut_par / (Mc * kG3 / pow(eta, 0.6));
 }
 
 __device__ inline bool grid_setup(GridEv& g, const DetDev& d, const EvBatch& ev, const WfDesc& wf, long long n,
@@ -275,9 +290,11 @@ __device__ __forceinline__ void grid_point(const GridEv& g, int spacing, int k, 
 
 template <int MODEL>
 __device__ inline void event_setup(EvUnion& E, const DetDev& d, const WfDesc& wf, const double* q, int nq,
-                                   double Mc, double eta, double chi1, double chi2, double dL) {
+                                   double Mc, double eta, double chi1, double chi2, double dL, double lam_t,
+                                   double del_lam) {
   const D4 mc = D4::seed(Mc, P_MC), et = D4::seed(eta, P_ETA), c1 = D4::seed(chi1, P_CHI1), c2 = D4::seed(chi2, P_CHI2);
-  if (MODEL == 0) tf2_setup(E.tf2, mc, et, c1, c2, dL, wf.spin_ho != 0);
+  if (MODEL == 3) tf2t_setup(E.tf2t, mc, et, c1, c2, dL, wf.spin_ho != 0, lam_t, del_lam);
+  else if (MODEL == 0) tf2_setup(E.tf2, mc, et, c1, c2, dL, wf.spin_ho != 0);
   else if (MODEL == 1) phd_setup(E.phd, mc, et, c1, c2, dL, d.fmin, q, q + nq, q + 2 * nq, nq);
   else hm_setup_core(E.hm, mc, et, c1, c2, dL, d.fmin);
 }
@@ -303,16 +320,18 @@ __device__ __forceinline__ void wave_point_dual(const EvUnion& E, const ProjEv& 
     if (EARTH) tau = tau_star_point<D4>(E.hm.k.Ms, E.hm.k.vM, E.hm.k.eta, exp(lnf / 3.0));
   } else {
     D4 A, Phi;
-    if (MODEL == 0) {
+    if (MODEL == 0 || MODEL == 3) {
+      const TF2Ev& t = MODEL == 3 ? E.tf2t.b : E.tf2;
       const double f13 = exp(lnf / 3.0);
-      tf2_point<D4>(E.tf2, f, f13, lnf, exp(lnf * (-7.0 / 6.0)), A, Phi);
-      if (EARTH) tau = tau_star_point<D4>(E.tf2.Ms, E.tf2.vM, E.tf2.eta, f13);
+      tf2_point<D4>(t, f, f13, lnf, exp(lnf * (-7.0 / 6.0)), A, Phi);
+      if (MODEL == 3) Phi = Phi + tf2_tidal_phase<D4>(E.tf2t, t.vM * f13);
+      if (EARTH) tau = tau_star_point<D4>(t.Ms, t.vM, t.eta, f13);
     } else {
       phd_point<D4>(E.phd.k, f, A, Phi);
       if (EARTH) tau = tau_star_point<D4>(E.phd.k.Ms, E.phd.k.vM, E.phd.k.eta, exp(lnf / 3.0));
     }
     // W = A e^{-i Phi} with the common phase dropped: value A, tangent dA - i A dPhi
-    phi0 = Phi.v + (MODEL == 0 ? kTF2PhaseConst : 0.0);
+    phi0 = Phi.v + ((MODEL == 0 || MODEL == 3) ? kTF2PhaseConst : 0.0);
     P = {pj.cp * A.v, 0.0};
     C = {pj.ci * A.v, 0.0};
 #pragma unroll
@@ -339,17 +358,19 @@ __device__ __forceinline__ void wave_point_full(const EvUnion& E, const ProjEv& 
     if (EARTH) tau = tau_star_point<double>(E.hm.k.Ms, E.hm.k.vM, E.hm.k.eta, exp(lnf / 3.0));
   } else {
     double A, Phi;
-    if (MODEL == 0) {
+    if (MODEL == 0 || MODEL == 3) {
+      const TF2Ev& t = MODEL == 3 ? E.tf2t.b : E.tf2;
       const double f13 = exp(lnf / 3.0);
-      tf2_point<double>(E.tf2, f, f13, lnf, exp(lnf * (-7.0 / 6.0)), A, Phi);
-      if (EARTH) tau = tau_star_point<double>(E.tf2.Ms, E.tf2.vM, E.tf2.eta, f13);
+      tf2_point<double>(t, f, f13, lnf, exp(lnf * (-7.0 / 6.0)), A, Phi);
+      if (MODEL == 3) Phi += tf2_tidal_phase<double>(E.tf2t, t.vM.v * f13);
+      if (EARTH) tau = tau_star_point<double>(t.Ms, t.vM, t.eta, f13);
     } else {
       phd_point<double>(E.phd.k, f, A, Phi);
       if (EARTH) tau = tau_star_point<double>(E.phd.k.Ms, E.phd.k.vM, E.phd.k.eta, exp(lnf / 3.0));
     }
     P = {pj.cp * A, 0.0};
     C = {pj.ci * A, 0.0};
-    phi0 = Phi + (MODEL == 0 ? kTF2PhaseConst : 0.0);
+    phi0 = Phi + ((MODEL == 0 || MODEL == 3) ? kTF2PhaseConst : 0.0);
   }
 }
 
@@ -365,10 +386,11 @@ __device__ __forceinline__ void wave_point_val(const EvUnion& E, const ProjEv& p
     if (EARTH) tau = tau_star_point<double>(E.hm.k.Ms, E.hm.k.vM, E.hm.k.eta, exp(lnf / 3.0));
   } else {
     double A, Phi;
-    if (MODEL == 0) {
+    if (MODEL == 0 || MODEL == 3) {
+      const TF2Ev& t = MODEL == 3 ? E.tf2t.b : E.tf2;
       const double f13 = exp(lnf / 3.0);
-      tf2_point<double>(E.tf2, f, f13, lnf, exp(lnf * (-7.0 / 6.0)), A, Phi);
-      if (EARTH) tau = tau_star_point<double>(E.tf2.Ms, E.tf2.vM, E.tf2.eta, f13);
+      tf2_point<double>(t, f, f13, lnf, exp(lnf * (-7.0 / 6.0)), A, Phi);
+      if (EARTH) tau = tau_star_point<double>(t.Ms, t.vM, t.eta, f13);
     } else {
       phd_point<double>(E.phd.k, f, A, Phi);
       if (EARTH) tau = tau_star_point<double>(E.phd.k.Ms, E.phd.k.vM, E.phd.k.eta, exp(lnf / 3.0));
@@ -389,7 +411,7 @@ struct SetupHdr {
 
 template <int MODEL>
 __host__ __device__ constexpr size_t wave_bytes() {
-  return MODEL == 0 ? sizeof(TF2Ev) : (MODEL == 1 ? sizeof(PhdEv) : sizeof(HMEv));
+  return MODEL == 0 ? sizeof(TF2Ev) : (MODEL == 1 ? sizeof(PhdEv) : (MODEL == 2 ? sizeof(HMEv) : sizeof(TF2TEv)));
 }
 // the 22-mode models also carry the phase-tangent basis used by the FP32 kernel
 template <int MODEL>
@@ -424,6 +446,7 @@ __global__ void __launch_bounds__(64) setup_kernel(EvBatch ev, DetDev det, WfDes
   const double Mc = p[0 * ld + n], eta = p[1 * ld + n], dL = p[2 * ld + n];
   const double th = p[3 * ld + n], ph = p[4 * ld + n], io = p[5 * ld + n], ps = p[6 * ld + n];
   const double tc = p[7 * ld + n], c1 = p[9 * ld + n], c2 = p[10 * ld + n];
+  const double lt = MODEL == 3 ? p[11 * ld + n] : 0.0, dlt = MODEL == 3 ? p[12 * ld + n] : 0.0;
   if (grid_setup(h.g, det, ev, wf, n, Mc, eta)) {
     constexpr int nw = (int)(wave_bytes<MODEL>() / 8);
     const long long crow = core_idx ? core_idx[n] : n;   // a gathered batch reads the rows of its events
@@ -434,7 +457,7 @@ __global__ void __launch_bounds__(64) setup_kernel(EvBatch ev, DetDev det, WfDes
       if (MODEL == 1) phd_ref(E.phd, det.fmin);
       if (MODEL == 2) hm_ref(E.hm, det.fmin);
     } else {
-      event_setup<MODEL>(E, det, wf, qnm, nq, Mc, eta, c1, c2, dL);
+      event_setup<MODEL>(E, det, wf, qnm, nq, Mc, eta, c1, c2, dL, lt, dlt);
       if (MODEL == 2)
         for (int mode = 0; mode < 6; ++mode)
           hm_setup_mode(E.hm, mode, D4::seed(eta, P_ETA), D4::seed(c1, P_CHI1), D4::seed(c2, P_CHI2), io);
@@ -495,19 +518,22 @@ struct ColMix {
   }
 };
 
-// write the event's matrices from gsum[NG][NE] (upper triangles): column changes undone, scaled
-template <int NG>
+// write the event's matrices from gsum[NG][nex_of(NPR)] (upper triangles, then the strain
+// products): column changes undone, scaled; outputs are NPR x NPR per event
+template <int NG, int NPR = NP>
 __device__ void write_gram(const double* gsum, double scale, ColMix mix, long long n, long long N, double* out_arm,
                            double* out_det, double* out_sd_arm, double* out_sd_det, int accum) {
-  for (int e = threadIdx.x; e < NE; e += blockDim.x) {
-    const int a = kPairA[e], b = kPairB[e];
+  constexpr int NEP = ne_of(NPR), NEXP = nex_of(NPR);
+  for (int e = threadIdx.x; e < NEP; e += blockDim.x) {
+    int a, b;
+    pair_n(NPR, e, a, b);
     double ka, kb;
     const int ca = mix.partner(a, ka), cb = mix.partner(b, kb);
     double sdet = 0.0;
 #pragma unroll
     for (int gs = 0; gs < NG; ++gs) {
-      const double* G = gsum + gs * NEX;
-      auto at = [&](int x, int y) { return x <= y ? G[pidx(x, y)] : G[pidx(y, x)]; };
+      const double* G = gsum + gs * NEXP;
+      auto at = [&](int x, int y) { return x <= y ? G[pidx_n(NPR, x, y)] : G[pidx_n(NPR, y, x)]; };
       double v = G[e];
       if (ca >= 0) v += ka * at(ca, b);
       if (cb >= 0) v += kb * at(a, cb);
@@ -515,33 +541,33 @@ __device__ void write_gram(const double* gsum, double scale, ColMix mix, long lo
       v *= scale;
       sdet += v;
       if (out_arm && (NG == 1 || NG == 3)) {
-        double* o = out_arm + ((size_t)gs * N + n) * (NP * NP);
-        o[a * NP + b] = v;
-        o[b * NP + a] = v;
+        double* o = out_arm + ((size_t)gs * N + n) * (NPR * NPR);
+        o[a * NPR + b] = v;
+        o[b * NPR + a] = v;
       }
     }
     if (out_det) {
-      double* o = out_det + (size_t)n * (NP * NP);
-      if (accum) { o[a * NP + b] += sdet; if (a != b) o[b * NP + a] += sdet; }
-      else { o[a * NP + b] = sdet; o[b * NP + a] = sdet; }
+      double* o = out_det + (size_t)n * (NPR * NPR);
+      if (accum) { o[a * NPR + b] += sdet; if (a != b) o[b * NPR + a] += sdet; }
+      else { o[a * NPR + b] = sdet; o[b * NPR + a] = sdet; }
     }
   }
   if (out_sd_arm || out_sd_det) {   // Re<dh/dtheta_a | h>, the same column changes undone
-    for (int a = threadIdx.x; a < NP; a += blockDim.x) {
+    for (int a = threadIdx.x; a < NPR; a += blockDim.x) {
       double k;
       const int c = mix.partner(a, k);
       double sdet = 0.0;
 #pragma unroll
       for (int gs = 0; gs < NG; ++gs) {
-        const double* H = gsum + gs * NEX + NE;
+        const double* H = gsum + gs * NEXP + NEP;
         double v = H[a];
         if (c >= 0) v += k * H[c];
         v *= scale;
         sdet += v;
-        if (out_sd_arm && (NG == 1 || NG == 3)) out_sd_arm[((size_t)gs * N + n) * NP + a] = v;
+        if (out_sd_arm && (NG == 1 || NG == 3)) out_sd_arm[((size_t)gs * N + n) * NPR + a] = v;
       }
       if (out_sd_det) {
-        double* o = out_sd_det + (size_t)n * NP + a;
+        double* o = out_sd_det + (size_t)n * NPR + a;
         *o = accum ? *o + sdet : sdet;
       }
     }
@@ -549,19 +575,20 @@ __device__ void write_gram(const double* gsum, double scale, ColMix mix, long lo
 }
 
 // per-event state of the FP64 kernels (shared memory)
-template <int NARM, int NG>
+template <int NARM, int NG, int NPR = NP>
 struct F64State {
   EvUnion E;
   ProjEv pj;
   GridEv g;
   ArmPat apc[NARM];
   TimeState tsc;
-  double gsum[NG * NEX];
+  double gsum[NG * nex_of(NPR)];
   long long rec;
 };
 
 template <int MODEL, bool EARTH, int NARM, int NG>
-__device__ inline void f64_prepare(const DetDev& det, const unsigned char* scratch, long long rec, F64State<NARM, NG>& S) {
+__device__ inline void f64_prepare(const DetDev& det, const unsigned char* scratch, long long rec,
+                                   F64State<NARM, NG, np_of<MODEL>()>& S) {
   block_load<MODEL>(S.E, S.pj, S.g, scratch, rec);
   if (!EARTH) {
     if (threadIdx.x == 0) {
@@ -577,18 +604,31 @@ __device__ inline void f64_prepare(const DetDev& det, const unsigned char* scrat
 // point; with an odd stride those rows fall in different banks (32 gives 8-way conflicts)
 constexpr int kSR64 = 33;
 
-// Gram of points [k0, k1) into S.gsum (summed over warps); stage: [warp][NG][NP + 1][kSR64] complex,
-// column NP holding the strain itself when sd (SNR derivatives) is set
+// Gram of points [k0, k1) into S.gsum (summed over warps); stage: [warp][NG][NPM + 1][kSR64] complex,
+// column NPM holding the strain itself when sd (SNR derivatives) is set (NPM = np_of<MODEL>())
 template <int MODEL, bool EARTH, int NARM, int NG>
-__device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<NARM, NG>& S, cd* stage, int k0, int k1,
-                                bool sd) {
+__device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<NARM, NG, np_of<MODEL>()>& S, cd* stage,
+                                int k0, int k1, bool sd) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  constexpr int NPS = NP + 1;
-  constexpr int NENT = NEX * NG;
+  constexpr int NPM = np_of<MODEL>();
+  constexpr int NEM = ne_of(NPM), NEXM = nex_of(NPM);
+  constexpr int NPS = NPM + 1;
+  constexpr int NENT = NEXM * NG;
   constexpr int EPT = (NENT + 31) / 32;
   double acc[EPT];
+  int ea[EPT], eb[EPT], eg[EPT];   // this lane's entries: rows, set (-1: none)
 #pragma unroll
-  for (int i = 0; i < EPT; ++i) acc[i] = 0.0;
+  for (int i = 0; i < EPT; ++i) {
+    acc[i] = 0.0;
+    const int e = lane + 32 * i;
+    eg[i] = -1;
+    ea[i] = eb[i] = 0;
+    if (e < NENT) {
+      const int gs = e / NEXM, pe = e - gs * NEXM;
+      if (pe < NEM) { pair_n(NPM, pe, ea[i], eb[i]); eg[i] = gs; }
+      else if (sd) { ea[i] = pe - NEM; eb[i] = NPM; eg[i] = gs; }   // (a, NPM): strain products
+    }
+  }
   cd* my = stage + (size_t)warp * NG * NPS * kSR64;
   for (int base = k0; base < k1; base += kThreads) {
     const int k = base + tid;
@@ -613,13 +653,26 @@ __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<N
       } else {
         ts = S.tsc;
       }
+      // tidal TaylorF2: d Phi / d LambdaTilde and d Phi / d deltaLambda at this point
+      double dphl = 0.0, dphd = 0.0;
+      if (MODEL == 3) {
+        const TF2TEv& t = S.E.tf2t;
+        const double v = t.b.vM.v * exp(lnf / 3.0), v2 = v * v, v5 = v2 * v2 * v;
+        dphl = t.b.pn.A.v * v5 * (-19.5 - (3115.0 / 64.0) * v2);
+        dphd = t.b.pn.A.v * v5 * v2 * t.s12.v;
+      }
 #pragma unroll
       for (int a = 0; a < NARM; ++a) {
         ArmPat ap;
         if (EARTH) arm_pattern(S.pj, det.sin_zeta, ts.x, a, ap);
         else ap = S.apc[a];
         arm_derivs(S.pj, ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D[a]);
-        D[a][NP] = sd ? cadd(cscale(P, ap.Fp), cscale(cmuli(C), ap.Fc)) : cd{0.0, 0.0};
+        const cd H = cadd(cscale(P, ap.Fp), cscale(cmuli(C), ap.Fc));
+        if (MODEL == 3) {   // h ~ e^{-i Phi}: d h / d Lambda = -i h d Phi / d Lambda
+          D[a][NPS - 3] = cscale(cmuli(H), -dphl);
+          D[a][NPS - 2] = cscale(cmuli(H), -dphd);
+        }
+        D[a][NPM] = sd ? H : cd{0.0, 0.0};
       }
     } else {
 #pragma unroll
@@ -646,17 +699,13 @@ __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<N
     __syncwarp();
 #pragma unroll
     for (int i = 0; i < EPT; ++i) {
-      const int e = lane + 32 * i;
-      if (e < NENT) {
-        const int gs = e / NEX, pe = e - gs * NEX;
-        if (pe >= NE && !sd) continue;
-        const int a = pe < NE ? kPairA[pe] : pe - NE, b = pe < NE ? kPairB[pe] : NP;
-        const cd* ra = my + (gs * NPS + a) * kSR64;
-        const cd* rb = my + (gs * NPS + b) * kSR64;
-        double s = 0.0;
+      if (eg[i] >= 0) {
+        const cd* ra = my + (eg[i] * NPS + ea[i]) * kSR64;
+        const cd* rb = my + (eg[i] * NPS + eb[i]) * kSR64;
+        double s2 = 0.0;
 #pragma unroll 8
-        for (int j = 0; j < 32; ++j) s += ra[j].re * rb[j].re + ra[j].im * rb[j].im;
-        acc[i] += s;
+        for (int j = 0; j < 32; ++j) s2 += ra[j].re * rb[j].re + ra[j].im * rb[j].im;
+        acc[i] += s2;
       }
     }
     __syncwarp();
@@ -671,10 +720,10 @@ __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<N
   }
   __syncthreads();
   for (int e = tid; e < NENT; e += kThreads) {
-    double s = 0.0;
+    double s2 = 0.0;
 #pragma unroll
-    for (int w = 0; w < kWarps; ++w) s += red[w * NENT + e];
-    S.gsum[e] = s;
+    for (int w = 0; w < kWarps; ++w) s2 += red[w * NENT + e];
+    S.gsum[e] = s2;
   }
   __syncthreads();
 }
@@ -686,13 +735,14 @@ __global__ void __launch_bounds__(kThreads) fisher_kernel(EvBatch ev, DetDev det
                                                           double* out_arm, double* out_det, double* out_sd_arm,
                                                           double* out_sd_det, int accum) {
   extern __shared__ __align__(16) unsigned char stage_raw[];
-  __shared__ F64State<NARM, NG> S;
+  __shared__ F64State<NARM, NG, np_of<MODEL>()> S;
   const long long n = ev.n0 + blockIdx.x;
   if (n >= ev.N) return;
   f64_prepare<MODEL, EARTH, NARM, NG>(det, scratch, blockIdx.x, S);
   f64_item<MODEL, EARTH, NARM, NG>(ev, det, S, reinterpret_cast<cd*>(stage_raw), 0, S.g.ok ? S.g.R : 0,
                                    out_sd_arm || out_sd_det);
-  write_gram<NG>(S.gsum, 1.0, ColMix{0.0, 0.0}, n, ev.N, out_arm, out_det, out_sd_arm, out_sd_det, accum);
+  write_gram<NG, np_of<MODEL>()>(S.gsum, 1.0, ColMix{0.0, 0.0}, n, ev.N, out_arm, out_det, out_sd_arm, out_sd_det,
+                                 accum);
 }
 
 // ------------------------------------------------------------------ segmented (persistent) launches
@@ -771,8 +821,9 @@ __device__ inline bool next_item(const SegInfo& si, long long count, long long& 
 template <int MODEL, bool EARTH, int NARM, int NG>
 __global__ void __launch_bounds__(kThreads) fisher_seg_kernel(EvBatch ev, DetDev det, const unsigned char* scratch,
                                                               long long count, SegInfo si, int sd) {
+  static_assert(np_of<MODEL>() == NP, "segmented launches carry 11-parameter partial Grams");
   extern __shared__ __align__(16) unsigned char stage_raw[];
-  __shared__ F64State<NARM, NG> S;
+  __shared__ F64State<NARM, NG, np_of<MODEL>()> S;
   if (threadIdx.x == 0) S.rec = -1;
   __syncthreads();
   long long item, rec;

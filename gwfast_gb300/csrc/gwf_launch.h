@@ -44,6 +44,10 @@ cudaError_t launch_fisher_m2(const LaunchArgs& a);
 cudaError_t launch_snr_m0(const LaunchArgs& a);
 cudaError_t launch_snr_m1(const LaunchArgs& a);
 cudaError_t launch_snr_m2(const LaunchArgs& a);
+cudaError_t launch_fisher_m3(const LaunchArgs& a);   // tidal TaylorF2: FP64, 13 parameters
+cudaError_t launch_snr_m3(const LaunchArgs& a);
+size_t setup_stride_m3();
+size_t core_bytes_m3();
 // strain tangent / strain / overlap outputs (gwf_wave_out.cuh): set-up and output launch for
 // events [o.n0, o.n0 + o.cnt) of a.ev; a.scratch holds at least o.cnt records
 cudaError_t launch_wave_m0(const LaunchArgs& a, const WaveOut& o);
@@ -60,7 +64,8 @@ size_t core_bytes_m1();
 size_t core_bytes_m2();
 size_t setup_stride_m1();
 size_t setup_stride_m2();
-cudaError_t launch_cov(const double* F, long long N, double* cov, double* eps, double* cond, cudaStream_t st);
+cudaError_t launch_cov(const double* F, long long N, double* cov, double* eps, double* cond, cudaStream_t st,
+                       int np = NP);
 // mixed precision (gwf_mixed.cu)
 cudaError_t launch_cond(const double* F, long long N, double* cond, cudaStream_t st);
 cudaError_t launch_select(const double* cond, long long N, double thresh, long long* idx, unsigned long long* count,

@@ -101,6 +101,32 @@ __device__ inline void tf2_setup(TF2Ev& e, const D4& Mc, const D4& eta, const D4
   e.ampK = (sqrt(5.0 / 24.0) * pow(kPi, -2.0 / 3.0) * kCGpc / dL) * dpowc(kG3 * Mc, 5.0 / 6.0);
 }
 
+// TaylorF2 with the tidal terms (gwfast/waveforms.py:849-855, PhysRevD.89.103012): the phase
+// series gains (-39/2 LambdaTilde) v^10 + (-3115/64 LambdaTilde + 6595/364 sqrt(1-4 eta) deltaLambda) v^12.
+// LambdaTilde and deltaLambda are Fisher parameters of their own (their tangents are formed
+// analytically per point); the coefficients carry the eta tangent of sqrt(1 - 4 eta).
+template <class C> struct TF2TEvT {
+  TF2EvT<C> b;
+  C t10, t12;   // series coefficients of v^10 and v^12
+  C s12;        // d t12 / d deltaLambda
+};
+using TF2TEv = TF2TEvT<D4>;
+
+__device__ inline void tf2t_setup(TF2TEv& e, const D4& Mc, const D4& eta, const D4& chi1, const D4& chi2, double dL,
+                                  bool spin_ho, double lam_t, double del_lam) {
+  tf2_setup(e.b, Mc, eta, chi1, chi2, dL, spin_ho);
+  e.t10 = D4(-19.5 * lam_t);
+  e.s12 = (6595.0 / 364.0) * seta_of(eta);
+  e.t12 = (-3115.0 / 64.0) * lam_t + e.s12 * del_lam;
+}
+
+// the tidal part of the phase, A (t10 v^10 + t12 v^12) / v^5, at v = (pi M f)^(1/3)
+template <class S, class C>
+__device__ __forceinline__ S tf2_tidal_phase(const TF2TEvT<C>& e, const S& v) {
+  const S v2 = v * v;
+  return co<S>(e.b.pn.A) * (v2 * v2 * v) * (co<S>(e.t10) + co<S>(e.t12) * v2);
+}
+
 // TF2 phase (without the constant offset, which cancels in every output) and amplitude.
 template <class S, class C>
 __device__ __forceinline__ void tf2_point(const TF2EvT<C>& e, typename Real<S>::T f, typename Real<S>::T f13,

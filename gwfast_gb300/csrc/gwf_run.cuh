@@ -31,8 +31,10 @@ cudaError_t chunked(const LaunchArgs& a, bool f32, MAIN main) {
     const long long cnt = (a.ev.N - n0) < kChunk ? (a.ev.N - n0) : kChunk;
     const unsigned nb = (unsigned)((cnt + 63) / 64);
     setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, a.det, a.wf, a.qnm, a.nq, a.scratch, cnt, a.core, a.core_mode, a.core_idx);
-    if (f32) setup_f32_kernel<M><<<nb, 64, 0, a.stream>>>(a.det, a.scratch, scratch32_of(a), cnt,
-                                                          a.det.shape == 1 ? 2 : 1, a.det.earth);
+    if constexpr (M != 3) {   // (the tidal model has no FP32 form)
+      if (f32) setup_f32_kernel<M><<<nb, 64, 0, a.stream>>>(a.det, a.scratch, scratch32_of(a), cnt,
+                                                            a.det.shape == 1 ? 2 : 1, a.det.earth);
+    }
     const cudaError_t e = main(ev, cnt);
     if (e != cudaSuccess) return e;
   }
@@ -75,8 +77,8 @@ cudaError_t persist_grid(K k, int smem, int* grid) {
 
 template <bool EARTH, int NARM, int NG>
 cudaError_t fisher_one(const LaunchArgs& a) {
-  const int smem = kWarps * NG * (NP + 1) * kSR64 * (int)sizeof(cd);
-  if (a.seg <= 0) {
+  const int smem = kWarps * NG * (np_of<M>() + 1) * kSR64 * (int)sizeof(cd);
+  if (a.seg <= 0 || M == 3) {
     auto k = fisher_kernel<M, EARTH, NARM, NG>;
     cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (err != cudaSuccess) return err;
@@ -86,14 +88,18 @@ cudaError_t fisher_one(const LaunchArgs& a) {
       return cudaSuccess;
     });
   }
-  auto ks = fisher_seg_kernel<M, EARTH, NARM, NG>;
-  cudaError_t err = cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  int grid = 0;
-  if (err == cudaSuccess) err = persist_grid(ks, smem, &grid);
-  if (err != cudaSuccess) return err;
-  return chunked(a, false, [&](const EvBatch& ev, long long cnt) {
-    return seg_chunk<NG>(a, ev, cnt, ks, a.scratch, smem, grid, nullptr, 0);
-  });
+  if constexpr (M == 3) {
+    return cudaErrorNotSupported;   // not reached: the tidal model always runs one CTA per event
+  } else {
+    auto ks = fisher_seg_kernel<M, EARTH, NARM, NG>;
+    cudaError_t err = cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int grid = 0;
+    if (err == cudaSuccess) err = persist_grid(ks, smem, &grid);
+    if (err != cudaSuccess) return err;
+    return chunked(a, false, [&](const EvBatch& ev, long long cnt) {
+      return seg_chunk<NG>(a, ev, cnt, ks, a.scratch, smem, grid, nullptr, 0);
+    });
+  }
 }
 
 template <bool EARTH, int NARM, int NG>
@@ -135,12 +141,16 @@ cudaError_t snr_one(const LaunchArgs& a) {
 cudaError_t fisher_dispatch(const LaunchArgs& a) {
   const bool tri = a.det.shape == 1;
   if (a.precision == 1) {
-    if (a.det.earth) {
-      if (!tri) return fisher_one_f32<true, 1, 1>(a);
-      return a.per_arm ? fisher_one_f32<true, 2, 3>(a) : fisher_one_f32<true, 2, 2>(a);
+    if constexpr (M == 3) {
+      return cudaErrorNotSupported;
+    } else {
+      if (a.det.earth) {
+        if (!tri) return fisher_one_f32<true, 1, 1>(a);
+        return a.per_arm ? fisher_one_f32<true, 2, 3>(a) : fisher_one_f32<true, 2, 2>(a);
+      }
+      if (!tri) return fisher_one_f32<false, 1, 1>(a);
+      return a.per_arm ? fisher_one_f32<false, 2, 3>(a) : fisher_one_f32<false, 2, 2>(a);
     }
-    if (!tri) return fisher_one_f32<false, 1, 1>(a);
-    return a.per_arm ? fisher_one_f32<false, 2, 3>(a) : fisher_one_f32<false, 2, 2>(a);
   }
   if (a.det.earth) {
     if (!tri) return fisher_one<true, 1, 1>(a);
@@ -207,7 +217,8 @@ cudaError_t group_one(const LaunchArgs& a, GroupDev g) {
 }
 
 cudaError_t group_dispatch(const LaunchArgs& a, const GroupDev& g) {
-  return a.det.earth ? group_one<true>(a, g) : group_one<false>(a, g);
+  if constexpr (M == 3) return cudaErrorNotSupported;
+  else return a.det.earth ? group_one<true>(a, g) : group_one<false>(a, g);
 }
 
 template <bool EARTH, int NARM>
@@ -221,10 +232,14 @@ cudaError_t wave_one(const LaunchArgs& a, const WaveOut& o) {
 }
 
 cudaError_t wave_dispatch(const LaunchArgs& a, const WaveOut& o) {
-  if (o.cnt <= 0) return cudaSuccess;
-  const bool tri = a.det.shape == 1;
-  if (a.det.earth) return tri ? wave_one<true, 2>(a, o) : wave_one<true, 1>(a, o);
-  return tri ? wave_one<false, 2>(a, o) : wave_one<false, 1>(a, o);
+  if constexpr (M == 3) {
+    return cudaErrorNotSupported;   // 11-parameter outputs only
+  } else {
+    if (o.cnt <= 0) return cudaSuccess;
+    const bool tri = a.det.shape == 1;
+    if (a.det.earth) return tri ? wave_one<true, 2>(a, o) : wave_one<true, 1>(a, o);
+    return tri ? wave_one<false, 2>(a, o) : wave_one<false, 1>(a, o);
+  }
 }
 
 }  // namespace

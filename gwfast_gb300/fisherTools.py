@@ -21,21 +21,22 @@ def CovMatr(FisherMatrix, invMethodIn='cho', condNumbMax=1e50, truncate=False, s
         raise NotImplementedError('singular-value truncation is not implemented on the GPU path')
     F = np.ascontiguousarray(np.moveaxis(np.asarray(FisherMatrix, dtype=np.float64), -1, 0))
     P = F.shape[1]
-    if F.shape[1:] != (P, P) or P > 11:
-        raise NotImplementedError('the GPU inversion handles up to 11x11 matrices')
-    if P < 11:
+    if F.shape[1:] != (P, P) or P > 13:
+        raise NotImplementedError('the GPU inversion handles up to 13x13 matrices')
+    K = 11 if P <= 11 else 13   # the kernel sizes (11 parameters; 13 for the tidal model)
+    if P < K:
         # block-diagonal embedding with an identity block (e.g. after fixParams): the inverse of
         # the leading block is the leading block of the inverse; an equilibrated matrix has
         # eigenvalues on both sides of 1, so the condition number is unchanged, and the identity
         # block adds no inversion error
-        Fp = np.broadcast_to(np.eye(11), (F.shape[0], 11, 11)).copy()
+        Fp = np.broadcast_to(np.eye(K), (F.shape[0], K, K)).copy()
         Fp[:, :P, :P] = F
         F = Fp
     N = F.shape[0]
     cov = np.empty_like(F)
     eps = np.empty(N)
     cond = np.empty(N)
-    _lib.context(device).cov(F, cov=cov, eps=eps, cond=cond)
+    _lib.context(device).cov(F, cov=cov, eps=eps, cond=cond, n_params=K)
     out = np.moveaxis(np.ascontiguousarray(cov[:, :P, :P]), 0, -1)
     if return_cond:
         return out, eps, cond

@@ -16,17 +16,21 @@ from .waveforms import PARAMS
 DAY = 3600. * 24.
 
 
-def event_array(evParams):
-    """(11, N) float64 array in the Fisher order from the events dict."""
-    cols = [np.atleast_1d(np.asarray(evParams[k], dtype=np.float64)) for k in PARAMS]
+def event_array(evParams, params=PARAMS):
+    """(P, N) float64 array in the Fisher order from the events dict (P = 11, or 13 with the tidal
+    parameters)."""
+    cols = [np.atleast_1d(np.asarray(evParams[k], dtype=np.float64)) for k in params]
     n = max(len(c) for c in cols)
     cols = [np.broadcast_to(c, (n,)) if len(c) != n else c for c in cols]
     return np.ascontiguousarray(np.stack(cols))
 
 
-def _prep(evParams):
+def _prep(evParams, wf=None):
     utils.check_evparams(evParams)
     utils.fill_spins(evParams)
+    if wf is not None and wf.is_tidal:
+        utils.fill_tidal(evParams)
+        return event_array(evParams, wf.params)
     return event_array(evParams)
 
 
@@ -38,8 +42,8 @@ def snr_batch(signals, evParams, res=1000, device=0, precision='fp64', res_per_e
     """Per-arm SNRs of all signals in one library call.  Returns a list (per signal) of (arms, N) arrays.
 
     precision: 'fp64' or 'fp32' (TaylorF2 and IMRPhenomD); res_per_event as in fisher_batch."""
-    p = _prep(evParams)
     wf = signals[0].wf_model
+    p = _prep(evParams, wf)
     if any(type(s.wf_model) is not type(wf) for s in signals):
         return [s._snr_arms(evParams, res, precision) for s in signals]
     N = p.shape[1]
@@ -61,7 +65,8 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
                  refine_cond=None, res_per_event=None, snr_derivs=False):
     """Fisher matrices of all signals in one library call.
 
-    per_arm: list (per signal) of (arms, N, 11, 11); otherwise the network total (N, 11, 11).
+    per_arm: list (per signal) of (arms, N, P, P); otherwise the network total (N, P, P); P = 11, or 13
+    for the tidal TaylorF2 (LambdaTilde, deltaLambda last).
     res_per_event: optional (N,) grid lengths, one per event (an extension: gwfast uses one res).
     snr_derivs: also return, per signal, (arms, N, 11) of 4 trapz(Re(h conj(dh/dtheta)) / S) (the
     per-arm SNR-derivative integrals of gwfast's return_SNR_derivatives); the Fisher part is then
@@ -70,9 +75,10 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
     'mixed' ('fp32', then FP64 for the events whose network Fisher has an equilibrated condition
     number above refine_cond, default 1e12).
     """
-    p = _prep(evParams)
     wf = signals[0].wf_model
+    p = _prep(evParams, wf)
     N = p.shape[1]
+    P = wf.nParams
     slots = _arm_slots(signals)
     ctx = _lib.context(device)
     if precision == 'mixed':
@@ -81,8 +87,8 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
     rev = None if res_per_event is None else np.ascontiguousarray(np.broadcast_to(res_per_event, (N,)), dtype=np.int32)
     duty = any(s.DutyFactor is not None for s in signals)
     if per_arm or duty or snr_derivs:
-        out = np.empty((sum(slots), N, 11, 11))
-        sd = np.empty((sum(slots), N, 11)) if snr_derivs else None
+        out = np.empty((sum(slots), N, P, P))
+        sd = np.empty((sum(slots), N, P)) if snr_derivs else None
         ctx.fisher([s.det_id for s in signals], wf.gpu_desc(), p, res, res_ev=rev, spacing=sp, per_arm=True,
                    out_arm=out, precision=precision, out_sd_arm=sd)
         res_l, sd_l, i = [], [], 0
@@ -96,7 +102,7 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
         if per_arm:
             return res_l
         return sum(r.sum(axis=0) for r in res_l)
-    out = np.empty((N, 11, 11))
+    out = np.empty((N, P, P))
     ctx.fisher([s.det_id for s in signals], wf.gpu_desc(), p, res, res_ev=rev, spacing=sp, per_arm=False,
                out_net=out, precision=precision)
     return out
@@ -128,8 +134,8 @@ def overlap_batch(signals, WF1, WF2, evParams1, evParams2, res=1000):
     return ov, n1, n2
 
 
-def _jacobian(evParams, N, use_m1m2, use_chi1chi2):
-    J = np.broadcast_to(np.eye(11), (N, 11, 11)).copy()
+def _jacobian(evParams, N, use_m1m2, use_chi1chi2, P=11):
+    J = np.broadcast_to(np.eye(P), (N, P, P)).copy()
     if use_m1m2:
         m1, m2 = utils.m1m2_from_Mceta(np.asarray(evParams['Mc']), np.asarray(evParams['eta']))
         Mc, eta = utils.Mceta_from_m1m2(m1, m2)
@@ -148,7 +154,7 @@ def reparametrise(F, evParams, use_m1m2=False, use_chi1chi2=True):
     """Chain rule to (m1, m2) and/or (chiS, chiA), F: (..., N, 11, 11) (gwfast/signal.py:818-842)."""
     if not use_m1m2 and use_chi1chi2:
         return F
-    J = _jacobian(evParams, F.shape[-3], use_m1m2, use_chi1chi2)
+    J = _jacobian(evParams, F.shape[-3], use_m1m2, use_chi1chi2, F.shape[-1])
     return np.einsum('nai,...nab,nbj->...nij', J, F, J)
 
 
@@ -156,7 +162,7 @@ def reparametrise_derivs(D, evParams, use_m1m2=False, use_chi1chi2=True):
     """The chain rule for strain derivatives, D: (arms, 11, N, R)."""
     if not use_m1m2 and use_chi1chi2:
         return D
-    J = _jacobian(evParams, D.shape[2], use_m1m2, use_chi1chi2)
+    J = _jacobian(evParams, D.shape[2], use_m1m2, use_chi1chi2, D.shape[1])
     return np.einsum('naj,xanr->xjnr', J, D)
 
 
@@ -164,7 +170,7 @@ def reparametrise_vec(v, evParams, use_m1m2=False, use_chi1chi2=True):
     """The same chain rule for derivative vectors, v: (..., N, 11)."""
     if not use_m1m2 and use_chi1chi2:
         return v
-    J = _jacobian(evParams, v.shape[-2], use_m1m2, use_chi1chi2)
+    J = _jacobian(evParams, v.shape[-2], use_m1m2, use_chi1chi2, v.shape[-1])
     return np.einsum('nai,...na->...ni', J, v)
 
 
@@ -250,7 +256,7 @@ class GWSignal:
     def FisherMatr(self, evParams, res=1000, df=None, spacing='geom', use_m1m2=False, use_chi1chi2=True,
                    use_prec_ang=True, computeDerivFinDiff=False, computeAnalyticalDeriv=True, return_all=False,
                    return_derivatives=False, return_SNR_derivatives=False, precision='fp64', **kwargs):
-        """gwfast/signal.py:782-1098; returns (11, 11, N), or a list per arm with return_all.
+        """gwfast/signal.py:782-1098; returns (P, P, N), or a list per arm with return_all (P = nParams).
 
         precision='fp32' selects the split-precision kernel (all three models), 'mixed' the
         split-precision kernel with FP64 recomputation of ill-conditioned events (refine_cond)."""

@@ -3,8 +3,8 @@
 The waveforms themselves are evaluated inside the fused CUDA kernels; these
 objects carry what gwfast's callers read from a model (``ParNums``, ``nParams``,
 the ``is_*`` flags, ``objType``, ``fcut``) plus the descriptor the C ABI needs.
-Supported: TaylorF2_RestrictedPN (optionally with the 3.5PN spin-spin terms),
-IMRPhenomD and IMRPhenomHM, aligned spins, no tides or eccentricity.
+Supported: TaylorF2_RestrictedPN (optionally with the 3.5PN spin-spin terms and with the tidal
+terms, 13 parameters), IMRPhenomD and IMRPhenomHM, aligned spins, no eccentricity.
 """
 import numpy as np
 
@@ -12,6 +12,7 @@ from . import _lib
 from . import gwfastGlobals as glob
 
 PARAMS = ('Mc', 'eta', 'dL', 'theta', 'phi', 'iota', 'psi', 'tcoal', 'Phicoal', 'chi1z', 'chi2z')
+PARAMS_TIDAL = PARAMS + ('LambdaTilde', 'deltaLambda')   # gwfast/waveforms.py:106-109
 
 
 class WaveFormModel:
@@ -20,8 +21,9 @@ class WaveFormModel:
     def __init__(self, objType, fcutPar, is_newtonian=False, is_tidal=False, is_HigherModes=False, is_chi1chi2=True,
                  is_Precessing=False, is_LAL=False, is_prec_ang=False, is_eccentric=False, is_holomorphic=False,
                  apply_fcut=True):
-        for flag, name in ((is_newtonian, 'is_newtonian'), (is_tidal, 'is_tidal'), (is_Precessing, 'is_Precessing'),
-                           (is_LAL, 'is_LAL'), (is_eccentric, 'is_eccentric')):
+        tidal_ok = type(self).__name__ == 'TaylorF2_RestrictedPN'
+        for flag, name in ((is_newtonian, 'is_newtonian'), (is_tidal and not tidal_ok, 'is_tidal'),
+                           (is_Precessing, 'is_Precessing'), (is_LAL, 'is_LAL'), (is_eccentric, 'is_eccentric')):
             if flag:
                 raise NotImplementedError('%s waveforms are not implemented on the GPU path' % name)
         if not apply_fcut:
@@ -38,21 +40,29 @@ class WaveFormModel:
         self.is_eccentric = is_eccentric
         self.is_holomorphic = is_holomorphic
         self.apply_fcut = apply_fcut
-        self.nParams = 11
+        self.nParams = 13 if is_tidal else 11
         if is_chi1chi2:
             self.ParNums = {'Mc': 0, 'eta': 1, 'dL': 2, 'theta': 3, 'phi': 4, 'iota': 5, 'psi': 6, 'tcoal': 7,
                             'Phicoal': 8, 'chi1z': 9, 'chi2z': 10}
         else:
             self.ParNums = {'Mc': 0, 'eta': 1, 'dL': 2, 'theta': 3, 'phi': 4, 'iota': 5, 'psi': 6, 'tcoal': 7,
                             'Phicoal': 8, 'chiS': 9, 'chiA': 10}
+        if is_tidal:
+            self.ParNums['LambdaTilde'] = 11
+            self.ParNums['deltaLambda'] = 12
+
+    @property
+    def params(self):
+        """Names of the Fisher parameters in order (the rows of the event array)."""
+        return PARAMS_TIDAL if self.is_tidal else PARAMS
 
     def fcut(self, **kwargs):
         """Cut frequency in Hz (gwfast/waveforms.py:190-199)."""
         return self.fcutPar / (np.asarray(kwargs['Mc']) / (np.asarray(kwargs['eta']) ** (3. / 5.)))
 
     def gpu_desc(self):
-        return _lib.WfDesc(_lib.MODEL_IDS[type(self).__name__], int(getattr(self, 'use_3p5PN_SpinHO', False)),
-                           float(self.fcutPar))
+        model = _lib.MODEL_TF2_TIDAL if self.is_tidal else _lib.MODEL_IDS[type(self).__name__]
+        return _lib.WfDesc(model, int(getattr(self, 'use_3p5PN_SpinHO', False)), float(self.fcutPar))
 
     def _device_only(self, *a, **k):
         raise NotImplementedError('%s is evaluated inside the fused GPU kernels; use GWSignal / DetNet'
@@ -62,7 +72,8 @@ class WaveFormModel:
 
 
 class TaylorF2_RestrictedPN(WaveFormModel):
-    """gwfast/waveforms.py:697-953 (fcut: twice the Schwarzschild ISCO by default)."""
+    """gwfast/waveforms.py:697-953 (fcut: twice the Schwarzschild ISCO by default). is_tidal adds the
+    5PN and 6PN tidal phase terms and the parameters LambdaTilde, deltaLambda (FP64 path only)."""
 
     def __init__(self, fHigh=None, is_tidal=False, use_3p5PN_SpinHO=False, phiref_vlso=False, is_eccentric=False,
                  fRef_ecc=None, which_ISCO='Schw', use_QuadMonTid=False, **kwargs):

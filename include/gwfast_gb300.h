@@ -13,14 +13,15 @@
  *    parameter k of event n, k in the Fisher order
  *      0 Mc [Msun, detector frame], 1 eta, 2 dL [Gpc], 3 theta, 4 phi, 5 iota,
  *      6 psi [rad], 7 tcoal [GMST days], 8 Phicoal [rad], 9 chi1z, 10 chi2z
- *    (gwfast/waveforms.py:78, :125-129).
+ *    (gwfast/waveforms.py:78, :125-129); the tidal TaylorF2 (GWF_WF_TAYLORF2_TIDAL) adds
+ *      11 LambdaTilde, 12 deltaLambda (gwfast/waveforms.py:106-109), 13 rows in all.
  *  - mem = GWF_MEM_HOST: params, res_per_event and outputs are host pointers; the
  *    call copies in, runs, copies out and returns when the outputs are written.
  *    mem = GWF_MEM_DEVICE: all pointers are device pointers owned by the caller;
  *    the work is queued on `stream` (NULL = the context's stream) and the call
  *    returns without waiting.
- *  - Fisher matrices are written row-major, 11 x 11 per event, tcoal in seconds
- *    (gwfast/signal.py:918-920).
+ *  - Fisher matrices are written row-major, P x P per event (P = 11, 13 for the tidal model),
+ *    tcoal in seconds (gwfast/signal.py:918-920).
  *  - One context per thread; calls on one context are serialised on its stream.
  */
 #ifndef GWFAST_GB300_H
@@ -33,6 +34,7 @@ extern "C" {
 #endif
 
 #define GWF_NPARAMS 11
+#define GWF_NPARAMS_TIDAL 13
 
 enum {
   GWF_OK = 0,
@@ -43,7 +45,8 @@ enum {
   GWF_ERR_UNSUPPORTED = -5
 };
 
-enum { GWF_WF_TAYLORF2 = 0, GWF_WF_PHENOMD = 1, GWF_WF_PHENOMHM = 2 };
+/* GWF_WF_TAYLORF2_TIDAL: TaylorF2_RestrictedPN(is_tidal=True), gwfast/waveforms.py:849-855; FP64 only */
+enum { GWF_WF_TAYLORF2 = 0, GWF_WF_PHENOMD = 1, GWF_WF_PHENOMHM = 2, GWF_WF_TAYLORF2_TIDAL = 3 };
 enum { GWF_SHAPE_L = 0, GWF_SHAPE_T = 1 };
 enum { GWF_SPACING_GEOM = 0, GWF_SPACING_LIN = 1 };
 enum { GWF_MEM_HOST = 0, GWF_MEM_DEVICE = 1 };
@@ -63,8 +66,8 @@ typedef struct {
   double fmax;         /* Hz, <= 0 for none */
 } gwf_det_desc;
 
-/* Waveform model (gwfast/waveforms.py:49-199 WaveFormModel; :697 TaylorF2_RestrictedPN,
- * :959 IMRPhenomD, :1838 IMRPhenomHM). */
+/* Waveform model (gwfast/waveforms.py:49-199 WaveFormModel; :697 TaylorF2_RestrictedPN (is_tidal:
+ * model 3), :959 IMRPhenomD, :1838 IMRPhenomHM). */
 typedef struct {
   int model;           /* GWF_WF_* */
   int spin_ho;         /* TaylorF2 use_3p5PN_SpinHO */
@@ -187,6 +190,10 @@ int gwf_autotune_segments(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf
  * Events whose equilibrated matrix is not positive definite get NaN covariances. */
 int gwf_cov(gwf_ctx* ctx, const double* F, int64_t n_events, int mem, double* cov, double* eps, double* cond,
             void* stream);
+
+/* gwf_cov for P x P matrices, P = n_params = 11 or 13 (the tidal model); F, cov [N][P][P]. */
+int gwf_cov_n(gwf_ctx* ctx, const double* F, int64_t N, int n_params, int mem, double* cov, double* eps, double* cond,
+              void* stream);
 
 /* Learned SNR screen (no counterpart in gwfast: a method-level addition). A multilayer perceptron,
  * 11 features -> `layers` hidden layers of `hidden` SiLU units -> ln(network SNR), trained on SNRs

@@ -38,6 +38,7 @@ EULER_GAMMA = 0.5772156649015329
 DAY_S = 3600. * 24.
 
 PARAMS = ('Mc', 'eta', 'dL', 'theta', 'phi', 'iota', 'psi', 'tcoal', 'Phicoal', 'chi1z', 'chi2z')
+PARAMS_TIDAL = PARAMS + ('LambdaTilde', 'deltaLambda')   # gwfast/waveforms.py:106-109
 NPAR = 11
 TC_INDEX = 7
 
@@ -121,14 +122,19 @@ def tf2_fcut(Mc, eta):
     return fhigh / (Mc / eta ** (3. / 5.))
 
 
-def tf2_phase(f, Mc, eta, chi1, chi2, spin_ho=False):
-    """gwfast/waveforms.py:743-862 (not tidal, not eccentric, fRef at v = 0)."""
+def tf2_phase(f, Mc, eta, chi1, chi2, spin_ho=False, lam_t=None, del_lam=None):
+    """gwfast/waveforms.py:743-862 (not eccentric, fRef at v = 0); with lam_t/del_lam the tidal terms
+    (-39/2 LambdaTilde) v^10 + (-3115/64 LambdaTilde + 6595/364 sqrt(1-4 eta) deltaLambda) v^12 of
+    :849-855 join the series."""
     Mtot_s = Mc * GMSUN_OVER_C3 / eta ** (3. / 5.)
     v = (PI * Mtot_s * f) ** (1. / 3.)
     c = pn_coeffs(eta, chi1, chi2, spin_ho=spin_ho)
     lv = torch.log(v)
     ser = (1. + c['two'] * v * v + c['three'] * v ** 3 + c['four'] * v ** 4
            + (c['five'] + c['five_log'] * lv) * v ** 5 + (c['six'] + c['six_log'] * lv) * v ** 6 + c['seven'] * v ** 7)
+    if lam_t is not None:
+        seta = torch.sqrt(torch.where(eta < 0.25, 1.0 - 4.0 * eta, torch.zeros_like(eta)))
+        ser = ser + (-0.5 * 39. * lam_t) * v ** 10 + (-3115. / 64. * lam_t + 6595. / 364. * seta * del_lam) * v ** 12
     return 3. / (128. * eta) * ser / v ** 5 + PI - PI * 0.25
 
 
@@ -635,10 +641,16 @@ def delt_loc(det, theta, phi, t):
 class Model:
     """Which waveform to evaluate: 'TF2', 'PhenomD' or 'PhenomHM'."""
 
-    def __init__(self, name, spin_ho=False):
+    def __init__(self, name, spin_ho=False, tidal=False):
         assert name in ('TF2', 'PhenomD', 'PhenomHM')
+        assert not tidal or name == 'TF2'
         self.name = name
         self.spin_ho = spin_ho
+        self.tidal = tidal
+
+    @property
+    def params(self):
+        return PARAMS_TIDAL if self.tidal else PARAMS
 
     @property
     def is_hm(self):
@@ -654,6 +666,9 @@ class Model:
 
     def phase(self, f, p):
         if self.name == 'TF2':
+            if self.tidal:
+                return tf2_phase(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'], self.spin_ho, p['LambdaTilde'],
+                                 p['deltaLambda'])
             return tf2_phase(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'], self.spin_ho)
         return phd_phase(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'])
 
@@ -686,9 +701,9 @@ def event_grid(det, model, p, res, spacing='geom'):
     return torch.as_tensor(f, dtype=DT), psd_on_grid(det, f)
 
 
-def to_params(events):
+def to_params(events, params=PARAMS):
     """dict of 1-D arrays -> dict of (N,1) float64 tensors in the Fisher order."""
-    return {k: torch.as_tensor(np.asarray(events[k], dtype=np.float64), dtype=DT).reshape(-1, 1) for k in PARAMS}
+    return {k: torch.as_tensor(np.asarray(events[k], dtype=np.float64), dtype=DT).reshape(-1, 1) for k in params}
 
 
 # ---------------------------------------------------------------- strain
@@ -738,7 +753,7 @@ def strain(det, model, f, p, rot=0.):
 def strain_jacobian(det, model, f, p, rot=0.):
     """d h / d theta_i for the 11 parameters, (11, N, R) complex, tcoal in days (as gwfast/signal.py:1301)."""
     out = []
-    for name in PARAMS:
+    for name in model.params:
         def fn(x, name=name):
             q = dict(p)
             q[name] = x

@@ -6,7 +6,7 @@ stand-in modules before importing it:
 
 * ``jax.numpy`` is numpy itself (float64, same function names);
 * ``jax.jacrev`` is a 5-point central finite difference (only used for the Fisher
-  golden; the derivative error it leaves is measured and stored beside it);
+  golden; its rounding through the ~1e5-rad phase limits that golden, see the tests);
 * ``jax.vmap`` loops over the leading (event) axis;
 * ``h5py`` / ``numdifftools`` are empty modules (only touched off the hot path).
 
@@ -53,7 +53,20 @@ def _install_shims():
             for j in nums:
                 x = args[j]
                 xr = np.real(x)
-                h = 1e-7 * max(abs(float(xr)), 1e-1) if j in (1, 2) else 1e-6
+                # Mc, eta: relative steps. LambdaTilde, deltaLambda (arguments 16, 17): the phase is
+                # linear in them and their tangents are tiny at low frequency, so the steps must be
+                # large enough to keep the rounding of the ~1e5-rad phase out of the difference and
+                # small enough that the phase change stays << 1 rad at the top of the band
+                # (d Phi / d deltaLambda ~ sqrt(1 - 4 eta) v^7 is far smaller than d Phi / d LambdaTilde).
+                # The rest: 1e-6.
+                if j in (1, 2):
+                    h = 1e-7 * max(abs(float(xr)), 1e-1)
+                elif j == 16:
+                    h = 1e-3 * max(abs(float(xr)), 1.)
+                elif j == 17:
+                    h = 10.
+                else:
+                    h = 1e-6
                 def at(d):
                     a = list(args)
                     a[j] = x + d
@@ -157,7 +170,7 @@ KEYS = ('Mc', 'eta', 'dL', 'theta', 'phi', 'iota', 'psi', 'tcoal', 'Phicoal', 'c
 
 def make_case(name, wf, dets, events, res, fisher=True):
     out = {'res': np.array(res)}
-    for k in KEYS:
+    for k in KEYS + (('Lambda1', 'Lambda2', 'LambdaTilde', 'deltaLambda') if wf.is_tidal else ()):
         out['ev_' + k] = np.asarray(events[k], dtype=np.float64)
     sigs = {}
     for dname, (fwall, earth) in dets.items():
@@ -192,9 +205,11 @@ def make_case(name, wf, dets, events, res, fisher=True):
             args = [fgd] + [ev[k] for k in ('Mc', 'eta', 'dL', 'theta', 'phi', 'iota', 'psi', 'tcoal', 'Phicoal',
                                              'chi1z', 'chi2z')]
             z = np.zeros_like(ev['Mc'])
-            h = s.GWstrain(*args, z, z, z, z, z, z, z, rot=r, is_chi1chi2=True)
+            lt = ev['LambdaTilde'] if wf.is_tidal else z
+            dl = ev['deltaLambda'] if wf.is_tidal else z
+            h = s.GWstrain(*args, z, z, z, z, lt, dl, z, rot=r, is_chi1chi2=True)
             out['strain_' + tag] = h
-            der = s._AnalyticalDerivatives(*args, z, z, z, z, z, z, z, rot=r, use_chi1chi2=True)
+            der = s._AnalyticalDerivatives(*args, z, z, z, z, lt, dl, z, rot=r, use_chi1chi2=True)
             for nm, dv in zip(('dL', 'theta', 'phi', 'iota', 'psi', 'tcoal', 'Phicoal'), der):
                 if dv is not None:
                     out['dana_%s_%s' % (nm, tag)] = np.asarray(dv)
@@ -218,6 +233,14 @@ def main():
     rng = np.random.default_rng(1003)
     make_case('phm_net_earth', WF.IMRPhenomHM(), {'L1': (10., True), 'ETS': (5., True)},
               events_bbh(rng, 3, mmax=150., qmin=0.1, chimax=0.9), 300)
+    rng = np.random.default_rng(1004)
+    ev = events_bns(rng, 3)
+    ev['Lambda1'] = rng.uniform(100., 1000., 3)
+    ev['Lambda2'] = rng.uniform(100., 1000., 3)
+    import gwfast.gwfastUtils as UT
+    ev['LambdaTilde'], ev['deltaLambda'] = UT.Lamt_delLam_from_Lam12(ev['Lambda1'], ev['Lambda2'], ev['eta'])
+    make_case('tf2tidal_T_earth', WF.TaylorF2_RestrictedPN(is_tidal=True), {'ETS': (5., True), 'Virgo': (10., True)},
+              ev, 300)
     # KAT from the reference tutorial: GW170817-like TF2 Schwarzschild cut frequency 1590.1 Hz
     z = 0.00980
     ev = {'Mc': np.array([1.1859 * (1. + z)]), 'eta': np.array([0.24786618323504223])}

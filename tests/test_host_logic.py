@@ -170,3 +170,29 @@ def test_mlp_oracle_gradient_matches_finite_differences():
         fd = (M.forward_backward(w + d, norm, p, t, hidden, layers)[0]
               - M.forward_backward(w - d, norm, p, t, hidden, layers)[0]) / 2e-6
         assert abs(fd - g[i]) < 1e-6 * max(1., abs(g[i]))
+
+
+def test_tidal_parameters_and_descriptor():
+    """LambdaTilde/deltaLambda from Lambda1/Lambda2 and back (gwfast/gwfastUtils.py:398-446); the tidal
+    TaylorF2 descriptor has 13 parameters and model id 3."""
+    from gwfast_gb300 import gwfastUtils as U
+    from gwfast_gb300 import waveforms as W
+    rng = np.random.default_rng(3)
+    eta = rng.uniform(0.2, 0.25, 50)
+    l1, l2 = rng.uniform(0., 3000., 50), rng.uniform(0., 3000., 50)
+    lt, dl = U.Lamt_delLam_from_Lam12(l1, l2, eta)
+    r1, r2 = U.Lam12_from_Lamt_delLam(lt, dl, eta)
+    np.testing.assert_allclose(r1, l1, rtol=1e-9, atol=1e-8)
+    np.testing.assert_allclose(r2, l2, rtol=1e-9, atol=1e-8)
+    # equal masses, equal deformabilities: LambdaTilde = Lambda, deltaLambda = 0
+    lt0, dl0 = U.Lamt_delLam_from_Lam12(np.array([400.]), np.array([400.]), np.array([0.25]))
+    np.testing.assert_allclose(lt0, 400., rtol=1e-14)
+    np.testing.assert_allclose(dl0, 0., atol=1e-12)
+    wf = W.TaylorF2_RestrictedPN(is_tidal=True)
+    assert wf.nParams == 13 and wf.params[-2:] == ('LambdaTilde', 'deltaLambda')
+    assert wf.gpu_desc().model == 3 and wf.objType == 'BNS'
+    ev = {'Mc': np.array([1.2]), 'eta': np.array([0.24])}
+    with pytest.raises(ValueError):
+        U.fill_tidal(ev)
+    with pytest.raises(NotImplementedError):
+        W.IMRPhenomD(is_tidal=True)

@@ -13,13 +13,15 @@ CASES = {
     'tf2_T_earth': (O.Model('TF2', spin_ho=True), {'ETS': (10., True)}),
     'phd_net_earth': (O.Model('PhenomD'), {'L1': (10., True), 'H1': (10., True), 'ETS': (5., True)}),
     'phm_net_earth': (O.Model('PhenomHM'), {'L1': (10., True), 'ETS': (5., True)}),
+    'tf2tidal_T_earth': (O.Model('TF2', tidal=True), {'ETS': (5., True), 'Virgo': (10., True)}),
 }
 
 
 def load(name):
     g = np.load(os.path.join(GOLD, name + '.npz'))
-    ev = {k: g['ev_' + k] for k in O.PARAMS}
-    return g, O.to_params(ev), int(g['res'])
+    params = CASES[name][0].params if name in CASES else O.PARAMS
+    ev = {k: g['ev_' + k] for k in params}
+    return g, O.to_params(ev, params), int(g['res'])
 
 
 def det_of(name, fw, earth):
