@@ -13,7 +13,7 @@ from . import _build
 
 GWF_OK = 0
 ERRORS = {-1: 'invalid argument', -2: 'CUDA error', -3: 'out of memory', -4: 'timeout', -5: 'unsupported'}
-MODEL_IDS = {'TaylorF2_RestrictedPN': 0, 'IMRPhenomD': 1, 'IMRPhenomHM': 2}
+MODEL_IDS = {'TaylorF2_RestrictedPN': 0, 'IMRPhenomD': 1, 'IMRPhenomHM': 2, 'IMRPhenomD_NRTidalv2': 4}
 MODEL_TF2_TIDAL = 3
 MEM_HOST, MEM_DEVICE = 0, 1
 PRECISION = {'fp64': 0, 'fp32': 1, 'mixed': 2}

@@ -118,7 +118,7 @@ struct gwf_ctx {
 namespace {
 
 // Fisher parameters of a waveform model: 11, or 13 for the tidal TaylorF2 (LambdaTilde, deltaLambda)
-int npar_of(int model) { return model == GWF_WF_TAYLORF2_TIDAL ? 13 : 11; }
+int npar_of(int model) { return model >= GWF_WF_TAYLORF2_TIDAL ? 13 : 11; }
 
 int check_ctx(gwf_ctx* ctx) {
   if (!ctx) return fail(GWF_ERR_INVALID_ARG, "null context");
@@ -160,8 +160,9 @@ int validate_common(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_de
   if (!det_ids || n_det < 1) return fail(GWF_ERR_INVALID_ARG, "need at least one detector");
   for (int i = 0; i < n_det; ++i)
     if (det_ids[i] < 0 || det_ids[i] >= (int)ctx->dets.size()) return fail(GWF_ERR_INVALID_ARG, "unknown detector id");
-  if (!wf || wf->model < 0 || wf->model > 3) return fail(GWF_ERR_INVALID_ARG, "unknown waveform model");
-  if (wf->model == GWF_WF_PHENOMD && ctx->nq < 2) return fail(GWF_ERR_INVALID_ARG, "IMRPhenomD needs the QNM table (gwf_set_qnm_table)");
+  if (!wf || wf->model < 0 || wf->model > 4) return fail(GWF_ERR_INVALID_ARG, "unknown waveform model");
+  if ((wf->model == GWF_WF_PHENOMD || wf->model == GWF_WF_PHENOMD_NRTIDALV2) && ctx->nq < 2)
+    return fail(GWF_ERR_INVALID_ARG, "IMRPhenomD needs the QNM table (gwf_set_qnm_table)");
   if (!(wf->fcut_par > 0.0)) return fail(GWF_ERR_INVALID_ARG, "fcut_par must be positive");
   if (N < 0 || (N > 0 && !params)) return fail(GWF_ERR_INVALID_ARG, "bad event array");
   if (ld < N) return fail(GWF_ERR_INVALID_ARG, "ld must be >= n_events");
@@ -358,8 +359,8 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
     return fail(GWF_ERR_INVALID_ARG, "bad precision");
   if (precision != GWF_PREC_FP64 && wf->model == GWF_WF_PHENOMHM && !fisher)
     return fail(GWF_ERR_UNSUPPORTED, "the FP32 SNR is implemented for TaylorF2 and IMRPhenomD");
-  if (precision != GWF_PREC_FP64 && wf->model == GWF_WF_TAYLORF2_TIDAL)
-    return fail(GWF_ERR_UNSUPPORTED, "the tidal TaylorF2 is implemented in FP64");
+  if (precision != GWF_PREC_FP64 && wf->model >= GWF_WF_TAYLORF2_TIDAL)
+    return fail(GWF_ERR_UNSUPPORTED, "the tidal models are implemented in FP64");
   if (precision == GWF_PREC_MIXED && !fisher) return fail(GWF_ERR_INVALID_ARG, "the mixed form is a Fisher form");
   if (fisher && !per_arm) out_arm = nullptr;
   if (fisher && per_arm && !out_arm) return fail(GWF_ERR_INVALID_ARG, "per_arm needs out_arm");
@@ -468,7 +469,8 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   }
   const size_t stride = wf->model == 0 ? gwf::setup_stride_m0()
                         : (wf->model == 1 ? gwf::setup_stride_m1()
-                                          : (wf->model == 2 ? gwf::setup_stride_m2() : gwf::setup_stride_m3()));
+                                          : (wf->model == 2 ? gwf::setup_stride_m2()
+                                                            : (wf->model == 3 ? gwf::setup_stride_m3() : gwf::setup_stride_m4())));
   const size_t chunk = (size_t)(N < gwf::kChunk ? N : gwf::kChunk);
   // FP32 network totals: detectors with the same grid (fmin, fmax, Earth rotation) form groups
   // that one launch evaluates together (the waveform once per point for the whole group)
@@ -495,14 +497,15 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   // a network shares the source-dependent part of the per-event set-up between its detectors
   const size_t core_b = wf->model == 0 ? gwf::core_bytes_m0()
                         : (wf->model == 1 ? gwf::core_bytes_m1()
-                                          : (wf->model == 2 ? gwf::core_bytes_m2() : gwf::core_bytes_m3()));
+                                          : (wf->model == 2 ? gwf::core_bytes_m2()
+                                                            : (wf->model == 3 ? gwf::core_bytes_m3() : gwf::core_bytes_m4())));
   const bool share = n_det > 1 && ctx->core.ensure((size_t)N * core_b) == 0;
   // the scratch is shared by every call on this context: order this call after the previous one
   if (!capturing) GWF_CK(cudaStreamWaitEvent(st, ctx->scratch_free, 0));
   gwf::LaunchArgs a;
   a.scratch = (unsigned char*)ctx->setup.p;
   a.cap_events = (long long)chunk;
-  if (fisher && ctx->seg_points > 0 && wf->model != GWF_WF_TAYLORF2_TIDAL) {
+  if (fisher && ctx->seg_points > 0 && wf->model < GWF_WF_TAYLORF2_TIDAL) {
     int64_t rmax = 0;
     if (capturing && res_ev) rmax = ctx->graph_rmax;   // from the uncaptured run of the same call
     else rc = max_res(res, res_ev, N, mem, &rmax);
@@ -557,10 +560,14 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
     a.out_sd_det = dsdn;
     if (fisher)
       err = wf->model == 0 ? gwf::launch_fisher_m0(a)
-            : (wf->model == 1 ? gwf::launch_fisher_m1(a) : (wf->model == 2 ? gwf::launch_fisher_m2(a) : gwf::launch_fisher_m3(a)));
+            : (wf->model == 1 ? gwf::launch_fisher_m1(a)
+                              : (wf->model == 2 ? gwf::launch_fisher_m2(a)
+                                                : (wf->model == 3 ? gwf::launch_fisher_m3(a) : gwf::launch_fisher_m4(a))));
     else
       err = wf->model == 0 ? gwf::launch_snr_m0(a)
-            : (wf->model == 1 ? gwf::launch_snr_m1(a) : (wf->model == 2 ? gwf::launch_snr_m2(a) : gwf::launch_snr_m3(a)));
+            : (wf->model == 1 ? gwf::launch_snr_m1(a)
+                              : (wf->model == 2 ? gwf::launch_snr_m2(a)
+                                                : (wf->model == 3 ? gwf::launch_snr_m3(a) : gwf::launch_snr_m4(a))));
     if (err != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(err));
     slot += r.desc.shape == GWF_SHAPE_T ? 3 : 1;
   }
@@ -887,7 +894,7 @@ int gwf_strain_derivs(gwf_ctx* ctx, int det_id, const gwf_wf_desc* wf, const dou
   rc = validate_common(ctx, 1, &det_id, wf, params, ld, n_events, res, nullptr, spacing, mem);
   if (rc) return rc;
   if (!out) return fail(GWF_ERR_INVALID_ARG, "no output requested");
-  if (wf->model == GWF_WF_TAYLORF2_TIDAL) return fail(GWF_ERR_UNSUPPORTED, "strain derivatives are implemented for the 11-parameter models");
+  if (wf->model >= GWF_WF_TAYLORF2_TIDAL) return fail(GWF_ERR_UNSUPPORTED, "strain derivatives are implemented for the 11-parameter models");
   const int64_t N = n_events;
   if (N == 0) return GWF_OK;
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
@@ -961,7 +968,7 @@ int gwf_overlap(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* 
   if (!rc) rc = validate_common(ctx, n_det, det_ids, wf2, params2, ld2, n_events, res, nullptr, GWF_SPACING_GEOM, mem);
   if (rc) return rc;
   if (!out_ov || !out_n1 || !out_n2) return fail(GWF_ERR_INVALID_ARG, "overlap needs all three outputs");
-  if (wf1->model == GWF_WF_TAYLORF2_TIDAL || wf2->model == GWF_WF_TAYLORF2_TIDAL)
+  if (wf1->model >= GWF_WF_TAYLORF2_TIDAL || wf2->model >= GWF_WF_TAYLORF2_TIDAL)
     return fail(GWF_ERR_UNSUPPORTED, "the overlap is implemented for the 11-parameter models");
   const int64_t N = n_events;
   if (N == 0) return GWF_OK;

@@ -22,7 +22,11 @@ constexpr int NE = 66;    // upper-triangle entries
 enum { I_MC = 0, I_ETA, I_DL, I_TH, I_PH, I_IO, I_PS, I_TC, I_PC, I_C1, I_C2, I_LT, I_DLT };
 
 // Fisher parameters of a model, upper-triangle entries, entries plus strain products, entry index
-template <int MODEL> __host__ __device__ constexpr int np_of() { return MODEL == 3 ? 13 : 11; }
+template <int MODEL> __host__ __device__ constexpr int np_of() { return MODEL >= 3 ? 13 : 11; }
+// intrinsic tangent directions of the per-event duals: Mc, eta, chi1z, chi2z (+ LambdaTilde,
+// deltaLambda for IMRPhenomD_NRTidalv2, model 4, whose set-up depends on them non-linearly)
+template <int MODEL> __host__ __device__ constexpr int ndir_of() { return MODEL == 4 ? 6 : 4; }
+template <int MODEL> using DualOf = Dual<double, ndir_of<MODEL>()>;
 __host__ __device__ constexpr int ne_of(int npr) { return npr * (npr + 1) / 2; }
 __host__ __device__ constexpr int nex_of(int npr) { return ne_of(npr) + npr; }
 __host__ __device__ constexpr int pidx_n(int npr, int a, int b) { return a * npr - a * (a - 1) / 2 + (b - a); }
@@ -202,6 +206,7 @@ __device__ __forceinline__ void arm_pattern(const ProjEv& pj, double sz, double 
 // strain derivatives of one arm, without the common phase factor.
 // hp = P, hc = i C; dP[k], dC[k] are the intrinsic tangents (k = Mc, eta, chi1, chi2),
 // dPi/dCi the iota derivatives; dtn[k] = d t_noloc / d theta_k (days).
+template <int NI = 4>
 __device__ __forceinline__ void arm_derivs(const ProjEv& pj, const ArmPat& ap, const TimeState& ts, double f,
                                            cd P, cd C, const cd* dP, const cd* dC, cd dPi, cd dCi,
                                            const double* dtn, cd* out) {
@@ -216,9 +221,9 @@ __device__ __forceinline__ void arm_derivs(const ProjEv& pj, const ArmPat& ap, c
   const double x_tc = -kTwoPi * G;
   const cd hx = cadd(cscale(hp, ap.Fp_x), cscale(hc, ap.Fc_x)); // d(h)/dx at fixed waveform
   const cd hd = cadd(cscale(hp, ap.Fp_d), cscale(hc, ap.Fc_d)); // d(h)/d(dec)
-  const int map[4] = {I_MC, I_ETA, I_C1, I_C2};
+  const int map[6] = {I_MC, I_ETA, I_C1, I_C2, I_LT, I_DLT};
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < NI; ++k) {
     cd v = cadd(cscale(cmuli(dC[k]), ap.Fc), cscale(dP[k], ap.Fp));
     if (dtn[k] != 0.0) {
       v = cadd(v, cscale(hx, -kTwoPi * G * dtn[k]));
@@ -241,6 +246,7 @@ union EvUnion {
   PhdEv phd;
   HMEv hm;
   TF2TEv tf2t;
+  NRTEv nrt;
 };
 
 // upper grid frequency of the model (gwfast/waveforms.py:903-920, :1324-1333, :2737-2750)
@@ -250,8 +256,8 @@ __host__ __device__ inline double model_fcut(const WfDesc& wf, double Mc, double
 }
 
 __device__ inline bool grid_setup(GridEv& g, const DetDev& d, const EvBatch& ev, const WfDesc& wf, long long n,
-                                  double Mc, double eta) {
-  double fcut = model_fcut(wf, Mc, eta);
+                                  double Mc, double eta, double fcut_model = -1.0) {
+  double fcut = fcut_model >= 0.0 ? fcut_model : model_fcut(wf, Mc, eta);
   if (d.fmax > 0.0 && fcut > d.fmax) fcut = d.fmax;
   if (ev.fcut_ev) fcut = ev.fcut_ev[n];
   const int R = ev.res_ev ? ev.res_ev[n] : ev.res;
@@ -293,6 +299,11 @@ __device__ inline void event_setup(EvUnion& E, const DetDev& d, const WfDesc& wf
                                    double Mc, double eta, double chi1, double chi2, double dL, double lam_t,
                                    double del_lam) {
   const D4 mc = D4::seed(Mc, P_MC), et = D4::seed(eta, P_ETA), c1 = D4::seed(chi1, P_CHI1), c2 = D4::seed(chi2, P_CHI2);
+  if (MODEL == 4) {
+    nrt_setup(E.nrt, D6::seed(Mc, P_MC), D6::seed(eta, P_ETA), D6::seed(chi1, P_CHI1), D6::seed(chi2, P_CHI2), dL,
+              d.fmin, q, q + nq, q + 2 * nq, nq, D6::seed(lam_t, P_LT), D6::seed(del_lam, P_DLT));
+    return;
+  }
   if (MODEL == 3) tf2t_setup(E.tf2t, mc, et, c1, c2, dL, wf.spin_ho != 0, lam_t, del_lam);
   else if (MODEL == 0) tf2_setup(E.tf2, mc, et, c1, c2, dL, wf.spin_ho != 0);
   else if (MODEL == 1) phd_setup(E.phd, mc, et, c1, c2, dL, d.fmin, q, q + nq, q + 2 * nq, nq);
@@ -306,10 +317,11 @@ constexpr double kTF2PhaseConst = 0.75 * kPi;
 // phi0: the waveform phase left out of P and C (22-mode models: Phi(f); HM: 0, the mode phases are in P, C)
 template <int MODEL, bool EARTH>
 __device__ __forceinline__ void wave_point_dual(const EvUnion& E, const ProjEv& pj, double f, double lnf,
-                                                cd& P, cd& C, cd* dP, cd* dC, cd& dPi, cd& dCi, D4& tau,
+                                                cd& P, cd& C, cd* dP, cd* dC, cd& dPi, cd& dCi, DualOf<MODEL>& tau,
                                                 double& phi0) {
+  constexpr int NI = ndir_of<MODEL>();
   phi0 = 0.0;
-  if (MODEL == 2) {
+  if constexpr (MODEL == 2) {
     Cplx<D4> Pd, Cd;
     Cplx<double> dPv, dCv;
     hm_point<D4>(E.hm, f, Pd, Cd, dPv, dCv);
@@ -318,6 +330,21 @@ __device__ __forceinline__ void wave_point_dual(const EvUnion& E, const ProjEv& 
     for (int k = 0; k < 4; ++k) { dP[k] = {Pd.re.d[k], Pd.im.d[k]}; dC[k] = {Cd.re.d[k], Cd.im.d[k]}; }
     dPi = {dPv.re, dPv.im}; dCi = {dCv.re, dCv.im};
     if (EARTH) tau = tau_star_point<D4>(E.hm.k.Ms, E.hm.k.vM, E.hm.k.eta, exp(lnf / 3.0));
+  } else if constexpr (MODEL == 4) {
+    D6 A, Phi;
+    nrt_point<D6>(E.nrt, f, A, Phi);
+    if (EARTH) tau = tau_star_point<D6>(E.nrt.k.Ms, E.nrt.k.vM, E.nrt.k.eta, exp(lnf / 3.0));
+    phi0 = Phi.v;
+    P = {pj.cp * A.v, 0.0};
+    C = {pj.ci * A.v, 0.0};
+#pragma unroll
+    for (int k = 0; k < NI; ++k) {
+      const cd dW = {A.d[k], -A.v * Phi.d[k]};
+      dP[k] = cscale(dW, pj.cp);
+      dC[k] = cscale(dW, pj.ci);
+    }
+    dPi = {pj.dcp * A.v, 0.0};
+    dCi = {pj.dci * A.v, 0.0};
   } else {
     D4 A, Phi;
     if (MODEL == 0 || MODEL == 3) {
@@ -358,7 +385,10 @@ __device__ __forceinline__ void wave_point_full(const EvUnion& E, const ProjEv& 
     if (EARTH) tau = tau_star_point<double>(E.hm.k.Ms, E.hm.k.vM, E.hm.k.eta, exp(lnf / 3.0));
   } else {
     double A, Phi;
-    if (MODEL == 0 || MODEL == 3) {
+    if (MODEL == 4) {
+      nrt_point<double>(E.nrt, f, A, Phi);
+      if (EARTH) tau = tau_star_point<double>(E.nrt.k.Ms, E.nrt.k.vM, E.nrt.k.eta, exp(lnf / 3.0));
+    } else if (MODEL == 0 || MODEL == 3) {
       const TF2Ev& t = MODEL == 3 ? E.tf2t.b : E.tf2;
       const double f13 = exp(lnf / 3.0);
       tf2_point<double>(t, f, f13, lnf, exp(lnf * (-7.0 / 6.0)), A, Phi);
@@ -386,7 +416,10 @@ __device__ __forceinline__ void wave_point_val(const EvUnion& E, const ProjEv& p
     if (EARTH) tau = tau_star_point<double>(E.hm.k.Ms, E.hm.k.vM, E.hm.k.eta, exp(lnf / 3.0));
   } else {
     double A, Phi;
-    if (MODEL == 0 || MODEL == 3) {
+    if (MODEL == 4) {
+      nrt_point<double>(E.nrt, f, A, Phi);
+      if (EARTH) tau = tau_star_point<double>(E.nrt.k.Ms, E.nrt.k.vM, E.nrt.k.eta, exp(lnf / 3.0));
+    } else if (MODEL == 0 || MODEL == 3) {
       const TF2Ev& t = MODEL == 3 ? E.tf2t.b : E.tf2;
       const double f13 = exp(lnf / 3.0);
       tf2_point<double>(t, f, f13, lnf, exp(lnf * (-7.0 / 6.0)), A, Phi);
@@ -411,7 +444,8 @@ struct SetupHdr {
 
 template <int MODEL>
 __host__ __device__ constexpr size_t wave_bytes() {
-  return MODEL == 0 ? sizeof(TF2Ev) : (MODEL == 1 ? sizeof(PhdEv) : (MODEL == 2 ? sizeof(HMEv) : sizeof(TF2TEv)));
+  return MODEL == 0 ? sizeof(TF2Ev)
+                    : (MODEL == 1 ? sizeof(PhdEv) : (MODEL == 2 ? sizeof(HMEv) : (MODEL == 3 ? sizeof(TF2TEv) : sizeof(NRTEv))));
 }
 // the 22-mode models also carry the phase-tangent basis used by the FP32 kernel
 template <int MODEL>
@@ -446,8 +480,9 @@ __global__ void __launch_bounds__(64) setup_kernel(EvBatch ev, DetDev det, WfDes
   const double Mc = p[0 * ld + n], eta = p[1 * ld + n], dL = p[2 * ld + n];
   const double th = p[3 * ld + n], ph = p[4 * ld + n], io = p[5 * ld + n], ps = p[6 * ld + n];
   const double tc = p[7 * ld + n], c1 = p[9 * ld + n], c2 = p[10 * ld + n];
-  const double lt = MODEL == 3 ? p[11 * ld + n] : 0.0, dlt = MODEL == 3 ? p[12 * ld + n] : 0.0;
-  if (grid_setup(h.g, det, ev, wf, n, Mc, eta)) {
+  const double lt = MODEL >= 3 ? p[11 * ld + n] : 0.0, dlt = MODEL >= 3 ? p[12 * ld + n] : 0.0;
+  // IMRPhenomD_NRTidalv2 ends at 1.2 times its merger frequency, which depends on the deformabilities
+  if (grid_setup(h.g, det, ev, wf, n, Mc, eta, MODEL == 4 ? nrt_fcut(Mc, eta, lt, dlt) : -1.0)) {
     constexpr int nw = (int)(wave_bytes<MODEL>() / 8);
     const long long crow = core_idx ? core_idx[n] : n;   // a gathered batch reads the rows of its events
     unsigned long long* cw = core ? reinterpret_cast<unsigned long long*>(core + (size_t)crow * wave_bytes<MODEL>()) : nullptr;
@@ -456,6 +491,7 @@ __global__ void __launch_bounds__(64) setup_kernel(EvBatch ev, DetDev det, WfDes
       for (int w = 0; w < nw; ++w) ew[w] = cw[w];
       if (MODEL == 1) phd_ref(E.phd, det.fmin);
       if (MODEL == 2) hm_ref(E.hm, det.fmin);
+      if (MODEL == 4) nrt_ref(E.nrt, det.fmin);
     } else {
       event_setup<MODEL>(E, det, wf, qnm, nq, Mc, eta, c1, c2, dL, lt, dlt);
       if (MODEL == 2)
@@ -639,16 +675,19 @@ __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<N
       grid_point(S.g, ev.spacing, k, f, lnf, w);
       const double Sn = psd_at(det, f, lnf);
       sw = sqrt(4.0 * w / Sn);
-      cd P, C, dP[4], dC[4], dPi, dCi;
-      D4 tau(0.0);
+      constexpr int NI = ndir_of<MODEL>();
+      cd P, C, dP[NI], dC[NI], dPi, dCi;
+      DualOf<MODEL> tau(0.0);
       double phi0;
       wave_point_dual<MODEL, EARTH>(S.E, S.pj, f, lnf, P, C, dP, dC, dPi, dCi, tau, phi0);
-      double dtn[4] = {0.0, 0.0, 0.0, 0.0};
+      double dtn[NI];
+#pragma unroll
+      for (int q = 0; q < NI; ++q) dtn[q] = 0.0;
       TimeState ts;
       if (EARTH) {
         const double tn = S.pj.tc - tau.v / kDay;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) dtn[q] = -tau.d[q] / kDay;
+        for (int q = 0; q < NI; ++q) dtn[q] = -tau.d[q] / kDay;
         time_state(S.pj, tn, ts);
       } else {
         ts = S.tsc;
@@ -666,7 +705,7 @@ __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<N
         ArmPat ap;
         if (EARTH) arm_pattern(S.pj, det.sin_zeta, ts.x, a, ap);
         else ap = S.apc[a];
-        arm_derivs(S.pj, ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D[a]);
+        arm_derivs<NI>(S.pj, ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D[a]);
         const cd H = cadd(cscale(P, ap.Fp), cscale(cmuli(C), ap.Fc));
         if (MODEL == 3) {   // h ~ e^{-i Phi}: d h / d Lambda = -i h d Phi / d Lambda
           D[a][NPS - 3] = cscale(cmuli(H), -dphl);

@@ -48,6 +48,10 @@ cudaError_t launch_fisher_m3(const LaunchArgs& a);   // tidal TaylorF2: FP64, 13
 cudaError_t launch_snr_m3(const LaunchArgs& a);
 size_t setup_stride_m3();
 size_t core_bytes_m3();
+cudaError_t launch_fisher_m4(const LaunchArgs& a);   // IMRPhenomD_NRTidalv2: FP64, 13 parameters
+cudaError_t launch_snr_m4(const LaunchArgs& a);
+size_t setup_stride_m4();
+size_t core_bytes_m4();
 // strain tangent / strain / overlap outputs (gwf_wave_out.cuh): set-up and output launch for
 // events [o.n0, o.n0 + o.cnt) of a.ev; a.scratch holds at least o.cnt records
 cudaError_t launch_wave_m0(const LaunchArgs& a, const WaveOut& o);

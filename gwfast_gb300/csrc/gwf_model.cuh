@@ -12,17 +12,20 @@
 namespace gwf {
 
 using D4 = Dual<double, 4>;
-enum { P_MC = 0, P_ETA = 1, P_CHI1 = 2, P_CHI2 = 3 };
+enum { P_MC = 0, P_ETA = 1, P_CHI1 = 2, P_CHI2 = 3, P_LT = 4, P_DLT = 5 };   // tangent slots (4, 5: tidal model)
+using D6 = Dual<double, 6>;   // IMRPhenomD_NRTidalv2: the tidal parameters enter the set-up non-linearly
 
 // coefficient access: per-event coefficients are stored as duals (D4 for FP64, DF4 for FP32);
 // a per-point scalar S of matching precision reads either the full dual or its value.
 using DF4 = Dual<float, 4>;
 template <class S, class C> struct CoT;
-template <> struct CoT<double, D4> { __device__ __forceinline__ static double get(const D4& c) { return c.v; } };
+template <class U, int N> struct CoT<U, Dual<U, N>> {
+  __device__ __forceinline__ static U get(const Dual<U, N>& c) { return c.v; }
+};
+template <class U, int N> struct CoT<Dual<U, N>, Dual<U, N>> {
+  __device__ __forceinline__ static Dual<U, N> get(const Dual<U, N>& c) { return c; }
+};
 template <> struct CoT<double, double> { __device__ __forceinline__ static double get(double c) { return c; } };
-template <> struct CoT<D4, D4> { __device__ __forceinline__ static D4 get(const D4& c) { return c; } };
-template <> struct CoT<float, DF4> { __device__ __forceinline__ static float get(const DF4& c) { return c.v; } };
-template <> struct CoT<DF4, DF4> { __device__ __forceinline__ static DF4 get(const DF4& c) { return c; } };
 template <class S, class C> __device__ __forceinline__ S co(const C& c) { return CoT<S, C>::get(c); }
 
 template <class S> struct Real;
@@ -30,47 +33,56 @@ template <> struct Real<double> { typedef double T; };
 template <> struct Real<float> { typedef float T; };
 template <class U, int N> struct Real<Dual<U, N>> { typedef U T; };
 
-__device__ __forceinline__ D4 seta_of(const D4& eta) {
+template <class D>
+__device__ __forceinline__ D seta_of(const D& eta) {
   // sqrt(1-4 eta) guarded at equal mass (gwfast/waveforms.py:759)
-  return eta.v < 0.25 ? dsqrt(1.0 - 4.0 * eta) : D4(0.0);
+  return eta.v < 0.25 ? dsqrt(1.0 - 4.0 * eta) : D(0.0);
 }
 
 // ------------------------------------------------------------------ PN phase coefficients
 template <class C> struct PNCT { C A, c2, c3, c4, c5, c5l, c6, c6l, c7; };
 using PNC = PNCT<D4>;
 
-// TaylorF2 coefficients, gwfast/waveforms.py:784-812 (QuadMon = 1); drop_ss removes the 3PN
-// spin-spin part as IMRPhenomD does (gwfast/waveforms.py:1077).
-__device__ inline PNC pn_coeffs(const D4& eta, const D4& chi1, const D4& chi2, bool spin_ho, bool drop_ss) {
-  const D4 seta = seta_of(eta);
-  const D4 m1 = 0.5 * (1.0 + seta), m2 = 0.5 * (1.0 - seta);
-  const D4 chis = 0.5 * (chi1 + chi2), chia = 0.5 * (chi1 - chi2);
-  const D4 eta2 = eta * eta;
-  PNC c;
+// TaylorF2 coefficients, gwfast/waveforms.py:784-812; drop_ss removes the 3PN spin-spin part as
+// IMRPhenomD does (gwfast/waveforms.py:1077). dq1, dq2: spin-induced quadrupole moments minus 1
+// (zero for black holes), as IMRPhenomD_NRTidalv2 uses them (gwfast/waveforms.py:1461-1467).
+template <class D>
+__device__ inline PNCT<D> pn_coeffs(const D& eta, const D& chi1, const D& chi2, bool spin_ho, bool drop_ss,
+                                    const D& dq1 = D(0.0), const D& dq2 = D(0.0)) {
+  const D seta = seta_of(eta);
+  const D m1 = 0.5 * (1.0 + seta), m2 = 0.5 * (1.0 - seta);
+  const D chis = 0.5 * (chi1 + chi2), chia = 0.5 * (chi1 - chi2);
+  const D eta2 = eta * eta;
+  PNCT<D> c;
   c.A = 3.0 / (128.0 * eta);
   c.c2 = 3715. / 756. + 55. / 9. * eta;
   c.c3 = -16. * kPi + (113. / 3.) * seta * chia + (113. / 3. - 76. / 3. * eta) * chis;
-  const D4 m1s = m1 * m1 * chi1 * chi1, m2s = m2 * m2 * chi2 * chi2;
+  const D m1s = m1 * m1 * chi1 * chi1, m2s = m2 * m2 * chi2 * chi2;
   c.c4 = 5. / 72. * (3058.673 / 7.056 + 5429. / 7. * eta + 617. * eta2) + ((247. - 721.) / 4.8) * eta * chi1 * chi2
          + ((-720. + 1. + 240. - 7.) / 9.6) * (m1s + m2s);
-  const D4 t5 = (732985. / 2268. - 24260. / 81. * eta - 340. / 9. * eta2) * chis
+  // spin-induced quadrupole moments QuadMon_i = 1 + dq_i (tidal models, gwfast/waveforms.py:1461)
+  c.c4 = c.c4 - 50.0 * (dq1 * m1s + dq2 * m2s);
+  const D t5 = (732985. / 2268. - 24260. / 81. * eta - 340. / 9. * eta2) * chis
                 + (732985. / 2268. + 140. / 9. * eta) * seta * chia;
   c.c5 = 38645. * kPi / 756. - 65. * kPi / 9. * eta - t5;
   c.c5l = 3.0 * c.c5;
-  D4 six = 11583.231236531 / 4.694215680 - 640. / 3. * kPi * kPi - 684.8 / 2.1 * kEulerGamma
+  D six = 11583.231236531 / 4.694215680 - 640. / 3. * kPi * kPi - 684.8 / 2.1 * kEulerGamma
            + (-15737.765635 / 3.048192 + 225.5 / 1.2 * kPi * kPi) * eta + 76.055 / 1.728 * eta2
            - 127.825 / 1.296 * eta2 * eta - log(4.0) * (684.8 / 2.1)
            + kPi * chi1 * m1 * (1490. / 3. + 260. * m1) + kPi * chi2 * m2 * (1490. / 3. + 260. * m2);
+  if (drop_ss)   // the quadrupole excess of the 3PN spin-spin terms (:1464-1467; zero for black holes)
+    six = six + (4703.5 / 8.4 + 2935. / 6. * m1 - 120. * m1 * m1) * m1s * dq1
+              + (4703.5 / 8.4 + 2935. / 6. * m2 - 120. * m2 * m2) * m2s * dq2;
   if (!drop_ss) {
-    const D4 ss1 = (4703.5 / 8.4 - 4108.25 / 6.72) + (2935. / 6. - 108.5 / 1.2) * m1 + (125.5 / 3.6 - 120.) * m1 * m1;
-    const D4 ss2 = (4703.5 / 8.4 - 4108.25 / 6.72) + (2935. / 6. - 108.5 / 1.2) * m2 + (125.5 / 3.6 - 120.) * m2 * m2;
+    const D ss1 = (4703.5 / 8.4 - 4108.25 / 6.72) + (2935. / 6. - 108.5 / 1.2) * m1 + (125.5 / 3.6 - 120.) * m1 * m1;
+    const D ss2 = (4703.5 / 8.4 - 4108.25 / 6.72) + (2935. / 6. - 108.5 / 1.2) * m2 + (125.5 / 3.6 - 120.) * m2 * m2;
     six = six + (326.75 / 1.12 + 557.5 / 1.8 * eta) * eta * chi1 * chi2 + ss1 * m1s + ss2 * m2s;
   }
   c.c6 = six;
-  c.c6l = D4(-6848. / 21.);
-  D4 sev = 77096675. * kPi / 254016. + 378515. * kPi / 1512. * eta - 74045. * kPi / 756. * eta2;
-  D4 cs = -25150083775. / 3048192. + 10566655595. / 762048. * eta - 1042165. / 3024. * eta2 + 5345. / 36. * eta2 * eta;
-  D4 ca = -25150083775. / 3048192. + 26804935. / 6048. * eta - 1985. / 48. * eta2;
+  c.c6l = D(-6848. / 21.);
+  D sev = 77096675. * kPi / 254016. + 378515. * kPi / 1512. * eta - 74045. * kPi / 756. * eta2;
+  D cs = -25150083775. / 3048192. + 10566655595. / 762048. * eta - 1042165. / 3024. * eta2 + 5345. / 36. * eta2 * eta;
+  D ca = -25150083775. / 3048192. + 26804935. / 6048. * eta - 1985. / 48. * eta2;
   if (spin_ho) {
     cs = cs + (14585. / 8. - 7270. * eta + 80. * eta2) * chia * chia;
     sev = sev + (14585. / 24. - 475. / 6. * eta + 100. / 3. * eta2) * chis * chis * chis
@@ -180,29 +192,32 @@ template <class C> struct PhdCoreT {
 };
 using PhdCore = PhdCoreT<D4>;
 
-__device__ __forceinline__ D4 fit11(int k, const D4& eta, const D4& xi) {
+template <class D>
+__device__ __forceinline__ D fit11(int k, const D& eta, const D& xi) {
   const double* c = kFits[k];
-  const D4 e2 = eta * eta;
+  const D e2 = eta * eta;
   return c[0] + c[1] * eta + (c[2] + c[3] * eta + c[4] * e2 + (c[5] + c[6] * eta + c[7] * e2) * xi
                               + (c[8] + c[9] * eta + c[10] * e2) * xi * xi) * xi;
 }
 
 // final spin (gwfast/waveforms.py:1256-1276) and radiated energy (:1278-1297)
-__device__ inline D4 final_spin(const D4& eta, const D4& chi1, const D4& chi2) {
-  const D4 seta = seta_of(eta);
-  const D4 m1 = 0.5 * (1.0 + seta), m2 = 0.5 * (1.0 - seta);
-  const D4 s = m1 * m1 * chi1 + m2 * m2 * chi2;
-  const D4 e2 = eta * eta;
+template <class D>
+__device__ inline D final_spin(const D& eta, const D& chi1, const D& chi2) {
+  const D seta = seta_of(eta);
+  const D m1 = 0.5 * (1.0 + seta), m2 = 0.5 * (1.0 - seta);
+  const D s = m1 * m1 * chi1 + m2 * m2 * chi2;
+  const D e2 = eta * eta;
   return eta * (3.4641016151377544 - 4.399247300629289 * eta + 9.397292189321194 * e2 - 13.180949901606242 * e2 * eta)
          + eta * (s * ((1.0 / eta - 0.0850917821418767 - 5.837029316602263 * eta) + (0.1014665242971878 - 2.0967746996832157 * eta) * s))
          + eta * (s * ((-1.3546806617824356 + 4.108962025369336 * eta) * s * s + (-0.8676969352555539 + 2.064046835273906 * eta) * s * s * s));
 }
-__device__ inline D4 radiated_energy(const D4& eta, const D4& chi1, const D4& chi2) {
-  const D4 seta = seta_of(eta);
-  const D4 m1 = 0.5 * (1.0 + seta), m2 = 0.5 * (1.0 - seta);
-  const D4 s = (m1 * m1 * chi1 + m2 * m2 * chi2) / (m1 * m1 + m2 * m2);
-  const D4 e2 = eta * eta;
-  const D4 ens = eta * (0.055974469826360077 + 0.5809510763115132 * eta - 0.9606726679372312 * e2 + 3.352411249771192 * e2 * eta);
+template <class D>
+__device__ inline D radiated_energy(const D& eta, const D& chi1, const D& chi2) {
+  const D seta = seta_of(eta);
+  const D m1 = 0.5 * (1.0 + seta), m2 = 0.5 * (1.0 - seta);
+  const D s = (m1 * m1 * chi1 + m2 * m2 * chi2) / (m1 * m1 + m2 * m2);
+  const D e2 = eta * eta;
+  const D ens = eta * (0.055974469826360077 + 0.5809510763115132 * eta - 0.9606726679372312 * e2 + 3.352411249771192 * e2 * eta);
   return ens * (1. + (-0.0030302335878845507 - 2.0066110851351073 * eta + 7.7050567802399215 * e2) * s)
          / (1. + (-0.6714403054720589 - 1.4756929437702908 * eta + 7.304676214885011 * e2) * s);
 }
@@ -280,22 +295,23 @@ __device__ __forceinline__ S complete_amp_shape(const PhdCoreT<C>& k, const S& x
 }
 
 // ---- per-event setup of the IMRPhenomD core given fring, fdamp
-__device__ inline void phenom_core_setup(PhdCore& k, const D4& Mc, const D4& eta, const D4& chi1, const D4& chi2,
-                                         const D4& fring, const D4& fdamp) {
+template <class D>
+__device__ inline void phenom_core_setup(PhdCoreT<D>& k, const D& Mc, const D& eta, const D& chi1, const D& chi2,
+                                         const D& fring, const D& fdamp, const D& dq1 = D(0.0), const D& dq2 = D(0.0)) {
   k.eta = eta;
   k.MG = Mc * kG3 / dpowc(eta, 0.6);
   k.Ms = k.MG;
   k.vM = dcbrt(kPi * k.MG);
   k.fring = fring;
   k.fdamp = fdamp;
-  const D4 seta = seta_of(eta);
-  const D4 chis = 0.5 * (chi1 + chi2), chia = 0.5 * (chi1 - chi2);
-  const D4 xi = chis * (1.0 - eta * (76.0 / 113.0)) + seta * chia - 1.0;
+  const D seta = seta_of(eta);
+  const D chis = 0.5 * (chi1 + chi2), chia = 0.5 * (chi1 - chi2);
+  const D xi = chis * (1.0 - eta * (76.0 / 113.0)) + seta * chia - 1.0;
   for (int i = 0; i < 4; ++i) k.sig[i] = fit11(FIT_SIGMA1 + i, eta, xi);
   for (int i = 0; i < 3; ++i) k.bet[i] = fit11(FIT_BETA1 + i, eta, xi);
   for (int i = 0; i < 5; ++i) k.alp[i] = fit11(FIT_ALPHA1 + i, eta, xi);
   for (int i = 0; i < 3; ++i) k.gam[i] = fit11(FIT_GAMMA1 + i, eta, xi);
-  k.pn = pn_coeffs(eta, chi1, chi2, false, true);
+  k.pn = pn_coeffs(eta, chi1, chi2, false, true, dq1, dq2);
   // inspiral -> intermediate C1 join at Mf = 0.018 (gwfast/waveforms.py:1098-1120)
   {
     const double fj = kPhiFJoin;
@@ -303,33 +319,33 @@ __device__ inline void phenom_core_setup(PhdCore& k, const D4& Mc, const D4& eta
     const double x13 = cbrt(x);
     const double lx = log(x) / 3.0;
     // d/dMf of the inspiral phase
-    const D4 dtf2 = (-5. / 3.) * pow(x, -8. / 3.) - k.pn.c2 / (x * x) - (2. / 3.) * k.pn.c3 * pow(x, -5. / 3.)
+    const D dtf2 = (-5. / 3.) * pow(x, -8. / 3.) - k.pn.c2 / (x * x) - (2. / 3.) * k.pn.c3 * pow(x, -5. / 3.)
                     - (1. / 3.) * k.pn.c4 * pow(x, -4. / 3.) + k.pn.c5l / (3. * x) + k.pn.c6l * (x13 / (3. * x))
                     + (k.pn.c6 + k.pn.c6l * lx) * (x13 / (3. * x)) + (2. / 3.) * k.pn.c7 * (x13 * x13 / x);
-    const D4 dins = k.pn.A * dtf2 * kPi + (k.sig[0] + k.sig[1] * cbrt(fj) + k.sig[2] * cbrt(fj) * cbrt(fj) + k.sig[3] * fj) / eta;
-    const D4 dint = (k.bet[0] + k.bet[2] / (fj * fj * fj * fj) + k.bet[1] / fj) / eta;
+    const D dins = k.pn.A * dtf2 * kPi + (k.sig[0] + k.sig[1] * cbrt(fj) + k.sig[2] * cbrt(fj) * cbrt(fj) + k.sig[3] * fj) / eta;
+    const D dint = (k.bet[0] + k.bet[2] / (fj * fj * fj * fj) + k.bet[1] / fj) / eta;
     k.C2Int = dins - dint;
-    const D4 xj(fj);
-    const D4 insj = ins_phase<D4>(k, xj);
-    k.C1Int = insj - int_phase_raw<D4>(k, xj) - k.C2Int * fj;
+    const D xj(fj);
+    const D insj = ins_phase<D>(k, xj);
+    k.C1Int = insj - int_phase_raw<D>(k, xj) - k.C2Int * fj;
   }
   // intermediate -> merger-ringdown at 0.5 fring (gwfast/waveforms.py:1122-1129)
   k.fMRD = 0.5 * fring;
   {
-    const D4& fm = k.fMRD;
-    k.PhiIntTemp = int_phase_raw<D4>(k, fm) + k.C1Int + k.C2Int * fm;
+    const D& fm = k.fMRD;
+    k.PhiIntTemp = int_phase_raw<D>(k, fm) + k.C1Int + k.C2Int * fm;
     k.DPhiIntTemp = k.C2Int + (k.bet[0] + k.bet[2] / (fm * fm * fm * fm) + k.bet[1] / fm) / eta;
-    const D4 one(1.0);
-    const D4 u = (fm - k.alp[4] * fring) / fdamp;
-    const D4 dmrd = (k.alp[0] + k.alp[1] / (fm * fm) + k.alp[2] / dsqrt(dsqrt(fm)) + k.alp[3] / (fdamp * (1.0 + u * u))) / eta;
+    const D one(1.0);
+    const D u = (fm - k.alp[4] * fring) / fdamp;
+    const D dmrd = (k.alp[0] + k.alp[1] / (fm * fm) + k.alp[2] / dsqrt(dsqrt(fm)) + k.alp[3] / (fdamp * (1.0 + u * u))) / eta;
     k.C2MRD = k.DPhiIntTemp - dmrd;
-    k.C1MRD = k.PhiIntTemp - mrd_phase_raw<D4>(k, fm, one, one) - k.C2MRD * fm;
+    k.C1MRD = k.PhiIntTemp - mrd_phase_raw<D>(k, fm, one, one) - k.C2MRD * fm;
   }
   // amplitude (gwfast/waveforms.py:1189-1245)
   {
-    const D4 sp1 = 1.0 + seta;
-    const D4 e2 = eta * eta;
-    const D4 c12 = chi1 * chi1, c22 = chi2 * chi2;
+    const D sp1 = 1.0 + seta;
+    const D e2 = eta * eta;
+    const D c12 = chi1 * chi1, c22 = chi2 * chi2;
     k.a23 = (-969. + 1804. * eta) * (pow(kPi, 2.0 / 3.0) / 672.);
     k.a1 = (chi1 * (81. * sp1 - 44. * eta) + chi2 * (81. - 81. * seta - 44. * eta)) * (kPi / 48.);
     k.a43 = (-27312085.0 - 10287648. * c22 - 10287648. * c12 * sp1 + 10287648. * c22 * seta
@@ -349,34 +365,34 @@ __device__ inline void phenom_core_setup(PhdCore& k, const D4& Mc, const D4& eta
     k.r1 = fit11(FIT_RHO1, eta, xi);
     k.r2 = fit11(FIT_RHO2, eta, xi);
     k.r3 = fit11(FIT_RHO3, eta, xi);
-    const D4& g1 = k.gam[0];
-    const D4& g2 = k.gam[1];
-    const D4& g3 = k.gam[2];
+    const D& g1 = k.gam[0];
+    const D& g2 = k.gam[1];
+    const D& g3 = k.gam[2];
     k.fpA = (g2.v >= 1.0) ? dabs(fring - fdamp * g3 / g2)
                           : fring + fdamp * (dsqrt(1.0 - g2 * g2) - 1.0) * g3 / g2;
     // collocation data: value and slope of the inspiral at f1, value v2 at f2, value and slope of the ringdown at f3
     const double f1 = kAmpFJoin;
-    const D4 f3 = k.fpA;
-    const D4 f2 = f1 + 0.5 * (f3 - f1);
+    const D f3 = k.fpA;
+    const D f2 = f1 + 0.5 * (f3 - f1);
     k.f2 = f2;
-    const D4 v1 = ins_amp<D4>(k, D4(f1));
+    const D v1 = ins_amp<D>(k, D(f1));
     const double f113 = cbrt(f1);
-    const D4 d1 = (2. / 3.) * k.a23 / f113 + k.a1 + (4. / 3.) * k.a43 * f113 + (5. / 3.) * k.a53 * f113 * f113 + 2. * k.a2 * f1
+    const D d1 = (2. / 3.) * k.a23 / f113 + k.a1 + (4. / 3.) * k.a43 * f113 + (5. / 3.) * k.a53 * f113 * f113 + 2. * k.a2 * f1
                   + (7. / 3.) * k.r1 * f1 * f113 + (8. / 3.) * k.r2 * f1 * f113 * f113 + 3. * k.r3 * f1 * f1;
-    const D4 v2 = fit11(FIT_V2, eta, xi);
-    const D4 v3 = mrd_amp<D4>(k, f3);
-    const D4 fdg3 = fdamp * g3;
-    const D4 dx3 = f3 - fring;
-    const D4 den3 = dx3 * dx3 + fdg3 * fdg3;
-    const D4 d2 = (-2.0 * fdamp * dx3 * g3 * g1 / den3 - g2 * g1) / (dexp(dx3 * g2 / fdg3) * den3);
+    const D v2 = fit11(FIT_V2, eta, xi);
+    const D v3 = mrd_amp<D>(k, f3);
+    const D fdg3 = fdamp * g3;
+    const D dx3 = f3 - fring;
+    const D den3 = dx3 * dx3 + fdg3 * fdg3;
+    const D d2 = (-2.0 * fdamp * dx3 * g3 * g1 / den3 - g2 * g1) / (dexp(dx3 * g2 / fdg3) * den3);
     // divided differences over the nodes (f1, f1, f2, f3, f3)
-    const D4 q12 = (v2 - v1) / (f2 - f1);
-    const D4 q23 = (v3 - v2) / (f3 - f2);
-    const D4 q012 = (q12 - d1) / (f2 - f1);
-    const D4 q123 = (q23 - q12) / (f3 - f1);
-    const D4 q234 = (d2 - q23) / (f3 - f2);
-    const D4 q0123 = (q123 - q012) / (f3 - f1);
-    const D4 q1234 = (q234 - q123) / (f3 - f1);
+    const D q12 = (v2 - v1) / (f2 - f1);
+    const D q23 = (v3 - v2) / (f3 - f2);
+    const D q012 = (q12 - d1) / (f2 - f1);
+    const D q123 = (q23 - q12) / (f3 - f1);
+    const D q234 = (d2 - q23) / (f3 - f2);
+    const D q0123 = (q123 - q012) / (f3 - f1);
+    const D q1234 = (q234 - q123) / (f3 - f1);
     k.h0 = v1;
     k.h1 = d1;
     k.h2 = q012;
@@ -386,20 +402,22 @@ __device__ inline void phenom_core_setup(PhdCore& k, const D4& Mc, const D4& eta
 }
 
 // t0 and phiRef (detector-dependent through fRef = M G fmin); gwfast/waveforms.py:1131-1147
-__device__ inline void phenom_ref_setup(PhdCore& k, const D4& fpeak, double fmin_hz, const D4& C1, const D4& C2) {
-  const D4 u = (fpeak - k.alp[4] * k.fring) / k.fdamp;
+template <class D>
+__device__ inline void phenom_ref_setup(PhdCoreT<D>& k, const D& fpeak, double fmin_hz, const D& C1, const D& C2) {
+  const D u = (fpeak - k.alp[4] * k.fring) / k.fdamp;
   k.t0 = (k.alp[0] + k.alp[1] / (fpeak * fpeak) + k.alp[2] / dsqrt(dsqrt(fpeak)) + k.alp[3] / (k.fdamp * (1.0 + u * u))) / k.eta;
   k.fRef = k.MG * fmin_hz;
-  const D4 one(1.0);
-  k.phiRef = complete_phase<D4>(k, k.fRef, C1, C2, one, one);
+  const D one(1.0);
+  k.phiRef = complete_phase<D>(k, k.fRef, C1, C2, one, one);
 }
 
 struct PhdEv {
   PhdCore k;
 };
 
-__device__ inline void qnm_lookup(const double* qa, const double* qr, const double* qd, int n, const D4& a,
-                                  D4& fr, D4& fd) {
+template <class D>
+__device__ inline void qnm_lookup(const double* qa, const double* qr, const double* qd, int n, const D& a,
+                                  D& fr, D& fd) {
   // jnp.interp semantics: segment [j, j+1] with qa[j] <= a < qa[j+1]; slope carries the tangent
   int lo = 0, hi = n - 1;
   const double x = a.v;
@@ -553,6 +571,173 @@ __device__ inline void phd_phase_basis(const PhdCore& k, PhaseBasis& b) {
   b.MG = MG;
   b.fMRD = k.fMRD.v;
   b.pad = 0.0;
+}
+
+// ------------------------------------------------------------------ IMRPhenomD_NRTidalv2 (gwfast/waveforms.py:1339-1836)
+// IMRPhenomD with the spin-induced quadrupole (from the tidal deformabilities) in its 2PN and 3PN
+// spin-spin phase terms, the NRTidalv2 tidal phase (Pade approximant, arXiv:1905.06011 eq. 17), the
+// 3.5PN spin-squared and spin-cubed terms (eq. 27), the tidal amplitude (eq. 24) and a Planck taper
+// ending the waveform at 1.2 times the merger frequency. The tidal deformabilities enter the phase
+// connection constants through the quadrupole moments, so the per-event set-up carries six
+// tangent directions (Mc, eta, chi1z, chi2z, LambdaTilde, deltaLambda).
+template <class C> struct NRTEvT {
+  PhdCoreT<C> k;
+  C tidP;   // -kappa2T c_Newt / (m1 m2): coefficient of the tidal phase
+  C ssA;    // (SS_3p5PN + SSS_3p5PN) 3 / (128 eta): coefficient of (pi M f)^(2/3)
+  C tidA;   // 2 sqrt(pi/5) (-9 kappa2T) / amp0: the tidal amplitude relative to the prefactor
+  C fmer;   // Planck-taper merger frequency in M f
+};
+using NRTEv = NRTEvT<D6>;
+
+// quadrupole moment from the tidal deformability, arXiv:1608.02582 eq. 15 (gwfast/waveforms.py:1402-1403)
+template <class D>
+__device__ inline D quad_mon(const D& lam) {
+  if (lam.v < 1.0) return 1.0 + lam * (0.427688866723244 + lam * (-0.324336526985068 + lam * 0.1107439432180572));
+  const D l = dlog(lam);
+  return dexp(0.1940 + l * (0.09163 + l * (0.04812 + l * (-4.283e-3 + l * 1.245e-4))));
+}
+// octupole moment minus 1 from the quadrupole moment (gwfast/waveforms.py:1564-1565)
+template <class D>
+__device__ inline D oct_mon_m1(const D& q) {
+  const D l = dlog(q);
+  return dexp(0.003131 + l * (2.071 + l * (-0.7152 + l * (0.2458 + l * -0.03309)))) - 1.0;
+}
+
+// Lambda1, Lambda2 from (LambdaTilde, deltaLambda): the inverse of the linear map of
+// gwfast/gwfastUtils.py:398-417 (its inverse, :419-446)
+template <class D>
+__device__ inline void lam12_of(const D& lt, const D& dlt, const D& eta, D& l1, D& l2) {
+  const D e2 = eta * eta;
+  const D seta = seta_of(eta);
+  const D ap = (8. / 13.) * (1. + 7. * eta - 31. * e2), am = (8. / 13.) * seta * (1. + 9. * eta - 11. * e2);
+  const D bp = 0.5 * seta * (1. - 13272. / 1319. * eta + 8944. / 1319. * e2);
+  const D bm = 0.5 * (1. - 15910. / 1319. * eta + 32850. / 1319. * e2 + 3380. / 1319. * e2 * eta);
+  const D det = ap * bm - am * bp;
+  const D lp = (bm * lt - am * dlt) / det, lm = (ap * dlt - bp * lt) / det;
+  l1 = 0.5 * (lp + lm);
+  l2 = 0.5 * (lp - lm);
+}
+
+// merger frequency of the Planck taper in M f (gwfast/waveforms.py:1681-1694, :1813-1832)
+template <class D>
+__device__ inline D nrt_fmerger(const D& eta, const D& kap) {
+  const D seta = seta_of(eta);
+  const D q = 0.5 * (1.0 + seta - 2.0 * eta) / eta;
+  const D num = 1.0 + kap * (3.35411203e-2 + kap * 4.31460284e-5);
+  const D den = 1.0 + kap * (7.54224145e-2 + kap * 2.23626859e-4);
+  return (0.3586 / dsqrt(q)) * (num / den) / (2.0 * kPi);
+}
+
+template <class D>
+__device__ inline D nrt_kappa2t(const D& eta, const D& l1, const D& l2) {
+  const D seta = seta_of(eta);
+  const D xa = 0.5 * (1.0 + seta), xb = 0.5 * (1.0 - seta);
+  const D xa2 = xa * xa, xb2 = xb * xb;
+  return (3.0 / 13.0) * ((1.0 + 12.0 * xb / xa) * (xa2 * xa2 * xa) * l1 + (1.0 + 12.0 * xa / xb) * (xb2 * xb2 * xb) * l2);
+}
+
+// upper grid frequency in Hz: 1.2 times the merger frequency (gwfast/waveforms.py:1798-1832)
+__device__ inline double nrt_fcut(double Mc, double eta, double lt, double dlt) {
+  typedef Dual<double, 1> D1;   // value-only use of the dual helpers
+  D1 l1, l2;
+  lam12_of(D1(lt), D1(dlt), D1(eta), l1, l2);
+  const D1 kap = nrt_kappa2t(D1(eta), l1, l2);
+  return 1.2 * nrt_fmerger(D1(eta), kap).v / (Mc / pow(eta, 0.6) * kG3);
+}
+
+__device__ inline void nrt_ref(NRTEv& e, double fmin_hz) {
+  PhdCoreT<D6>& k = e.k;
+  const D6& g2 = k.gam[1];
+  const D6& g3 = k.gam[2];
+  const D6 fpP = (g2.v >= 1.0) ? dabs(k.fring - k.fdamp * g3 / g2) : dabs(k.fring + k.fdamp * (dsqrt(1.0 - g2 * g2) - 1.0) * g3 / g2);
+  phenom_ref_setup(k, fpP, fmin_hz, k.C1MRD, k.C2MRD);
+}
+
+__device__ inline void nrt_setup(NRTEv& e, const D6& Mc, const D6& eta, const D6& chi1, const D6& chi2, double dL,
+                                 double fmin_hz, const double* qa, const double* qr, const double* qd, int nq,
+                                 const D6& lt, const D6& dlt) {
+  PhdCoreT<D6>& k = e.k;
+  D6 l1, l2;
+  lam12_of(lt, dlt, eta, l1, l2);
+  const D6 q1 = quad_mon(l1), q2 = quad_mon(l2);
+  const D6 af = final_spin(eta, chi1, chi2);
+  const D6 er = radiated_energy(eta, chi1, chi2);
+  D6 fr, fd;
+  qnm_lookup(qa, qr, qd, nq, af, fr, fd);
+  fr = fr / (1.0 - er);
+  fd = fd / (1.0 - er);
+  phenom_core_setup(k, Mc, eta, chi1, chi2, fr, fd, q1 - 1.0, q2 - 1.0);
+  nrt_ref(e, fmin_hz);
+  const D6 M = Mc / dpowc(eta, 0.6);
+  const D6 amp0 = dsqrt(eta * (2.0 / 3.0)) * pow(kPi, -1.0 / 6.0);
+  k.ampPref = (2.0 * sqrt(5.0 / (64.0 * kPi)) * kG2Gpc * kG3 / dL) * M * M * amp0;
+  const D6 seta = seta_of(eta);
+  const D6 m1 = 0.5 * (1.0 + seta), m2 = 0.5 * (1.0 - seta);
+  const D6 kap = nrt_kappa2t(eta, l1, l2);
+  e.tidP = (-2.4375) * kap / (m1 * m2);
+  e.tidA = (2.0 * sqrt(kPi / 5.0) * -9.0) * kap / amp0;
+  e.fmer = nrt_fmerger(eta, kap);
+  // 3.5PN spin-squared and spin-cubed terms (gwfast/waveforms.py:1567-1568)
+  const D6 c12 = chi1 * chi1, c22 = chi2 * chi2, m12 = m1 * m1, m22 = m2 * m2;
+  const D6 dq1 = q1 - 1.0, dq2 = q2 - 1.0;
+  const D6 ss = -400. * kPi * dq1 * c12 * m12 - 400. * kPi * dq2 * c22 * m22;
+  const D6 sss = 10. * ((m12 + 308. / 3. * m1) * chi1 + (m22 - 89. / 3. * m2) * chi2) * dq1 * m12 * c12
+                 + 10. * ((m22 + 308. / 3. * m2) * chi2 + (m12 - 89. / 3. * m1) * chi1) * dq2 * m22 * c22
+                 - 440. * oct_mon_m1(q1) * m12 * m1 * c12 * chi1 - 440. * oct_mon_m1(q2) * m22 * m2 * c22 * chi2;
+  e.ssA = (ss + sss) * (3.0 / (128.0 * eta));
+}
+
+__device__ __forceinline__ double taper_make(double, double t, double) { return t; }
+template <class U, int N>
+__device__ __forceinline__ Dual<U, N> taper_make(const Dual<U, N>& y, U t, U dy) { return chain(y, t, dy); }
+
+// Planck taper (gwfast/waveforms.py:1696-1716) at x = M f for merger frequency y: its tangent is
+// carried only through y, as gwfast's custom derivative of the taper does (the x dependence is
+// left out there)
+template <class S, class C>
+__device__ __forceinline__ S planck_taper(typename Real<S>::T x, const C& y_) {
+  typedef typename Real<S>::T T;
+  const S y = co<S>(y_);
+  const T yv = val(y), a = T(1.2), yp = a * yv;
+  if (x < yv) return S(T(1));
+  if (x > yp) return S(T(0));
+  const T u = (yp - yv) / (x - yv) + (yp - yv) / (x - yp);
+  const T E = exp(u);
+  T t = T(1) - T(1) / (E + T(1));
+  if (!(t == t)) t = T(0);   // nan_to_num
+  T dy = E * ((a - T(1)) / (x - yv) + (a - T(1)) / (x - yp) + (yp - yv) / ((x - yv) * (x - yv))
+              + a * (yp - yv) / ((x - yp) * (x - yp))) / ((E + T(1)) * (E + T(1)));
+  if (!(dy == dy) || isinf(dy)) dy = T(0);
+  return taper_make(y, t, dy);
+}
+
+// amplitude and phase of IMRPhenomD_NRTidalv2 at physical frequency f (Hz)
+template <class S, class C>
+__device__ __forceinline__ void nrt_point(const NRTEvT<C>& e, typename Real<S>::T f, S& amp, S& phase) {
+  typedef typename Real<S>::T T;
+  const PhdCoreT<C>& k = e.k;
+  const S x = co<S>(k.MG) * f;
+  const T xv = val(x);
+  const S one(T(1));
+  const S xm76 = T(1) / (x * dsqrt(dcbrt(x)));
+  const S px = T(kPi) * x;
+  const S xt = dcbrt(px) * dcbrt(px);   // (pi M f)^(2/3)
+  const S xt2 = xt * xt;
+  const S poly = (T(1) + T(4.157407407407407) * xt + T(2519.111111111111) * dexp(T(2.89) * dlog(xt)))
+                 / (T(1) + T(13477.8073677) * xt2 * xt2);
+  const S tidal_amp = co<S>(e.tidA) * dexp(T(3.25) * dlog(xt)) * poly;
+  const S taper = planck_taper<S, C>(xv, e.fmer);
+  amp = co<S>(k.ampPref) * (xm76 * complete_amp_shape(k, x) + tidal_amp) * taper;
+  S ph = complete_phase(k, x, co<S>(k.C1MRD), co<S>(k.C2MRD), one, one);
+  if (xv < T(kMfCut)) {
+    const S x13 = dcbrt(px);
+    const S num = T(1) + x13 * x13 * T(-12.615214237993088) + px * T(19.0537346970349)
+                  + x13 * px * T(-21.166863146081035) + x13 * x13 * px * T(90.55082156324926) + px * px * T(-60.25357801943598);
+    const S den = T(1) + x13 * x13 * T(-15.11120782773667) + px * T(22.195327350624694) + x13 * px * T(8.064109635305156);
+    const S tidal_ph = co<S>(e.tidP) * (x13 * x13 * px) * num / den;   // (pi M f)^(5/3) num / den
+    ph = ph - co<S>(k.t0) * (x - co<S>(k.fRef)) - co<S>(k.phiRef) + tidal_ph + co<S>(e.ssA) * xt;
+  }
+  phase = ph;
 }
 
 // ------------------------------------------------------------------ IMRPhenomHM (gwfast/waveforms.py:2256-2616)

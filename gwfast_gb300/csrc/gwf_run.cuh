@@ -31,7 +31,7 @@ cudaError_t chunked(const LaunchArgs& a, bool f32, MAIN main) {
     const long long cnt = (a.ev.N - n0) < kChunk ? (a.ev.N - n0) : kChunk;
     const unsigned nb = (unsigned)((cnt + 63) / 64);
     setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, a.det, a.wf, a.qnm, a.nq, a.scratch, cnt, a.core, a.core_mode, a.core_idx);
-    if constexpr (M != 3) {   // (the tidal model has no FP32 form)
+    if constexpr (M < 3) {   // (the tidal models have no FP32 form)
       if (f32) setup_f32_kernel<M><<<nb, 64, 0, a.stream>>>(a.det, a.scratch, scratch32_of(a), cnt,
                                                             a.det.shape == 1 ? 2 : 1, a.det.earth);
     }
@@ -78,7 +78,7 @@ cudaError_t persist_grid(K k, int smem, int* grid) {
 template <bool EARTH, int NARM, int NG>
 cudaError_t fisher_one(const LaunchArgs& a) {
   const int smem = kWarps * NG * (np_of<M>() + 1) * kSR64 * (int)sizeof(cd);
-  if (a.seg <= 0 || M == 3) {
+  if (a.seg <= 0 || M >= 3) {
     auto k = fisher_kernel<M, EARTH, NARM, NG>;
     cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (err != cudaSuccess) return err;
@@ -88,8 +88,8 @@ cudaError_t fisher_one(const LaunchArgs& a) {
       return cudaSuccess;
     });
   }
-  if constexpr (M == 3) {
-    return cudaErrorNotSupported;   // not reached: the tidal model always runs one CTA per event
+  if constexpr (M >= 3) {
+    return cudaErrorNotSupported;   // not reached: the tidal models always run one CTA per event
   } else {
     auto ks = fisher_seg_kernel<M, EARTH, NARM, NG>;
     cudaError_t err = cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -141,7 +141,7 @@ cudaError_t snr_one(const LaunchArgs& a) {
 cudaError_t fisher_dispatch(const LaunchArgs& a) {
   const bool tri = a.det.shape == 1;
   if (a.precision == 1) {
-    if constexpr (M == 3) {
+    if constexpr (M >= 3) {
       return cudaErrorNotSupported;
     } else {
       if (a.det.earth) {
@@ -217,7 +217,7 @@ cudaError_t group_one(const LaunchArgs& a, GroupDev g) {
 }
 
 cudaError_t group_dispatch(const LaunchArgs& a, const GroupDev& g) {
-  if constexpr (M == 3) return cudaErrorNotSupported;
+  if constexpr (M >= 3) return cudaErrorNotSupported;
   else return a.det.earth ? group_one<true>(a, g) : group_one<false>(a, g);
 }
 
@@ -232,7 +232,7 @@ cudaError_t wave_one(const LaunchArgs& a, const WaveOut& o) {
 }
 
 cudaError_t wave_dispatch(const LaunchArgs& a, const WaveOut& o) {
-  if constexpr (M == 3) {
+  if constexpr (M >= 3) {
     return cudaErrorNotSupported;   // 11-parameter outputs only
   } else {
     if (o.cnt <= 0) return cudaSuccess;

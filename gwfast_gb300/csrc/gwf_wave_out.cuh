@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(kThreads) wave_out_kernel(EvBatch ev, DetDev d
     grid_point(g, ev.spacing, k, f, lnf, w);
     if (o.mode == WAVE_DERIVS) {
       cd P, C, dP[4], dC[4], dPi, dCi;
-      D4 tau(0.0);
+      DualOf<MODEL> tau(0.0);   // (11-parameter models only: four tangent directions)
       double phi0;
       wave_point_dual<MODEL, EARTH>(E, pj, f, lnf, P, C, dP, dC, dPi, dCi, tau, phi0);
       double dtn[4] = {0.0, 0.0, 0.0, 0.0};

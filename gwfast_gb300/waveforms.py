@@ -4,7 +4,8 @@ The waveforms themselves are evaluated inside the fused CUDA kernels; these
 objects carry what gwfast's callers read from a model (``ParNums``, ``nParams``,
 the ``is_*`` flags, ``objType``, ``fcut``) plus the descriptor the C ABI needs.
 Supported: TaylorF2_RestrictedPN (optionally with the 3.5PN spin-spin terms and with the tidal
-terms, 13 parameters), IMRPhenomD and IMRPhenomHM, aligned spins, no eccentricity.
+terms, 13 parameters), IMRPhenomD, IMRPhenomHM and IMRPhenomD_NRTidalv2 (13 parameters), aligned
+spins, no eccentricity.
 """
 import numpy as np
 
@@ -21,7 +22,7 @@ class WaveFormModel:
     def __init__(self, objType, fcutPar, is_newtonian=False, is_tidal=False, is_HigherModes=False, is_chi1chi2=True,
                  is_Precessing=False, is_LAL=False, is_prec_ang=False, is_eccentric=False, is_holomorphic=False,
                  apply_fcut=True):
-        tidal_ok = type(self).__name__ == 'TaylorF2_RestrictedPN'
+        tidal_ok = type(self).__name__ in ('TaylorF2_RestrictedPN', 'IMRPhenomD_NRTidalv2')
         for flag, name in ((is_newtonian, 'is_newtonian'), (is_tidal and not tidal_ok, 'is_tidal'),
                            (is_Precessing, 'is_Precessing'), (is_LAL, 'is_LAL'), (is_eccentric, 'is_eccentric')):
             if flag:
@@ -61,7 +62,8 @@ class WaveFormModel:
         return self.fcutPar / (np.asarray(kwargs['Mc']) / (np.asarray(kwargs['eta']) ** (3. / 5.)))
 
     def gpu_desc(self):
-        model = _lib.MODEL_TF2_TIDAL if self.is_tidal else _lib.MODEL_IDS[type(self).__name__]
+        name = type(self).__name__
+        model = _lib.MODEL_TF2_TIDAL if (self.is_tidal and name == 'TaylorF2_RestrictedPN') else _lib.MODEL_IDS[name]
         return _lib.WfDesc(model, int(getattr(self, 'use_3p5PN_SpinHO', False)), float(self.fcutPar))
 
     def _device_only(self, *a, **k):
@@ -113,3 +115,37 @@ class IMRPhenomHM(IMRPhenomD):
         kwargs['is_HigherModes'] = True
         super().__init__(fRef=fRef, **kwargs)
         self.complShiftm = np.array([0., np.pi * 0.5, 0., -np.pi * 0.5, np.pi, np.pi * 0.5, 0.])
+
+
+class IMRPhenomD_NRTidalv2(WaveFormModel):
+    """gwfast/waveforms.py:1339-1836: IMRPhenomD with the spin-induced quadrupole, the NRTidalv2 tidal
+    phase and amplitude and a Planck taper (13 parameters, FP64 path only)."""
+
+    def __init__(self, fRef=None, **kwargs):
+        if fRef is not None:
+            raise NotImplementedError('a fixed fRef is not implemented on the GPU path')
+        self.AMP_fJoin_INS = 0.014
+        self.PHI_fJoin_INS = 0.018
+        self.fRef = fRef
+        super().__init__('BNS', 0.2, is_tidal=True, **kwargs)
+
+    def fcut(self, **kwargs):
+        """1.2 times the merger frequency of the Planck taper, in Hz (gwfast/waveforms.py:1798-1832)."""
+        from . import gwfastUtils as utils
+        Mc, eta = np.asarray(kwargs['Mc']), np.asarray(kwargs['eta'])
+        M = Mc / eta ** (3. / 5.)
+        if 'Lambda1' in kwargs:
+            l1, l2 = np.asarray(kwargs['Lambda1']), np.asarray(kwargs['Lambda2'])
+        elif 'LambdaTilde' in kwargs:
+            l1, l2 = utils.Lam12_from_Lamt_delLam(np.asarray(kwargs['LambdaTilde']), np.asarray(kwargs['deltaLambda']), eta)
+        else:
+            l1, l2 = np.zeros(M.shape), np.zeros(M.shape)
+        seta = np.sqrt(np.where(eta < 0.25, 1.0 - 4.0 * eta, 0.))
+        q = 0.5 * (1.0 + seta - 2.0 * eta) / eta
+        xa, xb = 0.5 * (1.0 + seta), 0.5 * (1.0 - seta)
+        kap = (3.0 / 13.0) * ((1.0 + 12.0 * xb / xa) * xa ** 5 * l1 + (1.0 + 12.0 * xa / xb) * xb ** 5 * l2)
+        num = 1.0 + 3.35411203e-2 * kap + 4.31460284e-5 * kap * kap
+        den = 1.0 + 7.54224145e-2 * kap + 2.23626859e-4 * kap * kap
+        f_merger = 0.3586 / np.sqrt(q) * (num / den) / (2. * np.pi)
+        return 1.2 * f_merger / (M * glob.GMsun_over_c3)
+

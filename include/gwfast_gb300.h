@@ -13,7 +13,7 @@
  *    parameter k of event n, k in the Fisher order
  *      0 Mc [Msun, detector frame], 1 eta, 2 dL [Gpc], 3 theta, 4 phi, 5 iota,
  *      6 psi [rad], 7 tcoal [GMST days], 8 Phicoal [rad], 9 chi1z, 10 chi2z
- *    (gwfast/waveforms.py:78, :125-129); the tidal TaylorF2 (GWF_WF_TAYLORF2_TIDAL) adds
+ *    (gwfast/waveforms.py:78, :125-129); the tidal models (GWF_WF_TAYLORF2_TIDAL, GWF_WF_PHENOMD_NRTIDALV2) add
  *      11 LambdaTilde, 12 deltaLambda (gwfast/waveforms.py:106-109), 13 rows in all.
  *  - mem = GWF_MEM_HOST: params, res_per_event and outputs are host pointers; the
  *    call copies in, runs, copies out and returns when the outputs are written.
@@ -45,8 +45,12 @@ enum {
   GWF_ERR_UNSUPPORTED = -5
 };
 
-/* GWF_WF_TAYLORF2_TIDAL: TaylorF2_RestrictedPN(is_tidal=True), gwfast/waveforms.py:849-855; FP64 only */
-enum { GWF_WF_TAYLORF2 = 0, GWF_WF_PHENOMD = 1, GWF_WF_PHENOMHM = 2, GWF_WF_TAYLORF2_TIDAL = 3 };
+/* GWF_WF_TAYLORF2_TIDAL: TaylorF2_RestrictedPN(is_tidal=True), gwfast/waveforms.py:849-855;
+ * GWF_WF_PHENOMD_NRTIDALV2: IMRPhenomD_NRTidalv2, gwfast/waveforms.py:1339-1836 (its cut frequency
+ * follows from the deformabilities; fcut_par is the M f cut 0.2 of the IMRPhenomD part). Both FP64,
+ * 13 parameters. */
+enum { GWF_WF_TAYLORF2 = 0, GWF_WF_PHENOMD = 1, GWF_WF_PHENOMHM = 2, GWF_WF_TAYLORF2_TIDAL = 3,
+       GWF_WF_PHENOMD_NRTIDALV2 = 4 };
 enum { GWF_SHAPE_L = 0, GWF_SHAPE_T = 1 };
 enum { GWF_SPACING_GEOM = 0, GWF_SPACING_LIN = 1 };
 enum { GWF_MEM_HOST = 0, GWF_MEM_DEVICE = 1 };

@@ -67,11 +67,12 @@ def _seta(eta):
 
 
 # ---------------------------------------------------------------- PN phase coefficients
-def pn_coeffs(eta, chi1, chi2, spin_ho=False, drop_3pn_ss=False):
-    """TaylorF2 phase coefficients (gwfast/waveforms.py:784-812; QuadMon = 1).
+def pn_coeffs(eta, chi1, chi2, spin_ho=False, drop_3pn_ss=False, dq1=0., dq2=0.):
+    """TaylorF2 phase coefficients (gwfast/waveforms.py:784-812).
 
     ``drop_3pn_ss`` removes the 3PN spin-spin terms, as IMRPhenomD does
-    (gwfast/waveforms.py:1077).
+    (gwfast/waveforms.py:1077). ``dq1``, ``dq2``: spin-induced quadrupole moments minus one, which
+    IMRPhenomD_NRTidalv2 keeps in its 2PN and 3PN spin-spin terms (gwfast/waveforms.py:1461-1467).
     """
     seta = _seta(eta)
     m1 = 0.5 * (1.0 + seta)
@@ -83,9 +84,11 @@ def pn_coeffs(eta, chi1, chi2, spin_ho=False, drop_3pn_ss=False):
     c['two'] = 3715. / 756. + 55. * eta / 9.
     c['three'] = -16. * PI + 113. * seta * chia / 3. + (113. / 3. - 76. * eta / 3.) * chis
     m1s, m2s = m1 * m1 * chi1 * chi1, m2 * m2 * chi2 * chi2
+    q1, q2 = 1. + dq1, 1. + dq2
     c['four'] = (5. * (3058.673 / 7.056 + 5429. / 7. * eta + 617. * eta2) / 72.
                  + (247. / 4.8 - 721. / 4.8) * eta * chi1 * chi2
-                 + ((-720. / 9.6 + 1. / 9.6) + (240. / 9.6 - 7. / 9.6)) * (m1s + m2s))
+                 + (-720. / 9.6 * q1 + 1. / 9.6) * m1s + (-720. / 9.6 * q2 + 1. / 9.6) * m2s
+                 + (240. / 9.6 * q1 - 7. / 9.6) * m1s + (240. / 9.6 * q2 - 7. / 9.6) * m2s)
     t5 = ((732985. / 2268. - 24260. * eta / 81. - 340. * eta2 / 9.) * chis
           + (732985. / 2268. + 140. * eta / 9.) * seta * chia)
     c['five'] = 38645. * PI / 756. - 65. * PI * eta / 9. - t5
@@ -94,6 +97,9 @@ def pn_coeffs(eta, chi1, chi2, spin_ho=False, drop_3pn_ss=False):
            + eta * (-15737.765635 / 3.048192 + 225.5 / 1.2 * PI * PI)
            + eta2 * 76.055 / 1.728 - eta2 * eta * 127.825 / 1.296 - math.log(4.) * 684.8 / 2.1
            + PI * chi1 * m1 * (1490. / 3. + 260. * m1) + PI * chi2 * m2 * (1490. / 3. + 260. * m2))
+    if drop_3pn_ss:
+        six = six + ((4703.5 / 8.4 + 2935. / 6. * m1 - 120. * m1 * m1) * m1s * dq1
+                     + (4703.5 / 8.4 + 2935. / 6. * m2 - 120. * m2 * m2) * m2s * dq2)
     if not drop_3pn_ss:
         def ss(m):
             return (4703.5 / 8.4 + 2935. / 6. * m - 120. * m * m) + (-4108.25 / 6.72 - 108.5 / 1.2 * m + 125.5 / 3.6 * m * m)
@@ -281,8 +287,9 @@ def _mrd_phase_raw_d(Mf, a, fring, fdamp, eta, rho=1., tau=1.):
     return (a[0] + a[1] / (Mf * Mf) + a[2] / Mf ** 0.25 + a[3] / (fdamp * tau * (1. + u * u))) / eta
 
 
-def _phenom_core(Mc, eta, chi1, chi2, fring, fdamp):
-    """Per-event IMRPhenomD phase/amplitude coefficients common to PhenomD and PhenomHM."""
+def _phenom_core(Mc, eta, chi1, chi2, fring, fdamp, dq1=0., dq2=0.):
+    """Per-event IMRPhenomD phase/amplitude coefficients common to PhenomD, PhenomHM and
+    PhenomD_NRTidalv2 (whose spin-induced quadrupole moments enter through ``dq1``, ``dq2``)."""
     seta = _seta(eta)
     chis, chia = 0.5 * (chi1 + chi2), 0.5 * (chi1 - chi2)
     chiPN = chis * (1.0 - eta * 76.0 / 113.0) + seta * chia
@@ -292,7 +299,7 @@ def _phenom_core(Mc, eta, chi1, chi2, fring, fdamp):
     k['eta'] = eta
     k['seta'] = seta
     k['fring'], k['fdamp'] = fring, fdamp
-    c = pn_coeffs(eta, chi1, chi2, drop_3pn_ss=True)
+    c = pn_coeffs(eta, chi1, chi2, drop_3pn_ss=True, dq1=dq1, dq2=dq2)
     k['c'] = c
     k['A'] = 3. / (128. * eta) * PI ** (-5. / 3.)
     # normalise the TF2 series so that x**(-5/3) carries coefficient 1 (A absorbs it)
@@ -406,18 +413,18 @@ def _amp_pieces(Mf, k, a, delta, fpeak):
     return torch.where(Mf < AMP_FJOIN_INS, ins, torch.where(Mf < fpeak, itm, torch.where(Mf < MF_CUT, mrd, zero)))
 
 
-def _phd_event(Mc, eta, chi1, chi2):
+def _phd_event(Mc, eta, chi1, chi2, dq1=0., dq2=0.):
     aeff = final_spin(eta, chi1, chi2)
     Erad = radiated_energy(eta, chi1, chi2)
     q = qnm_table()
     fring = interp(aeff, q[:, 0].contiguous(), q[:, 1].contiguous()) / (1.0 - Erad)
     fdamp = interp(aeff, q[:, 0].contiguous(), q[:, 2].contiguous()) / (1.0 - Erad)
-    return _phenom_core(Mc, eta, chi1, chi2, fring, fdamp)
+    return _phenom_core(Mc, eta, chi1, chi2, fring, fdamp, dq1, dq2)
 
 
-def phd_phase(f, Mc, eta, chi1, chi2):
+def phd_phase(f, Mc, eta, chi1, chi2, dq1=0., dq2=0.):
     """IMRPhenomD.Phi with fRef = min of the grid (gwfast/waveforms.py:992-1147)."""
-    k = _phd_event(Mc, eta, chi1, chi2)
+    k = _phd_event(Mc, eta, chi1, chi2, dq1, dq2)
     M = k['M']
     Mf = M * GMSUN_OVER_C3 * f
     fr, fd, g2, g3 = k['fring'], k['fdamp'], k['gamma2'], k['gamma3']
@@ -447,6 +454,132 @@ def phd_ampl(f, Mc, eta, chi1, chi2, dL):
     amp0 = torch.sqrt(2.0 * eta / 3.0) * PI ** (-1. / 6.)
     over = 2. * math.sqrt(5. / (64. * PI)) * M * GMSUN_OVER_C2_GPC * M * GMSUN_OVER_C3 / dL
     return over * amp0 * Mf ** (-7. / 6.) * _amp_pieces(Mf, k, a, delta, fpeak)
+
+
+# ---------------------------------------------------------------- IMRPhenomD_NRTidalv2
+def lam12_from_lamt_dellam(lt, dlt, eta):
+    """Lambda1, Lambda2 from (LambdaTilde, deltaLambda), gwfast/gwfastUtils.py:419-446."""
+    e2 = eta * eta
+    seta = _seta(eta)
+    lp_ = (8. / 13.) * (1. + 7. * eta - 31. * e2)
+    lm_ = (8. / 13.) * seta * (1. + 9. * eta - 11. * e2)
+    dp_ = 0.5 * seta * (1. - 13272. / 1319. * eta + 8944. / 1319. * e2)
+    dm_ = 0.5 * (1. - 15910. / 1319. * eta + 32850. / 1319. * e2 + 3380. / 1319. * e2 * eta)
+    det = (306656. / 1319.) * eta ** 5 - (5936. / 1319.) * eta ** 4
+    return ((dp_ - dm_) * lt + (lm_ - lp_) * dlt) / det, ((-dm_ - dp_) * lt + (lm_ + lp_) * dlt) / det
+
+
+def quad_mon(lam):
+    """Spin-induced quadrupole moment from Lambda (arXiv:1608.02582 eq. 15; gwfast/waveforms.py:1402-1403)."""
+    ll = torch.log(torch.clamp(lam, min=1.))
+    big = torch.exp(0.1940 + 0.09163 * ll + 0.04812 * ll ** 2 - 4.283e-3 * ll ** 3 + 1.245e-4 * ll ** 4)
+    small = 1. + lam * (0.427688866723244 + lam * (-0.324336526985068 + lam * 0.1107439432180572))
+    return torch.where(lam < 1., small, big)
+
+
+def oct_mon_m1(qm):
+    """Octupole moment minus one from the quadrupole moment (gwfast/waveforms.py:1564-1565)."""
+    lq = torch.log(qm)
+    return torch.exp(0.003131 + 2.071 * lq - 0.7152 * lq ** 2 + 0.2458 * lq ** 3 - 0.03309 * lq ** 4) - 1.
+
+
+def nrt_kappa2t(eta, l1, l2):
+    """Tidal coupling constant kappa_2^T (arXiv:1905.06011 eq. 8; gwfast/waveforms.py:1546)."""
+    seta = _seta(eta)
+    xa, xb = 0.5 * (1. + seta), 0.5 * (1. - seta)
+    return (3. / 13.) * ((1. + 12. * xb / xa) * xa ** 5 * l1 + (1. + 12. * xa / xb) * xb ** 5 * l2)
+
+
+def nrt_fmerger(eta, kap):
+    """Merger frequency in M f of the Planck taper (gwfast/waveforms.py:1688-1700)."""
+    seta = _seta(eta)
+    q = 0.5 * (1. + seta - 2. * eta) / eta
+    num = 1. + 3.35411203e-2 * kap + 4.31460284e-5 * kap * kap
+    den = 1. + 7.54224145e-2 * kap + 2.23626859e-4 * kap * kap
+    return 0.3586 / torch.sqrt(q) * (num / den) / (2. * PI)
+
+
+def nrt_fcut(Mc, eta, lt, dlt):
+    """1.2 times the merger frequency, in Hz (gwfast/waveforms.py:1798-1832)."""
+    l1, l2 = lam12_from_lamt_dellam(lt, dlt, eta)
+    return 1.2 * nrt_fmerger(eta, nrt_kappa2t(eta, l1, l2)) / (Mc * GMSUN_OVER_C3 / eta ** (3. / 5.))
+
+
+def planck_taper(x, y):
+    """Planck taper between y and 1.2 y (gwfast/waveforms.py:1702-1723). As gwfast's custom derivative,
+    the tangent flows through the merger frequency y only; NaN values and tangents become zero."""
+    a = 1.2
+    xv, yv = x.detach(), y.detach()
+    yp = a * yv
+    z = (yp - yv) / (xv - yv) + (yp - yv) / (xv - yp)
+    E = torch.exp(z)
+    mid = 1. - 1. / (E + 1.)
+    dmid = E * ((a - 1.) / (xv - yv) + (a - 1.) / (xv - yp) + (yp - yv) / (xv - yv) ** 2
+                + a * (yp - yv) / (xv - yp) ** 2) / (E + 1.) ** 2
+    inside = (xv >= yv) & (xv <= yp)
+    t = torch.where(xv < yv, torch.ones_like(xv), torch.where(xv > yp, torch.zeros_like(xv), mid))
+    dt = torch.where(inside, dmid, torch.zeros_like(xv))
+    t = torch.nan_to_num(t, nan=0.)
+    dt = torch.where(torch.isfinite(dt), dt, torch.zeros_like(dt))
+    return t + dt * (y - yv)
+
+
+def _nrt_event(Mc, eta, chi1, chi2, lt, dlt):
+    l1, l2 = lam12_from_lamt_dellam(lt, dlt, eta)
+    q1, q2 = quad_mon(l1), quad_mon(l2)
+    return l1, l2, q1, q2
+
+
+def nrt_phase(f, Mc, eta, chi1, chi2, lt, dlt):
+    """IMRPhenomD_NRTidalv2.Phi (gwfast/waveforms.py:1375-1582): IMRPhenomD with the quadrupole moments
+    in the 2PN and 3PN spin-spin terms, plus the NRTidalv2 Pade tidal phase and the 3.5PN spin-squared
+    and spin-cubed terms, all under the Mf < 0.2 cut."""
+    l1, l2, q1, q2 = _nrt_event(Mc, eta, chi1, chi2, lt, dlt)
+    ph = phd_phase(f, Mc, eta, chi1, chi2, q1 - 1., q2 - 1.)
+    M = Mc / eta ** (3. / 5.)
+    Mf = M * GMSUN_OVER_C3 * f
+    px = PI * Mf
+    seta = _seta(eta)
+    m1, m2 = 0.5 * (1. + seta), 0.5 * (1. - seta)
+    kap = nrt_kappa2t(eta, l1, l2)
+    num = (1. - 12.615214237993088 * px ** (2. / 3.) + 19.0537346970349 * px - 21.166863146081035 * px ** (4. / 3.)
+           + 90.55082156324926 * px ** (5. / 3.) - 60.25357801943598 * px * px)
+    den = 1. - 15.11120782773667 * px ** (2. / 3.) + 22.195327350624694 * px + 8.064109635305156 * px ** (4. / 3.)
+    tidal = -kap * 2.4375 / (m1 * m2) * px ** (5. / 3.) * num / den
+    c12, c22 = chi1 * chi1, chi2 * chi2
+    ss = -400. * PI * (q1 - 1.) * c12 * m1 * m1 - 400. * PI * (q2 - 1.) * c22 * m2 * m2
+    sss = (10. * ((m1 * m1 + 308. / 3. * m1) * chi1 + (m2 * m2 - 89. / 3. * m2) * chi2) * (q1 - 1.) * m1 * m1 * c12
+           + 10. * ((m2 * m2 + 308. / 3. * m2) * chi2 + (m1 * m1 - 89. / 3. * m1) * chi1) * (q2 - 1.) * m2 * m2 * c22
+           - 440. * oct_mon_m1(q1) * m1 ** 3 * c12 * chi1 - 440. * oct_mon_m1(q2) * m2 ** 3 * c22 * chi2)
+    extra = tidal + (ss + sss) * 3. / (128. * eta) * px ** (2. / 3.)
+    return ph + torch.where(Mf < MF_CUT, extra, torch.zeros_like(extra))
+
+
+def nrt_ampl(f, Mc, eta, chi1, chi2, dL, lt, dlt, taper_last=None):
+    """IMRPhenomD_NRTidalv2.Ampl (gwfast/waveforms.py:1584-1723): the IMRPhenomD amplitude plus the
+    NRTidalv2 tidal amplitude, times the Planck taper.
+
+    The grid ends at fcut = 1.2 f_merger, so its last point sits on the end of the taper, x = 1.2 y,
+    up to rounding; there the formula gives 1 when x equals 1.2 y exactly (the exponent is +inf) and 0
+    on either side. ``taper_last`` (bool per event, shape (N, 1)) fixes that point's taper to 1 or 0,
+    with no tangent, to reproduce either outcome.
+    """
+    l1, l2, _, _ = _nrt_event(Mc, eta, chi1, chi2, lt, dlt)
+    M = Mc / eta ** (3. / 5.)
+    Mf = M * GMSUN_OVER_C3 * f
+    kap = nrt_kappa2t(eta, l1, l2)
+    xt = (PI * Mf) ** (2. / 3.)
+    poly = (1. + 4.157407407407407 * xt + 2519.111111111111 * xt ** 2.89) / (1. + 13477.8073677 * xt ** 4)
+    amp_t = -9. * kap * xt ** 3.25 * poly
+    over = 2. * math.sqrt(5. / (64. * PI)) * M * GMSUN_OVER_C2_GPC * M * GMSUN_OVER_C3 / dL
+    base = phd_ampl(f, Mc, eta, chi1, chi2, dL)
+    taper = planck_taper(Mf, nrt_fmerger(eta, kap))
+    if taper_last is not None:
+        last = torch.zeros(taper.shape, dtype=torch.bool)
+        last[..., -1] = True
+        forced = torch.as_tensor(taper_last, dtype=DT).reshape(-1, 1).expand(taper.shape)
+        taper = torch.where(last, forced, taper)
+    return (base + over * 2. * math.sqrt(PI / 5.) * amp_t) * taper
 
 
 # ---------------------------------------------------------------- IMRPhenomHM
@@ -639,14 +772,17 @@ def delt_loc(det, theta, phi, t):
 
 # ---------------------------------------------------------------- model descriptor
 class Model:
-    """Which waveform to evaluate: 'TF2', 'PhenomD' or 'PhenomHM'."""
+    """Which waveform to evaluate: 'TF2' (``tidal``: with the tidal terms), 'PhenomD', 'PhenomHM' or
+    'PhenomD_NRTidalv2'."""
 
-    def __init__(self, name, spin_ho=False, tidal=False):
-        assert name in ('TF2', 'PhenomD', 'PhenomHM')
+    def __init__(self, name, spin_ho=False, tidal=False, taper_last=None):
+        assert name in ('TF2', 'PhenomD', 'PhenomHM', 'PhenomD_NRTidalv2')
         assert not tidal or name == 'TF2'
         self.name = name
         self.spin_ho = spin_ho
-        self.tidal = tidal
+        self.tidal = tidal or name == 'PhenomD_NRTidalv2'
+        self.taper_last = taper_last   # PhenomD_NRTidalv2: see nrt_ampl
+
 
     @property
     def params(self):
@@ -659,9 +795,18 @@ class Model:
     def fcut(self, Mc, eta):
         return tf2_fcut(Mc, eta) if self.name == 'TF2' else phd_fcut(Mc, eta)
 
+    def fcut_of(self, p):
+        """Upper grid frequency of each event, in Hz."""
+        if self.name == 'PhenomD_NRTidalv2':
+            return nrt_fcut(p['Mc'], p['eta'], p['LambdaTilde'], p['deltaLambda'])
+        return self.fcut(p['Mc'], p['eta'])
+
     def ampl(self, f, p):
         if self.name == 'TF2':
             return tf2_ampl(f, p['Mc'], p['dL'])
+        if self.name == 'PhenomD_NRTidalv2':
+            return nrt_ampl(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'], p['dL'], p['LambdaTilde'], p['deltaLambda'],
+                            self.taper_last)
         return phd_ampl(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'], p['dL'])
 
     def phase(self, f, p):
@@ -670,6 +815,8 @@ class Model:
                 return tf2_phase(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'], self.spin_ho, p['LambdaTilde'],
                                  p['deltaLambda'])
             return tf2_phase(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'], self.spin_ho)
+        if self.name == 'PhenomD_NRTidalv2':
+            return nrt_phase(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'], p['LambdaTilde'], p['deltaLambda'])
         return phd_phase(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'])
 
     def hphc(self, f, p):
@@ -694,7 +841,7 @@ def psd_on_grid(det, f):
 
 
 def event_grid(det, model, p, res, spacing='geom'):
-    fc = model.fcut(p['Mc'], p['eta']).reshape(-1).detach().numpy()
+    fc = model.fcut_of(p).reshape(-1).detach().numpy()
     if det.fmax is not None:
         fc = np.where(fc > det.fmax, det.fmax, fc)
     f = freq_grid(det.fmin, fc, res, spacing)
@@ -911,8 +1058,8 @@ def overlap_parts(det, model1, p1, model2, p2, res=1000):
     """One detector of WFOverlap (gwfast/signal.py:1759-1921): (h1|h2), SNR_1^2, SNR_2^2 summed over
     the arms, on the geometric grid from fmin to max(fcut_1, fcut_2) (with fmax: fmax where that
     maximum exceeds it, else fcut_1, as :1865-1866 reads)."""
-    fc1 = model1.fcut(p1['Mc'], p1['eta']).reshape(-1).detach().numpy()
-    fc2 = model2.fcut(p2['Mc'], p2['eta']).reshape(-1).detach().numpy()
+    fc1 = model1.fcut_of(p1).reshape(-1).detach().numpy()
+    fc2 = model2.fcut_of(p2).reshape(-1).detach().numpy()
     fu = np.where(fc1 > fc2, fc1, fc2)
     if det.fmax is not None:
         fu = np.where(fu > det.fmax, det.fmax, fc1)

@@ -8,6 +8,10 @@ stand-in modules before importing it:
 * ``jax.jacrev`` is a 5-point central finite difference (only used for the Fisher
   golden; its rounding through the ~1e5-rad phase limits that golden, see the tests);
 * ``jax.vmap`` loops over the leading (event) axis;
+* ``jax.custom_jvp`` calls the function; for a function whose tangents gwfast gives with
+  ``defjvps`` (the Planck taper of IMRPhenomD_NRTidalv2, with no tangent in its first argument),
+  the perturbed evaluations of the finite differences return the unperturbed value plus those
+  registered tangents times the argument changes, so the differences follow the same rule;
 * ``h5py`` / ``numdifftools`` are empty modules (only touched off the hot path).
 
 numpy 2 removed ``trapz`` and scipy removed ``cumtrapz``; aliases to
@@ -27,6 +31,12 @@ OUT = os.path.dirname(os.path.abspath(__file__))
 
 
 # ------------------------------------------------------------------ stand-in modules
+# finite-difference state shared by the jacrev and custom_jvp stand-ins: 'record' stores the
+# arguments and value of every defjvps custom_jvp call of the unperturbed evaluation, 'replay'
+# linearises the perturbed calls, in call order, about them
+_FD = {'mode': None, 'store': [], 'i': 0, 'lam_h': None}
+
+
 def _install_shims():
     jax = types.ModuleType('jax')
     jax.numpy = np
@@ -58,9 +68,14 @@ def _install_shims():
                 # large enough to keep the rounding of the ~1e5-rad phase out of the difference and
                 # small enough that the phase change stays << 1 rad at the top of the band
                 # (d Phi / d deltaLambda ~ sqrt(1 - 4 eta) v^7 is far smaller than d Phi / d LambdaTilde).
+                # IMRPhenomD_NRTidalv2 is not linear in them (the spin-induced moments depend on
+                # Lambda1, Lambda2 through exp(poly(log Lambda))) and its events include stars with
+                # Lambda < 1: there a fixed small step (_FD['lam_h']) keeps both Lambdas positive.
                 # The rest: 1e-6.
                 if j in (1, 2):
                     h = 1e-7 * max(abs(float(xr)), 1e-1)
+                elif j in (16, 17) and _FD['lam_h'] is not None:
+                    h = _FD['lam_h']
                 elif j == 16:
                     h = 1e-3 * max(abs(float(xr)), 1.)
                 elif j == 17:
@@ -70,8 +85,13 @@ def _install_shims():
                 def at(d):
                     a = list(args)
                     a[j] = x + d
+                    _FD['i'] = 0
                     return np.asarray(fn(*a))
+                _FD['mode'], _FD['store'] = 'record', []
+                at(0.)
+                _FD['mode'] = 'replay'
                 d1 = (-at(2 * h) + 8 * at(h) - 8 * at(-h) + at(-2 * h)) / (12 * h)
+                _FD['mode'] = None
                 res.append(d1)
             return tuple(res) if isinstance(argnums, tuple) else res[0]
         return run
@@ -84,12 +104,28 @@ def _install_shims():
     class custom_jvp:
         def __init__(self, fun, nondiff_argnums=()):
             self.fun = fun
+            self.jvps = None
 
         def defjvp(self, jvp):
             return jvp
 
+        def defjvps(self, *jvps):
+            self.jvps = jvps
+
         def __call__(self, *a, **k):
-            return self.fun(*a, **k)
+            if self.jvps is None or _FD['mode'] is None:
+                return self.fun(*a, **k)
+            if _FD['mode'] == 'record':
+                out = self.fun(*a, **k)
+                _FD['store'].append((a, out))
+                return out
+            a0, out0 = _FD['store'][_FD['i']]
+            _FD['i'] += 1
+            out = out0
+            for q, jv in enumerate(self.jvps):
+                if jv is not None:
+                    out = out + jv(a[q] - a0[q], out0, *a0)
+            return out
     jax.custom_jvp = custom_jvp
     interp = types.ModuleType('jax.interpreters')
     interp.xla = types.ModuleType('jax.interpreters.xla')
@@ -241,6 +277,18 @@ def main():
     ev['LambdaTilde'], ev['deltaLambda'] = UT.Lamt_delLam_from_Lam12(ev['Lambda1'], ev['Lambda2'], ev['eta'])
     make_case('tf2tidal_T_earth', WF.TaylorF2_RestrictedPN(is_tidal=True), {'ETS': (5., True), 'Virgo': (10., True)},
               ev, 300)
+    # IMRPhenomD_NRTidalv2: spins up to 0.3 so that the quadrupole-moment terms matter, one event
+    # with Lambda < 1 on one star (the polynomial branch of the quadrupole-moment relation)
+    rng = np.random.default_rng(1005)
+    ev = events_bns(rng, 4)
+    ev['chi1z'] = rng.uniform(-.3, .3, 4)
+    ev['chi2z'] = rng.uniform(-.3, .3, 4)
+    ev['Lambda1'] = np.array([150., 800., 400., 0.6])
+    ev['Lambda2'] = np.array([300., 1500., 0.4, 250.])
+    ev['LambdaTilde'], ev['deltaLambda'] = UT.Lamt_delLam_from_Lam12(ev['Lambda1'], ev['Lambda2'], ev['eta'])
+    _FD['lam_h'] = 2e-2
+    make_case('nrt_net_earth', WF.IMRPhenomD_NRTidalv2(), {'L1': (10., True), 'ETS': (5., True)}, ev, 300)
+    _FD['lam_h'] = None
     # KAT from the reference tutorial: GW170817-like TF2 Schwarzschild cut frequency 1590.1 Hz
     z = 0.00980
     ev = {'Mc': np.array([1.1859 * (1. + z)]), 'eta': np.array([0.24786618323504223])}
