@@ -14,8 +14,8 @@ stand-in modules before importing it:
   registered tangents times the argument changes, so the differences follow the same rule;
 * ``h5py`` / ``numdifftools`` are empty modules (only touched off the hot path).
 
-numpy 2 removed ``trapz`` and scipy removed ``cumtrapz``; aliases to
-``trapezoid``/``cumulative_trapezoid`` are installed for the reference's calls.
+numpy 2 removed ``trapz`` and ``NaN`` and scipy removed ``cumtrapz``; aliases to
+``trapezoid``/``nan``/``cumulative_trapezoid`` are installed for the reference's calls.
 
 The outputs are written to ``tests/golden/*.npz`` and committed; the GPU machine
 never needs the reference.  Run:  python tests/golden/make_golden.py [/root/reference]
@@ -142,6 +142,7 @@ def _install_shims():
     sys.modules['numdifftools'] = ndt
     sys.modules['numdifftools.step_generators'] = sg
     np.trapz = np.trapezoid
+    np.NaN = np.nan
     import scipy.integrate as igt
     igt.cumtrapz = igt.cumulative_trapezoid
 
@@ -257,6 +258,60 @@ def make_case(name, wf, dets, events, res, fisher=True):
     print('wrote', name, sorted(out.keys())[:6], '...')
 
 
+def make_gw170817():
+    """Known answer of gwfast's tutorial (notebooks/gwfast_tutorial.ipynb, 'COMPLETE EXAMPLE: GW170817'):
+    IMRPhenomD_NRTidalv2, L1 + H1 + Virgo with the O2 ASDs shipped in psds/LVC_O1O2O3, fmin 10 Hz,
+    no Earth rotation, default resolution; published network SNR 33.16 and, after fixing
+    deltaLambda, a 90 % sky area of 19.9 deg^2. The event is the tutorial's as it prints it (dL from
+    Planck18 and tcoal from the GPS time need astropy, which is not installed). Stores the ASD
+    tables, gwfast's own SNRs, Fisher matrix (finite-difference stand-in for jacrev) and sky area."""
+    import gwfast.fisherTools as FT
+    import gwfast.gwfastUtils as UT
+    base = os.path.join(REF, 'psds', 'LVC_O1O2O3')
+    files = {'L1': '2017-08-06_DCH_C02_L1_O2_Sensitivity_strain_asd.txt',
+             'H1': '2017-06-10_DCH_C02_H1_O2_Sensitivity_strain_asd.txt',
+             'Virgo': 'Hrec_hoft_V1O2Repro2A_16384Hz.txt'}
+    ev = {'Mc': np.array([1.1859 * (1. + 0.00980)]), 'dL': np.array([0.04374755]),
+          'theta': np.array([np.pi / 2. + 0.4080839999999999]), 'phi': np.array([3.4461599999999994]),
+          'iota': np.array([2.545065595974997]), 'psi': np.array([0.]), 'tcoal': np.array([0.43432288]),
+          'eta': np.array([0.24786618323504223]), 'Phicoal': np.array([0.]),
+          'chi1z': np.array([0.005136138323169717]), 'chi2z': np.array([0.003235146993487445]),
+          'Lambda1': np.array([368.17802383555687]), 'Lambda2': np.array([586.5487031450857])}
+    out = {'ev_' + k: v for k, v in ev.items()}
+    sigs = {}
+    for d, fn in files.items():
+        path = os.path.join(base, fn)
+        tab = np.loadtxt(path, usecols=(0, 1))
+        # the frequency columns are uniform grids of binary fractions: stored as (f0, df, n), exactly
+        f0, df, n = tab[0, 0], tab[1, 0] - tab[0, 0], tab.shape[0]
+        assert np.array_equal(tab[:, 0], f0 + df * np.arange(n))
+        out['asd_grid_' + d], out['asd_' + d] = np.array([f0, df, n]), tab[:, 1].copy()
+        g = glob.detectors[d]
+        sigs[d] = SIG.GWSignal(WF.IMRPhenomD_NRTidalv2(), psd_path=path, detector_shape=g['shape'], det_lat=g['lat'],
+                               det_long=g['long'], det_xax=g['xax'], verbose=False, is_ASD=True,
+                               useEarthMotion=False, fmin=10.)
+    net = NET.DetNet(sigs, verbose=False)
+    for k, v in net.SNR(dict(ev), return_all=True).items():
+        out['snr_' + k] = np.asarray(v)
+    out['snr_net'] = np.asarray(net.SNR(dict(ev)))
+    # the amplitude at the grid end, where the taper is 0 or 1 by rounding (same on every detector's grid)
+    wf = WF.IMRPhenomD_NRTidalv2()
+    evt = dict(ev)
+    evt['LambdaTilde'], evt['deltaLambda'] = UT.Lamt_delLam_from_Lam12(ev['Lambda1'], ev['Lambda2'], ev['eta'])
+    fc = wf.fcut(**evt)
+    fg = np.geomspace(np.full(fc.shape, 10.), fc, num=1000)
+    out['ampl_last'] = np.asarray(wf.Ampl(fg, **evt)[-1])
+    F = net.FisherMatr(dict(ev))
+    out['fisher_net'] = np.asarray(F)
+    pn = WF.IMRPhenomD_NRTidalv2().ParNums
+    Ff, pf = FT.fixParams(F, pn, ['deltaLambda'])
+    cov, _ = FT.CovMatr(Ff)
+    # gwfast's CovMatr returns long doubles, whose layout differs between x86 and Arm: store float64
+    out['sky_area'] = np.asarray(FT.compute_localization_region(cov, pf, ev['theta']), dtype=np.float64)
+    np.savez_compressed(os.path.join(OUT, 'kat_gw170817.npz'), **out)
+    print('wrote kat_gw170817: SNR %.4f, sky area %.2f deg^2' % (out['snr_net'][0], out['sky_area'][0]))
+
+
 def main():
     rng = np.random.default_rng(1000)
     make_case('tf2_L_noearth', WF.TaylorF2_RestrictedPN(), {'Virgo': (10., False)}, events_bns(rng, 4), 400)
@@ -289,6 +344,7 @@ def main():
     _FD['lam_h'] = 2e-2
     make_case('nrt_net_earth', WF.IMRPhenomD_NRTidalv2(), {'L1': (10., True), 'ETS': (5., True)}, ev, 300)
     _FD['lam_h'] = None
+    make_gw170817()
     # KAT from the reference tutorial: GW170817-like TF2 Schwarzschild cut frequency 1590.1 Hz
     z = 0.00980
     ev = {'Mc': np.array([1.1859 * (1. + z)]), 'eta': np.array([0.24786618323504223])}

@@ -119,3 +119,41 @@ def test_nrtidal_fp32_is_rejected(gpu_lib):
     net = synthetic.make_network(W.IMRPhenomD_NRTidalv2(), dets=(('L1', 10.),), earth=False)
     with pytest.raises(_lib.GWFError):
         net.FisherMatr(dict(ev), res=100, precision='fp32')
+
+
+def test_kat_gw170817(gpu_lib):
+    """gwfast's GW170817 example: IMRPhenomD_NRTidalv2, L1 + H1 + Virgo with the O2 ASD tables, fmin
+    10 Hz, no Earth rotation, default resolution: network SNR 33.16 and, with deltaLambda fixed, a
+    90 % sky area of 19.9 deg^2. The SNRs are compared with gwfast's own to 1e-6 (the last-point
+    taper, 0 or 1 by rounding, is worth ~1e-7 of the SNR), the Fisher matrix with the oracle."""
+    from gwfast_gb300 import gwfastGlobals as glob
+    from gwfast_gb300.network import DetNet
+    from gwfast_gb300.signal import GWSignal
+    from test_oracle_golden import gw170817
+    g, ev, tabs = gw170817()
+    sigs = {}
+    for d, (f, asd) in tabs.items():
+        c = glob.detectors[d]
+        sigs[d] = GWSignal(W.IMRPhenomD_NRTidalv2(), psd_path=(f, asd), detector_shape=c['shape'], det_lat=c['lat'],
+                           det_long=c['long'], det_xax=c['xax'], verbose=False, is_ASD=True, useEarthMotion=False,
+                           fmin=10.)
+    net = DetNet(sigs, verbose=False)
+    snrs = net.SNR(dict(ev), return_all=True)
+    for d in tabs:
+        assert abs(snrs[d][0] - g['snr_' + d][0]) < 1e-6 * g['snr_' + d][0], d
+    snr = net.SNR(dict(ev))
+    assert abs(snr[0] - g['snr_net'][0]) < 1e-6 * snr[0]
+    assert round(float(snr[0]), 2) == 33.16
+    evd = dict(ev)
+    F = net.FisherMatr(evd)
+    assert F.shape == (13, 13, 1)
+    p = O.to_params(evd, O.PARAMS_TIDAL)
+    dets = [O.Detector(*O.DETECTORS[d][:3], O.DETECTORS[d][3], fmin=10., psd_f=f, psd_S=asd * asd, earth=False)
+            for d, (f, asd) in tabs.items()]
+    Fo = oracle_both(lambda m: sum(O.fisher(det, m, p, 1000) for det in dets).numpy())
+    assert np.minimum(*(fisher_err_per_event(np.moveaxis(F, -1, 0), x) for x in Fo)).max() < F_TOL
+    Ff, pf = fisherTools.fixParams(F, W.IMRPhenomD_NRTidalv2().ParNums, ['deltaLambda'])
+    cov, _ = fisherTools.CovMatr(Ff)
+    area = fisherTools.compute_localization_region(cov, pf, ev['theta'])
+    assert abs(area[0] - g['sky_area'][0]) < 2e-3 * g['sky_area'][0]
+    assert round(float(area[0]), 1) == 19.9

@@ -132,3 +132,56 @@ def test_identities(name):
     dL = p['dL'].reshape(-1)
     assert np.allclose(F[:, 2, 2], (snr / dL) ** 2, rtol=1e-12)
     assert np.allclose(F[:, 8, 8], snr ** 2, rtol=1e-12)
+
+
+def gw170817():
+    """The GW170817 example of gwfast's tutorial: event, O2 ASD tables, gwfast's own outputs."""
+    g = np.load(os.path.join(GOLD, 'kat_gw170817.npz'))
+    ev = {k[3:]: g[k] for k in g.files if k.startswith('ev_')}
+    tabs = {}
+    for d in ('L1', 'H1', 'Virgo'):
+        f0, df, n = g['asd_grid_' + d]
+        tabs[d] = (f0 + df * np.arange(int(n)), g['asd_' + d])
+    return g, ev, tabs
+
+
+def test_kat_gw170817_oracle():
+    """Network SNR 33.16 and, with deltaLambda fixed, a 90 % sky area of 19.9 deg^2
+    (gwfast_tutorial, IMRPhenomD_NRTidalv2, L1 + H1 + Virgo at O2 sensitivity, no Earth rotation).
+
+    The grid ends where M f = 1.2 f_merger, and the taper there is 1 or 0 by rounding: gwfast's SNR
+    path evaluates the amplitude with the Lambda1, Lambda2 it was given (for this event that point
+    is 1, ``ampl_last``), its Fisher path with the pair recovered from (LambdaTilde, deltaLambda)
+    (there it falls to 0). Both branches are checked against the matching output."""
+    from gwfast_gb300 import fisherTools as FT
+    from gwfast_gb300 import gwfastUtils as U
+    from gwfast_gb300 import waveforms as W
+    g, ev, tabs = gw170817()
+    U.fill_tidal(ev)
+    dets = []
+    for d, (f, asd) in tabs.items():
+        lat, lon, xax, sh = O.DETECTORS[d]
+        dets.append(O.Detector(lat, lon, xax, sh, fmin=10., psd_f=f, psd_S=asd * asd, earth=False))
+    m_snr = O.Model('PhenomD_NRTidalv2', taper_last=g['ampl_last'] != 0.)
+    p = O.to_params(ev, m_snr.params)
+    snrs = [float(O.snr(det, m_snr, p, 1000)[0]) for det in dets]
+    for d, s in zip(tabs, snrs):
+        assert abs(s - float(g['snr_' + d][0])) < 1e-12 * s, d
+    net = float(np.sqrt(sum(s * s for s in snrs)))
+    assert abs(net - float(g['snr_net'][0])) < 1e-12 * net
+    assert round(net, 2) == 33.16
+    Fr = g['fisher_net'][..., 0]
+    dg = np.sqrt(np.abs(np.diag(Fr)))
+    errs, areas = [], []
+    for last in (False, True):
+        model = O.Model('PhenomD_NRTidalv2', taper_last=np.array([last]))
+        F = sum(O.fisher(det, model, p, 1000) for det in dets).numpy()[0]
+        errs.append((np.abs(F - Fr) / np.outer(dg, dg)).max())
+        Ff, pf = FT.fixParams(F[:, :, None], W.IMRPhenomD_NRTidalv2().ParNums, ['deltaLambda'])
+        cov, _ = O.cov_matr_fast(np.moveaxis(Ff, -1, 0))
+        areas.append(float(FT.compute_localization_region(np.moveaxis(cov, 0, -1), pf, ev['theta'])[0]))
+    # finite-difference golden: ~1e-4 of sqrt(F_aa F_bb), as for the other Fisher goldens
+    assert min(errs) < 5e-4, errs
+    for a in areas:
+        assert abs(a - float(g['sky_area'][0])) < 2e-3 * a
+        assert round(a, 1) == 19.9
