@@ -15,6 +15,9 @@ GWF_OK = 0
 ERRORS = {-1: 'invalid argument', -2: 'CUDA error', -3: 'out of memory', -4: 'timeout', -5: 'unsupported'}
 MODEL_IDS = {'TaylorF2_RestrictedPN': 0, 'IMRPhenomD': 1, 'IMRPhenomHM': 2, 'IMRPhenomD_NRTidalv2': 4}
 MODEL_TF2_TIDAL = 3
+MODEL_TF2_ECC = 5
+MODEL_TF2_TIDAL_ECC = 6
+TF2_PHIREF_VLSO, TF2_KERR_ISCO, TF2_QUADMON_TIDAL = 1, 2, 4   # gwf_wf_desc.flags
 MEM_HOST, MEM_DEVICE = 0, 1
 PRECISION = {'fp64': 0, 'fp32': 1, 'mixed': 2}
 
@@ -30,7 +33,8 @@ class DetDesc(ctypes.Structure):
 
 
 class WfDesc(ctypes.Structure):
-    _fields_ = [('model', ctypes.c_int), ('spin_ho', ctypes.c_int), ('fcut_par', ctypes.c_double)]
+    _fields_ = [('model', ctypes.c_int), ('spin_ho', ctypes.c_int), ('fcut_par', ctypes.c_double),
+                ('flags', ctypes.c_int), ('reserved', ctypes.c_int), ('fref_ecc', ctypes.c_double)]
 
 
 _P = ctypes.POINTER

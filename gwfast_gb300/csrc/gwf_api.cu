@@ -117,8 +117,73 @@ struct gwf_ctx {
 
 namespace {
 
-// Fisher parameters of a waveform model: 11, or 13 for the tidal TaylorF2 (LambdaTilde, deltaLambda)
-int npar_of(int model) { return model >= GWF_WF_TAYLORF2_TIDAL ? 13 : 11; }
+// Fisher parameters of a waveform model: 11; 13 for the tidal models (LambdaTilde, deltaLambda); the
+// eccentric TaylorF2 adds ecc (12, or 14 with the tidal terms)
+int npar_of(int model) {
+  return model == GWF_WF_TAYLORF2_ECC ? 12 : (model == GWF_WF_TAYLORF2_TIDAL_ECC ? 14 : (model >= GWF_WF_TAYLORF2_TIDAL ? 13 : 11));
+}
+
+// per-model entry points of the FP64 launch code (one translation unit per model)
+size_t setup_stride_any(int model) {
+  switch (model) {
+    case 0: return gwf::setup_stride_m0();
+    case 1: return gwf::setup_stride_m1();
+    case 2: return gwf::setup_stride_m2();
+    case 3: return gwf::setup_stride_m3();
+    case 4: return gwf::setup_stride_m4();
+    case 5: return gwf::setup_stride_m5();
+    default: return gwf::setup_stride_m6();
+  }
+}
+size_t core_bytes_any(int model) {
+  switch (model) {
+    case 0: return gwf::core_bytes_m0();
+    case 1: return gwf::core_bytes_m1();
+    case 2: return gwf::core_bytes_m2();
+    case 3: return gwf::core_bytes_m3();
+    case 4: return gwf::core_bytes_m4();
+    case 5: return gwf::core_bytes_m5();
+    default: return gwf::core_bytes_m6();
+  }
+}
+cudaError_t launch_fisher_any(int model, const gwf::LaunchArgs& a) {
+  switch (model) {
+    case 0: return gwf::launch_fisher_m0(a);
+    case 1: return gwf::launch_fisher_m1(a);
+    case 2: return gwf::launch_fisher_m2(a);
+    case 3: return gwf::launch_fisher_m3(a);
+    case 4: return gwf::launch_fisher_m4(a);
+    case 5: return gwf::launch_fisher_m5(a);
+    default: return gwf::launch_fisher_m6(a);
+  }
+}
+cudaError_t launch_snr_any(int model, const gwf::LaunchArgs& a) {
+  switch (model) {
+    case 0: return gwf::launch_snr_m0(a);
+    case 1: return gwf::launch_snr_m1(a);
+    case 2: return gwf::launch_snr_m2(a);
+    case 3: return gwf::launch_snr_m3(a);
+    case 4: return gwf::launch_snr_m4(a);
+    case 5: return gwf::launch_snr_m5(a);
+    default: return gwf::launch_snr_m6(a);
+  }
+}
+
+bool is_tf2_model(int model) {
+  return model == GWF_WF_TAYLORF2 || model == GWF_WF_TAYLORF2_TIDAL || model == GWF_WF_TAYLORF2_ECC ||
+         model == GWF_WF_TAYLORF2_TIDAL_ECC;
+}
+
+gwf::WfDesc wf_dev(const gwf_wf_desc* wf) {
+  gwf::WfDesc w;
+  w.model = wf->model;
+  w.spin_ho = wf->spin_ho;
+  w.fcut_par = wf->fcut_par;
+  w.flags = wf->flags;
+  w.pad_ = 0;
+  w.fref_ecc = wf->fref_ecc;
+  return w;
+}
 
 int check_ctx(gwf_ctx* ctx) {
   if (!ctx) return fail(GWF_ERR_INVALID_ARG, "null context");
@@ -160,7 +225,13 @@ int validate_common(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_de
   if (!det_ids || n_det < 1) return fail(GWF_ERR_INVALID_ARG, "need at least one detector");
   for (int i = 0; i < n_det; ++i)
     if (det_ids[i] < 0 || det_ids[i] >= (int)ctx->dets.size()) return fail(GWF_ERR_INVALID_ARG, "unknown detector id");
-  if (!wf || wf->model < 0 || wf->model > 4) return fail(GWF_ERR_INVALID_ARG, "unknown waveform model");
+  if (!wf || wf->model < 0 || wf->model > GWF_WF_TAYLORF2_TIDAL_ECC) return fail(GWF_ERR_INVALID_ARG, "unknown waveform model");
+  if (wf->flags & ~(GWF_TF2_PHIREF_VLSO | GWF_TF2_KERR_ISCO | GWF_TF2_QUADMON_TIDAL))
+    return fail(GWF_ERR_INVALID_ARG, "unknown waveform flags");
+  if (wf->flags && !is_tf2_model(wf->model))
+    return fail(GWF_ERR_INVALID_ARG, "waveform flags apply to the TaylorF2 models only");
+  if ((wf->flags & GWF_TF2_QUADMON_TIDAL) && wf->model != GWF_WF_TAYLORF2_TIDAL && wf->model != GWF_WF_TAYLORF2_TIDAL_ECC)
+    return fail(GWF_ERR_INVALID_ARG, "GWF_TF2_QUADMON_TIDAL needs a tidal TaylorF2 model");
   if ((wf->model == GWF_WF_PHENOMD || wf->model == GWF_WF_PHENOMD_NRTIDALV2) && ctx->nq < 2)
     return fail(GWF_ERR_INVALID_ARG, "IMRPhenomD needs the QNM table (gwf_set_qnm_table)");
   if (!(wf->fcut_par > 0.0)) return fail(GWF_ERR_INVALID_ARG, "fcut_par must be positive");
@@ -467,10 +538,7 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
     if (ctx->onet.ensure((size_t)N * per * sizeof(double))) return fail(GWF_ERR_OOM, "device allocation failed (out)");
     dnet = (double*)ctx->onet.p;
   }
-  const size_t stride = wf->model == 0 ? gwf::setup_stride_m0()
-                        : (wf->model == 1 ? gwf::setup_stride_m1()
-                                          : (wf->model == 2 ? gwf::setup_stride_m2()
-                                                            : (wf->model == 3 ? gwf::setup_stride_m3() : gwf::setup_stride_m4())));
+  const size_t stride = setup_stride_any(wf->model);
   const size_t chunk = (size_t)(N < gwf::kChunk ? N : gwf::kChunk);
   // FP32 network totals: detectors with the same grid (fmin, fmax, Earth rotation) form groups
   // that one launch evaluates together (the waveform once per point for the whole group)
@@ -495,10 +563,7 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   for (auto& g : groups) gmax = g.size() > gmax ? g.size() : gmax;
   if (ctx->setup.ensure(gmax * chunk * stride)) return fail(GWF_ERR_OOM, "device allocation failed (set-up scratch)");
   // a network shares the source-dependent part of the per-event set-up between its detectors
-  const size_t core_b = wf->model == 0 ? gwf::core_bytes_m0()
-                        : (wf->model == 1 ? gwf::core_bytes_m1()
-                                          : (wf->model == 2 ? gwf::core_bytes_m2()
-                                                            : (wf->model == 3 ? gwf::core_bytes_m3() : gwf::core_bytes_m4())));
+  const size_t core_b = core_bytes_any(wf->model);
   const bool share = n_det > 1 && ctx->core.ensure((size_t)N * core_b) == 0;
   // the scratch is shared by every call on this context: order this call after the previous one
   if (!capturing) GWF_CK(cudaStreamWaitEvent(st, ctx->scratch_free, 0));
@@ -520,9 +585,7 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   a.ev.res = res;
   a.ev.res_ev = dres;
   a.ev.spacing = spacing;
-  a.wf.model = wf->model;
-  a.wf.spin_ho = wf->spin_ho;
-  a.wf.fcut_par = wf->fcut_par;
+  a.wf = wf_dev(wf);
   a.qnm = ctx->d_qnm;
   a.nq = ctx->nq;
   a.per_arm = per_arm || dsda;   // per-arm SNR derivatives need the per-arm Gram sets
@@ -558,16 +621,7 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
     a.out_arm = darm ? darm + (size_t)slot * N * per : nullptr;
     a.out_sd_arm = dsda ? dsda + (size_t)slot * N * npar : nullptr;
     a.out_sd_det = dsdn;
-    if (fisher)
-      err = wf->model == 0 ? gwf::launch_fisher_m0(a)
-            : (wf->model == 1 ? gwf::launch_fisher_m1(a)
-                              : (wf->model == 2 ? gwf::launch_fisher_m2(a)
-                                                : (wf->model == 3 ? gwf::launch_fisher_m3(a) : gwf::launch_fisher_m4(a))));
-    else
-      err = wf->model == 0 ? gwf::launch_snr_m0(a)
-            : (wf->model == 1 ? gwf::launch_snr_m1(a)
-                              : (wf->model == 2 ? gwf::launch_snr_m2(a)
-                                                : (wf->model == 3 ? gwf::launch_snr_m3(a) : gwf::launch_snr_m4(a))));
+    err = fisher ? launch_fisher_any(wf->model, a) : launch_snr_any(wf->model, a);
     if (err != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(err));
     slot += r.desc.shape == GWF_SHAPE_T ? 3 : 1;
   }
@@ -597,19 +651,11 @@ __global__ void fcut_pair_kernel(const double* p1, long long ld1, gwf::WfDesc w1
                                  gwf::WfDesc w2, double fmax, long long N, double* out) {
   const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= N) return;
-  const double f1 = gwf::model_fcut(w1, p1[n], p1[ld1 + n]);
-  const double f2 = gwf::model_fcut(w2, p2[n], p2[ld2 + n]);
+  const double f1 = gwf::model_fcut(w1, p1[n], p1[ld1 + n], p1[9 * ld1 + n], p1[10 * ld1 + n]);
+  const double f2 = gwf::model_fcut(w2, p2[n], p2[ld2 + n], p2[9 * ld2 + n], p2[10 * ld2 + n]);
   double fu = f1 > f2 ? f1 : f2;
   if (fmax > 0.0) fu = fu > fmax ? fmax : f1;
   out[n] = fu;
-}
-
-gwf::WfDesc wf_dev(const gwf_wf_desc* wf) {
-  gwf::WfDesc w;
-  w.model = wf->model;
-  w.spin_ho = wf->spin_ho;
-  w.fcut_par = wf->fcut_par;
-  return w;
 }
 
 size_t stride_of(int model) {
@@ -1053,7 +1099,8 @@ int gwf_cov_n(gwf_ctx* ctx, const double* F, int64_t N, int n_params, int mem, d
               void* stream) {
   int rc = check_ctx(ctx);
   if (rc) return rc;
-  if (n_params != 11 && n_params != 13) return fail(GWF_ERR_INVALID_ARG, "n_params must be 11 or 13");
+  if (n_params != 11 && n_params != 13 && n_params != 14)
+    return fail(GWF_ERR_INVALID_ARG, "n_params must be 11, 13 or 14");
   if (N < 0 || (N > 0 && (!F || !cov))) return fail(GWF_ERR_INVALID_ARG, "bad covariance arguments");
   if (mem != GWF_MEM_HOST && mem != GWF_MEM_DEVICE) return fail(GWF_ERR_INVALID_ARG, "bad memory mode");
   if (N == 0) return GWF_OK;

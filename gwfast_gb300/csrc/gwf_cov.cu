@@ -146,7 +146,8 @@ cudaError_t launch_cov(const double* F, long long N, double* cov, double* eps, d
   if (N <= 0) return cudaSuccess;
   const int bs = 64;
   const long long nb = (N + bs - 1) / bs;
-  if (np == 13) cov_kernel<13><<<(unsigned)nb, bs, 0, st>>>(F, N, cov, eps, cond);
+  if (np == 14) cov_kernel<14><<<(unsigned)nb, bs, 0, st>>>(F, N, cov, eps, cond);
+  else if (np == 13) cov_kernel<13><<<(unsigned)nb, bs, 0, st>>>(F, N, cov, eps, cond);
   else if (np == 11) cov_kernel<11><<<(unsigned)nb, bs, 0, st>>>(F, N, cov, eps, cond);
   else return cudaErrorInvalidValue;
   return cudaGetLastError();

@@ -22,7 +22,15 @@ constexpr int NE = 66;    // upper-triangle entries
 enum { I_MC = 0, I_ETA, I_DL, I_TH, I_PH, I_IO, I_PS, I_TC, I_PC, I_C1, I_C2, I_LT, I_DLT };
 
 // Fisher parameters of a model, upper-triangle entries, entries plus strain products, entry index
-template <int MODEL> __host__ __device__ constexpr int np_of() { return MODEL >= 3 ? 13 : 11; }
+// Fisher parameters: 11; the tidal models (3, 4) add LambdaTilde, deltaLambda; the eccentric
+// TaylorF2 adds ecc after them (5: 12 parameters, 6: with the tidal terms, 14)
+template <int MODEL> __host__ __device__ constexpr int np_of() {
+  return MODEL == 5 ? 12 : (MODEL == 6 ? 14 : (MODEL >= 3 ? 13 : 11));
+}
+template <int MODEL> __host__ __device__ constexpr bool is_tf2() { return MODEL == 0 || MODEL == 3 || MODEL >= 5; }
+template <int MODEL> __host__ __device__ constexpr bool has_tidal() { return MODEL == 3 || MODEL == 4 || MODEL == 6; }
+template <int MODEL> __host__ __device__ constexpr bool has_ecc() { return MODEL >= 5; }
+template <int MODEL> __host__ __device__ constexpr int ecc_col() { return MODEL == 6 ? 13 : 11; }
 // intrinsic tangent directions of the per-event duals: Mc, eta, chi1z, chi2z (+ LambdaTilde,
 // deltaLambda for IMRPhenomD_NRTidalv2, model 4, whose set-up depends on them non-linearly)
 template <int MODEL> __host__ __device__ constexpr int ndir_of() { return MODEL == 4 ? 6 : 4; }
@@ -66,9 +74,13 @@ struct EvBatch {
 };
 
 struct WfDesc {
-  int model;             // 0 = TaylorF2, 1 = IMRPhenomD, 2 = IMRPhenomHM
+  int model;             // 0 = TaylorF2, 1 = IMRPhenomD, 2 = IMRPhenomHM, 3 = tidal TaylorF2,
+                         // 4 = IMRPhenomD_NRTidalv2, 5 = eccentric TaylorF2, 6 = tidal eccentric TaylorF2
   int spin_ho;
   double fcut_par;       // TaylorF2: fHigh in Hz; IMR: cut in Mf
+  int flags;             // TaylorF2 options: kTF2Vlso | kTF2KerrIsco | kTF2QuadMon
+  int pad_;
+  double fref_ecc;       // eccentric TaylorF2: reference frequency of ecc in Hz (<= 0: lowest grid frequency)
 };
 
 static __constant__ unsigned char kPairA[NE] = {0,0,0,0,0,0,0,0,0,0,0,1,1,1,1,1,1,1,1,1,1,2,2,2,2,2,2,2,2,2,3,3,3,3,3,3,3,3,4,4,4,4,4,4,4,5,5,5,5,5,5,6,6,6,6,6,7,7,7,7,8,8,8,9,9,10};
@@ -247,17 +259,55 @@ union EvUnion {
   HMEv hm;
   TF2TEv tf2t;
   NRTEv nrt;
+  TF2EEv tf2e;
 };
 
-// upper grid frequency of the model (gwfast/waveforms.py:903-920, :1324-1333, :2737-2750)
-__host__ __device__ inline double model_fcut(const WfDesc& wf, double Mc, double eta) {
-  // TaylorF2 (models 0 and 3): fcut_par is fHigh in Hz Msun; the IMR models: a cut in M f
-  return (wf.model == 0 || wf.model == 3) ? wf.fcut_par / (Mc / pow(eta, 0.6)) : wf.fcut_par / (Mc * kG3 / pow(eta, 0.6));
+// Kerr ISCO radius (prograde for chi > 0), gwfast/waveforms.py:934-937
+__host__ __device__ inline double r_isco_kerr(double chi) {
+  const double z1 = 1.0 + cbrt(1.0 - chi * chi) * (cbrt(1.0 + chi) + cbrt(1.0 - chi));
+  const double z2 = sqrt(3.0 * chi * chi + z1 * z1);
+  const double r = sqrt((3.0 - z1) * (3.0 + z1 + 2.0 * z2));
+  return chi > 0.0 ? 3.0 + z2 - r : 3.0 + z2 + r;
+}
+
+// twice the ISCO frequency of the Kerr remnant (gwfast/waveforms.py:921-951: final spin and mass from
+// the fits of arXiv:1605.01938, arXiv:2108.05861 App. C), in Hz
+__host__ __device__ inline double tf2_kerr_fcut(double Mc, double eta, double chi1, double chi2) {
+  const double eta2 = eta * eta;
+  const double Mtot = Mc / pow(eta, 0.6);
+  const double sv = eta < 0.25 ? sqrt(1.0 - 4.0 * eta) : 0.0;
+  const double m1 = 0.5 * (1.0 + sv), m2 = 0.5 * (1.0 - sv);
+  const double s = (m1 * m1 * chi1 + m2 * m2 * chi2) / (m1 * m1 + m2 * m2);
+  const double q = m2 / m1;
+  const double atot = (chi1 + chi2 * q * q) / ((1.0 + q) * (1.0 + q));
+  const double aeff = atot + 0.41616 * eta * (chi1 + chi2);
+  const double r_isco = r_isco_kerr(aeff);
+  const double ens = eta * (0.055974469826360077 + 0.5809510763115132 * eta - 0.9606726679372312 * eta2
+                            + 3.352411249771192 * eta2 * eta);
+  const double erad = ens * (1.0 + (-0.0030302335878845507 - 2.0066110851351073 * eta + 7.7050567802399215 * eta2) * s)
+                      / (1.0 + (-0.6714403054720589 - 1.4756929437702908 * eta + 7.304676214885011 * eta2) * s);
+  const double Mfin = Mtot * (1.0 - erad);
+  const double L = 2.0 / (3.0 * sqrt(3.0)) * (1.0 + 2.0 * sqrt(3.0 * r_isco - 2.0));
+  const double E = sqrt(1.0 - 2.0 / (3.0 * r_isco));
+  const double chif = atot + eta * (L - 2.0 * atot * (E - 1.0)) + (-3.821158961 - 1.2019 * aeff - 1.20764 * aeff * aeff) * eta2
+                      + (3.79245 + 1.18385 * aeff + 4.90494 * aeff * aeff) * eta2 * eta;
+  const double rf = r_isco_kerr(chif);
+  const double om = 1.0 / (rf * sqrt(rf) + chif);
+  return om / (kPi * Mfin * kG3);
+}
+
+// upper grid frequency of the model (gwfast/waveforms.py:903-951, :1324-1333, :2737-2750)
+__host__ __device__ inline double model_fcut(const WfDesc& wf, double Mc, double eta, double chi1 = 0.0,
+                                             double chi2 = 0.0) {
+  // TaylorF2 (models 0, 3, 5, 6): fcut_par is fHigh in Hz Msun, or the Kerr ISCO; the IMR models: a cut in M f
+  const bool tf2 = wf.model == 0 || wf.model == 3 || wf.model >= 5;
+  if (tf2 && (wf.flags & kTF2KerrIsco)) return tf2_kerr_fcut(Mc, eta, chi1, chi2);
+  return tf2 ? wf.fcut_par / (Mc / pow(eta, 0.6)) : wf.fcut_par / (Mc * kG3 / pow(eta, 0.6));
 }
 
 __device__ inline bool grid_setup(GridEv& g, const DetDev& d, const EvBatch& ev, const WfDesc& wf, long long n,
-                                  double Mc, double eta, double fcut_model = -1.0) {
-  double fcut = fcut_model >= 0.0 ? fcut_model : model_fcut(wf, Mc, eta);
+                                  double Mc, double eta, double fcut_model = -1.0, double chi1 = 0.0, double chi2 = 0.0) {
+  double fcut = fcut_model >= 0.0 ? fcut_model : model_fcut(wf, Mc, eta, chi1, chi2);
   if (d.fmax > 0.0 && fcut > d.fmax) fcut = d.fmax;
   if (ev.fcut_ev) fcut = ev.fcut_ev[n];
   const int R = ev.res_ev ? ev.res_ev[n] : ev.res;
@@ -297,21 +347,45 @@ __device__ __forceinline__ void grid_point(const GridEv& g, int spacing, int k, 
 template <int MODEL>
 __device__ inline void event_setup(EvUnion& E, const DetDev& d, const WfDesc& wf, const double* q, int nq,
                                    double Mc, double eta, double chi1, double chi2, double dL, double lam_t,
-                                   double del_lam) {
+                                   double del_lam, double ecc = 0.0) {
   const D4 mc = D4::seed(Mc, P_MC), et = D4::seed(eta, P_ETA), c1 = D4::seed(chi1, P_CHI1), c2 = D4::seed(chi2, P_CHI2);
   if (MODEL == 4) {
     nrt_setup(E.nrt, D6::seed(Mc, P_MC), D6::seed(eta, P_ETA), D6::seed(chi1, P_CHI1), D6::seed(chi2, P_CHI2), dL,
               d.fmin, q, q + nq, q + 2 * nq, nq, D6::seed(lam_t, P_LT), D6::seed(del_lam, P_DLT));
     return;
   }
-  if (MODEL == 3) tf2t_setup(E.tf2t, mc, et, c1, c2, dL, wf.spin_ho != 0, lam_t, del_lam);
-  else if (MODEL == 0) tf2_setup(E.tf2, mc, et, c1, c2, dL, wf.spin_ho != 0);
+  if (MODEL >= 5)
+    tf2e_setup(E.tf2e, mc, et, c1, c2, dL, wf.spin_ho != 0, lam_t, del_lam, wf.flags, ecc, d.fmin, wf.fref_ecc);
+  else if (MODEL == 3) tf2t_setup(E.tf2t, mc, et, c1, c2, dL, wf.spin_ho != 0, lam_t, del_lam, wf.flags);
+  else if (MODEL == 0) tf2_setup(E.tf2, mc, et, c1, c2, dL, wf.spin_ho != 0, wf.flags);
   else if (MODEL == 1) phd_setup(E.phd, mc, et, c1, c2, dL, d.fmin, q, q + nq, q + 2 * nq, nq);
   else hm_setup_core(E.hm, mc, et, c1, c2, dL, d.fmin);
 }
 
 // constant pi - pi/4 of the TaylorF2 phase (gwfast/waveforms.py:802, :862), left out of tf2_point
+// (with phiref_vlso the pi is absent: the strain outputs subtract it)
 constexpr double kTF2PhaseConst = 0.75 * kPi;
+
+// the TaylorF2 record of the TaylorF2 models (0, 3, 5, 6)
+template <int MODEL> __device__ __forceinline__ const TF2Ev& tf2_base(const EvUnion& E) {
+  return MODEL == 3 ? E.tf2t.b : (MODEL >= 5 ? E.tf2e.t.b : E.tf2);
+}
+template <int MODEL> __device__ __forceinline__ const TF2TEv& tf2_tidal(const EvUnion& E) {
+  return MODEL >= 5 ? E.tf2e.t : E.tf2t;
+}
+
+// TaylorF2 phase and amplitude of models 0, 3, 5, 6 at one point (tidal and eccentric parts added)
+template <int MODEL, class S>
+__device__ __forceinline__ void tf2_any_point(const EvUnion& E, double f, double f13, double lnf, S& A, S& Phi) {
+  const TF2Ev& t = tf2_base<MODEL>(E);
+  tf2_point<S>(t, f, f13, lnf, exp(lnf * (-7.0 / 6.0)), A, Phi);
+  if constexpr (has_tidal<MODEL>()) Phi = Phi + tf2_tidal_phase<S>(tf2_tidal<MODEL>(E), co<S>(t.vM) * f13);
+  if constexpr (has_ecc<MODEL>()) {
+    const S v = co<S>(t.vM) * f13;
+    const S lnv = co<S>(t.lnvM) + lnf * (1.0 / 3.0);
+    Phi = Phi + tf2_ecc_phase<S>(E.tf2e, v, lnv, lnf);
+  }
+}
 
 // waveform at one point: P, C (hp = P, hc = i C) with tangents, iota derivatives, and tau_star tangent.
 // phi0: the waveform phase left out of P and C (22-mode models: Phi(f); HM: 0, the mode phases are in P, C)
@@ -347,18 +421,17 @@ __device__ __forceinline__ void wave_point_dual(const EvUnion& E, const ProjEv& 
     dCi = {pj.dci * A.v, 0.0};
   } else {
     D4 A, Phi;
-    if (MODEL == 0 || MODEL == 3) {
-      const TF2Ev& t = MODEL == 3 ? E.tf2t.b : E.tf2;
+    if (is_tf2<MODEL>()) {
+      const TF2Ev& t = tf2_base<MODEL>(E);
       const double f13 = exp(lnf / 3.0);
-      tf2_point<D4>(t, f, f13, lnf, exp(lnf * (-7.0 / 6.0)), A, Phi);
-      if (MODEL == 3) Phi = Phi + tf2_tidal_phase<D4>(E.tf2t, t.vM * f13);
+      tf2_any_point<MODEL, D4>(E, f, f13, lnf, A, Phi);
       if (EARTH) tau = tau_star_point<D4>(t.Ms, t.vM, t.eta, f13);
     } else {
       phd_point<D4>(E.phd.k, f, A, Phi);
       if (EARTH) tau = tau_star_point<D4>(E.phd.k.Ms, E.phd.k.vM, E.phd.k.eta, exp(lnf / 3.0));
     }
     // W = A e^{-i Phi} with the common phase dropped: value A, tangent dA - i A dPhi
-    phi0 = Phi.v + ((MODEL == 0 || MODEL == 3) ? kTF2PhaseConst : 0.0);
+    phi0 = Phi.v + (is_tf2<MODEL>() ? kTF2PhaseConst : 0.0);
     P = {pj.cp * A.v, 0.0};
     C = {pj.ci * A.v, 0.0};
 #pragma unroll
@@ -388,11 +461,10 @@ __device__ __forceinline__ void wave_point_full(const EvUnion& E, const ProjEv& 
     if (MODEL == 4) {
       nrt_point<double>(E.nrt, f, A, Phi);
       if (EARTH) tau = tau_star_point<double>(E.nrt.k.Ms, E.nrt.k.vM, E.nrt.k.eta, exp(lnf / 3.0));
-    } else if (MODEL == 0 || MODEL == 3) {
-      const TF2Ev& t = MODEL == 3 ? E.tf2t.b : E.tf2;
+    } else if (is_tf2<MODEL>()) {
+      const TF2Ev& t = tf2_base<MODEL>(E);
       const double f13 = exp(lnf / 3.0);
-      tf2_point<double>(t, f, f13, lnf, exp(lnf * (-7.0 / 6.0)), A, Phi);
-      if (MODEL == 3) Phi += tf2_tidal_phase<double>(E.tf2t, t.vM.v * f13);
+      tf2_any_point<MODEL, double>(E, f, f13, lnf, A, Phi);
       if (EARTH) tau = tau_star_point<double>(t.Ms, t.vM, t.eta, f13);
     } else {
       phd_point<double>(E.phd.k, f, A, Phi);
@@ -400,7 +472,7 @@ __device__ __forceinline__ void wave_point_full(const EvUnion& E, const ProjEv& 
     }
     P = {pj.cp * A, 0.0};
     C = {pj.ci * A, 0.0};
-    phi0 = Phi + ((MODEL == 0 || MODEL == 3) ? kTF2PhaseConst : 0.0);
+    phi0 = Phi + (is_tf2<MODEL>() ? kTF2PhaseConst : 0.0);
   }
 }
 
@@ -419,8 +491,8 @@ __device__ __forceinline__ void wave_point_val(const EvUnion& E, const ProjEv& p
     if (MODEL == 4) {
       nrt_point<double>(E.nrt, f, A, Phi);
       if (EARTH) tau = tau_star_point<double>(E.nrt.k.Ms, E.nrt.k.vM, E.nrt.k.eta, exp(lnf / 3.0));
-    } else if (MODEL == 0 || MODEL == 3) {
-      const TF2Ev& t = MODEL == 3 ? E.tf2t.b : E.tf2;
+    } else if (is_tf2<MODEL>()) {
+      const TF2Ev& t = tf2_base<MODEL>(E);
       const double f13 = exp(lnf / 3.0);
       tf2_point<double>(t, f, f13, lnf, exp(lnf * (-7.0 / 6.0)), A, Phi);
       if (EARTH) tau = tau_star_point<double>(t.Ms, t.vM, t.eta, f13);
@@ -445,7 +517,9 @@ struct SetupHdr {
 template <int MODEL>
 __host__ __device__ constexpr size_t wave_bytes() {
   return MODEL == 0 ? sizeof(TF2Ev)
-                    : (MODEL == 1 ? sizeof(PhdEv) : (MODEL == 2 ? sizeof(HMEv) : (MODEL == 3 ? sizeof(TF2TEv) : sizeof(NRTEv))));
+                    : (MODEL == 1 ? sizeof(PhdEv)
+                                  : (MODEL == 2 ? sizeof(HMEv)
+                                                : (MODEL == 3 ? sizeof(TF2TEv) : (MODEL == 4 ? sizeof(NRTEv) : sizeof(TF2EEv)))));
 }
 // the 22-mode models also carry the phase-tangent basis used by the FP32 kernel
 template <int MODEL>
@@ -480,9 +554,10 @@ __global__ void __launch_bounds__(64) setup_kernel(EvBatch ev, DetDev det, WfDes
   const double Mc = p[0 * ld + n], eta = p[1 * ld + n], dL = p[2 * ld + n];
   const double th = p[3 * ld + n], ph = p[4 * ld + n], io = p[5 * ld + n], ps = p[6 * ld + n];
   const double tc = p[7 * ld + n], c1 = p[9 * ld + n], c2 = p[10 * ld + n];
-  const double lt = MODEL >= 3 ? p[11 * ld + n] : 0.0, dlt = MODEL >= 3 ? p[12 * ld + n] : 0.0;
+  const double lt = has_tidal<MODEL>() ? p[11 * ld + n] : 0.0, dlt = has_tidal<MODEL>() ? p[12 * ld + n] : 0.0;
+  const double ecc = has_ecc<MODEL>() ? p[ecc_col<MODEL>() * ld + n] : 0.0;
   // IMRPhenomD_NRTidalv2 ends at 1.2 times its merger frequency, which depends on the deformabilities
-  if (grid_setup(h.g, det, ev, wf, n, Mc, eta, MODEL == 4 ? nrt_fcut(Mc, eta, lt, dlt) : -1.0)) {
+  if (grid_setup(h.g, det, ev, wf, n, Mc, eta, MODEL == 4 ? nrt_fcut(Mc, eta, lt, dlt) : -1.0, c1, c2)) {
     constexpr int nw = (int)(wave_bytes<MODEL>() / 8);
     const long long crow = core_idx ? core_idx[n] : n;   // a gathered batch reads the rows of its events
     unsigned long long* cw = core ? reinterpret_cast<unsigned long long*>(core + (size_t)crow * wave_bytes<MODEL>()) : nullptr;
@@ -492,8 +567,9 @@ __global__ void __launch_bounds__(64) setup_kernel(EvBatch ev, DetDev det, WfDes
       if (MODEL == 1) phd_ref(E.phd, det.fmin);
       if (MODEL == 2) hm_ref(E.hm, det.fmin);
       if (MODEL == 4) nrt_ref(E.nrt, det.fmin);
+      if (MODEL >= 5) tf2e_ref(E.tf2e, det.fmin, wf.fref_ecc);
     } else {
-      event_setup<MODEL>(E, det, wf, qnm, nq, Mc, eta, c1, c2, dL, lt, dlt);
+      event_setup<MODEL>(E, det, wf, qnm, nq, Mc, eta, c1, c2, dL, lt, dlt, ecc);
       if (MODEL == 2)
         for (int mode = 0; mode < 6; ++mode)
           hm_setup_mode(E.hm, mode, D4::seed(eta, P_ETA), D4::seed(c1, P_CHI1), D4::seed(c2, P_CHI2), io);
@@ -692,13 +768,24 @@ __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<N
       } else {
         ts = S.tsc;
       }
-      // tidal TaylorF2: d Phi / d LambdaTilde and d Phi / d deltaLambda at this point
-      double dphl = 0.0, dphd = 0.0;
-      if (MODEL == 3) {
-        const TF2TEv& t = S.E.tf2t;
+      // tidal TaylorF2: d Phi / d LambdaTilde and d Phi / d deltaLambda at this point (with
+      // use_QuadMonTid also through c4 v^-1 and c6 v of the series); eccentric TaylorF2: the
+      // eccentric phase is proportional to ecc^2, so d Phi / d ecc = 2 Phi_ecc / ecc
+      double dphl = 0.0, dphd = 0.0, dphe = 0.0;
+      if constexpr (MODEL == 3 || MODEL == 6) {
+        const TF2TEv& t = tf2_tidal<MODEL>(S.E);
         const double v = t.b.vM.v * exp(lnf / 3.0), v2 = v * v, v5 = v2 * v2 * v;
-        dphl = t.b.pn.A.v * v5 * (-19.5 - (3115.0 / 64.0) * v2);
-        dphd = t.b.pn.A.v * v5 * v2 * t.s12.v;
+        const double A = t.b.pn.A.v;
+        dphl = A * (v5 * (-19.5 - (3115.0 / 64.0) * v2) + t.q4l / v + t.q6l * v);
+        dphd = A * (v5 * v2 * t.s12.v + t.q4d / v + t.q6d * v);
+      }
+      if constexpr (has_ecc<MODEL>()) {
+        const TF2EEv& e = S.E.tf2e;
+        if (e.ecc != 0.0) {
+          const double f13 = exp(lnf / 3.0);
+          const double v = e.t.b.vM.v * f13, lnv = e.t.b.lnvM.v + lnf / 3.0;
+          dphe = 2.0 * tf2_ecc_phase<double>(e, v, lnv, lnf) / e.ecc;
+        }
       }
 #pragma unroll
       for (int a = 0; a < NARM; ++a) {
@@ -707,10 +794,11 @@ __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<N
         else ap = S.apc[a];
         arm_derivs<NI>(S.pj, ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D[a]);
         const cd H = cadd(cscale(P, ap.Fp), cscale(cmuli(C), ap.Fc));
-        if (MODEL == 3) {   // h ~ e^{-i Phi}: d h / d Lambda = -i h d Phi / d Lambda
-          D[a][NPS - 3] = cscale(cmuli(H), -dphl);
-          D[a][NPS - 2] = cscale(cmuli(H), -dphd);
+        if constexpr (MODEL == 3 || MODEL == 6) {   // h ~ e^{-i Phi}: d h / d Lambda = -i h d Phi / d Lambda
+          D[a][I_LT] = cscale(cmuli(H), -dphl);
+          D[a][I_DLT] = cscale(cmuli(H), -dphd);
         }
+        if constexpr (has_ecc<MODEL>()) D[a][ecc_col<MODEL>()] = cscale(cmuli(H), -dphe);
         D[a][NPM] = sd ? H : cd{0.0, 0.0};
       }
     } else {

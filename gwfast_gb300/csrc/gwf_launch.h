@@ -52,6 +52,14 @@ cudaError_t launch_fisher_m4(const LaunchArgs& a);   // IMRPhenomD_NRTidalv2: FP
 cudaError_t launch_snr_m4(const LaunchArgs& a);
 size_t setup_stride_m4();
 size_t core_bytes_m4();
+cudaError_t launch_fisher_m5(const LaunchArgs& a);   // eccentric TaylorF2: FP64, 12 parameters
+cudaError_t launch_snr_m5(const LaunchArgs& a);
+size_t setup_stride_m5();
+size_t core_bytes_m5();
+cudaError_t launch_fisher_m6(const LaunchArgs& a);   // tidal eccentric TaylorF2: FP64, 14 parameters
+cudaError_t launch_snr_m6(const LaunchArgs& a);
+size_t setup_stride_m6();
+size_t core_bytes_m6();
 // strain tangent / strain / overlap outputs (gwf_wave_out.cuh): set-up and output launch for
 // events [o.n0, o.n0 + o.cnt) of a.ev; a.scratch holds at least o.cnt records
 cudaError_t launch_wave_m0(const LaunchArgs& a, const WaveOut& o);

@@ -45,7 +45,8 @@ using PNC = PNCT<D4>;
 
 // TaylorF2 coefficients, gwfast/waveforms.py:784-812; drop_ss removes the 3PN spin-spin part as
 // IMRPhenomD does (gwfast/waveforms.py:1077). dq1, dq2: spin-induced quadrupole moments minus 1
-// (zero for black holes), as IMRPhenomD_NRTidalv2 uses them (gwfast/waveforms.py:1461-1467).
+// (zero for black holes), as IMRPhenomD_NRTidalv2 (gwfast/waveforms.py:1461-1467) and TaylorF2 with
+// use_QuadMonTid (:794-806) use them.
 template <class D>
 __device__ inline PNCT<D> pn_coeffs(const D& eta, const D& chi1, const D& chi2, bool spin_ho, bool drop_ss,
                                     const D& dq1 = D(0.0), const D& dq2 = D(0.0)) {
@@ -70,9 +71,9 @@ __device__ inline PNCT<D> pn_coeffs(const D& eta, const D& chi1, const D& chi2, 
            + (-15737.765635 / 3.048192 + 225.5 / 1.2 * kPi * kPi) * eta + 76.055 / 1.728 * eta2
            - 127.825 / 1.296 * eta2 * eta - log(4.0) * (684.8 / 2.1)
            + kPi * chi1 * m1 * (1490. / 3. + 260. * m1) + kPi * chi2 * m2 * (1490. / 3. + 260. * m2);
-  if (drop_ss)   // the quadrupole excess of the 3PN spin-spin terms (:1464-1467; zero for black holes)
-    six = six + (4703.5 / 8.4 + 2935. / 6. * m1 - 120. * m1 * m1) * m1s * dq1
-              + (4703.5 / 8.4 + 2935. / 6. * m2 - 120. * m2 * m2) * m2s * dq2;
+  // the quadrupole excess of the 3PN spin-spin terms (:806, :1464-1467; zero for black holes)
+  six = six + (4703.5 / 8.4 + 2935. / 6. * m1 - 120. * m1 * m1) * m1s * dq1
+            + (4703.5 / 8.4 + 2935. / 6. * m2 - 120. * m2 * m2) * m2s * dq2;
   if (!drop_ss) {
     const D ss1 = (4703.5 / 8.4 - 4108.25 / 6.72) + (2935. / 6. - 108.5 / 1.2) * m1 + (125.5 / 3.6 - 120.) * m1 * m1;
     const D ss2 = (4703.5 / 8.4 - 4108.25 / 6.72) + (2935. / 6. - 108.5 / 1.2) * m2 + (125.5 / 3.6 - 120.) * m2 * m2;
@@ -103,8 +104,16 @@ template <class C> struct TF2EvT {
 };
 using TF2Ev = TF2EvT<D4>;
 
-__device__ inline void tf2_setup(TF2Ev& e, const D4& Mc, const D4& eta, const D4& chi1, const D4& chi2, double dL, bool spin_ho) {
-  e.pn = pn_coeffs(eta, chi1, chi2, spin_ho, false);
+// TaylorF2 options (WfDesc::flags): phase referenced at the last stable orbit, cut at twice the Kerr
+// ISCO, spin-induced quadrupole moments from the tidal deformabilities
+enum { kTF2Vlso = 1, kTF2KerrIsco = 2, kTF2QuadMon = 4 };
+
+__device__ inline void tf2_setup(TF2Ev& e, const D4& Mc, const D4& eta, const D4& chi1, const D4& chi2, double dL,
+                                 bool spin_ho, int flags = 0, const D4& dq1 = D4(0.0), const D4& dq2 = D4(0.0)) {
+  e.pn = pn_coeffs(eta, chi1, chi2, spin_ho, false, dq1, dq2);
+  // phiref_vlso: the 2.5PN constant times (1 - 3 ln v_lso), v_lso = 1/sqrt(6) (gwfast/waveforms.py:816-818);
+  // its log partner keeps the plain coefficient
+  if (flags & kTF2Vlso) e.pn.c5 = e.pn.c5 * (1.0 + 1.5 * log(6.0));
   e.eta = eta;
   e.Ms = Mc * kG3 / dpowc(eta, 0.6);
   e.vM = dcbrt(kPi * e.Ms);
@@ -121,15 +130,118 @@ template <class C> struct TF2TEvT {
   TF2EvT<C> b;
   C t10, t12;   // series coefficients of v^10 and v^12
   C s12;        // d t12 / d deltaLambda
+  // use_QuadMonTid: d c4 / d LambdaTilde, d c4 / d deltaLambda, d c6 / d LambdaTilde, d c6 / d deltaLambda
+  // (the quadrupole moments follow Lambda1, Lambda2); zero otherwise
+  double q4l, q4d, q6l, q6d;
 };
 using TF2TEv = TF2TEvT<D4>;
 
+template <class D> __device__ inline void lam12_of(const D& lt, const D& dlt, const D& eta, D& l1, D& l2);
+template <class D> __device__ inline D quad_mon(const D& lam);
+
 __device__ inline void tf2t_setup(TF2TEv& e, const D4& Mc, const D4& eta, const D4& chi1, const D4& chi2, double dL,
-                                  bool spin_ho, double lam_t, double del_lam) {
-  tf2_setup(e.b, Mc, eta, chi1, chi2, dL, spin_ho);
+                                  bool spin_ho, double lam_t, double del_lam, int flags = 0) {
+  e.q4l = e.q4d = e.q6l = e.q6d = 0.0;
+  if (flags & kTF2QuadMon) {
+    // quadrupole moments with their eta tangent (Lambda1, Lambda2 depend on eta at fixed LambdaTilde,
+    // deltaLambda), then their tangents in (LambdaTilde, deltaLambda) for the analytic columns
+    D4 l1, l2;
+    lam12_of(D4(lam_t), D4(del_lam), eta, l1, l2);
+    const D4 q1 = quad_mon(l1), q2 = quad_mon(l2);
+    tf2_setup(e.b, Mc, eta, chi1, chi2, dL, spin_ho, flags, q1 - 1.0, q2 - 1.0);
+    typedef Dual<double, 2> D2;
+    D2 k1, k2;
+    lam12_of(D2::seed(lam_t, 0), D2::seed(del_lam, 1), D2(eta.v), k1, k2);
+    const D2 r1 = quad_mon(k1), r2 = quad_mon(k2);
+    const double sv = eta.v < 0.25 ? sqrt(1.0 - 4.0 * eta.v) : 0.0;
+    const double m1 = 0.5 * (1.0 + sv), m2 = 0.5 * (1.0 - sv);
+    const double a1 = m1 * m1 * chi1.v * chi1.v, a2 = m2 * m2 * chi2.v * chi2.v;
+    const double b1 = (4703.5 / 8.4 + 2935. / 6. * m1 - 120. * m1 * m1) * a1;
+    const double b2 = (4703.5 / 8.4 + 2935. / 6. * m2 - 120. * m2 * m2) * a2;
+    e.q4l = -50.0 * (a1 * r1.d[0] + a2 * r2.d[0]);
+    e.q4d = -50.0 * (a1 * r1.d[1] + a2 * r2.d[1]);
+    e.q6l = b1 * r1.d[0] + b2 * r2.d[0];
+    e.q6d = b1 * r1.d[1] + b2 * r2.d[1];
+  } else {
+    tf2_setup(e.b, Mc, eta, chi1, chi2, dL, spin_ho, flags);
+  }
   e.t10 = D4(-19.5 * lam_t);
   e.s12 = (6595.0 / 364.0) * seta_of(eta);
   e.t12 = (-3115.0 / 64.0) * lam_t + e.s12 * del_lam;
+}
+
+// eccentric TaylorF2 (gwfast/waveforms.py:814-845; low-eccentricity phase to 3PN, arXiv:1605.00304):
+// the series gains K e0^2 (v0/v)^(19/3) S(v, v0), K = -2355/1462, with v0 = (pi M f0)^(1/3) at the
+// eccentricity's reference frequency f0 (the lowest grid frequency unless fRef_ecc is given). Written
+// as a polynomial in v, S = s0 + s2 v^2 + ... + s6 v^6 + sl ln(16 v^2) v^6, whose coefficients depend on
+// v0 and eta; (v0/v)^(19/3) = (f0/f)^(19/9) carries no parameter. Stored already multiplied by
+// A K e0^2 (A = 3/(128 eta)). With f0 the lowest grid frequency the record depends on the detector.
+template <class C> struct TF2EEvT {
+  TF2TEvT<C> t;   // tidal part zero without the tidal terms
+  C es[6];        // A K e0^2 times s0, s2, s3, s4, s5, s6
+  C el;           // A K e0^2 times the ln(16 v^2) v^6 coefficient
+  double ecc, lnf0;
+};
+using TF2EEv = TF2EEvT<D4>;
+
+__device__ inline void tf2e_ref(TF2EEv& e, double fmin_hz, double fref_ecc) {
+  const double f0 = fref_ecc > 0.0 ? fref_ecc : fmin_hz;
+  e.lnf0 = log(f0);
+  const D4& eta = e.t.b.eta;
+  const D4 eta2 = eta * eta, eta3 = eta2 * eta;
+  const D4 v0 = e.t.b.vM * exp(e.lnf0 / 3.0);
+  const D4 w2 = v0 * v0, w3 = w2 * v0, w4 = w2 * w2, w5 = w4 * v0, w6 = w3 * w3;
+  const D4 lw = log(16.0) + 2.0 * dlog(v0);   // ln(16 v0^2)
+  const double pi2 = kPi * kPi, l2 = log(2.0), l3 = log(3.0);
+  const D4 twoV = 29.9076223 / 8.1976608 + 18.766963 / 2.927736 * eta;
+  const D4 twoV0 = 2.833 / 1.008 - 19.7 / 3.6 * eta;
+  const double threeV = -28.19123 / 2.82600 * kPi, threeV0 = 37.7 / 7.2 * kPi;
+  const D4 fourV4 = 16.237683263 / 3.330429696 + 241.33060753 / 9.71375328 * eta + 156.2608261 / 6.9383952 * eta2;
+  const D4 fourV2V02 = 84.7282939759 / 8.2632420864 - 7.18901219 / 3.68894736 * eta - 36.97091711 / 1.05398496 * eta2;
+  const D4 fourV04 = -1.193251 / 3.048192 - 66.317 / 9.072 * eta + 18.155 / 1.296 * eta2;
+  const D4 fiveV5 = kPi * (-28.31492681 / 1.18395270 - 115.52066831 / 2.70617760 * eta);
+  const D4 fiveV3V02 = kPi * (-79.86575459 / 2.84860800 + 55.5367231 / 1.0173600 * eta);
+  const D4 fiveV2V03 = kPi * (112.751736071 / 5.902315776 + 70.75145051 / 2.10796992 * eta);
+  const D4 fiveV05 = kPi * (76.4881 / 9.0720 - 94.9457 / 2.2680 * eta);
+  const D4 sixV6 = -436.03153867072577087 / 1.32658535116800000 + 53.6803271 / 1.9782000 * kEulerGamma
+                   + 157.22503703 / 3.25555200 * pi2 + (2991.72861614477 / 6.89135247360 - 15.075413 / 1.446912 * pi2) * eta
+                   + 345.5209264991 / 4.1019955200 * eta2 + 506.12671711 / 8.78999040 * eta3
+                   + 384.3505163 / 5.9346000 * l2 - 112.1397129 / 1.7584000 * l3;
+  const D4 sixV4V02 = 46.001356684079 / 3.357073133568 + 253.471410141755 / 5.874877983744 * eta
+                      - 169.3852244423 / 2.3313007872 * eta2 - 307.833827417 / 2.497822272 * eta3;
+  const double sixV3V03 = -106.2809371 / 2.0347200 * pi2;
+  const D4 sixV2V04 = -3.56873002170973 / 2.49880440692736 - 260.399751935005 / 8.924301453312 * eta
+                      + 15.0484695827 / 3.5413894656 * eta2 + 340.714213265 / 3.794345856 * eta3;
+  const D4 sixV06 = 265.31900578691 / 1.68991764480 - 33.17 / 1.26 * kEulerGamma + 12.2833 / 1.0368 * pi2
+                    + (91.55185261 / 5.48674560 - 3.977 / 1.152 * pi2) * eta - 5.732473 / 1.306368 * eta2
+                    - 30.90307 / 1.39968 * eta3 + 87.419 / 1.890 * l2 - 260.01 / 5.60 * l3;
+  const D4 pre = e.t.b.pn.A * ((-2.355 / 1.462) * e.ecc * e.ecc);
+  e.es[0] = pre * (1.0 + twoV0 * w2 + threeV0 * w3 + fourV04 * w4 + fiveV05 * w5 + (sixV06 - 33.17 / 2.52 * lw) * w6);
+  e.es[1] = pre * (twoV + fourV2V02 * w2 + fiveV2V03 * w3 + sixV2V04 * w4);
+  e.es[2] = pre * (threeV + fiveV3V02 * w2 + sixV3V03 * w3);
+  e.es[3] = pre * (fourV4 + sixV4V02 * w2);
+  e.es[4] = pre * fiveV5;
+  e.es[5] = pre * sixV6;
+  e.el = pre * (53.6803271 / 3.9564000);
+}
+
+__device__ inline void tf2e_setup(TF2EEv& e, const D4& Mc, const D4& eta, const D4& chi1, const D4& chi2, double dL,
+                                  bool spin_ho, double lam_t, double del_lam, int flags, double ecc, double fmin_hz,
+                                  double fref_ecc) {
+  tf2t_setup(e.t, Mc, eta, chi1, chi2, dL, spin_ho, lam_t, del_lam, flags);
+  e.ecc = ecc;
+  tf2e_ref(e, fmin_hz, fref_ecc);
+}
+
+// eccentric part of the phase, (f0/f)^(19/9) S(v) / v^5, at v = (pi M f)^(1/3), ln v = lnv
+template <class S, class C>
+__device__ __forceinline__ S tf2_ecc_phase(const TF2EEvT<C>& e, const S& v, const S& lnv, typename Real<S>::T lnf) {
+  typedef typename Real<S>::T T;
+  const S v2 = v * v, v3 = v2 * v;
+  const S ser = co<S>(e.es[0])
+                + v2 * (co<S>(e.es[1]) + v * (co<S>(e.es[2]) + v * (co<S>(e.es[3]) + v * (co<S>(e.es[4]) + v * co<S>(e.es[5])))))
+                + co<S>(e.el) * (T(log(16.0)) + T(2) * lnv) * v3 * v3;
+  return ser * (exp(T(19.0 / 9.0) * (T(e.lnf0) - lnf)) / (v2 * v3));
 }
 
 // the tidal part of the phase, A (t10 v^10 + t12 v^12) / v^5, at v = (pi M f)^(1/3)

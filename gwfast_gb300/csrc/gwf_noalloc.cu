@@ -91,6 +91,9 @@ extern "C" int gwf_fisher_noalloc(const gwf_det_desc* det, const double* psd_f, 
     if (i && !(psd_f[i] > psd_f[i - 1])) return fail(GWF_ERR_INVALID_ARG, "PSD frequencies must be strictly increasing");
   }
   if (wf->model < 0 || wf->model > 2) return fail(GWF_ERR_INVALID_ARG, "unknown waveform model");
+  if (wf->flags & ~(GWF_TF2_PHIREF_VLSO | GWF_TF2_KERR_ISCO)) return fail(GWF_ERR_INVALID_ARG, "unknown waveform flags");
+  if (wf->flags && wf->model != GWF_WF_TAYLORF2)
+    return fail(GWF_ERR_INVALID_ARG, "waveform flags apply to the TaylorF2 models only");
   if (!(wf->fcut_par > 0.0)) return fail(GWF_ERR_INVALID_ARG, "fcut_par must be positive");
   if (wf->model == GWF_WF_PHENOMD) {
     if (!qnm_spin || !qnm_fring || !qnm_fdamp || n_qnm < 2)
@@ -155,6 +158,9 @@ extern "C" int gwf_fisher_noalloc(const gwf_det_desc* det, const double* psd_f, 
   a.wf.model = wf->model;
   a.wf.spin_ho = wf->spin_ho;
   a.wf.fcut_par = wf->fcut_par;
+  a.wf.flags = wf->flags;
+  a.wf.pad_ = 0;
+  a.wf.fref_ecc = wf->fref_ecc;
   a.qnm = reinterpret_cast<const double*>(base + kOffQnm);
   a.nq = wf->model == GWF_WF_PHENOMD ? (int)n_qnm : 0;
   a.out_arm = nullptr;

@@ -21,9 +21,9 @@ def CovMatr(FisherMatrix, invMethodIn='cho', condNumbMax=1e50, truncate=False, s
         raise NotImplementedError('singular-value truncation is not implemented on the GPU path')
     F = np.ascontiguousarray(np.moveaxis(np.asarray(FisherMatrix, dtype=np.float64), -1, 0))
     P = F.shape[1]
-    if F.shape[1:] != (P, P) or P > 13:
-        raise NotImplementedError('the GPU inversion handles up to 13x13 matrices')
-    K = 11 if P <= 11 else 13   # the kernel sizes (11 parameters; 13 for the tidal model)
+    if F.shape[1:] != (P, P) or P > 14:
+        raise NotImplementedError('the GPU inversion handles up to 14x14 matrices')
+    K = 11 if P <= 11 else (13 if P <= 13 else 14)   # the kernel sizes (11, 13 tidal, 14 tidal eccentric)
     if P < K:
         # block-diagonal embedding with an identity block (e.g. after fixParams): the inverse of
         # the leading block is the leading block of the inverse; an equilibrated matrix has

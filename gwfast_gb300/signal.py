@@ -30,6 +30,9 @@ def _prep(evParams, wf=None):
     utils.fill_spins(evParams)
     if wf is not None and wf.is_tidal:
         utils.fill_tidal(evParams)
+    if wf is not None and wf.is_eccentric and 'ecc' not in evParams:
+        raise ValueError('Eccentricity has to be provided.')   # gwfast/signal.py:876-880
+    if wf is not None and (wf.is_tidal or wf.is_eccentric):
         return event_array(evParams, wf.params)
     return event_array(evParams)
 

@@ -3,9 +3,10 @@
 The waveforms themselves are evaluated inside the fused CUDA kernels; these
 objects carry what gwfast's callers read from a model (``ParNums``, ``nParams``,
 the ``is_*`` flags, ``objType``, ``fcut``) plus the descriptor the C ABI needs.
-Supported: TaylorF2_RestrictedPN (optionally with the 3.5PN spin-spin terms and with the tidal
-terms, 13 parameters), IMRPhenomD, IMRPhenomHM and IMRPhenomD_NRTidalv2 (13 parameters), aligned
-spins, no eccentricity.
+Supported: TaylorF2_RestrictedPN (with its options: the 3.5PN spin-spin terms, the tidal terms (13
+parameters), orbital eccentricity (+ ecc: 12 or 14 parameters), the phase referenced at the last
+stable orbit, the Kerr-ISCO cut, the spin-induced quadrupole of tidal bodies), IMRPhenomD,
+IMRPhenomHM and IMRPhenomD_NRTidalv2 (13 parameters), aligned spins.
 """
 import numpy as np
 
@@ -23,8 +24,10 @@ class WaveFormModel:
                  is_Precessing=False, is_LAL=False, is_prec_ang=False, is_eccentric=False, is_holomorphic=False,
                  apply_fcut=True):
         tidal_ok = type(self).__name__ in ('TaylorF2_RestrictedPN', 'IMRPhenomD_NRTidalv2')
+        ecc_ok = type(self).__name__ == 'TaylorF2_RestrictedPN'
         for flag, name in ((is_newtonian, 'is_newtonian'), (is_tidal and not tidal_ok, 'is_tidal'),
-                           (is_Precessing, 'is_Precessing'), (is_LAL, 'is_LAL'), (is_eccentric, 'is_eccentric')):
+                           (is_Precessing, 'is_Precessing'), (is_LAL, 'is_LAL'),
+                           (is_eccentric and not ecc_ok, 'is_eccentric')):
             if flag:
                 raise NotImplementedError('%s waveforms are not implemented on the GPU path' % name)
         if not apply_fcut:
@@ -41,7 +44,7 @@ class WaveFormModel:
         self.is_eccentric = is_eccentric
         self.is_holomorphic = is_holomorphic
         self.apply_fcut = apply_fcut
-        self.nParams = 13 if is_tidal else 11
+        self.nParams = 11 + (2 if is_tidal else 0) + (1 if is_eccentric else 0)
         if is_chi1chi2:
             self.ParNums = {'Mc': 0, 'eta': 1, 'dL': 2, 'theta': 3, 'phi': 4, 'iota': 5, 'psi': 6, 'tcoal': 7,
                             'Phicoal': 8, 'chi1z': 9, 'chi2z': 10}
@@ -51,20 +54,20 @@ class WaveFormModel:
         if is_tidal:
             self.ParNums['LambdaTilde'] = 11
             self.ParNums['deltaLambda'] = 12
+        if is_eccentric:   # gwfast/waveforms.py:110-123
+            self.ParNums['ecc'] = 13 if is_tidal else 11
 
     @property
     def params(self):
         """Names of the Fisher parameters in order (the rows of the event array)."""
-        return PARAMS_TIDAL if self.is_tidal else PARAMS
+        return (PARAMS_TIDAL if self.is_tidal else PARAMS) + (('ecc',) if self.is_eccentric else ())
 
     def fcut(self, **kwargs):
         """Cut frequency in Hz (gwfast/waveforms.py:190-199)."""
         return self.fcutPar / (np.asarray(kwargs['Mc']) / (np.asarray(kwargs['eta']) ** (3. / 5.)))
 
     def gpu_desc(self):
-        name = type(self).__name__
-        model = _lib.MODEL_TF2_TIDAL if (self.is_tidal and name == 'TaylorF2_RestrictedPN') else _lib.MODEL_IDS[name]
-        return _lib.WfDesc(model, int(getattr(self, 'use_3p5PN_SpinHO', False)), float(self.fcutPar))
+        return _lib.WfDesc(_lib.MODEL_IDS[type(self).__name__], 0, float(self.fcutPar))
 
     def _device_only(self, *a, **k):
         raise NotImplementedError('%s is evaluated inside the fused GPU kernels; use GWSignal / DetNet'
@@ -74,15 +77,18 @@ class WaveFormModel:
 
 
 class TaylorF2_RestrictedPN(WaveFormModel):
-    """gwfast/waveforms.py:697-953 (fcut: twice the Schwarzschild ISCO by default). is_tidal adds the
-    5PN and 6PN tidal phase terms and the parameters LambdaTilde, deltaLambda (FP64 path only)."""
+    """gwfast/waveforms.py:697-953 (fcut: twice the Schwarzschild ISCO by default, or of the Kerr
+    remnant with which_ISCO='Kerr'). is_tidal adds the 5PN and 6PN tidal phase terms and the parameters
+    LambdaTilde, deltaLambda (with use_QuadMonTid also the spin-induced quadrupole moments);
+    is_eccentric adds the low-eccentricity phase to 3PN and the parameter ecc, referenced at fRef_ecc
+    (None: the lowest grid frequency). The tidal and eccentric forms run on the FP64 path only."""
 
     def __init__(self, fHigh=None, is_tidal=False, use_3p5PN_SpinHO=False, phiref_vlso=False, is_eccentric=False,
                  fRef_ecc=None, which_ISCO='Schw', use_QuadMonTid=False, **kwargs):
         if fHigh is None:
             fHigh = 1. / (6. * np.pi * np.sqrt(6.) * glob.GMsun_over_c3)
-        if phiref_vlso or which_ISCO != 'Schw' or use_QuadMonTid:
-            raise NotImplementedError('phiref_vlso, Kerr ISCO and QuadMonTid are not implemented on the GPU path')
+        if which_ISCO not in ('Schw', 'Kerr'):
+            raise ValueError("which_ISCO must be 'Schw' or 'Kerr'")
         self.use_3p5PN_SpinHO = use_3p5PN_SpinHO
         self.phiref_vlso = phiref_vlso
         self.fRef_ecc = fRef_ecc
@@ -90,6 +96,48 @@ class TaylorF2_RestrictedPN(WaveFormModel):
         self.use_QuadMonTid = use_QuadMonTid
         super().__init__('BNS' if is_tidal else 'BBH', fHigh, is_tidal=is_tidal, is_eccentric=is_eccentric,
                          is_holomorphic=True, **kwargs)
+
+    def fcut(self, **kwargs):
+        """Cut frequency in Hz (gwfast/waveforms.py:903-951)."""
+        Mc, eta = np.asarray(kwargs['Mc'], dtype=np.float64), np.asarray(kwargs['eta'], dtype=np.float64)
+        if self.which_ISCO == 'Schw':
+            return self.fcutPar / (Mc / (eta ** (3. / 5.)))
+        chi1, chi2 = np.asarray(kwargs['chi1z'], dtype=np.float64), np.asarray(kwargs['chi2z'], dtype=np.float64)
+        eta2 = eta * eta
+        Mtot = Mc / eta ** (3. / 5.)
+        seta = np.sqrt(np.where(eta < 0.25, 1.0 - 4.0 * eta, 0.))
+        m1, m2 = 0.5 * (1.0 + seta), 0.5 * (1.0 - seta)
+        s = (m1 * m1 * chi1 + m2 * m2 * chi2) / (m1 * m1 + m2 * m2)
+        atot = (chi1 + chi2 * (m2 / m1) ** 2) / (1. + m2 / m1) ** 2
+        aeff = atot + 0.41616 * eta * (chi1 + chi2)
+
+        def r_isco(chi):
+            z1 = 1.0 + np.cbrt(1.0 - chi * chi) * (np.cbrt(1.0 + chi) + np.cbrt(1.0 - chi))
+            z2 = np.sqrt(3.0 * chi * chi + z1 * z1)
+            r = np.sqrt((3.0 - z1) * (3.0 + z1 + 2.0 * z2))
+            return np.where(chi > 0., 3.0 + z2 - r, 3.0 + z2 + r)
+
+        r0 = r_isco(aeff)
+        ens = eta * (0.055974469826360077 + 0.5809510763115132 * eta - 0.9606726679372312 * eta2
+                     + 3.352411249771192 * eta2 * eta)
+        erad = (ens * (1. + (-0.0030302335878845507 - 2.0066110851351073 * eta + 7.7050567802399215 * eta2) * s)
+                / (1. + (-0.6714403054720589 - 1.4756929437702908 * eta + 7.304676214885011 * eta2) * s))
+        L = 2. / (3. * np.sqrt(3.)) * (1. + 2. * np.sqrt(3. * r0 - 2.))
+        E = np.sqrt(1. - 2. / (3. * r0))
+        chif = (atot + eta * (L - 2. * atot * (E - 1.)) + (-3.821158961 - 1.2019 * aeff - 1.20764 * aeff ** 2) * eta2
+                + (3.79245 + 1.18385 * aeff + 4.90494 * aeff ** 2) * eta2 * eta)
+        rf = r_isco(chif)
+        return 1. / (rf ** 1.5 + chif) / (np.pi * Mtot * (1. - erad) * glob.GMsun_over_c3)
+
+    def gpu_desc(self):
+        if self.is_eccentric:
+            model = _lib.MODEL_TF2_TIDAL_ECC if self.is_tidal else _lib.MODEL_TF2_ECC
+        else:
+            model = _lib.MODEL_TF2_TIDAL if self.is_tidal else _lib.MODEL_IDS['TaylorF2_RestrictedPN']
+        flags = ((_lib.TF2_PHIREF_VLSO if self.phiref_vlso else 0) | (_lib.TF2_KERR_ISCO if self.which_ISCO == 'Kerr' else 0)
+                 | (_lib.TF2_QUADMON_TIDAL if (self.use_QuadMonTid and self.is_tidal) else 0))
+        fre = float(self.fRef_ecc) if (self.is_eccentric and self.fRef_ecc is not None) else 0.
+        return _lib.WfDesc(model, int(self.use_3p5PN_SpinHO), float(self.fcutPar), flags, 0, fre)
 
 
 class IMRPhenomD(WaveFormModel):

@@ -13,14 +13,16 @@
  *    parameter k of event n, k in the Fisher order
  *      0 Mc [Msun, detector frame], 1 eta, 2 dL [Gpc], 3 theta, 4 phi, 5 iota,
  *      6 psi [rad], 7 tcoal [GMST days], 8 Phicoal [rad], 9 chi1z, 10 chi2z
- *    (gwfast/waveforms.py:78, :125-129); the tidal models (GWF_WF_TAYLORF2_TIDAL, GWF_WF_PHENOMD_NRTIDALV2) add
- *      11 LambdaTilde, 12 deltaLambda (gwfast/waveforms.py:106-109), 13 rows in all.
+ *    (gwfast/waveforms.py:78, :125-129); the tidal models (GWF_WF_TAYLORF2_TIDAL, GWF_WF_PHENOMD_NRTIDALV2,
+ *    GWF_WF_TAYLORF2_TIDAL_ECC) add 11 LambdaTilde, 12 deltaLambda (gwfast/waveforms.py:106-109), and the
+ *    eccentric TaylorF2 adds ecc after them (GWF_WF_TAYLORF2_ECC: row 11, 12 rows; GWF_WF_TAYLORF2_TIDAL_ECC:
+ *    row 13, 14 rows; gwfast/waveforms.py:110-123).
  *  - mem = GWF_MEM_HOST: params, res_per_event and outputs are host pointers; the
  *    call copies in, runs, copies out and returns when the outputs are written.
  *    mem = GWF_MEM_DEVICE: all pointers are device pointers owned by the caller;
  *    the work is queued on `stream` (NULL = the context's stream) and the call
  *    returns without waiting.
- *  - Fisher matrices are written row-major, P x P per event (P = 11, 13 for the tidal model),
+ *  - Fisher matrices are written row-major, P x P per event (P = the number of parameter rows),
  *    tcoal in seconds (gwfast/signal.py:918-920).
  *  - One context per thread; calls on one context are serialised on its stream.
  */
@@ -35,6 +37,8 @@ extern "C" {
 
 #define GWF_NPARAMS 11
 #define GWF_NPARAMS_TIDAL 13
+#define GWF_NPARAMS_ECC 12
+#define GWF_NPARAMS_TIDAL_ECC 14
 
 enum {
   GWF_OK = 0,
@@ -48,9 +52,16 @@ enum {
 /* GWF_WF_TAYLORF2_TIDAL: TaylorF2_RestrictedPN(is_tidal=True), gwfast/waveforms.py:849-855;
  * GWF_WF_PHENOMD_NRTIDALV2: IMRPhenomD_NRTidalv2, gwfast/waveforms.py:1339-1836 (its cut frequency
  * follows from the deformabilities; fcut_par is the M f cut 0.2 of the IMRPhenomD part). Both FP64,
- * 13 parameters. */
+ * 13 parameters.
+ * GWF_WF_TAYLORF2_ECC, GWF_WF_TAYLORF2_TIDAL_ECC: TaylorF2_RestrictedPN(is_eccentric=True), without or with
+ * is_tidal (gwfast/waveforms.py:814-845): FP64, 12 and 14 parameters. */
 enum { GWF_WF_TAYLORF2 = 0, GWF_WF_PHENOMD = 1, GWF_WF_PHENOMHM = 2, GWF_WF_TAYLORF2_TIDAL = 3,
-       GWF_WF_PHENOMD_NRTIDALV2 = 4 };
+       GWF_WF_PHENOMD_NRTIDALV2 = 4, GWF_WF_TAYLORF2_ECC = 5, GWF_WF_TAYLORF2_TIDAL_ECC = 6 };
+/* gwf_wf_desc.flags, TaylorF2 models only (gwfast/waveforms.py:726-741):
+ * GWF_TF2_PHIREF_VLSO    phiref_vlso=True (2.5PN constant referenced at the last stable orbit, :796-798)
+ * GWF_TF2_KERR_ISCO      which_ISCO='Kerr' (cut at twice the Kerr-remnant ISCO frequency, :921-951)
+ * GWF_TF2_QUADMON_TIDAL  use_QuadMonTid=True (tidal models: spin-induced quadrupole moments, :780-788) */
+enum { GWF_TF2_PHIREF_VLSO = 1, GWF_TF2_KERR_ISCO = 2, GWF_TF2_QUADMON_TIDAL = 4 };
 enum { GWF_SHAPE_L = 0, GWF_SHAPE_T = 1 };
 enum { GWF_SPACING_GEOM = 0, GWF_SPACING_LIN = 1 };
 enum { GWF_MEM_HOST = 0, GWF_MEM_DEVICE = 1 };
@@ -76,6 +87,9 @@ typedef struct {
   int model;           /* GWF_WF_* */
   int spin_ho;         /* TaylorF2 use_3p5PN_SpinHO */
   double fcut_par;     /* TaylorF2: fHigh [Hz] (default 2 f_ISCO); IMR models: Mf cut (0.2) */
+  int flags;           /* GWF_TF2_* (0 for the defaults) */
+  int reserved;        /* 0 */
+  double fref_ecc;     /* eccentric TaylorF2: fRef_ecc [Hz]; <= 0: the lowest grid frequency (gwfast's None) */
 } gwf_wf_desc;
 
 /* Context: device selection, PSD tables, staging memory.
@@ -195,7 +209,8 @@ int gwf_autotune_segments(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf
 int gwf_cov(gwf_ctx* ctx, const double* F, int64_t n_events, int mem, double* cov, double* eps, double* cond,
             void* stream);
 
-/* gwf_cov for P x P matrices, P = n_params = 11 or 13 (the tidal model); F, cov [N][P][P]. */
+/* gwf_cov for P x P matrices, P = n_params = 11, 13 (tidal models) or 14 (tidal eccentric TaylorF2; smaller
+ * matrices, e.g. after fixParams, are embedded with an identity block by the caller); F, cov [N][P][P]. */
 int gwf_cov_n(gwf_ctx* ctx, const double* F, int64_t N, int n_params, int mem, double* cov, double* eps, double* cond,
               void* stream);
 

@@ -97,9 +97,9 @@ def pn_coeffs(eta, chi1, chi2, spin_ho=False, drop_3pn_ss=False, dq1=0., dq2=0.)
            + eta * (-15737.765635 / 3.048192 + 225.5 / 1.2 * PI * PI)
            + eta2 * 76.055 / 1.728 - eta2 * eta * 127.825 / 1.296 - math.log(4.) * 684.8 / 2.1
            + PI * chi1 * m1 * (1490. / 3. + 260. * m1) + PI * chi2 * m2 * (1490. / 3. + 260. * m2))
-    if drop_3pn_ss:
-        six = six + ((4703.5 / 8.4 + 2935. / 6. * m1 - 120. * m1 * m1) * m1s * dq1
-                     + (4703.5 / 8.4 + 2935. / 6. * m2 - 120. * m2 * m2) * m2s * dq2)
+    # the quadrupole excess of the 3PN spin-spin terms (:806, :1464-1467; zero for black holes)
+    six = six + ((4703.5 / 8.4 + 2935. / 6. * m1 - 120. * m1 * m1) * m1s * dq1
+                 + (4703.5 / 8.4 + 2935. / 6. * m2 - 120. * m2 * m2) * m2s * dq2)
     if not drop_3pn_ss:
         def ss(m):
             return (4703.5 / 8.4 + 2935. / 6. * m - 120. * m * m) + (-4108.25 / 6.72 - 108.5 / 1.2 * m + 125.5 / 3.6 * m * m)
@@ -128,20 +128,104 @@ def tf2_fcut(Mc, eta):
     return fhigh / (Mc / eta ** (3. / 5.))
 
 
-def tf2_phase(f, Mc, eta, chi1, chi2, spin_ho=False, lam_t=None, del_lam=None):
-    """gwfast/waveforms.py:743-862 (not eccentric, fRef at v = 0); with lam_t/del_lam the tidal terms
+def _r_isco(chi):
+    z1 = 1.0 + (1.0 - chi * chi) ** (1. / 3.) * ((1.0 + chi) ** (1. / 3.) + (1.0 - chi) ** (1. / 3.))
+    z2 = torch.sqrt(3.0 * chi * chi + z1 * z1)
+    r = torch.sqrt((3.0 - z1) * (3.0 + z1 + 2.0 * z2))
+    return torch.where(chi > 0., 3.0 + z2 - r, 3.0 + z2 + r)
+
+
+def tf2_fcut_kerr(Mc, eta, chi1, chi2):
+    """Twice the ISCO frequency of the Kerr remnant (which_ISCO='Kerr'): gwfast/waveforms.py:921-951."""
+    eta2 = eta * eta
+    Mtot = Mc / eta ** (3. / 5.)
+    seta = _seta(eta)
+    m1, m2 = 0.5 * (1. + seta), 0.5 * (1. - seta)
+    s = (m1 * m1 * chi1 + m2 * m2 * chi2) / (m1 * m1 + m2 * m2)
+    atot = (chi1 + chi2 * (m2 / m1) ** 2) / (1. + m2 / m1) ** 2
+    aeff = atot + 0.41616 * eta * (chi1 + chi2)
+    r0 = _r_isco(aeff)
+    ens = eta * (0.055974469826360077 + 0.5809510763115132 * eta - 0.9606726679372312 * eta2 + 3.352411249771192 * eta2 * eta)
+    erad = (ens * (1. + (-0.0030302335878845507 - 2.0066110851351073 * eta + 7.7050567802399215 * eta2) * s)
+            / (1. + (-0.6714403054720589 - 1.4756929437702908 * eta + 7.304676214885011 * eta2) * s))
+    L = 2. / (3. * math.sqrt(3.)) * (1. + 2. * torch.sqrt(3. * r0 - 2.))
+    E = torch.sqrt(1. - 2. / (3. * r0))
+    chif = (atot + eta * (L - 2. * atot * (E - 1.)) + (-3.821158961 - 1.2019 * aeff - 1.20764 * aeff ** 2) * eta2
+            + (3.79245 + 1.18385 * aeff + 4.90494 * aeff ** 2) * eta2 * eta)
+    rf = _r_isco(chif)
+    return 1. / (rf ** 1.5 + chif) / (PI * Mtot * (1. - erad) * GMSUN_OVER_C3)
+
+
+# eccentric TaylorF2 coefficients (arXiv:1605.00304, as gwfast/waveforms.py:826-843 writes them):
+# name -> function of eta
+def _ecc_coeffs(eta):
+    e2, e3 = eta * eta, eta * eta * eta
+    pi2, l2, l3, g = PI * PI, math.log(2.), math.log(3.), EULER_GAMMA
+    return {
+        'twoV': 29.9076223 / 8.1976608 + 18.766963 / 2.927736 * eta,
+        'twoV0': 2.833 / 1.008 - 19.7 / 3.6 * eta,
+        'threeV': -28.19123 / 2.82600 * PI,
+        'threeV0': 37.7 / 7.2 * PI,
+        'fourV4': 16.237683263 / 3.330429696 + 241.33060753 / 9.71375328 * eta + 156.2608261 / 6.9383952 * e2,
+        'fourV2V02': 84.7282939759 / 8.2632420864 - 7.18901219 / 3.68894736 * eta - 36.97091711 / 1.05398496 * e2,
+        'fourV04': -1.193251 / 3.048192 - 66.317 / 9.072 * eta + 18.155 / 1.296 * e2,
+        'fiveV5': -28.31492681 / 1.18395270 * PI - 115.52066831 / 2.70617760 * PI * eta,
+        'fiveV3V02': -79.86575459 / 2.84860800 * PI + 55.5367231 / 1.0173600 * PI * eta,
+        'fiveV2V03': 112.751736071 / 5.902315776 * PI + 70.75145051 / 2.10796992 * PI * eta,
+        'fiveV05': 76.4881 / 9.0720 * PI - 94.9457 / 2.2680 * PI * eta,
+        'sixV6': (-436.03153867072577087 / 1.32658535116800000 + 53.6803271 / 1.9782000 * g + 157.22503703 / 3.25555200 * pi2
+                  + (2991.72861614477 / 6.89135247360 - 15.075413 / 1.446912 * pi2) * eta + 345.5209264991 / 4.1019955200 * e2
+                  + 506.12671711 / 8.78999040 * e3 + 384.3505163 / 5.9346000 * l2 - 112.1397129 / 1.7584000 * l3),
+        'sixV4V02': (46.001356684079 / 3.357073133568 + 253.471410141755 / 5.874877983744 * eta
+                     - 169.3852244423 / 2.3313007872 * e2 - 307.833827417 / 2.497822272 * e3),
+        'sixV3V03': -106.2809371 / 2.0347200 * pi2,
+        'sixV2V04': (-3.56873002170973 / 2.49880440692736 - 260.399751935005 / 8.924301453312 * eta
+                     + 15.0484695827 / 3.5413894656 * e2 + 340.714213265 / 3.794345856 * e3),
+        'sixV06': (265.31900578691 / 1.68991764480 - 33.17 / 1.26 * g + 12.2833 / 1.0368 * pi2
+                   + (91.55185261 / 5.48674560 - 3.977 / 1.152 * pi2) * eta - 5.732473 / 1.306368 * e2
+                   - 30.90307 / 1.39968 * e3 + 87.419 / 1.890 * l2 - 260.01 / 5.60 * l3),
+    }
+
+
+def tf2_ecc_series(v, v0, eta, ecc):
+    """phi_Ecc of gwfast/waveforms.py:824-845: -2355/1462 e0^2 (v0/v)^(19/3) times the 3PN series in v, v0."""
+    k = _ecc_coeffs(eta)
+    pre = -2.355 / 1.462 * ecc * ecc * (v0 / v) ** (19. / 3.)
+    ser = (1. + (k['twoV'] * v * v + k['twoV0'] * v0 * v0) + (k['threeV'] * v ** 3 + k['threeV0'] * v0 ** 3)
+           + (k['fourV4'] * v ** 4 + k['fourV2V02'] * v * v * v0 * v0 + k['fourV04'] * v0 ** 4)
+           + (k['fiveV5'] * v ** 5 + k['fiveV3V02'] * v ** 3 * v0 ** 2 + k['fiveV2V03'] * v ** 2 * v0 ** 3
+              + k['fiveV05'] * v0 ** 5)
+           + ((k['sixV6'] + 53.6803271 / 3.9564000 * torch.log(16. * v * v)) * v ** 6 + k['sixV4V02'] * v ** 4 * v0 ** 2
+              + k['sixV3V03'] * v ** 3 * v0 ** 3 + k['sixV2V04'] * v ** 2 * v0 ** 4
+              + (k['sixV06'] - 33.17 / 2.52 * torch.log(16. * v0 * v0)) * v0 ** 6))
+    return pre * ser
+
+
+def tf2_phase(f, Mc, eta, chi1, chi2, spin_ho=False, lam_t=None, del_lam=None, ecc=None, fref_ecc=None, vlso=False,
+              quadmon=False):
+    """gwfast/waveforms.py:743-862 (fRef at v = 0); with lam_t/del_lam the tidal terms
     (-39/2 LambdaTilde) v^10 + (-3115/64 LambdaTilde + 6595/364 sqrt(1-4 eta) deltaLambda) v^12 of
-    :849-855 join the series."""
+    :849-855 join the series (``quadmon``: with the spin-induced quadrupole moments of :780-788); with
+    ``ecc`` the eccentric terms of :814-845, referenced at fref_ecc or the lowest frequency of each
+    row of f; ``vlso``: phiref_vlso (:796-798)."""
     Mtot_s = Mc * GMSUN_OVER_C3 / eta ** (3. / 5.)
     v = (PI * Mtot_s * f) ** (1. / 3.)
-    c = pn_coeffs(eta, chi1, chi2, spin_ho=spin_ho)
+    dq1 = dq2 = 0.
+    if quadmon and lam_t is not None:
+        l1, l2 = lam12_from_lamt_dellam(lam_t, del_lam, eta)
+        dq1, dq2 = quad_mon(l1) - 1., quad_mon(l2) - 1.
+    c = pn_coeffs(eta, chi1, chi2, spin_ho=spin_ho, dq1=dq1, dq2=dq2)
+    five = c['five'] * (1. - 3. * math.log(1. / math.sqrt(6.))) if vlso else c['five']
     lv = torch.log(v)
     ser = (1. + c['two'] * v * v + c['three'] * v ** 3 + c['four'] * v ** 4
-           + (c['five'] + c['five_log'] * lv) * v ** 5 + (c['six'] + c['six_log'] * lv) * v ** 6 + c['seven'] * v ** 7)
+           + (five + c['five_log'] * lv) * v ** 5 + (c['six'] + c['six_log'] * lv) * v ** 6 + c['seven'] * v ** 7)
     if lam_t is not None:
         seta = torch.sqrt(torch.where(eta < 0.25, 1.0 - 4.0 * eta, torch.zeros_like(eta)))
         ser = ser + (-0.5 * 39. * lam_t) * v ** 10 + (-3115. / 64. * lam_t + 6595. / 364. * seta * del_lam) * v ** 12
-    return 3. / (128. * eta) * ser / v ** 5 + PI - PI * 0.25
+    if ecc is not None:
+        v0 = torch.amin(v, dim=-1, keepdim=True) if fref_ecc is None else (PI * Mtot_s * fref_ecc) ** (1. / 3.)
+        ser = ser + tf2_ecc_series(v, v0, eta, ecc)
+    return 3. / (128. * eta) * ser / v ** 5 + (0. if vlso else PI) - PI * 0.25
 
 
 def tf2_ampl(f, Mc, dL):
@@ -775,18 +859,21 @@ class Model:
     """Which waveform to evaluate: 'TF2' (``tidal``: with the tidal terms), 'PhenomD', 'PhenomHM' or
     'PhenomD_NRTidalv2'."""
 
-    def __init__(self, name, spin_ho=False, tidal=False, taper_last=None):
+    def __init__(self, name, spin_ho=False, tidal=False, taper_last=None, ecc=False, fref_ecc=None, vlso=False,
+                 kerr=False, quadmon=False):
         assert name in ('TF2', 'PhenomD', 'PhenomHM', 'PhenomD_NRTidalv2')
-        assert not tidal or name == 'TF2'
+        assert not (tidal or ecc or vlso or kerr or quadmon) or name == 'TF2'
         self.name = name
         self.spin_ho = spin_ho
         self.tidal = tidal or name == 'PhenomD_NRTidalv2'
         self.taper_last = taper_last   # PhenomD_NRTidalv2: see nrt_ampl
+        # TaylorF2 options: is_eccentric (fRef_ecc), phiref_vlso, which_ISCO='Kerr', use_QuadMonTid
+        self.ecc, self.fref_ecc, self.vlso, self.kerr, self.quadmon = ecc, fref_ecc, vlso, kerr, quadmon
 
 
     @property
     def params(self):
-        return PARAMS_TIDAL if self.tidal else PARAMS
+        return (PARAMS_TIDAL if self.tidal else PARAMS) + (('ecc',) if self.ecc else ())
 
     @property
     def is_hm(self):
@@ -799,6 +886,8 @@ class Model:
         """Upper grid frequency of each event, in Hz."""
         if self.name == 'PhenomD_NRTidalv2':
             return nrt_fcut(p['Mc'], p['eta'], p['LambdaTilde'], p['deltaLambda'])
+        if self.kerr:
+            return tf2_fcut_kerr(p['Mc'], p['eta'], p['chi1z'], p['chi2z'])
         return self.fcut(p['Mc'], p['eta'])
 
     def ampl(self, f, p):
@@ -811,10 +900,9 @@ class Model:
 
     def phase(self, f, p):
         if self.name == 'TF2':
-            if self.tidal:
-                return tf2_phase(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'], self.spin_ho, p['LambdaTilde'],
-                                 p['deltaLambda'])
-            return tf2_phase(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'], self.spin_ho)
+            lt, dl = (p['LambdaTilde'], p['deltaLambda']) if self.tidal else (None, None)
+            return tf2_phase(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'], self.spin_ho, lt, dl,
+                             p['ecc'] if self.ecc else None, self.fref_ecc, self.vlso, self.quadmon)
         if self.name == 'PhenomD_NRTidalv2':
             return nrt_phase(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'], p['LambdaTilde'], p['deltaLambda'])
         return phd_phase(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'])

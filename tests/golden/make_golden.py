@@ -207,7 +207,8 @@ KEYS = ('Mc', 'eta', 'dL', 'theta', 'phi', 'iota', 'psi', 'tcoal', 'Phicoal', 'c
 
 def make_case(name, wf, dets, events, res, fisher=True):
     out = {'res': np.array(res)}
-    for k in KEYS + (('Lambda1', 'Lambda2', 'LambdaTilde', 'deltaLambda') if wf.is_tidal else ()):
+    for k in (KEYS + (('Lambda1', 'Lambda2', 'LambdaTilde', 'deltaLambda') if wf.is_tidal else ())
+              + (('ecc',) if wf.is_eccentric else ())):
         out['ev_' + k] = np.asarray(events[k], dtype=np.float64)
     sigs = {}
     for dname, (fwall, earth) in dets.items():
@@ -244,9 +245,10 @@ def make_case(name, wf, dets, events, res, fisher=True):
             z = np.zeros_like(ev['Mc'])
             lt = ev['LambdaTilde'] if wf.is_tidal else z
             dl = ev['deltaLambda'] if wf.is_tidal else z
-            h = s.GWstrain(*args, z, z, z, z, lt, dl, z, rot=r, is_chi1chi2=True)
+            ec = ev['ecc'] if wf.is_eccentric else z
+            h = s.GWstrain(*args, z, z, z, z, lt, dl, ec, rot=r, is_chi1chi2=True)
             out['strain_' + tag] = h
-            der = s._AnalyticalDerivatives(*args, z, z, z, z, lt, dl, z, rot=r, use_chi1chi2=True)
+            der = s._AnalyticalDerivatives(*args, z, z, z, z, lt, dl, ec, rot=r, use_chi1chi2=True)
             for nm, dv in zip(('dL', 'theta', 'phi', 'iota', 'psi', 'tcoal', 'Phicoal'), der):
                 if dv is not None:
                     out['dana_%s_%s' % (nm, tag)] = np.asarray(dv)
@@ -313,6 +315,7 @@ def make_gw170817():
 
 
 def main():
+    import gwfast.gwfastUtils as UT
     rng = np.random.default_rng(1000)
     make_case('tf2_L_noearth', WF.TaylorF2_RestrictedPN(), {'Virgo': (10., False)}, events_bns(rng, 4), 400)
     rng = np.random.default_rng(1001)
@@ -328,7 +331,6 @@ def main():
     ev = events_bns(rng, 3)
     ev['Lambda1'] = rng.uniform(100., 1000., 3)
     ev['Lambda2'] = rng.uniform(100., 1000., 3)
-    import gwfast.gwfastUtils as UT
     ev['LambdaTilde'], ev['deltaLambda'] = UT.Lamt_delLam_from_Lam12(ev['Lambda1'], ev['Lambda2'], ev['eta'])
     make_case('tf2tidal_T_earth', WF.TaylorF2_RestrictedPN(is_tidal=True), {'ETS': (5., True), 'Virgo': (10., True)},
               ev, 300)
@@ -344,6 +346,30 @@ def main():
     _FD['lam_h'] = 2e-2
     make_case('nrt_net_earth', WF.IMRPhenomD_NRTidalv2(), {'L1': (10., True), 'ETS': (5., True)}, ev, 300)
     _FD['lam_h'] = None
+    # TaylorF2 options: eccentricity (referenced at each detector's lowest grid frequency, so the two
+    # detectors' fmin differ on purpose), then tidal + eccentric with the quadrupole moments, phiref_vlso
+    # and fRef_ecc, then the Kerr-ISCO cut with the 3.5PN spin terms
+    rng = np.random.default_rng(1006)
+    ev = events_bns(rng, 4)
+    ev['ecc'] = rng.uniform(0.01, 0.15, 4)
+    make_case('tf2ecc_net_earth', WF.TaylorF2_RestrictedPN(is_eccentric=True), {'L1': (10., True), 'ETS': (5., True)},
+              ev, 300)
+    rng = np.random.default_rng(1007)
+    ev = events_bns(rng, 3)
+    ev['chi1z'] = rng.uniform(-.3, .3, 3)
+    ev['chi2z'] = rng.uniform(-.3, .3, 3)
+    ev['ecc'] = rng.uniform(0.01, 0.15, 3)
+    ev['Lambda1'] = np.array([300., 900., 0.7])
+    ev['Lambda2'] = np.array([500., 200., 400.])
+    ev['LambdaTilde'], ev['deltaLambda'] = UT.Lamt_delLam_from_Lam12(ev['Lambda1'], ev['Lambda2'], ev['eta'])
+    _FD['lam_h'] = 2e-2
+    make_case('tf2tidalecc_opts', WF.TaylorF2_RestrictedPN(is_tidal=True, is_eccentric=True, use_QuadMonTid=True,
+                                                           phiref_vlso=True, fRef_ecc=8.),
+              {'Virgo': (10., True), 'ETS': (5., True)}, ev, 300)
+    _FD['lam_h'] = None
+    rng = np.random.default_rng(1008)
+    make_case('tf2kerr_T', WF.TaylorF2_RestrictedPN(which_ISCO='Kerr', use_3p5PN_SpinHO=True), {'ETS': (5., True)},
+              events_bbh(rng, 4, mmax=40., chimax=0.9), 300)
     make_gw170817()
     # KAT from the reference tutorial: GW170817-like TF2 Schwarzschild cut frequency 1590.1 Hz
     z = 0.00980

@@ -15,6 +15,10 @@ CASES = {
     'phm_net_earth': (O.Model('PhenomHM'), {'L1': (10., True), 'ETS': (5., True)}),
     'tf2tidal_T_earth': (O.Model('TF2', tidal=True), {'ETS': (5., True), 'Virgo': (10., True)}),
     'nrt_net_earth': (O.Model('PhenomD_NRTidalv2'), {'L1': (10., True), 'ETS': (5., True)}),
+    'tf2ecc_net_earth': (O.Model('TF2', ecc=True), {'L1': (10., True), 'ETS': (5., True)}),
+    'tf2tidalecc_opts': (O.Model('TF2', tidal=True, ecc=True, quadmon=True, vlso=True, fref_ecc=8.),
+                         {'Virgo': (10., True), 'ETS': (5., True)}),
+    'tf2kerr_T': (O.Model('TF2', spin_ho=True, kerr=True), {'ETS': (5., True)}),
 }
 
 
