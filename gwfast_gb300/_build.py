@@ -10,7 +10,7 @@ INC = os.path.join(os.path.dirname(HERE), 'include')
 OBJ = os.path.join(HERE, '_build')
 LIB = os.path.join(HERE, 'libgwfast_gb300.so')
 SOURCES = ('gwf_run_tf2.cu', 'gwf_run_phd.cu', 'gwf_run_phm.cu', 'gwf_run_tf2t.cu', 'gwf_run_nrt.cu', 'gwf_run_tf2e.cu',
-           'gwf_run_tf2et.cu', 'gwf_cov.cu', 'gwf_api.cu', 'gwf_noalloc.cu', 'gwf_mixed.cu', 'gwf_mlp.cu')
+           'gwf_run_tf2et.cu', 'gwf_run_nsbh.cu', 'gwf_cov.cu', 'gwf_api.cu', 'gwf_noalloc.cu', 'gwf_mixed.cu', 'gwf_mlp.cu')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-I' + CSRC, '-I' + INC]
 

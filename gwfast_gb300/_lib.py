@@ -13,7 +13,8 @@ from . import _build
 
 GWF_OK = 0
 ERRORS = {-1: 'invalid argument', -2: 'CUDA error', -3: 'out of memory', -4: 'timeout', -5: 'unsupported'}
-MODEL_IDS = {'TaylorF2_RestrictedPN': 0, 'IMRPhenomD': 1, 'IMRPhenomHM': 2, 'IMRPhenomD_NRTidalv2': 4}
+MODEL_IDS = {'TaylorF2_RestrictedPN': 0, 'IMRPhenomD': 1, 'IMRPhenomHM': 2, 'IMRPhenomD_NRTidalv2': 4,
+             'IMRPhenomNSBH': 7}
 MODEL_TF2_TIDAL = 3
 MODEL_TF2_ECC = 5
 MODEL_TF2_TIDAL_ECC = 6
@@ -60,6 +61,7 @@ SIGNATURES = {
     'gwf_overlap': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32,
                      ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     'gwf_cov': ([_vp, _vp, _i64, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
+    'gwf_xitide': ([_vp, _vp, _vp, _vp, _i64, _vp], ctypes.c_int),
     'gwf_cov_n': ([_vp, _vp, _i64, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     'gwf_set_refine_cond': ([_vp, _d], ctypes.c_int),
     'gwf_set_segments': ([_vp, ctypes.c_int], ctypes.c_int),
@@ -222,6 +224,13 @@ class Context:
     def cov(self, F, mem=MEM_HOST, cov=None, eps=None, cond=None, n=None, stream=None, n_params=11):
         n = F.shape[0] if n is None else n
         check(load().gwf_cov_n(self.h, ptr(F), n, int(n_params), mem, ptr(cov), ptr(eps), ptr(cond), stream))
+
+    def xitide(self, comp, q, chi_bh):
+        """IMRPhenomNSBH's interpolated xi_tide at the given (compactness, m1/m2, BH spin) points."""
+        c, qq, x = (np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1)) for a in (comp, q, chi_bh))
+        out = np.empty(c.shape[0])
+        check(load().gwf_xitide(self.h, ptr(c), ptr(qq), ptr(x), c.shape[0], ptr(out)))
+        return out
 
 
 def context(device=0):

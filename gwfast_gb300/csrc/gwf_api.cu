@@ -113,6 +113,8 @@ struct gwf_ctx {
   DevBuf wbuf, par2, fcutb, ovb;   // strain-tangent and overlap outputs
   DevBuf core;                     // source-dependent model records, shared by the detectors of a call
   int groups = 1;                  // FP32 network totals: detectors sharing the grid in one launch
+  DevBuf xit;                      // IMRPhenomNSBH xi_tide table, built on first use
+  bool xit_ready = false;
 };
 
 namespace {
@@ -132,7 +134,8 @@ size_t setup_stride_any(int model) {
     case 3: return gwf::setup_stride_m3();
     case 4: return gwf::setup_stride_m4();
     case 5: return gwf::setup_stride_m5();
-    default: return gwf::setup_stride_m6();
+    case 6: return gwf::setup_stride_m6();
+    default: return gwf::setup_stride_m7();
   }
 }
 size_t core_bytes_any(int model) {
@@ -143,7 +146,8 @@ size_t core_bytes_any(int model) {
     case 3: return gwf::core_bytes_m3();
     case 4: return gwf::core_bytes_m4();
     case 5: return gwf::core_bytes_m5();
-    default: return gwf::core_bytes_m6();
+    case 6: return gwf::core_bytes_m6();
+    default: return gwf::core_bytes_m7();
   }
 }
 cudaError_t launch_fisher_any(int model, const gwf::LaunchArgs& a) {
@@ -154,7 +158,8 @@ cudaError_t launch_fisher_any(int model, const gwf::LaunchArgs& a) {
     case 3: return gwf::launch_fisher_m3(a);
     case 4: return gwf::launch_fisher_m4(a);
     case 5: return gwf::launch_fisher_m5(a);
-    default: return gwf::launch_fisher_m6(a);
+    case 6: return gwf::launch_fisher_m6(a);
+    default: return gwf::launch_fisher_m7(a);
   }
 }
 cudaError_t launch_snr_any(int model, const gwf::LaunchArgs& a) {
@@ -165,8 +170,21 @@ cudaError_t launch_snr_any(int model, const gwf::LaunchArgs& a) {
     case 3: return gwf::launch_snr_m3(a);
     case 4: return gwf::launch_snr_m4(a);
     case 5: return gwf::launch_snr_m5(a);
-    default: return gwf::launch_snr_m6(a);
+    case 6: return gwf::launch_snr_m6(a);
+    default: return gwf::launch_snr_m7(a);
   }
+}
+
+// the IMRPhenomNSBH xi_tide table (64 MiB), built on the device the first time it is needed, ordered
+// on the stream of the call that needs it
+int ensure_xitide(gwf_ctx* ctx, cudaStream_t st) {
+  if (ctx->xit_ready) return GWF_OK;
+  const size_t bytes = (size_t)gwf::kXiN * gwf::kXiN * gwf::kXiN * sizeof(double);
+  if (ctx->xit.ensure(bytes)) return fail(GWF_ERR_OOM, "device allocation failed (xi_tide table)");
+  cudaError_t e = gwf::launch_xitide_table((double*)ctx->xit.p, st);
+  if (e != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("xi_tide table: ") + cudaGetErrorString(e));
+  ctx->xit_ready = true;
+  return GWF_OK;
 }
 
 bool is_tf2_model(int model) {
@@ -225,14 +243,15 @@ int validate_common(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_de
   if (!det_ids || n_det < 1) return fail(GWF_ERR_INVALID_ARG, "need at least one detector");
   for (int i = 0; i < n_det; ++i)
     if (det_ids[i] < 0 || det_ids[i] >= (int)ctx->dets.size()) return fail(GWF_ERR_INVALID_ARG, "unknown detector id");
-  if (!wf || wf->model < 0 || wf->model > GWF_WF_TAYLORF2_TIDAL_ECC) return fail(GWF_ERR_INVALID_ARG, "unknown waveform model");
+  if (!wf || wf->model < 0 || wf->model > GWF_WF_PHENOMNSBH) return fail(GWF_ERR_INVALID_ARG, "unknown waveform model");
   if (wf->flags & ~(GWF_TF2_PHIREF_VLSO | GWF_TF2_KERR_ISCO | GWF_TF2_QUADMON_TIDAL))
     return fail(GWF_ERR_INVALID_ARG, "unknown waveform flags");
   if (wf->flags && !is_tf2_model(wf->model))
     return fail(GWF_ERR_INVALID_ARG, "waveform flags apply to the TaylorF2 models only");
   if ((wf->flags & GWF_TF2_QUADMON_TIDAL) && wf->model != GWF_WF_TAYLORF2_TIDAL && wf->model != GWF_WF_TAYLORF2_TIDAL_ECC)
     return fail(GWF_ERR_INVALID_ARG, "GWF_TF2_QUADMON_TIDAL needs a tidal TaylorF2 model");
-  if ((wf->model == GWF_WF_PHENOMD || wf->model == GWF_WF_PHENOMD_NRTIDALV2) && ctx->nq < 2)
+  if ((wf->model == GWF_WF_PHENOMD || wf->model == GWF_WF_PHENOMD_NRTIDALV2 || wf->model == GWF_WF_PHENOMNSBH) &&
+      ctx->nq < 2)
     return fail(GWF_ERR_INVALID_ARG, "IMRPhenomD needs the QNM table (gwf_set_qnm_table)");
   if (!(wf->fcut_par > 0.0)) return fail(GWF_ERR_INVALID_ARG, "fcut_par must be positive");
   if (N < 0 || (N > 0 && !params)) return fail(GWF_ERR_INVALID_ARG, "bad event array");
@@ -586,6 +605,11 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   a.ev.res_ev = dres;
   a.ev.spacing = spacing;
   a.wf = wf_dev(wf);
+  if (wf->model == GWF_WF_PHENOMNSBH) {
+    const int xrc = ensure_xitide(ctx, st);
+    if (xrc) return xrc;
+    a.wf.xitide = (const double*)ctx->xit.p;
+  }
   a.qnm = ctx->d_qnm;
   a.nq = ctx->nq;
   a.per_arm = per_arm || dsda;   // per-arm SNR derivatives need the per-arm Gram sets
@@ -651,19 +675,34 @@ __global__ void fcut_pair_kernel(const double* p1, long long ld1, gwf::WfDesc w1
                                  gwf::WfDesc w2, double fmax, long long N, double* out) {
   const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= N) return;
-  const double f1 = gwf::model_fcut(w1, p1[n], p1[ld1 + n], p1[9 * ld1 + n], p1[10 * ld1 + n]);
-  const double f2 = gwf::model_fcut(w2, p2[n], p2[ld2 + n], p2[9 * ld2 + n], p2[10 * ld2 + n]);
+  // IMRPhenomD_NRTidalv2 ends at 1.2 times its merger frequency (its deformabilities in rows 11, 12)
+  const double f1 = w1.model == GWF_WF_PHENOMD_NRTIDALV2
+                        ? gwf::nrt_fcut(p1[n], p1[ld1 + n], p1[11 * ld1 + n], p1[12 * ld1 + n])
+                        : gwf::model_fcut(w1, p1[n], p1[ld1 + n], p1[9 * ld1 + n], p1[10 * ld1 + n]);
+  const double f2 = w2.model == GWF_WF_PHENOMD_NRTIDALV2
+                        ? gwf::nrt_fcut(p2[n], p2[ld2 + n], p2[11 * ld2 + n], p2[12 * ld2 + n])
+                        : gwf::model_fcut(w2, p2[n], p2[ld2 + n], p2[9 * ld2 + n], p2[10 * ld2 + n]);
   double fu = f1 > f2 ? f1 : f2;
   if (fmax > 0.0) fu = fu > fmax ? fmax : f1;
   out[n] = fu;
 }
 
-size_t stride_of(int model) {
-  return model == 0 ? gwf::setup_stride_m0() : (model == 1 ? gwf::setup_stride_m1() : gwf::setup_stride_m2());
-}
+size_t stride_of(int model) { return setup_stride_any(model); }
+
+// the phase constant the strain outputs add for TaylorF2 with phiref_vlso (gwfast/waveforms.py:796-802)
+double wave_dphi(const gwf_wf_desc* wf) { return (is_tf2_model(wf->model) && (wf->flags & GWF_TF2_PHIREF_VLSO)) ? -M_PI : 0.0; }
 
 cudaError_t launch_wave(const gwf::LaunchArgs& a, const gwf::WaveOut& o) {
-  return a.wf.model == 0 ? gwf::launch_wave_m0(a, o) : (a.wf.model == 1 ? gwf::launch_wave_m1(a, o) : gwf::launch_wave_m2(a, o));
+  switch (a.wf.model) {
+    case 0: return gwf::launch_wave_m0(a, o);
+    case 1: return gwf::launch_wave_m1(a, o);
+    case 2: return gwf::launch_wave_m2(a, o);
+    case 3: return gwf::launch_wave_m3(a, o);
+    case 4: return gwf::launch_wave_m4(a, o);
+    case 5: return gwf::launch_wave_m5(a, o);
+    case 6: return gwf::launch_wave_m6(a, o);
+    default: return gwf::launch_wave_m7(a, o);
+  }
 }
 
 // events per output launch so that a staging buffer of per_event bytes each stays near 1 GiB
@@ -721,12 +760,31 @@ int gwf_ctx_destroy(gwf_ctx* ctx) {
   ctx->osda.release(); ctx->osdn.release(); ctx->mix_sda.release(); ctx->mix_sdn.release();
   ctx->wbuf.release(); ctx->par2.release(); ctx->fcutb.release(); ctx->ovb.release();
   ctx->core.release();
+  ctx->xit.release();
   for (auto& g : ctx->graph_cache) cudaGraphExecDestroy(g.second.exec);
   ctx->graph_cache.clear();
   ctx->hpar.release(); ctx->hout.release();
   cudaEventDestroy(ctx->scratch_free);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
+  return GWF_OK;
+}
+
+int gwf_xitide(gwf_ctx* ctx, const double* comp, const double* q, const double* chi_bh, int64_t n, double* out) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && (!comp || !q || !chi_bh || !out))) return fail(GWF_ERR_INVALID_ARG, "bad arguments");
+  cudaStream_t st = ctx->stream;
+  rc = ensure_xitide(ctx, st);
+  if (rc || n == 0) return rc;
+  if (ctx->fin.ensure((size_t)n * 4 * sizeof(double))) return fail(GWF_ERR_OOM, "device allocation failed");
+  double* d = (double*)ctx->fin.p;
+  GWF_CK(cudaMemcpyAsync(d, comp, n * sizeof(double), cudaMemcpyHostToDevice, st));
+  GWF_CK(cudaMemcpyAsync(d + n, q, n * sizeof(double), cudaMemcpyHostToDevice, st));
+  GWF_CK(cudaMemcpyAsync(d + 2 * n, chi_bh, n * sizeof(double), cudaMemcpyHostToDevice, st));
+  GWF_CK(gwf::launch_xitide_eval((const double*)ctx->xit.p, d, d + n, d + 2 * n, n, d + 3 * n, st));
+  GWF_CK(cudaMemcpyAsync(out, d + 3 * n, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  GWF_CK(cudaStreamSynchronize(st));
   return GWF_OK;
 }
 
@@ -940,18 +998,19 @@ int gwf_strain_derivs(gwf_ctx* ctx, int det_id, const gwf_wf_desc* wf, const dou
   rc = validate_common(ctx, 1, &det_id, wf, params, ld, n_events, res, nullptr, spacing, mem);
   if (rc) return rc;
   if (!out) return fail(GWF_ERR_INVALID_ARG, "no output requested");
-  if (wf->model >= GWF_WF_TAYLORF2_TIDAL) return fail(GWF_ERR_UNSUPPORTED, "strain derivatives are implemented for the 11-parameter models");
   const int64_t N = n_events;
   if (N == 0) return GWF_OK;
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  const int npar = npar_of(wf->model);
   const double* dp;
   int64_t dld;
   const int* dres;
-  rc = stage_inputs(ctx, params, ld, N, nullptr, mem, st, &dp, &dld, &dres);
+  rc = stage_inputs(ctx, params, ld, N, nullptr, mem, st, &dp, &dld, &dres, npar);
   if (rc) return rc;
+  if (wf->model == GWF_WF_PHENOMNSBH && (rc = ensure_xitide(ctx, st))) return rc;
   const DetRec& r = ctx->dets[det_id];
   const int NA = r.desc.shape == GWF_SHAPE_T ? 3 : 1;
-  const size_t per_ev = (size_t)NA * gwf::NP * (size_t)res * 2 * sizeof(double);
+  const size_t per_ev = (size_t)NA * npar * (size_t)res * 2 * sizeof(double);
   const int64_t chunk = mem == GWF_MEM_DEVICE ? (N < gwf::kChunk ? N : gwf::kChunk) : wave_chunk(per_ev);
   const int64_t cap = chunk < N ? chunk : N;
   if (ctx->setup.ensure((size_t)cap * stride_of(wf->model))) return fail(GWF_ERR_OOM, "device allocation failed (set-up scratch)");
@@ -967,6 +1026,7 @@ int gwf_strain_derivs(gwf_ctx* ctx, int det_id, const gwf_wf_desc* wf, const dou
   a.ev.spacing = spacing;
   a.det = dev_of(r);
   a.wf = wf_dev(wf);
+  if (wf->model == GWF_WF_PHENOMNSBH) a.wf.xitide = (const double*)ctx->xit.p;
   a.qnm = ctx->d_qnm;
   a.nq = ctx->nq;
   a.out_arm = a.out_det = nullptr;
@@ -980,6 +1040,7 @@ int gwf_strain_derivs(gwf_ctx* ctx, int det_id, const gwf_wf_desc* wf, const dou
     const int64_t cnt = (N - n0) < chunk ? (N - n0) : chunk;
     gwf::WaveOut o{};
     o.mode = gwf::WAVE_DERIVS;
+    o.dphi = wave_dphi(wf);
     o.n0 = n0;
     o.cnt = cnt;
     o.R_out = res;
@@ -997,7 +1058,7 @@ int gwf_strain_derivs(gwf_ctx* ctx, int det_id, const gwf_wf_desc* wf, const dou
     if (mem == GWF_MEM_HOST) {   // rows [n0, n0 + cnt) of each (arm, parameter) block
       const size_t row = (size_t)res * 2 * sizeof(double);
       GWF_CK(cudaMemcpy2DAsync(out + (size_t)n0 * res * 2, (size_t)N * row, ctx->wbuf.p, (size_t)cnt * row,
-                               (size_t)cnt * row, (size_t)NA * gwf::NP, cudaMemcpyDeviceToHost, st));
+                               (size_t)cnt * row, (size_t)NA * npar, cudaMemcpyDeviceToHost, st));
     }
   }
   GWF_CK(cudaEventRecord(ctx->scratch_free, st));
@@ -1014,17 +1075,16 @@ int gwf_overlap(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* 
   if (!rc) rc = validate_common(ctx, n_det, det_ids, wf2, params2, ld2, n_events, res, nullptr, GWF_SPACING_GEOM, mem);
   if (rc) return rc;
   if (!out_ov || !out_n1 || !out_n2) return fail(GWF_ERR_INVALID_ARG, "overlap needs all three outputs");
-  if (wf1->model >= GWF_WF_TAYLORF2_TIDAL || wf2->model >= GWF_WF_TAYLORF2_TIDAL)
-    return fail(GWF_ERR_UNSUPPORTED, "the overlap is implemented for the 11-parameter models");
   const int64_t N = n_events;
   if (N == 0) return GWF_OK;
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
   const double *dp1, *dp2;
   int64_t dld1, dld2;
   const int* dres;
-  rc = stage_inputs(ctx, params1, ld1, N, nullptr, mem, st, &dp1, &dld1, &dres);
-  if (!rc) rc = stage_inputs_to(ctx, ctx->par2, params2, ld2, N, nullptr, mem, st, &dp2, &dld2, &dres);
+  rc = stage_inputs(ctx, params1, ld1, N, nullptr, mem, st, &dp1, &dld1, &dres, npar_of(wf1->model));
+  if (!rc) rc = stage_inputs_to(ctx, ctx->par2, params2, ld2, N, nullptr, mem, st, &dp2, &dld2, &dres, npar_of(wf2->model));
   if (rc) return rc;
+  if ((wf1->model == GWF_WF_PHENOMNSBH || wf2->model == GWF_WF_PHENOMNSBH) && (rc = ensure_xitide(ctx, st))) return rc;
   const size_t per_ev = (size_t)2 * res * 2 * sizeof(double);   // at most two computed arms
   const int64_t chunk = wave_chunk(per_ev);
   const int64_t cap = chunk < N ? chunk : N;
@@ -1072,14 +1132,18 @@ int gwf_overlap(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* 
       o.n1 = dn1 + (size_t)i * N;
       o.n2 = dn2 + (size_t)i * N;
       o.mode = gwf::WAVE_STORE;
+      o.dphi = wave_dphi(wf1);
       a.ev.p = dp1;
       a.ev.ld = dld1;
       a.wf = wf_dev(wf1);
+      a.wf.xitide = (const double*)ctx->xit.p;
       cudaError_t e = launch_wave(a, o);
       o.mode = gwf::WAVE_OVERLAP;
+      o.dphi = wave_dphi(wf2);
       a.ev.p = dp2;
       a.ev.ld = dld2;
       a.wf = wf_dev(wf2);
+      a.wf.xitide = (const double*)ctx->xit.p;
       if (e == cudaSuccess) e = launch_wave(a, o);
       if (e != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
     }

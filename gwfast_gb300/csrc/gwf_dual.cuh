@@ -29,6 +29,9 @@ template <> __host__ __device__ __forceinline__ float tatan(float x) { return at
 template <class T> __host__ __device__ __forceinline__ T tpow(T x, T y);
 template <> __host__ __device__ __forceinline__ double tpow(double x, double y) { return pow(x, y); }
 template <> __host__ __device__ __forceinline__ float tpow(float x, float y) { return powf(x, y); }
+template <class T> __host__ __device__ __forceinline__ T ttanh(T x);
+template <> __host__ __device__ __forceinline__ double ttanh(double x) { return tanh(x); }
+template <> __host__ __device__ __forceinline__ float ttanh(float x) { return tanhf(x); }
 template <class T> __host__ __device__ __forceinline__ void tsincos(T x, T* s, T* c);
 template <> __host__ __device__ __forceinline__ void tsincos(double x, double* s, double* c) { sincos(x, s, c); }
 template <> __host__ __device__ __forceinline__ void tsincos(float x, float* s, float* c) { sincosf(x, s, c); }
@@ -160,6 +163,10 @@ template <class T, int N> __host__ __device__ __forceinline__ Dual<T, N> datan(c
 template <class T> __host__ __device__ __forceinline__ T dpowc(T x, T p) { return tpow(x, p); }
 template <class T, int N> __host__ __device__ __forceinline__ Dual<T, N> dpowc(const Dual<T, N>& a, T p) {
   const T y = tpow(a.v, p); return chain(a, y, p * y / a.v);
+}
+template <class T> __host__ __device__ __forceinline__ T dtanh(T x) { return ttanh(x); }
+template <class T, int N> __host__ __device__ __forceinline__ Dual<T, N> dtanh(const Dual<T, N>& a) {
+  const T t = ttanh(a.v); return chain(a, t, T(1) - t * t);
 }
 template <class T> __host__ __device__ __forceinline__ T dabs(T x) { return x < T(0) ? -x : x; }
 template <class T, int N> __host__ __device__ __forceinline__ Dual<T, N> dabs(const Dual<T, N>& a) {

@@ -27,13 +27,13 @@ enum { I_MC = 0, I_ETA, I_DL, I_TH, I_PH, I_IO, I_PS, I_TC, I_PC, I_C1, I_C2, I_
 template <int MODEL> __host__ __device__ constexpr int np_of() {
   return MODEL == 5 ? 12 : (MODEL == 6 ? 14 : (MODEL >= 3 ? 13 : 11));
 }
-template <int MODEL> __host__ __device__ constexpr bool is_tf2() { return MODEL == 0 || MODEL == 3 || MODEL >= 5; }
-template <int MODEL> __host__ __device__ constexpr bool has_tidal() { return MODEL == 3 || MODEL == 4 || MODEL == 6; }
-template <int MODEL> __host__ __device__ constexpr bool has_ecc() { return MODEL >= 5; }
+template <int MODEL> __host__ __device__ constexpr bool is_tf2() { return MODEL == 0 || MODEL == 3 || MODEL == 5 || MODEL == 6; }
+template <int MODEL> __host__ __device__ constexpr bool has_tidal() { return MODEL == 3 || MODEL == 4 || MODEL == 6 || MODEL == 7; }
+template <int MODEL> __host__ __device__ constexpr bool has_ecc() { return MODEL == 5 || MODEL == 6; }
 template <int MODEL> __host__ __device__ constexpr int ecc_col() { return MODEL == 6 ? 13 : 11; }
 // intrinsic tangent directions of the per-event duals: Mc, eta, chi1z, chi2z (+ LambdaTilde,
 // deltaLambda for IMRPhenomD_NRTidalv2, model 4, whose set-up depends on them non-linearly)
-template <int MODEL> __host__ __device__ constexpr int ndir_of() { return MODEL == 4 ? 6 : 4; }
+template <int MODEL> __host__ __device__ constexpr int ndir_of() { return (MODEL == 4 || MODEL == 7) ? 6 : 4; }
 template <int MODEL> using DualOf = Dual<double, ndir_of<MODEL>()>;
 __host__ __device__ constexpr int ne_of(int npr) { return npr * (npr + 1) / 2; }
 __host__ __device__ constexpr int nex_of(int npr) { return ne_of(npr) + npr; }
@@ -81,6 +81,7 @@ struct WfDesc {
   int flags;             // TaylorF2 options: kTF2Vlso | kTF2KerrIsco | kTF2QuadMon
   int pad_;
   double fref_ecc;       // eccentric TaylorF2: reference frequency of ecc in Hz (<= 0: lowest grid frequency)
+  const double* xitide = nullptr;   // IMRPhenomNSBH: the xi_tide table on the device (200^3)
 };
 
 static __constant__ unsigned char kPairA[NE] = {0,0,0,0,0,0,0,0,0,0,0,1,1,1,1,1,1,1,1,1,1,2,2,2,2,2,2,2,2,2,3,3,3,3,3,3,3,3,4,4,4,4,4,4,4,5,5,5,5,5,5,6,6,6,6,6,7,7,7,7,8,8,8,9,9,10};
@@ -260,6 +261,7 @@ union EvUnion {
   TF2TEv tf2t;
   NRTEv nrt;
   TF2EEv tf2e;
+  NSBHEv nsbh;
 };
 
 // Kerr ISCO radius (prograde for chi > 0), gwfast/waveforms.py:934-937
@@ -300,7 +302,7 @@ __host__ __device__ inline double tf2_kerr_fcut(double Mc, double eta, double ch
 __host__ __device__ inline double model_fcut(const WfDesc& wf, double Mc, double eta, double chi1 = 0.0,
                                              double chi2 = 0.0) {
   // TaylorF2 (models 0, 3, 5, 6): fcut_par is fHigh in Hz Msun, or the Kerr ISCO; the IMR models: a cut in M f
-  const bool tf2 = wf.model == 0 || wf.model == 3 || wf.model >= 5;
+  const bool tf2 = wf.model == 0 || wf.model == 3 || wf.model == 5 || wf.model == 6;
   if (tf2 && (wf.flags & kTF2KerrIsco)) return tf2_kerr_fcut(Mc, eta, chi1, chi2);
   return tf2 ? wf.fcut_par / (Mc / pow(eta, 0.6)) : wf.fcut_par / (Mc * kG3 / pow(eta, 0.6));
 }
@@ -347,14 +349,19 @@ __device__ __forceinline__ void grid_point(const GridEv& g, int spacing, int k, 
 template <int MODEL>
 __device__ inline void event_setup(EvUnion& E, const DetDev& d, const WfDesc& wf, const double* q, int nq,
                                    double Mc, double eta, double chi1, double chi2, double dL, double lam_t,
-                                   double del_lam, double ecc = 0.0) {
+                                   double del_lam, double ecc = 0.0, double fgrid_max = 0.0) {
   const D4 mc = D4::seed(Mc, P_MC), et = D4::seed(eta, P_ETA), c1 = D4::seed(chi1, P_CHI1), c2 = D4::seed(chi2, P_CHI2);
+  if (MODEL == 7) {
+    nsbh_setup(E.nsbh, D6::seed(Mc, P_MC), D6::seed(eta, P_ETA), D6::seed(chi1, P_CHI1), D6::seed(chi2, P_CHI2), dL,
+               d.fmin, fgrid_max, q, q + nq, q + 2 * nq, nq, D6::seed(lam_t, P_LT), D6::seed(del_lam, P_DLT), wf.xitide);
+    return;
+  }
   if (MODEL == 4) {
     nrt_setup(E.nrt, D6::seed(Mc, P_MC), D6::seed(eta, P_ETA), D6::seed(chi1, P_CHI1), D6::seed(chi2, P_CHI2), dL,
               d.fmin, q, q + nq, q + 2 * nq, nq, D6::seed(lam_t, P_LT), D6::seed(del_lam, P_DLT));
     return;
   }
-  if (MODEL >= 5)
+  if (MODEL == 5 || MODEL == 6)
     tf2e_setup(E.tf2e, mc, et, c1, c2, dL, wf.spin_ho != 0, lam_t, del_lam, wf.flags, ecc, d.fmin, wf.fref_ecc);
   else if (MODEL == 3) tf2t_setup(E.tf2t, mc, et, c1, c2, dL, wf.spin_ho != 0, lam_t, del_lam, wf.flags);
   else if (MODEL == 0) tf2_setup(E.tf2, mc, et, c1, c2, dL, wf.spin_ho != 0, wf.flags);
@@ -368,10 +375,10 @@ constexpr double kTF2PhaseConst = 0.75 * kPi;
 
 // the TaylorF2 record of the TaylorF2 models (0, 3, 5, 6)
 template <int MODEL> __device__ __forceinline__ const TF2Ev& tf2_base(const EvUnion& E) {
-  return MODEL == 3 ? E.tf2t.b : (MODEL >= 5 ? E.tf2e.t.b : E.tf2);
+  return MODEL == 3 ? E.tf2t.b : (MODEL == 5 || MODEL == 6 ? E.tf2e.t.b : E.tf2);
 }
 template <int MODEL> __device__ __forceinline__ const TF2TEv& tf2_tidal(const EvUnion& E) {
-  return MODEL >= 5 ? E.tf2e.t : E.tf2t;
+  return MODEL == 5 || MODEL == 6 ? E.tf2e.t : E.tf2t;
 }
 
 // TaylorF2 phase and amplitude of models 0, 3, 5, 6 at one point (tidal and eccentric parts added)
@@ -404,10 +411,12 @@ __device__ __forceinline__ void wave_point_dual(const EvUnion& E, const ProjEv& 
     for (int k = 0; k < 4; ++k) { dP[k] = {Pd.re.d[k], Pd.im.d[k]}; dC[k] = {Cd.re.d[k], Cd.im.d[k]}; }
     dPi = {dPv.re, dPv.im}; dCi = {dCv.re, dCv.im};
     if (EARTH) tau = tau_star_point<D4>(E.hm.k.Ms, E.hm.k.vM, E.hm.k.eta, exp(lnf / 3.0));
-  } else if constexpr (MODEL == 4) {
+  } else if constexpr (MODEL == 4 || MODEL == 7) {
     D6 A, Phi;
-    nrt_point<D6>(E.nrt, f, A, Phi);
-    if (EARTH) tau = tau_star_point<D6>(E.nrt.k.Ms, E.nrt.k.vM, E.nrt.k.eta, exp(lnf / 3.0));
+    const PhdCoreT<D6>& kc = MODEL == 4 ? E.nrt.k : E.nsbh.k;
+    if constexpr (MODEL == 4) nrt_point<D6>(E.nrt, f, A, Phi);
+    else nsbh_point<D6>(E.nsbh, f, A, Phi);
+    if (EARTH) tau = tau_star_point<D6>(kc.Ms, kc.vM, kc.eta, exp(lnf / 3.0));
     phi0 = Phi.v;
     P = {pj.cp * A.v, 0.0};
     C = {pj.ci * A.v, 0.0};
@@ -445,6 +454,37 @@ __device__ __forceinline__ void wave_point_dual(const EvUnion& E, const ProjEv& 
   }
 }
 
+// Fisher columns formed analytically per point (their parameters enter the phase only):
+// tidal TaylorF2 d Phi / d LambdaTilde, d Phi / d deltaLambda (with use_QuadMonTid also through c4 v^-1
+// and c6 v of the series); eccentric TaylorF2 d Phi / d ecc = 2 Phi_ecc / ecc (the eccentric phase is
+// proportional to ecc^2). Written as d h = -i h d Phi into D.
+template <int MODEL>
+__device__ __forceinline__ void analytic_tangents(const EvUnion& E, double lnf, double& dphl, double& dphd, double& dphe) {
+  dphl = dphd = dphe = 0.0;
+  if constexpr (MODEL == 3 || MODEL == 6) {
+    const TF2TEv& t = tf2_tidal<MODEL>(E);
+    const double v = t.b.vM.v * exp(lnf / 3.0), v2 = v * v, v5 = v2 * v2 * v;
+    const double A = t.b.pn.A.v;
+    dphl = A * (v5 * (-19.5 - (3115.0 / 64.0) * v2) + t.q4l / v + t.q6l * v);
+    dphd = A * (v5 * v2 * t.s12.v + t.q4d / v + t.q6d * v);
+  }
+  if constexpr (has_ecc<MODEL>()) {
+    const TF2EEv& e = E.tf2e;
+    if (e.ecc != 0.0) {
+      const double v = e.t.b.vM.v * exp(lnf / 3.0), lnv = e.t.b.lnvM.v + lnf / 3.0;
+      dphe = 2.0 * tf2_ecc_phase<double>(e, v, lnv, lnf) / e.ecc;
+    }
+  }
+}
+template <int MODEL>
+__device__ __forceinline__ void analytic_columns(const cd& H, double dphl, double dphd, double dphe, cd* D) {
+  if constexpr (MODEL == 3 || MODEL == 6) {
+    D[I_LT] = cscale(cmuli(H), -dphl);
+    D[I_DLT] = cscale(cmuli(H), -dphd);
+  }
+  if constexpr (has_ecc<MODEL>()) D[ecc_col<MODEL>()] = cscale(cmuli(H), -dphe);
+}
+
 // value-only waveform with its phase: P, C (hp = P, hc = i C) and phi0 as in wave_point_dual
 template <int MODEL, bool EARTH>
 __device__ __forceinline__ void wave_point_full(const EvUnion& E, const ProjEv& pj, double f, double lnf,
@@ -458,9 +498,11 @@ __device__ __forceinline__ void wave_point_full(const EvUnion& E, const ProjEv& 
     if (EARTH) tau = tau_star_point<double>(E.hm.k.Ms, E.hm.k.vM, E.hm.k.eta, exp(lnf / 3.0));
   } else {
     double A, Phi;
-    if (MODEL == 4) {
-      nrt_point<double>(E.nrt, f, A, Phi);
-      if (EARTH) tau = tau_star_point<double>(E.nrt.k.Ms, E.nrt.k.vM, E.nrt.k.eta, exp(lnf / 3.0));
+    if (MODEL == 4 || MODEL == 7) {
+      const PhdCoreT<D6>& kc = MODEL == 4 ? E.nrt.k : E.nsbh.k;
+      if (MODEL == 4) nrt_point<double>(E.nrt, f, A, Phi);
+      else nsbh_point<double>(E.nsbh, f, A, Phi);
+      if (EARTH) tau = tau_star_point<double>(kc.Ms, kc.vM, kc.eta, exp(lnf / 3.0));
     } else if (is_tf2<MODEL>()) {
       const TF2Ev& t = tf2_base<MODEL>(E);
       const double f13 = exp(lnf / 3.0);
@@ -488,9 +530,11 @@ __device__ __forceinline__ void wave_point_val(const EvUnion& E, const ProjEv& p
     if (EARTH) tau = tau_star_point<double>(E.hm.k.Ms, E.hm.k.vM, E.hm.k.eta, exp(lnf / 3.0));
   } else {
     double A, Phi;
-    if (MODEL == 4) {
-      nrt_point<double>(E.nrt, f, A, Phi);
-      if (EARTH) tau = tau_star_point<double>(E.nrt.k.Ms, E.nrt.k.vM, E.nrt.k.eta, exp(lnf / 3.0));
+    if (MODEL == 4 || MODEL == 7) {
+      const PhdCoreT<D6>& kc = MODEL == 4 ? E.nrt.k : E.nsbh.k;
+      if (MODEL == 4) nrt_point<double>(E.nrt, f, A, Phi);
+      else nsbh_point<double>(E.nsbh, f, A, Phi);
+      if (EARTH) tau = tau_star_point<double>(kc.Ms, kc.vM, kc.eta, exp(lnf / 3.0));
     } else if (is_tf2<MODEL>()) {
       const TF2Ev& t = tf2_base<MODEL>(E);
       const double f13 = exp(lnf / 3.0);
@@ -519,7 +563,8 @@ __host__ __device__ constexpr size_t wave_bytes() {
   return MODEL == 0 ? sizeof(TF2Ev)
                     : (MODEL == 1 ? sizeof(PhdEv)
                                   : (MODEL == 2 ? sizeof(HMEv)
-                                                : (MODEL == 3 ? sizeof(TF2TEv) : (MODEL == 4 ? sizeof(NRTEv) : sizeof(TF2EEv)))));
+                                                : (MODEL == 3 ? sizeof(TF2TEv)
+                                                              : (MODEL == 4 ? sizeof(NRTEv) : (MODEL == 7 ? sizeof(NSBHEv) : sizeof(TF2EEv))))));
 }
 // the 22-mode models also carry the phase-tangent basis used by the FP32 kernel
 template <int MODEL>
@@ -567,9 +612,10 @@ __global__ void __launch_bounds__(64) setup_kernel(EvBatch ev, DetDev det, WfDes
       if (MODEL == 1) phd_ref(E.phd, det.fmin);
       if (MODEL == 2) hm_ref(E.hm, det.fmin);
       if (MODEL == 4) nrt_ref(E.nrt, det.fmin);
-      if (MODEL >= 5) tf2e_ref(E.tf2e, det.fmin, wf.fref_ecc);
+      if (MODEL == 5 || MODEL == 6) tf2e_ref(E.tf2e, det.fmin, wf.fref_ecc);
+      if (MODEL == 7) nsbh_ref(E.nsbh, det.fmin, h.g.fcut);
     } else {
-      event_setup<MODEL>(E, det, wf, qnm, nq, Mc, eta, c1, c2, dL, lt, dlt, ecc);
+      event_setup<MODEL>(E, det, wf, qnm, nq, Mc, eta, c1, c2, dL, lt, dlt, ecc, h.g.fcut);
       if (MODEL == 2)
         for (int mode = 0; mode < 6; ++mode)
           hm_setup_mode(E.hm, mode, D4::seed(eta, P_ETA), D4::seed(c1, P_CHI1), D4::seed(c2, P_CHI2), io);
@@ -768,25 +814,8 @@ __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<N
       } else {
         ts = S.tsc;
       }
-      // tidal TaylorF2: d Phi / d LambdaTilde and d Phi / d deltaLambda at this point (with
-      // use_QuadMonTid also through c4 v^-1 and c6 v of the series); eccentric TaylorF2: the
-      // eccentric phase is proportional to ecc^2, so d Phi / d ecc = 2 Phi_ecc / ecc
-      double dphl = 0.0, dphd = 0.0, dphe = 0.0;
-      if constexpr (MODEL == 3 || MODEL == 6) {
-        const TF2TEv& t = tf2_tidal<MODEL>(S.E);
-        const double v = t.b.vM.v * exp(lnf / 3.0), v2 = v * v, v5 = v2 * v2 * v;
-        const double A = t.b.pn.A.v;
-        dphl = A * (v5 * (-19.5 - (3115.0 / 64.0) * v2) + t.q4l / v + t.q6l * v);
-        dphd = A * (v5 * v2 * t.s12.v + t.q4d / v + t.q6d * v);
-      }
-      if constexpr (has_ecc<MODEL>()) {
-        const TF2EEv& e = S.E.tf2e;
-        if (e.ecc != 0.0) {
-          const double f13 = exp(lnf / 3.0);
-          const double v = e.t.b.vM.v * f13, lnv = e.t.b.lnvM.v + lnf / 3.0;
-          dphe = 2.0 * tf2_ecc_phase<double>(e, v, lnv, lnf) / e.ecc;
-        }
-      }
+      double dphl, dphd, dphe;
+      analytic_tangents<MODEL>(S.E, lnf, dphl, dphd, dphe);
 #pragma unroll
       for (int a = 0; a < NARM; ++a) {
         ArmPat ap;
@@ -794,11 +823,7 @@ __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<N
         else ap = S.apc[a];
         arm_derivs<NI>(S.pj, ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D[a]);
         const cd H = cadd(cscale(P, ap.Fp), cscale(cmuli(C), ap.Fc));
-        if constexpr (MODEL == 3 || MODEL == 6) {   // h ~ e^{-i Phi}: d h / d Lambda = -i h d Phi / d Lambda
-          D[a][I_LT] = cscale(cmuli(H), -dphl);
-          D[a][I_DLT] = cscale(cmuli(H), -dphd);
-        }
-        if constexpr (has_ecc<MODEL>()) D[a][ecc_col<MODEL>()] = cscale(cmuli(H), -dphe);
+        analytic_columns<MODEL>(H, dphl, dphd, dphe, D[a]);
         D[a][NPM] = sd ? H : cd{0.0, 0.0};
       }
     } else {

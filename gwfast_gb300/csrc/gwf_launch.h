@@ -60,11 +60,24 @@ cudaError_t launch_fisher_m6(const LaunchArgs& a);   // tidal eccentric TaylorF2
 cudaError_t launch_snr_m6(const LaunchArgs& a);
 size_t setup_stride_m6();
 size_t core_bytes_m6();
+cudaError_t launch_fisher_m7(const LaunchArgs& a);   // IMRPhenomNSBH: FP64, 13 parameters
+cudaError_t launch_snr_m7(const LaunchArgs& a);
+size_t setup_stride_m7();
+size_t core_bytes_m7();
+// IMRPhenomNSBH xi_tide table (200^3 doubles) and its interpolation at given points
+cudaError_t launch_xitide_table(double* tab, cudaStream_t st);
+cudaError_t launch_xitide_eval(const double* tab, const double* C, const double* q, const double* chi, long long n,
+                               double* out, cudaStream_t st);
 // strain tangent / strain / overlap outputs (gwf_wave_out.cuh): set-up and output launch for
 // events [o.n0, o.n0 + o.cnt) of a.ev; a.scratch holds at least o.cnt records
 cudaError_t launch_wave_m0(const LaunchArgs& a, const WaveOut& o);
 cudaError_t launch_wave_m1(const LaunchArgs& a, const WaveOut& o);
 cudaError_t launch_wave_m2(const LaunchArgs& a, const WaveOut& o);
+cudaError_t launch_wave_m3(const LaunchArgs& a, const WaveOut& o);
+cudaError_t launch_wave_m4(const LaunchArgs& a, const WaveOut& o);
+cudaError_t launch_wave_m5(const LaunchArgs& a, const WaveOut& o);
+cudaError_t launch_wave_m6(const LaunchArgs& a, const WaveOut& o);
+cudaError_t launch_wave_m7(const LaunchArgs& a, const WaveOut& o);
 // FP32 network total of a group of detectors sharing the grid (gwf_kernels_f32.cuh); a.det is the
 // group's first detector, a.scratch holds g.nd slices of a.cap_events set-up records
 cudaError_t launch_group_m0(const LaunchArgs& a, const GroupDev& g);

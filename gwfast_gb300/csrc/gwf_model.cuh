@@ -852,6 +852,314 @@ __device__ __forceinline__ void nrt_point(const NRTEvT<C>& e, typename Real<S>::
   phase = ph;
 }
 
+// ------------------------------------------------------------------ IMRPhenomNSBH (gwfast/waveforms.py:2752-3284)
+// Object 1 is the black hole, object 2 the neutron star; only Lambda2 enters (the BH deformability
+// recovered from LambdaTilde, deltaLambda is discarded).
+
+// xi_tide grid (gwfast/waveforms.py:3306-3308): numpy linspace values, k * step + start with the last
+// node set to the end point, so that the cell search matches numpy's searchsorted exactly
+constexpr int kXiN = 200;
+__host__ __device__ inline double xi_grid(int dim, int k) {
+  const double lo = dim == 0 ? 0.1 : (dim == 1 ? 1.0 : -1.0), hi = dim == 0 ? 0.5 : (dim == 1 ? 100.0 : 1.0);
+  if (k == kXiN - 1) return hi;
+#ifdef __CUDA_ARCH__
+  return __dadd_rn(__dmul_rn((double)k, (hi - lo) / (kXiN - 1)), lo);
+#else
+  const volatile double t = (double)k * ((hi - lo) / (kXiN - 1));
+  return t + lo;
+#endif
+}
+
+// trilinear interpolation of the table tab[i][j][k] as gwfast's RegularGridInterpolator_JAX
+// (gwfast/gwfastUtils.py:1113-1200): cell from searchsorted - 1 clamped to the grid (linear
+// extrapolation outside), edge sum in itertools.product order, NaN where that code's out-of-bounds
+// test (as written: (oob + x) < lo, then (oob + x) > hi, per dimension in turn) is set
+template <class D>
+__device__ inline D xitide_interp(const double* tab, const D& C, const D& q, const D& chi) {
+  const D* x[3] = {&C, &q, &chi};
+  int idx[3];
+  D y[3];
+  bool oob = false;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const double xv = val(*x[d]);
+    // searchsorted(grid, x, 'left') - 1: the last node below x (a guess from the spacing, then exact)
+    double t = (xv - xi_grid(d, 0)) / ((xi_grid(d, kXiN - 1) - xi_grid(d, 0)) / (kXiN - 1));
+    t = t == t ? fmin(fmax(t, -2.0), (double)kXiN) : 0.0;
+    int i = (int)floor(t);
+    i = i < -1 ? -1 : (i > kXiN - 1 ? kXiN - 1 : i);
+    while (i >= 0 && !(xi_grid(d, i) < xv)) --i;
+    while (i + 1 <= kXiN - 1 && xi_grid(d, i + 1) < xv) ++i;
+    i = i < 0 ? 0 : (i > kXiN - 2 ? kXiN - 2 : i);
+    idx[d] = i;
+    const double g0 = xi_grid(d, i), g1 = xi_grid(d, i + 1);
+    y[d] = (*x[d] - g0) / (g1 - g0);
+    oob = ((double)oob + xv) < xi_grid(d, 0);
+    oob = ((double)oob + xv) > xi_grid(d, kXiN - 1);
+  }
+  D out(0.0);
+#pragma unroll
+  for (int e0 = 0; e0 < 2; ++e0)
+#pragma unroll
+    for (int e1 = 0; e1 < 2; ++e1)
+#pragma unroll
+      for (int e2 = 0; e2 < 2; ++e2) {
+        const double v = tab[((size_t)(idx[0] + e0) * kXiN + (idx[1] + e1)) * kXiN + (idx[2] + e2)];
+        const D w = (e0 ? y[0] : 1.0 - y[0]) * (e1 ? y[1] : 1.0 - y[1]) * (e2 ? y[2] : 1.0 - y[2]);
+        out = out + v * w;
+      }
+  if (oob) out = D(nan(""));
+  return out;
+}
+
+// remnant fits (gwfast/waveforms.py:2854-2874, :3124-3151): remnant-spin and remnant-mass models of
+// arXiv:1903.11622, the orbital angular momentum fit of arXiv:1611.00332 eq. 16 and its radiated energy
+// eq. 27
+template <class D>
+__device__ inline D nsbh_rem_model(const double* c, const D& eta, const D& chi1, const D& lam) {
+  const D p1 = ((c[0] * chi1 + c[1]) + (c[2] * chi1 + c[3]) * eta) * eta;
+  const D p2 = ((c[4] * chi1 + c[5]) + (c[6] * chi1 + c[7]) * eta) * eta;
+  const D p3 = ((c[8] * chi1 + c[9]) + (c[10] * chi1 + c[11]) * eta) * eta;
+  const D den = 1.0 + lam * p3 * p3;
+  const D m = (1.0 + lam * p1 + lam * lam * p2) / (den * den);
+  if ((chi1.v < 0.0 && eta.v < 0.188) || chi1.v < -0.5 || m.v > 1.0) return D(1.0);
+  return m;
+}
+
+template <class D>
+__device__ inline void nsbh_remnant(const D& eta, const D& chi1, const D& lam, D& chif, D& mfin) {
+  const double csp[12] = {-5.44187381e-03, 7.91165608e-03, 2.33362046e-02, 2.47764497e-02, -8.56844797e-07,
+                          -2.81727682e-06, 6.61290966e-06, 4.28979016e-05, -3.04174272e-02, 2.54889050e-01,
+                          1.47549350e-01, -4.27905832e-01};
+  const double cm[12] = {-1.83417425e-03, 2.39226041e-03, 4.29407902e-03, 9.79775571e-03, 2.33868869e-07,
+                         -8.28090025e-07, -1.64315549e-06, 8.08340931e-06, -2.00726981e-02, 1.31986011e-01,
+                         6.50754064e-02, -1.42749961e-01};
+  const D rsp = nsbh_rem_model(csp, eta, chi1, lam), rm = nsbh_rem_model(cm, eta, chi1, lam);
+  const D seta = seta_of(eta);
+  const D m1 = 0.5 * (1.0 + seta), m2 = 0.5 * (1.0 - seta);
+  const D e2 = eta * eta, e3 = e2 * eta;
+  const D S1 = chi1 * m1 * m1;
+  const D Sh = S1 / (m1 * m1 + m2 * m2);
+  const D Sh2 = Sh * Sh, Sh3 = Sh2 * Sh;
+  const D lorb = (2.0 * sqrt(3.0) * eta + 5.24 * 3.8326341618708577 * e2 + 1.3 * (-9.487364155598392) * e3)
+                     / (1.0 + 2.88 * 2.5134875145648374 * eta)
+                 + ((-0.194) * 1.0009563702914628 * Sh * (4.409160174224525 * eta + 0.5118334706832706 * e2
+                                                         + (64. - 16. * 4.409160174224525 - 4. * 0.5118334706832706) * e3)
+                    + 0.0851 * 0.7877509372255369 * Sh2 * (8.77367320110712 * eta + (-32.060648277652994) * e2
+                                                           + (64. - 16. * 8.77367320110712 - 4. * (-32.060648277652994)) * e3)
+                    + 0.00954 * 0.6540138407185817 * Sh3 * (22.830033250479833 * eta + (-153.83722669033995) * e2
+                                                            + (64. - 16. * 22.830033250479833 - 4. * (-153.83722669033995)) * e3))
+                       / (1.0 + (-0.579) * 0.8396665722805308 * Sh
+                                    * (1.8804718791591157 + (-4.770246856212403) * eta
+                                       + (64. - 64. * 1.8804718791591157 - 16. * (-4.770246856212403)) * e3))
+                 + 0.3223660562764661 * seta * e2 * (1.0 + 9.332575956437443 * eta) * chi1
+                 + 2.3170397514509933 * Sh * seta * e3 * (1.0 + (-3.2624649875884852) * eta) * chi1
+                 + (-0.059808322561702126) * e3 * chi1 * chi1;
+  chif = (lorb + S1) * rsp;
+  const D erad = ((1.0 - 2.0 / 3.0 * sqrt(2.0)) * eta + 0.5609904135313374 * e2 + (-0.84667563764404) * e3
+                  + 3.145145224278187 * e2 * e2)
+                     * (1.0 + 0.346 * (-0.2091189048177395) * Sh
+                                  * (1.8083565298668276 + 15.738082204419655 * eta
+                                     + (16. - 16. * 1.8083565298668276 - 4. * 15.738082204419655) * e2)
+                        + 0.211 * (-0.19709136361080587) * Sh2 * (4.271313308472851 + (16. - 16. * 4.271313308472851) * e2)
+                        + 0.128 * (-0.1588185739358418) * Sh3
+                              * (31.08987570280556 + (-243.6299258830685) * eta
+                                 + (16. - 16. * 31.08987570280556 - 4. * (-243.6299258830685)) * e2))
+                     / (1.0 + (-0.212) * 2.9852925538232014 * Sh
+                                  * (1.5673498395263061 + (-0.5808669012986468) * eta
+                                     + (16. - 16. * 1.5673498395263061 - 4. * (-0.5808669012986468)) * e2))
+                 + (-0.09803730445895877) * seta * e2 * (1.0 + (-3.2283713377939134) * eta) * chi1
+                 + (-0.01978238971523653) * Sh * seta * eta * (1.0 + (-4.91667749015812) * eta) * chi1
+                 + 0.01118530335431078 * e3 * chi1 * chi1;
+  mfin = (1.0 - erad) * rm;
+}
+
+// NS spin-induced quadrupole moment, arXiv:1303.1528 eq. 54 (gwfast/waveforms.py:2832)
+template <class D>
+__device__ inline D nsbh_quad_mon(const D& lam) {
+  if (lam.v < 1e-5) return D(1.0);
+  const D l = dlog(lam);
+  return dexp(0.194 + l * (0.0936 + l * (0.0474 + l * (-0.00421 + l * 0.000123))));
+}
+
+template <class C> struct NSBHEvT {
+  PhdCoreT<C> k;   // phase: IMRPhenomD with the NSBH ringdown
+  C tidP;          // -kappa2T c_Newt / (m1 m2)
+  C xd[7];         // xdotaN, xdota2, xdota3, xdota4, xdota5, xdota6, xdota7 (gwfast/waveforms.py:3047-3054)
+  C an[8];         // AN, A2, A3, A4, A5, A5imag, A6, A6imag (:3056-3065)
+  C aPM;           // gamma_correction g1
+  C aRD;           // epsilon_tide del1
+  C frA, sig;      // amplitude ringdown frequency (M f) and Lorentzian width
+  C c0pn, c0pm, c0rd;   // window centres in M f (epsilon_ins f0_PN, f0_PM, f0_RD)
+  C wsc;           // 4 / (d0 + sigma_tide)
+};
+using NSBHEv = NSBHEvT<D6>;
+
+// the detector-dependent part: fRef = M G fmin and t0 at the highest grid frequency (:2991-2993)
+__device__ inline void nsbh_ref(NSBHEv& e, double fmin_hz, double fmax_grid_hz) {
+  PhdCoreT<D6>& k = e.k;
+  phenom_ref_setup(k, k.MG * fmax_grid_hz, fmin_hz, k.C1MRD, k.C2MRD);
+}
+
+__device__ inline void nsbh_setup(NSBHEv& e, const D6& Mc, const D6& eta, const D6& chi1, const D6& chi2, double dL,
+                                  double fmin_hz, double fmax_grid_hz, const double* qa, const double* qr,
+                                  const double* qd, int nq, const D6& lt, const D6& dlt, const double* xit) {
+  PhdCoreT<D6>& k = e.k;
+  D6 l1, lam;
+  lam12_of(lt, dlt, eta, l1, lam);
+  D6 chif, mfin;
+  nsbh_remnant(eta, chi1, lam, chif, mfin);
+  // phase (gwfast/waveforms.py:2874-3015): ringdown from the remnant spin, IMRPhenomD radiated energy
+  const D6 er = radiated_energy(eta, chi1, chi2);
+  D6 fr, fd;
+  qnm_lookup(qa, qr, qd, nq, chif, fr, fd);
+  fr = fr / (1.0 - er);
+  fd = fd / (1.0 - er);
+  phenom_core_setup(k, Mc, eta, chi1, chi2, fr, fd, D6(0.0), nsbh_quad_mon(lam) - 1.0);
+  nsbh_ref(e, fmin_hz, fmax_grid_hz);
+  const D6 seta = seta_of(eta);
+  const D6 m1 = 0.5 * (1.0 + seta), m2 = 0.5 * (1.0 - seta);
+  const D6 m22 = m2 * m2;
+  const D6 kap = (3.0 / 13.0) * ((1.0 + 12.0 * m1 / m2) * (m22 * m22 * m2) * lam);
+  e.tidP = (-2.4375) * kap / (m1 * m2);
+  // amplitude (gwfast/waveforms.py:3017-3226)
+  const D6 M = Mc / dpowc(eta, 0.6);
+  k.ampPref = (2.0 * sqrt(5.0 / (64.0 * kPi)) * kG2Gpc * kG3 / dL) * M * M;
+  const D6 q = 0.5 * (1.0 + seta - 2.0 * eta) / eta;
+  const D6 e2 = eta * eta;
+  const D6 ce = m1 * chi1 + m2 * chi2, cs = 2.0 * ce, cp = ce * ce;
+  const double pi2 = kPi * kPi, eg = kEulerGamma;
+  e.xd[0] = 64.0 * eta / 5.0;
+  e.xd[1] = -7.43 / 3.36 - 11.0 * eta / 4.0;
+  e.xd[2] = 4.0 * kPi - 11.3 * ce / 1.2 + 19.0 * eta * cs / 6.0;
+  e.xd[3] = 3.4103 / 1.8144 + 5.0 * cp + eta * (13.661 / 2.016 - cp / 8.0) + 5.9 * e2 / 1.8;
+  e.xd[4] = -kPi * (41.59 / 6.72 + 189.0 * eta / 8.0) - ce * (31.571 / 1.008 - 116.5 * eta / 2.4)
+            + cs * (21.863 * eta / 1.008 - 79.0 * e2 / 6.0) - 3.0 * ce * cp / 4.0 + 9.0 * eta * ce * cp / 4.0;
+  e.xd[5] = 164.47322263 / 1.39708800 - 17.12 * eg / 1.05 + 16.0 * pi2 / 3.0 - 8.56 * log(16.0) / 1.05
+            + eta * (45.1 * pi2 / 4.8 - 561.98689 / 2.17728) + 5.41 * e2 / 8.96 - 5.605 * eta * e2 / 2.592
+            - 80.0 * kPi * ce / 3.0 + eta * cs * (20.0 * kPi / 3.0 - 113.5 * ce / 3.6)
+            + cp * (64.153 / 1.008 - 45.7 * eta / 3.6) - cp * (7.87 * eta / 1.44 - 30.37 * e2 / 1.44);
+  e.xd[6] = -kPi * (4.415 / 4.032 - 358.675 * eta / 6.048 - 91.495 * e2 / 1.512)
+            - ce * (252.9407 / 2.7216 - 845.827 * eta / 6.048 + 415.51 * e2 / 8.64)
+            + cs * (158.0239 * eta / 5.4432 - 451.597 * e2 / 6.048 + 20.45 * e2 * eta / 4.32 + 107.0 * eta * cp / 6.0
+                    - 5.0 * e2 * cp / 24.0)
+            + 12.0 * kPi * cp - cp * ce * (150.5 / 2.4 + eta / 8.0) + ce * cp * (10.1 * eta / 2.4 + 3.0 * e2 / 8.0);
+  e.an[0] = 8.0 * sqrt(kPi / 5.0) * eta;
+  e.an[1] = (-107.0 + 55.0 * eta) / 42.0;
+  e.an[2] = 2.0 * kPi - 4.0 * ce / 3.0 + 2.0 * eta * cs / 3.0;
+  e.an[3] = -2.173 / 1.512 - eta * (10.69 / 2.16 - 2.0 * cp) + 2.047 * e2 / 1.512;
+  e.an[4] = -10.7 * kPi / 2.1 + eta * (3.4 * kPi / 2.1);
+  e.an[5] = -24.0 * eta;
+  e.an[6] = 270.27409 / 6.46800 - 8.56 * eg / 1.05 + 2.0 * pi2 / 3.0 + eta * (4.1 * pi2 / 9.6 - 27.8185 / 3.3264)
+            - 20.261 * e2 / 2.772 + 11.4635 * eta * e2 / 9.9792 - 4.28 * log(16.0) / 1.05;
+  e.an[7] = D6(4.28 * kPi / 1.05);
+  D6 g1 = 4.149e+00 * ce + (-4.070e+00) * cp + (-8.752e+01) * eta * ce + (-4.897e+01) * eta + 6.665e+02 * e2;
+  if (g1.v < 0.0) g1 = D6(0.0);
+  D6 del1 = (-5.472e-02) * ce + 2.094e-02 * cp + 3.554e-01 * eta * ce + 1.151e-01 * eta + 9.640e-01 * e2;
+  D6 del2 = (-1.235e+00) * ce + 3.423e-01 * cp + 6.062e+00 * eta * ce + 5.949e+00 * eta + (-1.069e+01) * e2;
+  if (del1.v < 0.0) del1 = D6(0.0);
+  if (del2.v < 1.0e-4) del2 = D6(1.0e-4);
+  // NS compactness (arXiv:1608.02582 eq. 78) and torus mass (arXiv:1509.00512 eq. 11)
+  D6 Comp;
+  if (lam.v > 1.0) {
+    const D6 ll = dlog(lam);
+    Comp = 0.360 + (-0.0355) * ll + 0.000705 * ll * ll;
+  } else {
+    Comp = 0.5 + (3.0 * 0.360 + 0.0355 - 1.5) * lam * lam + (-2.0 * 0.360 - 0.0355 + 1.0) * lam * lam * lam;
+  }
+  const D6 xi = xitide_interp(xit, Comp, q, chi1);
+  const D6 z1 = 1.0 + dcbrt(1.0 - chi1 * chi1) * (dcbrt(1.0 + chi1) + dcbrt(1.0 - chi1));
+  const D6 z2 = dsqrt(3.0 * chi1 * chi1 + z1 * z1);
+  const D6 rr = dsqrt((3.0 - z1) * (3.0 + z1 + 2.0 * z2));
+  const D6 r_isco = chi1.v > 0.0 ? 3.0 + z2 - rr : 3.0 + z2 + rr;
+  D6 Mtor = 0.296 * xi * (1.0 - 2.0 * Comp) - 0.171 * q * Comp * r_isco;
+  if (!(Mtor.v > 0.0)) Mtor = D6(0.0);
+  // 22 quasi-normal mode of the remnant (complex fit in kappa)
+  const D6 kp = dsqrt(dlog(2.0 - chif) / log(3.0));
+  const double ca[5] = {1.5578, 1.9510, 2.0997, 1.4109, 0.4106}, cb[5] = {2.9031, 5.9210, 2.7606, 5.9143, 2.7952};
+  D6 sre(0.0), sim(0.0);
+  for (int n = 4; n >= 0; --n) {
+    sre = sre * kp + ca[n] * cos(cb[n]);
+    sim = sim * kp + ca[n] * sin(cb[n]);
+  }
+  const D6 om_re = 1.0 + kp * sre, om_im = kp * sim;
+  const D6 frA = 0.5 * om_re / kPi / mfin;
+  const D6 rt = xi * (1.0 - 2.0 * Comp) / (q * Comp);
+  const D6 qf = 0.5 * om_re / om_im;
+  const D6 ftide = dabs(1.0 / (kPi * (chi1 + dsqrt(rt * rt * rt))) * (1.0 + 1.0 / q));
+  const D6 frt = (0.99 * 0.98) * frA;
+  const D6 gcorr = lam.v > 1.0 ? D6(1.25) : 1.0 + 0.5 * lam - 0.25 * lam * lam;
+  const D6 u = ftide / frt - 1.0;
+  const D6 d2p = lam.v > 1.0 ? 1.62496 * 0.25 * (1.0 + dtanh(4.0 * (u - 0.0188092) / 0.338737))
+                             : del2 - 2.0 * (del2 - 0.81248) * lam + (del2 - 0.81248) * lam * lam;
+  const D6 sig = d2p * frA / qf;
+  const bool low = ftide.v < frA.v;
+  const D6 eps_tide = low ? D6(0.0) : 0.5 * (1.0 + dtanh(4.0 * ((u * u - 0.571505 * Comp - 0.00508451 * chi1) + 0.0796251) / 0.0801192));
+  const D6 X = 1.29971 - 1.61724 * (Mtor + 0.424912 * Comp + 0.363604 * dsqrt(eta) - 0.0605591 * chi1);
+  const D6 eps_ins = low ? (X.v > 1.0 ? D6(1.0) : X) : (Mtor.v > 0.0 ? X : D6(1.0));
+  const D6 Y = 0.137722 - 0.293237 * (Mtor - 0.132754 * Comp + 0.576669 * dsqrt(eta) - 0.0603749 * chi1
+                                      - 0.0601185 * chi1 * chi1 - 0.0729134 * chi1 * chi1 * chi1);
+  const D6 W = 0.5 * (1.0 - dtanh(4.0 * ((u * u - 0.657424 * Comp - 0.0259977 * chi1) + 0.206465) / 0.226844));
+  const D6 sig_tide = low ? (Mtor.v > 0.0 ? Y : 0.5 * Y + W) : W;
+  // window centres, in M f (gwfast writes them in Hz and multiplies back by M G)
+  const D6& MG = k.MG;
+  const D6 ring_end = lam.v > 1.0 ? frt : (1.0 - 0.02 * lam + 0.01 * lam * lam) * 0.98 * frA;
+  const D6 f0pn = low ? (Mtor.v > 0.0 ? ftide : (1.0 - 1.0 / q) * frt + eps_ins * ftide / q) : ring_end;
+  const D6 f0pm = low ? (Mtor.v > 0.0 ? ftide : (1.0 - 1.0 / q) * frt + ftide / q) : ring_end;
+  e.c0pn = eps_ins * ((f0pn / MG) * MG);
+  e.c0pm = (f0pm / MG) * MG;
+  e.c0rd = low ? D6(0.0) : (ring_end / MG) * MG;
+  e.wsc = 4.0 / (0.015 + sig_tide);
+  e.aPM = gcorr * g1;
+  e.aRD = eps_tide * del1;
+  e.frA = frA;
+  e.sig = sig;
+}
+
+// amplitude and phase of IMRPhenomNSBH at physical frequency f (Hz)
+template <class S, class C>
+__device__ __forceinline__ void nsbh_point(const NSBHEvT<C>& e, typename Real<S>::T f, S& amp, S& phase) {
+  typedef typename Real<S>::T T;
+  const PhdCoreT<C>& k = e.k;
+  const S x = co<S>(k.MG) * f;
+  const T xv = val(x);
+  const S one(T(1));
+  const S px = T(kPi) * x;
+  const S v = dcbrt(px), v2 = v * v;
+  const S lv2 = T(2) * dlog(v);
+  const S px2 = px * px;
+  const S xdot = co<S>(e.xd[0]) * (v2 * v2 * v2 * v2 * v2)
+                 * (T(1) + co<S>(e.xd[1]) * v2 + co<S>(e.xd[2]) * px + co<S>(e.xd[3]) * px * v + co<S>(e.xd[4]) * v2 * px
+                    + (co<S>(e.xd[5]) + T(-856. / 105.) * lv2) * px2 + co<S>(e.xd[6]) * v * px2);
+  const S aft = dsqrt(dabs(T(kPi) / (T(1.5) * v * xdot)));
+  const S base = aft * co<S>(e.an[0]) * v2;
+  const S re = base * (T(1) + co<S>(e.an[1]) * v2 + co<S>(e.an[2]) * px + co<S>(e.an[3]) * v * px + co<S>(e.an[4]) * v2 * px
+                       + (co<S>(e.an[6]) + T(-428. / 105.) * lv2) * px2);
+  const S im = base * (co<S>(e.an[5]) * v2 * px + co<S>(e.an[7]) * px2);
+  const S aPN = dsqrt(re * re + im * im);
+  const S x56 = dexp(T(5.0 / 6.0) * dlog(x));
+  const S aPM = co<S>(e.aPM) * x56;
+  const S sg = co<S>(e.sig);
+  const S dr = x - co<S>(e.frA);
+  const S LRD = sg * sg / (dr * dr + sg * sg * T(0.25));
+  const S aRD = co<S>(e.aRD) * LRD / (x * dsqrt(dcbrt(x)));
+  const S wsc = co<S>(e.wsc);
+  const S wpn = T(0.5) * (T(1) - dtanh(wsc * (x - co<S>(e.c0pn))));
+  const S wpm = T(0.5) * (T(1) - dtanh(wsc * (x - co<S>(e.c0pm))));
+  const S wrd = T(0.5) * (T(1) + dtanh(wsc * (x - co<S>(e.c0rd))));
+  amp = xv < T(kMfCut) ? co<S>(k.ampPref) * (aPN * wpn + aPM * wpm + aRD * wrd) : S(T(0));
+  S ph = complete_phase(k, x, co<S>(k.C1MRD), co<S>(k.C2MRD), one, one);
+  if (xv < T(kMfCut)) {
+    const S x13 = v;
+    const S num = T(1) + x13 * x13 * T(-12.615214237993088) + px * T(19.0537346970349)
+                  + x13 * px * T(-21.166863146081035) + x13 * x13 * px * T(90.55082156324926) + px * px * T(-60.25357801943598);
+    const S den = T(1) + x13 * x13 * T(-15.11120782773667) + px * T(22.195327350624694) + x13 * px * T(8.064109635305156);
+    const S tidal_ph = co<S>(e.tidP) * (x13 * x13 * px) * num / den;
+    ph = ph - co<S>(k.t0) * (x - co<S>(k.fRef)) - co<S>(k.phiRef) + T(kPi) + tidal_ph;
+  }
+  phase = ph;
+}
+
 // ------------------------------------------------------------------ IMRPhenomHM (gwfast/waveforms.py:2256-2616)
 template <class C> struct HMModeT {
   C rho, tau, C1, C2, frlm;

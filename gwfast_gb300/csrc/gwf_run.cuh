@@ -232,14 +232,10 @@ cudaError_t wave_one(const LaunchArgs& a, const WaveOut& o) {
 }
 
 cudaError_t wave_dispatch(const LaunchArgs& a, const WaveOut& o) {
-  if constexpr (M >= 3) {
-    return cudaErrorNotSupported;   // 11-parameter outputs only
-  } else {
-    if (o.cnt <= 0) return cudaSuccess;
-    const bool tri = a.det.shape == 1;
-    if (a.det.earth) return tri ? wave_one<true, 2>(a, o) : wave_one<true, 1>(a, o);
-    return tri ? wave_one<false, 2>(a, o) : wave_one<false, 1>(a, o);
-  }
+  if (o.cnt <= 0) return cudaSuccess;
+  const bool tri = a.det.shape == 1;
+  if (a.det.earth) return tri ? wave_one<true, 2>(a, o) : wave_one<true, 1>(a, o);
+  return tri ? wave_one<false, 2>(a, o) : wave_one<false, 1>(a, o);
 }
 
 }  // namespace

@@ -9,5 +9,6 @@ size_t setup_stride_m5() { return rec_stride<5>(); }
 size_t core_bytes_m5() { return wave_bytes<5>(); }
 cudaError_t launch_fisher_m5(const LaunchArgs& a) { return fisher_dispatch(a); }
 cudaError_t launch_snr_m5(const LaunchArgs& a) { return snr_dispatch(a); }
+cudaError_t launch_wave_m5(const LaunchArgs& a, const WaveOut& o) { return wave_dispatch(a, o); }
 
 }  // namespace gwf

@@ -11,9 +11,10 @@ namespace gwf {
 enum { WAVE_DERIVS = 0, WAVE_STORE = 1, WAVE_OVERLAP = 2 };
 
 // One launch of wave_out_kernel over events [n0, n0 + cnt) of the batch.
-//  WAVE_DERIVS:  out[((arm * NP + p) * out_n + n - out_base) * R_out + k] = d h_arm / d theta_p at
+//  WAVE_DERIVS:  out[((arm * P + p) * out_n + n - out_base) * R_out + k] = d h_arm / d theta_p at
 //                point k (tcoal in seconds; triangle: 3 arms, the third minus the sum of the first
-//                two), the layout of gwfast's return_derivatives per arm (signal.py:938-939).
+//                two; P = the model's parameter count), the layout of gwfast's return_derivatives per arm
+//                (signal.py:938-939).
 //  WAVE_STORE:   out[(arm * out_n + n - out_base) * R_out + k] = h_arm sqrt(4 w_k / S_k), computed
 //                arms only (1 or 2).
 //  WAVE_OVERLAP: reads the WAVE_STORE output of the first waveform at the same place and writes,
@@ -21,6 +22,7 @@ enum { WAVE_DERIVS = 0, WAVE_STORE = 1, WAVE_OVERLAP = 2 };
 //                n2[n] = sum |u2|^2: the trapezoid integrals 4 int Re(h1 conj h2) / S df etc.
 struct WaveOut {
   int mode;
+  double dphi;   // added to the phase constant (TaylorF2 with phiref_vlso: -pi)
   long long n0, cnt;
   cd* out;
   long long out_n, out_base;
@@ -62,6 +64,8 @@ __global__ void __launch_bounds__(kThreads) wave_out_kernel(EvBatch ev, DetDev d
     __syncthreads();
   }
   constexpr int NA = NARM == 2 ? 3 : 1;
+  constexpr int NPM = np_of<MODEL>();
+  constexpr int NI = ndir_of<MODEL>();
   const double phic = ev.p[8 * ev.ld + n];
   const int R = g.ok ? g.R : 0;
   const long long row = n - o.out_base;
@@ -70,7 +74,7 @@ __global__ void __launch_bounds__(kThreads) wave_out_kernel(EvBatch ev, DetDev d
     if (k >= R) {   // no valid grid for this event: zeros
       if (o.mode == WAVE_DERIVS)
         for (int a = 0; a < NA; ++a)
-          for (int p = 0; p < NP; ++p) o.out[((long long)(a * NP + p) * o.out_n + row) * o.R_out + k] = {0.0, 0.0};
+          for (int p = 0; p < NPM; ++p) o.out[((long long)(a * NPM + p) * o.out_n + row) * o.R_out + k] = {0.0, 0.0};
       else if (o.mode == WAVE_STORE)
         for (int a = 0; a < NARM; ++a) o.out[((long long)a * o.out_n + row) * o.R_out + k] = {0.0, 0.0};
       continue;
@@ -78,34 +82,39 @@ __global__ void __launch_bounds__(kThreads) wave_out_kernel(EvBatch ev, DetDev d
     double f, lnf, w;
     grid_point(g, ev.spacing, k, f, lnf, w);
     if (o.mode == WAVE_DERIVS) {
-      cd P, C, dP[4], dC[4], dPi, dCi;
-      DualOf<MODEL> tau(0.0);   // (11-parameter models only: four tangent directions)
+      cd P, C, dP[NI], dC[NI], dPi, dCi;
+      DualOf<MODEL> tau(0.0);
       double phi0;
       wave_point_dual<MODEL, EARTH>(E, pj, f, lnf, P, C, dP, dC, dPi, dCi, tau, phi0);
-      double dtn[4] = {0.0, 0.0, 0.0, 0.0};
+      double dtn[NI];
+#pragma unroll
+      for (int q = 0; q < NI; ++q) dtn[q] = 0.0;
+      double dphl, dphd, dphe;
+      analytic_tangents<MODEL>(E, lnf, dphl, dphd, dphe);
       TimeState ts;
       if (EARTH) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) dtn[q] = -tau.d[q] / kDay;
+        for (int q = 0; q < NI; ++q) dtn[q] = -tau.d[q] / kDay;
         time_state(pj, pj.tc - tau.v / kDay, ts);
       } else {
         ts = tsc;
       }
-      const cd ph = common_phase(f, pj.tc, ts.D, phic + phi0);
-      cd D[NARM][NP];
+      const cd ph = common_phase(f, pj.tc, ts.D, phic + phi0 + o.dphi);
+      cd D[NARM][NPM];
 #pragma unroll
       for (int a = 0; a < NARM; ++a) {
         ArmPat ap;
         if (EARTH) arm_pattern(pj, det.sin_zeta, ts.x, a, ap);
         else ap = apc[a];
-        arm_derivs(pj, ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D[a]);
+        arm_derivs<NI>(pj, ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D[a]);
+        analytic_columns<MODEL>(cadd(cscale(P, ap.Fp), cscale(cmuli(C), ap.Fc)), dphl, dphd, dphe, D[a]);
       }
 #pragma unroll
       for (int a = 0; a < NA; ++a)
 #pragma unroll
-        for (int p = 0; p < NP; ++p) {
+        for (int p = 0; p < NPM; ++p) {
           const cd v = a < NARM ? D[a][p] : cscale(cadd(D[0][p], D[NARM - 1][p]), -1.0);
-          o.out[((long long)(a * NP + p) * o.out_n + row) * o.R_out + k] = cmul(v, ph);
+          o.out[((long long)(a * NPM + p) * o.out_n + row) * o.R_out + k] = cmul(v, ph);
         }
     } else {
       cd P, C;
@@ -115,7 +124,7 @@ __global__ void __launch_bounds__(kThreads) wave_out_kernel(EvBatch ev, DetDev d
       if (EARTH) time_state(pj, pj.tc - tau / kDay, ts);
       else ts = tsc;
       const double sw = sqrt(4.0 * w / psd_at(det, f, lnf));
-      const cd ph = cscale(common_phase(f, pj.tc, ts.D, phic + phi0), sw);
+      const cd ph = cscale(common_phase(f, pj.tc, ts.D, phic + phi0 + o.dphi), sw);
       cd u[NARM];
 #pragma unroll
       for (int a = 0; a < NARM; ++a) {

@@ -112,12 +112,13 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
 
 
 def strain_derivs_batch(signal, evParams, res=1000, spacing='geom'):
-    """d h / d theta on each event's grid for one detector: complex128 (arms, 11, N, res), tcoal
+    """d h / d theta on each event's grid for one detector: complex128 (arms, P, N, res), tcoal
     row in 1/s (the per-arm arrays of gwfast's return_derivatives, gwfast/signal.py:938-939)."""
-    p = _prep(evParams)
+    wf = signal.wf_model
+    p = _prep(evParams, wf)
     N = p.shape[1]
     arms = 1 if signal.detector_shape == 'L' else 3
-    out = np.empty((arms, 11, N, int(res)), dtype=np.complex128)
+    out = np.empty((arms, wf.nParams, N, int(res)), dtype=np.complex128)
     _lib.context(signal.device).strain_derivs(signal.det_id, signal.wf_model.gpu_desc(), p, res,
                                               spacing=0 if spacing == 'geom' else 1, out=out)
     return out
@@ -126,9 +127,9 @@ def strain_derivs_batch(signal, evParams, res=1000, spacing='geom'):
 def overlap_batch(signals, WF1, WF2, evParams1, evParams2, res=1000):
     """Per detector (n_det, N) arrays (4 trapz(Re(h1 conj h2)/S), 4 trapz(|h1|^2/S), 4 trapz(|h2|^2/S)),
     summed over each detector's arms (gwfast/signal.py:1759-1921)."""
-    p1 = _prep(evParams1)
-    p2 = _prep(evParams2)
-    if p1.shape != p2.shape:
+    p1 = _prep(evParams1, WF1)
+    p2 = _prep(evParams2, WF2)
+    if p1.shape[1] != p2.shape[1]:
         raise ValueError('the two parameter sets must hold the same number of events')
     N = p1.shape[1]
     ov, n1, n2 = (np.empty((len(signals), N)) for _ in range(3))

@@ -6,7 +6,7 @@ the ``is_*`` flags, ``objType``, ``fcut``) plus the descriptor the C ABI needs.
 Supported: TaylorF2_RestrictedPN (with its options: the 3.5PN spin-spin terms, the tidal terms (13
 parameters), orbital eccentricity (+ ecc: 12 or 14 parameters), the phase referenced at the last
 stable orbit, the Kerr-ISCO cut, the spin-induced quadrupole of tidal bodies), IMRPhenomD,
-IMRPhenomHM and IMRPhenomD_NRTidalv2 (13 parameters), aligned spins.
+IMRPhenomHM, IMRPhenomD_NRTidalv2 and IMRPhenomNSBH (13 parameters), aligned spins.
 """
 import numpy as np
 
@@ -23,7 +23,7 @@ class WaveFormModel:
     def __init__(self, objType, fcutPar, is_newtonian=False, is_tidal=False, is_HigherModes=False, is_chi1chi2=True,
                  is_Precessing=False, is_LAL=False, is_prec_ang=False, is_eccentric=False, is_holomorphic=False,
                  apply_fcut=True):
-        tidal_ok = type(self).__name__ in ('TaylorF2_RestrictedPN', 'IMRPhenomD_NRTidalv2')
+        tidal_ok = type(self).__name__ in ('TaylorF2_RestrictedPN', 'IMRPhenomD_NRTidalv2', 'IMRPhenomNSBH')
         ecc_ok = type(self).__name__ == 'TaylorF2_RestrictedPN'
         for flag, name in ((is_newtonian, 'is_newtonian'), (is_tidal and not tidal_ok, 'is_tidal'),
                            (is_Precessing, 'is_Precessing'), (is_LAL, 'is_LAL'),
@@ -197,3 +197,21 @@ class IMRPhenomD_NRTidalv2(WaveFormModel):
         f_merger = 0.3586 / np.sqrt(q) * (num / den) / (2. * np.pi)
         return 1.2 * f_merger / (M * glob.GMsun_over_c3)
 
+
+class IMRPhenomNSBH(WaveFormModel):
+    """gwfast/waveforms.py:2752-3374: object 1 is the black hole, object 2 the neutron star (only Lambda2
+    enters); IMRPhenomD phase with the NSBH remnant and the NRTidalv2 tidal phase, IMRPhenomC-based
+    amplitude with the merger-type windows of arXiv:1509.00512 (13 parameters, FP64 path only). Its
+    xi_tide table is built on the GPU, as gwfast tabulates it when the h5 file is absent."""
+
+    def __init__(self, fRef=None, verbose=True, **kwargs):
+        if fRef is not None:
+            raise NotImplementedError('a fixed fRef is not implemented on the GPU path')
+        self.PHI_fJoin_INS = 0.018
+        self.verbose = verbose
+        self.fRef = fRef
+        super().__init__('NSBH', 0.2, is_tidal=True, **kwargs)
+
+    def fcut(self, **kwargs):
+        """gwfast/waveforms.py:3274-3284."""
+        return self.fcutPar / (np.asarray(kwargs['Mc']) * glob.GMsun_over_c3 / (np.asarray(kwargs['eta']) ** (3. / 5.)))

@@ -56,7 +56,11 @@ enum {
  * GWF_WF_TAYLORF2_ECC, GWF_WF_TAYLORF2_TIDAL_ECC: TaylorF2_RestrictedPN(is_eccentric=True), without or with
  * is_tidal (gwfast/waveforms.py:814-845): FP64, 12 and 14 parameters. */
 enum { GWF_WF_TAYLORF2 = 0, GWF_WF_PHENOMD = 1, GWF_WF_PHENOMHM = 2, GWF_WF_TAYLORF2_TIDAL = 3,
-       GWF_WF_PHENOMD_NRTIDALV2 = 4, GWF_WF_TAYLORF2_ECC = 5, GWF_WF_TAYLORF2_TIDAL_ECC = 6 };
+       GWF_WF_PHENOMD_NRTIDALV2 = 4, GWF_WF_TAYLORF2_ECC = 5, GWF_WF_TAYLORF2_TIDAL_ECC = 6, GWF_WF_PHENOMNSBH = 7 };
+/* GWF_WF_PHENOMNSBH: IMRPhenomNSBH, gwfast/waveforms.py:2752-3374 (object 1 the black hole, object 2 the
+ * neutron star; LambdaTilde, deltaLambda rows as for the tidal models, 13 parameters, FP64; needs the QNM
+ * table). Its xi_tide table (gwfast ships it as WFfiles/xiTide_Table_200.h5 or tabulates it,
+ * :3286-3373) is built on the device on first use: 200^3 nodes, 64 MiB per context. */
 /* gwf_wf_desc.flags, TaylorF2 models only (gwfast/waveforms.py:726-741):
  * GWF_TF2_PHIREF_VLSO    phiref_vlso=True (2.5PN constant referenced at the last stable orbit, :796-798)
  * GWF_TF2_KERR_ISCO      which_ISCO='Kerr' (cut at twice the Kerr-remnant ISCO frequency, :921-951)
@@ -98,6 +102,11 @@ int gwf_ctx_create(int device, gwf_ctx** out);
 int gwf_ctx_destroy(gwf_ctx* ctx);
 const char* gwf_last_error(void);
 int gwf_version(void);
+
+/* IMRPhenomNSBH's xi_tide (arXiv:1509.00512 eq. 8) interpolated on its table at n points (NS compactness,
+ * mass ratio m1/m2 >= 1, BH spin); host arrays. Replaces IMRPhenomNSBH.xiTide_interp
+ * (gwfast/waveforms.py:3373, gwfast/gwfastUtils.py:1024-1200); builds the table if needed. */
+int gwf_xitide(gwf_ctx* ctx, const double* comp, const double* q, const double* chi_bh, int64_t n, double* out);
 
 /* IMRPhenomD quasi-normal-mode table (spin, fring, fdamp), gwfast/waveforms.py:988-990. */
 int gwf_set_qnm_table(gwf_ctx* ctx, const double* spin, const double* fring, const double* fdamp, int64_t n);

@@ -666,6 +666,316 @@ def nrt_ampl(f, Mc, eta, chi1, chi2, dL, lt, dlt, taper_last=None):
     return (base + over * 2. * math.sqrt(PI / 5.) * amp_t) * taper
 
 
+# ---------------------------------------------------------------- IMRPhenomNSBH
+# xi_tide of arXiv:1509.00512 eq. 8 on gwfast's regular grid (gwfast/waveforms.py:3286-3343): compactness
+# in [0.1, 0.5], mass ratio in [1, 100], BH spin in [-1, 1], 200 points each (numpy linspace)
+XI_GRID = (np.linspace(0.1, 0.5, 200), np.linspace(1., 100., 200), np.linspace(-1., 1., 200))
+_XI_CACHE = {}
+
+
+def xitide_node(i, j, k):
+    """The table value at grid node (i, j, k): the largest square of the real positive roots of the
+    degree-10 polynomial in sqrt(xi) (:3310-3330), found by numpy's companion-matrix roots as gwfast does."""
+    key = (i, j, k)
+    if key not in _XI_CACHE:
+        C, q, chi = XI_GRID[0][i], XI_GRID[1][j], XI_GRID[2][k]
+        mu = q * C
+        coeffs = np.array([1., 0., -3. * mu, 2. * chi * (mu ** (3. / 2.)), 0., 0., -3. * q, 0., 6. * q * mu, 0.,
+                           -3. * q * mu * chi * mu * chi])
+        r = np.roots(coeffs)
+        rp = np.real(r[(abs(np.imag(r)) < 1e-5) & (np.real(r) > 0.)])
+        _XI_CACHE[key] = max(rp * rp)
+    return _XI_CACHE[key]
+
+
+_XI_DENSE = None
+_XI_GRID_T = tuple(torch.as_tensor(g, dtype=DT) for g in XI_GRID)
+
+
+def _xi_dense():
+    """The table as a dense tensor, filled node by node as events need them (NaN elsewhere)."""
+    global _XI_DENSE
+    if _XI_DENSE is None:
+        _XI_DENSE = torch.full((200, 200, 200), float('nan'), dtype=DT)
+    return _XI_DENSE
+
+
+def _xi_cells(xs):
+    """Cell indices and the out-of-bounds flag of gwfast's RegularGridInterpolator_JAX
+    (gwfast/gwfastUtils.py:1182-1200), from plain (detached) coordinates."""
+    idx = []
+    oob = torch.zeros(xs[0].shape[0], dtype=DT)
+    for x, g in zip(xs, _XI_GRID_T):
+        i = torch.searchsorted(g, x.contiguous()) - 1
+        idx.append(torch.clamp(i, 0, g.numel() - 2))
+        oob = ((oob + x) < g[0]).to(DT)
+        oob = ((oob + x) > g[-1]).to(DT)
+    return idx, oob > 0
+
+
+def xitide_prepare(C, q, chi):
+    """Fill the table nodes around the given points (numpy roots, as gwfast tabulates them)."""
+    xs = tuple(torch.as_tensor(np.asarray(a, dtype=np.float64).reshape(-1)) for a in (C, q, chi))
+    idx, _ = _xi_cells(xs)
+    T = _xi_dense()
+    for a, b, c in zip(*(i.numpy() for i in idx)):
+        for e0 in (0, 1):
+            for e1 in (0, 1):
+                for e2 in (0, 1):
+                    if torch.isnan(T[a + e0, b + e1, c + e2]):
+                        T[a + e0, b + e1, c + e2] = xitide_node(a + e0, b + e1, c + e2)
+
+
+def xitide_interp(C, q, chi):
+    """Trilinear interpolation on the xi_tide grid as gwfast's RegularGridInterpolator_JAX
+    (gwfast/gwfastUtils.py:1024-1200): the cell from searchsorted (clamped to the grid), linear
+    extrapolation outside it, the edge sum in itertools.product order, and the out-of-bounds test as
+    that code writes it (which in effect only flags BH spins above 1). Written in torch operations so
+    that it runs inside torch.func.jvp; the nodes are filled beforehand (xitide_prepare, which runs
+    here directly when the inputs are plain tensors)."""
+    xs = (C.reshape(-1), q.reshape(-1), chi.reshape(-1))
+    try:
+        xitide_prepare(*(x.detach().numpy() for x in xs))
+    except RuntimeError:   # inside a functorch transform: Model.prepare filled the nodes
+        pass
+    idx, oob = _xi_cells(tuple(x.detach() for x in xs))
+    nd = [(x - g[i]) / (g[i + 1] - g[i]) for x, g, i in zip(xs, _XI_GRID_T, idx)]
+    T = _xi_dense()
+    out = torch.zeros_like(xs[0])
+    for e0 in (0, 1):
+        for e1 in (0, 1):
+            for e2 in (0, 1):
+                vals = T[idx[0] + e0, idx[1] + e1, idx[2] + e2]
+                w = ((1. - nd[0]) if e0 == 0 else nd[0]) * ((1. - nd[1]) if e1 == 0 else nd[1]) \
+                    * ((1. - nd[2]) if e2 == 0 else nd[2])
+                out = out + vals * w
+    out = torch.where(oob, torch.full_like(out, float('nan')), out)
+    return out.reshape(C.shape)
+
+
+def nsbh_xi_inputs(eta, chi1, lt, dlt):
+    """(compactness, m1/m2, BH spin) at which IMRPhenomNSBH reads xi_tide."""
+    lam = _nsbh_lambda(eta, lt, dlt)
+    seta = _seta(eta)
+    q = 0.5 * (1.0 + seta - 2.0 * eta) / eta
+    ll = torch.log(torch.clamp(lam, min=1e-300))
+    Comp = torch.where(lam > 1., 0.360 - 0.0355 * ll + 0.000705 * ll * ll,
+                       0.5 + (3. * 0.360 + 0.0355 - 1.5) * lam * lam + (-2. * 0.360 - 0.0355 + 1.) * lam ** 3)
+    return Comp, q, chi1
+
+
+def _nsbh_common(eta, chi1, lam):
+    """Remnant fits shared by the phase and the amplitude (gwfast/waveforms.py:2854-2874, :3124-3151):
+    remnant spin chif (arXiv:1903.11622, arXiv:1611.00332 eq. 16) and the spin-weighted BH spin."""
+    seta = _seta(eta)
+    m1, m2 = 0.5 * (1. + seta), 0.5 * (1. - seta)
+    eta2 = eta * eta
+    chi12 = chi1 * chi1
+
+    def rem_model(c):
+        p1 = ((c[0] * chi1 + c[1]) + (c[2] * chi1 + c[3]) * eta) * eta
+        p2 = ((c[4] * chi1 + c[5]) + (c[6] * chi1 + c[7]) * eta) * eta
+        p3 = ((c[8] * chi1 + c[9]) + (c[10] * chi1 + c[11]) * eta) * eta
+        m = (1. + lam * p1 + lam * lam * p2) / ((1. + lam * p3 * p3) * (1. + lam * p3 * p3))
+        one = torch.ones_like(m)
+        m = torch.where((chi1 < 0.) & (eta < 0.188), one, m)
+        m = torch.where(chi1 < -0.5, one, m)
+        return torch.where(m > 1., one, m)
+
+    rem_sp = rem_model((-5.44187381e-03, 7.91165608e-03, 2.33362046e-02, 2.47764497e-02, -8.56844797e-07,
+                        -2.81727682e-06, 6.61290966e-06, 4.28979016e-05, -3.04174272e-02, 2.54889050e-01,
+                        1.47549350e-01, -4.27905832e-01))
+    rem_m = rem_model((-1.83417425e-03, 2.39226041e-03, 4.29407902e-03, 9.79775571e-03, 2.33868869e-07,
+                       -8.28090025e-07, -1.64315549e-06, 8.08340931e-06, -2.00726981e-02, 1.31986011e-01,
+                       6.50754064e-02, -1.42749961e-01))
+    S1 = chi1 * m1 * m1
+    Sh = S1 / (m1 * m1 + m2 * m2)
+    lorb = ((2. * math.sqrt(3.) * eta + 5.24 * 3.8326341618708577 * eta2 + 1.3 * (-9.487364155598392) * eta * eta2)
+            / (1. + 2.88 * 2.5134875145648374 * eta)
+            + ((-0.194) * 1.0009563702914628 * Sh * (4.409160174224525 * eta + 0.5118334706832706 * eta2
+                                                    + (64. - 16. * 4.409160174224525 - 4. * 0.5118334706832706) * eta2 * eta)
+               + 0.0851 * 0.7877509372255369 * Sh * Sh * (8.77367320110712 * eta + (-32.060648277652994) * eta2
+                                                          + (64. - 16. * 8.77367320110712 - 4. * (-32.060648277652994)) * eta2 * eta)
+               + 0.00954 * 0.6540138407185817 * Sh * Sh * Sh * (22.830033250479833 * eta + (-153.83722669033995) * eta2
+                                                                + (64. - 16. * 22.830033250479833 - 4. * (-153.83722669033995)) * eta2 * eta))
+            / (1. + (-0.579) * 0.8396665722805308 * Sh * (1.8804718791591157 + (-4.770246856212403) * eta + 0. * eta2
+                                                        + (64. - 64. * 1.8804718791591157 - 16. * (-4.770246856212403) - 4. * 0.) * eta2 * eta))
+            + 0.3223660562764661 * seta * eta2 * (1. + 9.332575956437443 * eta) * chi1
+            + 2.3170397514509933 * Sh * seta * eta2 * eta * (1. + (-3.2624649875884852) * eta) * chi1
+            + (-0.059808322561702126) * eta2 * eta * chi12)
+    chif = (lorb + S1) * rem_sp
+    erad = ((((1. - 2.0 / 3.0 * math.sqrt(2.)) * eta + 0.5609904135313374 * eta2 + (-0.84667563764404) * eta2 * eta
+              + 3.145145224278187 * eta2 * eta2)
+             * (1. + 0.346 * (-0.2091189048177395) * Sh * (1.8083565298668276 + 15.738082204419655 * eta
+                                                          + (16. - 16. * 1.8083565298668276 - 4. * 15.738082204419655) * eta2)
+                + 0.211 * (-0.19709136361080587) * Sh * Sh * (4.271313308472851 + 0. * eta + (16. - 16. * 4.271313308472851 - 4. * 0.) * eta2)
+                + 0.128 * (-0.1588185739358418) * Sh * Sh * Sh * (31.08987570280556 + (-243.6299258830685) * eta
+                                                                  + (16. - 16. * 31.08987570280556 - 4. * (-243.6299258830685)) * eta2)))
+            / (1. + (-0.212) * 2.9852925538232014 * Sh * (1.5673498395263061 + (-0.5808669012986468) * eta
+                                                        + (16. - 16. * 1.5673498395263061 - 4. * (-0.5808669012986468)) * eta2))
+            + (-0.09803730445895877) * seta * eta2 * (1. + (-3.2283713377939134) * eta) * chi1
+            + (-0.01978238971523653) * Sh * seta * eta * (1. + (-4.91667749015812) * eta) * chi1
+            + 0.01118530335431078 * eta2 * eta * chi12)
+    final_mass = (1. - erad) * rem_m
+    return m1, m2, chif, final_mass
+
+
+def nsbh_quad_mon(lam):
+    """NS spin-induced quadrupole moment of IMRPhenomNSBH (arXiv:1303.1528 eq. 54; gwfast/waveforms.py:2832)."""
+    ll = torch.log(torch.clamp(lam, min=1e-5))
+    return torch.where(lam < 1e-5, torch.ones_like(lam),
+                       torch.exp(0.194 + 0.0936 * ll + 0.0474 * ll ** 2 - 0.00421 * ll ** 3 + 0.000123 * ll ** 4))
+
+
+def _nsbh_lambda(eta, lt, dlt):
+    # the BH deformability recovered from (LambdaTilde, deltaLambda) is discarded (:2825-2828)
+    _, l2 = lam12_from_lamt_dellam(lt, dlt, eta)
+    return l2
+
+
+def _mf_last(Mf, cut_last):
+    """M f with its last column moved to just below (cut_last False) or to (True) the M f = 0.2 cut,
+    keeping its tangent: the grid ends at M f = 0.2 up to rounding, which decides the side."""
+    if cut_last is None:
+        return Mf
+    c = torch.as_tensor(cut_last).reshape(-1, 1).expand(Mf.shape[0], 1)
+    last = Mf[..., -1:]
+    tgt = torch.where(c, torch.full_like(last, MF_CUT), torch.full_like(last, np.nextafter(MF_CUT, 0.)))
+    return torch.cat([Mf[..., :-1], last + (tgt - last.detach())], dim=-1)
+
+
+def nsbh_phase(f, Mc, eta, chi1, chi2, lt, dlt, cut_last=None):
+    """IMRPhenomNSBH.Phi (gwfast/waveforms.py:2802-3015): IMRPhenomD with the NS quadrupole moment, the
+    ringdown from the NSBH remnant spin, t0 taken at the highest grid frequency, + pi, and the NRTidalv2
+    tidal phase of the NS."""
+    lam = _nsbh_lambda(eta, lt, dlt)
+    _, m2, chif, _ = _nsbh_common(eta, chi1, lam)
+    seta = _seta(eta)
+    m1 = 0.5 * (1. + seta)
+    Erad = radiated_energy(eta, chi1, chi2)
+    qt = qnm_table()
+    fring = interp(chif, qt[:, 0].contiguous(), qt[:, 1].contiguous()) / (1.0 - Erad)
+    fdamp = interp(chif, qt[:, 0].contiguous(), qt[:, 2].contiguous()) / (1.0 - Erad)
+    k = _phenom_core(Mc, eta, chi1, chi2, fring, fdamp, 0., nsbh_quad_mon(lam) - 1.)
+    M = k['M']
+    Mf0 = M * GMSUN_OVER_C3 * f
+    fpeak = torch.amax(Mf0, dim=-1, keepdim=True)
+    Mf = _mf_last(Mf0, cut_last)
+    t0 = _mrd_phase_raw_d(fpeak, k['alp'], fring, fdamp, eta)
+    fRef = torch.amin(Mf, dim=-1, keepdim=True)
+    phis = _phase_pieces(Mf, k, k['C1MRD'], k['C2MRD'])
+    phiRef = _phase_pieces(fRef, k, k['C1MRD'], k['C2MRD'])
+    kap = (3. / 13.) * ((1. + 12. * m1 / m2) * m2 ** 5 * lam)
+    px = PI * Mf
+    num = (1. - 12.615214237993088 * px ** (2. / 3.) + 19.0537346970349 * px - 21.166863146081035 * px ** (4. / 3.)
+           + 90.55082156324926 * px ** (5. / 3.) - 60.25357801943598 * px * px)
+    den = 1. - 15.11120782773667 * px ** (2. / 3.) + 22.195327350624694 * px + 8.064109635305156 * px ** (4. / 3.)
+    tidal = -kap * 2.4375 / (m1 * m2) * px ** (5. / 3.) * num / den
+    extra = -t0 * (Mf - fRef) - phiRef + PI + tidal
+    return phis + torch.where(Mf < MF_CUT, extra, torch.zeros_like(extra))
+
+
+def nsbh_ampl(f, Mc, eta, chi1, chi2, dL, lt, dlt, cut_last=None):
+    """IMRPhenomNSBH.Ampl (gwfast/waveforms.py:3017-3226): the IMRPhenomC-based amplitude with the
+    NSBH merger-type windows (arXiv:1509.00512). ``cut_last`` (bool per event) puts the last grid
+    point on either side of the M f = 0.2 cut (see _mf_last)."""
+    lam = _nsbh_lambda(eta, lt, dlt)
+    m1, m2, chif, final_mass = _nsbh_common(eta, chi1, lam)
+    seta = _seta(eta)
+    q = 0.5 * (1.0 + seta - 2.0 * eta) / eta
+    eta2 = eta * eta
+    M = Mc / eta ** (3. / 5.)
+    MG = M * GMSUN_OVER_C3
+    Mf = _mf_last(MG * f, cut_last)
+    chieff = m1 * chi1 + m2 * chi2
+    chisum = 2. * chieff
+    chiprod = chieff * chieff
+    eg = EULER_GAMMA
+    xdotaN = 64. * eta / 5.
+    xdota2 = -7.43 / 3.36 - 11. * eta / 4.
+    xdota3 = 4. * PI - 11.3 * chieff / 1.2 + 19. * eta * chisum / 6.
+    xdota4 = 3.4103 / 1.8144 + 5 * chiprod + eta * (13.661 / 2.016 - chiprod / 8.) + 5.9 * eta2 / 1.8
+    xdota5 = (-PI * (41.59 / 6.72 + 189. * eta / 8.) - chieff * (31.571 / 1.008 - 116.5 * eta / 2.4)
+              + chisum * (21.863 * eta / 1.008 - 79. * eta2 / 6.) - 3 * chieff * chiprod / 4. + 9. * eta * chieff * chiprod / 4.)
+    xdota6 = (164.47322263 / 1.39708800 - 17.12 * eg / 1.05 + 16. * PI * PI / 3 - 8.56 * math.log(16.) / 1.05
+              + eta * (45.1 * PI * PI / 4.8 - 561.98689 / 2.17728) + 5.41 * eta2 / 8.96 - 5.605 * eta * eta2 / 2.592
+              - 80. * PI * chieff / 3. + eta * chisum * (20. * PI / 3. - 113.5 * chieff / 3.6)
+              + chiprod * (64.153 / 1.008 - 45.7 * eta / 3.6) - chiprod * (7.87 * eta / 1.44 - 30.37 * eta2 / 1.44))
+    xdota6log = -856. / 105.
+    xdota7 = (-PI * (4.415 / 4.032 - 358.675 * eta / 6.048 - 91.495 * eta2 / 1.512)
+              - chieff * (252.9407 / 2.7216 - 845.827 * eta / 6.048 + 415.51 * eta2 / 8.64)
+              + chisum * (158.0239 * eta / 5.4432 - 451.597 * eta2 / 6.048 + 20.45 * eta2 * eta / 4.32
+                          + 107. * eta * chiprod / 6. - 5. * eta2 * chiprod / 24.)
+              + 12. * PI * chiprod - chiprod * chieff * (150.5 / 2.4 + eta / 8.) + chieff * chiprod * (10.1 * eta / 2.4 + 3. * eta2 / 8.))
+    AN = 8. * eta * math.sqrt(PI / 5.)
+    A2 = (-107. + 55. * eta) / 42.
+    A3 = 2. * PI - 4. * chieff / 3. + 2. * eta * chisum / 3.
+    A4 = -2.173 / 1.512 - eta * (10.69 / 2.16 - 2. * chiprod) + 2.047 * eta2 / 1.512
+    A5 = -10.7 * PI / 2.1 + eta * (3.4 * PI / 2.1)
+    A5imag = -24. * eta
+    A6 = (270.27409 / 6.46800 - 8.56 * eg / 1.05 + 2. * PI * PI / 3. + eta * (4.1 * PI * PI / 9.6 - 27.8185 / 3.3264)
+          - 20.261 * eta2 / 2.772 + 11.4635 * eta * eta2 / 9.9792 - 4.28 * math.log(16.) / 1.05)
+    A6log = -428. / 105.
+    A6imag = 4.28 * PI / 1.05
+    g1 = 4.149e+00 * chieff - 4.070e+00 * chiprod - 8.752e+01 * eta * chieff - 4.897e+01 * eta + 6.665e+02 * eta2
+    g1 = torch.where(g1 < 0., torch.zeros_like(g1), g1)
+    del1 = -5.472e-02 * chieff + 2.094e-02 * chiprod + 3.554e-01 * eta * chieff + 1.151e-01 * eta + 9.640e-01 * eta2
+    del2 = -1.235e+00 * chieff + 3.423e-01 * chiprod + 6.062e+00 * eta * chieff + 5.949e+00 * eta - 1.069e+01 * eta2
+    del1 = torch.where(del1 < 0., torch.zeros_like(del1), del1)
+    del2 = torch.where(del2 < 1.0e-4, torch.full_like(del2, 1.0e-4), del2)
+    d0 = 0.015
+    Comp, _, _ = nsbh_xi_inputs(eta, chi1, lt, dlt)
+    xi = xitide_interp(Comp, q, chi1)
+    r_isco = _r_isco(chi1)
+    mt = 0.296 * xi * (1.0 - 2.0 * Comp) - 0.171 * q * Comp * r_isco
+    Mtorus = torch.where(mt > 0., mt, torch.zeros_like(mt))
+    kap = torch.sqrt(torch.log(2. - chif) / math.log(3.))
+    cw = [(1.5578, 2.9031), (1.9510, 5.9210), (2.0997, 2.7606), (1.4109, 5.9143), (0.4106, 2.7952)]
+    om_re = 1.0 + kap * sum(a * math.cos(b) * kap ** n for n, (a, b) in enumerate(cw))
+    om_im = kap * sum(a * math.sin(b) * kap ** n for n, (a, b) in enumerate(cw))
+    fring = 0.5 * om_re / PI / final_mass
+    rtide = xi * (1.0 - 2.0 * Comp) / (q * Comp)
+    qfac = 0.5 * om_re / om_im
+    ftide = torch.abs(1.0 / (PI * (chi1 + torch.sqrt(rtide * rtide * rtide))) * (1.0 + 1.0 / q))
+    frt = 0.99 * 0.98 * fring
+    gcorr = torch.where(lam > 1.0, torch.full_like(lam, 1.25), 1.0 + 0.5 * lam - 0.25 * lam * lam)
+    d2p = torch.where(lam > 1.0, 1.62496 * 0.25 * (1. + torch.tanh(4.0 * ((ftide / frt - 1.) - 0.0188092) / 0.338737)),
+                      del2 - 2. * (del2 - 0.81248) * lam + (del2 - 0.81248) * lam * lam)
+    sigma = d2p * fring / qfac
+    low = ftide < fring
+    eps_tide = torch.where(low, torch.zeros_like(ftide),
+                           2. * 0.25 * (1 + torch.tanh(4.0 * (((ftide / frt - 1.) * (ftide / frt - 1.) - 0.571505 * Comp
+                                                                - 0.00508451 * chi1) + 0.0796251) / 0.0801192)))
+    X = 1.29971 - 1.61724 * (Mtorus + 0.424912 * Comp + 0.363604 * torch.sqrt(eta) - 0.0605591 * chi1)
+    eps_ins = torch.where(low, torch.where(X > 1., torch.ones_like(X), X), torch.where(Mtorus > 0., X, torch.ones_like(X)))
+    Y = 0.137722 - 0.293237 * (Mtorus - 0.132754 * Comp + 0.576669 * torch.sqrt(eta) - 0.0603749 * chi1
+                               - 0.0601185 * chi1 * chi1 - 0.0729134 * chi1 * chi1 * chi1)
+    W = 0.5 * (1. - torch.tanh(4.0 * (((ftide / frt - 1.) * (ftide / frt - 1.) - 0.657424 * Comp - 0.0259977 * chi1)
+                                      + 0.206465) / 0.226844))
+    sig_tide = torch.where(low, torch.where(Mtorus > 0., Y, 0.5 * Y + W), W)
+    ring_end = torch.where(lam > 1., frt, (1.0 - 0.02 * lam + 0.01 * lam * lam) * 0.98 * fring) / MG
+    f0_pn = torch.where(low, torch.where(Mtorus > 0., ftide / MG, ((1.0 - 1.0 / q) * frt + eps_ins * ftide / q) / MG), ring_end)
+    f0_pm = torch.where(low, torch.where(Mtorus > 0., ftide / MG, ((1.0 - 1.0 / q) * frt + ftide / q) / MG), ring_end)
+    f0_rd = torch.where(low, torch.zeros_like(ring_end), ring_end)
+    v = (Mf * PI) ** (1. / 3.)
+    px = Mf * PI
+    xdot = xdotaN * v ** 10 * (1. + xdota2 * v * v + xdota3 * px + xdota4 * px * v + xdota5 * v * v * px
+                               + (xdota6 + xdota6log * 2. * torch.log(v)) * px * px + xdota7 * v * px * px)
+    amp_t = torch.sqrt(torch.abs(PI / (1.5 * v * xdot)))
+    re = amp_t * AN * v * v * (1. + A2 * v * v + A3 * px + A4 * v * px + A5 * v * v * px + (A6 + A6log * 2. * torch.log(v)) * px * px)
+    im = amp_t * AN * v * v * (A5imag * v * v * px + A6imag * px * px)
+    aPN = torch.sqrt(re * re + im * im)
+    aPM = gcorr * g1 * Mf ** (5. / 6.)
+    LRD = sigma * sigma / ((Mf - fring) * (Mf - fring) + sigma * sigma * 0.25)
+    aRD = eps_tide * del1 * LRD * Mf ** (-7. / 6.)
+    w_pn = 0.5 * (1. - torch.tanh(4. * (Mf - (eps_ins * f0_pn) * MG) / (d0 + sig_tide)))
+    w_pm = 0.5 * (1. - torch.tanh(4. * (Mf - f0_pm * MG) / (d0 + sig_tide)))
+    w_rd = 0.5 * (1. + torch.tanh(4. * (Mf - f0_rd * MG) / (d0 + sig_tide)))
+    imr = aPN * w_pn + aPM * w_pm + aRD * w_rd
+    over = 2. * math.sqrt(5. / (64. * PI)) * M * GMSUN_OVER_C2_GPC * M * GMSUN_OVER_C3 / dL
+    return over * torch.where(Mf < MF_CUT, imr, torch.zeros_like(imr))
+
+
 # ---------------------------------------------------------------- IMRPhenomHM
 HM_MODES = ((2, 1), (2, 2), (3, 2), (3, 3), (4, 3), (4, 4))
 # complex ringdown-frequency fits in kappa (gwfast/waveforms.py:2661-2710): list of (modulus, phase)
@@ -860,13 +1170,14 @@ class Model:
     'PhenomD_NRTidalv2'."""
 
     def __init__(self, name, spin_ho=False, tidal=False, taper_last=None, ecc=False, fref_ecc=None, vlso=False,
-                 kerr=False, quadmon=False):
-        assert name in ('TF2', 'PhenomD', 'PhenomHM', 'PhenomD_NRTidalv2')
+                 kerr=False, quadmon=False, cut_last=None):
+        assert name in ('TF2', 'PhenomD', 'PhenomHM', 'PhenomD_NRTidalv2', 'PhenomNSBH')
         assert not (tidal or ecc or vlso or kerr or quadmon) or name == 'TF2'
         self.name = name
         self.spin_ho = spin_ho
-        self.tidal = tidal or name == 'PhenomD_NRTidalv2'
+        self.tidal = tidal or name in ('PhenomD_NRTidalv2', 'PhenomNSBH')
         self.taper_last = taper_last   # PhenomD_NRTidalv2: see nrt_ampl
+        self.cut_last = cut_last       # PhenomNSBH: see _mf_last
         # TaylorF2 options: is_eccentric (fRef_ecc), phiref_vlso, which_ISCO='Kerr', use_QuadMonTid
         self.ecc, self.fref_ecc, self.vlso, self.kerr, self.quadmon = ecc, fref_ecc, vlso, kerr, quadmon
 
@@ -874,6 +1185,12 @@ class Model:
     @property
     def params(self):
         return (PARAMS_TIDAL if self.tidal else PARAMS) + (('ecc',) if self.ecc else ())
+
+    def prepare(self, p):
+        """Work done outside torch.func transforms: IMRPhenomNSBH's xi_tide nodes around the events."""
+        if self.name == 'PhenomNSBH':
+            C, q, chi = nsbh_xi_inputs(p['eta'], p['chi1z'], p['LambdaTilde'], p['deltaLambda'])
+            xitide_prepare(C.detach().numpy(), q.detach().numpy(), chi.detach().numpy())
 
     @property
     def is_hm(self):
@@ -896,6 +1213,9 @@ class Model:
         if self.name == 'PhenomD_NRTidalv2':
             return nrt_ampl(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'], p['dL'], p['LambdaTilde'], p['deltaLambda'],
                             self.taper_last)
+        if self.name == 'PhenomNSBH':
+            return nsbh_ampl(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'], p['dL'], p['LambdaTilde'], p['deltaLambda'],
+                             self.cut_last)
         return phd_ampl(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'], p['dL'])
 
     def phase(self, f, p):
@@ -905,6 +1225,9 @@ class Model:
                              p['ecc'] if self.ecc else None, self.fref_ecc, self.vlso, self.quadmon)
         if self.name == 'PhenomD_NRTidalv2':
             return nrt_phase(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'], p['LambdaTilde'], p['deltaLambda'])
+        if self.name == 'PhenomNSBH':
+            return nsbh_phase(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'], p['LambdaTilde'], p['deltaLambda'],
+                              self.cut_last)
         return phd_phase(f, p['Mc'], p['eta'], p['chi1z'], p['chi2z'])
 
     def hphc(self, f, p):
@@ -987,6 +1310,7 @@ def strain(det, model, f, p, rot=0.):
 
 def strain_jacobian(det, model, f, p, rot=0.):
     """d h / d theta_i for the 11 parameters, (11, N, R) complex, tcoal in days (as gwfast/signal.py:1301)."""
+    model.prepare(p)
     out = []
     for name in model.params:
         def fn(x, name=name):

@@ -6,7 +6,10 @@ stand-in modules before importing it:
 
 * ``jax.numpy`` is numpy itself (float64, same function names);
 * ``jax.jacrev`` is a 5-point central finite difference (only used for the Fisher
-  golden; its rounding through the ~1e5-rad phase limits that golden, see the tests);
+  golden; its rounding through the ~1e5-rad phase limits that golden, see the tests); where the
+  unperturbed strain is exactly zero (the frequency cut of the IMR models, ``np.where(Mf < 0.2, ..., 0)``)
+  the derivative is zero, as JAX's derivative of that branch is, instead of the jump a finite
+  difference across the cut would see at the last grid point;
 * ``jax.vmap`` loops over the leading (event) axis;
 * ``jax.custom_jvp`` calls the function; for a function whose tangents gwfast gives with
   ``defjvps`` (the Planck taper of IMRPhenomD_NRTidalv2, with no tangent in its first argument),
@@ -88,10 +91,11 @@ def _install_shims():
                     _FD['i'] = 0
                     return np.asarray(fn(*a))
                 _FD['mode'], _FD['store'] = 'record', []
-                at(0.)
+                base = at(0.)
                 _FD['mode'] = 'replay'
                 d1 = (-at(2 * h) + 8 * at(h) - 8 * at(-h) + at(-2 * h)) / (12 * h)
                 _FD['mode'] = None
+                d1 = np.where(base == 0, 0., d1)
                 res.append(d1)
             return tuple(res) if isinstance(argnums, tuple) else res[0]
         return run
@@ -134,7 +138,22 @@ def _install_shims():
     sys.modules['jax.numpy'] = np
     sys.modules['jax.interpreters'] = interp
     sys.modules['jax.interpreters.xla'] = interp.xla
-    sys.modules['h5py'] = types.ModuleType('h5py')
+    h5 = types.ModuleType('h5py')
+
+    class _NoFile:   # IMRPhenomNSBH stores its xi_tide table with h5py: written nowhere here
+        def __init__(self, *a, **k):
+            self.attrs = {}
+
+        def __enter__(self):
+            return self
+
+        def __exit__(self, *a):
+            return False
+
+        def create_dataset(self, *a, **k):
+            return None
+    h5.File = _NoFile
+    sys.modules['h5py'] = h5
     ndt = types.ModuleType('numdifftools')
     sg = types.ModuleType('numdifftools.step_generators')
     sg.MaxStepGenerator = lambda **k: None
@@ -153,6 +172,27 @@ import gwfast.gwfastGlobals as glob          # noqa: E402
 import gwfast.waveforms as WF                 # noqa: E402
 import gwfast.signal as SIG                   # noqa: E402
 import gwfast.network as NET                  # noqa: E402
+import time                                   # noqa: E402
+
+WF.time = time   # gwfast/waveforms.py:3316 times the xi_tide tabulation without importing time
+
+# IMRPhenomNSBH tabulates xi_tide on its 200^3 grid with gwfast's own routine (8 million np.roots
+# calls, minutes) when xiTide_Table_200.h5 is absent, as here; the result is kept in /tmp between runs
+_XI_CACHE = '/tmp/gwf_xitide_200.npz'
+_tabulate = WF.IMRPhenomNSBH._tabulate_xiTide
+
+
+def _tabulate_cached(self, res=200, store=True, Compmin=.1, qmax=100.):
+    if res == 200 and Compmin == .1 and qmax == 100. and os.path.exists(_XI_CACHE):
+        z = np.load(_XI_CACHE)
+        return z['xi'], z['C'], z['q'], z['chi']
+    out = _tabulate(self, res=res, store=False, Compmin=Compmin, qmax=qmax)
+    if res == 200:
+        np.savez(_XI_CACHE, xi=out[0], C=out[1], q=out[2], chi=out[3])
+    return out
+
+
+WF.IMRPhenomNSBH._tabulate_xiTide = _tabulate_cached
 
 
 def _init_no_jit(self):
@@ -370,6 +410,20 @@ def main():
     rng = np.random.default_rng(1008)
     make_case('tf2kerr_T', WF.TaylorF2_RestrictedPN(which_ISCO='Kerr', use_3p5PN_SpinHO=True), {'ETS': (5., True)},
               events_bbh(rng, 4, mmax=40., chimax=0.9), 300)
+    # IMRPhenomNSBH: BH 1, NS 2 (Lambda1 = 0); disruptive with a torus, mildly disruptive, non-disruptive,
+    # a NS with Lambda < 1 and a fast-spinning BH
+    m1 = np.array([5., 8., 15., 6., 10.])
+    m2 = np.array([1.4, 1.35, 1.5, 1.6, 1.3])
+    ev = {'Mc': (m1 * m2) ** 0.6 / (m1 + m2) ** 0.2, 'eta': m1 * m2 / (m1 + m2) ** 2,
+          'chi1z': np.array([0.8, 0.3, 0.0, -0.3, 0.95]), 'chi2z': np.zeros(5), 'dL': np.array([0.1, 0.2, 0.3, 0.15, 0.4])}
+    ev = _angles(np.random.default_rng(1009), 5, ev)
+    ev['Lambda1'] = np.zeros(5)
+    ev['Lambda2'] = np.array([1500., 600., 300., 0.5, 2500.])
+    ev['LambdaTilde'], ev['deltaLambda'] = UT.Lamt_delLam_from_Lam12(ev['Lambda1'], ev['Lambda2'], ev['eta'])
+    # (smaller Lambda steps: one event lies within 0.1 in deltaLambda of a switch of the merger type)
+    _FD['lam_h'] = 2e-3
+    make_case('nsbh_net_earth', WF.IMRPhenomNSBH(verbose=False), {'L1': (10., True), 'ETS': (5., True)}, ev, 300)
+    _FD['lam_h'] = None
     make_gw170817()
     # KAT from the reference tutorial: GW170817-like TF2 Schwarzschild cut frequency 1590.1 Hz
     z = 0.00980

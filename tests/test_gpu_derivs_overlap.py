@@ -134,3 +134,95 @@ def test_overlap_identity_and_fmax(gpu_lib):
     np.testing.assert_allclose(s1 ** 2, o[1], rtol=1e-9)
     np.testing.assert_allclose(s2 ** 2, o[2], rtol=1e-9)
     assert np.max(np.abs(ov - o[0]) / np.sqrt(o[1] * o[2])) < 1e-7
+
+
+# the tidal, eccentric and NSBH models: (descriptor, oracle model, event kind)
+def _tidal_events(n, seed, nsbh=False, ecc=False):
+    rng = np.random.default_rng(seed + 7)
+    if nsbh:
+        m1, m2 = rng.uniform(5., 15., n), rng.uniform(1.2, 2., n)
+        ev = events('bns', n, seed)
+        ev['Mc'], ev['eta'] = (m1 * m2) ** 0.6 / (m1 + m2) ** 0.2, m1 * m2 / (m1 + m2) ** 2
+        ev['chi1z'], ev['chi2z'] = rng.uniform(-0.5, 0.9, n), np.zeros(n)
+        ev['Lambda1'], ev['Lambda2'] = np.zeros(n), rng.uniform(10., 2000., n)
+        return ev
+    ev = events('bns', n, seed)
+    ev['Lambda1'], ev['Lambda2'] = rng.uniform(50., 1500., n), rng.uniform(50., 1500., n)
+    if ecc:
+        ev['ecc'] = rng.uniform(0.01, 0.15, n)
+    return ev
+
+
+MODELS_X = {
+    'TF2_tidal_quadmon': (lambda: W.TaylorF2_RestrictedPN(is_tidal=True, use_QuadMonTid=True),
+                          O.Model('TF2', tidal=True, quadmon=True), {}),
+    'TF2_tidal_ecc_vlso': (lambda: W.TaylorF2_RestrictedPN(is_tidal=True, is_eccentric=True, phiref_vlso=True),
+                           O.Model('TF2', tidal=True, ecc=True, vlso=True), dict(ecc=True)),
+    'NRTidalv2': (lambda: W.IMRPhenomD_NRTidalv2(), O.Model('PhenomD_NRTidalv2'), {}),
+    'NSBH': (lambda: W.IMRPhenomNSBH(verbose=False), O.Model('PhenomNSBH'), dict(nsbh=True)),
+}
+
+
+@pytest.mark.parametrize('model', list(MODELS_X))
+def test_strain_derivatives_tidal_models(gpu_lib, model):
+    """return_derivatives for the 12-14 parameter models: the (P, N, R) arrays against the oracle (the
+    last point of the IMR-based models excluded: it sits on their cut or taper end, see
+    test_gpu_nrtidal and test_gpu_nsbh), and the returned Fisher is the Gram of the returned arrays."""
+    mk, om, kw = MODELS_X[model]
+    ev = _tidal_events(3, 23, **kw)
+    res = 200
+    wf = mk()
+    net = synthetic.make_network(wf, dets=(('ETS', 5.),), earth=True)
+    sig = list(net.signals.values())[0]
+    evd = dict(ev)
+    Fa, Da = sig.FisherMatr(evd, res=res, return_derivatives=True)
+    P = wf.nParams
+    p = O.to_params(evd, om.params)
+    od = oracle_det('ETS', 5., True)
+    om.prepare(p)
+    Do = O.strain_derivs_arms(od, om, p, res)
+    f, S = O.event_grid(od, om, p, res)
+    last = None if om.name == 'TF2' else -1
+    for a, (D, Dr) in enumerate(zip(Da, Do)):
+        Dr = Dr.numpy()
+        assert D.shape == Dr.shape == (P, 3, res)
+        scale = np.abs(Dr[..., :last]).max(axis=-1, keepdims=True)
+        rel = np.abs(D[..., :last] - Dr[..., :last]) / np.where(scale > 0, scale, 1.)
+        assert rel.max() < D_TOL, (a, rel.max())
+        Fg = O._gram(torch.as_tensor(D), S, f).numpy()
+        d = np.sqrt(np.abs(np.einsum('nii->ni', Fg)))
+        ferr = (np.abs(np.moveaxis(Fa[a], -1, 0) - Fg) / (d[:, :, None] * d[:, None, :])).max()
+        assert ferr < 1e-6, (a, ferr)
+
+
+PAIRS_X = [('TF2_tidal_quadmon', 'TF2_tidal_ecc_vlso', 1e-7), ('NRTidalv2', 'NRTidalv2', 1e-5),
+           ('NSBH', 'NSBH', 1e-5)]
+
+
+@pytest.mark.parametrize('pair', PAIRS_X, ids=['-'.join(p[:2]) for p in PAIRS_X])
+def test_overlap_tidal_models(gpu_lib, pair):
+    """WFOverlap with the tidal, eccentric and NSBH models against the oracle. The IMR-based models'
+    last grid point (cut or taper end, decided by rounding) moves their integrals by up to ~1e-6,
+    hence the looser tolerance there."""
+    m1, m2, tol = pair
+    mk1, om1, kw1 = MODELS_X[m1]
+    mk2, om2, kw2 = MODELS_X[m2]
+    ev1 = _tidal_events(3, 31, **{**kw1, **kw2})
+    ev2 = {k: np.array(v, copy=True) for k, v in ev1.items()}
+    ev2['Mc'] = ev2['Mc'] * (1. + 1e-4)
+    ev2['dL'] = ev2['dL'] * 1.01
+    res = 300
+    dets = (('L1', 10.), ('ETS', 5.))
+    net = synthetic.make_network(mk1(), dets=dets, earth=True)
+    sigs = list(net.signals.values())
+    e1, e2 = dict(ev1), dict(ev2)
+    ov_net = net.WFOverlap(mk1(), mk2(), e1, e2, res=res)
+    p1, p2 = O.to_params(e1, om1.params), O.to_params(e2, om2.params)
+    for (name, fmin), s in zip(dets, sigs):
+        ov, s1, s2 = s.WFOverlap(mk1(), mk2(), dict(ev1), dict(ev2), res=res, return_separate=True)
+        o_ov, o_n1, o_n2 = (x.numpy().reshape(-1) for x in O.overlap_parts(oracle_det(name, fmin, True), om1, p1, om2,
+                                                                            p2, res))
+        assert np.max(np.abs(s1 ** 2 - o_n1) / o_n1) < tol, name
+        assert np.max(np.abs(s2 ** 2 - o_n2) / o_n2) < tol, name
+        assert np.max(np.abs(ov - o_ov) / np.sqrt(o_n1 * o_n2)) < max(tol, 1e-7), name
+    assert np.all(np.abs(ov_net) <= 1. + 1e-12)

@@ -19,6 +19,7 @@ CASES = {
     'tf2tidalecc_opts': (O.Model('TF2', tidal=True, ecc=True, quadmon=True, vlso=True, fref_ecc=8.),
                          {'Virgo': (10., True), 'ETS': (5., True)}),
     'tf2kerr_T': (O.Model('TF2', spin_ho=True, kerr=True), {'ETS': (5., True)}),
+    'nsbh_net_earth': (O.Model('PhenomNSBH'), {'L1': (10., True), 'ETS': (5., True)}),
 }
 
 
