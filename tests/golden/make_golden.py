@@ -354,6 +354,32 @@ def make_gw170817():
     print('wrote kat_gw170817: SNR %.4f, sky area %.2f deg^2' % (out['snr_net'][0], out['sky_area'][0]))
 
 
+def make_fishertools_helpers():
+    """gwfast's fisherTools change-of-variable and prior helpers on Fisher and covariance matrices of the
+    IMRPhenomD golden case (gwfast/fisherTools.py:378-823)."""
+    import gwfast.fisherTools as FT
+    g = np.load(os.path.join(OUT, 'phd_net_earth.npz'))
+    F = np.asarray(g['fisher_L1'], dtype=np.float64)   # (11, 11, N)
+    ev = {k: g['ev_' + k] for k in ('Mc', 'eta', 'dL')}
+    pn = WF.IMRPhenomD().ParNums
+    out = {'F': F, 'ev_Mc': ev['Mc'], 'ev_eta': ev['eta'], 'ev_dL': ev['dL']}
+    out['prior'] = FT.addPrior(F, [1e2, 4e3], pn, ['psi', 'iota'])
+    out['logdl_fish'] = np.asarray(FT.log_dL_to_dL_derivative_fish(F, pn, ev))
+    out['logdl_cov'] = np.asarray(FT.log_dL_to_dL_derivative_cov(F, pn, ev))
+    e0 = {k: float(v[0]) for k, v in ev.items()}
+    F0 = F[:, :, 0]
+    out['m1m2_to_Mceta_fish'] = FT.m1m2_to_Mceta_fish(F0, pn, e0)
+    out['m1m2_to_Mceta_cov'] = FT.m1m2_to_Mceta_cov(F0, pn, e0)
+    out['Mceta_to_m1m2_fish'] = FT.Mceta_to_m1m2_fish(F0, pn, e0)
+    out['Mceta_to_m1m2_cov'] = FT.Mceta_to_m1m2_cov(F0, pn, e0)
+    out['chi1chi2_to_chieffDeltachi_fish'] = FT.chi1chi2_to_chieffDeltachi_fish(F0, pn, e0)
+    pns = WF.IMRPhenomD(is_chi1chi2=False).ParNums
+    out['chiSchiA_to_chi1chi2_fish'] = FT.chiSchiA_to_chi1chi2_fish(F0, pns, e0)
+    out['m1m2'] = np.array(FT.m1m2_from_Mceta(e0['Mc'], e0['eta']))
+    np.savez_compressed(os.path.join(OUT, 'fishertools_helpers.npz'), **out)
+    print('wrote fishertools_helpers')
+
+
 def main():
     import gwfast.gwfastUtils as UT
     rng = np.random.default_rng(1000)
@@ -425,6 +451,7 @@ def main():
     make_case('nsbh_net_earth', WF.IMRPhenomNSBH(verbose=False), {'L1': (10., True), 'ETS': (5., True)}, ev, 300)
     _FD['lam_h'] = None
     make_gw170817()
+    make_fishertools_helpers()
     # KAT from the reference tutorial: GW170817-like TF2 Schwarzschild cut frequency 1590.1 Hz
     z = 0.00980
     ev = {'Mc': np.array([1.1859 * (1. + z)]), 'eta': np.array([0.24786618323504223])}

@@ -196,3 +196,28 @@ def test_tidal_parameters_and_descriptor():
         U.fill_tidal(ev)
     with pytest.raises(NotImplementedError):
         W.IMRPhenomD(is_tidal=True)
+
+
+def test_fishertools_helpers_against_gwfast():
+    """Priors, log(dL) and mass/spin changes of variables against gwfast's own fisherTools
+    (tests/golden/make_golden.py: make_fishertools_helpers)."""
+    import os
+    from gwfast_gb300 import fisherTools as FT
+    from gwfast_gb300 import waveforms as W
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden', 'fishertools_helpers.npz'))
+    F = g['F']
+    ev = {'Mc': g['ev_Mc'], 'eta': g['ev_eta'], 'dL': g['ev_dL']}
+    pn = W.IMRPhenomD().ParNums
+    close = lambda a, b: np.testing.assert_allclose(a, b, rtol=1e-13, atol=0)
+    close(FT.addPrior(F, [1e2, 4e3], pn, ['psi', 'iota']), g['prior'])
+    close(FT.log_dL_to_dL_derivative_fish(F, pn, ev), g['logdl_fish'])
+    close(FT.log_dL_to_dL_derivative_cov(F, pn, ev), g['logdl_cov'])
+    e0 = {k: float(v[0]) for k, v in ev.items()}
+    F0 = F[:, :, 0]
+    for name in ('m1m2_to_Mceta_fish', 'm1m2_to_Mceta_cov', 'Mceta_to_m1m2_fish', 'Mceta_to_m1m2_cov',
+                 'chi1chi2_to_chieffDeltachi_fish'):
+        close(getattr(FT, name)(F0, pn, e0), g[name])
+    close(FT.chiSchiA_to_chi1chi2_fish(F0, W.IMRPhenomD(is_chi1chi2=False).ParNums, e0), g['chiSchiA_to_chi1chi2_fish'])
+    close(np.array(FT.m1m2_from_Mceta(e0['Mc'], e0['eta'])), g['m1m2'])
+    Mc, eta = FT.Mceta_from_m1m2(*g['m1m2'])
+    close(np.array([Mc, eta]), np.array([e0['Mc'], e0['eta']]))
