@@ -543,10 +543,16 @@ def main():
     for _ in range(max(1, args.warmup // 2)):
         net.FisherMatr(dict(ev), res=RES, precision='mixed', refine_cond=args.refine_cond)
     torch.cuda.synchronize()
+    # three calls per step: each is ~10 ms of wall clock, so a few more keep one slow call from
+    # dominating the mean
+    e2e_iter = []
+    n_e2e = 3 * args.steps
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(n_e2e):
+        ti = time.perf_counter()
         F_host = net.FisherMatr(dict(ev), res=RES, precision='mixed', refine_cond=args.refine_cond)
-    e2e_s = (time.perf_counter() - t0) / args.steps
+        e2e_iter.append(time.perf_counter() - ti)
+    e2e_s = (time.perf_counter() - t0) / n_e2e
     # the forecast pipeline: SNR pass (FP32) on every event, threshold SNR > 12, network Fisher of the
     # detected events (mixed form), covariances; Fisher/s = detected events / wall time of SNR + Fisher
     from gwfast_gb300 import pipeline
@@ -597,6 +603,7 @@ def main():
         'gpu_launches': 8 + 2 + (14 if refined > 0 else 0),
         'e2e': {'value': world * N / e2e_s, 'unit': 'Fisher/s', 'h2d_bytes_per_step': int(p_host.nbytes),
                 'd2h_bytes_per_step': int(F_host.nbytes),
+                'ms_per_step_each': [round(1e3 * t, 3) for t in e2e_iter],
                 'what': 'DetNet.FisherMatr(precision=mixed) on a host events dict, host (11, 11, N) out, wall clock'},
         'forecast_pipeline': {'value': world * ndet / pipe_s, 'unit': 'Fisher/s', 'detected': ndet, 'events': N,
                               'snr_plus_fisher_s': pipe_s, 'covariance_s': cov_t / args.steps,

@@ -1,5 +1,7 @@
 // C-ABI layer: context, detector tables, staging and launches (see include/gwfast_gb300.h).
 #include <cuda_runtime.h>
+#include <sys/mman.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <cmath>
@@ -118,6 +120,25 @@ struct gwf_ctx {
 };
 
 namespace {
+
+// Map every page of a host output buffer before a device-to-host copy into it. A buffer the caller
+// has just allocated is not mapped yet; the copy would then take its page faults one by one inside
+// the driver (~1 ms per MB measured on the GB300 host), while mapping them here first is several
+// times cheaper: one madvise(MADV_POPULATE_WRITE) (Linux 5.14+), or else a touch per page that
+// writes back the byte it read, so the contents are unchanged either way.
+#ifndef MADV_POPULATE_WRITE
+#define MADV_POPULATE_WRITE 23
+#endif
+void prefault_host(void* p, size_t bytes) {
+  if (!p || !bytes) return;
+  static const size_t page = [] { long s = sysconf(_SC_PAGESIZE); return s > 0 ? (size_t)s : (size_t)4096; }();
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)(page - 1);
+  const size_t len = ((reinterpret_cast<uintptr_t>(p) + bytes - a) + page - 1) & ~(page - 1);
+  if (madvise(reinterpret_cast<void*>(a), len, MADV_POPULATE_WRITE) == 0) return;
+  volatile unsigned char* c = reinterpret_cast<volatile unsigned char*>(p);
+  for (size_t i = 0; i < bytes; i += page) c[i] = c[i];
+  c[bytes - 1] = c[bytes - 1];
+}
 
 // Fisher parameters of a waveform model: 11; 13 for the tidal models (LambdaTilde, deltaLambda); the
 // eccentric TaylorF2 adds ecc (12, or 14 with the tidal terms)
@@ -655,6 +676,8 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   }
   if (!capturing) GWF_CK(cudaEventRecord(ctx->scratch_free, st));
   if (mem == GWF_MEM_HOST) {
+    prefault_host(out_arm, out_arm ? (size_t)slots * N * per * sizeof(double) : 0);
+    prefault_host(out_net, out_net ? (size_t)N * per * sizeof(double) : 0);
     if (out_arm) GWF_CK(cudaMemcpyAsync(out_arm, darm, (size_t)slots * N * per * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (out_net) GWF_CK(cudaMemcpyAsync(out_net, dnet, (size_t)N * per * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (sd_arm) GWF_CK(cudaMemcpyAsync(sd_arm, dsda, (size_t)slots * N * npar * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1057,6 +1080,7 @@ int gwf_strain_derivs(gwf_ctx* ctx, int det_id, const gwf_wf_desc* wf, const dou
     if (e != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
     if (mem == GWF_MEM_HOST) {   // rows [n0, n0 + cnt) of each (arm, parameter) block
       const size_t row = (size_t)res * 2 * sizeof(double);
+      if (n0 == 0) prefault_host(out, (size_t)NA * npar * N * row);
       GWF_CK(cudaMemcpy2DAsync(out + (size_t)n0 * res * 2, (size_t)N * row, ctx->wbuf.p, (size_t)cnt * row,
                                (size_t)cnt * row, (size_t)NA * npar, cudaMemcpyDeviceToHost, st));
     }
