@@ -10,7 +10,7 @@ value: events/s of the chosen form with the event arrays resident in HBM, CUDA-e
        per step (L2 flushed by a 256 MB write before each step, outside the timed interval).
        The chosen form is 'mixed': the FP32 split-precision kernel for every event, the
        condition number of every network Fisher, and the FP64 kernel again for the events
-       above 1e12 (gathered, recomputed, scattered back), all inside the step.  The plain FP64
+       above 1e13 (gathered, recomputed, scattered back), all inside the step.  The plain FP64
        kernel and the FP32 form alone are timed the same way (`plain_fp64`, `fp32_only`), and
        the marginalised 1-sigma errors of both reduced forms are compared with the FP64 ones
        on the workload's events (`sigma_err`, `sigma_err_fp32_only`).
@@ -403,7 +403,7 @@ def main():
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--only-device', action='store_true', help='only the device-resident Fisher steps (for ncu)')
     ap.add_argument('--precision', default='fp32', choices=('fp32', 'fp64', 'mixed'), help='form used with --only-device')
-    ap.add_argument('--refine-cond', type=float, default=1e12, help='condition-number threshold of the mixed form')
+    ap.add_argument('--refine-cond', type=float, default=1e13, help='condition-number threshold of the mixed form')
     ap.add_argument('--no-autotune', action='store_true', help='per-event launches, no segment autotuning')
     ap.add_argument('--workload', default='lhet', choices=('lhet', 'mixed-catalogue', 'screen', 'hm'),
                     help='lhet: the headline workload; mixed-catalogue: the batching workload; screen: the learned '

@@ -98,7 +98,9 @@ struct gwf_ctx {
   int nq = 0;
   DevBuf par, res, oarm, onet, fin, fout, feps, fcond, setup;
   DevBuf mix_idx, mix_cnt, mix_par, mix_res, mix_net, mix_arm;  // FP64 recomputation of GWF_PREC_MIXED
-  double refine_cond = 1e12;
+  // below 1e13 the FP32 form's marginalised errors are within 1e-4 of FP64 on every event of the
+  // IMRPhenomD headline workload (max 7.0e-5 with either threshold 1e12 or 1e13)
+  double refine_cond = 1e13;
   int seg_points = 0;      // Fisher launches: 0 = one CTA per event, > 0 = persistent, segments of this many points
   int refine_seg = 256;    // segment length of the FP64 recomputation of GWF_PREC_MIXED
   DevBuf seg_off, seg_ctr, seg_part, seg_ovf, tune_out;
@@ -117,6 +119,12 @@ struct gwf_ctx {
   int groups = 1;                  // FP32 network totals: detectors sharing the grid in one launch
   DevBuf xit;                      // IMRPhenomNSBH xi_tide table, built on first use
   bool xit_ready = false;
+  // GWF_PREC_MIXED recomputation: one stream per detector, so that the detectors' FP64 passes over
+  // the few ill-conditioned events run side by side; per-detector scratch and segment buffers
+  std::vector<cudaStream_t> aux;
+  std::vector<cudaEvent_t> aux_done;
+  cudaEvent_t fork = nullptr;
+  DevBuf mix_scr, mix_soff, mix_sctr, mix_spart, mix_sovf;
 };
 
 namespace {
@@ -352,8 +360,25 @@ int seg_setup(gwf_ctx* ctx, gwf::LaunchArgs& a, int seg, int64_t chunk, int64_t 
   return GWF_OK;
 }
 
+int ensure_aux(gwf_ctx* ctx, int n) {
+  if (!ctx->fork) GWF_CK(cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming));
+  while ((int)ctx->aux.size() < n) {
+    cudaStream_t s;
+    cudaEvent_t e;
+    GWF_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      cudaStreamDestroy(s);
+      return fail(GWF_ERR_CUDA, "event creation failed");
+    }
+    ctx->aux.push_back(s);
+    ctx->aux_done.push_back(e);
+  }
+  return GWF_OK;
+}
+
 // GWF_PREC_MIXED, second stage: condition numbers of the FP32 network Fishers, then the FP64
-// Fisher of the events above the threshold, computed as a compact batch and scattered back
+// Fisher of the events above the threshold, computed as a compact batch (the detectors side by side
+// on their own streams) and scattered back
 int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const double* dp, int64_t dld,
            const int* dres, int64_t N, int slots, double* darm, double* dnet, double* dsda, double* dsdn,
            bool core_filled, cudaStream_t st) {
@@ -370,7 +395,7 @@ int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("mixed precision: ") + cudaGetErrorString(e));
   if (M == 0) return GWF_OK;
-  if (ctx->mix_par.ensure(M * gwf::NP * sizeof(double)) || ctx->mix_net.ensure(M * per * sizeof(double)) ||
+  if (ctx->mix_par.ensure(M * gwf::NP * sizeof(double)) || ctx->mix_net.ensure((size_t)n_det * M * per * sizeof(double)) ||
       (dres && ctx->mix_res.ensure(M * sizeof(int))) || (darm && ctx->mix_arm.ensure((size_t)slots * M * per * sizeof(double))))
     return fail(GWF_ERR_OOM, "device allocation failed (mixed precision)");
   double* cpar = (double*)ctx->mix_par.p;
@@ -378,7 +403,7 @@ int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const
   double* carm = darm ? (double*)ctx->mix_arm.p : nullptr;
   int* cres = dres ? (int*)ctx->mix_res.p : nullptr;
   if ((dsda && ctx->mix_sda.ensure((size_t)slots * M * gwf::NP * sizeof(double))) ||
-      (dsdn && ctx->mix_sdn.ensure((size_t)M * gwf::NP * sizeof(double))))
+      (dsdn && ctx->mix_sdn.ensure((size_t)n_det * M * gwf::NP * sizeof(double))))
     return fail(GWF_ERR_OOM, "device allocation failed (mixed precision)");
   double* csda = dsda ? (double*)ctx->mix_sda.p : nullptr;
   double* csdn = dsdn ? (double*)ctx->mix_sdn.p : nullptr;
@@ -399,29 +424,53 @@ int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const
     int rc = max_res(a.ev.res, dres, N, GWF_MEM_DEVICE, &rmax);
     if (rc) return rc;
   }
-  {
-    const int64_t chunk = (int64_t)M < gwf::kChunk ? (int64_t)M : gwf::kChunk;
-    int rc = seg_setup(ctx, a, ctx->refine_seg, chunk, rmax, st);
-    if (rc) return rc;
-  }
+  // per-detector scratch and segment buffers
+  const int64_t chunk = (int64_t)M < gwf::kChunk ? (int64_t)M : gwf::kChunk;
+  const int seg = ctx->refine_seg;
+  const long long per_ev = (long long)((rmax + seg - 1) / seg);
+  const long long cap = (long long)chunk * (per_ev > 0 ? per_ev : 1);
+  const size_t stride = setup_stride_any(a.wf.model);
+  if (ctx->mix_scr.ensure((size_t)n_det * chunk * stride) ||
+      ctx->mix_soff.ensure((size_t)n_det * (gwf::kChunk + 1) * sizeof(long long)) ||
+      ctx->mix_sctr.ensure((size_t)n_det * sizeof(unsigned long long)) ||
+      ctx->mix_spart.ensure((size_t)n_det * cap * 3 * gwf::NEX * sizeof(double)) ||
+      ctx->mix_sovf.ensure((size_t)n_det * sizeof(int)))
+    return fail(GWF_ERR_OOM, "device allocation failed (mixed precision)");
+  int rc = ensure_aux(ctx, n_det);
+  if (rc) return rc;
+  GWF_CK(cudaMemsetAsync(ctx->mix_sovf.p, 0, (size_t)n_det * sizeof(int), st));
+  GWF_CK(cudaEventRecord(ctx->fork, st));
   int slot = 0;
   for (int i = 0; i < n_det; ++i) {
     const DetRec& r = ctx->dets[det_ids[i]];
-    a.det = dev_of(r);
-    a.out_arm = carm ? carm + (size_t)slot * M * per : nullptr;
-    a.out_det = cnet;
-    a.out_sd_arm = csda ? csda + (size_t)slot * M * gwf::NP : nullptr;
-    a.out_sd_det = csdn;
-    a.accum = i > 0;
-    const int model = a.wf.model;
-    e = model == 0 ? gwf::launch_fisher_m0(a) : (model == 1 ? gwf::launch_fisher_m1(a) : gwf::launch_fisher_m2(a));
+    gwf::LaunchArgs ai = a;
+    ai.stream = ctx->aux[i];
+    GWF_CK(cudaStreamWaitEvent(ai.stream, ctx->fork, 0));
+    ai.det = dev_of(r);
+    ai.scratch = (unsigned char*)ctx->mix_scr.p + (size_t)i * chunk * stride;
+    ai.cap_events = chunk;
+    ai.seg = seg;
+    ai.seg_off = (long long*)ctx->mix_soff.p + (size_t)i * (gwf::kChunk + 1);
+    ai.seg_ctr = (unsigned long long*)ctx->mix_sctr.p + i;
+    ai.seg_part = (double*)ctx->mix_spart.p + (size_t)i * cap * 3 * gwf::NEX;
+    ai.seg_cap = cap;
+    ai.seg_ovf = (int*)ctx->mix_sovf.p + i;
+    ai.out_arm = carm ? carm + (size_t)slot * M * per : nullptr;
+    ai.out_det = cnet + (size_t)i * M * per;
+    ai.out_sd_arm = csda ? csda + (size_t)slot * M * gwf::NP : nullptr;
+    ai.out_sd_det = csdn ? csdn + (size_t)i * M * gwf::NP : nullptr;
+    ai.accum = 0;
+    e = launch_fisher_any(ai.wf.model, ai);
     if (e != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    GWF_CK(cudaEventRecord(ctx->aux_done[i], ai.stream));
     slot += r.desc.shape == GWF_SHAPE_T ? 3 : 1;
   }
-  e = gwf::launch_scatter(cnet, idx, (long long)M, (int)per, dnet, st);
+  for (int i = 0; i < n_det; ++i) GWF_CK(cudaStreamWaitEvent(st, ctx->aux_done[i], 0));
+  e = gwf::launch_sum_scatter(cnet, n_det, (long long)M * per, idx, (long long)M, (int)per, dnet, st);
   for (int s = 0; carm && s < slots && e == cudaSuccess; ++s)
     e = gwf::launch_scatter(carm + (size_t)s * M * per, idx, (long long)M, (int)per, darm + (size_t)s * N * per, st);
-  if (csdn && e == cudaSuccess) e = gwf::launch_scatter(csdn, idx, (long long)M, gwf::NP, dsdn, st);
+  if (csdn && e == cudaSuccess)
+    e = gwf::launch_sum_scatter(csdn, n_det, (long long)M * gwf::NP, idx, (long long)M, gwf::NP, dsdn, st);
   for (int s = 0; csda && s < slots && e == cudaSuccess; ++s)
     e = gwf::launch_scatter(csda + (size_t)s * M * gwf::NP, idx, (long long)M, gwf::NP,
                             dsda + (size_t)s * N * gwf::NP, st);
@@ -683,9 +732,13 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
     if (sd_arm) GWF_CK(cudaMemcpyAsync(sd_arm, dsda, (size_t)slots * N * npar * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (sd_net) GWF_CK(cudaMemcpyAsync(sd_net, dsdn, (size_t)N * npar * sizeof(double), cudaMemcpyDeviceToHost, st));
     int ovf = 0;
-    if (fisher && (a.seg > 0 || precision == GWF_PREC_MIXED) && ctx->seg_ovf.p)
+    std::vector<int> movf(precision == GWF_PREC_MIXED && ctx->mix_sovf.p ? n_det : 0, 0);
+    if (fisher && a.seg > 0 && ctx->seg_ovf.p)
       GWF_CK(cudaMemcpyAsync(&ovf, ctx->seg_ovf.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (fisher && !movf.empty())
+      GWF_CK(cudaMemcpyAsync(movf.data(), ctx->mix_sovf.p, movf.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
     GWF_CK(cudaStreamSynchronize(st));
+    for (int v : movf) ovf |= v;
     if (ovf) return fail(GWF_ERR_CUDA, "segment buffer overflow (internal error)");
   }
   return GWF_OK;
@@ -784,6 +837,11 @@ int gwf_ctx_destroy(gwf_ctx* ctx) {
   ctx->wbuf.release(); ctx->par2.release(); ctx->fcutb.release(); ctx->ovb.release();
   ctx->core.release();
   ctx->xit.release();
+  ctx->mix_scr.release(); ctx->mix_soff.release(); ctx->mix_sctr.release(); ctx->mix_spart.release();
+  ctx->mix_sovf.release();
+  for (auto s : ctx->aux) cudaStreamDestroy(s);
+  for (auto e : ctx->aux_done) cudaEventDestroy(e);
+  if (ctx->fork) cudaEventDestroy(ctx->fork);
   for (auto& g : ctx->graph_cache) cudaGraphExecDestroy(g.second.exec);
   ctx->graph_cache.clear();
   ctx->hpar.release(); ctx->hout.release();

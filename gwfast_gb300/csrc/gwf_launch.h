@@ -98,5 +98,7 @@ cudaError_t launch_select(const double* cond, long long N, double thresh, long l
 cudaError_t launch_gather(const double* p, long long ld, const int* res, const long long* idx, long long M, double* out,
                           int* res_out, cudaStream_t st);
 cudaError_t launch_scatter(const double* src, const long long* idx, long long M, int per, double* dst, cudaStream_t st);
+cudaError_t launch_sum_scatter(const double* src, int nslice, long long slice_stride, const long long* idx, long long M,
+                               int per, double* dst, cudaStream_t st);
 
 }  // namespace gwf

@@ -109,6 +109,18 @@ __global__ void gather_kernel(const double* __restrict__ p, long long ld, const 
   if (res) res_out[m] = res[n];
 }
 
+// dst[idx[m]][j] = sum over s < nslice of src[s][m][j] (slices nslice_stride apart), j < per
+__global__ void sum_scatter_kernel(const double* __restrict__ src, int nslice, long long slice_stride,
+                                   const long long* __restrict__ idx, long long M, int per, double* __restrict__ dst) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= M * per) return;
+  const long long m = t / per;
+  const int j = (int)(t - m * per);
+  double v = 0.0;
+  for (int s = 0; s < nslice; ++s) v += src[s * slice_stride + t];
+  dst[idx[m] * per + j] = v;
+}
+
 // dst[idx[m]][j] = src[m][j], j < per
 __global__ void scatter_kernel(const double* __restrict__ src, const long long* __restrict__ idx, long long M,
                                int per, double* __restrict__ dst) {
@@ -141,6 +153,13 @@ cudaError_t launch_gather(const double* p, long long ld, const int* res, const l
                           int* res_out, cudaStream_t st) {
   if (M <= 0) return cudaSuccess;
   gather_kernel<<<blocks(M, 256), 256, 0, st>>>(p, ld, res, idx, M, out, res_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sum_scatter(const double* src, int nslice, long long slice_stride, const long long* idx, long long M,
+                               int per, double* dst, cudaStream_t st) {
+  if (M <= 0) return cudaSuccess;
+  sum_scatter_kernel<<<blocks(M * per, 256), 256, 0, st>>>(src, nslice, slice_stride, idx, M, per, dst);
   return cudaGetLastError();
 }
 

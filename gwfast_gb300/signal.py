@@ -76,7 +76,7 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
     per arm.
     precision: 'fp64' (the drop-in), 'fp32' (split precision; IMRPhenomHM with FP64 mode phases), or
     'mixed' ('fp32', then FP64 for the events whose network Fisher has an equilibrated condition
-    number above refine_cond, default 1e12).
+    number above refine_cond, default 1e13).
     """
     wf = signals[0].wf_model
     p = _prep(evParams, wf)
@@ -85,7 +85,7 @@ def fisher_batch(signals, evParams, res=1000, per_arm=False, spacing='geom', dev
     slots = _arm_slots(signals)
     ctx = _lib.context(device)
     if precision == 'mixed':
-        ctx.set_refine_cond(1e12 if refine_cond is None else refine_cond)
+        ctx.set_refine_cond(1e13 if refine_cond is None else refine_cond)
     sp = 0 if spacing == 'geom' else 1
     rev = None if res_per_event is None else np.ascontiguousarray(np.broadcast_to(res_per_event, (N,)), dtype=np.int32)
     duty = any(s.DutyFactor is not None for s in signals)

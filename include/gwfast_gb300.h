@@ -136,7 +136,8 @@ int gwf_snr(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, 
  * FP64, per-point arithmetic in FP32, outputs in FP64; IMRPhenomHM with its mode phases in FP64), or
  * GWF_PREC_MIXED: GWF_PREC_FP32 for all events, then the events whose network Fisher has an
  * equilibrated condition number above the context's threshold (gwf_set_refine_cond, default
- * 1e12) or a non-finite one are recomputed in FP64 (all outputs). With mem = GWF_MEM_DEVICE,
+ * 1e13) or a non-finite one are recomputed in FP64 (all outputs), each detector's pass on its own
+ * stream. With mem = GWF_MEM_DEVICE,
  * GWF_PREC_MIXED waits on the stream once, to read how many events need FP64. */
 int gwf_fisher(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params, int64_t ld,
                int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int per_arm, int precision,
