@@ -125,6 +125,10 @@ struct gwf_ctx {
   std::vector<cudaEvent_t> aux_done;
   cudaEvent_t fork = nullptr;
   DevBuf mix_scr, mix_soff, mix_sctr, mix_spart, mix_sovf;
+  // detector groups of one call side by side (each on an aux stream after the first, which runs on
+  // the call's stream and fills the source-record cache): per-group network totals, summed at the end
+  cudaEvent_t core_ev = nullptr;
+  DevBuf gnet;
 };
 
 namespace {
@@ -650,7 +654,19 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   }
   size_t gmax = 1;
   for (auto& g : groups) gmax = g.size() > gmax ? g.size() : gmax;
-  if (ctx->setup.ensure(gmax * chunk * stride)) return fail(GWF_ERR_OOM, "device allocation failed (set-up scratch)");
+  // the groups run side by side when each has its own scratch and output: network totals and
+  // per-arm slots without SNR derivatives, not in a graph capture, no segmented launches
+  const int ngr = (int)groups.size();
+  const bool side = ngr > 1 && !capturing && !dsda && !dsdn && !(fisher && ctx->seg_points > 0) && dnet;
+  if (ctx->setup.ensure((side ? ngr : 1) * gmax * chunk * stride))
+    return fail(GWF_ERR_OOM, "device allocation failed (set-up scratch)");
+  if (side) {
+    if (ctx->gnet.ensure((size_t)(ngr - 1) * N * per * sizeof(double))) return fail(GWF_ERR_OOM, "device allocation failed (out)");
+    rc = ensure_aux(ctx, ngr);
+    if (!rc && !ctx->core_ev && cudaEventCreateWithFlags(&ctx->core_ev, cudaEventDisableTiming) != cudaSuccess)
+      rc = fail(GWF_ERR_CUDA, "event creation failed");
+    if (rc) return rc;
+  }
   // a network shares the source-dependent part of the per-event set-up between its detectors
   const size_t core_b = core_bytes_any(wf->model);
   const bool share = n_det > 1 && ctx->core.ensure((size_t)N * core_b) == 0;
@@ -687,12 +703,26 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   a.stream = st;
   int slot = 0;
   bool first = true;
+  if (side) GWF_CK(cudaEventRecord(ctx->fork, st));
+  int gi = 0;
   for (auto& grp : groups) {
     a.core = share ? (unsigned char*)ctx->core.p : nullptr;
     a.core_mode = share ? (first ? 1 : 2) : 0;
     a.accum = !first;
     a.out_det = dnet;
+    if (side) {
+      a.accum = 0;
+      a.core_done = first && share ? ctx->core_ev : nullptr;
+      a.scratch = (unsigned char*)ctx->setup.p + (size_t)gi * gmax * chunk * stride;
+      if (!first) {
+        a.stream = ctx->aux[gi];
+        a.out_det = (double*)ctx->gnet.p + (size_t)(gi - 1) * N * per;
+        GWF_CK(cudaStreamWaitEvent(a.stream, ctx->fork, 0));
+        if (share) GWF_CK(cudaStreamWaitEvent(a.stream, ctx->core_ev, 0));
+      }
+    }
     first = false;
+    ++gi;
     cudaError_t err;
     if (grp.size() > 1) {   // (grouping implies: FP32 Fisher, network total only)
       gwf::GroupDev g;
@@ -708,6 +738,7 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
       a.out_sd_det = nullptr;
       err = wf->model == 0 ? gwf::launch_group_m0(a, g) : (wf->model == 1 ? gwf::launch_group_m1(a, g) : gwf::launch_group_m2(a, g));
       if (err != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(err));
+      if (side && gi > 1) GWF_CK(cudaEventRecord(ctx->aux_done[gi - 1], a.stream));
       continue;
     }
     const DetRec& r = ctx->dets[det_ids[grp[0]]];
@@ -717,7 +748,15 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
     a.out_sd_det = dsdn;
     err = fisher ? launch_fisher_any(wf->model, a) : launch_snr_any(wf->model, a);
     if (err != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(err));
+    if (side && gi > 1) GWF_CK(cudaEventRecord(ctx->aux_done[gi - 1], a.stream));
     slot += r.desc.shape == GWF_SHAPE_T ? 3 : 1;
+  }
+  if (side) {   // join the groups and add their network totals
+    for (int g = 1; g < ngr; ++g) GWF_CK(cudaStreamWaitEvent(st, ctx->aux_done[g], 0));
+    a.stream = st;
+    a.scratch = (unsigned char*)ctx->setup.p;
+    a.core_done = nullptr;
+    GWF_CK(gwf::launch_add_slices((const double*)ctx->gnet.p, ngr - 1, (long long)N * per, (long long)N * per, dnet, st));
   }
   if (precision == GWF_PREC_MIXED) {
     rc = refine(ctx, n_det, det_ids, a, dp, dld, dres, N, slots, darm, dnet, dsda, dsdn, share, st);
@@ -842,6 +881,8 @@ int gwf_ctx_destroy(gwf_ctx* ctx) {
   for (auto s : ctx->aux) cudaStreamDestroy(s);
   for (auto e : ctx->aux_done) cudaEventDestroy(e);
   if (ctx->fork) cudaEventDestroy(ctx->fork);
+  if (ctx->core_ev) cudaEventDestroy(ctx->core_ev);
+  ctx->gnet.release();
   for (auto& g : ctx->graph_cache) cudaGraphExecDestroy(g.second.exec);
   ctx->graph_cache.clear();
   ctx->hpar.release(); ctx->hout.release();

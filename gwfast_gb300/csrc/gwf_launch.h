@@ -36,6 +36,7 @@ struct LaunchArgs {
   unsigned char* core = nullptr;           // N x core_bytes(model)
   int core_mode = 0;                       // 0: none, 1: compute and store, 2: load
   const long long* core_idx = nullptr;     // cache row of each event of a gathered batch
+  cudaEvent_t core_done = nullptr;         // recorded after each set-up that stores into the cache
 };
 
 cudaError_t launch_fisher_m0(const LaunchArgs& a);
@@ -98,6 +99,8 @@ cudaError_t launch_select(const double* cond, long long N, double thresh, long l
 cudaError_t launch_gather(const double* p, long long ld, const int* res, const long long* idx, long long M, double* out,
                           int* res_out, cudaStream_t st);
 cudaError_t launch_scatter(const double* src, const long long* idx, long long M, int per, double* dst, cudaStream_t st);
+cudaError_t launch_add_slices(const double* src, int nslice, long long slice_stride, long long n, double* dst,
+                              cudaStream_t st);
 cudaError_t launch_sum_scatter(const double* src, int nslice, long long slice_stride, const long long* idx, long long M,
                                int per, double* dst, cudaStream_t st);
 

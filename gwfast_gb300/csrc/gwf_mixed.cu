@@ -121,6 +121,16 @@ __global__ void sum_scatter_kernel(const double* __restrict__ src, int nslice, l
   dst[idx[m] * per + j] = v;
 }
 
+// dst[t] += sum over s < nslice of src[s][t] (slices slice_stride apart), t < n
+__global__ void add_slices_kernel(const double* __restrict__ src, int nslice, long long slice_stride, long long n,
+                                  double* __restrict__ dst) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  double v = dst[t];
+  for (int s = 0; s < nslice; ++s) v += src[s * slice_stride + t];
+  dst[t] = v;
+}
+
 // dst[idx[m]][j] = src[m][j], j < per
 __global__ void scatter_kernel(const double* __restrict__ src, const long long* __restrict__ idx, long long M,
                                int per, double* __restrict__ dst) {
@@ -160,6 +170,13 @@ cudaError_t launch_sum_scatter(const double* src, int nslice, long long slice_st
                                int per, double* dst, cudaStream_t st) {
   if (M <= 0) return cudaSuccess;
   sum_scatter_kernel<<<blocks(M * per, 256), 256, 0, st>>>(src, nslice, slice_stride, idx, M, per, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_add_slices(const double* src, int nslice, long long slice_stride, long long n, double* dst,
+                              cudaStream_t st) {
+  if (n <= 0 || nslice <= 0) return cudaSuccess;
+  add_slices_kernel<<<blocks(n, 256), 256, 0, st>>>(src, nslice, slice_stride, n, dst);
   return cudaGetLastError();
 }
 

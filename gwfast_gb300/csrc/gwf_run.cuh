@@ -31,6 +31,10 @@ cudaError_t chunked(const LaunchArgs& a, bool f32, MAIN main) {
     const long long cnt = (a.ev.N - n0) < kChunk ? (a.ev.N - n0) : kChunk;
     const unsigned nb = (unsigned)((cnt + 63) / 64);
     setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, a.det, a.wf, a.qnm, a.nq, a.scratch, cnt, a.core, a.core_mode, a.core_idx);
+    if (a.core_done && a.core_mode == 1) {
+      const cudaError_t er = cudaEventRecord(a.core_done, a.stream);
+      if (er != cudaSuccess) return er;
+    }
     if constexpr (M < 3) {   // (the tidal models have no FP32 form)
       if (f32) setup_f32_kernel<M><<<nb, 64, 0, a.stream>>>(a.det, a.scratch, scratch32_of(a), cnt,
                                                             a.det.shape == 1 ? 2 : 1, a.det.earth);
@@ -206,6 +210,10 @@ cudaError_t group_one(const LaunchArgs& a, GroupDev g) {
       unsigned char* sc = a.scratch + (size_t)d * chunk * stride;
       const int mode = d == 0 ? a.core_mode : (a.core ? 2 : 0);
       setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, g.det[d], a.wf, a.qnm, a.nq, sc, cnt, a.core, mode, nullptr);
+      if (a.core_done && mode == 1) {
+        err = cudaEventRecord(a.core_done, a.stream);
+        if (err != cudaSuccess) return err;
+      }
       setup_f32_kernel<M><<<nb, 64, 0, a.stream>>>(g.det[d], sc, sc + (size_t)chunk * rec_stride<M>(), cnt,
                                                    g.det[d].shape == 1 ? 2 : 1, g.det[d].earth);
     }
