@@ -892,7 +892,8 @@ struct GroupProj {
   TimeF tsc[kMaxGroup];
 };
 
-template <int MODEL, bool EARTH>
+// TRI: the group holds a triangle; without one the triangle branch (and its registers) is left out
+template <int MODEL, bool EARTH, bool TRI>
 __device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32State<MODEL, 1>& S, const GroupProj& gp,
                                       int2* stage, int k1) {
   constexpr int NQ = 12;
@@ -978,7 +979,7 @@ __device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32S
       float sw = 0.0f;
       if (valid) sw = sqrtf(4.0f * w / psd_at_f(det, f, lnf, (float)det.acc_l0, (float)det.acc_idl)) * g.wr[d];
       cf u[NP];
-      if (det.shape == 0) {
+      if (!TRI || det.shape == 0) {
         cf D[1][NP], Hs[1];
         if (valid) project_f32<EARTH, 1>(wv, gp.pf[d], gp.apc[d], gp.tsc[d], f, D, Hs);
 #pragma unroll
@@ -1019,7 +1020,7 @@ __device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32S
   __syncthreads();
 }
 
-template <int MODEL, bool EARTH>
+template <int MODEL, bool EARTH, bool TRI>
 __global__ void __launch_bounds__(kThreads, 5) fisher_group_kernel_f32(EvBatch ev, GroupDev g,
                                                                        const unsigned char* scratch32, double* out_det,
                                                                        int accum) {
@@ -1038,7 +1039,7 @@ __global__ void __launch_bounds__(kThreads, 5) fisher_group_kernel_f32(EvBatch e
     gp.tsc[d] = rd.tsc;
   }
   f32_prepare<MODEL, 1>(scratch32, blockIdx.x, S);
-  f32_item_group<MODEL, EARTH>(ev, g, S, gp, reinterpret_cast<int2*>(stage_raw), S.r.gf.R);
+  f32_item_group<MODEL, EARTH, TRI>(ev, g, S, gp, reinterpret_cast<int2*>(stage_raw), S.r.gf.R);
   write_gram<1>(S.gsum, S.r.scale, ColMix{2.0 * S.r.psi_sgn, S.r.chi_alpha}, n, ev.N, nullptr, out_det, nullptr, nullptr,
                 accum);
 }

@@ -192,10 +192,10 @@ cudaError_t snr_dispatch(const LaunchArgs& a) {
 
 // a group of detectors sharing the grid (network total, FP32 form): per chunk, the set-up of each
 // detector into its own scratch slice, then one launch over all of them
-template <bool EARTH>
+template <bool EARTH, bool TRI>
 cudaError_t group_one(const LaunchArgs& a, GroupDev g) {
   const int smem = kWarps * 12 * kSR * (int)sizeof(int2);
-  auto k = fisher_group_kernel_f32<M, EARTH>;
+  auto k = fisher_group_kernel_f32<M, EARTH, TRI>;
   cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (err != cudaSuccess) return err;
   const long long chunk = a.cap_events;
@@ -226,7 +226,12 @@ cudaError_t group_one(const LaunchArgs& a, GroupDev g) {
 
 cudaError_t group_dispatch(const LaunchArgs& a, const GroupDev& g) {
   if constexpr (M >= 3) return cudaErrorNotSupported;
-  else return a.det.earth ? group_one<true>(a, g) : group_one<false>(a, g);
+  else {
+    bool tri = false;
+    for (int d = 0; d < g.nd; ++d) tri |= g.det[d].shape == 1;
+    if (tri) return a.det.earth ? group_one<true, true>(a, g) : group_one<false, true>(a, g);
+    return a.det.earth ? group_one<true, false>(a, g) : group_one<false, false>(a, g);
+  }
 }
 
 template <bool EARTH, int NARM>
