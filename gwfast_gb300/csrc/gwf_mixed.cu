@@ -17,72 +17,98 @@ namespace {
 // eigen-decomposition of the covariance kernel; only used to pick events for FP64, where a
 // factor of a few does not matter: the largest eigenvalue of an equilibrated 11 x 11 matrix lies
 // in [1, 11] and the Rayleigh quotients converge quadratically, so 12 and 8 steps suffice.
-__global__ void cond_kernel(const double* __restrict__ F, long long N, double* __restrict__ cond) {
+__global__ void __launch_bounds__(64) cond_kernel(const double* __restrict__ F, long long N, double* __restrict__ cond) {
   const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= N) return;
   constexpr int K = NP;
+  // the factor is kept as a packed lower triangle and every loop over rows and columns is unrolled,
+  // so that it stays in registers (indexed arrays would live in local memory)
+  auto T = [](int i, int k) { return i * (i + 1) / 2 + k; };
   const double* f = F + n * K * K;
-  double w[K], L[K * K];
+  double w[K], L[K * (K + 1) / 2], il[K];
+#pragma unroll
   for (int i = 0; i < K; ++i) {
     const double d = f[i * K + i];
     if (!(d > 0.0)) { cond[n] = INFINITY; return; }
     w[i] = 1.0 / sqrt(d);
   }
-  // Cholesky of A = diag(w) F diag(w), lower triangle of L
+  // Cholesky of A = diag(w) F diag(w)
+#pragma unroll
   for (int j = 0; j < K; ++j) {
     double s = f[j * K + j] * w[j] * w[j];
-    for (int k = 0; k < j; ++k) s -= L[j * K + k] * L[j * K + k];
+#pragma unroll
+    for (int k = 0; k < j; ++k) s -= L[T(j, k)] * L[T(j, k)];
     if (!(s > 0.0)) { cond[n] = INFINITY; return; }
     const double ljj = sqrt(s);
-    L[j * K + j] = ljj;
+    L[T(j, j)] = ljj;
+    il[j] = 1.0 / ljj;
+#pragma unroll
     for (int i = j + 1; i < K; ++i) {
       double t = f[i * K + j] * w[i] * w[j];
-      for (int k = 0; k < j; ++k) t -= L[i * K + k] * L[j * K + k];
-      L[i * K + j] = t / ljj;
+#pragma unroll
+      for (int k = 0; k < j; ++k) t -= L[T(i, k)] * L[T(j, k)];
+      L[T(i, j)] = t * il[j];
     }
   }
   double x[K], y[K];
   // largest eigenvalue: power iteration on A = L L^T
+#pragma unroll
   for (int i = 0; i < K; ++i) x[i] = 1.0 + 0.1 * i;
   double lmax = 0.0;
+#pragma unroll 1
   for (int it = 0; it < 12; ++it) {
     double nx = 0.0;
+#pragma unroll
     for (int i = 0; i < K; ++i) nx += x[i] * x[i];
     nx = 1.0 / sqrt(nx);
+#pragma unroll
     for (int i = 0; i < K; ++i) x[i] *= nx;
+#pragma unroll
     for (int i = 0; i < K; ++i) {   // y = L^T x
       double s = 0.0;
-      for (int k = i; k < K; ++k) s += L[k * K + i] * x[k];
+#pragma unroll
+      for (int k = i; k < K; ++k) s += L[T(k, i)] * x[k];
       y[i] = s;
     }
     double q = 0.0;
+#pragma unroll
     for (int i = 0; i < K; ++i) {   // x = L y, Rayleigh quotient |L^T x|^2
       q += y[i] * y[i];
       double s = 0.0;
-      for (int k = 0; k <= i; ++k) s += L[i * K + k] * y[k];
+#pragma unroll
+      for (int k = 0; k <= i; ++k) s += L[T(i, k)] * y[k];
       x[i] = s;
     }
     lmax = q;
   }
   // smallest eigenvalue: inverse iteration, x <- A^{-1} x by forward and back substitution
+#pragma unroll
   for (int i = 0; i < K; ++i) x[i] = (i & 1) ? -1.0 : 1.0 + 0.05 * i;
   double lmin = INFINITY;
+#pragma unroll 1
   for (int it = 0; it < 8; ++it) {
     double nx = 0.0;
+#pragma unroll
     for (int i = 0; i < K; ++i) nx += x[i] * x[i];
     nx = 1.0 / sqrt(nx);
+#pragma unroll
     for (int i = 0; i < K; ++i) x[i] *= nx;
+#pragma unroll
     for (int i = 0; i < K; ++i) {   // L y = x
       double s = x[i];
-      for (int k = 0; k < i; ++k) s -= L[i * K + k] * y[k];
-      y[i] = s / L[i * K + i];
+#pragma unroll
+      for (int k = 0; k < i; ++k) s -= L[T(i, k)] * y[k];
+      y[i] = s * il[i];
     }
     double q = 0.0;                 // x^T A^{-1} x = |y|^2
+#pragma unroll
     for (int i = 0; i < K; ++i) q += y[i] * y[i];
+#pragma unroll
     for (int i = K - 1; i >= 0; --i) {   // L^T x = y
       double s = y[i];
-      for (int k = i + 1; k < K; ++k) s -= L[k * K + i] * x[k];
-      x[i] = s / L[i * K + i];
+#pragma unroll
+      for (int k = i + 1; k < K; ++k) s -= L[T(k, i)] * x[k];
+      x[i] = s * il[i];
     }
     lmin = 1.0 / q;
   }
