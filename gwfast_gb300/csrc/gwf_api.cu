@@ -383,9 +383,10 @@ int ensure_aux(gwf_ctx* ctx, int n) {
 // GWF_PREC_MIXED, second stage: condition numbers of the FP32 network Fishers, then the FP64
 // Fisher of the events above the threshold, computed as a compact batch (the detectors side by side
 // on their own streams) and scattered back
+// recs[i]: where the first pass left detector i's FP64 set-up records for the whole batch, or null
 int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const double* dp, int64_t dld,
            const int* dres, int64_t N, int slots, double* darm, double* dnet, double* dsda, double* dsdn,
-           bool core_filled, cudaStream_t st) {
+           bool core_filled, const std::vector<const unsigned char*>& recs, cudaStream_t st) {
   const size_t per = (size_t)gwf::NP * gwf::NP;
   if (ctx->fcond.ensure((size_t)N * sizeof(double)) || ctx->mix_idx.ensure((size_t)N * sizeof(long long)) ||
       ctx->mix_cnt.ensure(sizeof(unsigned long long)))
@@ -451,6 +452,10 @@ int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const
     ai.stream = ctx->aux[i];
     GWF_CK(cudaStreamWaitEvent(ai.stream, ctx->fork, 0));
     ai.det = dev_of(r);
+    if (recs[i]) {   // copy the records of these events instead of recomputing them
+      ai.rec_src = recs[i];
+      ai.core_idx = idx;
+    }
     ai.scratch = (unsigned char*)ctx->mix_scr.p + (size_t)i * chunk * stride;
     ai.cap_events = chunk;
     ai.seg = seg;
@@ -704,6 +709,10 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   int slot = 0;
   bool first = true;
   if (side) GWF_CK(cudaEventRecord(ctx->fork, st));
+  // the mixed form's second stage reuses the FP64 set-up records of this pass when they all stay in
+  // the scratch until then: one chunk, and every group in its own scratch area
+  std::vector<const unsigned char*> recs(n_det, nullptr);
+  const bool keep_recs = precision == GWF_PREC_MIXED && fisher && N <= gwf::kChunk && (side || ngr == 1);
   int gi = 0;
   for (auto& grp : groups) {
     a.core = share ? (unsigned char*)ctx->core.p : nullptr;
@@ -732,6 +741,7 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
         g.wr[d] = (float)std::sqrt(g.det[0].psd_scale / g.det[d].psd_scale);
       }
       g.slice = 0;
+      for (int d = 0; keep_recs && d < g.nd; ++d) recs[grp[d]] = a.scratch + (size_t)d * chunk * stride;
       a.det = g.det[0];
       a.out_arm = nullptr;
       a.out_sd_arm = nullptr;
@@ -742,6 +752,7 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
       continue;
     }
     const DetRec& r = ctx->dets[det_ids[grp[0]]];
+    if (keep_recs) recs[grp[0]] = a.scratch;
     a.det = dev_of(r);
     a.out_arm = darm ? darm + (size_t)slot * N * per : nullptr;
     a.out_sd_arm = dsda ? dsda + (size_t)slot * N * npar : nullptr;
@@ -759,7 +770,7 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
     GWF_CK(gwf::launch_add_slices((const double*)ctx->gnet.p, ngr - 1, (long long)N * per, (long long)N * per, dnet, st));
   }
   if (precision == GWF_PREC_MIXED) {
-    rc = refine(ctx, n_det, det_ids, a, dp, dld, dres, N, slots, darm, dnet, dsda, dsdn, share, st);
+    rc = refine(ctx, n_det, det_ids, a, dp, dld, dres, N, slots, darm, dnet, dsda, dsdn, share, recs, st);
     if (rc) return rc;
   }
   if (!capturing) GWF_CK(cudaEventRecord(ctx->scratch_free, st));

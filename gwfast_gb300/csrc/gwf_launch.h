@@ -37,6 +37,10 @@ struct LaunchArgs {
   int core_mode = 0;                       // 0: none, 1: compute and store, 2: load
   const long long* core_idx = nullptr;     // cache row of each event of a gathered batch
   cudaEvent_t core_done = nullptr;         // recorded after each set-up that stores into the cache
+  // FP64 set-up records of this detector for the whole batch, left by an earlier pass of the same
+  // call (event n at rec_src + n * rec_stride): a gathered batch (core_idx) copies its rows from
+  // there instead of running the set-up again
+  const unsigned char* rec_src = nullptr;
 };
 
 cudaError_t launch_fisher_m0(const LaunchArgs& a);

@@ -16,6 +16,16 @@ constexpr int M = GWF_MODEL;
 
 unsigned char* scratch32_of(const LaunchArgs& a) { return a.scratch + (size_t)a.cap_events * rec_stride<M>(); }
 
+// set-up records idx[i] of src -> record i of dst, in 16-byte words (rec_stride is a multiple of 16)
+__global__ void copy_records_kernel(const uint4* __restrict__ src, const long long* __restrict__ idx, long long cnt,
+                                    uint4* __restrict__ dst) {
+  constexpr long long W = (long long)(rec_stride<M>() / 16);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= cnt * W) return;
+  const long long i = t / W;
+  dst[t] = src[idx[i] * W + (t - i * W)];
+}
+
 int sm_count() {
   int dev = 0, n = 0;
   cudaGetDevice(&dev);
@@ -30,7 +40,14 @@ cudaError_t chunked(const LaunchArgs& a, bool f32, MAIN main) {
     ev.n0 = n0;
     const long long cnt = (a.ev.N - n0) < kChunk ? (a.ev.N - n0) : kChunk;
     const unsigned nb = (unsigned)((cnt + 63) / 64);
-    setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, a.det, a.wf, a.qnm, a.nq, a.scratch, cnt, a.core, a.core_mode, a.core_idx);
+    if (a.rec_src && a.core_idx) {
+      const long long words = cnt * (long long)(rec_stride<M>() / 16);
+      copy_records_kernel<<<(unsigned)((words + 255) / 256), 256, 0, a.stream>>>(
+          reinterpret_cast<const uint4*>(a.rec_src), a.core_idx + n0, cnt, reinterpret_cast<uint4*>(a.scratch));
+    } else {
+      setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, a.det, a.wf, a.qnm, a.nq, a.scratch, cnt, a.core, a.core_mode,
+                                               a.core_idx);
+    }
     if (a.core_done && a.core_mode == 1) {
       const cudaError_t er = cudaEventRecord(a.core_done, a.stream);
       if (er != cudaSuccess) return er;

@@ -141,6 +141,20 @@ def test_mixed_all_refined_is_fp64(gpu_lib):
         assert entry_err(np.moveaxis(Fm[k], -1, 0), np.moveaxis(F64[k], -1, 0)).max() < 1e-12, k
 
 
+@pytest.mark.parametrize('model,dets,maker', [
+    ('IMRPhenomD', synthetic.NETWORK_LHET, synthetic.bbh_events),
+    ('TaylorF2_RestrictedPN', (('L1', 10.), ('H1', 10.), ('Virgo', 10.), ('ETS', 5.)), synthetic.bns_events)])
+def test_mixed_all_refined_grouped_network(gpu_lib, model, dets, maker):
+    """Network total only, so the detectors that share a grid run as one group (ETS beside them):
+    with every event refined, the FP64 stage starts from the FP64 set-up records that the FP32 pass
+    left in its scratch, and the result equals the FP64 kernel's up to summation order."""
+    ev = maker(300, seed=9)
+    net = synthetic.make_network(getattr(W, model)(), dets=dets, earth=True)
+    F64 = np.moveaxis(net.FisherMatr(dict(ev), res=1000), -1, 0)
+    Fm = np.moveaxis(net.FisherMatr(dict(ev), res=1000, precision='mixed', refine_cond=1.0), -1, 0)
+    assert entry_err(Fm, F64).max() < 1e-12
+
+
 def test_mixed_condition_estimate(gpu_lib):
     """The mixed form's condition-number estimate against the covariance kernel's (Jacobi) one."""
     ev = synthetic.bbh_events(400, seed=77)
