@@ -1,8 +1,8 @@
-// Launch sequences of one waveform model. Each of gwf_run_tf2.cu, gwf_run_phd.cu and
-// gwf_run_phm.cu defines GWF_MODEL and includes this file, so the three models compile as
-// separate translation units in parallel.
+// Launch sequences of one waveform model. Each gwf_run_*.cu (one per model id) defines GWF_MODEL
+// and includes this file, so the models compile as separate translation units in parallel.
 //
-// Per chunk of events: the per-event set-up kernel (FP64 records), for the FP32 form the FP32
+// Per chunk of events: the per-event set-up kernel (FP64 records; a gathered batch whose records
+// an earlier pass of the call left in scratch copies them instead), for the FP32 form the FP32
 // record kernel, then either the classic Fisher/SNR kernel (one CTA per event) or, when the
 // launch asks for segments, the segment scan, the persistent work-stealing Fisher kernel and the
 // per-event reduction of the segment partials.
