@@ -21,7 +21,8 @@ numpy 2 removed ``trapz`` and ``NaN`` and scipy removed ``cumtrapz``; aliases to
 ``trapezoid``/``nan``/``cumulative_trapezoid`` are installed for the reference's calls.
 
 The outputs are written to ``tests/golden/*.npz`` and committed; the GPU machine
-never needs the reference.  Run:  python tests/golden/make_golden.py [/root/reference]
+never needs the reference.  Run:  python tests/golden/make_golden.py [/root/reference] [part ...]
+(with parts, e.g. ``overlap``, only those ``make_<part>()`` run).
 """
 import os
 import sys
@@ -380,7 +381,45 @@ def make_fishertools_helpers():
     print('wrote fishertools_helpers')
 
 
+def make_overlap(res=300):
+    """WFOverlap (gwfast/signal.py:1759-1921 per detector with return_separate, network.py:198-227 for
+    the network): TaylorF2 against IMRPhenomD on the same BNS events, IMRPhenomD against itself with
+    shifted masses and spins on BBH events; L1 and the ET triangle with Earth rotation."""
+    dets = {'L1': (10., True), 'ETS': (5., True)}
+    out = {'res': np.array(res)}
+    ev_a = events_bns(np.random.default_rng(1010), 3)
+    ev_b = events_bbh(np.random.default_rng(1011), 3)
+    ev_b2 = dict(ev_b)
+    ev_b2['Mc'] = ev_b['Mc'] * (1. + 2e-4)
+    ev_b2['chi1z'] = ev_b['chi1z'] + 0.01
+    cases = (('tf2_phd', WF.TaylorF2_RestrictedPN(), WF.IMRPhenomD(), ev_a, dict(ev_a)),
+             ('phd_phd', WF.IMRPhenomD(), WF.IMRPhenomD(), ev_b, ev_b2))
+    for tag, wf1, wf2, ev1, ev2 in cases:
+        for k in KEYS:
+            out['%s_ev1_%s' % (tag, k)] = np.asarray(ev1[k], dtype=np.float64)
+            out['%s_ev2_%s' % (tag, k)] = np.asarray(ev2[k], dtype=np.float64)
+        sigs = {}
+        for dname, (fwall, earth) in dets.items():
+            d = glob.detectors[dname]
+            sigs[dname] = SIG.GWSignal(wf1, psd_path=psd_file(fwall), detector_shape=d['shape'], det_lat=d['lat'],
+                                       det_long=d['long'], det_xax=d['xax'], verbose=False, is_ASD=False,
+                                       useEarthMotion=earth, fmin=fwall)
+            ov, s1, s2 = sigs[dname].WFOverlap(wf1, wf2, dict(ev1), dict(ev2), res=res, return_separate=True)
+            out['%s_%s_ov' % (tag, dname)] = np.asarray(ov)
+            out['%s_%s_snr1' % (tag, dname)] = np.asarray(s1)
+            out['%s_%s_snr2' % (tag, dname)] = np.asarray(s2)
+        net = NET.DetNet(sigs, verbose=False)
+        out['%s_net' % tag] = np.asarray(net.WFOverlap(wf1, wf2, dict(ev1), dict(ev2), res=res))
+    np.savez_compressed(os.path.join(OUT, 'overlap_net_earth.npz'), **out)
+    print('wrote overlap_net_earth')
+
+
 def main():
+    only = sys.argv[2:]
+    if only:   # regenerate only the named parts: make_<part>()
+        for part in only:
+            globals()['make_' + part]()
+        return
     import gwfast.gwfastUtils as UT
     rng = np.random.default_rng(1000)
     make_case('tf2_L_noearth', WF.TaylorF2_RestrictedPN(), {'Virgo': (10., False)}, events_bns(rng, 4), 400)
@@ -452,6 +491,7 @@ def main():
     _FD['lam_h'] = None
     make_gw170817()
     make_fishertools_helpers()
+    make_overlap()
     # KAT from the reference tutorial: GW170817-like TF2 Schwarzschild cut frequency 1590.1 Hz
     z = 0.00980
     ev = {'Mc': np.array([1.1859 * (1. + z)]), 'eta': np.array([0.24786618323504223])}

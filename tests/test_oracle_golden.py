@@ -190,3 +190,23 @@ def test_kat_gw170817_oracle():
     for a in areas:
         assert abs(a - float(g['sky_area'][0])) < 2e-3 * a
         assert round(a, 1) == 19.9
+
+
+@pytest.mark.parametrize('tag,m1,m2', [('tf2_phd', 'TF2', 'PhenomD'), ('phd_phd', 'PhenomD', 'PhenomD')])
+def test_overlap_against_reference(tag, m1, m2):
+    """WFOverlap: the oracle's per-detector parts ((h1|h2) and the two SNRs, return_separate=True) and
+    the network overlap against gwfast's own (tests/golden/overlap_net_earth.npz)."""
+    g = np.load(os.path.join(GOLD, 'overlap_net_earth.npz'))
+    res = int(g['res'])
+    om1, om2 = O.Model(m1), O.Model(m2)
+    p1 = O.to_params({k: g['%s_ev1_%s' % (tag, k)] for k in O.PARAMS})
+    p2 = O.to_params({k: g['%s_ev2_%s' % (tag, k)] for k in O.PARAMS})
+    tot = [0., 0., 0.]
+    for name, fw in (('L1', 10.), ('ETS', 5.)):
+        ov, n1, n2 = (x.numpy().reshape(-1) for x in O.overlap_parts(det_of(name, fw, True), om1, p1, om2, p2, res))
+        assert rel(ov, g['%s_%s_ov' % (tag, name)]) < 1e-10, name
+        assert rel(np.sqrt(n1), g['%s_%s_snr1' % (tag, name)]) < 1e-12, name
+        assert rel(np.sqrt(n2), g['%s_%s_snr2' % (tag, name)]) < 1e-12, name
+        tot = [t + x for t, x in zip(tot, (ov, n1, n2))]
+    net = tot[0] / np.sqrt(tot[1] * tot[2])
+    assert rel(net, g['%s_net' % tag]) < 1e-10
