@@ -53,7 +53,8 @@ class DetNet:
         return_SNR_derivatives=True returns (allF, allDer) as gwfast: per-arm Fisher matrices and
         per-arm SNR-derivative integrals (11, N) keyed by detector (name_0..2 for triangles), plus
         'net': the Fisher total and dSNR/dtheta = sum of the integrals / network SNR (SNRs from
-        kwargs['SNRs'] if given)."""
+        kwargs['SNRs'] if given, else DetNet.SNR at its default resolution of 1000 points whatever
+        res the Fisher uses, as gwfast/network.py:139-143 calls it)."""
         utils.check_evparams(evParams)
         names, sigs = self._list()
         res = kwargs.get('res', 1000)
@@ -90,8 +91,8 @@ class DetNet:
                 for i, k in enumerate(keys):
                     allF[k] = np.moveaxis(Fa[i], 0, -1)
                     allDer[k] = np.moveaxis(Da[i], 0, -1)
-            snrs = kwargs['SNRs'] if 'SNRs' in kwargs else self.SNR(evParams, res=res, precision='fp64' if precision ==
-                                                                    'fp64' else 'fp32')
+            snrs = kwargs['SNRs'] if 'SNRs' in kwargs else self.SNR(evParams, precision='fp64' if precision == 'fp64'
+                                                                    else 'fp32')
             allF['net'] = np.array([allF[k] for k in allF]).sum(axis=0)
             allDer['net'] = np.array([allDer[k] for k in allDer]).sum(axis=0) / snrs
             return allF, allDer

@@ -414,6 +414,40 @@ def make_overlap(res=300):
     print('wrote overlap_net_earth')
 
 
+def make_snr_derivs(res=300):
+    """DetNet.FisherMatr(return_SNR_derivatives=True) (gwfast/signal.py:938-945, :1016-1022,
+    :1090-1094; network.py:124-145): per arm 4 trapz(Re(h conj(dh/dtheta)) / S, f) and the network sum
+    divided by the network SNR, for TaylorF2 on the ET triangle with rotation and Virgo without. The
+    derivatives are the finite-difference stand-in's. gwfast passes its complex128 parameters to
+    GWstrain unchanged on this path, where IMRPhenomD calls np.fabs, which numpy refuses for complex
+    input: the IMR models are not run here."""
+    out = {'res': np.array(res)}
+    cases = (('tf2', WF.TaylorF2_RestrictedPN(), {'ETS': (5., True), 'Virgo': (10., False)},
+              events_bns(np.random.default_rng(1013), 3)),)
+    for tag, wf, dets, ev in cases:
+        for k in KEYS:
+            out['%s_ev_%s' % (tag, k)] = np.asarray(ev[k], dtype=np.float64)
+        sigs = {}
+        for dname, (fwall, earth) in dets.items():
+            d = glob.detectors[dname]
+            sigs[dname] = SIG.GWSignal(wf, psd_path=psd_file(fwall), detector_shape=d['shape'], det_lat=d['lat'],
+                                       det_long=d['long'], det_xax=d['xax'], verbose=False, is_ASD=False,
+                                       useEarthMotion=earth, fmin=fwall)
+        net = NET.DetNet(sigs, verbose=False)
+        snrs = net.SNR(dict(ev), res=res, return_all=True)
+        F, D = net.FisherMatr(dict(ev), res=res, return_SNR_derivatives=True)
+        for k in D:
+            out['%s_sd_%s' % (tag, k)] = np.asarray(D[k])
+            out['%s_fisher_%s' % (tag, k)] = np.asarray(F[k])
+        for k, v in snrs.items():
+            out['%s_snr_%s' % (tag, k)] = np.asarray(v)
+        # the 'net' entry is divided by DetNet.SNR at its default resolution (network.py:139-143
+        # passes no res), whatever res the Fisher used
+        out['%s_snr_default_res' % tag] = np.asarray(net.SNR(dict(ev)))
+    np.savez_compressed(os.path.join(OUT, 'snr_derivs.npz'), **out)
+    print('wrote snr_derivs')
+
+
 def main():
     only = sys.argv[2:]
     if only:   # regenerate only the named parts: make_<part>()
@@ -492,6 +526,7 @@ def main():
     make_gw170817()
     make_fishertools_helpers()
     make_overlap()
+    make_snr_derivs()
     # KAT from the reference tutorial: GW170817-like TF2 Schwarzschild cut frequency 1590.1 Hz
     z = 0.00980
     ev = {'Mc': np.array([1.1859 * (1. + z)]), 'eta': np.array([0.24786618323504223])}

@@ -192,7 +192,7 @@ def test_snr_derivatives(gpu_lib, model):
             worst = max(worst, np.max(np.abs(allDer[k] - r.numpy()) / scale))
     print('%s SNR derivatives: max normalised error %.2e' % (model, worst))
     assert worst < (F_TOL_HM if model == 'PhenomHM' else F_TOL)
-    snr_net = net.SNR(dict(ev), res=res)
+    snr_net = net.SNR(dict(ev))   # the divisor of the 'net' entry: DetNet.SNR at its default res, as gwfast
     d = allDer['net']
     assert np.allclose(d[2] * snr_net, -ev['dL'] * allF['net'][2, 2], rtol=1e-9)
     assert np.all(np.abs(d[8]) < 1e-9 * np.sqrt(np.einsum('iin->in', allF['net'])[8]))
