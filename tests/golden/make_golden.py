@@ -448,6 +448,29 @@ def make_snr_derivs(res=300):
     print('wrote snr_derivs')
 
 
+def make_derivs(res=200):
+    """DetNet.FisherMatr(return_derivatives=True) (gwfast/signal.py:913-916, :938-939, :1057;
+    network.py:124-137): per arm the (11, N, R) derivative arrays of the strain on the event grid
+    (tcoal row per second), TaylorF2 on the ET triangle with rotation and on Virgo without. The
+    intrinsic rows (Mc, eta, chi1z, chi2z) are the finite-difference stand-in's, the others gwfast's
+    closed forms."""
+    out = {'res': np.array(res)}
+    ev = events_bns(np.random.default_rng(1014), 3)
+    for k in KEYS:
+        out['ev_' + k] = np.asarray(ev[k], dtype=np.float64)
+    sigs = {}
+    for dname, (fwall, earth) in {'ETS': (5., True), 'Virgo': (10., False)}.items():
+        d = glob.detectors[dname]
+        sigs[dname] = SIG.GWSignal(WF.TaylorF2_RestrictedPN(), psd_path=psd_file(fwall), detector_shape=d['shape'],
+                                   det_lat=d['lat'], det_long=d['long'], det_xax=d['xax'], verbose=False, is_ASD=False,
+                                   useEarthMotion=earth, fmin=fwall)
+    F, D = NET.DetNet(sigs, verbose=False).FisherMatr(dict(ev), res=res, return_derivatives=True)
+    for k in D:
+        out['der_' + k] = np.asarray(D[k])
+    np.savez_compressed(os.path.join(OUT, 'derivs_tf2.npz'), **out)
+    print('wrote derivs_tf2')
+
+
 def main():
     only = sys.argv[2:]
     if only:   # regenerate only the named parts: make_<part>()
@@ -527,6 +550,7 @@ def main():
     make_fishertools_helpers()
     make_overlap()
     make_snr_derivs()
+    make_derivs()
     # KAT from the reference tutorial: GW170817-like TF2 Schwarzschild cut frequency 1590.1 Hz
     z = 0.00980
     ev = {'Mc': np.array([1.1859 * (1. + z)]), 'eta': np.array([0.24786618323504223])}
