@@ -381,6 +381,23 @@ def make_fishertools_helpers():
     print('wrote fishertools_helpers')
 
 
+def make_covariance():
+    """fisherTools.CovMatr with its defaults (gwfast/fisherTools.py:32-212: equilibrated Cholesky in
+    mpmath, inversion error) on the network Fisher matrices of the IMRPhenomD (11 x 11) and
+    IMRPhenomD_NRTidalv2 (13 x 13) golden cases."""
+    import gwfast.fisherTools as FT
+    out = {}
+    for tag, src in (('phd', 'phd_net_earth'), ('nrt', 'nrt_net_earth')):
+        g = np.load(os.path.join(OUT, src + '.npz'))
+        F = np.asarray(g['fisher_net'], dtype=np.float64)
+        cov, eps = FT.CovMatr(F)
+        out[tag + '_F'] = F
+        out[tag + '_cov'] = np.asarray(cov, dtype=np.float64)
+        out[tag + '_eps'] = np.asarray(eps, dtype=np.float64)
+    np.savez_compressed(os.path.join(OUT, 'covariance.npz'), **out)
+    print('wrote covariance')
+
+
 def make_overlap(res=300):
     """WFOverlap (gwfast/signal.py:1759-1921 per detector with return_separate, network.py:198-227 for
     the network): TaylorF2 against IMRPhenomD on the same BNS events, IMRPhenomD against itself with
@@ -548,6 +565,7 @@ def main():
     _FD['lam_h'] = None
     make_gw170817()
     make_fishertools_helpers()
+    make_covariance()
     make_overlap()
     make_snr_derivs()
     make_derivs()
