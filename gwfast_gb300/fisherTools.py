@@ -51,11 +51,37 @@ def compute_inversion_error(Fisher, Cov):
 
 
 def CheckFisher(FisherM, condNumbMax=1.0e15, use_mpmath=True, verbose=False):
-    """Eigenvalues, eigenvectors and condition numbers (gwfast/fisherTools.py:216-279), float64 on the host."""
-    evals, evecs = np.linalg.eigh(np.moveaxis(FisherM, -1, 0))
+    """Eigenvalues (N, P), eigenvectors (N, P, P) and condition numbers (N,) of (P, P, N) Fisher
+    matrices (gwfast/fisherTools.py:216-279). The decomposition is LAPACK's in float64 on the host
+    (use_mpmath is accepted for the signature: gwfast's mpmath eigh runs at its default 53-bit
+    precision too). As there, an all-NaN matrix gives NaN rows, a matrix whose decomposition fails
+    gives NaN rows, and negative eigenvalues are reported."""
+    F = np.moveaxis(np.asarray(FisherM, dtype=np.float64), -1, 0)
+    evals = np.full(F.shape[:2], np.nan)
+    evecs = np.full(F.shape, np.nan)
+    ok = ~np.all(np.isnan(F), axis=(1, 2))
+    if verbose:
+        for k in np.where(~ok)[0]:
+            print('Fisher is nan at position %s. ' % k)
+    idx = np.where(ok)[0]
+    try:
+        if idx.size:
+            evals[idx], evecs[idx] = np.linalg.eigh(F[idx])
+    except np.linalg.LinAlgError:
+        for k in idx:
+            try:
+                evals[k], evecs[k] = np.linalg.eigh(F[k])
+            except np.linalg.LinAlgError as e:
+                print(e)
+                print('Event is number %s' % k)
+    if np.any(evals <= 0.):
+        print('WARNING: one or more eigenvalues are negative at position(s) %s' % str(np.unique(np.where(evals < 0)[0])))
     cond = np.abs(evals).max(axis=1) / np.abs(evals).min(axis=1)
-    if verbose and np.any(cond > condNumbMax):
-        print('WARNING: the condition number is too large at positions %s' % np.where(cond > condNumbMax)[0])
+    if np.any(cond > condNumbMax) and verbose:
+        print('WARNING: the condition number is too large (%s>%s)' % (cond, condNumbMax))
+        print('Unreliable covariance at positions ' + str(cond > condNumbMax))
+    elif verbose:
+        print('Condition number= %s . Ok. ' % cond)
     return evals, evecs, cond
 
 

@@ -383,8 +383,8 @@ def make_fishertools_helpers():
 
 def make_covariance():
     """fisherTools.CovMatr with its defaults (gwfast/fisherTools.py:32-212: equilibrated Cholesky in
-    mpmath, inversion error) on the network Fisher matrices of the IMRPhenomD (11 x 11) and
-    IMRPhenomD_NRTidalv2 (13 x 13) golden cases."""
+    mpmath, inversion error) and CheckFisher (:216-279, mpmath eigh) on the network Fisher matrices
+    of the IMRPhenomD (11 x 11) and IMRPhenomD_NRTidalv2 (13 x 13) golden cases."""
     import gwfast.fisherTools as FT
     out = {}
     for tag, src in (('phd', 'phd_net_earth'), ('nrt', 'nrt_net_earth')):
@@ -394,6 +394,9 @@ def make_covariance():
         out[tag + '_F'] = F
         out[tag + '_cov'] = np.asarray(cov, dtype=np.float64)
         out[tag + '_eps'] = np.asarray(eps, dtype=np.float64)
+        ev_, _, cond = FT.CheckFisher(F)
+        out[tag + '_evals'] = np.asarray(ev_, dtype=np.float64)
+        out[tag + '_cond'] = np.asarray(cond, dtype=np.float64)
     np.savez_compressed(os.path.join(OUT, 'covariance.npz'), **out)
     print('wrote covariance')
 

@@ -221,3 +221,27 @@ def test_fishertools_helpers_against_gwfast():
     close(np.array(FT.m1m2_from_Mceta(e0['Mc'], e0['eta'])), g['m1m2'])
     Mc, eta = FT.Mceta_from_m1m2(*g['m1m2'])
     close(np.array([Mc, eta]), np.array([e0['Mc'], e0['eta']]))
+
+
+def test_check_fisher_against_gwfast(capsys):
+    """fisherTools.CheckFisher against gwfast's own (mpmath eigh, tests/golden/covariance.npz): the
+    eigenvalues agree to 1e-14 of the largest; the condition numbers, whose smallest eigenvalue is
+    only as good as 1e-16 of the largest, within 1e-15 cond for the IMRPhenomD matrices (cond up to
+    1e12; the 13 x 13 ones sit at 1e16, at the rounding floor, where gwfast itself reports negative
+    eigenvalues, as does this one). An all-NaN matrix gives NaN rows, as there."""
+    import os
+    from gwfast_gb300 import fisherTools as FT
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden', 'covariance.npz'))
+    for tag in ('phd', 'nrt'):
+        ev, vec, cond = FT.CheckFisher(g[tag + '_F'])
+        er = g[tag + '_evals']
+        assert ev.shape == er.shape and vec.shape == (ev.shape[0],) + ev.shape[1:] * 2
+        assert np.all(np.abs(ev - er).max(axis=1) <= 1e-14 * np.abs(er).max(axis=1)), tag
+        if tag == 'phd':
+            assert np.all(np.abs(cond / g['phd_cond'] - 1.) <= 1e-15 * g['phd_cond'])
+    F = g['phd_F'].copy()
+    F[:, :, 1] = np.nan
+    ev, vec, cond = FT.CheckFisher(F, verbose=True)
+    assert np.all(np.isnan(ev[1])) and np.all(np.isnan(vec[1])) and np.isnan(cond[1])
+    assert np.all(np.isfinite(cond[[0, 2, 3]]))
+    assert 'Fisher is nan at position 1' in capsys.readouterr().out
