@@ -437,15 +437,21 @@ def make_overlap(res=300):
 def make_snr_derivs(res=300):
     """DetNet.FisherMatr(return_SNR_derivatives=True) (gwfast/signal.py:938-945, :1016-1022,
     :1090-1094; network.py:124-145): per arm 4 trapz(Re(h conj(dh/dtheta)) / S, f) and the network sum
-    divided by the network SNR, for TaylorF2 on the ET triangle with rotation and Virgo without. The
-    derivatives are the finite-difference stand-in's. gwfast passes its complex128 parameters to
-    GWstrain unchanged on this path, where IMRPhenomD calls np.fabs, which numpy refuses for complex
-    input: the IMR models are not run here."""
+    divided by the network SNR, for TaylorF2 on the ET triangle with rotation and Virgo without, and
+    tidal eccentric TaylorF2 (14 parameters) on ET. The derivatives are the finite-difference
+    stand-in's. gwfast passes its complex128 parameters to GWstrain unchanged on this path, where
+    IMRPhenomD calls np.fabs, which numpy refuses for complex input: the IMR models are not run here."""
+    import gwfast.gwfastUtils as UT
     out = {'res': np.array(res)}
+    evt = events_bns(np.random.default_rng(1015), 3)
+    evt['Lambda1'], evt['Lambda2'] = np.array([300., 900., 150.]), np.array([500., 200., 700.])
+    evt['LambdaTilde'], evt['deltaLambda'] = UT.Lamt_delLam_from_Lam12(evt['Lambda1'], evt['Lambda2'], evt['eta'])
+    evt['ecc'] = np.array([0.02, 0.1, 0.05])
     cases = (('tf2', WF.TaylorF2_RestrictedPN(), {'ETS': (5., True), 'Virgo': (10., False)},
-              events_bns(np.random.default_rng(1013), 3)),)
+              events_bns(np.random.default_rng(1013), 3)),
+             ('tf2te', WF.TaylorF2_RestrictedPN(is_tidal=True, is_eccentric=True), {'ETS': (5., True)}, evt))
     for tag, wf, dets, ev in cases:
-        for k in KEYS:
+        for k in KEYS + (('Lambda1', 'Lambda2', 'LambdaTilde', 'deltaLambda', 'ecc') if wf.is_tidal else ()):
             out['%s_ev_%s' % (tag, k)] = np.asarray(ev[k], dtype=np.float64)
         sigs = {}
         for dname, (fwall, earth) in dets.items():

@@ -212,35 +212,39 @@ def test_overlap_against_reference(tag, m1, m2):
     assert rel(net, g['%s_net' % tag]) < 1e-10
 
 
-def test_snr_derivatives_against_reference():
+@pytest.mark.parametrize('tag,model,dets', [
+    ('tf2', O.Model('TF2'), (('ETS', 5., True), ('Virgo', 10., False))),
+    ('tf2te', O.Model('TF2', tidal=True, ecc=True), (('ETS', 5., True),))])
+def test_snr_derivatives_against_reference(tag, model, dets):
     """return_SNR_derivatives: the oracle's per-arm 4 trapz(Re(h conj(dh/dtheta)) / S, f) and the
-    network sum over the network SNR against gwfast's own (tests/golden/snr_derivs.npz: TaylorF2,
-    ET triangle with rotation and Virgo without). gwfast's derivatives there are the golden
-    generator's finite differences; measured against the Cauchy-Schwarz scale sqrt(F_aa) SNR_arm
-    (which bounds |dS_a|) the two agree to ~4e-10, and the bound is 1e-8 of it. (Entries that vanish
-    in exact arithmetic, such as the Phicoal row, Re(h conj(-i h)) = 0, differ by rounding only.)"""
+    network sum over the network SNR against gwfast's own (tests/golden/snr_derivs.npz: TaylorF2 on
+    ET with rotation and Virgo without; tidal eccentric TaylorF2, 14 parameters, on ET). gwfast's
+    derivatives there are the golden generator's finite differences; measured against the
+    Cauchy-Schwarz scale sqrt(F_aa) SNR_arm (which bounds |dS_a|) the two agree to ~4e-10, and the
+    bound is 1e-8 of it. (Entries that vanish in exact arithmetic, such as the Phicoal row,
+    Re(h conj(-i h)) = 0, differ by rounding only.)"""
     g = np.load(os.path.join(GOLD, 'snr_derivs.npz'))
     res = int(g['res'])
-    model = O.Model('TF2')
-    p = O.to_params({k: g['tf2_ev_' + k] for k in O.PARAMS})
+    p = O.to_params({k: g['%s_ev_%s' % (tag, k)] for k in model.params}, model.params)
     tot = 0.
-    for name, fw, earth in (('ETS', 5., True), ('Virgo', 10., False)):
+    for name, fw, earth in dets:
         arms = O.snr_derivs_arms(det_of(name, fw, earth), model, p, res)
         keys = [name] if len(arms) == 1 else ['%s_%d' % (name, i) for i in range(3)]
         for k, a in zip(keys, arms):
             a = a.numpy()
-            ref = g['tf2_sd_' + k]
-            scale = np.sqrt(np.einsum('iin->in', g['tf2_fisher_' + k])) * g['tf2_snr_' + k][None]
+            ref = g['%s_sd_%s' % (tag, k)]
+            assert a.shape == ref.shape == (len(model.params), ref.shape[1]), k
+            scale = np.sqrt(np.einsum('iin->in', g['%s_fisher_%s' % (tag, k)])) * g['%s_snr_%s' % (tag, k)][None]
             assert np.all(np.abs(a - ref) <= 1e-8 * scale), k
             tot = tot + a
     # gwfast divides the network entry by DetNet.SNR at its default resolution (1000 points), not at
     # the Fisher's res
-    snr_def = g['tf2_snr_default_res']
-    dets = [det_of('ETS', 5., True), det_of('Virgo', 10., False)]
-    assert rel(O.network_snr(dets, model, p, 1000).numpy(), snr_def) < 1e-12
+    snr_def = g[tag + '_snr_default_res']
+    odets = [det_of(n, fw, e) for n, fw, e in dets]
+    assert rel(O.network_snr(odets, model, p, 1000).numpy(), snr_def) < 1e-12
     net = tot / snr_def
-    scale = np.sqrt(np.einsum('iin->in', g['tf2_fisher_net']))
-    assert np.all(np.abs(net - g['tf2_sd_net']) <= 1e-8 * scale)
+    scale = np.sqrt(np.einsum('iin->in', g[tag + '_fisher_net']))
+    assert np.all(np.abs(net - g[tag + '_sd_net']) <= 1e-8 * scale)
 
 
 def test_strain_derivative_arrays_against_reference():
