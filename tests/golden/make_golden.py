@@ -476,23 +476,31 @@ def make_snr_derivs(res=300):
 
 def make_derivs(res=200):
     """DetNet.FisherMatr(return_derivatives=True) (gwfast/signal.py:913-916, :938-939, :1057;
-    network.py:124-137): per arm the (11, N, R) derivative arrays of the strain on the event grid
-    (tcoal row per second), TaylorF2 on the ET triangle with rotation and on Virgo without. The
-    intrinsic rows (Mc, eta, chi1z, chi2z) are the finite-difference stand-in's, the others gwfast's
-    closed forms."""
+    network.py:124-137): per arm the (P, N, R) derivative arrays of the strain on the event grid
+    (tcoal row per second), TaylorF2 on the ET triangle with rotation and on Virgo without, and
+    tidal eccentric TaylorF2 (14 parameters) on ET. The intrinsic rows (Mc, eta, chi1z, chi2z and the
+    tidal and ecc rows) are the finite-difference stand-in's, the others gwfast's closed forms."""
+    import gwfast.gwfastUtils as UT
     out = {'res': np.array(res)}
-    ev = events_bns(np.random.default_rng(1014), 3)
-    for k in KEYS:
-        out['ev_' + k] = np.asarray(ev[k], dtype=np.float64)
-    sigs = {}
-    for dname, (fwall, earth) in {'ETS': (5., True), 'Virgo': (10., False)}.items():
-        d = glob.detectors[dname]
-        sigs[dname] = SIG.GWSignal(WF.TaylorF2_RestrictedPN(), psd_path=psd_file(fwall), detector_shape=d['shape'],
-                                   det_lat=d['lat'], det_long=d['long'], det_xax=d['xax'], verbose=False, is_ASD=False,
-                                   useEarthMotion=earth, fmin=fwall)
-    F, D = NET.DetNet(sigs, verbose=False).FisherMatr(dict(ev), res=res, return_derivatives=True)
-    for k in D:
-        out['der_' + k] = np.asarray(D[k])
+    evt = events_bns(np.random.default_rng(1016), 3)
+    evt['Lambda1'], evt['Lambda2'] = np.array([400., 800., 250.]), np.array([600., 300., 900.])
+    evt['LambdaTilde'], evt['deltaLambda'] = UT.Lamt_delLam_from_Lam12(evt['Lambda1'], evt['Lambda2'], evt['eta'])
+    evt['ecc'] = np.array([0.03, 0.08, 0.12])
+    cases = (('', WF.TaylorF2_RestrictedPN(), {'ETS': (5., True), 'Virgo': (10., False)},
+              events_bns(np.random.default_rng(1014), 3)),
+             ('te_', WF.TaylorF2_RestrictedPN(is_tidal=True, is_eccentric=True), {'ETS': (5., True)}, evt))
+    for pre, wf, dets, ev in cases:
+        for k in KEYS + (('Lambda1', 'Lambda2', 'LambdaTilde', 'deltaLambda', 'ecc') if wf.is_tidal else ()):
+            out[pre + 'ev_' + k] = np.asarray(ev[k], dtype=np.float64)
+        sigs = {}
+        for dname, (fwall, earth) in dets.items():
+            d = glob.detectors[dname]
+            sigs[dname] = SIG.GWSignal(wf, psd_path=psd_file(fwall), detector_shape=d['shape'], det_lat=d['lat'],
+                                       det_long=d['long'], det_xax=d['xax'], verbose=False, is_ASD=False,
+                                       useEarthMotion=earth, fmin=fwall)
+        F, D = NET.DetNet(sigs, verbose=False).FisherMatr(dict(ev), res=res, return_derivatives=True)
+        for k in D:
+            out[pre + 'der_' + k] = np.asarray(D[k])
     np.savez_compressed(os.path.join(OUT, 'derivs_tf2.npz'), **out)
     print('wrote derivs_tf2')
 

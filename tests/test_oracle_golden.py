@@ -247,23 +247,31 @@ def test_snr_derivatives_against_reference(tag, model, dets):
     assert np.all(np.abs(net - g[tag + '_sd_net']) <= 1e-8 * scale)
 
 
-def test_strain_derivative_arrays_against_reference():
-    """return_derivatives: the oracle's per-arm (11, N, R) derivative arrays (tcoal row per second,
+@pytest.mark.parametrize('pre,model,dets', [
+    ('', O.Model('TF2'), (('ETS', 5., True), ('Virgo', 10., False))),
+    ('te_', O.Model('TF2', tidal=True, ecc=True), (('ETS', 5., True),))], ids=['tf2', 'tf2_tidal_ecc'])
+def test_strain_derivative_arrays_against_reference(pre, model, dets):
+    """return_derivatives: the oracle's per-arm (P, N, R) derivative arrays (tcoal row per second,
     triangle arms 0, 60 degrees and minus their sum) against gwfast's own (tests/golden/derivs_tf2.npz:
-    TaylorF2, ET with rotation and Virgo without). Per (arm, parameter, event) row, relative to the
-    row's maximum: the closed-form rows agree to ~1e-8 (bound 1e-7); the intrinsic rows are the
-    generator's finite differences, ~1e-5 at worst (bound 5e-5)."""
+    TaylorF2 on ET with rotation and Virgo without; tidal eccentric TaylorF2, 14 parameters, on ET).
+    Per (arm, parameter, event) row, relative to the row's maximum: the closed-form rows agree to
+    ~1e-8 (bound 3e-7); the intrinsic rows are the generator's finite differences, ~1e-5 at worst
+    (bound 5e-5), deltaLambda's (a step of 10) ~6e-5 (bound 2e-4)."""
     g = np.load(os.path.join(GOLD, 'derivs_tf2.npz'))
     res = int(g['res'])
-    p = O.to_params({k: g['ev_' + k] for k in O.PARAMS})
-    tol = np.full(11, 1e-7)
+    p = O.to_params({k: g[pre + 'ev_' + k] for k in model.params}, model.params)
+    P = len(model.params)
+    tol = np.full(P, 3e-7)
     tol[[0, 1, 9, 10]] = 5e-5   # Mc, eta, chi1z, chi2z
-    for name, fw, earth in (('ETS', 5., True), ('Virgo', 10., False)):
-        arms = O.strain_derivs_arms(det_of(name, fw, earth), O.Model('TF2'), p, res)
+    tol[11:] = 5e-5             # LambdaTilde, deltaLambda, ecc
+    if model.tidal:
+        tol[12] = 2e-4
+    for name, fw, earth in dets:
+        arms = O.strain_derivs_arms(det_of(name, fw, earth), model, p, res)
         keys = [name] if len(arms) == 1 else ['%s_%d' % (name, i) for i in range(3)]
         for k, a in zip(keys, arms):
-            r = g['der_' + k]
-            assert a.shape == r.shape, k
+            r = g[pre + 'der_' + k]
+            assert a.shape == r.shape and r.shape[0] == P, k
             e = np.abs(a.numpy() - r).max(axis=2) / np.abs(r).max(axis=2)
             assert np.all(e.max(axis=1) < tol), (k, e.max(axis=1))
 
