@@ -412,10 +412,16 @@ def make_overlap(res=300):
     ev_b2 = dict(ev_b)
     ev_b2['Mc'] = ev_b['Mc'] * (1. + 2e-4)
     ev_b2['chi1z'] = ev_b['chi1z'] + 0.01
+    import gwfast.gwfastUtils as UT
+    ev_c = events_bns(np.random.default_rng(1017), 3)
+    ev_c['chi1z'], ev_c['chi2z'] = np.array([0.2, -0.1, 0.05]), np.array([-0.15, 0.25, 0.1])
+    ev_c['Lambda1'], ev_c['Lambda2'] = np.array([400., 900., 200.]), np.array([700., 300., 1100.])
+    ev_c['LambdaTilde'], ev_c['deltaLambda'] = UT.Lamt_delLam_from_Lam12(ev_c['Lambda1'], ev_c['Lambda2'], ev_c['eta'])
     cases = (('tf2_phd', WF.TaylorF2_RestrictedPN(), WF.IMRPhenomD(), ev_a, dict(ev_a)),
-             ('phd_phd', WF.IMRPhenomD(), WF.IMRPhenomD(), ev_b, ev_b2))
+             ('phd_phd', WF.IMRPhenomD(), WF.IMRPhenomD(), ev_b, ev_b2),
+             ('nrt_tf2t', WF.IMRPhenomD_NRTidalv2(), WF.TaylorF2_RestrictedPN(is_tidal=True), ev_c, dict(ev_c)))
     for tag, wf1, wf2, ev1, ev2 in cases:
-        for k in KEYS:
+        for k in KEYS + (('Lambda1', 'Lambda2', 'LambdaTilde', 'deltaLambda') if wf1.is_tidal else ()):
             out['%s_ev1_%s' % (tag, k)] = np.asarray(ev1[k], dtype=np.float64)
             out['%s_ev2_%s' % (tag, k)] = np.asarray(ev2[k], dtype=np.float64)
         sigs = {}

@@ -192,24 +192,41 @@ def test_kat_gw170817_oracle():
         assert round(a, 1) == 19.9
 
 
-@pytest.mark.parametrize('tag,m1,m2', [('tf2_phd', 'TF2', 'PhenomD'), ('phd_phd', 'PhenomD', 'PhenomD')])
-def test_overlap_against_reference(tag, m1, m2):
+def _overlap_models(tag, last):
+    if tag == 'nrt_tf2t':
+        return O.Model('PhenomD_NRTidalv2', taper_last=np.full((1,), last)), O.Model('TF2', tidal=True)
+    names = {'tf2_phd': ('TF2', 'PhenomD'), 'phd_phd': ('PhenomD', 'PhenomD')}[tag]
+    return O.Model(names[0]), O.Model(names[1])
+
+
+@pytest.mark.parametrize('tag', ['tf2_phd', 'phd_phd', 'nrt_tf2t'])
+def test_overlap_against_reference(tag):
     """WFOverlap: the oracle's per-detector parts ((h1|h2) and the two SNRs, return_separate=True) and
-    the network overlap against gwfast's own (tests/golden/overlap_net_earth.npz)."""
+    the network overlap against gwfast's own (tests/golden/overlap_net_earth.npz): TaylorF2 against
+    IMRPhenomD, IMRPhenomD against itself with shifted masses and spins, IMRPhenomD_NRTidalv2 against
+    tidal TaylorF2. In the last, the grid ends on IMRPhenomD_NRTidalv2's cut, where its Planck taper
+    is 0 or 1 by the last bit, so each event is compared with the oracle taken both ways."""
     g = np.load(os.path.join(GOLD, 'overlap_net_earth.npz'))
     res = int(g['res'])
-    om1, om2 = O.Model(m1), O.Model(m2)
-    p1 = O.to_params({k: g['%s_ev1_%s' % (tag, k)] for k in O.PARAMS})
-    p2 = O.to_params({k: g['%s_ev2_%s' % (tag, k)] for k in O.PARAMS})
-    tot = [0., 0., 0.]
-    for name, fw in (('L1', 10.), ('ETS', 5.)):
-        ov, n1, n2 = (x.numpy().reshape(-1) for x in O.overlap_parts(det_of(name, fw, True), om1, p1, om2, p2, res))
-        assert rel(ov, g['%s_%s_ov' % (tag, name)]) < 1e-10, name
-        assert rel(np.sqrt(n1), g['%s_%s_snr1' % (tag, name)]) < 1e-12, name
-        assert rel(np.sqrt(n2), g['%s_%s_snr2' % (tag, name)]) < 1e-12, name
-        tot = [t + x for t, x in zip(tot, (ov, n1, n2))]
-    net = tot[0] / np.sqrt(tot[1] * tot[2])
-    assert rel(net, g['%s_net' % tag]) < 1e-10
+    lasts = (False, True) if tag == 'nrt_tf2t' else (None,)
+    errs = []
+    for last in lasts:
+        om1, om2 = _overlap_models(tag, last)
+        p1 = O.to_params({k: g['%s_ev1_%s' % (tag, k)] for k in om1.params}, om1.params)
+        p2 = O.to_params({k: g['%s_ev2_%s' % (tag, k)] for k in om2.params}, om2.params)
+        tot = [0., 0., 0.]
+        e = 0.
+        for name, fw in (('L1', 10.), ('ETS', 5.)):
+            ov, n1, n2 = (x.numpy().reshape(-1) for x in O.overlap_parts(det_of(name, fw, True), om1, p1, om2, p2,
+                                                                         res))
+            ref = [g['%s_%s_%s' % (tag, name, q)] for q in ('ov', 'snr1', 'snr2')]
+            e = np.maximum(e, np.abs(ov - ref[0]) / np.abs(ref[0]).max())
+            e = np.maximum(e, np.abs(np.sqrt(n1) / ref[1] - 1.))
+            e = np.maximum(e, np.abs(np.sqrt(n2) / ref[2] - 1.))
+            tot = [t + x for t, x in zip(tot, (ov, n1, n2))]
+        net = tot[0] / np.sqrt(tot[1] * tot[2])
+        errs.append(np.maximum(e, np.abs(net - g['%s_net' % tag]) / np.abs(g['%s_net' % tag]).max()))
+    assert np.all(np.min(errs, axis=0) < 1e-10), errs
 
 
 @pytest.mark.parametrize('tag,model,dets', [
