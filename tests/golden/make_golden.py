@@ -417,9 +417,16 @@ def make_overlap(res=300):
     ev_c['chi1z'], ev_c['chi2z'] = np.array([0.2, -0.1, 0.05]), np.array([-0.15, 0.25, 0.1])
     ev_c['Lambda1'], ev_c['Lambda2'] = np.array([400., 900., 200.]), np.array([700., 300., 1100.])
     ev_c['LambdaTilde'], ev_c['deltaLambda'] = UT.Lamt_delLam_from_Lam12(ev_c['Lambda1'], ev_c['Lambda2'], ev_c['eta'])
+    m1, m2 = np.array([6., 9., 12.]), np.array([1.35, 1.5, 1.4])
+    ev_d = {'Mc': (m1 * m2) ** 0.6 / (m1 + m2) ** 0.2, 'eta': m1 * m2 / (m1 + m2) ** 2,
+            'chi1z': np.array([0.5, -0.2, 0.1]), 'chi2z': np.zeros(3), 'dL': np.array([0.1, 0.2, 0.15])}
+    ev_d = _angles(np.random.default_rng(1018), 3, ev_d)
+    ev_d['Lambda1'], ev_d['Lambda2'] = np.zeros(3), np.array([1200., 500., 300.])
+    ev_d['LambdaTilde'], ev_d['deltaLambda'] = UT.Lamt_delLam_from_Lam12(ev_d['Lambda1'], ev_d['Lambda2'], ev_d['eta'])
     cases = (('tf2_phd', WF.TaylorF2_RestrictedPN(), WF.IMRPhenomD(), ev_a, dict(ev_a)),
              ('phd_phd', WF.IMRPhenomD(), WF.IMRPhenomD(), ev_b, ev_b2),
-             ('nrt_tf2t', WF.IMRPhenomD_NRTidalv2(), WF.TaylorF2_RestrictedPN(is_tidal=True), ev_c, dict(ev_c)))
+             ('nrt_tf2t', WF.IMRPhenomD_NRTidalv2(), WF.TaylorF2_RestrictedPN(is_tidal=True), ev_c, dict(ev_c)),
+             ('nsbh_phd', WF.IMRPhenomNSBH(verbose=False), WF.IMRPhenomD(), ev_d, dict(ev_d)))
     for tag, wf1, wf2, ev1, ev2 in cases:
         for k in KEYS + (('Lambda1', 'Lambda2', 'LambdaTilde', 'deltaLambda') if wf1.is_tidal else ()):
             out['%s_ev1_%s' % (tag, k)] = np.asarray(ev1[k], dtype=np.float64)
