@@ -423,10 +423,12 @@ def make_overlap(res=300):
     ev_d = _angles(np.random.default_rng(1018), 3, ev_d)
     ev_d['Lambda1'], ev_d['Lambda2'] = np.zeros(3), np.array([1200., 500., 300.])
     ev_d['LambdaTilde'], ev_d['deltaLambda'] = UT.Lamt_delLam_from_Lam12(ev_d['Lambda1'], ev_d['Lambda2'], ev_d['eta'])
+    ev_e = events_bbh(np.random.default_rng(1019), 3, mmax=150., qmin=0.1, chimax=0.9)
     cases = (('tf2_phd', WF.TaylorF2_RestrictedPN(), WF.IMRPhenomD(), ev_a, dict(ev_a)),
              ('phd_phd', WF.IMRPhenomD(), WF.IMRPhenomD(), ev_b, ev_b2),
              ('nrt_tf2t', WF.IMRPhenomD_NRTidalv2(), WF.TaylorF2_RestrictedPN(is_tidal=True), ev_c, dict(ev_c)),
-             ('nsbh_phd', WF.IMRPhenomNSBH(verbose=False), WF.IMRPhenomD(), ev_d, dict(ev_d)))
+             ('nsbh_phd', WF.IMRPhenomNSBH(verbose=False), WF.IMRPhenomD(), ev_d, dict(ev_d)),
+             ('phm_phd', WF.IMRPhenomHM(), WF.IMRPhenomD(), ev_e, dict(ev_e)))
     for tag, wf1, wf2, ev1, ev2 in cases:
         for k in KEYS + (('Lambda1', 'Lambda2', 'LambdaTilde', 'deltaLambda') if wf1.is_tidal else ()):
             out['%s_ev1_%s' % (tag, k)] = np.asarray(ev1[k], dtype=np.float64)

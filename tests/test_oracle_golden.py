@@ -197,16 +197,17 @@ def _overlap_models(tag, last):
         return O.Model('PhenomD_NRTidalv2', taper_last=np.full((1,), last)), O.Model('TF2', tidal=True)
     if tag == 'nsbh_phd':
         return O.Model('PhenomNSBH', cut_last=np.full((1,), last)), O.Model('PhenomD')
-    names = {'tf2_phd': ('TF2', 'PhenomD'), 'phd_phd': ('PhenomD', 'PhenomD')}[tag]
+    names = {'tf2_phd': ('TF2', 'PhenomD'), 'phd_phd': ('PhenomD', 'PhenomD'), 'phm_phd': ('PhenomHM', 'PhenomD')}[tag]
     return O.Model(names[0]), O.Model(names[1])
 
 
-@pytest.mark.parametrize('tag', ['tf2_phd', 'phd_phd', 'nrt_tf2t', 'nsbh_phd'])
+@pytest.mark.parametrize('tag', ['tf2_phd', 'phd_phd', 'nrt_tf2t', 'nsbh_phd', 'phm_phd'])
 def test_overlap_against_reference(tag):
     """WFOverlap: the oracle's per-detector parts ((h1|h2) and the two SNRs, return_separate=True) and
     the network overlap against gwfast's own (tests/golden/overlap_net_earth.npz): TaylorF2 against
     IMRPhenomD, IMRPhenomD against itself with shifted masses and spins, IMRPhenomD_NRTidalv2 against
-    tidal TaylorF2, IMRPhenomNSBH against IMRPhenomD. In the last two the grid ends on a knife edge
+    tidal TaylorF2, IMRPhenomNSBH against IMRPhenomD, IMRPhenomHM against IMRPhenomD. With the two
+    tidal models the grid ends on a knife edge
     (the Planck taper's end, Mf = 0.2) that the last point falls on either side of by rounding, so
     each event is compared with the oracle taken both ways."""
     g = np.load(os.path.join(GOLD, 'overlap_net_earth.npz'))
