@@ -18,6 +18,7 @@ REarth = 6371.00                                            # km
 clight = 2.99792458e5                                       # km/s
 clightGpc = clight / 3.0856778570831e+22                    # Gpc/s
 f_isco = 1. / (np.sqrt(6.) * 6. * 2. * np.pi * GMsun_over_c3)
+siderealDay = 23.9344696                                    # hours
 
 detectors = {
     'L1': {'lat': 30.563, 'long': -90.774, 'xax': 242.71636956358617, 'shape': 'L'},

@@ -1,5 +1,9 @@
-"""Host-side helpers used on the hot path (gwfast/gwfastUtils.py:151-164, :450-482, :965-1020)."""
+"""Host-side helpers used on the hot path (gwfast/gwfastUtils.py:151-164, :450-482, :731-769, :965-1020)."""
+import datetime as _dt
+
 import numpy as np
+
+from . import gwfastGlobals as _glob
 
 
 def ra_dec_from_th_phi_rad(theta, phi):
@@ -25,17 +29,75 @@ def Mceta_from_m1m2(m1, m2):
     return Mc, eta
 
 
-def check_evparams(evParams):
-    """Fill the derived parameters in place, as gwfast/gwfastUtils.py:965-1020 does.
+# UTC dates at which a leap second took effect (published by the IERS); GPS - UTC is the number of
+# these at or before an instant (GPS time started at 1980-01-06 00:00:00 UTC, GPS - UTC = 0)
+_LEAP_DATES = ((1981, 7, 1), (1982, 7, 1), (1983, 7, 1), (1985, 7, 1), (1988, 1, 1), (1990, 1, 1), (1991, 1, 1),
+               (1992, 7, 1), (1993, 7, 1), (1994, 7, 1), (1996, 1, 1), (1997, 7, 1), (1999, 1, 1), (2006, 1, 1),
+               (2009, 1, 1), (2012, 7, 1), (2015, 7, 1), (2017, 1, 1))
+_GPS_EPOCH = _dt.date(1980, 1, 6)
+# GPS second of the leap second inserted before each date (the i leaps before it already counted)
+_LEAP_GPS = np.array([(_dt.date(*d) - _GPS_EPOCH).days * 86400 + i for i, d in enumerate(_LEAP_DATES)],
+                     dtype=np.float64)
+# 2000-01-01 12:00:00 on the GPS calendar, in GPS seconds (7300 days and 12 h after the GPS epoch)
+_GPS_NOON_J2000 = float((_dt.date(2000, 1, 1) - _GPS_EPOCH).days * 86400 + 43200)
+_TT_MINUS_GPS = 19.0 + 32.184   # TAI - GPS = 19 s, TT - TAI = 32.184 s
 
-    tcoal from tGPS needs a GMST conversion (astropy in gwfast); it is not provided
-    here, so a dict without tcoal raises the same ValueError as a dict without tGPS.
+
+def GPSt_to_J200t(t_GPS):
+    """Seconds since J2000 (gwfast/gwfastUtils.py:731-733, the same constant)."""
+    return t_GPS - 630763148.0
+
+
+def leap_seconds(t_GPS):
+    """GPS - UTC in seconds at GPS time(s) t_GPS (from the published leap-second dates)."""
+    return np.searchsorted(_LEAP_GPS, np.asarray(t_GPS, dtype=np.float64), side='right').astype(np.float64)
+
+
+def GPSt_to_GMST(t_GPS):
+    """Greenwich mean sidereal time as a fraction of a day, from GPS time (s).
+
+    gwfast calls astropy (``Time(t, format='gps').sidereal_time('mean')``, gwfast/gwfastUtils.py:735-755),
+    which evaluates the IAU 2006 GMST: the Earth rotation angle of UT1,
+    ERA = 2 pi (0.7790572732640 + 1.00273781191135448 Du), Du = JD(UT1) - 2451545.0, plus the precession
+    polynomial 0.014506" + 4612.156534" t + 1.3915817" t^2 - 0.00000044" t^3 - 0.000029956" t^4
+    - 0.0000000368" t^5 in TT Julian centuries t (Capitaine et al. 2003, A&A 412, 567; IERS Conventions
+    2010 eq. 5.32). This evaluates the same formula with UTC (GPS minus the leap seconds) standing in
+    for UT1: |UT1 - UTC| <= 0.9 s by the definition of UTC, so the result is within 1.05e-5 of a day of
+    astropy's value (0.34 s for GW170817, when UT1 - UTC was +0.34 s). Du is split into whole days and
+    the fraction so that the fraction keeps full precision.
     """
+    t = np.asarray(t_GPS, dtype=np.float64)
+    du = (t - leap_seconds(t) - _GPS_NOON_J2000) / 86400.
+    era = np.mod(np.mod(du, 1.0) + 0.7790572732640 + 0.00273781191135448 * du, 1.0)
+    T = (t + _TT_MINUS_GPS - _GPS_NOON_J2000) / 86400. / 36525.
+    arcsec = 0.014506 + T * (4612.156534 + T * (1.3915817 + T * (-0.00000044 + T * (-0.000029956 + T * (-0.0000000368)))))
+    return np.mod(era + arcsec / (3600. * 360.), 1.0)
+
+
+def GPSt_to_LMST(t_GPS, lat, long):
+    """Local mean sidereal time as a fraction of a day (gwfast/gwfastUtils.py:735-755): GMST plus the
+    longitude (deg). The latitude does not enter the mean sidereal time."""
+    del lat
+    return np.mod(GPSt_to_GMST(t_GPS) + np.asarray(long, dtype=np.float64) / 360., 1.0)
+
+
+def GPSt_to_GMST_alt(t_GPS):
+    """gwfast's approximate GMST (fraction of a day), linear in GPS time with no leap seconds
+    (gwfast/gwfastUtils.py:757-769)."""
+    return np.mod(9.533088395981618 + (np.asarray(t_GPS, dtype=np.float64) - 1126260000.) / 3600. * 24.
+                  / _glob.siderealDay, 24.) / 24.
+
+
+def check_evparams(evParams):
+    """Fill the derived parameters in place, as gwfast/gwfastUtils.py:965-1020 does: tcoal (GMST,
+    fraction of a day) from tGPS, iota from thetaJN, (Mc, eta) from (m1, m2), (theta, phi) from (ra, dec)."""
     if 'tcoal' not in evParams:
         if 'tGPS' in evParams:
-            raise ValueError('tcoal must be given as GMST (days); the tGPS conversion needs astropy, which this '
-                             'package does not use.')
-        raise ValueError('One among tGPS and tcoal has to be provided.')
+            print('Adding tcoal from tGPS')
+            # gwfast's convention: GMST, i.e. the local mean sidereal time at longitude 0
+            evParams['tcoal'] = GPSt_to_LMST(evParams['tGPS'], lat=0., long=0.)
+        else:
+            raise ValueError('One among tGPS and tcoal has to be provided.')
     if 'iota' not in evParams:
         if 'thetaJN' in evParams:
             evParams['iota'] = evParams['thetaJN']
@@ -43,11 +105,13 @@ def check_evparams(evParams):
             raise ValueError('One among iota and thetaJN has to be provided.')
     if 'Mc' not in evParams:
         if 'm1' in evParams and 'm2' in evParams:
+            print('Adding Mc and eta from the individual detector-frame masses')
             evParams['Mc'], evParams['eta'] = Mceta_from_m1m2(evParams['m1'], evParams['m2'])
         else:
             raise ValueError('Two among (Mc, eta) and (m1, m2) have to be provided.')
     if 'theta' not in evParams:
         if 'dec' in evParams and 'ra' in evParams:
+            print('Adding (theta, phi) from (ra, dec)')
             evParams['theta'] = np.pi / 2 - evParams['dec']
             evParams['phi'] = evParams['ra']
         else:

@@ -1,4 +1,6 @@
 """Host-side logic that needs no GPU: parameter handling, reparametrisation, duty cycle, sharding."""
+import os
+
 import numpy as np
 import pytest
 import torch
@@ -32,6 +34,32 @@ def test_check_evparams_mutates_and_raises():
     e2 = {'chiS': np.array([0.1]), 'chiA': np.array([0.05])}
     U.fill_spins(e2)
     assert np.isclose(e2['chi1z'][0], 0.15) and np.isclose(e2['chi2z'][0], 0.05)
+
+
+def test_tcoal_from_tgps():
+    """tcoal (GMST, fraction of a day) from tGPS, as gwfast/gwfastUtils.py:972-981 fills it.
+
+    Known answer: gwfast's tutorial event GW170817 (tGPS 1187008882.4) carries the GMST that gwfast's
+    astropy conversion printed, 0.43432288 (stored in tests/golden/kat_gw170817.npz). This conversion
+    evaluates the same IAU 2006 formula with UTC for UT1, so it may differ by |UT1 - UTC| <= 0.9 s,
+    i.e. 1.05e-5 of a day (it differs by 0.34 s here). J2000.0 (2000-01-01 12:00 UTC): GMST
+    18.697374558 h (the published IAU 1982 value; IAU 2006 differs by < 1e-6 h). gwfast's linear
+    approximation GPSt_to_GMST_alt ignores leap seconds and precession and stays within 3 s over
+    2001-2036."""
+    kat = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'kat_gw170817.npz'))
+    t = np.array([1187008882.4])
+    g = U.GPSt_to_LMST(t, lat=0., long=0.)
+    assert abs(g[0] - kat['ev_tcoal'][0]) <= 0.9 / 86400. + 1e-8
+    assert abs(U.GPSt_to_GMST(630763213.) * 24. - 18.697374558) < 1e-6 * 24.
+    ts = np.linspace(1.0e9, 1.8e9, 101)
+    d = (U.GPSt_to_GMST(ts) - U.GPSt_to_GMST_alt(ts) + 0.5) % 1.0 - 0.5
+    assert np.max(np.abs(d)) * 86400. < 3.0
+    assert np.allclose(U.GPSt_to_LMST(t, 40., 90.), (g + 0.25) % 1.0)
+    assert U.leap_seconds(1187008882.4) == 18 and U.leap_seconds(1.0e8) == 2
+    ev = {'Mc': np.array([1.2]), 'eta': np.array([0.25]), 'theta': np.array([1.]), 'phi': np.array([2.]),
+          'iota': np.array([0.5]), 'tGPS': t}
+    U.check_evparams(ev)
+    assert ev['tcoal'][0] == g[0]
 
 
 def test_mass_conversions_roundtrip():
