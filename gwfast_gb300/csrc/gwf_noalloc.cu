@@ -8,12 +8,16 @@
 // space, and that lives in one fixed-size array in this file.
 //
 // The scratch is a file-scope __device__ array: every GPU that loads the library holds it
-// (kScratchBytes) until the process exits. Its device address is looked up once per device,
-// by the first call made with that device current; that first call should therefore come
-// before any stream capture on the device. All calls share the array and it keeps the last
-// call's contents. Each call rewrites every byte it reads (PSD and QNM tables, PSD index,
-// per-event set-up records) before its kernels read them, so nothing has to start at zero.
-// Calls whose GPU work overlaps (different streams without ordering) race on the array.
+// (kScratchBytes) until the process exits. In host code its name is only a host-side stand-in,
+// so its device address is looked up with cudaGetSymbolAddress. The lookup is done by the first
+// call made in a CUDA context (with that context's device current) and cached under the
+// context's unique ID, so a context created later on the same device (after cudaDeviceReset, or a
+// caller's own context) gets its own lookup instead of a stale address; that first call in a
+// context should come before any stream capture in it. All calls share the array and it keeps the
+// last call's contents. Each call rewrites every byte it reads (PSD and QNM tables, PSD index,
+// per-event set-up records) before its kernels read them, so nothing has to start at zero. Calls
+// whose GPU work overlaps (different streams without ordering) race on the array.
+#include <cuda.h>   // CUcontext and the driver function types only (no link against libcuda)
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -45,32 +49,94 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 namespace {
 
-constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-unsigned char* g_ptr[kMaxDevices] = {};
 
 int fail(int code, const char* msg) {
   gwf::set_last_error(msg);
   return code;
 }
 
-// device address of the scratch on the current device, looked up on first use
+// unique ID of the current CUDA context (0 when none is current yet); the driver functions come
+// through the runtime's entry-point query, so the library needs no link against libcuda
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_get_current = nullptr;
+CtxGetIdFn g_get_id = nullptr;
+
+int current_ctx_id(unsigned long long* id) {
+  *id = 0;
+  if (!g_get_current || !g_get_id) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 4000, cudaEnableDefault, &q1) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return fail(GWF_ERR_CUDA, "gwf_fisher_noalloc: cuCtxGetCurrent/cuCtxGetId not available from the driver");
+    g_get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    g_get_id = reinterpret_cast<CtxGetIdFn>(f2);
+  }
+  CUcontext c = nullptr;
+  if (g_get_current(&c) != CUDA_SUCCESS) return fail(GWF_ERR_CUDA, "gwf_fisher_noalloc: cuCtxGetCurrent failed");
+  if (c && g_get_id(c, id) != CUDA_SUCCESS) return fail(GWF_ERR_CUDA, "gwf_fisher_noalloc: cuCtxGetId failed");
+  return GWF_OK;
+}
+
+// scratch addresses already looked up, keyed by context ID (oldest entry replaced when full)
+constexpr int kCacheSlots = 64;
+unsigned long long g_ctx_id[kCacheSlots] = {};
+unsigned char* g_ptr[kCacheSlots] = {};
+int g_next_slot = 0;
+
+// device address of the scratch in the current context, looked up on the first call in it
 int scratch_ptr(unsigned char** out) {
   int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0)
     return fail(GWF_ERR_CUDA, "gwf_fisher_noalloc: no usable current CUDA device");
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_ptr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      gwf::set_last_error(cudaGetErrorString(e));
-      return GWF_ERR_CUDA;
-    }
-    g_ptr[dev] = static_cast<unsigned char*>(p);
+  unsigned long long id = 0;
+  int rc = current_ctx_id(&id);
+  if (rc) return rc;
+  if (id)
+    for (int i = 0; i < kCacheSlots; ++i)
+      if (g_ctx_id[i] == id) {
+        *out = g_ptr[i];
+        return GWF_OK;
+      }
+  // first call in this context (the lookup also makes the device's primary context current when
+  // the runtime has not done so yet)
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
+    gwf::set_last_error(cudaGetErrorString(e));
+    return GWF_ERR_CUDA;
   }
-  *out = g_ptr[dev];
+  if (!id) {
+    rc = current_ctx_id(&id);
+    if (rc) return rc;
+  }
+  if (id) {
+    g_ctx_id[g_next_slot] = id;
+    g_ptr[g_next_slot] = static_cast<unsigned char*>(p);
+    g_next_slot = (g_next_slot + 1) % kCacheSlots;
+  }
+  *out = static_cast<unsigned char*>(p);
   return GWF_OK;
+}
+
+// PSD index: for each of nacc log-frequency bins, the last table row at or below the bin's lower
+// edge (a starting point for the lookup, which corrects it in either direction), by binary search
+__global__ void psd_index_kernel(const double* psd_f, int n, double l0, double idl, int* acc, int nacc) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nacc) return;
+  const double fb = exp(l0 + b / idl);
+  int lo = 0, hi = n - 2;   // answer in [0, n - 2]
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (psd_f[mid] <= fb) lo = mid;
+    else hi = mid - 1;
+  }
+  acc[b] = lo;
 }
 
 }  // namespace
@@ -113,27 +179,26 @@ extern "C" int gwf_fisher_noalloc(const gwf_det_desc* det, const double* psd_f, 
   if (rc) return rc;
   const cudaStream_t st = (cudaStream_t)stream;
 
-  // PSD table, its log-frequency index and the QNM table go into the scratch
+  // PSD table and the QNM table are copied into the scratch; the PSD index is built there on the
+  // device from the copied table (no library-owned host buffer is copied)
   const double l0 = std::log(psd_f[0]);
   const double idl = kAccBins / (std::log(psd_f[n_psd - 1]) - l0);
-  int acc[kAccBins];
-  int64_t j = 0;
-  for (int b = 0; b < kAccBins; ++b) {
-    const double fb = std::exp(l0 + b / idl);
-    while (j + 1 < n_psd - 1 && psd_f[j + 1] <= fb) ++j;
-    acc[b] = (int)j;
-  }
   cudaError_t e = cudaMemcpyAsync(base + kOffPsdF, psd_f, n_psd * sizeof(double), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(base + kOffPsdS, psd_S, n_psd * sizeof(double), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(base + kOffAcc, acc, sizeof(acc), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    psd_index_kernel<<<(kAccBins + 255) / 256, 256, 0, st>>>(reinterpret_cast<const double*>(base + kOffPsdF),
+                                                            (int)n_psd, l0, idl, reinterpret_cast<int*>(base + kOffAcc),
+                                                            kAccBins);
+    e = cudaGetLastError();
+  }
   if (e == cudaSuccess && wf->model == GWF_WF_PHENOMD) {
     double* q = reinterpret_cast<double*>(base + kOffQnm);
     e = cudaMemcpyAsync(q, qnm_spin, n_qnm * sizeof(double), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(q + n_qnm, qnm_fring, n_qnm * sizeof(double), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(q + 2 * n_qnm, qnm_fdamp, n_qnm * sizeof(double), cudaMemcpyHostToDevice, st);
   }
-  // (copies from pageable host memory return once the source has been read, so the stack copy
-  // of the index table may go out of scope)
+  // (copies from pageable host memory return once the source has been read; copies from
+  // page-locked memory read it when the stream reaches them)
   if (e != cudaSuccess) return fail(GWF_ERR_CUDA, cudaGetErrorString(e));
 
   gwf::LaunchArgs a;

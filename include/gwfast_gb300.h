@@ -272,10 +272,15 @@ int gwf_mlp_predict(gwf_mlp* mlp, const double* params, int64_t ld, int64_t n_ev
  * Scratch (the PSD table and its index, the QNM table and the per-event set-up records) lives
  * in a file-scope __device__ array of GWF_NOALLOC_SCRATCH_MIB MiB; events run in passes that fit
  * it. PSD tables longer than GWF_NOALLOC_MAX_PSD rows or QNM tables longer than
- * GWF_NOALLOC_MAX_QNM rows are rejected with GWF_ERR_INVALID_ARG. The first call on a device
- * (with that device current) looks the array's address up; make that first call before any
- * stream capture. Every call shares the array and rewrites what it reads; calls whose GPU work
- * overlaps (unordered streams) race on it. stream NULL = the default stream. */
+ * GWF_NOALLOC_MAX_QNM rows are rejected with GWF_ERR_INVALID_ARG. The array belongs to the CUDA
+ * context that is current at the call: the first call in a context (with its device current)
+ * looks the array's address up and caches it under the context's unique ID, so a context made
+ * later (after cudaDeviceReset, say) does its own lookup; make that first call before any stream
+ * capture in the context. Every call shares the array and rewrites what it reads; calls whose GPU
+ * work overlaps (unordered streams) race on it. The host tables are copied with
+ * cudaMemcpyAsync on the stream: from pageable memory the call returns after they have been
+ * read, but page-locked tables are read when the stream reaches the copy, so keep them
+ * unchanged until then. stream NULL = the default stream. */
 int gwf_fisher_noalloc(const gwf_det_desc* det, const double* psd_f, const double* psd_S, int64_t n_psd,
                        const gwf_wf_desc* wf, const double* qnm_spin, const double* qnm_fring, const double* qnm_fdamp,
                        int64_t n_qnm, const double* params, int64_t ld, int64_t n_events, int32_t res, int accumulate,

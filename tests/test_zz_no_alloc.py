@@ -1,8 +1,11 @@
 """gwf_fisher_noalloc (the Fisher entry point that allocates no device memory) against gwf_fisher.
 
-The library's scratch for this entry point is a fixed __device__ array shared by all calls, so
-the GPU test makes calls in a row with different models, detectors and event sets: each must
-match the context-based entry point on the same inputs.
+Callers whose device memory belongs to their own pool allocator, or whose loops cannot take the
+device synchronisation of cudaMalloc/cudaFree, use this entry point: its scratch is one fixed
+__device__ array in the library, shared by all calls. The GPU tests therefore make calls in a row
+with different models, detectors and event sets (IMRPhenomD, TaylorF2 and IMRPhenomHM), a batch
+larger than one pass of the scratch, and a two-detector network summed with accumulate=1: each
+must match the context-based entry point on the same inputs.
 """
 import ctypes
 
@@ -50,6 +53,7 @@ def test_noalloc_matches_fisher_calls_in_a_row():
     cases = [  # (model, detector, wall, Earth rotation, events, seed)
         (W.IMRPhenomD(), 'ETS', 5., True, 300, 11),
         (W.TaylorF2_RestrictedPN(), 'L1', 10., False, 200, 12),
+        (W.IMRPhenomHM(), 'ETS', 5., True, 150, 14),
         (W.IMRPhenomD(), 'H1', 10., True, 257, 13),
     ]
     stream = torch.cuda.Stream()
@@ -75,3 +79,59 @@ def test_noalloc_matches_fisher_calls_in_a_row():
         print('%s %s: max normalised |dF| %.2e' % (type(model).__name__, name, err.max()))
         assert np.all(np.isfinite(O))
         assert err.max() <= TOL
+
+
+def _compare(ref, out):
+    R, O = ref.cpu().numpy(), out.cpu().numpy()
+    dg = np.sqrt(np.abs(np.einsum('nii->ni', R)))
+    err = np.abs(O - R) / (dg[:, :, None] * dg[:, None, :])
+    assert np.all(np.isfinite(O))
+    return err.max()
+
+
+@pytest.mark.gpu
+def test_noalloc_multiple_passes_and_network_accumulate():
+    """7000 IMRPhenomD events need two passes of the scratch (6869 events per pass): the second
+    pass reads params + 6869 with the same leading dimension and writes out + 6869 matrices. Then a
+    two-detector network summed by two calls (accumulate=0, then 1) against gwf_fisher's network
+    total over the same detectors."""
+    torch = pytest.importorskip('torch')
+    assert torch.cuda.is_available()
+    lib = _lib.load()
+    ctx = _lib.Context(0)
+    q = _lib._qnm_table()
+    stream = torch.cuda.Stream()
+    wf = W.IMRPhenomD().gpu_desc()
+    f, S = aligo_table(10., rows=8000)
+    dets, ids = [], []
+    for name in ('L1', 'H1'):
+        det = _det(name, 10., True)
+        dets.append(det)
+        ids.append(ctx.add_detector(det.lat_rad, det.long_rad, det.xax_rad, 'L', True, 10., None, f, S))
+    n = 7000
+    params = torch.from_numpy(event_array(synthetic.bbh_events(n, seed=21))).cuda()
+    ref = torch.empty((n, 11, 11), dtype=torch.float64, device='cuda')
+    out = torch.full((n, 11, 11), float('nan'), dtype=torch.float64, device='cuda')
+    with torch.cuda.stream(stream):
+        ctx.fisher([ids[0]], wf, params, 2000, mem=_lib.MEM_DEVICE, out_net=ref, stream=stream.cuda_stream, ld=n, n=n)
+        rc = _noalloc(lib, dets[0], f, S, wf, q, params, n, out, stream=stream.cuda_stream)
+    assert rc == 0, lib.gwf_last_error()
+    stream.synchronize()
+    e1 = _compare(ref, out)
+    print('two passes, %d events: max normalised |dF| %.2e' % (n, e1))
+    assert e1 <= TOL
+
+    m = 600
+    params = torch.from_numpy(event_array(synthetic.bbh_events(m, seed=22))).cuda()
+    ref = torch.empty((m, 11, 11), dtype=torch.float64, device='cuda')
+    out = torch.full((m, 11, 11), float('nan'), dtype=torch.float64, device='cuda')
+    with torch.cuda.stream(stream):
+        ctx.fisher(ids, wf, params, 2000, mem=_lib.MEM_DEVICE, out_net=ref, stream=stream.cuda_stream, ld=m, n=m)
+        rc = _noalloc(lib, dets[0], f, S, wf, q, params, m, out, accumulate=0, stream=stream.cuda_stream)
+        assert rc == 0, lib.gwf_last_error()
+        rc = _noalloc(lib, dets[1], f, S, wf, q, params, m, out, accumulate=1, stream=stream.cuda_stream)
+    assert rc == 0, lib.gwf_last_error()
+    stream.synchronize()
+    e2 = _compare(ref, out)
+    print('L1 + H1 network by accumulation: max normalised |dF| %.2e' % e2)
+    assert e2 <= TOL
