@@ -66,6 +66,8 @@ SIGNATURES = {
     'gwf_set_refine_cond': ([_vp, _d], ctypes.c_int),
     'gwf_set_segments': ([_vp, ctypes.c_int], ctypes.c_int),
     'gwf_set_detector_groups': ([_vp, ctypes.c_int], ctypes.c_int),
+    'gwf_set_kernel_timing': ([_vp, ctypes.c_int], ctypes.c_int),
+    'gwf_kernel_times': ([_vp, ctypes.c_int, _vp, _vp, _P(ctypes.c_int)], ctypes.c_int),
     'gwf_set_graphs': ([_vp, ctypes.c_int], ctypes.c_int),
     'gwf_autotune_segments': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32, _vp, ctypes.c_int,
                                ctypes.c_int, ctypes.c_int, _P(ctypes.c_int)], ctypes.c_int),
@@ -201,6 +203,20 @@ class Context:
     def set_detector_groups(self, on):
         """FP32 network totals: evaluate detectors that share the grid in one launch (default on)."""
         check(load().gwf_set_detector_groups(self.h, int(bool(on))))
+
+    KT_NAMES = {1: 'setup', 2: 'group_f32', 3: 'fisher_f32', 4: 'fisher_f64', 5: 'segmented'}
+
+    def set_kernel_timing(self, on):
+        """Record CUDA events around the main launches of the following calls (see kernel_times)."""
+        check(load().gwf_set_kernel_timing(self.h, int(bool(on))))
+
+    def kernel_times(self):
+        """[(section, ms)] of the last call: set-up launches, group/per-detector Fisher launches."""
+        kind = np.zeros(64, dtype=np.int32)
+        ms = np.zeros(64, dtype=np.float64)
+        n = ctypes.c_int()
+        check(load().gwf_kernel_times(self.h, 64, ptr(kind), ptr(ms), ctypes.byref(n)))
+        return [(self.KT_NAMES.get(int(k), str(int(k))), float(t)) for k, t in zip(kind[:n.value], ms[:n.value])]
 
     def set_segments(self, points):
         """0: one CTA per event; > 0: persistent launches over frequency segments of this many points."""

@@ -129,6 +129,9 @@ struct gwf_ctx {
   // the call's stream and fills the source-record cache): per-group network totals, summed at the end
   cudaEvent_t core_ev = nullptr;
   DevBuf gnet;
+  // gwf_set_kernel_timing: events around the main sections of the last call
+  gwf::KernelTimer* ktimer = nullptr;
+  bool ktiming = false;
 };
 
 namespace {
@@ -526,8 +529,6 @@ int run(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf_wf_d
   if (!out_arm && !out_net) return fail(GWF_ERR_INVALID_ARG, "no output requested");
   if (precision != GWF_PREC_FP64 && precision != GWF_PREC_FP32 && precision != GWF_PREC_MIXED)
     return fail(GWF_ERR_INVALID_ARG, "bad precision");
-  if (precision != GWF_PREC_FP64 && wf->model == GWF_WF_PHENOMHM && !fisher)
-    return fail(GWF_ERR_UNSUPPORTED, "the FP32 SNR is implemented for TaylorF2 and IMRPhenomD");
   if (precision != GWF_PREC_FP64 && wf->model >= GWF_WF_TAYLORF2_TIDAL)
     return fail(GWF_ERR_UNSUPPORTED, "the tidal models are implemented in FP64");
   if (precision == GWF_PREC_MIXED && !fisher) return fail(GWF_ERR_INVALID_ARG, "the mixed form is a Fisher form");
@@ -680,6 +681,11 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   gwf::LaunchArgs a;
   a.scratch = (unsigned char*)ctx->setup.p;
   a.cap_events = (long long)chunk;
+  if (ctx->ktiming && ctx->ktimer && !capturing) {
+    ctx->ktimer->n = 0;
+    ctx->ktimer->open = false;
+    a.timer = ctx->ktimer;
+  }
   if (fisher && ctx->seg_points > 0 && wf->model < GWF_WF_TAYLORF2_TIDAL) {
     int64_t rmax = 0;
     if (capturing && res_ev) rmax = ctx->graph_rmax;   // from the uncaptured run of the same call
@@ -897,6 +903,10 @@ int gwf_ctx_destroy(gwf_ctx* ctx) {
   for (auto& g : ctx->graph_cache) cudaGraphExecDestroy(g.second.exec);
   ctx->graph_cache.clear();
   ctx->hpar.release(); ctx->hout.release();
+  if (ctx->ktimer) {
+    for (auto e : ctx->ktimer->ev) cudaEventDestroy(e);
+    delete ctx->ktimer;
+  }
   cudaEventDestroy(ctx->scratch_free);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -1019,6 +1029,42 @@ int gwf_set_graphs(gwf_ctx* ctx, int on) {
     for (auto& g : ctx->graph_cache) cudaGraphExecDestroy(g.second.exec);
     ctx->graph_cache.clear();
     ctx->graph_pending.clear();
+  }
+  return GWF_OK;
+}
+
+int gwf_set_kernel_timing(gwf_ctx* ctx, int on) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (on && !ctx->ktimer) {
+    auto* t = new gwf::KernelTimer();
+    for (int i = 0; i < 2 * gwf::KernelTimer::kMax; ++i) {
+      if (cudaEventCreate(&t->ev[i]) != cudaSuccess) {
+        for (int j = 0; j < i; ++j) cudaEventDestroy(t->ev[j]);
+        delete t;
+        return fail(GWF_ERR_CUDA, "event creation failed");
+      }
+    }
+    ctx->ktimer = t;
+  }
+  ctx->ktiming = on != 0;
+  return GWF_OK;
+}
+
+int gwf_kernel_times(gwf_ctx* ctx, int max_entries, int* kind, double* ms, int* n_entries) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  if (!n_entries || max_entries < 0 || (max_entries > 0 && (!kind || !ms)))
+    return fail(GWF_ERR_INVALID_ARG, "bad output arrays");
+  gwf::KernelTimer* t = ctx->ktimer;
+  const int n = t ? t->n : 0;
+  *n_entries = n;
+  for (int i = 0; i < n && i < max_entries; ++i) {
+    GWF_CK(cudaEventSynchronize(t->ev[2 * i + 1]));
+    float v = 0.0f;
+    GWF_CK(cudaEventElapsedTime(&v, t->ev[2 * i], t->ev[2 * i + 1]));
+    kind[i] = t->kind[i];
+    ms[i] = v;
   }
   return GWF_OK;
 }

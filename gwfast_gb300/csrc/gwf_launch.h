@@ -1,6 +1,7 @@
 // Launch descriptors shared by the per-model translation units and the C-ABI layer.
 #pragma once
 #include <cuda_runtime.h>
+#include "gwfast_gb300.h"
 #include "gwf_kernels_f32.cuh"
 #include "gwf_wave_out.cuh"
 
@@ -8,6 +9,32 @@ namespace gwf {
 
 // events per set-up/main launch pair (bounds the set-up scratch: chunk x record stride)
 constexpr long long kChunk = 16384;
+
+// Optional CUDA-event timing of the main launches of one call (gwf_set_kernel_timing): a start and
+// a stop event around each timed section on the stream it runs on. Nothing is recorded inside a
+// stream capture or once kMax sections are taken.
+struct KernelTimer {
+  static constexpr int kMax = 64;
+  cudaEvent_t ev[2 * kMax] = {};
+  int kind[kMax] = {};
+  int n = 0;
+  bool open = false;
+  static bool capturing(cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone;
+  }
+  cudaError_t begin(cudaStream_t st, int k) {
+    if (open || n >= kMax || capturing(st)) return cudaSuccess;
+    kind[n] = k;
+    open = true;
+    return cudaEventRecord(ev[2 * n], st);
+  }
+  cudaError_t end(cudaStream_t st) {
+    if (!open) return cudaSuccess;
+    open = false;
+    return cudaEventRecord(ev[2 * n++ + 1], st);
+  }
+};
 
 struct LaunchArgs {
   EvBatch ev;
@@ -41,6 +68,7 @@ struct LaunchArgs {
   // call (event n at rec_src + n * rec_stride): a gathered batch (core_idx) copies its rows from
   // there instead of running the set-up again
   const unsigned char* rec_src = nullptr;
+  KernelTimer* timer = nullptr;            // gwf_set_kernel_timing: events around the main launches
 };
 
 cudaError_t launch_fisher_m0(const LaunchArgs& a);

@@ -40,6 +40,10 @@ cudaError_t chunked(const LaunchArgs& a, bool f32, MAIN main) {
     ev.n0 = n0;
     const long long cnt = (a.ev.N - n0) < kChunk ? (a.ev.N - n0) : kChunk;
     const unsigned nb = (unsigned)((cnt + 63) / 64);
+    if (a.timer) {
+      const cudaError_t et = a.timer->begin(a.stream, GWF_KT_SETUP);
+      if (et != cudaSuccess) return et;
+    }
     if (a.rec_src && a.core_idx) {
       const long long words = cnt * (long long)(rec_stride<M>() / 16);
       copy_records_kernel<<<(unsigned)((words + 255) / 256), 256, 0, a.stream>>>(
@@ -55,6 +59,10 @@ cudaError_t chunked(const LaunchArgs& a, bool f32, MAIN main) {
     if constexpr (M < 3) {   // (the tidal models have no FP32 form)
       if (f32) setup_f32_kernel<M><<<nb, 64, 0, a.stream>>>(a.det, a.scratch, scratch32_of(a), cnt,
                                                             a.det.shape == 1 ? 2 : 1, a.det.earth);
+    }
+    if (a.timer) {
+      const cudaError_t et = a.timer->end(a.stream);
+      if (et != cudaSuccess) return et;
     }
     const cudaError_t e = main(ev, cnt);
     if (e != cudaSuccess) return e;
@@ -77,14 +85,18 @@ SegInfo seg_info(const LaunchArgs& a) {
 template <int NG, class KSEG>
 cudaError_t seg_chunk(const LaunchArgs& a, const EvBatch& ev, long long cnt, KSEG ks, const unsigned char* kscratch,
                       int smem, int grid, const double* rec, long long stride_d) {
+  cudaError_t e = a.timer ? a.timer->begin(a.stream, GWF_KT_SEGMENTED) : cudaSuccess;
+  if (e != cudaSuccess) return e;
   seg_scan_kernel<M><<<1, 1024, 0, a.stream>>>(a.scratch, cnt, a.seg, a.seg_off);
-  cudaError_t e = cudaMemsetAsync(a.seg_ctr, 0, sizeof(unsigned long long), a.stream);
+  e = cudaMemsetAsync(a.seg_ctr, 0, sizeof(unsigned long long), a.stream);
   if (e != cudaSuccess) return e;
   const SegInfo si = seg_info(a);
   ks<<<grid, kThreads, smem, a.stream>>>(ev, a.det, kscratch, cnt, si, (a.out_sd_arm || a.out_sd_det) ? 1 : 0);
   gram_reduce_kernel<NG><<<(unsigned)cnt, kThreads, 0, a.stream>>>(ev.n0, ev.N, cnt, si, rec, stride_d, a.out_arm,
                                                                    a.out_det, a.out_sd_arm, a.out_sd_det, a.accum);
-  return cudaGetLastError();
+  e = cudaGetLastError();
+  if (e == cudaSuccess && a.timer) e = a.timer->end(a.stream);
+  return e;
 }
 
 template <class K>
@@ -104,9 +116,10 @@ cudaError_t fisher_one(const LaunchArgs& a) {
     cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (err != cudaSuccess) return err;
     return chunked(a, false, [&](const EvBatch& ev, long long cnt) {
+      if (a.timer) a.timer->begin(a.stream, GWF_KT_FISHER_F64);
       k<<<(unsigned)cnt, kThreads, smem, a.stream>>>(ev, a.det, a.scratch, a.out_arm, a.out_det, a.out_sd_arm,
                                                      a.out_sd_det, a.accum);
-      return cudaSuccess;
+      return a.timer ? a.timer->end(a.stream) : cudaSuccess;
     });
   }
   if constexpr (M >= 3) {
@@ -132,9 +145,10 @@ cudaError_t fisher_one_f32(const LaunchArgs& a) {
     cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (err != cudaSuccess) return err;
     return chunked(a, true, [&](const EvBatch& ev, long long cnt) {
+      if (a.timer) a.timer->begin(a.stream, GWF_KT_FISHER_F32);
       k<<<(unsigned)cnt, kThreads, smem, a.stream>>>(ev, a.det, s32, a.out_arm, a.out_det, a.out_sd_arm, a.out_sd_det,
                                                      a.accum);
-      return cudaSuccess;
+      return a.timer ? a.timer->end(a.stream) : cudaSuccess;
     });
   }
   auto ks = fisher_seg_kernel_f32<M, EARTH, NARM, NG>;
@@ -181,7 +195,7 @@ cudaError_t fisher_dispatch(const LaunchArgs& a) {
   return a.per_arm ? fisher_one<false, 2, 3>(a) : fisher_one<false, 2, 2>(a);
 }
 
-#if GWF_MODEL < 2
+#if GWF_MODEL < 3
 template <bool EARTH, int NARM>
 cudaError_t snr_one_f32(const LaunchArgs& a) {
   unsigned char* s32 = scratch32_of(a);
@@ -196,7 +210,7 @@ cudaError_t snr_one_f32(const LaunchArgs& a) {
 cudaError_t snr_dispatch(const LaunchArgs& a) {
   const bool tri = a.det.shape == 1;
   if (a.precision == 1) {
-#if GWF_MODEL < 2
+#if GWF_MODEL < 3
     if (a.det.earth) return tri ? snr_one_f32<true, 2>(a) : snr_one_f32<true, 1>(a);
     return tri ? snr_one_f32<false, 2>(a) : snr_one_f32<false, 1>(a);
 #else
@@ -223,6 +237,10 @@ cudaError_t group_one(const LaunchArgs& a, GroupDev g) {
     ev.n0 = n0;
     const long long cnt = (a.ev.N - n0) < chunk ? (a.ev.N - n0) : chunk;
     const unsigned nb = (unsigned)((cnt + 63) / 64);
+    if (a.timer) {
+      err = a.timer->begin(a.stream, GWF_KT_SETUP);
+      if (err != cudaSuccess) return err;
+    }
     for (int d = 0; d < g.nd; ++d) {
       unsigned char* sc = a.scratch + (size_t)d * chunk * stride;
       const int mode = d == 0 ? a.core_mode : (a.core ? 2 : 0);
@@ -234,8 +252,14 @@ cudaError_t group_one(const LaunchArgs& a, GroupDev g) {
       setup_f32_kernel<M><<<nb, 64, 0, a.stream>>>(g.det[d], sc, sc + (size_t)chunk * rec_stride<M>(), cnt,
                                                    g.det[d].shape == 1 ? 2 : 1, g.det[d].earth);
     }
+    if (a.timer) {
+      err = a.timer->end(a.stream);
+      if (err == cudaSuccess) err = a.timer->begin(a.stream, GWF_KT_GROUP_F32);
+      if (err != cudaSuccess) return err;
+    }
     k<<<(unsigned)cnt, kThreads, smem, a.stream>>>(ev, g, a.scratch + (size_t)chunk * rec_stride<M>(), a.out_det, a.accum);
     err = cudaGetLastError();
+    if (err == cudaSuccess && a.timer) err = a.timer->end(a.stream);
     if (err != cudaSuccess) return err;
   }
   return cudaSuccess;

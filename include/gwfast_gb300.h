@@ -117,19 +117,20 @@ int gwf_detector_add(gwf_ctx* ctx, const gwf_det_desc* desc, const double* psd_f
                      int64_t n, int* det_id);
 
 /* Optimal SNR of N events in n_det detectors.
- * Replaces GWSignal.SNRInteg (gwfast/signal.py:658-777) and DetNet.SNR (gwfast/network.py:278-306).
+ * Replaces GWSignal.SNRInteg (gwfast/signal.py:658-777) and DetNet.SNR (gwfast/network.py:53-82).
  * out_arm (may be NULL): per arm slot (L: 1 slot, triangle: 3 slots, in det_ids order),
  *   [slots][N] of trapz((A+^2 + Ax^2)/S, f), i.e. (SNR_arm / 2)^2.
  * out_net (may be NULL): [N] network SNR^2 = sum over arms of 4 * out_arm.
- * precision: GWF_PREC_FP64, or GWF_PREC_FP32 (TaylorF2 and IMRPhenomD: per-point amplitude, pattern
- * functions and Earth-rotation time in FP32, per-thread compensated sums, FP64 block sums). */
+ * precision: GWF_PREC_FP64, or GWF_PREC_FP32 (TaylorF2, IMRPhenomD and IMRPhenomHM: per-point
+ * amplitude, pattern functions and Earth-rotation time in FP32, IMRPhenomHM's mode phases in FP64
+ * reduced modulo 2 pi, per-thread compensated sums, FP64 block sums). */
 int gwf_snr(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* wf, const double* params, int64_t ld,
             int64_t n_events, int32_t res, const int32_t* res_per_event, int spacing, int precision, int mem,
             double* out_arm, double* out_net, void* stream);
 
 /* Fisher matrices of N events in n_det detectors.
  * Replaces GWSignal.FisherMatr (gwfast/signal.py:782-1098, default arguments
- * use_chi1chi2=True, computeAnalyticalDeriv=True) and DetNet.FisherMatr (gwfast/network.py:309-343).
+ * use_chi1chi2=True, computeAnalyticalDeriv=True) and DetNet.FisherMatr (gwfast/network.py:84-153).
  * per_arm != 0: out_arm receives [slots][N][11][11] per arm (return_all=True);
  * out_net (may be NULL): [N][11][11] network total.
  * precision: GWF_PREC_FP64 (the drop-in) or GWF_PREC_FP32 (split precision: per-event set-up in
@@ -181,6 +182,19 @@ int gwf_overlap(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* 
  * four) are evaluated by one launch that computes the waveform and its tangent once per frequency
  * point and accumulates all their derivative vectors into one Gram. on = 0: one launch per detector. */
 int gwf_set_detector_groups(gwf_ctx* ctx, int on);
+
+/* Kernel timing (an extension for measurement; no counterpart in gwfast). on != 0: the following
+ * gwf_snr / gwf_fisher calls record CUDA events around their main sections, each on the stream it
+ * runs on, so that the time of a kernel is measured without the rest of the call: the per-event
+ * set-up launches of a chunk (GWF_KT_SETUP), the FP32 launch of a detector group
+ * (GWF_KT_GROUP_F32), a per-detector FP32 or FP64 Fisher launch (GWF_KT_FISHER_F32,
+ * GWF_KT_FISHER_F64) and a segmented launch sequence (GWF_KT_SEGMENTED: scan, persistent kernel,
+ * reduction). Nothing is recorded inside a CUDA-graph capture or a replay. Each call starts a new
+ * list (at most 64 sections). gwf_kernel_times waits for the last call's events and writes up to
+ * max_entries (kind, milliseconds) pairs and the number of sections taken. */
+enum { GWF_KT_SETUP = 1, GWF_KT_GROUP_F32 = 2, GWF_KT_FISHER_F32 = 3, GWF_KT_FISHER_F64 = 4, GWF_KT_SEGMENTED = 5 };
+int gwf_set_kernel_timing(gwf_ctx* ctx, int on);
+int gwf_kernel_times(gwf_ctx* ctx, int max_entries, int* kind, double* ms, int* n_entries);
 
 /* Condition-number threshold of GWF_PREC_MIXED (no counterpart in gwfast: a property of the
  * reduced-precision form). kappa > 0; events with equilibrated condition number above it get FP64. */
