@@ -20,12 +20,14 @@ class SNRScreen:
         self.train_loss = None
         self.res = None
 
-    def fit(self, events, snr=None, res=1000, epochs=30, batch=4096, lr=2e-3, seed=0, snr_precision='fp32'):
-        """Train on the events' exact network SNRs (computed here unless given). Returns the mean
-        squared error in ln SNR over the last epoch."""
+    def fit(self, events, snr=None, res=1000, epochs=30, batch=4096, lr=2e-3, seed=0, snr_precision='fp32',
+            res_per_event=None):
+        """Train on the events' exact network SNRs (computed here unless given, on res points or on
+        the per-event grid lengths res_per_event). Returns the mean squared error in ln SNR over the
+        last epoch."""
         p = _prep(events)
         if snr is None:
-            snr = self.net.SNR(events, res=res, precision=snr_precision)
+            snr = self.net.SNR(events, res=res, precision=snr_precision, res_per_event=res_per_event)
         self.res = res
         self.train_loss = self.mlp.train(p, np.log(np.maximum(np.asarray(snr, dtype=np.float64), 1e-30)),
                                          epochs=epochs, batch=batch, lr=lr, seed=seed)

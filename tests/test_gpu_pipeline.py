@@ -42,3 +42,38 @@ def test_compute_errs_fixed_params(gpu_lib):
     ok = full['cond'] < 1e12
     rel = np.abs(np.sqrt(np.einsum('iin->in', C)) - fx['errors']) / fx['errors']
     assert np.max(rel[:, ok]) < 1e-6
+
+
+def test_run_catalogue_batches_and_resume(gpu_lib, tmp_path, monkeypatch):
+    """The driver loop: batches written under gwfast's file names, results equal to one compute_errs
+    over the whole catalogue, and a resumed run recomputes only the batch whose files are missing."""
+    ev = synthetic.bbh_events(300, seed=83)
+    ev['dL'] = ev['dL'] * 1.5          # part of the catalogue below threshold
+    net = synthetic.make_network(W.IMRPhenomD(), earth=True)
+    kw = dict(snr_th=12., res=1000, precision='fp64', snr_precision='fp64')
+    whole = pipeline.compute_errs(net, dict(ev), check_fisher=True, **kw)
+    assert 0 < whole['detected'].sum() < 300
+    tot = pipeline.run_catalogue(net, dict(ev), str(tmp_path), batch_size=128, **kw)
+    names = sorted(p.name for p in tmp_path.iterdir())
+    for a, b in ((0, 128), (128, 256), (256, 300)):
+        assert 'snrs_%d_to_%d.txt' % (a, b) in names
+        assert ('fishers_%d_to_%d.npy' % (a, b) in names) == bool(whole['detected'][a:b].any())
+    assert np.allclose(tot['snrs'], whole['snr'], rtol=1e-12)
+    assert np.array_equal(tot['idxs_det'].astype(int), np.where(whole['detected'])[0])
+    assert np.allclose(tot['fishers'], whole['fisher'], rtol=1e-12, atol=0)
+    assert np.allclose(tot['cond_numbers'], whole['cond_numbers'], rtol=1e-6)
+    ok = whole['cond'] < 1e12
+    assert np.allclose(tot['errors'][:, ok], whole['errors'][:, ok], rtol=1e-9)
+    for p in tmp_path.iterdir():
+        if p.name.endswith('_128_to_256.txt') or p.name.endswith('_128_to_256.npy'):
+            p.unlink()
+    calls = []
+    orig = pipeline.compute_errs
+
+    def counting(*a, **k):
+        calls.append(len(a[1]['Mc']))
+        return orig(*a, **k)
+    monkeypatch.setattr(pipeline, 'compute_errs', counting)
+    tot2 = pipeline.run_catalogue(net, dict(ev), str(tmp_path), batch_size=128, **kw)
+    assert calls == [128]
+    assert np.allclose(tot2['fishers'], tot['fishers'], rtol=1e-12, atol=0)

@@ -273,3 +273,22 @@ def test_check_fisher_against_gwfast(capsys):
     assert np.all(np.isnan(ev[1])) and np.all(np.isnan(vec[1])) and np.isnan(cond[1])
     assert np.all(np.isfinite(cond[[0, 2, 3]]))
     assert 'Fisher is nan at position 1' in capsys.readouterr().out
+
+
+def test_batch_files_roundtrip(tmp_path):
+    """Per-batch output files of the catalogue driver under gwfast's names and shapes, read back."""
+    from gwfast_gb300 import pipeline
+    rng = np.random.default_rng(3)
+    det = np.array([True, False, True, True])
+    F = rng.normal(size=(11, 11, 3))
+    out = {'snr': rng.uniform(5, 20, 4), 'detected': det, 'fisher': F, 'cov': F * 2, 'eps': rng.uniform(size=3),
+           'cond': rng.uniform(size=3), 'cond_numbers': rng.uniform(size=3), 'errors': rng.uniform(size=(11, 3)),
+           'sky_area_90': rng.uniform(size=3)}
+    pipeline.batch_to_file(out, 40, str(tmp_path))
+    back = pipeline.batch_from_file(str(tmp_path), 40, 44)
+    assert np.allclose(back['snrs'], out['snr']) and np.array_equal(back['fishers'], F)
+    assert np.array_equal(back['idxs_det'].astype(int), [40, 42, 43])
+    assert back['errors'].shape == (11, 3) and np.allclose(back['cond_numbers'], out['cond_numbers'])
+    none = dict(out, detected=np.zeros(4, bool), fisher=None)
+    pipeline.batch_to_file(none, 0, str(tmp_path))
+    assert set(pipeline.batch_from_file(str(tmp_path), 0, 4)) == {'snrs'}
