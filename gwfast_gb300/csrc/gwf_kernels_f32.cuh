@@ -1045,9 +1045,13 @@ __global__ void __launch_bounds__(kThreads, 5) fisher_group_kernel_f32(EvBatch e
 }
 
 // ------------------------------------------------------------------ FP32 SNR
-// Per arm: scale * sum_k w_k / S_k * A_k^2 ((cp F+)^2 + (ci Fx)^2) with A, the pattern functions and
-// the Earth-rotation time in FP32; each thread sums its points with Kahan compensation, the block
-// sums in FP64. Outputs as snr_kernel.
+// Per arm: scale * sum_k w_k / S_k (|h+|^2 F+^2 + |hx|^2 Fx^2) with the amplitudes, the pattern
+// functions and the Earth-rotation time in FP32; each thread sums its points with Kahan compensation,
+// the block sums in FP64. Outputs as snr_kernel. For the 22-mode models |h+| = A cp and |hx| = A ci;
+// for IMRPhenomHM they are the moduli of the two mode sums, each mode phase evaluated in FP64 and
+// reduced modulo 2 pi as in the FP32 Fisher kernel (only the values of wave_f32_hm are used; its
+// tangent arithmetic is dead code here), and the h+ hx cross term is left out, as gwfast's
+// GWAmplitudes does for higher modes (gwfast/signal.py:457-460).
 template <int MODEL, bool EARTH, int NARM>
 __global__ void __launch_bounds__(kThreads) snr_kernel_f32(EvBatch ev, DetDev det, const unsigned char* scratch32,
                                                            double* out_arm, double* out_det, int accum) {
@@ -1075,17 +1079,27 @@ __global__ void __launch_bounds__(kThreads) snr_kernel_f32(EvBatch ev, DetDev de
     float f, lnf, w;
     grid.point(r, ev.spacing, k, lane, f, lnf, w);
     const float ws = w / psd_at_f(det, f, lnf, r.gf.acc_l0, r.gf.acc_idl);
-    float A;
+    float ap, ac;
     TimeF ts;
-    if (MODEL == 0) {
-      const float f13 = cbrtf(f);
-      A = r.ef.tf2.ampK.v * (1.0f / (f * sqrtf(f13)));
-      if (EARTH) time_f(r.pf, -tau_star_point<float>(r.ef.tf2.Ms, r.ef.tf2.vM, r.ef.tf2.eta, f13) * (1.0f / 86400.0f), ts);
+    if constexpr (MODEL == 2) {
+      WaveF wv;
+      wave_f32_hm<EARTH>(r.ef, r.pf, f, wv);
+      ap = sqrtf(wv.P.re * wv.P.re + wv.P.im * wv.P.im);
+      ac = sqrtf(wv.C.re * wv.C.re + wv.C.im * wv.C.im);
+      if (EARTH) time_f(r.pf, -wv.tau * (1.0f / 86400.0f), ts);
     } else {
-      A = phd_amp_point<float>(r.ef.phd, f);
-      if (EARTH) time_f(r.pf, -tau_star_point<float>(r.ef.phd.Ms, r.ef.phd.vM, r.ef.phd.eta, cbrtf(f)) * (1.0f / 86400.0f), ts);
+      float A;
+      if (MODEL == 0) {
+        const float f13 = cbrtf(f);
+        A = r.ef.tf2.ampK.v * (1.0f / (f * sqrtf(f13)));
+        if (EARTH) time_f(r.pf, -tau_star_point<float>(r.ef.tf2.Ms, r.ef.tf2.vM, r.ef.tf2.eta, f13) * (1.0f / 86400.0f), ts);
+      } else {
+        A = phd_amp_point<float>(r.ef.phd, f);
+        if (EARTH) time_f(r.pf, -tau_star_point<float>(r.ef.phd.Ms, r.ef.phd.vM, r.ef.phd.eta, cbrtf(f)) * (1.0f / 86400.0f), ts);
+      }
+      ap = A * r.pf.cp;
+      ac = A * r.pf.ci;
     }
-    const float ap = A * r.pf.cp, ac = A * r.pf.ci;
     float p[2], c[2];
 #pragma unroll
     for (int a = 0; a < NARM; ++a) {

@@ -28,7 +28,7 @@ class DetNet:
             self.signals[d]._update_seed(seed=seeds[i])
 
     def SNR(self, evParams, res=1000, return_all=False, precision='fp64', res_per_event=None):
-        """Network SNR (gwfast/network.py:278-306); precision='fp32' selects the FP32 SNR kernel."""
+        """Network SNR (gwfast/network.py:53-82); precision='fp32' selects the FP32 SNR kernel."""
         utils.check_evparams(evParams)
         names, sigs = self._list()
         arms = snr_batch(sigs, evParams, res, device=sigs[0].device, precision=precision, res_per_event=res_per_event)
@@ -48,7 +48,7 @@ class DetNet:
         return net
 
     def FisherMatr(self, evParams, return_all=False, return_derivatives=False, return_SNR_derivatives=False, **kwargs):
-        """Network Fisher matrix, (11, 11, N) (gwfast/network.py:309-377).
+        """Network Fisher matrix, (11, 11, N) (gwfast/network.py:84-153).
 
         return_SNR_derivatives=True returns (allF, allDer) as gwfast: per-arm Fisher matrices and
         per-arm SNR-derivative integrals (11, N) keyed by detector (name_0..2 for triangles), plus

@@ -1368,12 +1368,12 @@ def fisher(det, model, p, res=1000):
 
 
 def network_snr(dets, model, p, res=1000):
-    """DetNet.SNR (gwfast/network.py:278-306)."""
+    """DetNet.SNR (gwfast/network.py:53-82)."""
     return torch.sqrt(sum(snr(d, model, p, res) ** 2 for d in dets))
 
 
 def network_fisher(dets, model, p, res=1000):
-    """DetNet.FisherMatr (gwfast/network.py:309-343): (N, 11, 11)."""
+    """DetNet.FisherMatr (gwfast/network.py:84-153): (N, 11, 11)."""
     return sum(fisher(d, model, p, res) for d in dets)
 
 
