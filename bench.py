@@ -42,6 +42,9 @@ N_EVENTS = 10000
 RES = 2000
 SNR_TH = 12.
 METRIC = 'network Fisher matrices/s (IMRPhenomD, L1+H1+ETS, Earth rotation, R=2000)'
+# DRAM bytes (read + write) per event of the L1 + H1 group launch, from one ncu capture of a
+# 2048-event launch (5.708 MB read, 0 written)
+GRP_DRAM_BYTES_PER_EVENT = 5.707776e6 / 2048
 
 
 def dist_info():
@@ -165,18 +168,38 @@ def gemm_peak(torch, dev, dtype, n):
     return 2 * n ** 3 / best / 1e12
 
 
-def run_mixed_catalogue(args):
+def _timed_stream(torch, stream, flush):
+    """CUDA-event timer on `stream`: mean ms of k calls after `warm` untimed ones, L2 flushed before each."""
+    def timed(fn, k, warm=0):
+        for _ in range(warm):
+            fn()
+        tot = 0.0
+        for _ in range(k):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot / k
+    return timed
+
+
+def measure_mixed_catalogue(n_events, steps, warmup, refine_cond=1e13, fp64_sample=2000):
     """Batching workload: 50 % BNS + 50 % BBH, per-event grid lengths from the chirp time at 2 Hz
     (200 to 40000 points), L1 + H1 (10 Hz) + ET triangle (2 Hz wall), IMRPhenomD, Earth rotation.
-    Times the per-event launches against the autotuned persistent segmented launches (CUDA-graph
-    replay for the device-resident FP64 and FP32 forms) and the mixed form."""
+    FP32 and mixed forms over all events, per-event launches against the autotuned persistent
+    segmented launches (CUDA-graph replay for the device-resident FP32 form); the plain FP64 kernel
+    (per-event launches) timed on the first fp64_sample events (i.i.d. events, so the per-event rate
+    carries over). SNR/s of the FP32 and FP64 SNR kernels."""
     import torch
     from gwfast_gb300 import _build, _lib, synthetic
     from gwfast_gb300 import waveforms as W
     from gwfast_gb300.signal import event_array
     _build.build()
     dev = torch.device('cuda', 0)
-    N = args.events
+    N = n_events
     ev = synthetic.mixed_events(N, seed=1002)
     res_ev = synthetic.res_from_chirp_time(ev['Mc'], 2.)
     rmax = int(res_ev.max())
@@ -184,6 +207,7 @@ def run_mixed_catalogue(args):
     net = synthetic.make_network(wf, dets=synthetic.NETWORK_LHET2, earth=True)
     ids = [s.det_id for s in net.signals.values()]
     ctx = _lib.context(0)
+    ctx.set_refine_cond(refine_cond)
     p_dev = torch.from_numpy(event_array(ev)).to(dev)
     r_dev = torch.from_numpy(np.ascontiguousarray(res_ev, dtype=np.int32)).to(dev)
     out = torch.empty((N, 11, 11), dtype=torch.float64, device=dev)
@@ -192,165 +216,196 @@ def run_mixed_catalogue(args):
     torch.cuda.set_stream(stream)
     desc = wf.gpu_desc()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    timed = _timed_stream(torch, stream, flush)
+    n64 = min(N, fp64_sample)
 
-    def step(precision):
+    def step(precision, n=N):
         ctx.fisher(ids, desc, p_dev, rmax, res_ev=r_dev, per_arm=False, mem=_lib.MEM_DEVICE, out_net=out,
-                   stream=stream.cuda_stream, ld=N, n=N, precision=precision)
-
-    def timed(fn, k, warm):
-        for _ in range(warm):
-            fn()
-        tot = 0.0
-        for _ in range(k):
-            flush.zero_()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            fn()
-            e1.record(stream)
-            e1.synchronize()
-            tot += e0.elapsed_time(e1)
-        return tot / k
+                   stream=stream.cuda_stream, ld=N, n=n, precision=precision)
 
     forms = {}
-    ctx.set_graphs(False)
-    for prec in ('fp64', 'fp32'):
-        ctx.set_segments(0)
-        forms[prec + '_per_event'] = timed(lambda: step(prec), args.steps, args.warmup)
-        ns = min(N, 2000)
-        seg = ctx.autotune_segments(ids, desc, p_dev, rmax, res_ev=r_dev, precision=prec, mem=_lib.MEM_DEVICE,
-                                    ld=N, n=ns)
-        ctx.set_graphs(True)
-        forms[prec + '_segmented_graph'] = timed(lambda: step(prec), args.steps, args.warmup)
-        forms[prec + '_segment_points'] = seg
+    try:
         ctx.set_graphs(False)
-    forms['mixed_segmented'] = timed(lambda: step('mixed'), args.steps, args.warmup)
-    ctx.set_segments(0)
-    ms_snr = timed(lambda: ctx.snr(ids, desc, p_dev, rmax, res_ev=r_dev, mem=_lib.MEM_DEVICE, out_net=snr_out,
-                                   stream=stream.cuda_stream, ld=N, n=N), args.steps, args.warmup)
-    line = {
+        ctx.set_segments(0)
+        forms['fp64_per_event'] = timed(lambda: step('fp64', n64), max(1, steps // 2), 1) * N / n64
+        forms['fp32_per_event'] = timed(lambda: step('fp32'), steps, warmup)
+        forms['mixed_per_event'] = timed(lambda: step('mixed'), steps, warmup)
+        seg = ctx.autotune_segments(ids, desc, p_dev, rmax, res_ev=r_dev, precision='fp32', mem=_lib.MEM_DEVICE,
+                                    ld=N, n=min(N, 4000))
+        forms['fp32_segment_points'] = seg
+        ctx.set_graphs(True)
+        forms['fp32_segmented_graph'] = timed(lambda: step('fp32'), steps, warmup)
+        ctx.set_graphs(False)
+        forms['mixed_segmented'] = timed(lambda: step('mixed'), steps, warmup)
+        ctx.set_segments(0)
+        ms_snr = timed(lambda: ctx.snr(ids, desc, p_dev, rmax, res_ev=r_dev, mem=_lib.MEM_DEVICE, out_net=snr_out,
+                                       stream=stream.cuda_stream, ld=N, n=N, precision='fp32'), steps, warmup)
+        ms_snr64 = timed(lambda: ctx.snr(ids, desc, p_dev, rmax, res_ev=r_dev, mem=_lib.MEM_DEVICE, out_net=snr_out,
+                                         stream=stream.cuda_stream, ld=N, n=n64), max(1, steps // 2), 1) * N / n64
+    finally:
+        ctx.set_graphs(False)
+        ctx.set_segments(0)
+    best = min(('mixed_per_event', 'mixed_segmented'), key=lambda k: forms[k])
+    return {
         'metric': 'network Fisher matrices/s, mixed BNS+BBH catalogue (per-event grids 200-40000 points)',
-        'value': N / (forms['mixed_segmented'] / 1e3), 'unit': 'Fisher/s', 'n_gpus': 1, 'steps': args.steps,
-        'warmup': args.warmup, 'ms_per_step': forms['mixed_segmented'], 'higher_is_better': True, 'scaling': 'weak',
-        'vs_baseline': None, 'dtype': 'f32 per point, f64 for events with cond > %.0e' % args.refine_cond,
-        'data': 'synthetic (seeded mixed catalogue)',
+        'value': N / (forms[best] / 1e3), 'unit': 'Fisher/s', 'chosen': best, 'ms_per_step': forms[best],
+        'dtype': 'f32 per point, f64 for events with cond > %.0e' % refine_cond,
         'config': {'workload': 'IMRPhenomD, %d events (50%% BNS, 50%% BBH), L1+H1 (10 Hz) + ETS (2 Hz), Earth rotation, '
                                'per-event res from chirp time' % N, 'res_min': int(res_ev.min()), 'res_max': rmax,
-                   'points_total': int(res_ev.sum()), 'l2': 'flushed (256 MB write) before every step'},
+                   'points_total': int(res_ev.sum()), 'l2': 'flushed (256 MB write) before every step',
+                   'fp64_sampled_events': n64},
         'forms_ms_per_step': forms,
         'fisher_per_s': {k: N / (v / 1e3) for k, v in forms.items() if not k.endswith('points')},
-        'speedup_vs_fp64_per_event': forms['fp64_per_event'] / forms['mixed_segmented'],
-        'snr_per_s': N / (ms_snr / 1e3),
+        'speedup_vs_fp64_per_event': forms['fp64_per_event'] / forms[best],
+        'snr_per_s': {'fp32': N / (ms_snr / 1e3), 'fp64': N / (ms_snr64 / 1e3)},
     }
+
+
+def run_mixed_catalogue(args):
+    line = measure_mixed_catalogue(args.events, args.steps, args.warmup, args.refine_cond)
+    line.update({'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup, 'higher_is_better': True,
+                 'scaling': 'weak', 'vs_baseline': None, 'data': 'synthetic (seeded mixed catalogue)'})
     print(json.dumps(line))
 
 
-def run_screen(args):
-    """Learned-screen workload: 10^6 events of the mixed population with dL up to 30 Gpc, the
-    headline network, threshold SNR 12, R = 1000. The plain FP64 path (FP64 SNR of every event,
-    FP64 Fisher of the detected ones) against the screened path (MLP prediction, FP32 SNR for the
-    events near threshold and a 1 % audit of the skipped ones, mixed-form Fisher of the detected
-    ones). The network is trained first on 2 x 10^5 exact SNRs of other events of the population
-    (timed apart). Fisher/s = detected events / wall time, host dict in, host arrays out."""
+def measure_screen(n_events, train_events, train_epochs, steps, warmup, fp64_sample=50000, per_event_res=True):
+    """Learned-screen workload: n_events of the mixed population with dL up to 30 Gpc, the headline
+    network (L1 + H1 at 10 Hz, ET triangle at 5 Hz), IMRPhenomD, threshold SNR 12, per-event grid
+    lengths from the chirp time at 2 Hz (200 to 40000 points). The screened path (MLP prediction,
+    FP32 SNR for the events near threshold and a 1 % audit of the skipped ones, mixed-form Fisher of
+    the detected ones) over all events, against the plain FP64 path (FP64 SNR of every event, FP64
+    Fisher of the detected ones) timed on a random sample of fp64_sample events (the same population,
+    so detected events per second carry over). The network is trained first on train_events exact
+    SNRs of other events of the population (timed apart). Fisher/s = detected events / wall time,
+    host dict in, host arrays out. The sigma error of the screened path's Fishers against the FP64
+    kernel is checked on the detected events of the FP64 sample."""
     import torch
-    from gwfast_gb300 import _build, pipeline, synthetic
+    from gwfast_gb300 import _build, fisherTools, pipeline, synthetic
     from gwfast_gb300 import waveforms as W
     from gwfast_gb300.screen import SNRScreen
     _build.build()
     torch.cuda.set_device(0)
-    N, R = args.events, 1000
+    N = n_events
     net = synthetic.make_network(W.IMRPhenomD(), dets=synthetic.NETWORK_LHET, earth=True)
-    train = synthetic.screen_population(args.train_events, seed=2004)
+    train = synthetic.screen_population(train_events, seed=2004)
     ev = synthetic.screen_population(N, seed=1004)
+    rmax = 40000 if per_event_res else 1000
+    rtrain = synthetic.res_from_chirp_time(train['Mc'], 2.) if per_event_res else None
+    rev = synthetic.res_from_chirp_time(ev['Mc'], 2.) if per_event_res else None
     t0 = time.perf_counter()
     screen = SNRScreen(net, hidden=256, layers=4, seed=1)
-    loss = screen.fit(dict(train), res=R, epochs=args.train_epochs, batch=4096, lr=2e-3)
+    loss = screen.fit(dict(train), res=rmax, res_per_event=rtrain, epochs=train_epochs, batch=4096, lr=2e-3)
     t_train = time.perf_counter() - t0
-    for _ in range(max(1, args.warmup)):
-        pipeline.compute_errs(net, dict(ev), snr_th=SNR_TH, res=R, precision='mixed', sky_area=False, screen=screen)
-    ts, tp = [], []
-    for _ in range(args.steps):
+    kw = dict(snr_th=SNR_TH, res=rmax, sky_area=False)
+    for _ in range(max(1, warmup)):
+        pipeline.compute_errs(net, dict(ev), precision='mixed', screen=screen, res_per_event=rev, **kw)
+    ts = []
+    for _ in range(steps):
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        rs = pipeline.compute_errs(net, dict(ev), snr_th=SNR_TH, res=R, precision='mixed', sky_area=False,
-                                   screen=screen)
+        rs = pipeline.compute_errs(net, dict(ev), precision='mixed', screen=screen, res_per_event=rev, **kw)
         ts.append(time.perf_counter() - t0)
+    rng = np.random.default_rng(7)
+    samp = np.sort(rng.choice(N, size=min(N, fp64_sample), replace=False))
+    evs = {k: np.asarray(v)[samp] for k, v in ev.items()}
+    rs_samp = None if rev is None else rev[samp]
+    pipeline.compute_errs(net, dict(evs), precision='fp64', snr_precision='fp64', res_per_event=rs_samp, **kw)
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    rp = pipeline.compute_errs(net, dict(ev), snr_th=SNR_TH, res=R, precision='fp64', snr_precision='fp64',
-                               sky_area=False)
-    tp.append(time.perf_counter() - t0)
-    t_s, t_p = statistics.median(ts), statistics.median(tp)
+    rp = pipeline.compute_errs(net, dict(evs), precision='fp64', snr_precision='fp64', res_per_event=rs_samp, **kw)
+    t_p = time.perf_counter() - t0
+    t_s = statistics.median(ts)
     det_s, det_p = rs['detected'], rp['detected']
-    line = {
+    # sigma error of the screened path's Fisher matrices against the plain FP64 ones, on the events
+    # detected by both in the FP64 sample
+    pos_s = -np.ones(N, dtype=np.int64)
+    pos_s[np.where(det_s)[0]] = np.arange(det_s.sum())
+    both = det_p & det_s[samp]
+    Fp = rp['fisher'][..., np.where(both[det_p])[0]]
+    Fs = rs['fisher'][..., pos_s[samp[both]]]
+    c64, _, cond = fisherTools.CovMatr(Fp, return_cond=True)
+    cs, _, _ = fisherTools.CovMatr(Fs, return_cond=True)
+    s64, ss = np.sqrt(np.abs(np.einsum('iin->ni', c64))), np.sqrt(np.abs(np.einsum('iin->ni', cs)))
+    err = (np.abs(ss - s64) / s64).max(axis=1)
+    ok = cond < 1e13
+    rate_s = float(det_s.sum() / t_s)
+    rate_p = float(det_p.sum() / t_p)
+    return {
         'metric': 'forecast Fisher matrices/s with the learned SNR screen (detected events / wall time)',
-        'value': float(det_s.sum() / t_s), 'unit': 'Fisher/s', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
-        'ms_per_step': 1e3 * t_s, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
-        'dtype': 'bf16 weights / f32 MLP; f32 SNR; f32 Fisher with f64 for cond > 1e11',
-        'data': 'synthetic (seeded population, dL up to 30 Gpc)',
-        'config': {'workload': '%d events, 50%% BNS / 50%% BBH, dL <= 30 Gpc, L1+H1+ETS, IMRPhenomD, R=1000, '
-                               'SNR > %g' % (N, SNR_TH), 'mlp': '11 -> 4 x 256 SiLU -> 1, trained on %d exact SNRs, '
-                               '%d epochs' % (args.train_events, args.train_epochs), 'band_ln_snr': 0.3,
-                   'audit_fraction': 0.01},
+        'value': rate_s, 'unit': 'Fisher/s', 'ms_per_step': 1e3 * t_s, 'steps': steps, 'warmup': warmup,
+        'dtype': 'bf16 weights / f32 MLP; f32 SNR; f32 Fisher with f64 for cond > 1e13',
+        'config': {'workload': '%d events, 50%% BNS / 50%% BBH, dL <= 30 Gpc, L1+H1+ETS, IMRPhenomD, %s, SNR > %g'
+                               % (N, 'per-event res from chirp time at 2 Hz (200-40000)' if per_event_res else
+                                  'R=1000', SNR_TH),
+                   'mlp': '11 -> 4 x 256 SiLU -> 1, trained on %d exact SNRs, %d epochs' % (train_events, train_epochs),
+                   'band_ln_snr': 0.3, 'audit_fraction': 0.01,
+                   'points_total': int(rev.sum()) if rev is not None else N * 1000},
         'screen': rs['screen'], 'train_s': t_train, 'train_loss_ln_snr_mse': loss,
-        'plain_fp64_path': {'value': float(det_p.sum() / t_p), 'unit': 'Fisher/s', 's_per_step': t_p,
-                            'detected': int(det_p.sum())},
-        'speedup_vs_plain_fp64_path': float((det_s.sum() / t_s) / (det_p.sum() / t_p)),
+        'plain_fp64_path': {'value': rate_p, 'unit': 'Fisher/s', 's_sample': t_p, 'sample_events': int(len(samp)),
+                            'detected_in_sample': int(det_p.sum()),
+                            'what': 'FP64 SNR of every sampled event, FP64 Fisher of the detected ones'},
+        'speedup_vs_plain_fp64_path': rate_s / rate_p,
         'detected': int(det_s.sum()),
-        'recall_vs_exact_path': float(np.mean(det_s[det_p])) if det_p.any() else None,
-        'false_detections': int(np.sum(det_s & ~det_p)),
+        'recall_vs_exact_path_on_sample': float(np.mean(det_s[samp][det_p])) if det_p.any() else None,
+        'false_detections_on_sample': int(np.sum(det_s[samp] & ~det_p)),
+        'sigma_err_vs_fp64_on_sample': {'events_cond_lt_1e13': int(ok.sum()),
+                                        'median': float(np.median(err[ok])) if ok.any() else None,
+                                        'max': float(err[ok].max()) if ok.any() else None,
+                                        'events_cond_ge_1e13': int((~ok).sum())},
     }
+
+
+def run_screen(args):
+    line = measure_screen(args.events if args.events != N_EVENTS else 1000000, args.train_events, args.train_epochs,
+                          args.steps, args.warmup)
+    line.update({'n_gpus': 1, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+                 'data': 'synthetic (seeded population, dL up to 30 Gpc)'})
     print(json.dumps(line))
 
 
-def run_hm(args):
+def measure_hm(n_events, steps, warmup, refine_cond=1e13, fp64_sample=8192):
     """Higher-mode workload: IMRPhenomHM (modes 21, 22, 32, 33, 43, 44) aligned-spin BBH, m1 power law
     on [5, 150] Msun, q ~ U[0.1, 1], chi ~ U[-0.9, 0.9], dL ~ U[0.5, 20] Gpc; ET triangle + CE1Id +
     CE2NM (5 Hz walls), Earth rotation, R = 4000. Device-resident events; the FP32 split-precision
     form (FP64 mode phases) and the mixed form over all events, the FP64 kernel over the first
-    10^4 (i.i.d. events, so the per-event rate carries over); sigma errors of both forms against the
-    FP64 kernel on the first 4096 events."""
+    fp64_sample (i.i.d. events, so the per-event rate carries over); sigma errors of both forms against
+    the FP64 kernel on the first 4096 events; SNR/s of the FP64 and FP32 SNR kernels."""
     import torch
     from gwfast_gb300 import _build, _lib, fisherTools, synthetic
     from gwfast_gb300 import waveforms as W
     from gwfast_gb300.signal import event_array
     _build.build()
     dev = torch.device('cuda', 0)
-    N = args.events if args.events != N_EVENTS else 100000
+    N = n_events
     R = 4000
     ev = synthetic.bbh_events(N, seed=1003, mmax=150., qmin=0.1, chimax=0.9, dl=(0.5, 20.))
     wf = W.IMRPhenomHM()
     net = synthetic.make_network(wf, dets=synthetic.NETWORK_ET_CE, earth=True)
     ids = [s.det_id for s in net.signals.values()]
     ctx = _lib.context(0)
-    ctx.set_refine_cond(args.refine_cond)
+    ctx.set_refine_cond(refine_cond)
     p_dev = torch.from_numpy(event_array(ev)).to(dev)
     out = torch.empty((N, 11, 11), dtype=torch.float64, device=dev)
+    snr_out = torch.empty((N,), dtype=torch.float64, device=dev)
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
     desc = wf.gpu_desc()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    timed = _timed_stream(torch, stream, flush)
 
     def step(precision, n, o=out):
         ctx.fisher(ids, desc, p_dev, R, per_arm=False, mem=_lib.MEM_DEVICE, out_net=o, stream=stream.cuda_stream,
                    ld=N, n=n, precision=precision)
 
-    def timed(fn, k, warm):
-        for _ in range(warm):
-            fn()
-        tot = 0.0
-        for _ in range(k):
-            flush.zero_()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            fn()
-            e1.record(stream)
-            e1.synchronize()
-            tot += e0.elapsed_time(e1)
-        return tot / k
-
-    n64 = min(N, 10000)
+    n64 = min(N, fp64_sample)
     clk = ClockSampler(0)
-    ms32 = timed(lambda: step('fp32', N), args.steps, args.warmup)
-    msmix = timed(lambda: step('mixed', N), args.steps, args.warmup)
-    ms64 = timed(lambda: step('fp64', n64), max(1, args.steps // 2), 1)
+    ms32 = timed(lambda: step('fp32', N), steps, warmup)
+    msmix = timed(lambda: step('mixed', N), steps, warmup)
+    ms64 = timed(lambda: step('fp64', n64), max(1, steps // 2), 1)
+    ms_snr = timed(lambda: ctx.snr(ids, desc, p_dev, R, mem=_lib.MEM_DEVICE, out_net=snr_out,
+                                   stream=stream.cuda_stream, ld=N, n=N), steps, warmup)
+    ms_snr32 = timed(lambda: ctx.snr(ids, desc, p_dev, R, mem=_lib.MEM_DEVICE, out_net=snr_out,
+                                     stream=stream.cuda_stream, ld=N, n=N, precision='fp32'), steps, warmup)
     clocks = clk.stop()
     ns = min(N, 4096)
     F = {}
@@ -374,21 +429,24 @@ def run_hm(args):
                       'max_cond_lt_1e13': float(w[stable].max()), 'events_cond_lt_1e13': int(stable.sum()),
                       'events': int(ns), 'frac_le_1e-3': float(np.mean(w <= 1e-3))}
     rate64 = n64 / (ms64 / 1e3)
-    line = {
+    return {
         'metric': 'network Fisher matrices/s, IMRPhenomHM on ET + 2 CE (mixed form vs plain FP64 kernel)',
-        'value': N / (msmix / 1e3), 'unit': 'Fisher/s', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
-        'ms_per_step': msmix, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
-        'dtype': 'f64 mode phases, f32 amplitudes/tangents/mode sums, f64 for events with cond > %.0e'
-                 % args.refine_cond,
-        'data': 'synthetic (seeded BBH catalogue)',
+        'value': N / (msmix / 1e3), 'unit': 'Fisher/s', 'ms_per_step': msmix,
+        'dtype': 'f64 mode phases, f32 amplitudes/tangents/mode sums, f64 for events with cond > %.0e' % refine_cond,
         'config': {'workload': 'IMRPhenomHM, %d BBH, ETS + CE1Id + CE2NM (5 Hz), Earth rotation, R=%d' % (N, R),
-                   'l2': 'flushed (256 MB write) before every step'},
+                   'l2': 'flushed (256 MB write) before every step', 'fp64_sampled_events': n64},
         'fisher_per_s': {'mixed': N / (msmix / 1e3), 'fp32': N / (ms32 / 1e3), 'fp64': rate64},
-        'fp64_timed_on_events': n64,
         'speedup_mixed_vs_fp64': (N / (msmix / 1e3)) / rate64,
+        'snr_per_s': {'fp64': N / (ms_snr / 1e3), 'fp32': N / (ms_snr32 / 1e3)},
         'sigma_err_vs_fp64': errs,
         'clocks': clocks,
     }
+
+
+def run_hm(args):
+    line = measure_hm(args.events if args.events != N_EVENTS else 100000, args.steps, args.warmup, args.refine_cond)
+    line.update({'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup, 'higher_is_better': True,
+                 'scaling': 'weak', 'vs_baseline': None, 'data': 'synthetic (seeded BBH catalogue)'})
     print(json.dumps(line))
 
 
@@ -408,6 +466,7 @@ def main():
     ap.add_argument('--workload', default='lhet', choices=('lhet', 'mixed-catalogue', 'screen', 'hm'),
                     help='lhet: the headline workload; mixed-catalogue: the batching workload; screen: the learned '
                          'SNR screen on a 10^6-event population; hm: IMRPhenomHM on ET + CE (separate lines)')
+    ap.add_argument('--headline-only', action='store_true', help='leave out the other workloads\' keys')
     ap.add_argument('--train-events', type=int, default=200000)
     ap.add_argument('--train-epochs', type=int, default=40)
     args = ap.parse_args()
@@ -508,6 +567,27 @@ def main():
     # L1 + H1 share the grid: one group launch, the largest share of the step's GPU time
     ms_grp = timed(lambda: fisher_step(ids[:2], o=out32, precision='fp32'), args.steps)
     ms_et64 = timed(lambda: fisher_step([ids[2]], precision='fp64'), max(1, args.steps // 2))
+    # kernel-only times: the library's CUDA events around its own launches (the set-up launches of a
+    # chunk, each Fisher launch), on the stream each ran on; median over steps of the per-call sums
+    ctx.set_kernel_timing(True)
+
+    def sections(fn, k):
+        per = {}
+        for _ in range(k):
+            flush.zero_()
+            fn()
+            tot = {}
+            for name, t in ctx.kernel_times():
+                tot[name] = tot.get(name, 0.0) + t
+            for name, t in tot.items():
+                per.setdefault(name, []).append(t)
+        return {name: statistics.median(v) for name, v in per.items()}
+
+    kt_grp = sections(lambda: fisher_step(ids[:2], o=out32, precision='fp32'), args.steps)
+    kt_et = sections(lambda: fisher_step([ids[2]], o=out32, precision='fp32'), args.steps)
+    kt_et64 = sections(lambda: fisher_step([ids[2]], precision='fp64'), max(1, args.steps // 2))
+    kt_mixed = sections(fisher_step, args.steps)
+    ctx.set_kernel_timing(False)
     if world > 1:
         t = torch.tensor([ms, ms64, ms32, ms_snr], dtype=torch.float64, device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -579,11 +659,12 @@ def main():
     flops_grp = N * RES * 2 * flop_arm_pt
     peak32 = gemm_peak(torch, dev, torch.float32, 8192)
     peak64 = gemm_peak(torch, dev, torch.float64, 4096)
-    ach = flops_et / (ms_et / 1e3) / 1e12
-    ach_grp = flops_grp / (ms_grp / 1e3) / 1e12
-    ach64 = flops_et / (ms_et64 / 1e3) / 1e12
-    call_note = ('CUDA events around the whole call for that detector set (per-event set-up launches and the '
-                 'Fisher launch), so achieved is a lower bound for the kernel itself')
+    k_grp, k_et, k_et64 = kt_grp['group_f32'], kt_et['fisher_f32'], kt_et64['fisher_f64']
+    ach = flops_et / (k_et / 1e3) / 1e12
+    ach_grp = flops_grp / (k_grp / 1e3) / 1e12
+    ach64 = flops_et / (k_et64 / 1e3) / 1e12
+    kernel_note = ('CUDA events recorded by the library around this one launch on its stream (gwf_kernel_times), '
+                   'median over steps; the L2 is flushed before each call')
     line = {
         'metric': METRIC, 'value': world * N / (ms / 1e3), 'unit': 'Fisher/s', 'n_gpus': world, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
@@ -619,24 +700,37 @@ def main():
                               'h2d_bytes': int(8 * 11 * (N + ndet)), 'd2h_bytes': int(8 * (5 * N + 121 * ndet))},
         'roofline': {'bound': 'fp32', 'kernel': 'fisher_group_kernel_f32<IMRPhenomD, earth, no triangle> (L1+H1)',
                      'achieved': ach_grp, 'peak': peak32, 'unit': 'TFLOP/s', 'frac': ach_grp / peak32,
-                     'peak_source': 'cuBLAS SGEMM 8192^3 (TF32 off) measured in this run',
-                     'algorithmic_flop_per_launch': flops_grp, 'call_ms': ms_grp, 'timing': call_note,
-                     'traffic': None,
+                     'peak_source': 'cuBLAS SGEMM 8192^3 (TF32 off) measured in this run (MEASURED_PEAKS.json has '
+                                    'no FP32 CUDA-core figure)',
+                     'algorithmic_flop_per_launch': flops_grp, 'kernel_ms': k_grp, 'timing': kernel_note,
+                     'traffic': GRP_DRAM_BYTES_PER_EVENT * N,
+                     'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one 2048-event launch '
+                                       '(profiles/fisher_group_f32_phenomd_l1h1.md), scaled by events',
                      'flop_model': 'profiles/opcounts.json IMRPhenomD/earth fisher_per_arm_point x 2 arms x R x N'},
         'roofline_triangle': {'bound': 'fp32', 'kernel': 'fisher_kernel_f32<IMRPhenomD, earth, triangle>',
                               'achieved': ach, 'peak': peak32, 'unit': 'TFLOP/s', 'frac': ach / peak32,
-                              'algorithmic_flop_per_launch': flops_et, 'call_ms': ms_et, 'timing': call_note,
+                              'algorithmic_flop_per_launch': flops_et, 'kernel_ms': k_et, 'timing': kernel_note,
                               'traffic': 3.49e6 * N / 1024,
                               'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of a 1024-event '
                                                 'launch (3.49 MB, profiles/fisher_f32_phenomd_ets.md), scaled by events',
                               'flop_model': 'profiles/opcounts.json IMRPhenomD/earth fisher_per_arm_point x 3 arms x R x N'},
         'roofline_fp64': {'bound': 'fp64', 'kernel': 'fisher_kernel<IMRPhenomD, earth, triangle>', 'achieved': ach64,
-                          'peak': peak64, 'unit': 'TFLOP/s', 'frac': ach64 / peak64, 'call_ms': ms_et64, 'timing': call_note,
-                          'peak_source': 'cuBLAS DGEMM 4096^3 measured in this run'},
+                          'peak': peak64, 'unit': 'TFLOP/s', 'frac': ach64 / peak64, 'kernel_ms': k_et64,
+                          'timing': kernel_note, 'peak_source': 'cuBLAS DGEMM 4096^3 measured in this run'},
         'call_ms': {'L1': ms_l1, 'L1+H1': ms_grp, 'ETS': ms_et},
+        'kernel_ms': {'L1+H1 FP32 call': kt_grp, 'ETS FP32 call': kt_et, 'ETS FP64 call': kt_et64,
+                      'mixed step': kt_mixed,
+                      'what': 'per call, summed by section: setup = FP64 set-up + FP32 record launches of each chunk; '
+                              'in the mixed step the two detector groups run side by side, so sections overlap'},
         'clocks': clocks,
         'hbm_peak_gbs': measured_peaks().get('hbm_gbs'),
     }
+    if world == 1 and not args.headline_only:
+        # the other workloads as keys of the same line (each its own synthetic catalogue; plain FP64
+        # arms on samples of the same catalogue, as stated in each)
+        line['config4_north_star'] = measure_screen(1000000, args.train_events, args.train_epochs, 2, 1)
+        line['config2_mixed_catalogue'] = measure_mixed_catalogue(100000, 2, 1, args.refine_cond)
+        line['config3_phenomhm'] = measure_hm(100000, 2, 1, args.refine_cond)
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, _ = cpu_sample(args.ref_events, RES, threads)
