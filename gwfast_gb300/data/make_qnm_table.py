@@ -24,4 +24,6 @@ def main(src_dir):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference/WFfiles')
+    if len(sys.argv) != 2:
+        sys.exit('usage: python make_qnm_table.py <gwfast checkout>/WFfiles')
+    main(sys.argv[1])

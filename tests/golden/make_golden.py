@@ -21,7 +21,7 @@ numpy 2 removed ``trapz`` and ``NaN`` and scipy removed ``cumtrapz``; aliases to
 ``trapezoid``/``nan``/``cumulative_trapezoid`` are installed for the reference's calls.
 
 The outputs are written to ``tests/golden/*.npz`` and committed; the GPU machine
-never needs the reference.  Run:  python tests/golden/make_golden.py [/root/reference] [part ...]
+never needs the reference.  Run:  python tests/golden/make_golden.py <gwfast checkout> [part ...]
 (with parts, e.g. ``overlap``, only those ``make_<part>()`` run).
 """
 import os
@@ -30,7 +30,9 @@ import types
 
 import numpy as np
 
-REF = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+if __name__ == '__main__' and len(sys.argv) < 2:
+    sys.exit('usage: python make_golden.py <gwfast checkout> [part ...]')
+REF = sys.argv[1] if len(sys.argv) > 1 else None
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 
