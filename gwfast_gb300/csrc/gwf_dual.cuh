@@ -178,6 +178,60 @@ template <class T, int N> __host__ __device__ __forceinline__ void dsincos(const
   *s = chain(a, sv, cv); *c = chain(a, cv, -sv);
 }
 
+// ---- Dual<float, 4> on sm_100 and later: the four tangent lanes as two packed FP32x2 pairs, so an
+// addition or product of duals issues two instructions for the tangent instead of four. Each lane is
+// rounded exactly as the scalar operation (round to nearest); these overloads are more specialised
+// than the templates above and take precedence in device code.
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+__device__ __forceinline__ float2 dq01(const Dual<float, 4>& a) { return make_float2(a.d[0], a.d[1]); }
+__device__ __forceinline__ float2 dq23(const Dual<float, 4>& a) { return make_float2(a.d[2], a.d[3]); }
+__device__ __forceinline__ void dset(Dual<float, 4>& r, float2 lo, float2 hi) {
+  r.d[0] = lo.x; r.d[1] = lo.y; r.d[2] = hi.x; r.d[3] = hi.y;
+}
+__device__ __forceinline__ Dual<float, 4> operator+(const Dual<float, 4>& a, const Dual<float, 4>& b) {
+  Dual<float, 4> r; r.v = a.v + b.v;
+  dset(r, __fadd2_rn(dq01(a), dq01(b)), __fadd2_rn(dq23(a), dq23(b)));
+  return r;
+}
+__device__ __forceinline__ Dual<float, 4> operator-(const Dual<float, 4>& a, const Dual<float, 4>& b) {
+  Dual<float, 4> r; r.v = a.v - b.v;
+  dset(r, __fadd2_rn(dq01(a), make_float2(-b.d[0], -b.d[1])), __fadd2_rn(dq23(a), make_float2(-b.d[2], -b.d[3])));
+  return r;
+}
+__device__ __forceinline__ Dual<float, 4> operator*(const Dual<float, 4>& a, const Dual<float, 4>& b) {
+  Dual<float, 4> r; r.v = a.v * b.v;
+  const float2 av = make_float2(a.v, a.v), bv = make_float2(b.v, b.v);
+  dset(r, __ffma2_rn(dq01(a), bv, __fmul2_rn(av, dq01(b))), __ffma2_rn(dq23(a), bv, __fmul2_rn(av, dq23(b))));
+  return r;
+}
+__device__ __forceinline__ Dual<float, 4> operator/(const Dual<float, 4>& a, const Dual<float, 4>& b) {
+  Dual<float, 4> r; const float ib = 1.0f / b.v; r.v = a.v * ib;
+  const float2 nv = make_float2(-r.v, -r.v), i2 = make_float2(ib, ib);
+  dset(r, __fmul2_rn(__ffma2_rn(nv, dq01(b), dq01(a)), i2), __fmul2_rn(__ffma2_rn(nv, dq23(b), dq23(a)), i2));
+  return r;
+}
+__device__ __forceinline__ Dual<float, 4> operator*(const Dual<float, 4>& a, float b) {
+  Dual<float, 4> r; r.v = a.v * b;
+  const float2 b2 = make_float2(b, b);
+  dset(r, __fmul2_rn(dq01(a), b2), __fmul2_rn(dq23(a), b2));
+  return r;
+}
+__device__ __forceinline__ Dual<float, 4> operator*(float b, const Dual<float, 4>& a) { return a * b; }
+__device__ __forceinline__ Dual<float, 4> operator/(float a, const Dual<float, 4>& b) {
+  Dual<float, 4> r; const float ib = 1.0f / b.v; r.v = a * ib;
+  const float s = -r.v * ib;
+  const float2 s2 = make_float2(s, s);
+  dset(r, __fmul2_rn(dq01(b), s2), __fmul2_rn(dq23(b), s2));
+  return r;
+}
+__device__ __forceinline__ Dual<float, 4> chain(const Dual<float, 4>& a, float fv, float fp) {
+  Dual<float, 4> r; r.v = fv;
+  const float2 f2 = make_float2(fp, fp);
+  dset(r, __fmul2_rn(dq01(a), f2), __fmul2_rn(dq23(a), f2));
+  return r;
+}
+#endif
+
 // select helper that keeps plain and dual code identical
 template <class X> __host__ __device__ __forceinline__ X sel(bool c, const X& a, const X& b) { return c ? a : b; }
 

@@ -27,9 +27,15 @@
 
 namespace gwf {
 
-struct cf { float re, im; };
-__device__ __forceinline__ cf fadd(cf a, cf b) { return {a.re + b.re, a.im + b.im}; }
-__device__ __forceinline__ cf fscale(cf a, float s) { return {a.re * s, a.im * s}; }
+// Complex FP32 values as register pairs: additions and real scalings run as packed FP32x2
+// instructions (one instruction for the real and the imaginary part, IEEE round-to-nearest each)
+struct __align__(8) cf { float re, im; };
+__device__ __forceinline__ float2 f2_of(cf a) { return make_float2(a.re, a.im); }
+__device__ __forceinline__ cf cf_of(float2 v) { return {v.x, v.y}; }
+__device__ __forceinline__ cf fadd(cf a, cf b) { return cf_of(__fadd2_rn(f2_of(a), f2_of(b))); }
+__device__ __forceinline__ cf fscale(cf a, float s) { return cf_of(__fmul2_rn(f2_of(a), make_float2(s, s))); }
+// a s + c
+__device__ __forceinline__ cf ffma2(cf a, float s, cf c) { return cf_of(__ffma2_rn(f2_of(a), make_float2(s, s), f2_of(c))); }
 __device__ __forceinline__ cf fmuli(cf a) { return {-a.im, a.re}; }
 
 struct ProjF {
@@ -68,19 +74,24 @@ __device__ inline void projf_setup(ProjF& q, const ProjEv& p, double sz) {
   q.sgn = p.ci >= 0.0 ? 1.0f : -1.0f;
 }
 
-// delay and sin/cos x at t_noloc = tcoal + delta (days); x = ra - lon - 2 pi t (gwfast/signal.py:401-423)
-__device__ __forceinline__ void time_f(const ProjF& q, float delta, TimeF& ts) {
-  float sd, cd;
-  sincosf(6.2831853071795865f * delta, &sd, &cd);
+// delay and sin/cos x at t_noloc = tcoal + delta (days); x = ra - lon - 2 pi t (gwfast/signal.py:401-423).
+// (sd, cd) = sin, cos of the Earth-rotation angle 2 pi delta, which does not depend on the detector.
+// The rotation by the delay D (|D| <= R_earth / c = 0.0213 s, an angle below 1.6e-6 rad) is taken as
+// sin = angle, cos = 1: in FP32 those are the correctly rounded values of sin and cos of such an angle.
+__device__ __forceinline__ void time_f_rot(const ProjF& q, float sd, float cd, TimeF& ts) {
   const float su = q.sU0 * cd + q.cU0 * sd, cu = q.cU0 * cd - q.sU0 * sd;
   ts.D = -q.Rc * (q.cdcl * cu + q.sdsl);
   ts.D_th = q.Rc * (q.cdsl - q.sdcl * cu);
   ts.D_ph = -q.Rc * q.cdcl * su;
   ts.D_t = 6.2831853071795865f * q.Rc * q.cdcl * su;
-  float se, ce;
-  sincosf(6.2831853071795865f * ts.D * (1.0f / 86400.0f), &se, &ce);
-  ts.sx = -(su * ce + cu * se);
-  ts.cx = cu * ce - su * se;
+  const float se = 6.2831853071795865f * ts.D * (1.0f / 86400.0f);
+  ts.sx = -(su + cu * se);
+  ts.cx = cu - su * se;
+}
+__device__ __forceinline__ void time_f(const ProjF& q, float delta, TimeF& ts) {
+  float sd, cd;
+  sincosf(6.2831853071795865f * delta, &sd, &cd);
+  time_f_rot(q, sd, cd, ts);
 }
 
 __device__ __forceinline__ void arm_f(const ProjF& q, const TimeF& ts, int arm, ArmF& ap) {
@@ -114,29 +125,29 @@ __device__ __forceinline__ void arm_derivs_f(const ProjF& q, const ArmF& ap, con
                                              const cf* dP, const cf* dC, cf dPi, cf dCi, const float* dtn, cf* out) {
   const float tp = 6.2831853071795865f;
   const cf hp = P, hc = fmuli(C);
-  const cf H = fadd(fscale(hp, ap.Fp), fscale(hc, ap.Fc));
+  const cf H = ffma2(hp, ap.Fp, fscale(hc, ap.Fc));
   const cf iH = fmuli(H);
   const float tpf = tp * f;
   const float G = 1.0f + ts.D_t * (1.0f / 86400.0f);
   const float x_th = -tp * ts.D_th * (1.0f / 86400.0f);
   const float x_ph = 1.0f - tp * ts.D_ph * (1.0f / 86400.0f);
   const float x_tc = -tp * G;
-  const cf hx = fadd(fscale(hp, ap.Fp_x), fscale(hc, ap.Fc_x));
-  const cf hd = fadd(fscale(hp, ap.Fp_d), fscale(hc, ap.Fc_d));
+  const cf hx = ffma2(hp, ap.Fp_x, fscale(hc, ap.Fc_x));
+  const cf hd = ffma2(hp, ap.Fp_d, fscale(hc, ap.Fc_d));
   const int map[4] = {I_MC, I_ETA, I_C1, I_C2};
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    cf v = fadd(fscale(fmuli(dC[k]), ap.Fc), fscale(dP[k], ap.Fp));
-    v = fadd(v, fscale(hx, -tp * G * dtn[k]));
-    v = fadd(v, fscale(iH, tpf * ts.D_t * dtn[k]));
+    cf v = ffma2(fmuli(dC[k]), ap.Fc, fscale(dP[k], ap.Fp));
+    v = ffma2(hx, -tp * G * dtn[k], v);
+    v = ffma2(iH, tpf * ts.D_t * dtn[k], v);
     out[map[k]] = v;
   }
-  out[I_IO] = fadd(fscale(dPi, ap.Fp), fscale(fmuli(dCi), ap.Fc));
+  out[I_IO] = ffma2(dPi, ap.Fp, fscale(fmuli(dCi), ap.Fc));
   out[I_DL] = fscale(H, -q.idL);
-  out[I_TH] = fadd(fadd(fscale(hx, x_th), fscale(hd, -1.0f)), fscale(iH, tpf * ts.D_th));
-  out[I_PH] = fadd(fscale(hx, x_ph), fscale(iH, tpf * ts.D_ph));
-  out[I_PS] = fadd(fscale(hp, ap.Fp_s), fscale(hc, ap.Fc_s));
-  out[I_TC] = fadd(fscale(hx, x_tc * (1.0f / 86400.0f)), fscale(iH, tpf * G));
+  out[I_TH] = ffma2(iH, tpf * ts.D_th, ffma2(hx, x_th, fscale(hd, -1.0f)));
+  out[I_PH] = ffma2(hx, x_ph, fscale(iH, tpf * ts.D_ph));
+  out[I_PS] = ffma2(hp, ap.Fp_s, fscale(hc, ap.Fc_s));
+  out[I_TC] = ffma2(hx, x_tc * (1.0f / 86400.0f), fscale(iH, tpf * G));
   out[I_PC] = fscale(iH, -1.0f);
 }
 
@@ -189,24 +200,33 @@ __device__ inline void pbf_fill(const PhaseBasis& src, PBF& b, double alpha) {
 // compensated sum of NB basis terms: each product hi * basis is split exactly into p + e (FMA), p
 // is added to the running sum with an exact two-sum, and every rounding error goes to the low-order
 // sum. The terms cancel strongly (the result can be far smaller than the largest term), so a plain
-// FP32 sum would carry an error of an ulp of the largest partial sum.
+// FP32 sum would carry an error of an ulp of the largest partial sum. The four tangent directions run
+// as two packed FP32x2 pairs (each lane of a pair rounded exactly as the scalar operation).
+__device__ __forceinline__ float2 fneg2(float2 a) { return make_float2(-a.x, -a.y); }
 template <int NB>
 __device__ __forceinline__ void phase_terms(const PBF& b, int off, const float (&bas)[NB], float* sh, float* sl) {
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    float h_ = 0.0f, l_ = 0.0f;
+  for (int hq = 0; hq < 2; ++hq) {
+    float2 h_ = make_float2(0.0f, 0.0f), l_ = make_float2(0.0f, 0.0f);
 #pragma unroll
     for (int j = 0; j < NB; ++j) {
-      const float h = b.hi[off + j][q];
-      const float p = h * bas[j];
-      const float e = fmaf(h, bas[j], -p);
-      const float t = h_ + p, bp = t - h_;
-      l_ += ((h_ - (t - bp)) + (p - bp)) + e;
+      const float2 h = *reinterpret_cast<const float2*>(&b.hi[off + j][2 * hq]);
+      const float2 lo = *reinterpret_cast<const float2*>(&b.lo[off + j][2 * hq]);
+      const float2 bj = make_float2(bas[j], bas[j]);
+      const float2 p = __fmul2_rn(h, bj);
+      const float2 e = __ffma2_rn(h, bj, fneg2(p));
+      const float2 t = __fadd2_rn(h_, p);
+      const float2 bp = __fadd2_rn(t, fneg2(h_));
+      const float2 a1 = __fadd2_rn(h_, fneg2(__fadd2_rn(t, fneg2(bp))));
+      const float2 a2 = __fadd2_rn(p, fneg2(bp));
+      l_ = __fadd2_rn(l_, __fadd2_rn(__fadd2_rn(a1, a2), e));
       h_ = t;
-      l_ = fmaf(b.lo[off + j][q], bas[j], l_);
+      l_ = __ffma2_rn(lo, bj, l_);
     }
-    sh[q] = h_;
-    sl[q] = l_;
+    sh[2 * hq] = h_.x;
+    sh[2 * hq + 1] = h_.y;
+    sl[2 * hq] = l_.x;
+    sl[2 * hq + 1] = l_.y;
   }
 }
 
@@ -317,10 +337,10 @@ __device__ __forceinline__ void wave_f32(const EvUnionF& EF, const PBF& pbf, con
 // directly keeps its FP32 relative accuracy (the Gram of the original columns is restored in FP64
 // at the end).
 template <bool EARTH, int NARM>
-__device__ __forceinline__ void project_f32(const WaveF& w, const ProjF& pf, const ArmF* apc, const TimeF& tsc, float f,
-                                            cf (&D)[NARM][NP], cf (&H)[NARM]) {
+__device__ __forceinline__ void project_f32_rot(const WaveF& w, const ProjF& pf, const ArmF* apc, const TimeF& tsc,
+                                                float f, float sd, float cd, cf (&D)[NARM][NP], cf (&H)[NARM]) {
   TimeF ts;
-  if (EARTH) time_f(pf, -w.tau * (1.0f / 86400.0f), ts);
+  if (EARTH) time_f_rot(pf, sd, cd, ts);
   else ts = tsc;
 #pragma unroll
   for (int a = 0; a < NARM; ++a) {
@@ -330,8 +350,21 @@ __device__ __forceinline__ void project_f32(const WaveF& w, const ProjF& pf, con
     arm_derivs_f(pf, ap, ts, f, w.P, w.C, w.dP, w.dC, w.dPi, w.dCi, w.dtn, D[a]);
     const float wr = ap.Fc, wi = pf.sgn * ap.Fp;
     D[a][I_PS] = {2.0f * (w.Q.re * wr - w.Q.im * wi), 2.0f * (w.Q.re * wi + w.Q.im * wr)};
-    H[a] = fadd(fscale(w.P, ap.Fp), fscale(fmuli(w.C), ap.Fc));   // the strain (common phase dropped)
+    H[a] = ffma2(w.P, ap.Fp, fscale(fmuli(w.C), ap.Fc));   // the strain (common phase dropped)
   }
+}
+
+// sin and cos of the point's Earth-rotation angle 2 pi delta, delta = -tau_star / day
+__device__ __forceinline__ void rot_sc(const WaveF& w, float& sd, float& cd) {
+  sincosf(6.2831853071795865f * (-w.tau * (1.0f / 86400.0f)), &sd, &cd);
+}
+
+template <bool EARTH, int NARM>
+__device__ __forceinline__ void project_f32(const WaveF& w, const ProjF& pf, const ArmF* apc, const TimeF& tsc, float f,
+                                            cf (&D)[NARM][NP], cf (&H)[NARM]) {
+  float sd = 0.0f, cd = 1.0f;
+  if (EARTH) rot_sc(w, sd, cd);
+  project_f32_rot<EARTH, NARM>(w, pf, apc, tsc, f, sd, cd, D, H);
 }
 
 template <int MODEL, bool EARTH, int NARM>
@@ -974,6 +1007,8 @@ __device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32S
       if constexpr (MODEL == 2) wave_f32_hm<EARTH>(r.ef, r.pf, f, wv);
       else wave_f32<MODEL, EARTH>(r.ef, r.pbf, r.pf, f, lnf, wv);
     }
+    float sd = 0.0f, cd = 1.0f;   // the Earth-rotation angle is the same for every detector
+    if (EARTH && valid) rot_sc(wv, sd, cd);
     for (int d = 0; d < nd; ++d) {
       const DetDev& det = g.det[d];
       float sw = 0.0f;
@@ -981,14 +1016,14 @@ __device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32S
       cf u[NP];
       if (!TRI || det.shape == 0) {
         cf D[1][NP], Hs[1];
-        if (valid) project_f32<EARTH, 1>(wv, gp.pf[d], gp.apc[d], gp.tsc[d], f, D, Hs);
+        if (valid) project_f32_rot<EARTH, 1>(wv, gp.pf[d], gp.apc[d], gp.tsc[d], f, sd, cd, D, Hs);
 #pragma unroll
         for (int q = 0; q < NP; ++q) u[q] = valid ? fscale(D[0][q], sw) : cf{0.0f, 0.0f};
         add(u);
       } else {
         // triangle total: G(U) + G(V) + G(U+V) = G(sqrt(3/2)(U+V)) + G(sqrt(1/2)(U-V))
         cf D[2][NP], Hs[2];
-        if (valid) project_f32<EARTH, 2>(wv, gp.pf[d], gp.apc[d], gp.tsc[d], f, D, Hs);
+        if (valid) project_f32_rot<EARTH, 2>(wv, gp.pf[d], gp.apc[d], gp.tsc[d], f, sd, cd, D, Hs);
 #pragma unroll
         for (int q = 0; q < NP; ++q) u[q] = valid ? fscale(fadd(D[0][q], D[1][q]), sw * 1.2247448713915890f) : cf{0.0f, 0.0f};
         add(u);
