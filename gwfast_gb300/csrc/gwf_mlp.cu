@@ -1,8 +1,12 @@
 // Learned SNR screen: a small MLP that predicts ln(network SNR) of an event from its parameters,
-// trained on SNRs that the exact kernels produce. Everything runs on the GPU: feature map, tiled
-// GEMM forward and backward passes with fused bias / SiLU epilogues, mean-squared-error loss,
-// Adam. Weights are kept in FP32 (the optimiser's copy) and used in BF16 by both passes; all
-// arithmetic accumulates in FP32.
+// trained on SNRs that the exact kernels produce. Everything runs on the GPU: feature map, GEMM
+// forward and backward passes with fused bias / SiLU epilogues, mean-squared-error loss, Adam.
+// Weights are kept in FP32 (the optimiser's copy) and used in BF16 by both passes; all arithmetic
+// accumulates in FP32. The hidden-to-hidden layers (both widths multiples of 16, at most 256) run on
+// the tensor cores (gwf_umma.cuh: tcgen05.mma kind::f16, FP32 accumulation in tensor memory): their
+// forward product, weight gradient and input gradient take BF16 operands, i.e. the activations and
+// back-propagated gradients are rounded to BF16 where they enter those products. The input layer
+// (11 features) and the output layer (width 1) run on the CUDA cores in FP32 with BF16 weights.
 //
 // Layout: layer l maps A_l [batch][K_l] to Z_l = A_l W_l + b_l, W_l [K_l][M_l] row-major;
 // A_{l+1} = SiLU(Z_l) for the hidden layers, the last layer (M = 1) is linear.
@@ -21,6 +25,7 @@
 #include <vector>
 
 #include "gwf_launch.h"
+#include "gwf_umma.cuh"
 #include "gwfast_gb300.h"
 
 namespace gwf {
@@ -248,6 +253,8 @@ struct gwf_mlp {
   Buf w32, wbf, grad, adam_m, adam_v, norm;   // norm: mean[11], inv_std[11]
   Buf X, T, xb, tb, dy, loss, pred;            // data, batch, loss
   std::vector<Buf> act, pre, dact;             // per layer activations, pre-activations, gradients
+  Buf tc_err;                                  // set by a tensor-core GEMM whose MMA wait timed out
+  Buf tc_ws;                                   // split-K partial sums of the tensor-core weight gradients
   long long adam_t = 0;
   bool have_norm = false;
 };
@@ -262,7 +269,55 @@ cudaError_t gemm(cudaStream_t st, int M, int N, int K, const float* A, int lda, 
   return cudaGetLastError();
 }
 
+// C = op(A) op(B) (+ bias, SiLU) on the tensor cores (N a multiple of 16, at most 256). A long
+// reduction (K well above the tile's rows, the weight gradients over a batch) with few row tiles is
+// split over K into `ws` (splits x M x N floats, contiguous C with ldc = N, no bias or activation)
+// and reduced in split order.
+template <class TBE, bool TA, bool TB>
+cudaError_t gemm_tc(cudaStream_t st, int M, int N, int K, const float* A, int lda, const TBE* B, int ldb, float* C,
+                    int ldc, const float* bias, int act, float* Z, int* err, Buf* ws = nullptr) {
+  auto k = gwf::umma::gemm_tc_kernel<TA, TB, TBE>;
+  const int smem = gwf::umma::smem_bytes();
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  const unsigned mt = nblk(M, gwf::umma::kUM);
+  int splits = 1;
+  if (ws && !bias && act == 0 && !Z && ldc == N && mt < 32 && K >= 4 * gwf::umma::kUK) {
+    splits = (int)std::min<long long>(64 / mt, (K + 2 * gwf::umma::kUK - 1) / (2 * gwf::umma::kUK));
+    if (splits < 1) splits = 1;
+  }
+  if (splits > 1) {
+    const int kspan = (int)((((long long)K + splits - 1) / splits + gwf::umma::kUK - 1) / gwf::umma::kUK) * gwf::umma::kUK;
+    splits = (K + kspan - 1) / kspan;
+    if (!ws->ensure((size_t)splits * M * N * sizeof(float))) return cudaErrorMemoryAllocation;
+    k<<<dim3(mt, (unsigned)splits), 128, smem, st>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, act, Z, kspan,
+                                                   ws->as<float>(), err);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    gwf::umma::splitk_reduce_kernel<<<nblk((long long)M * N, 256), 256, 0, st>>>(ws->as<float>(), splits,
+                                                                                 (long long)M * N, C);
+    return cudaGetLastError();
+  }
+  k<<<dim3(mt, 1), 128, smem, st>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, act, Z, K, nullptr, err);
+  return cudaGetLastError();
+}
+
 int n_layers(const gwf_mlp* m) { return (int)m->dims.size() - 1; }
+
+// the hidden-to-hidden layers run on the tensor cores
+bool tc_layer(const gwf_mlp* m, int l) {
+  const int L = n_layers(m), K = m->dims[l], M = m->dims[l + 1];
+  return l >= 1 && l <= L - 2 && K % 16 == 0 && M % 16 == 0 && M <= gwf::umma::kUNMax;
+}
+
+// report a tensor-core GEMM whose wait for its MMAs gave up (waits on the stream)
+int check_tc(gwf_mlp* m) {
+  int v = 0;
+  MLP_CK(cudaMemcpyAsync(&v, m->tc_err.p, sizeof v, cudaMemcpyDeviceToHost, m->stream));
+  MLP_CK(cudaStreamSynchronize(m->stream));
+  if (v) return fail(GWF_ERR_TIMEOUT, "MLP tensor-core GEMM: MMA completion wait timed out");
+  return GWF_OK;
+}
 
 // forward pass over rows [0, B) of X (features); with train, the activations and pre-activations are kept
 int forward(gwf_mlp* m, const float* X, int B, float* out, bool train) {
@@ -276,8 +331,12 @@ int forward(gwf_mlp* m, const float* X, int B, float* out, bool train) {
     float* o = last && out ? out : m->act[l + 1].as<float>();
     const __nv_bfloat16* W = m->wbf.as<__nv_bfloat16>() + m->woff[l];
     const float* b = m->w32.as<float>() + m->boff[l];
-    MLP_CK((gemm<__nv_bfloat16, false, false>(m->stream, B, M, K, a, K, W, M, o, M, b, last ? 0 : 1,
-                                               train ? m->pre[l].as<float>() : nullptr)));
+    if (tc_layer(m, l))
+      MLP_CK((gemm_tc<__nv_bfloat16, false, false>(m->stream, B, M, K, a, K, W, M, o, M, b, last ? 0 : 1,
+                                                   train ? m->pre[l].as<float>() : nullptr, m->tc_err.as<int>())));
+    else
+      MLP_CK((gemm<__nv_bfloat16, false, false>(m->stream, B, M, K, a, K, W, M, o, M, b, last ? 0 : 1,
+                                                 train ? m->pre[l].as<float>() : nullptr)));
     a = o;
   }
   return GWF_OK;
@@ -304,14 +363,23 @@ int backward(gwf_mlp* m, const float* X, int B, const float* dY) {
     float* gW = m->grad.as<float>() + m->woff[l];
     float* gb = m->grad.as<float>() + m->boff[l];
     // dW = A_l^T dZ  (K x M, reduction over the batch)
-    MLP_CK((gemm<float, true, false>(m->stream, K, M, B, Al, K, dZ, M, gW, M, nullptr, 0, nullptr)));
+    const bool tc = tc_layer(m, l);
+    if (tc)
+      MLP_CK((gemm_tc<float, true, false>(m->stream, K, M, B, Al, K, dZ, M, gW, M, nullptr, 0, nullptr,
+                                          m->tc_err.as<int>(), &m->tc_ws)));
+    else
+      MLP_CK((gemm<float, true, false>(m->stream, K, M, B, Al, K, dZ, M, gW, M, nullptr, 0, nullptr)));
     colsum_kernel<<<nblk(M, 128), 128, 0, m->stream>>>(dZ, B, M, gb);
     MLP_CK(cudaGetLastError());
     if (l > 0) {
       // dA_l = dZ W_l^T  (B x K)
       const __nv_bfloat16* W = m->wbf.as<__nv_bfloat16>() + m->woff[l];
-      MLP_CK((gemm<__nv_bfloat16, false, true>(m->stream, B, K, M, dZ, M, W, M, m->dact[l].as<float>(), K, nullptr, 0,
-                                                nullptr)));
+      if (tc && K <= gwf::umma::kUNMax)
+        MLP_CK((gemm_tc<__nv_bfloat16, false, true>(m->stream, B, K, M, dZ, M, W, M, m->dact[l].as<float>(), K, nullptr,
+                                                    0, nullptr, m->tc_err.as<int>())));
+      else
+        MLP_CK((gemm<__nv_bfloat16, false, true>(m->stream, B, K, M, dZ, M, W, M, m->dact[l].as<float>(), K, nullptr,
+                                                  0, nullptr)));
       dA = m->dact[l].as<float>();
     }
   }
@@ -419,9 +487,10 @@ int gwf_mlp_create(gwf_ctx* ctx, int hidden, int layers, uint64_t seed, gwf_mlp*
   }
   const size_t nb = (size_t)m->nw * sizeof(float);
   bool ok = m->w32.ensure(nb) && m->wbf.ensure((size_t)m->nw * 2) && m->grad.ensure(nb) && m->adam_m.ensure(nb) &&
-            m->adam_v.ensure(nb) && m->loss.ensure(sizeof(double));
+            m->adam_v.ensure(nb) && m->loss.ensure(sizeof(double)) && m->tc_err.ensure(sizeof(int));
   if (ok) ok = cudaMemcpy(m->w32.p, w.data(), nb, cudaMemcpyHostToDevice) == cudaSuccess &&
-               cudaMemset(m->adam_m.p, 0, nb) == cudaSuccess && cudaMemset(m->adam_v.p, 0, nb) == cudaSuccess;
+               cudaMemset(m->adam_m.p, 0, nb) == cudaSuccess && cudaMemset(m->adam_v.p, 0, nb) == cudaSuccess &&
+               cudaMemset(m->tc_err.p, 0, sizeof(int)) == cudaSuccess;
   if (ok) {
     to_bf16_kernel<<<nblk(m->nw, 256), 256, 0, m->stream>>>(m->w32.as<float>(), m->nw, m->wbf.as<__nv_bfloat16>());
     ok = cudaStreamSynchronize(m->stream) == cudaSuccess;
@@ -439,7 +508,7 @@ int gwf_mlp_destroy(gwf_mlp* m) {
   cudaSetDevice(m->device);
   cudaStreamSynchronize(m->stream);
   for (Buf* b : {&m->w32, &m->wbf, &m->grad, &m->adam_m, &m->adam_v, &m->norm, &m->X, &m->T, &m->xb, &m->tb, &m->dy,
-                 &m->loss, &m->pred})
+                 &m->loss, &m->pred, &m->tc_err, &m->tc_ws})
     b->release();
   for (auto* v : {&m->act, &m->pre, &m->dact})
     for (auto& b : *v) b.release();
@@ -507,7 +576,7 @@ int gwf_mlp_gradients(gwf_mlp* m, const double* params, int64_t ld, int64_t n, c
   MLP_CK(cudaMemcpyAsync(&l, m->loss.p, sizeof l, cudaMemcpyDeviceToHost, m->stream));
   MLP_CK(cudaStreamSynchronize(m->stream));
   if (loss) *loss = l;
-  return GWF_OK;
+  return check_tc(m);
 }
 
 int gwf_mlp_train(gwf_mlp* m, const double* params, int64_t ld, int64_t n, const double* target, int epochs, int batch,
@@ -553,7 +622,7 @@ int gwf_mlp_train(gwf_mlp* m, const double* params, int64_t ld, int64_t n, const
   MLP_CK(cudaMemcpyAsync(&last, m->loss.p, sizeof last, cudaMemcpyDeviceToHost, m->stream));
   MLP_CK(cudaStreamSynchronize(m->stream));
   if (final_loss) *final_loss = last / (double)spe;
-  return GWF_OK;
+  return check_tc(m);
 }
 
 int gwf_mlp_predict(gwf_mlp* m, const double* params, int64_t ld, int64_t n, int mem, double* out_ln_snr) {
@@ -585,7 +654,7 @@ int gwf_mlp_predict(gwf_mlp* m, const double* params, int64_t ld, int64_t n, int
   if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
   dout.release();
   if (e != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("MLP predict: ") + cudaGetErrorString(e));
-  return GWF_OK;
+  return check_tc(m);
 }
 
 }  // extern "C"

@@ -1,8 +1,10 @@
 """CPU float64 model of the SNR-screen MLP (test infrastructure, the checker of the GPU kernels).
 
-Same feature map, standardisation, layer layout and BF16 rounding of the weights as the CUDA
-implementation (gwfast_gb300/csrc/gwf_mlp.cu); the arithmetic is float64, so comparing gradients
-shows the error of the GPU's FP32 accumulation and of nothing else.
+Same feature map, standardisation, layer layout and BF16 rounding as the CUDA implementation
+(gwfast_gb300/csrc/gwf_mlp.cu): the weights are used in BF16, and the hidden-to-hidden layers (both
+widths multiples of 16, at most 256), which run on the tensor cores, also round their activation and
+gradient operands to BF16 where they enter the products. The arithmetic is float64, so comparing
+gradients shows the error of the GPU's FP32 accumulation (and the rare BF16 rounding it tips over).
 """
 import numpy as np
 
@@ -33,15 +35,22 @@ def unpack(w, hidden, layers):
     return Ws, bs
 
 
+def tensor_core_layer(l, n_layers, hidden):
+    """The hidden-to-hidden layers run on the tensor cores (BF16 operands)."""
+    return 1 <= l <= n_layers - 2 and hidden % 16 == 0 and hidden <= 256
+
+
 def forward_backward(w, norm, p, target, hidden, layers):
     """Loss (mean squared error of ln SNR) and its gradient in the flat weight layout."""
     Ws, bs = unpack(np.asarray(w, dtype=np.float64), hidden, layers)
     Wq = [bf16(W.astype(np.float32)) for W in Ws]
+    L = len(Wq)
+    tc = [tensor_core_layer(l, L, hidden) for l in range(L)]
     x = (features(p).astype(np.float32).astype(np.float64) - norm[:11]) * norm[11:]
     acts, pres = [x], []
     a = x
     for l, (W, b) in enumerate(zip(Wq, bs)):
-        z = a @ W + b
+        z = (bf16(a) if tc[l] else a) @ W + b
         pres.append(z)
         a = z if l == len(Wq) - 1 else z / (1. + np.exp(-z))
         acts.append(a)
@@ -57,7 +66,11 @@ def forward_backward(w, norm, p, target, hidden, layers):
         else:
             s = 1. / (1. + np.exp(-z))
             dZ = dA * s * (1. + z * (1. - s))
-        gW[l] = acts[l].T @ dZ
         gb[l] = dZ.sum(axis=0)
-        dA = dZ @ Wq[l].T
+        if tc[l]:
+            gW[l] = bf16(acts[l]).T @ bf16(dZ)
+            dA = bf16(dZ) @ Wq[l].T
+        else:
+            gW[l] = acts[l].T @ dZ
+            dA = dZ @ Wq[l].T
     return loss, np.concatenate([g.ravel() for g in gW] + [g.ravel() for g in gb])

@@ -18,6 +18,8 @@ def params(n, seed):
 
 @pytest.mark.parametrize('hidden,layers,n', [(32, 2, 300), (256, 4, 600)])
 def test_mlp_gradients_match_cpu(gpu_lib, hidden, layers, n):
+    """GPU loss and gradients (tensor-core GEMMs for the hidden-to-hidden layers, tcgen05 kind::f16)
+    against the float64 model with the same BF16 roundings."""
     rng = np.random.default_rng(hidden)
     mlp = _lib.MLP(hidden=hidden, layers=layers, seed=3)
     p = params(n, 11)
@@ -28,7 +30,10 @@ def test_mlp_gradients_match_cpu(gpu_lib, hidden, layers, n):
     rel = np.linalg.norm(g_gpu - g_cpu) / np.linalg.norm(g_cpu)
     print('hidden %d layers %d: loss %.6e vs %.6e, gradient relative error %.2e' % (hidden, layers, loss_g, loss_c, rel))
     assert abs(loss_g - loss_c) <= 1e-5 * loss_c
-    assert rel < 1e-4
+    # the hidden-to-hidden layers take BF16 operands on the tensor cores; where the GPU's FP32 sum and
+    # the oracle's float64 sum of a pre-activation straddle a BF16 rounding boundary, that element
+    # differs by one BF16 ulp (2^-8 relative): 1.6e-5 (32 wide) and 1.0e-4 (256 wide) measured
+    assert rel < 3e-4
 
 
 def test_mlp_training_reduces_loss_and_predicts(gpu_lib):
