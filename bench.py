@@ -684,10 +684,11 @@ def main():
         'sigma_err_fp32_only': serr_fp32,
         'snr_per_s': world * N / (ms_snr / 1e3),
         'snr_per_s_fp32': world * N / (ms_snr32 / 1e3),
-        # first pass: 3 set-up + 3 FP32-record launches, the L1+H1 group kernel, the ET kernel and the
-        # join of the two groups' totals; the condition estimate and selection; with refined events:
-        # gather, 3 x (set-up record copy, segment scan, segmented FP64 kernel, reduction), sum-scatter
-        'gpu_launches': 9 + 2 + (14 if refined > 0 else 0),
+        # first pass: 2 set-up + 2 FP32-record launches (L1, ETS), H1's projection launch, the L1+H1
+        # group kernel, the ET kernel and the join of the two groups' totals; the condition estimate
+        # and selection; with refined events: gather, 3 x (set-up record copy, segment scan, segmented
+        # FP64 kernel, reduction), H1's projection patch, sum-scatter
+        'gpu_launches': 8 + 2 + (15 if refined > 0 else 0),
         'e2e': {'value': world * N / e2e_s, 'unit': 'Fisher/s', 'h2d_bytes_per_step': int(p_host.nbytes),
                 'd2h_bytes_per_step': int(F_host.nbytes),
                 'ms_per_step_each': [round(1e3 * t, 3) for t in e2e_iter],

@@ -386,10 +386,13 @@ int ensure_aux(gwf_ctx* ctx, int n) {
 // GWF_PREC_MIXED, second stage: condition numbers of the FP32 network Fishers, then the FP64
 // Fisher of the events above the threshold, computed as a compact batch (the detectors side by side
 // on their own streams) and scattered back
-// recs[i]: where the first pass left detector i's FP64 set-up records for the whole batch, or null
+// recs[i]: where the first pass left detector i's FP64 set-up records for the whole batch, or null;
+// patch[i]: those are another detector's records (same grid and model), to be given detector i's
+// projection header
 int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const double* dp, int64_t dld,
            const int* dres, int64_t N, int slots, double* darm, double* dnet, double* dsda, double* dsdn,
-           bool core_filled, const std::vector<const unsigned char*>& recs, cudaStream_t st) {
+           bool core_filled, const std::vector<const unsigned char*>& recs, const std::vector<int>& patch,
+           cudaStream_t st) {
   const size_t per = (size_t)gwf::NP * gwf::NP;
   if (ctx->fcond.ensure((size_t)N * sizeof(double)) || ctx->mix_idx.ensure((size_t)N * sizeof(long long)) ||
       ctx->mix_cnt.ensure(sizeof(unsigned long long)))
@@ -457,6 +460,7 @@ int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const
     ai.det = dev_of(r);
     if (recs[i]) {   // copy the records of these events instead of recomputing them
       ai.rec_src = recs[i];
+      ai.rec_patch_proj = patch[i];
       ai.core_idx = idx;
     }
     ai.scratch = (unsigned char*)ctx->mix_scr.p + (size_t)i * chunk * stride;
@@ -718,6 +722,7 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   // the mixed form's second stage reuses the FP64 set-up records of this pass when they all stay in
   // the scratch until then: one chunk, and every group in its own scratch area
   std::vector<const unsigned char*> recs(n_det, nullptr);
+  std::vector<int> patch(n_det, 0);
   const bool keep_recs = precision == GWF_PREC_MIXED && fisher && N <= gwf::kChunk && (side || ngr == 1);
   int gi = 0;
   for (auto& grp : groups) {
@@ -747,7 +752,13 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
         g.wr[d] = (float)std::sqrt(g.det[0].psd_scale / g.det[d].psd_scale);
       }
       g.slice = 0;
-      for (int d = 0; keep_recs && d < g.nd; ++d) recs[grp[d]] = a.scratch + (size_t)d * chunk * stride;
+      // the group's other detectors get only their projection in the first pass (their FP64 records
+      // would equal detector 0's but for the projection header): the FP64 stage copies detector 0's
+      // records for them and recomputes that header
+      for (int d = 0; keep_recs && d < g.nd; ++d) {
+        recs[grp[d]] = a.scratch;
+        patch[grp[d]] = d > 0;
+      }
       a.det = g.det[0];
       a.out_arm = nullptr;
       a.out_sd_arm = nullptr;
@@ -776,7 +787,7 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
     GWF_CK(gwf::launch_add_slices((const double*)ctx->gnet.p, ngr - 1, (long long)N * per, (long long)N * per, dnet, st));
   }
   if (precision == GWF_PREC_MIXED) {
-    rc = refine(ctx, n_det, det_ids, a, dp, dld, dres, N, slots, darm, dnet, dsda, dsdn, share, recs, st);
+    rc = refine(ctx, n_det, det_ids, a, dp, dld, dres, N, slots, darm, dnet, dsda, dsdn, share, recs, patch, st);
     if (rc) return rc;
   }
   if (!capturing) GWF_CK(cudaEventRecord(ctx->scratch_free, st));

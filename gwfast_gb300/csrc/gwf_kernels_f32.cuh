@@ -670,6 +670,41 @@ __global__ void __launch_bounds__(64) setup_f32_kernel(DetDev det, const unsigne
   }
 }
 
+// The other detectors of a group share detector 0's frequency grid and model record (same fmin, fmax
+// and Earth-rotation flag, hence the same reference frequency), and the group kernel reads only their
+// projection from their FP32 record slot: the pattern-function constants in FP64, rounded once
+// (one thread per event). Nothing else of their slot is written.
+template <int MODEL>
+__global__ void __launch_bounds__(64) proj_f32_kernel(EvBatch ev, DetDev det, unsigned char* scratch32, long long count,
+                                                      int narm, int earth) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = ev.n0 + i;
+  if (i >= count || n >= ev.N) return;
+  const double* p = ev.p;
+  const long long ld = ev.ld;
+  ProjEv pj;
+  proj_setup(pj, det, p[3 * ld + n], p[4 * ld + n], p[5 * ld + n], p[6 * ld + n], p[7 * ld + n], p[2 * ld + n]);
+  F32Rec<MODEL>& r = *reinterpret_cast<F32Rec<MODEL>*>(scratch32 + i * f32_stride<MODEL>());
+  projf_setup(r.pf, pj, det.sin_zeta);
+  if (!earth) {
+    time_f(r.pf, 0.0f, r.tsc);
+    for (int a = 0; a < narm; ++a) arm_f(r.pf, r.tsc, a, r.apc[a]);
+  }
+}
+
+// FP64 set-up records copied from another detector of the same grid: only the projection header is
+// the detector's own (events ev.n0 .. of a gathered batch, records 0 .. count - 1)
+template <int MODEL>
+__global__ void __launch_bounds__(64) proj_patch_kernel(EvBatch ev, DetDev det, unsigned char* scratch, long long count) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = ev.n0 + i;
+  if (i >= count || n >= ev.N) return;
+  const double* p = ev.p;
+  const long long ld = ev.ld;
+  SetupHdr& h = *reinterpret_cast<SetupHdr*>(scratch + i * rec_stride<MODEL>());
+  proj_setup(h.pj, det, p[3 * ld + n], p[4 * ld + n], p[5 * ld + n], p[6 * ld + n], p[7 * ld + n], p[2 * ld + n]);
+}
+
 // per-block state of the FP32 kernels (shared memory); the staging area is dynamic shared memory
 template <int MODEL, int NG>
 struct F32State {

@@ -68,6 +68,9 @@ struct LaunchArgs {
   // call (event n at rec_src + n * rec_stride): a gathered batch (core_idx) copies its rows from
   // there instead of running the set-up again
   const unsigned char* rec_src = nullptr;
+  // rec_src holds another detector's records (a detector group shares grid and model): the copied
+  // rows get this detector's projection header
+  int rec_patch_proj = 0;
   KernelTimer* timer = nullptr;            // gwf_set_kernel_timing: events around the main launches
 };
 

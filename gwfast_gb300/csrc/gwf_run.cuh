@@ -48,6 +48,9 @@ cudaError_t chunked(const LaunchArgs& a, bool f32, MAIN main) {
       const long long words = cnt * (long long)(rec_stride<M>() / 16);
       copy_records_kernel<<<(unsigned)((words + 255) / 256), 256, 0, a.stream>>>(
           reinterpret_cast<const uint4*>(a.rec_src), a.core_idx + n0, cnt, reinterpret_cast<uint4*>(a.scratch));
+      if constexpr (M < 3) {   // (only the detector groups of the FP32 forms share records)
+        if (a.rec_patch_proj) proj_patch_kernel<M><<<nb, 64, 0, a.stream>>>(ev, a.det, a.scratch, cnt);
+      }
     } else {
       setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, a.det, a.wf, a.qnm, a.nq, a.scratch, cnt, a.core, a.core_mode,
                                                a.core_idx);
@@ -243,14 +246,17 @@ cudaError_t group_one(const LaunchArgs& a, GroupDev g) {
     }
     for (int d = 0; d < g.nd; ++d) {
       unsigned char* sc = a.scratch + (size_t)d * chunk * stride;
-      const int mode = d == 0 ? a.core_mode : (a.core ? 2 : 0);
-      setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, g.det[d], a.wf, a.qnm, a.nq, sc, cnt, a.core, mode, nullptr);
-      if (a.core_done && mode == 1) {
+      unsigned char* s32 = sc + (size_t)chunk * rec_stride<M>();
+      if (d > 0) {   // same grid and model record as detector 0: only the projection is its own
+        proj_f32_kernel<M><<<nb, 64, 0, a.stream>>>(ev, g.det[d], s32, cnt, g.det[d].shape == 1 ? 2 : 1, g.det[d].earth);
+        continue;
+      }
+      setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, g.det[d], a.wf, a.qnm, a.nq, sc, cnt, a.core, a.core_mode, nullptr);
+      if (a.core_done && a.core_mode == 1) {
         err = cudaEventRecord(a.core_done, a.stream);
         if (err != cudaSuccess) return err;
       }
-      setup_f32_kernel<M><<<nb, 64, 0, a.stream>>>(g.det[d], sc, sc + (size_t)chunk * rec_stride<M>(), cnt,
-                                                   g.det[d].shape == 1 ? 2 : 1, g.det[d].earth);
+      setup_f32_kernel<M><<<nb, 64, 0, a.stream>>>(g.det[d], sc, s32, cnt, g.det[d].shape == 1 ? 2 : 1, g.det[d].earth);
     }
     if (a.timer) {
       err = a.timer->end(a.stream);
