@@ -221,6 +221,163 @@ __global__ void to_float_kernel(const double* __restrict__ y, long long n, float
   if (i < n) out[i] = (float)y[i];
 }
 
+// ---------------------------------------------------------------- fused inference on the tensor cores
+// One CTA of 128 threads per 128 events; thread t owns event (and tensor-memory lane) t of the tile.
+// The features and the input layer (11 -> H, FP32 with BF16 weights) run on the CUDA cores and leave
+// the activations, rounded to BF16, in shared memory in the K-major core-matrix layout. Each
+// hidden-to-hidden layer is one 128 x H x H product into tensor memory (its weights staged in 64-deep
+// K chunks), read back by the epilogue, which applies bias and SiLU and writes the next layer's
+// operand in place; the last epilogue feeds the output layer's dot product (FP32) directly, so no
+// activation leaves the chip. Same arithmetic as the layer-by-layer forward pass up to the order of
+// the FP32 sums.
+constexpr int kMaxLayers = 17;
+struct InferNet {
+  int L, H;                    // layers (weight matrices) and hidden width
+  long long woff[kMaxLayers];  // offsets of W_l (BF16 copy) and b_l (FP32) in the flat layout
+  long long boff[kMaxLayers];
+};
+
+__host__ __device__ constexpr int infer_smem_bytes() { return 64 * 1024 + 32 * 1024 + 1024; }
+
+__global__ void __launch_bounds__(128, 1) mlp_infer_tc_kernel(const double* __restrict__ p, long long ld, long long n,
+                                                             const float* __restrict__ norm, InferNet net,
+                                                             const __nv_bfloat16* __restrict__ wbf,
+                                                             const float* __restrict__ w32, double* __restrict__ out,
+                                                             int* __restrict__ err) {
+  using namespace gwf::umma;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* sa = smem_raw;               // activations: 128 x H BF16, [row/8][k/8] core matrices
+  unsigned char* sb = smem_raw + 64 * 1024;   // weights: H x 64 BF16 chunk, [n/8][k/8]
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_base;
+  const int H = net.H, L = net.L;
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const long long row = (long long)blockIdx.x * 128 + t;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(&tmem_base))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (t == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // features of this thread's event, standardised (zero for rows past n)
+  float x[kNF];
+  {
+    double f[kNF];
+    if (row < n) {
+      const double tp = 6.283185307179586;
+      const double ra = p[4 * ld + row] - tp * p[7 * ld + row];
+      f[0] = log(p[row]); f[1] = p[ld + row]; f[2] = log(p[2 * ld + row]); f[3] = cos(p[3 * ld + row]);
+      f[4] = sin(ra); f[5] = cos(ra); f[6] = cos(p[5 * ld + row]); f[7] = sin(2.0 * p[6 * ld + row]);
+      f[8] = cos(2.0 * p[6 * ld + row]); f[9] = p[9 * ld + row]; f[10] = p[10 * ld + row];
+    }
+#pragma unroll
+    for (int k = 0; k < kNF; ++k) x[k] = row < n ? ((float)f[k] - norm[k]) * norm[kNF + k] : 0.0f;
+  }
+  const int kb = H / 8;                         // core matrices along K of the activation buffer
+  float y = 0.0f;                               // output layer, accumulated by the last epilogue
+  const float* wl = w32 + net.woff[L - 1];      // output weights (FP32 copy rounded as BF16 below)
+  const __nv_bfloat16* wlb = wbf + net.woff[L - 1];
+  // input layer on the CUDA cores: 8 columns at a time into one 16-byte core-matrix row
+  {
+    const __nv_bfloat16* W0 = wbf + net.woff[0];
+    const float* b0 = w32 + net.boff[0];
+    for (int j0 = 0; j0 < H; j0 += 8) {
+      float a[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        float z = b0[j0 + j];
+#pragma unroll
+        for (int k = 0; k < kNF; ++k) z = fmaf(x[k], __bfloat162float(W0[k * H + j0 + j]), z);
+        a[j] = silu_f(z);
+      }
+      if (L == 2) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) y = fmaf(a[j], __bfloat162float(wlb[j0 + j]), y);
+      } else {
+        *reinterpret_cast<uint4*>(sa + ((t >> 3) * kb + (j0 >> 3)) * 128 + (t & 7) * 16) =
+            make_uint4(pack_bf16(a[0], a[1]), pack_bf16(a[2], a[3]), pack_bf16(a[4], a[5]), pack_bf16(a[6], a[7]));
+      }
+    }
+  }
+  (void)wl;
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tm = tmem_base;
+  const uint32_t idesc = instr_desc(128, H);
+  bool ok = true;
+  uint32_t phase = 0;
+  for (int l = 1; l <= L - 2 && ok; ++l) {
+    const __nv_bfloat16* W = wbf + net.woff[l];   // [H][H] row-major: element (k, n) at k H + n
+    for (int c = 0; c < H / 64 && ok; ++c) {
+      // weights of K rows [64 c, 64 c + 64) as the MMA's B operand (n rows, K-major)
+      for (int u = t; u < H * 8; u += 128) {
+        const int nn = u % H, kg = u / H;
+        uint32_t q[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const __nv_bfloat16 lo = W[(long long)(c * 64 + kg * 8 + 2 * j) * H + nn];
+          const __nv_bfloat16 hi = W[(long long)(c * 64 + kg * 8 + 2 * j + 1) * H + nn];
+          q[j] = (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+        }
+        *reinterpret_cast<uint4*>(sb + ((nn >> 3) * 8 + kg) * 128 + (nn & 7) * 16) = make_uint4(q[0], q[1], q[2], q[3]);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      if (t == 0) {
+        fence_after_sync();
+        const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
+#pragma unroll
+        for (int s = 0; s < 4; ++s)
+          mma_f16(tm, smem_desc(a0 + (c * 8 + s * 2) * 128, 128, kb * 128), smem_desc(b0 + s * 2 * 128, 128, 8 * 128),
+                  idesc, (c > 0 || s > 0) ? 1u : 0u);
+        mma_commit(&bar);
+      }
+      ok = __syncthreads_and(mbar_wait(&bar, phase)) != 0;
+      if (!ok) {
+        if (t == 0) {
+          atomicExch(err, 1);
+          mbar_wait(&bar, phase);
+        }
+        __syncthreads();
+      }
+      phase ^= 1u;
+      fence_after_sync();
+    }
+    if (!ok) break;
+    // epilogue: bias and SiLU; the next layer's operand in place, or the output layer's dot product
+    const float* bl = w32 + net.boff[l];
+    const bool last = l == L - 2;
+    for (int c0 = 0; c0 < H; c0 += 16) {
+      float v[16];
+      tmem_ld16(tm + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) v[j] = silu_f(v[j] + bl[c0 + j]);
+      if (last) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) y = fmaf(v[j], __bfloat162float(wlb[c0 + j]), y);
+      } else {
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+          *reinterpret_cast<uint4*>(sa + ((t >> 3) * kb + ((c0 >> 3) + h)) * 128 + (t & 7) * 16) =
+              make_uint4(pack_bf16(v[8 * h + 0], v[8 * h + 1]), pack_bf16(v[8 * h + 2], v[8 * h + 3]),
+                         pack_bf16(v[8 * h + 4], v[8 * h + 5]), pack_bf16(v[8 * h + 6], v[8 * h + 7]));
+      }
+    }
+    fence_before_sync();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    fence_after_sync();
+  }
+  if (ok && row < n) out[row] = (double)(y + w32[net.boff[L - 1]]);
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tm) : "memory");
+}
+
 struct Buf {
   void* p = nullptr;
   size_t cap = 0;
@@ -631,6 +788,46 @@ int gwf_mlp_predict(gwf_mlp* m, const double* params, int64_t ld, int64_t n, int
   if (!params || !out_ln_snr || n < 0 || ld < n) return fail(GWF_ERR_INVALID_ARG, "bad arguments");
   if (!m->have_norm) return fail(GWF_ERR_INVALID_ARG, "the MLP is not trained (no feature standardisation)");
   if (n == 0) return GWF_OK;
+  const int L = n_layers(m), H = m->dims[1];
+  if (L >= 2 && L <= kMaxLayers && H % 64 == 0 && H <= gwf::umma::kUNMax) {
+    // fused tensor-core inference: parameters in, ln SNR out, nothing else in global memory
+    Buf dpar, dout;
+    const double* dp = params;
+    int64_t dld = ld;
+    double* d = out_ln_snr;
+    cudaError_t e = cudaSuccess;
+    if (mem == GWF_MEM_HOST) {
+      if (!dpar.ensure((size_t)kNF * n * sizeof(double)) || !dout.ensure((size_t)n * sizeof(double)))
+        return fail(GWF_ERR_OOM, "device allocation failed (MLP input)");
+      e = cudaMemcpy2DAsync(dpar.p, n * sizeof(double), params, ld * sizeof(double), n * sizeof(double), kNF,
+                            cudaMemcpyHostToDevice, m->stream);
+      dp = dpar.as<double>();
+      dld = n;
+      d = dout.as<double>();
+    }
+    InferNet net;
+    net.L = L;
+    net.H = H;
+    for (int l = 0; l < L; ++l) {
+      net.woff[l] = m->woff[l];
+      net.boff[l] = m->boff[l];
+    }
+    const int smem = infer_smem_bytes();
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(mlp_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) {
+      mlp_infer_tc_kernel<<<nblk(n, 128), 128, smem, m->stream>>>(dp, dld, n, m->norm.as<float>(), net,
+                                                                  m->wbf.as<__nv_bfloat16>(), m->w32.as<float>(), d,
+                                                                  m->tc_err.as<int>());
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && mem == GWF_MEM_HOST)
+      e = cudaMemcpyAsync(out_ln_snr, d, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, m->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+    dpar.release();
+    dout.release();
+    if (e != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("MLP predict: ") + cudaGetErrorString(e));
+    return check_tc(m);
+  }
   rc = load_features(m, params, ld, n, mem, false);
   if (rc) return rc;
   // inference in slices that bound the activation memory

@@ -74,3 +74,15 @@ def forward_backward(w, norm, p, target, hidden, layers):
             gW[l] = acts[l].T @ dZ
             dA = dZ @ Wq[l].T
     return loss, np.concatenate([g.ravel() for g in gW] + [g.ravel() for g in gb])
+
+
+def predict(w, norm, p, hidden, layers):
+    """Predicted ln SNR (forward pass only) with the same roundings as the GPU's inference."""
+    Ws, bs = unpack(np.asarray(w, dtype=np.float64), hidden, layers)
+    Wq = [bf16(W.astype(np.float32)) for W in Ws]
+    L = len(Wq)
+    a = (features(p).astype(np.float32).astype(np.float64) - norm[:11]) * norm[11:]
+    for l, (W, b) in enumerate(zip(Wq, bs)):
+        z = (bf16(a) if tensor_core_layer(l, L, hidden) else a) @ W + b
+        a = z if l == L - 1 else z / (1. + np.exp(-z))
+    return a[:, 0]

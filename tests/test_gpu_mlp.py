@@ -36,6 +36,34 @@ def test_mlp_gradients_match_cpu(gpu_lib, hidden, layers, n):
     assert rel < 3e-4
 
 
+@pytest.mark.parametrize('hidden,layers', [(256, 4), (64, 2), (64, 1)])
+def test_mlp_predict_matches_cpu(gpu_lib, hidden, layers):
+    """Inference (one fused kernel per 128 events: features and input layer on the CUDA cores, the
+    hidden-to-hidden layers chained through tensor memory with the activations resident in shared
+    memory, the output layer in the last epilogue) against the float64 model with the same BF16
+    roundings, on random weights of realistic scale."""
+    rng = np.random.default_rng(hidden + layers)
+    mlp = _lib.MLP(hidden=hidden, layers=layers, seed=7)
+    p = params(3000, 41)
+    mlp.gradients(p, rng.normal(1.0, 1.5, p.shape[1]))   # sets the standardisation
+    w = mlp.get_weights()
+    w = w + rng.normal(0.0, 0.05, w.shape).astype(np.float32)   # non-zero biases as well
+    mlp.set_weights(w)
+    y = mlp.predict(p)
+    yc = M.predict(mlp.get_weights(), mlp.get_norm().astype(np.float64), p, hidden, layers)
+    d = np.abs(y - yc)
+    sc = max(1.0, np.std(yc))
+    print('hidden %d layers %d: predict vs float64 model max %.2e p99 %.2e median %.2e (scale %.2f)'
+          % (hidden, layers, d.max(), np.percentile(d, 99), np.median(d), np.std(yc)))
+    # typical events differ by the FP32 sums alone (~1e-7); a few differ more where a hidden activation
+    # lies on a BF16 rounding boundary and the GPU and the model round it to neighbouring BF16 values
+    # (one BF16 ulp, 2^-8 relative), which the following layers carry to the output (measured max:
+    # 5.5e-3 with three BF16 layers, 3.6e-4 with one, 1.3e-6 with none)
+    assert np.median(d) < 1e-5 * sc
+    assert np.percentile(d, 99) < 1e-3 * sc
+    assert d.max() < 2e-2 * sc
+
+
 def test_mlp_training_reduces_loss_and_predicts(gpu_lib):
     p = params(20000, 21)
     f = M.features(p)
