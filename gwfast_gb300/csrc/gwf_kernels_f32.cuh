@@ -280,6 +280,100 @@ __device__ inline void round_struct(const SRC& s, DST& d, const D4* amp_member, 
   }
 }
 
+// tau_star (3.5PN time to coalescence, gwfast/waveforms.py:878-901, :1299-1322) in the FP32 form.
+// tau = T0 v^-8 P(v), T0 = (5/256) Ms / eta, v = vM f^(1/3), P(v) = 1 + sum_{k=2..7} a_k v^k with the
+// a_k polynomials in eta (a_6 also carries a6l ln(16 v^2)). The parameters enter only through Ms, eta
+// and vM, and v's tangent is v d ln vM, so per point
+//   d tau = tau d ln T0 + T0 v^-8 [ (v P'(v) - 8 P(v)) d ln vM + (dP/deta)(v) d eta ]:
+// three polynomials in v with per-event coefficients (formed once per event in FP64) instead of the
+// four-direction dual arithmetic of the eta polynomials at every point; ln(16 v^2) comes from ln f.
+struct TauF {
+  float T0, lnv0, lg0;   // (5/256) Ms / eta; ln vM; ln 16 + 2 ln vM (ln(16 v^2) = lg0 + 2/3 ln f)
+  float a[6], b[6];      // a_2..a_7 (a_6 without its log term) and their eta derivatives
+  float dlnT0[4], dlnv[4], deta[4];   // tangents (chi1 slot: d/dchi1 - alpha d/dchi2)
+};
+constexpr double kTauA6l = 3424.0 / 105.0;
+
+__device__ inline void tau_setup(TauF& t, const D4& Ms, const D4& vM, const D4& eta_, double alpha) {
+  const double eta = eta_.v, e2 = eta * eta;
+  const double a[6] = {743. / 252. + 11. / 3. * eta, -32. / 5. * kPi,
+                       3058673. / 508032. + 5429. / 504. * eta + 617. / 72. * e2,
+                       -(7729. / 252. - 13. / 3. * eta) * kPi,
+                       -10052469856691. / 23471078400. + 128. / 3. * kPi * kPi + 6848. / 105. * kEulerGamma
+                           + (3147553127. / 3048192. - 451. / 12. * kPi * kPi) * eta - 15211. / 1728. * e2
+                           + 25565. / 1296. * e2 * eta,
+                       (-15419335. / 127008. - 75703. / 756. * eta + 14809. / 378. * e2) * kPi};
+  const double b[6] = {11. / 3., 0.0, 5429. / 504. + 2. * 617. / 72. * eta, 13. / 3. * kPi,
+                       3147553127. / 3048192. - 451. / 12. * kPi * kPi - 2. * 15211. / 1728. * eta
+                           + 3. * 25565. / 1296. * e2,
+                       (-75703. / 756. + 2. * 14809. / 378. * eta) * kPi};
+  for (int k = 0; k < 6; ++k) { t.a[k] = (float)a[k]; t.b[k] = (float)b[k]; }
+  t.T0 = (float)(5.0 / 256.0 * Ms.v / eta);
+  const double lnv0 = log(vM.v);
+  t.lnv0 = (float)lnv0;
+  t.lg0 = (float)(log(16.0) + 2.0 * lnv0);
+  auto tan = [&](const D4& d, int q) { return q == P_CHI1 ? d.d[P_CHI1] - alpha * d.d[P_CHI2] : d.d[q]; };
+  for (int q = 0; q < 4; ++q) {
+    t.dlnT0[q] = (float)(tan(Ms, q) / Ms.v - tan(eta_, q) / eta);
+    t.dlnv[q] = (float)(tan(vM, q) / vM.v);
+    t.deta[q] = (float)tan(eta_, q);
+  }
+}
+
+// tau_star (s) and its tangent at ln f
+__device__ __forceinline__ void tau_point_f32(const TauF& t, float lnf, float& tau, float (&dtau)[4]) {
+  const float lnv = fmaf(lnf, 1.0f / 3.0f, t.lnv0);
+  const float v = expf(lnv), iv8 = expf(-8.0f * lnv);
+  const float lg = fmaf(lnf, 2.0f / 3.0f, t.lg0);
+  const float a6e = fmaf((float)kTauA6l, lg, t.a[4]);
+  // P / v^2 - 1 / v^2, v P' / v^2, (dP/deta) / v^2 by Horner from v^5 down
+  float p = t.a[5], dp = 7.0f * t.a[5], q = t.b[5];
+  p = fmaf(p, v, a6e);  dp = fmaf(dp, v, fmaf(6.0f, a6e, 2.0f * (float)kTauA6l));  q = fmaf(q, v, t.b[4]);
+  p = fmaf(p, v, t.a[3]);  dp = fmaf(dp, v, 5.0f * t.a[3]);  q = fmaf(q, v, t.b[3]);
+  p = fmaf(p, v, t.a[2]);  dp = fmaf(dp, v, 4.0f * t.a[2]);  q = fmaf(q, v, t.b[2]);
+  p = fmaf(p, v, t.a[1]);  dp = fmaf(dp, v, 3.0f * t.a[1]);  q = fmaf(q, v, t.b[1]);
+  p = fmaf(p, v, t.a[0]);  dp = fmaf(dp, v, 2.0f * t.a[0]);  q = fmaf(q, v, t.b[0]);
+  const float v2 = v * v;
+  const float P = fmaf(p, v2, 1.0f);
+  const float c = t.T0 * iv8;
+  tau = c * P;
+  const float gv = c * fmaf(dp, v2, -8.0f * P), ge = c * q * v2;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) dtau[k] = fmaf(tau, t.dlnT0[k], fmaf(gv, t.dlnv[k], ge * t.deta[k]));
+}
+
+// IMRPhenomD amplitude in the FP32 form (gwfast/waveforms.py:1155-1254). In the inspiral region
+// A = ampPref x^(-7/6) S(x), S = 1 + sum_k c_k x^(k/3) (k = 2..9; c_k = a23, a1, a43, a53, a2, r1, r2, r3),
+// x = MG f with tangent x d ln MG, so
+//   d ln A = d ln ampPref + (-7/6 + x S'(x) / S) d ln MG + (sum_k d c_k x^(k/3)) / S:
+// the basis powers once, then scalar sums, instead of dual products of every term. Elsewhere the dual
+// evaluation of complete_amp_shape.
+__device__ __forceinline__ DF4 phd_amp_f32(const PhdCoreT<DF4>& k, float f) {
+  const float xv = k.MG.v * f;
+  if (!(xv < (float)kAmpFJoin)) return phd_amp_point<DF4>(k, f);
+  const float x13 = cbrtf(xv), x23 = x13 * x13, x2 = xv * xv;
+  const float bas[8] = {x23, xv, xv * x13, xv * x23, x2, x2 * x13, x2 * x23, x2 * xv};
+  const DF4* c[8] = {&k.a23, &k.a1, &k.a43, &k.a53, &k.a2, &k.r1, &k.r2, &k.r3};
+  float S = 1.0f, xS = 0.0f, T[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const float cb = c[j]->v * bas[j];
+    S += cb;
+    xS = fmaf((float)(j + 2) * (1.0f / 3.0f), cb, xS);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) T[q] = fmaf(c[j]->d[q], bas[j], T[q]);
+  }
+  const float xm76 = 1.0f / (xv * sqrtf(x13));
+  const float iP = 1.0f / k.ampPref.v, iS = 1.0f / S;
+  DF4 A;
+  A.v = k.ampPref.v * xm76 * S;
+  const float gx = -7.0f / 6.0f + xS * iS, iMG = 1.0f / k.MG.v;
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    A.d[q] = A.v * (k.ampPref.d[q] * iP + gx * k.MG.d[q] * iMG + T[q] * iS);
+  return A;
+}
+
 // The detector-independent part of one frequency point: hp = P, hc = i C without the common phase,
 // their tangents in (Mc, eta, chi1z, chi2z), the iota derivatives, Q = P - s C (s = sign cos iota, see
 // project_f32) and, with Earth rotation, tau_star and its tangent. The amplitude prefactor is
@@ -291,8 +385,8 @@ struct WaveF {
 };
 
 template <int MODEL, bool EARTH>
-__device__ __forceinline__ void wave_f32(const EvUnionF& EF, const PBF& pbf, const ProjF& pf, float f, float lnf,
-                                         WaveF& w) {
+__device__ __forceinline__ void wave_f32(const EvUnionF& EF, const PBF& pbf, const ProjF& pf, const TauF& tf, float f,
+                                         float lnf, WaveF& w) {
   DF4 A;
   float dphi[4];
   phase_tangent_f(pbf, f, lnf, dphi);
@@ -302,20 +396,14 @@ __device__ __forceinline__ void wave_f32(const EvUnionF& EF, const PBF& pbf, con
   if (MODEL == 0) {
     const float f13 = cbrtf(f);
     A = EF.tf2.ampK * (1.0f / (f * sqrtf(f13)));
-    if (EARTH) {
-      const DF4 tau = tau_star_point<DF4>(EF.tf2.Ms, EF.tf2.vM, EF.tf2.eta, f13);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) w.dtn[q] = -tau.d[q] * (1.0f / 86400.0f);
-      w.tau = tau.v;
-    }
   } else {
-    A = phd_amp_point<DF4>(EF.phd, f);
-    if (EARTH) {
-      const DF4 tau = tau_star_point<DF4>(EF.phd.Ms, EF.phd.vM, EF.phd.eta, cbrtf(f));
+    A = phd_amp_f32(EF.phd, f);
+  }
+  if (EARTH) {
+    float dtau[4];
+    tau_point_f32(tf, lnf, w.tau, dtau);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) w.dtn[q] = -tau.d[q] * (1.0f / 86400.0f);
-      w.tau = tau.v;
-    }
+    for (int q = 0; q < 4; ++q) w.dtn[q] = -dtau[q] * (1.0f / 86400.0f);
   }
   w.P = {pf.cp * A.v, 0.0f};
   w.C = {pf.ci * A.v, 0.0f};
@@ -368,10 +456,11 @@ __device__ __forceinline__ void project_f32(const WaveF& w, const ProjF& pf, con
 }
 
 template <int MODEL, bool EARTH, int NARM>
-__device__ __forceinline__ void point_f32(const EvUnionF& EF, const PBF& pbf, const ProjF& pf, const ArmF* apc,
-                                          const TimeF& tsc, float f, float lnf, cf (&D)[NARM][NP], cf (&H)[NARM]) {
+__device__ __forceinline__ void point_f32(const EvUnionF& EF, const PBF& pbf, const ProjF& pf, const TauF& tf,
+                                          const ArmF* apc, const TimeF& tsc, float f, float lnf, cf (&D)[NARM][NP],
+                                          cf (&H)[NARM]) {
   WaveF w;
-  wave_f32<MODEL, EARTH>(EF, pbf, pf, f, lnf, w);
+  wave_f32<MODEL, EARTH>(EF, pbf, pf, tf, f, lnf, w);
   project_f32<EARTH, NARM>(w, pf, apc, tsc, f, D, H);
 }
 
@@ -467,7 +556,7 @@ __device__ __forceinline__ double ins_phase_scaled(const PhdCoreT<double>& k, co
 // summed over the modes from the harmonic differences yp - s yc formed in FP64, so it keeps FP32
 // relative accuracy near face-on and face-off.
 template <bool EARTH>
-__device__ __forceinline__ void wave_f32_hm(const HMF32& H, const ProjF& pf, float f, WaveF& w) {
+__device__ __forceinline__ void wave_f32_hm(const HMF32& H, const ProjF& pf, const TauF& tf, float f, float lnf, WaveF& w) {
   const HMEvT<DF4>& e = H.e32;
   const HMEvT<double>& v = H.e64;
   const double x64 = v.k.MG * (double)f;
@@ -546,18 +635,18 @@ __device__ __forceinline__ void wave_f32_hm(const HMF32& H, const ProjF& pf, flo
 #pragma unroll
   for (int q = 0; q < 4; ++q) w.dtn[q] = 0.0f;
   if (EARTH) {
-    const DF4 tau = tau_star_point<DF4>(e.k.Ms, e.k.vM, e.k.eta, cbrtf(f));
+    float dtau[4];
+    tau_point_f32(tf, lnf, w.tau, dtau);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) w.dtn[q] = -tau.d[q] * (1.0f / 86400.0f);
-    w.tau = tau.v;
+    for (int q = 0; q < 4; ++q) w.dtn[q] = -dtau[q] * (1.0f / 86400.0f);
   }
 }
 
 template <bool EARTH, int NARM>
-__device__ __forceinline__ void point_f32_hm(const HMF32& H, const ProjF& pf, const ArmF* apc, const TimeF& tsc,
-                                             float f, cf (&D)[NARM][NP], cf (&Hs)[NARM]) {
+__device__ __forceinline__ void point_f32_hm(const HMF32& H, const ProjF& pf, const TauF& tf, const ArmF* apc,
+                                             const TimeF& tsc, float f, float lnf, cf (&D)[NARM][NP], cf (&Hs)[NARM]) {
   WaveF w;
-  wave_f32_hm<EARTH>(H, pf, f, w);
+  wave_f32_hm<EARTH>(H, pf, tf, f, lnf, w);
   project_f32<EARTH, NARM>(w, pf, apc, tsc, f, D, Hs);
 }
 
@@ -614,6 +703,7 @@ struct __align__(16) F32Rec {
   typename std::conditional<MODEL == 2, HMF32, EvUnionF>::type ef;
   typename std::conditional<MODEL == 2, NoRec, PBF>::type pbf;
   ProjF pf;
+  TauF tf;
   ArmF apc[2];
   TimeF tsc;
   GridF gf;
@@ -655,6 +745,11 @@ __global__ void __launch_bounds__(64) setup_f32_kernel(DetDev det, const unsigne
     }
   }
   r.chi_alpha = alpha;
+  if (g.ok) {
+    if constexpr (MODEL == 0) tau_setup(r.tf, E.tf2.Ms, E.tf2.vM, E.tf2.eta, alpha);
+    else if constexpr (MODEL == 1) tau_setup(r.tf, E.phd.k.Ms, E.phd.k.vM, E.phd.k.eta, alpha);
+    else tau_setup(r.tf, E.hm.k.Ms, E.hm.k.vM, E.hm.k.eta, alpha);
+  }
   r.scale = amp * amp / det.psd_scale;
   projf_setup(r.pf, h.pj, det.sin_zeta);
   r.psi_sgn = r.pf.sgn;
@@ -801,8 +896,8 @@ __device__ inline void f32_item(const EvBatch& ev, const DetDev& det, F32State<M
       grid.point(r, ev.spacing, k, lane, f, lnf, w);
       const float Sn = psd_at_f(det, f, lnf, gf.acc_l0, gf.acc_idl);
       sw = sqrtf(4.0f * w / Sn);
-      if constexpr (MODEL == 2) point_f32_hm<EARTH, NARM>(r.ef, r.pf, r.apc, r.tsc, f, D, Hs);
-      else point_f32<MODEL, EARTH, NARM>(r.ef, r.pbf, r.pf, r.apc, r.tsc, f, lnf, D, Hs);
+      if constexpr (MODEL == 2) point_f32_hm<EARTH, NARM>(r.ef, r.pf, r.tf, r.apc, r.tsc, f, lnf, D, Hs);
+      else point_f32<MODEL, EARTH, NARM>(r.ef, r.pbf, r.pf, r.tf, r.apc, r.tsc, f, lnf, D, Hs);
     } else {
 #pragma unroll
       for (int a = 0; a < NARM; ++a) {
@@ -1039,8 +1134,8 @@ __device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32S
     WaveF wv;
     if (valid) {
       grid.point(r, ev.spacing, k, lane, f, lnf, w);
-      if constexpr (MODEL == 2) wave_f32_hm<EARTH>(r.ef, r.pf, f, wv);
-      else wave_f32<MODEL, EARTH>(r.ef, r.pbf, r.pf, f, lnf, wv);
+      if constexpr (MODEL == 2) wave_f32_hm<EARTH>(r.ef, r.pf, r.tf, f, lnf, wv);
+      else wave_f32<MODEL, EARTH>(r.ef, r.pbf, r.pf, r.tf, f, lnf, wv);
     }
     float sd = 0.0f, cd = 1.0f;   // the Earth-rotation angle is the same for every detector
     if (EARTH && valid) rot_sc(wv, sd, cd);
@@ -1153,7 +1248,7 @@ __global__ void __launch_bounds__(kThreads) snr_kernel_f32(EvBatch ev, DetDev de
     TimeF ts;
     if constexpr (MODEL == 2) {
       WaveF wv;
-      wave_f32_hm<EARTH>(r.ef, r.pf, f, wv);
+      wave_f32_hm<EARTH>(r.ef, r.pf, r.tf, f, lnf, wv);
       ap = sqrtf(wv.P.re * wv.P.re + wv.P.im * wv.P.im);
       ac = sqrtf(wv.C.re * wv.C.re + wv.C.im * wv.C.im);
       if (EARTH) time_f(r.pf, -wv.tau * (1.0f / 86400.0f), ts);
