@@ -450,6 +450,45 @@ def run_hm(args):
     print(json.dumps(line))
 
 
+def run_mlp(args):
+    """The screen's network alone: train the 11 -> 4 x 256 SiLU -> 1 MLP for --train-epochs epochs on
+    --train-events events (batch 4096), then predict ln SNR for --events device-resident events (fused
+    tensor-core inference), CUDA wall clock per call, median of --steps after --warmup."""
+    import torch
+    from gwfast_gb300 import _build, _lib, synthetic
+    from gwfast_gb300.signal import event_array
+    _build.build()
+    torch.cuda.set_device(0)
+    n = args.events if args.events != N_EVENTS else 1000000
+    pt = event_array(synthetic.screen_population(args.train_events, seed=2004))
+    target = np.log(np.random.default_rng(0).uniform(1.0, 100.0, pt.shape[1]))
+    mlp = _lib.MLP(hidden=256, layers=4, seed=1)
+    t0 = time.perf_counter()
+    loss = mlp.train(pt, target, epochs=args.train_epochs, batch=4096, lr=1e-3)
+    t_train = time.perf_counter() - t0
+    lib = _lib.load()
+    dp = torch.from_numpy(event_array(synthetic.screen_population(n, seed=1004))).cuda()
+    out = torch.empty(n, dtype=torch.float64, device='cuda')
+
+    def pred():
+        _lib.check(lib.gwf_mlp_predict(mlp.h, _lib.ptr(dp), n, n, _lib.MEM_DEVICE, _lib.ptr(out)))
+
+    for _ in range(args.warmup):
+        pred()
+    ts = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pred()
+        ts.append(time.perf_counter() - t0)
+    t = statistics.median(ts)
+    print(json.dumps({'metric': 'MLP ln SNR predictions/s (11 -> 4 x 256 SiLU -> 1, BF16 weights, tensor cores)',
+                      'value': n / t, 'unit': 'predictions/s', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
+                      'ms_per_step': 1e3 * t, 'higher_is_better': True, 'events': n,
+                      'train_s': t_train, 'train_epochs': args.train_epochs, 'train_events': args.train_events,
+                      'train_loss': loss, 'data': 'synthetic (seeded population)'}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -463,9 +502,10 @@ def main():
     ap.add_argument('--precision', default='fp32', choices=('fp32', 'fp64', 'mixed'), help='form used with --only-device')
     ap.add_argument('--refine-cond', type=float, default=1e13, help='condition-number threshold of the mixed form')
     ap.add_argument('--no-autotune', action='store_true', help='per-event launches, no segment autotuning')
-    ap.add_argument('--workload', default='lhet', choices=('lhet', 'mixed-catalogue', 'screen', 'hm'),
+    ap.add_argument('--workload', default='lhet', choices=('lhet', 'mixed-catalogue', 'screen', 'hm', 'mlp'),
                     help='lhet: the headline workload; mixed-catalogue: the batching workload; screen: the learned '
-                         'SNR screen on a 10^6-event population; hm: IMRPhenomHM on ET + CE (separate lines)')
+                         'SNR screen on a 10^6-event population; hm: IMRPhenomHM on ET + CE; mlp: the screen network '
+                         'alone, training and inference (separate lines)')
     ap.add_argument('--headline-only', action='store_true', help='leave out the other workloads\' keys')
     ap.add_argument('--train-events', type=int, default=200000)
     ap.add_argument('--train-epochs', type=int, default=40)
@@ -478,6 +518,8 @@ def main():
         return run_screen(args)
     if args.workload == 'hm':
         return run_hm(args)
+    if args.workload == 'mlp':
+        return run_mlp(args)
     rank, world, local = dist_info()
     import torch
     if world > 1:
