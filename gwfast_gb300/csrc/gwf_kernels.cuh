@@ -15,6 +15,17 @@ namespace gwf {
 
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
+
+// Per-event kernels (set-up records, projections, condition numbers) run one thread per event,
+// epw events per warp (lanes >= epw idle), kEvBlock threads per block. Their FP64 chains are long
+// and latency-bound: a batch too small to give every SM sub-partition a few warps runs faster
+// spread over more, partly filled warps than packed into full ones (ev_lanes on the host).
+constexpr int kEvBlock = 64;
+__device__ __forceinline__ long long ev_thread(int epw) {
+  const int lane = threadIdx.x & 31;
+  if (lane >= epw) return -1;
+  return ((long long)blockIdx.x * (kEvBlock / 32) + (threadIdx.x >> 5)) * epw + lane;
+}
 constexpr int NP = 11;    // Fisher parameters
 constexpr int NE = 66;    // upper-triangle entries
 // Fisher order: Mc, eta, dL, theta, phi, iota, psi, tcoal, Phicoal, chi1z, chi2z
@@ -585,12 +596,12 @@ __device__ __forceinline__ const PhaseBasis* rec_basis(const unsigned char* scra
 // it and recomputes only the detector-dependent part (the per-event set-up is FP64-bound, and a
 // network evaluates it once per detector)
 template <int MODEL>
-__global__ void __launch_bounds__(64) setup_kernel(EvBatch ev, DetDev det, WfDesc wf, const double* qnm, int nq,
-                                                    unsigned char* scratch, long long count, unsigned char* core,
-                                                    int core_mode, const long long* core_idx) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kEvBlock) setup_kernel(EvBatch ev, DetDev det, WfDesc wf, const double* qnm, int nq,
+                                                          unsigned char* scratch, long long count, unsigned char* core,
+                                                          int core_mode, const long long* core_idx, int epw) {
+  const long long i = ev_thread(epw);
   const long long n = ev.n0 + i;
-  if (i >= count || n >= ev.N) return;
+  if (i < 0 || i >= count || n >= ev.N) return;
   unsigned char* rec = scratch + i * rec_stride<MODEL>();
   SetupHdr& h = *reinterpret_cast<SetupHdr*>(rec);
   EvUnion& E = *reinterpret_cast<EvUnion*>(rec + sizeof(SetupHdr));

@@ -712,10 +712,10 @@ template <int MODEL>
 __host__ __device__ constexpr size_t f32_stride() { return ((sizeof(F32Rec<MODEL>) + 15) / 16) * 16; }
 
 template <int MODEL>
-__global__ void __launch_bounds__(64) setup_f32_kernel(DetDev det, const unsigned char* scratch, unsigned char* scratch32,
-                                                       long long count, int narm, int earth) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= count) return;
+__global__ void __launch_bounds__(kEvBlock) setup_f32_kernel(DetDev det, const unsigned char* scratch, unsigned char* scratch32,
+                                                             long long count, int narm, int earth, int epw) {
+  const long long i = ev_thread(epw);
+  if (i < 0 || i >= count) return;
   const unsigned char* rec = scratch + i * rec_stride<MODEL>();
   const SetupHdr& h = *reinterpret_cast<const SetupHdr*>(rec);
   const EvUnion& E = *reinterpret_cast<const EvUnion*>(rec + sizeof(SetupHdr));
@@ -770,11 +770,11 @@ __global__ void __launch_bounds__(64) setup_f32_kernel(DetDev det, const unsigne
 // projection from their FP32 record slot: the pattern-function constants in FP64, rounded once
 // (one thread per event). Nothing else of their slot is written.
 template <int MODEL>
-__global__ void __launch_bounds__(64) proj_f32_kernel(EvBatch ev, DetDev det, unsigned char* scratch32, long long count,
-                                                      int narm, int earth) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kEvBlock) proj_f32_kernel(EvBatch ev, DetDev det, unsigned char* scratch32, long long count,
+                                                            int narm, int earth, int epw) {
+  const long long i = ev_thread(epw);
   const long long n = ev.n0 + i;
-  if (i >= count || n >= ev.N) return;
+  if (i < 0 || i >= count || n >= ev.N) return;
   const double* p = ev.p;
   const long long ld = ev.ld;
   ProjEv pj;
@@ -790,10 +790,11 @@ __global__ void __launch_bounds__(64) proj_f32_kernel(EvBatch ev, DetDev det, un
 // FP64 set-up records copied from another detector of the same grid: only the projection header is
 // the detector's own (events ev.n0 .. of a gathered batch, records 0 .. count - 1)
 template <int MODEL>
-__global__ void __launch_bounds__(64) proj_patch_kernel(EvBatch ev, DetDev det, unsigned char* scratch, long long count) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kEvBlock) proj_patch_kernel(EvBatch ev, DetDev det, unsigned char* scratch, long long count,
+                                                              int epw) {
+  const long long i = ev_thread(epw);
   const long long n = ev.n0 + i;
-  if (i >= count || n >= ev.N) return;
+  if (i < 0 || i >= count || n >= ev.N) return;
   const double* p = ev.p;
   const long long ld = ev.ld;
   SetupHdr& h = *reinterpret_cast<SetupHdr*>(scratch + i * rec_stride<MODEL>());

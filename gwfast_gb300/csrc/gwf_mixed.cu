@@ -17,9 +17,10 @@ namespace {
 // eigen-decomposition of the covariance kernel; only used to pick events for FP64, where a
 // factor of a few does not matter: the largest eigenvalue of an equilibrated 11 x 11 matrix lies
 // in [1, 11] and the Rayleigh quotients converge quadratically, so 12 and 8 steps suffice.
-__global__ void __launch_bounds__(64) cond_kernel(const double* __restrict__ F, long long N, double* __restrict__ cond) {
-  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= N) return;
+__global__ void __launch_bounds__(kEvBlock) cond_kernel(const double* __restrict__ F, long long N, double* __restrict__ cond,
+                                                       int epw) {
+  const long long n = ev_thread(epw);
+  if (n < 0 || n >= N) return;
   constexpr int K = NP;
   // the factor is kept as a packed lower triangle and every loop over rows and columns is unrolled,
   // so that it stays in registers (indexed arrays would live in local memory)
@@ -173,7 +174,8 @@ unsigned blocks(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 cudaError_t launch_cond(const double* F, long long N, double* cond, cudaStream_t st) {
   if (N <= 0) return cudaSuccess;
-  cond_kernel<<<blocks(N, 64), 64, 0, st>>>(F, N, cond);
+  const int epw = ev_lanes(N);
+  cond_kernel<<<ev_blocks(N, epw), kEvBlock, 0, st>>>(F, N, cond, epw);
   return cudaGetLastError();
 }
 

@@ -26,20 +26,14 @@ __global__ void copy_records_kernel(const uint4* __restrict__ src, const long lo
   dst[t] = src[idx[i] * W + (t - i * W)];
 }
 
-int sm_count() {
-  int dev = 0, n = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-  return n > 0 ? n : 1;
-}
-
 template <class MAIN>
 cudaError_t chunked(const LaunchArgs& a, bool f32, MAIN main) {
   for (long long n0 = 0; n0 < a.ev.N; n0 += kChunk) {
     EvBatch ev = a.ev;
     ev.n0 = n0;
     const long long cnt = (a.ev.N - n0) < kChunk ? (a.ev.N - n0) : kChunk;
-    const unsigned nb = (unsigned)((cnt + 63) / 64);
+    const int epw = ev_lanes(cnt);
+    const unsigned nb = ev_blocks(cnt, epw);
     if (a.timer) {
       const cudaError_t et = a.timer->begin(a.stream, GWF_KT_SETUP);
       if (et != cudaSuccess) return et;
@@ -49,19 +43,19 @@ cudaError_t chunked(const LaunchArgs& a, bool f32, MAIN main) {
       copy_records_kernel<<<(unsigned)((words + 255) / 256), 256, 0, a.stream>>>(
           reinterpret_cast<const uint4*>(a.rec_src), a.core_idx + n0, cnt, reinterpret_cast<uint4*>(a.scratch));
       if constexpr (M < 3) {   // (only the detector groups of the FP32 forms share records)
-        if (a.rec_patch_proj) proj_patch_kernel<M><<<nb, 64, 0, a.stream>>>(ev, a.det, a.scratch, cnt);
+        if (a.rec_patch_proj) proj_patch_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(ev, a.det, a.scratch, cnt, epw);
       }
     } else {
-      setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, a.det, a.wf, a.qnm, a.nq, a.scratch, cnt, a.core, a.core_mode,
-                                               a.core_idx);
+      setup_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(ev, a.det, a.wf, a.qnm, a.nq, a.scratch, cnt, a.core, a.core_mode,
+                                                     a.core_idx, epw);
     }
     if (a.core_done && a.core_mode == 1) {
       const cudaError_t er = cudaEventRecord(a.core_done, a.stream);
       if (er != cudaSuccess) return er;
     }
     if constexpr (M < 3) {   // (the tidal models have no FP32 form)
-      if (f32) setup_f32_kernel<M><<<nb, 64, 0, a.stream>>>(a.det, a.scratch, scratch32_of(a), cnt,
-                                                            a.det.shape == 1 ? 2 : 1, a.det.earth);
+      if (f32) setup_f32_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(a.det, a.scratch, scratch32_of(a), cnt,
+                                                                  a.det.shape == 1 ? 2 : 1, a.det.earth, epw);
     }
     if (a.timer) {
       const cudaError_t et = a.timer->end(a.stream);
@@ -107,7 +101,7 @@ cudaError_t persist_grid(K k, int smem, int* grid) {
   int occ = 0;
   const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kThreads, smem);
   if (e != cudaSuccess) return e;
-  *grid = (occ > 0 ? occ : 1) * sm_count();
+  *grid = (occ > 0 ? occ : 1) * device_sms();
   return cudaSuccess;
 }
 
@@ -239,7 +233,8 @@ cudaError_t group_one(const LaunchArgs& a, GroupDev g) {
     EvBatch ev = a.ev;
     ev.n0 = n0;
     const long long cnt = (a.ev.N - n0) < chunk ? (a.ev.N - n0) : chunk;
-    const unsigned nb = (unsigned)((cnt + 63) / 64);
+    const int epw = ev_lanes(cnt);
+    const unsigned nb = ev_blocks(cnt, epw);
     if (a.timer) {
       err = a.timer->begin(a.stream, GWF_KT_SETUP);
       if (err != cudaSuccess) return err;
@@ -248,15 +243,18 @@ cudaError_t group_one(const LaunchArgs& a, GroupDev g) {
       unsigned char* sc = a.scratch + (size_t)d * chunk * stride;
       unsigned char* s32 = sc + (size_t)chunk * rec_stride<M>();
       if (d > 0) {   // same grid and model record as detector 0: only the projection is its own
-        proj_f32_kernel<M><<<nb, 64, 0, a.stream>>>(ev, g.det[d], s32, cnt, g.det[d].shape == 1 ? 2 : 1, g.det[d].earth);
+        proj_f32_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(ev, g.det[d], s32, cnt, g.det[d].shape == 1 ? 2 : 1,
+                                                          g.det[d].earth, epw);
         continue;
       }
-      setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, g.det[d], a.wf, a.qnm, a.nq, sc, cnt, a.core, a.core_mode, nullptr);
+      setup_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(ev, g.det[d], a.wf, a.qnm, a.nq, sc, cnt, a.core, a.core_mode,
+                                                     nullptr, epw);
       if (a.core_done && a.core_mode == 1) {
         err = cudaEventRecord(a.core_done, a.stream);
         if (err != cudaSuccess) return err;
       }
-      setup_f32_kernel<M><<<nb, 64, 0, a.stream>>>(g.det[d], sc, s32, cnt, g.det[d].shape == 1 ? 2 : 1, g.det[d].earth);
+      setup_f32_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(g.det[d], sc, s32, cnt, g.det[d].shape == 1 ? 2 : 1,
+                                                         g.det[d].earth, epw);
     }
     if (a.timer) {
       err = a.timer->end(a.stream);
@@ -285,8 +283,9 @@ template <bool EARTH, int NARM>
 cudaError_t wave_one(const LaunchArgs& a, const WaveOut& o) {
   EvBatch ev = a.ev;
   ev.n0 = o.n0;
-  const unsigned nb = (unsigned)((o.cnt + 63) / 64);
-  setup_kernel<M><<<nb, 64, 0, a.stream>>>(ev, a.det, a.wf, a.qnm, a.nq, a.scratch, o.cnt, nullptr, 0, nullptr);
+  const int epw = ev_lanes(o.cnt);
+  setup_kernel<M><<<ev_blocks(o.cnt, epw), kEvBlock, 0, a.stream>>>(ev, a.det, a.wf, a.qnm, a.nq, a.scratch, o.cnt,
+                                                                    nullptr, 0, nullptr, epw);
   wave_out_kernel<M, EARTH, NARM><<<(unsigned)o.cnt, kThreads, 0, a.stream>>>(ev, a.det, a.scratch, o);
   return cudaGetLastError();
 }
