@@ -102,7 +102,10 @@ struct gwf_ctx {
   // IMRPhenomD headline workload (max 7.0e-5 with either threshold 1e12 or 1e13)
   double refine_cond = 1e13;
   int seg_points = 0;      // Fisher launches: 0 = one CTA per event, > 0 = persistent, segments of this many points
-  int refine_seg = 256;    // segment length of the FP64 recomputation of GWF_PREC_MIXED
+  // segment length of the FP64 recomputation of GWF_PREC_MIXED: one point per thread (few events,
+  // each thread's FP64 chain is the latency; 15 events of 10^4 at R = 2000: the recomputation took
+  // 1.16 ms of stream time at 256 points per segment, 0.79 ms at 128 with the grid capped)
+  int refine_seg = 128;
   DevBuf seg_off, seg_ctr, seg_part, seg_ovf, tune_out;
   // SNR-derivative outputs of the current gwf_fisher_ex call (host or device pointers, as mem says)
   double* call_sd_arm = nullptr;

@@ -1186,8 +1186,15 @@ __device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32S
   __syncthreads();
 }
 
+// Six blocks per SM (80 registers) for the 22-mode models: the fixed-latency FP32 chains are its top
+// stall and two more warps per SM outweigh the extra spills (IMRPhenomD, L1 + H1, 10^4 events:
+// 2.688 ms against 2.729 ms at five blocks and 96 registers); IMRPhenomHM, with its FP64 mode
+// phases, keeps five. (The triangle kernel was slower at six: 2.390 against 2.305 ms.)
+template <int MODEL>
+__host__ __device__ constexpr int group_min_blocks() { return MODEL == 2 ? 5 : 6; }
+
 template <int MODEL, bool EARTH, bool TRI>
-__global__ void __launch_bounds__(kThreads, 5) fisher_group_kernel_f32(EvBatch ev, GroupDev g,
+__global__ void __launch_bounds__(kThreads, group_min_blocks<MODEL>()) fisher_group_kernel_f32(EvBatch ev, GroupDev g,
                                                                        const unsigned char* scratch32, double* out_det,
                                                                        int accum) {
   extern __shared__ __align__(16) unsigned char stage_raw[];

@@ -88,6 +88,9 @@ cudaError_t seg_chunk(const LaunchArgs& a, const EvBatch& ev, long long cnt, KSE
   e = cudaMemsetAsync(a.seg_ctr, 0, sizeof(unsigned long long), a.stream);
   if (e != cudaSuccess) return e;
   const SegInfo si = seg_info(a);
+  // no more CTAs than items (seg_cap bounds them): a small batch then spreads over distinct SMs
+  // instead of stacking on the first SMs of a full persistent grid
+  if (a.seg_cap > 0 && a.seg_cap < grid) grid = (int)a.seg_cap;
   ks<<<grid, kThreads, smem, a.stream>>>(ev, a.det, kscratch, cnt, si, (a.out_sd_arm || a.out_sd_det) ? 1 : 0);
   gram_reduce_kernel<NG><<<(unsigned)cnt, kThreads, 0, a.stream>>>(ev.n0, ev.N, cnt, si, rec, stride_d, a.out_arm,
                                                                    a.out_det, a.out_sd_arm, a.out_sd_det, a.accum);
