@@ -71,10 +71,11 @@ struct DetRec {
   double* d_f = nullptr;
   double* d_S = nullptr;
   int* d_acc = nullptr;
-  float* d_f32 = nullptr;
-  float* d_s32 = nullptr;
+  float4* d_seg = nullptr;
   int n = 0, nacc = 0;
   double l0 = 0.0, idl = 0.0, scale = 1.0;
+  int psd_class = 0;   // id of the first detector added with an identical PSD table
+  std::vector<double> h_f, h_S;
 };
 
 struct GraphEntry {
@@ -271,8 +272,9 @@ gwf::DetDev dev_of(const DetRec& r) {
   d.nacc = r.nacc;
   d.acc_l0 = r.l0;
   d.acc_idl = r.idl;
-  d.psd_f32 = r.d_f32;
-  d.psd_s32 = r.d_s32;
+  d.psd_seg = r.d_seg;
+  d.psd_f32_lo = r.n > 0 ? (float)r.h_f.front() : 0.0f;
+  d.psd_f32_hi = r.n > 0 ? (float)r.h_f.back() : 0.0f;
   d.psd_scale = r.scale;
   return d;
 }
@@ -753,6 +755,7 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
       for (int d = 0; d < g.nd; ++d) {
         g.det[d] = dev_of(ctx->dets[det_ids[grp[d]]]);
         g.wr[d] = (float)std::sqrt(g.det[0].psd_scale / g.det[d].psd_scale);
+        g.same_psd[d] = d > 0 && ctx->dets[det_ids[grp[d]]].psd_class == ctx->dets[det_ids[grp[d - 1]]].psd_class;
       }
       g.slice = 0;
       // the group's other detectors get only their projection in the first pass (their FP64 records
@@ -893,8 +896,7 @@ int gwf_ctx_destroy(gwf_ctx* ctx) {
     cudaFree(r.d_f);
     cudaFree(r.d_S);
     cudaFree(r.d_acc);
-    cudaFree(r.d_f32);
-    cudaFree(r.d_s32);
+    cudaFree(r.d_seg);
   }
   cudaFree(ctx->d_qnm);
   ctx->par.release(); ctx->res.release(); ctx->oarm.release(); ctx->onet.release();
@@ -995,7 +997,7 @@ int gwf_detector_add(gwf_ctx* ctx, const gwf_det_desc* desc, const double* psd_f
   GWF_CK(cudaMemcpy(r.d_f, psd_f, n * sizeof(double), cudaMemcpyHostToDevice));
   GWF_CK(cudaMemcpy(r.d_S, psd_S, n * sizeof(double), cudaMemcpyHostToDevice));
   GWF_CK(cudaMemcpy(r.d_acc, acc.data(), r.nacc * sizeof(int), cudaMemcpyHostToDevice));
-  // FP32 copies: frequencies, and the PSD divided by its smallest positive value
+  // FP32 segments: frequencies, and the PSD divided by its smallest positive value
   double smin = INFINITY;
   for (int64_t i = 0; i < n; ++i)
     if (psd_S[i] > 0.0 && psd_S[i] < smin) smin = psd_S[i];
@@ -1005,10 +1007,18 @@ int gwf_detector_add(gwf_ctx* ctx, const gwf_det_desc* desc, const double* psd_f
     f32[i] = (float)psd_f[i];
     s32[i] = (float)(psd_S[i] / r.scale);
   }
-  GWF_CK(cudaMalloc(&r.d_f32, n * sizeof(float)));
-  GWF_CK(cudaMalloc(&r.d_s32, n * sizeof(float)));
-  GWF_CK(cudaMemcpy(r.d_f32, f32.data(), n * sizeof(float), cudaMemcpyHostToDevice));
-  GWF_CK(cudaMemcpy(r.d_s32, s32.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  std::vector<float4> seg(n - 1);
+  for (int64_t i = 0; i + 1 < n; ++i) {
+    const double y0 = psd_S[i] / r.scale, y1 = psd_S[i + 1] / r.scale;
+    seg[i] = make_float4(f32[i], f32[i + 1], s32[i], (float)((y1 - y0) / (psd_f[i + 1] - psd_f[i])));
+  }
+  GWF_CK(cudaMalloc(&r.d_seg, (n - 1) * sizeof(float4)));
+  GWF_CK(cudaMemcpy(r.d_seg, seg.data(), (n - 1) * sizeof(float4), cudaMemcpyHostToDevice));
+  r.h_f.assign(psd_f, psd_f + n);
+  r.h_S.assign(psd_S, psd_S + n);
+  r.psd_class = (int)ctx->dets.size();
+  for (const DetRec& o : ctx->dets)
+    if (o.h_f == r.h_f && o.h_S == r.h_S) { r.psd_class = o.psd_class; break; }
   ctx->dets.push_back(r);
   *det_id = (int)ctx->dets.size() - 1;
   return GWF_OK;

@@ -68,8 +68,10 @@ struct DetDev {
   const int* acc;        // log-frequency bin -> table index (accelerates the PSD lookup)
   int nacc;
   double acc_l0, acc_idl;
-  const float* psd_f32;  // FP32 copies for the split-precision kernel: frequencies and PSD / psd_scale
-  const float* psd_s32;
+  // FP32 copy for the split-precision kernels, as linear segments (one 16-byte load per step):
+  // segment j is (f_j, f_j+1, S_j / psd_scale, slope), the slope formed in FP64 and rounded once
+  const float4* psd_seg;
+  float psd_f32_lo, psd_f32_hi;   // first and last table frequency (FP32)
   double psd_scale;
 };
 

@@ -154,17 +154,16 @@ __device__ __forceinline__ void arm_derivs_f(const ProjF& q, const ArmF& ap, con
 // np.interp on the FP32 table normalised by its minimum; outside the table the reference PSD of 1
 // gives weights ~1e-46 of in-band ones, represented here as exactly zero.
 __device__ __forceinline__ float psd_at_f(const DetDev& d, float f, float lnf, float acc_l0, float acc_idl) {
-  const float* xf = d.psd_f32;
   const int n = d.npsd;
-  if (!(f >= xf[0]) || f > xf[n - 1]) return INFINITY;
+  if (!(f >= d.psd_f32_lo) || f > d.psd_f32_hi) return INFINITY;
   int b = (int)((lnf - acc_l0) * acc_idl);
   b = b < 0 ? 0 : (b >= d.nacc ? d.nacc - 1 : b);
-  int j = d.acc[b];
-  while (j > 0 && xf[j] > f) --j;
-  while (j < n - 2 && xf[j + 1] <= f) ++j;
-  const float x0 = xf[j], x1 = xf[j + 1];
-  const float y0 = d.psd_s32[j], y1 = d.psd_s32[j + 1];
-  return y0 + (f - x0) * ((y1 - y0) / (x1 - x0));
+  int j = __ldg(d.acc + b);
+  // the segment [f_j, f_j+1) holding f (the accelerator's row is at most a step or two off)
+  float4 sg = __ldg(d.psd_seg + j);
+  while (j > 0 && sg.x > f) sg = __ldg(d.psd_seg + --j);
+  while (j < n - 2 && sg.y <= f) sg = __ldg(d.psd_seg + ++j);
+  return fmaf(f - sg.x, sg.w, sg.z);
 }
 
 union EvUnionF {
@@ -1046,6 +1045,7 @@ constexpr int kMaxGroup = 4;
 struct GroupDev {
   DetDev det[kMaxGroup];
   float wr[kMaxGroup];   // sqrt(psd_scale of detector 0 / psd_scale of detector d): common Gram scale
+  int same_psd[kMaxGroup];   // detector d has detector d - 1's PSD table (and scale): same weight per point
   int nd;
   long long slice;       // bytes between the FP32 record areas of consecutive detectors
 };
@@ -1127,6 +1127,7 @@ __device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32S
   };
   GridIterF grid;
   const int nd = g.nd;
+  float sw = 0.0f;
   for (int base = 0; base < k1; base += kThreads) {
     const int k = base + tid;
     grid.step(r, ev.spacing, base, lane, warp);
@@ -1142,8 +1143,8 @@ __device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32S
     if (EARTH && valid) rot_sc(wv, sd, cd);
     for (int d = 0; d < nd; ++d) {
       const DetDev& det = g.det[d];
-      float sw = 0.0f;
-      if (valid) sw = sqrtf(4.0f * w / psd_at_f(det, f, lnf, (float)det.acc_l0, (float)det.acc_idl)) * g.wr[d];
+      if (!(d > 0 && g.same_psd[d]))   // (a detector sharing the previous one's table reuses its weight)
+        sw = valid ? sqrtf(4.0f * w / psd_at_f(det, f, lnf, (float)det.acc_l0, (float)det.acc_idl)) * g.wr[d] : 0.0f;
       cf u[NP];
       if (!TRI || det.shape == 0) {
         cf D[1][NP], Hs[1];

@@ -217,8 +217,8 @@ extern "C" int gwf_fisher_noalloc(const gwf_det_desc* det, const double* psd_f, 
   a.det.nacc = kAccBins;
   a.det.acc_l0 = l0;
   a.det.acc_idl = idl;
-  a.det.psd_f32 = nullptr;
-  a.det.psd_s32 = nullptr;
+  a.det.psd_seg = nullptr;
+  a.det.psd_f32_lo = a.det.psd_f32_hi = 0.0f;
   a.det.psd_scale = 1.0;
   a.wf.model = wf->model;
   a.wf.spin_ho = wf->spin_ho;
