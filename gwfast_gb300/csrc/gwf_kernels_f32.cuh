@@ -383,9 +383,20 @@ struct WaveF {
   float dtn[4];   // d t_noloc / d theta_k (days)
 };
 
+// The 22-mode waveform at one point in compact form: amplitude A, the tangent dW = dA - i A dPhi of
+// W = A e^{-i Phi} (common phase dropped) and the time to coalescence. The strain's polarisations are
+// W times per-event constants (hp = cp W, hx = i ci W), so a detector group keeps only this across
+// its detector loop and expands it per detector (expand22), which saves registers.
+struct Wave22 {
+  float A;
+  cf dW[4];
+  float tau;      // tau_star (s)
+  float dtn[4];   // d t_noloc / d theta_k (days)
+};
+
 template <int MODEL, bool EARTH>
-__device__ __forceinline__ void wave_f32(const EvUnionF& EF, const PBF& pbf, const ProjF& pf, const TauF& tf, float f,
-                                         float lnf, WaveF& w) {
+__device__ __forceinline__ void wave22_f32(const EvUnionF& EF, const PBF& pbf, const TauF& tf, float f, float lnf,
+                                           Wave22& w) {
   DF4 A;
   float dphi[4];
   phase_tangent_f(pbf, f, lnf, dphi);
@@ -404,17 +415,33 @@ __device__ __forceinline__ void wave_f32(const EvUnionF& EF, const PBF& pbf, con
 #pragma unroll
     for (int q = 0; q < 4; ++q) w.dtn[q] = -dtau[q] * (1.0f / 86400.0f);
   }
-  w.P = {pf.cp * A.v, 0.0f};
-  w.C = {pf.ci * A.v, 0.0f};
+  w.A = A.v;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) w.dW[q] = {A.d[q], -A.v * dphi[q]};
+}
+
+__device__ __forceinline__ void expand22(const Wave22& c, const ProjF& pf, WaveF& w) {
+  w.tau = c.tau;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) w.dtn[q] = c.dtn[q];
+  w.P = {pf.cp * c.A, 0.0f};
+  w.C = {pf.ci * c.A, 0.0f};
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    const cf dW = {A.d[q], -A.v * dphi[q]};
-    w.dP[q] = fscale(dW, pf.cp);
-    w.dC[q] = fscale(dW, pf.ci);
+    w.dP[q] = fscale(c.dW[q], pf.cp);
+    w.dC[q] = fscale(c.dW[q], pf.ci);
   }
-  w.dPi = {pf.dcp * A.v, 0.0f};
-  w.dCi = {pf.dci * A.v, 0.0f};
-  w.Q = {A.v * pf.dcs, 0.0f};   // P - s C = A (cp - s ci) = A (1 - |cos i|)^2 / 2
+  w.dPi = {pf.dcp * c.A, 0.0f};
+  w.dCi = {pf.dci * c.A, 0.0f};
+  w.Q = {c.A * pf.dcs, 0.0f};   // P - s C = A (cp - s ci) = A (1 - |cos i|)^2 / 2
+}
+
+template <int MODEL, bool EARTH>
+__device__ __forceinline__ void wave_f32(const EvUnionF& EF, const PBF& pbf, const ProjF& pf, const TauF& tf, float f,
+                                         float lnf, WaveF& w) {
+  Wave22 c;
+  wave22_f32<MODEL, EARTH>(EF, pbf, tf, f, lnf, c);
+  expand22(c, pf, w);
 }
 
 // The detector part: derivative vectors d h / d theta of every arm (11 parameters) and the strain.
@@ -442,9 +469,10 @@ __device__ __forceinline__ void project_f32_rot(const WaveF& w, const ProjF& pf,
 }
 
 // sin and cos of the point's Earth-rotation angle 2 pi delta, delta = -tau_star / day
-__device__ __forceinline__ void rot_sc(const WaveF& w, float& sd, float& cd) {
-  sincosf(6.2831853071795865f * (-w.tau * (1.0f / 86400.0f)), &sd, &cd);
+__device__ __forceinline__ void rot_sc_tau(float tau, float& sd, float& cd) {
+  sincosf(6.2831853071795865f * (-tau * (1.0f / 86400.0f)), &sd, &cd);
 }
+__device__ __forceinline__ void rot_sc(const WaveF& w, float& sd, float& cd) { rot_sc_tau(w.tau, sd, cd); }
 
 template <bool EARTH, int NARM>
 __device__ __forceinline__ void project_f32(const WaveF& w, const ProjF& pf, const ArmF* apc, const TimeF& tsc, float f,
@@ -1133,18 +1161,24 @@ __device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32S
     grid.step(r, ev.spacing, base, lane, warp);
     const bool valid = k < k1;
     float f = 0.0f, lnf = 0.0f, w = 0.0f;
+    // the waveform once per point for the group: the 22-mode models keep its compact form across
+    // the detector loop and expand it per detector (fewer live registers)
     WaveF wv;
+    Wave22 wc;
     if (valid) {
       grid.point(r, ev.spacing, k, lane, f, lnf, w);
       if constexpr (MODEL == 2) wave_f32_hm<EARTH>(r.ef, r.pf, r.tf, f, lnf, wv);
-      else wave_f32<MODEL, EARTH>(r.ef, r.pbf, r.pf, r.tf, f, lnf, wv);
+      else wave22_f32<MODEL, EARTH>(r.ef, r.pbf, r.tf, f, lnf, wc);
     }
     float sd = 0.0f, cd = 1.0f;   // the Earth-rotation angle is the same for every detector
-    if (EARTH && valid) rot_sc(wv, sd, cd);
+    if (EARTH && valid) rot_sc_tau(MODEL == 2 ? wv.tau : wc.tau, sd, cd);
     for (int d = 0; d < nd; ++d) {
       const DetDev& det = g.det[d];
       if (!(d > 0 && g.same_psd[d]))   // (a detector sharing the previous one's table reuses its weight)
         sw = valid ? sqrtf(4.0f * w / psd_at_f(det, f, lnf, (float)det.acc_l0, (float)det.acc_idl)) * g.wr[d] : 0.0f;
+      if constexpr (MODEL != 2) {
+        if (valid) expand22(wc, gp.pf[d], wv);
+      }
       cf u[NP];
       if (!TRI || det.shape == 0) {
         cf D[1][NP], Hs[1];
@@ -1189,8 +1223,9 @@ __device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32S
 
 // Six blocks per SM (80 registers) for the 22-mode models: the fixed-latency FP32 chains are its top
 // stall and two more warps per SM outweigh the extra spills (IMRPhenomD, L1 + H1, 10^4 events:
-// 2.688 ms against 2.729 ms at five blocks and 96 registers); IMRPhenomHM, with its FP64 mode
-// phases, keeps five. (The triangle kernel was slower at six: 2.390 against 2.305 ms.)
+// 2.688 ms against 2.729 ms at five blocks and 96 registers; seven blocks, 72 registers, 2.45 ms
+// against 2.39 ms once the compact waveform cut the spills); IMRPhenomHM, with its FP64 mode phases,
+// keeps five. (The triangle kernel was slower at six: 2.390 against 2.305 ms.)
 template <int MODEL>
 __host__ __device__ constexpr int group_min_blocks() { return MODEL == 2 ? 5 : 6; }
 
