@@ -43,8 +43,8 @@ RES = 2000
 SNR_TH = 12.
 METRIC = 'network Fisher matrices/s (IMRPhenomD, L1+H1+ETS, Earth rotation, R=2000)'
 # DRAM bytes (read + write) per event of the L1 + H1 group launch, from one ncu capture of a
-# 2048-event launch (6.513 MB read, 0.052 MB written)
-GRP_DRAM_BYTES_PER_EVENT = (6.513152e6 + 5.248e4) / 2048
+# 2048-event launch (6.575 MB read, 0.055 MB written)
+GRP_DRAM_BYTES_PER_EVENT = (6.575104e6 + 5.4784e4) / 2048
 
 
 def dist_info():
