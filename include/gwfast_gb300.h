@@ -244,7 +244,11 @@ int gwf_cov_n(gwf_ctx* ctx, const double* F, int64_t N, int n_params, int mem, d
  * accumulates in FP32. Features: ln Mc, eta, ln dL, cos theta, sin and cos of (phi - 2 pi tcoal),
  * cos iota, sin and cos of 2 psi, chi1z, chi2z, standardised by the mean and deviation of the
  * training events. params as in gwf_fisher ([11][ld], Fisher order); mem as in gwf_fisher. The MLP
- * lives on the context's device and runs on its own stream; calls are synchronous. */
+ * lives on the context's device and runs on its own stream; calls are synchronous. With hidden a
+ * multiple of 64 up to 256, the hidden-to-hidden products run on the tensor cores (tcgen05.mma, BF16
+ * operands, FP32 accumulation in tensor memory): in training as one GEMM per layer and pass, in
+ * gwf_mlp_predict as one fused kernel per 128 events with the activations kept on chip. A tensor-core
+ * completion wait that runs out returns GWF_ERR_TIMEOUT (the GPU stays usable). */
 int gwf_mlp_create(gwf_ctx* ctx, int hidden, int layers, uint64_t seed, gwf_mlp** out);
 int gwf_mlp_destroy(gwf_mlp* mlp);
 /* weights + biases in the flat layout [W_0 (11 x H), W_1 (H x H), ..., W_L (H x 1), b_0, ..., b_L],
