@@ -58,6 +58,8 @@ SIGNATURES = {
                        ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
     'gwf_strain_derivs': ([_vp, ctypes.c_int, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32, ctypes.c_int, ctypes.c_int,
                            _vp, _vp], ctypes.c_int),
+    'gwf_strain': ([_vp, ctypes.c_int, _P(WfDesc), _vp, _i64, _i64, _vp, _i64, ctypes.c_int32, ctypes.c_int, _vp, _vp,
+                    _vp, _vp], ctypes.c_int),
     'gwf_overlap': ([_vp, ctypes.c_int, _vp, _P(WfDesc), _vp, _i64, _P(WfDesc), _vp, _i64, _i64, ctypes.c_int32,
                      ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     'gwf_cov': ([_vp, _vp, _i64, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
@@ -186,6 +188,18 @@ class Context:
         ld = params.shape[1] if ld is None else ld
         check(load().gwf_strain_derivs(self.h, int(det_id), ctypes.byref(wf), ptr(params), ld, n, int(res), spacing,
                                        mem, ptr(out), stream))
+
+    def strain(self, det_id, wf, params, freqs, out_strain=None, out_amp=None, out_phase=None, mem=MEM_HOST,
+               stream=None, ld=None, n=None):
+        """Strain, amplitudes and phases at caller frequencies: freqs float64 (R,) shared by all events or
+        (N, R) per event; out_strain / out_amp complex128 [arms][N][R] (amp: A+ + i Ax), out_phase
+        float64 [2][N][R] (GWPhase, the strain's phase)."""
+        n = params.shape[1] if n is None else n
+        ld = params.shape[1] if ld is None else ld
+        R = freqs.shape[-1]
+        f_ld = freqs.shape[-1] if freqs.ndim == 2 else 0
+        check(load().gwf_strain(self.h, int(det_id), ctypes.byref(wf), ptr(params), ld, n, ptr(freqs), f_ld, int(R), mem,
+                                ptr(out_strain), ptr(out_amp), ptr(out_phase), stream))
 
     def overlap(self, det_ids, wf1, params1, wf2, params2, res, mem=MEM_HOST, out_ov=None, out_n1=None, out_n2=None,
                 stream=None, n=None):

@@ -119,6 +119,7 @@ struct gwf_ctx {
   cudaEvent_t scratch_free = nullptr;  // recorded after the last launch that used the set-up scratch
   HostBuf hpar, hout;
   DevBuf wbuf, par2, fcutb, ovb;   // strain-tangent and overlap outputs
+  DevBuf sfreq, samp, sph, srange;   // gwf_strain: caller frequencies, amplitude and phase staging, row ranges
   DevBuf core;                     // source-dependent model records, shared by the detectors of a call
   int groups = 1;                  // FP32 network totals: detectors sharing the grid in one launch
   DevBuf xit;                      // IMRPhenomNSBH xi_tide table, built on first use
@@ -820,6 +821,21 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
 // WFOverlap grid: upper frequency max(fcut_1, fcut_2) per event; with a detector fmax, gwfast
 // takes fmax where that maximum exceeds it and the first waveform's cut elsewhere
 // (gwfast/signal.py:1861-1867, reproduced as written)
+// lowest and highest of each event's frequencies (row n of f, or the one row shared by every event
+// when f_ld = 0): the models' reference frequency and the upper end that IMRPhenomNSBH reads
+__global__ void row_range_kernel(const double* f, long long f_ld, int R, long long N, double* lo, double* hi) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const double* r = f + (f_ld > 0 ? n * f_ld : 0);
+  double a = r[0], b = r[0];
+  for (int k = 1; k < R; ++k) {
+    a = fmin(a, r[k]);
+    b = fmax(b, r[k]);
+  }
+  lo[n] = a;
+  hi[n] = b;
+}
+
 __global__ void fcut_pair_kernel(const double* p1, long long ld1, gwf::WfDesc w1, const double* p2, long long ld2,
                                  gwf::WfDesc w2, double fmax, long long N, double* out) {
   const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -907,6 +923,7 @@ int gwf_ctx_destroy(gwf_ctx* ctx) {
   ctx->tune_out.release();
   ctx->osda.release(); ctx->osdn.release(); ctx->mix_sda.release(); ctx->mix_sdn.release();
   ctx->wbuf.release(); ctx->par2.release(); ctx->fcutb.release(); ctx->ovb.release();
+  ctx->sfreq.release(); ctx->samp.release(); ctx->sph.release(); ctx->srange.release();
   ctx->core.release();
   ctx->xit.release();
   ctx->mix_scr.release(); ctx->mix_soff.release(); ctx->mix_sctr.release(); ctx->mix_spart.release();
@@ -1192,6 +1209,119 @@ int gwf_fisher_ex(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc
                                                       : out_net, stream);
   ctx->call_sd_arm = ctx->call_sd_net = nullptr;
   return rc;
+}
+
+int gwf_strain(gwf_ctx* ctx, int det_id, const gwf_wf_desc* wf, const double* params, int64_t ld, int64_t n_events,
+               const double* freqs, int64_t f_ld, int32_t n_freq, int mem, double* out_strain, double* out_amp,
+               double* out_phase, void* stream) {
+  int rc = check_ctx(ctx);
+  if (rc) return rc;
+  rc = validate_common(ctx, 1, &det_id, wf, params, ld, n_events, 2, nullptr, 0, mem);
+  if (rc) return rc;
+  if (!out_strain && !out_amp && !out_phase) return fail(GWF_ERR_INVALID_ARG, "no output requested");
+  if (!freqs || n_freq < 1) return fail(GWF_ERR_INVALID_ARG, "need at least one frequency");
+  if (f_ld != 0 && f_ld < n_freq) return fail(GWF_ERR_INVALID_ARG, "f_ld must be 0 or >= n_freq");
+  if (out_phase && wf->model == GWF_WF_PHENOMHM)
+    return fail(GWF_ERR_UNSUPPORTED, "GWPhase of IMRPhenomHM: its phase is one per mode");
+  const int64_t N = n_events;
+  if (N == 0) return GWF_OK;
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  const int npar = npar_of(wf->model);
+  const double* dp;
+  int64_t dld;
+  const int* dres;
+  rc = stage_inputs(ctx, params, ld, N, nullptr, mem, st, &dp, &dld, &dres, npar);
+  if (rc) return rc;
+  if (wf->model == GWF_WF_PHENOMNSBH && (rc = ensure_xitide(ctx, st))) return rc;
+  const size_t nf = f_ld ? (size_t)N * (size_t)f_ld : (size_t)n_freq;
+  const double* dfreq = freqs;
+  if (mem == GWF_MEM_HOST) {
+    for (size_t i = 0; i < nf; ++i)
+      if (!(freqs[i] > 0.0) && (f_ld == 0 || (int64_t)(i % (size_t)f_ld) < n_freq))
+        return fail(GWF_ERR_INVALID_ARG, "frequencies must be positive");
+    if (ctx->sfreq.ensure(nf * sizeof(double))) return fail(GWF_ERR_OOM, "device allocation failed (frequencies)");
+    GWF_CK(cudaMemcpyAsync(ctx->sfreq.p, freqs, nf * sizeof(double), cudaMemcpyHostToDevice, st));
+    dfreq = (const double*)ctx->sfreq.p;
+  }
+  // per event: the lowest frequency sets the models' reference (as gwfast takes fRef = min of the
+  // grid it is given), the highest stands for the grid end
+  if (ctx->srange.ensure((size_t)2 * N * sizeof(double))) return fail(GWF_ERR_OOM, "device allocation failed (ranges)");
+  double* flo = (double*)ctx->srange.p;
+  row_range_kernel<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(dfreq, f_ld, n_freq, N, flo, flo + N);
+  GWF_CK(cudaGetLastError());
+  const DetRec& r = ctx->dets[det_id];
+  const int NA = r.desc.shape == GWF_SHAPE_T ? 3 : 1;
+  const size_t row_c = (size_t)n_freq * 2 * sizeof(double);   // one event's row of complex values
+  const size_t row_d = (size_t)n_freq * sizeof(double);
+  const size_t per_ev = (out_strain ? NA * row_c : 0) + (out_amp ? NA * row_c : 0) + (out_phase ? 2 * row_d : 0);
+  const int64_t chunk = mem == GWF_MEM_DEVICE ? (N < gwf::kChunk ? N : gwf::kChunk) : wave_chunk(per_ev);
+  const int64_t cap = chunk < N ? chunk : N;
+  if (ctx->setup.ensure((size_t)cap * stride_of(wf->model))) return fail(GWF_ERR_OOM, "device allocation failed (set-up scratch)");
+  if (mem == GWF_MEM_HOST && ((out_strain && ctx->wbuf.ensure((size_t)cap * NA * row_c)) ||
+                              (out_amp && ctx->samp.ensure((size_t)cap * NA * row_c)) ||
+                              (out_phase && ctx->sph.ensure((size_t)cap * 2 * row_d))))
+    return fail(GWF_ERR_OOM, "device allocation failed (strain)");
+  GWF_CK(cudaStreamWaitEvent(st, ctx->scratch_free, 0));
+  gwf::LaunchArgs a;
+  a.ev.p = dp;
+  a.ev.ld = dld;
+  a.ev.N = N;
+  a.ev.n0 = 0;
+  a.ev.res = 2;   // (the set-up needs a grid; the points are the caller's)
+  a.ev.res_ev = nullptr;
+  a.ev.spacing = 0;
+  a.ev.fmin_ev = flo;
+  a.ev.fcut_ev = flo + N;
+  a.det = dev_of(r);
+  a.wf = wf_dev(wf);
+  if (wf->model == GWF_WF_PHENOMNSBH) a.wf.xitide = (const double*)ctx->xit.p;
+  a.qnm = ctx->d_qnm;
+  a.nq = ctx->nq;
+  a.out_arm = a.out_det = nullptr;
+  a.accum = 0;
+  a.per_arm = 0;
+  a.precision = GWF_PREC_FP64;
+  a.scratch = (unsigned char*)ctx->setup.p;
+  a.cap_events = cap;
+  a.stream = st;
+  if (mem == GWF_MEM_HOST) {
+    if (out_strain) prefault_host(out_strain, (size_t)NA * N * row_c);
+    if (out_amp) prefault_host(out_amp, (size_t)NA * N * row_c);
+    if (out_phase) prefault_host(out_phase, (size_t)2 * N * row_d);
+  }
+  for (int64_t n0 = 0; n0 < N; n0 += chunk) {
+    const int64_t cnt = (N - n0) < chunk ? (N - n0) : chunk;
+    gwf::WaveOut o{};
+    o.mode = gwf::WAVE_STRAIN;
+    o.dphi = wave_dphi(wf);
+    o.n0 = n0;
+    o.cnt = cnt;
+    o.R_out = n_freq;
+    o.f_ld = f_ld;
+    const bool dev = mem == GWF_MEM_DEVICE;
+    o.out_n = dev ? N : cnt;
+    o.out_base = dev ? 0 : n0;
+    o.f_in = dev || f_ld == 0 ? dfreq : dfreq + (size_t)n0 * f_ld;
+    o.out = out_strain ? reinterpret_cast<gwf::cd*>(dev ? (void*)out_strain : ctx->wbuf.p) : nullptr;
+    o.amp = out_amp ? reinterpret_cast<gwf::cd*>(dev ? (void*)out_amp : ctx->samp.p) : nullptr;
+    o.phase = out_phase ? (dev ? out_phase : (double*)ctx->sph.p) : nullptr;
+    cudaError_t e = launch_wave(a, o);
+    if (e != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    if (!dev) {   // rows [n0, n0 + cnt) of each (arm) block
+      if (out_strain)
+        GWF_CK(cudaMemcpy2DAsync(out_strain + (size_t)n0 * n_freq * 2, (size_t)N * row_c, ctx->wbuf.p, (size_t)cnt * row_c,
+                                 (size_t)cnt * row_c, (size_t)NA, cudaMemcpyDeviceToHost, st));
+      if (out_amp)
+        GWF_CK(cudaMemcpy2DAsync(out_amp + (size_t)n0 * n_freq * 2, (size_t)N * row_c, ctx->samp.p, (size_t)cnt * row_c,
+                                 (size_t)cnt * row_c, (size_t)NA, cudaMemcpyDeviceToHost, st));
+      if (out_phase)
+        GWF_CK(cudaMemcpy2DAsync(out_phase + (size_t)n0 * n_freq, (size_t)N * row_d, ctx->sph.p, (size_t)cnt * row_d,
+                                 (size_t)cnt * row_d, 2, cudaMemcpyDeviceToHost, st));
+    }
+  }
+  GWF_CK(cudaEventRecord(ctx->scratch_free, st));
+  if (mem == GWF_MEM_HOST) GWF_CK(cudaStreamSynchronize(st));
+  return GWF_OK;
 }
 
 int gwf_strain_derivs(gwf_ctx* ctx, int det_id, const gwf_wf_desc* wf, const double* params, int64_t ld,

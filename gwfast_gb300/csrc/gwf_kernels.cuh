@@ -84,6 +84,8 @@ struct EvBatch {
   const int* res_ev;     // optional per-event grid length
   int spacing;           // 0 = geometric, 1 = linear
   const double* fcut_ev = nullptr;   // optional per-event upper grid frequency (replaces the model cut and fmax)
+  const double* fmin_ev = nullptr;   // optional per-event lower frequency (replaces the detector's fmin in the
+                                     // set-up: the models' reference frequency is the lowest of the event's points)
 };
 
 struct WfDesc {
@@ -598,12 +600,14 @@ __device__ __forceinline__ const PhaseBasis* rec_basis(const unsigned char* scra
 // it and recomputes only the detector-dependent part (the per-event set-up is FP64-bound, and a
 // network evaluates it once per detector)
 template <int MODEL>
-__global__ void __launch_bounds__(kEvBlock) setup_kernel(EvBatch ev, DetDev det, WfDesc wf, const double* qnm, int nq,
+__global__ void __launch_bounds__(kEvBlock) setup_kernel(EvBatch ev, DetDev det_in, WfDesc wf, const double* qnm, int nq,
                                                           unsigned char* scratch, long long count, unsigned char* core,
                                                           int core_mode, const long long* core_idx, int epw) {
   const long long i = ev_thread(epw);
   const long long n = ev.n0 + i;
   if (i < 0 || i >= count || n >= ev.N) return;
+  DetDev det = det_in;
+  if (ev.fmin_ev) det.fmin = ev.fmin_ev[n];
   unsigned char* rec = scratch + i * rec_stride<MODEL>();
   SetupHdr& h = *reinterpret_cast<SetupHdr*>(rec);
   EvUnion& E = *reinterpret_cast<EvUnion*>(rec + sizeof(SetupHdr));

@@ -8,7 +8,7 @@
 
 namespace gwf {
 
-enum { WAVE_DERIVS = 0, WAVE_STORE = 1, WAVE_OVERLAP = 2 };
+enum { WAVE_DERIVS = 0, WAVE_STORE = 1, WAVE_OVERLAP = 2, WAVE_STRAIN = 3 };
 
 // One launch of wave_out_kernel over events [n0, n0 + cnt) of the batch.
 //  WAVE_DERIVS:  out[((arm * P + p) * out_n + n - out_base) * R_out + k] = d h_arm / d theta_p at
@@ -20,6 +20,14 @@ enum { WAVE_DERIVS = 0, WAVE_STORE = 1, WAVE_OVERLAP = 2 };
 //  WAVE_OVERLAP: reads the WAVE_STORE output of the first waveform at the same place and writes,
 //                summed over the arms (triangle: 3), ov[n] = sum Re(u1 conj u2), n1[n] = sum |u1|^2,
 //                n2[n] = sum |u2|^2: the trapezoid integrals 4 int Re(h1 conj h2) / S df etc.
+//  WAVE_STRAIN:  at the caller's frequencies f_in[(n - out_base) * f_ld + k] (f_ld = 0: one row
+//                for every event) instead of the event grid (gwfast/signal.py:425-655):
+//                out[(arm * out_n + n - out_base) * R_out + k] = h_arm (GWstrain), amp[same index]
+//                = (A+, Ax) (GWAmplitudes), phase[(j * out_n + n - out_base) * R_out + k] with
+//                j = 0: GWPhase = 2 pi f tcoal - Phicoal - Phi(f), j = 1: the strain's phase Psi =
+//                GWPhase + 2 pi f Delta t_loc (the detector's delay, for the first arm's site; the
+//                22-mode models). Each output may be null; triangle: 3 arms, the third minus the
+//                sum of the first two.
 struct WaveOut {
   int mode;
   double dphi;   // added to the phase constant (TaylorF2 with phiref_vlso: -pi)
@@ -30,6 +38,10 @@ struct WaveOut {
   double* ov;
   double* n1;
   double* n2;
+  const double* f_in = nullptr;
+  long long f_ld = 0;
+  cd* amp = nullptr;
+  double* phase = nullptr;
 };
 
 // e^{i Psi} with Psi = 2 pi f (tc [days] + D [s]) - phi: the large tc term (up to ~1e9 rad) is
@@ -71,6 +83,53 @@ __global__ void __launch_bounds__(kThreads) wave_out_kernel(EvBatch ev, DetDev d
   const long long row = n - o.out_base;
   double s[3] = {0.0, 0.0, 0.0};
   for (int k = tid; k < o.R_out; k += kThreads) {
+    if (o.mode == WAVE_STRAIN) {
+      cd hs[NA], am[NA];
+      double gph = 0.0, psi = 0.0;
+      if (g.ok) {
+        const double f = o.f_in[(o.f_ld > 0 ? row * o.f_ld : 0) + k];
+        cd P, C;
+        double phi0, tau = 0.0;
+        wave_point_full<MODEL, EARTH>(E, pj, f, log(f), P, C, phi0, tau);
+        TimeState ts;
+        if (EARTH) time_state(pj, pj.tc - tau / kDay, ts);
+        else ts = tsc;
+        const double ph_c = phic + phi0 + o.dphi;
+        const cd ph = common_phase(f, pj.tc, ts.D, ph_c);
+        gph = kTwoPi * f * (pj.tc * kDay) - ph_c;
+        psi = gph + kTwoPi * f * ts.D;
+        // amplitudes: A (1 + cos^2 i) / 2 F+ and A cos i Fx for the 22-mode models (P, C real),
+        // |h+| F+ and |hx| Fx for IMRPhenomHM (gwfast/signal.py:457-463)
+        const double ap = MODEL == 2 ? sqrt(P.re * P.re + P.im * P.im) : P.re;
+        const double ac = MODEL == 2 ? sqrt(C.re * C.re + C.im * C.im) : C.re;
+#pragma unroll
+        for (int a = 0; a < NARM; ++a) {
+          ArmPat apt;
+          if (EARTH) arm_pattern(pj, det.sin_zeta, ts.x, a, apt);
+          else apt = apc[a];
+          hs[a] = cmul(cadd(cscale(P, apt.Fp), cscale(cmuli(C), apt.Fc)), ph);
+          am[a] = {ap * apt.Fp, ac * apt.Fc};
+        }
+        if (NA == 3) {
+          hs[NA - 1] = cscale(cadd(hs[0], hs[NARM - 1]), -1.0);
+          am[NA - 1] = cscale(cadd(am[0], am[NARM - 1]), -1.0);
+        }
+      } else {
+#pragma unroll
+        for (int a = 0; a < NA; ++a) hs[a] = am[a] = {0.0, 0.0};
+      }
+#pragma unroll
+      for (int a = 0; a < NA; ++a) {
+        const long long ix = ((long long)a * o.out_n + row) * o.R_out + k;
+        if (o.out) o.out[ix] = hs[a];
+        if (o.amp) o.amp[ix] = am[a];
+      }
+      if (o.phase) {
+        o.phase[row * o.R_out + k] = gph;
+        o.phase[(o.out_n + row) * o.R_out + k] = psi;
+      }
+      continue;
+    }
     if (k >= R) {   // no valid grid for this event: zeros
       if (o.mode == WAVE_DERIVS)
         for (int a = 0; a < NA; ++a)

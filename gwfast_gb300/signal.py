@@ -304,6 +304,110 @@ class GWSignal:
             return ov[0], np.sqrt(n1[0]), np.sqrt(n2[0])
         return ov[0] / np.sqrt(n1[0] * n2[0])
 
+    # ---- strain, amplitudes and phase at caller frequencies (gwfast/signal.py:425-655)
+    def _strain_parts(self, evParams, f, rot, strain=False, amp=False, phase=False):
+        """One library call: the requested parts for the detector's arm at rotation rot (degrees; 0 for
+        an L, 0/60/120 for the arms of a triangle), reshaped to the shape of f. f: a scalar or (R,)
+        for every event, or (R, N), one column per event (as gwfast's grids)."""
+        wf = self.wf_model
+        p = _prep(dict(evParams), wf)
+        N = p.shape[1]
+        fa = np.asarray(f, dtype=np.float64)
+        if fa.ndim > 2:
+            raise ValueError('f must be a scalar, (R,) or (R, N)')
+        if fa.ndim == 2:
+            if fa.shape[1] != N:
+                raise ValueError('f of shape (R, N) needs one column per event (N = %d)' % N)
+            freqs = np.ascontiguousarray(fa.T)
+        else:
+            freqs = np.ascontiguousarray(np.atleast_1d(fa))
+        if np.any(~(freqs > 0.)):
+            raise ValueError('frequencies must be positive')
+        rots = (0.,) if self.detector_shape == 'L' else (0., 60., 120.)
+        arm = [i for i, r in enumerate(rots) if abs(float(rot) - r) < 1e-9]
+        if not arm:
+            raise NotImplementedError('rot must be one of %s for this detector' % (rots,))
+        arms, R = len(rots), freqs.shape[-1]
+        hs = np.empty((arms, N, R), dtype=np.complex128) if strain else None
+        am = np.empty((arms, N, R), dtype=np.complex128) if amp else None
+        ph = np.empty((2, N, R)) if phase else None
+        _lib.context(self.device).strain(self.det_id, wf.gpu_desc(), p, freqs, out_strain=hs, out_amp=am, out_phase=ph)
+
+        def shaped(x):   # (N, R) -> the shape of f
+            if fa.ndim == 2:
+                return np.ascontiguousarray(x.T)
+            if fa.ndim == 0:
+                return x[0, 0] if N == 1 else x[:, 0]
+            return x[0] if N == 1 else np.ascontiguousarray(x.T)
+        out = {}
+        if strain:
+            out['h'] = shaped(hs[arm[0]])
+        if amp:
+            out['Ap'], out['Ac'] = shaped(am[arm[0]].real), shaped(am[arm[0]].imag)
+        if phase:
+            out['GWPhase'], out['Psi'] = shaped(ph[0]), shaped(ph[1])
+        return out
+
+    def GWAmplitudes(self, evParams, f, rot=0.):
+        """Plus and cross amplitudes at the detector (gwfast/signal.py:425-466): A F+ (1 + cos^2 i)/2 and
+        A Fx cos i (IMRPhenomHM: |h+| F+, |hx| Fx), pattern functions at the Earth-rotation time of each
+        frequency."""
+        o = self._strain_parts(evParams, f, rot, amp=True)
+        return o['Ap'], o['Ac']
+
+    def GWPhase(self, evParams, f):
+        """2 pi f tcoal - Phicoal - Phi(f) (gwfast/signal.py:468-483), tcoal in days; the 22-mode models
+        (IMRPhenomHM has one phase per mode)."""
+        if self.wf_model.is_HigherModes:
+            raise NotImplementedError('GWPhase of a higher-mode model: its phase is one per mode')
+        return self._strain_parts(evParams, f, 0., phase=True)['GWPhase']
+
+    def GWstrain(self, f, Mc, eta, dL, theta, phi, iota, psi, tcoal, Phicoal, chiS, chiA, chi1x=0., chi2x=0., chi1y=0.,
+                 chi2y=0., LambdaTilde=0., deltaLambda=0., ecc=0., rot=0., is_m1m2=False, is_chi1chi2=False,
+                 is_prec_ang=False, is_Lam1Lam2=False, return_single_comp=None):
+        """The complex strain at the detector, (A+ + i Ax) e^{i Psi} (gwfast/signal.py:485-655), or one
+        component with return_single_comp ('Ap', 'Ac', 'Psip', 'Psic', 'At', 'Psit'). Aligned spins:
+        chiS, chiA (or chi1z, chi2z with is_chi1chi2); the in-plane components must be zero."""
+        if is_prec_ang or self.wf_model.is_Precessing:
+            raise NotImplementedError('precessing waveforms are not implemented on the GPU path')
+        if np.any(np.asarray(chi1x) != 0.) or np.any(np.asarray(chi2x) != 0.) or np.any(np.asarray(chi1y) != 0.) \
+                or np.any(np.asarray(chi2y) != 0.):
+            raise NotImplementedError('in-plane spins need a precessing waveform')
+        if is_m1m2:
+            Mc, eta = utils.Mceta_from_m1m2(Mc, eta)
+        chi1z, chi2z = (chiS, chiA) if is_chi1chi2 else (chiS + chiA, chiS - chiA)
+        ev = {'Mc': Mc, 'eta': eta, 'dL': dL, 'theta': theta, 'phi': phi, 'iota': iota, 'psi': psi, 'tcoal': tcoal,
+              'Phicoal': Phicoal, 'chi1z': chi1z, 'chi2z': chi2z}
+        if self.wf_model.is_tidal:
+            if is_Lam1Lam2:
+                ev['Lambda1'], ev['Lambda2'] = LambdaTilde, deltaLambda
+            else:
+                ev['LambdaTilde'], ev['deltaLambda'] = LambdaTilde, deltaLambda
+        if self.wf_model.is_eccentric:
+            ev['ecc'] = ecc
+        hm = self.wf_model.is_HigherModes
+        if return_single_comp is None:
+            return self._strain_parts(ev, f, rot, strain=True)['h']
+        if return_single_comp not in ('Ap', 'Ac', 'Psip', 'Psic', 'At', 'Psit'):
+            raise ValueError('Single component to return has to be among Ap, Ac, Psip, Psic')
+        if hm:
+            if return_single_comp.startswith('Psi'):
+                raise NotImplementedError('the phases of a higher-mode strain are not returned separately')
+            if return_single_comp == 'At':
+                return np.abs(self._strain_parts(ev, f, rot, strain=True)['h'])
+            o = self._strain_parts(ev, f, rot, amp=True)
+            return np.abs(o[return_single_comp])
+        o = self._strain_parts(ev, f, rot, amp=True, phase=True)
+        if return_single_comp in ('Ap', 'Ac'):
+            return o[return_single_comp]
+        if return_single_comp == 'Psip':
+            return o['Psi']
+        if return_single_comp == 'Psic':
+            return o['Psi'] + np.pi * 0.5
+        if return_single_comp == 'At':
+            return np.abs(o['Ap'] + 1j * o['Ac'])
+        return o['Psi'] + np.arctan2(o['Ac'], o['Ap'])
+
     def _resolve_res(self, evParams, res, df):
         if res is None and df is not None:
             utils.check_evparams(evParams)

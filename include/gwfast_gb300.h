@@ -165,6 +165,22 @@ int gwf_fisher_ex(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc
 int gwf_strain_derivs(gwf_ctx* ctx, int det_id, const gwf_wf_desc* wf, const double* params, int64_t ld,
                       int64_t n_events, int32_t res, int spacing, int mem, double* out, void* stream);
 
+/* The strain on caller-given frequencies, one detector: GWSignal.GWstrain, GWAmplitudes and GWPhase
+ * (gwfast/signal.py:425-655). freqs (Hz, > 0, any order; mem as the other arrays): one row of n_freq
+ * frequencies for every event (f_ld = 0) or a row per event ([N][f_ld], f_ld >= n_freq). Beyond the
+ * model's cut the IMR amplitudes are zero, as in gwfast. Outputs, each may be NULL (not all):
+ *   out_strain [arms][N][n_freq] complex as interleaved (re, im) doubles: h = (A+ + i Ax) e^{i Psi};
+ *   out_amp    [arms][N][n_freq] (A+, Ax) pairs: A (1 + cos^2 iota) / 2 F+ and A cos iota Fx for the
+ *              22-mode models, |h+| F+ and |hx| Fx for IMRPhenomHM (gwfast/signal.py:457-463);
+ *   out_phase  [2][N][n_freq]: [0] GWPhase = 2 pi f tcoal - Phicoal - Phi(f) (tcoal in days of 86400 s),
+ *              [1] Psi = GWPhase + 2 pi f Delta t_loc, the strain's phase at the detector (the
+ *              22-mode models; IMRPhenomHM's phase is one per mode: GWF_ERR_UNSUPPORTED).
+ * arms = 1 (L) or 3 (triangle: the arms of rot = 0, 60, 120 degrees in gwfast, the third minus the
+ * sum of the first two). Parameters as in gwf_fisher (Fisher order). FP64. */
+int gwf_strain(gwf_ctx* ctx, int det_id, const gwf_wf_desc* wf, const double* params, int64_t ld, int64_t n_events,
+               const double* freqs, int64_t f_ld, int32_t n_freq, int mem, double* out_strain, double* out_amp,
+               double* out_phase, void* stream);
+
 /* Overlap integrals of two waveforms on two parameter sets (GWSignal.WFOverlap with
  * return_separate=True, gwfast/signal.py:1759-1921; DetNet.WFOverlap, gwfast/network.py:198-227).
  * Per detector i and event n, on the geometric grid from fmin to max(fcut_1, fcut_2) (with a

@@ -522,6 +522,42 @@ def make_derivs(res=200):
     print('wrote derivs_tf2')
 
 
+def make_strain_caller(R=64):
+    """GWstrain, GWAmplitudes and GWPhase at caller-given frequencies: per event an unsorted set,
+    log-uniform from 3 Hz to 1.3 times the model's cut (so the models' reference frequency, the
+    lowest of the given points, is not a detector's fmin, and the IMR models' cut is crossed)."""
+    out = {}
+    cases = (('phd', WF.IMRPhenomD(), {'L1': (10., True), 'ETS': (5., True)}, events_bbh(np.random.default_rng(1010), 3)),
+             ('tf2', WF.TaylorF2_RestrictedPN(), {'Virgo': (10., False)}, events_bns(np.random.default_rng(1011), 3)),
+             ('phm', WF.IMRPhenomHM(), {'ETS': (5., True)},
+              events_bbh(np.random.default_rng(1012), 3, mmax=150., qmin=0.1, chimax=0.9)))
+    for tag, wf, dets, ev in cases:
+        ev = {k: np.array(v) for k, v in ev.items()}
+        rng = np.random.default_rng(len(tag) * 7 + 3)
+        fc = wf.fcut(**ev)
+        f = np.exp(np.log(3.) + rng.uniform(0., 1., (R, len(fc))) * (np.log(1.3 * fc) - np.log(3.)))
+        out[tag + '_f'] = f
+        for k in KEYS:
+            out['%s_ev_%s' % (tag, k)] = ev[k]
+        for dname, (fwall, earth) in dets.items():
+            d = glob.detectors[dname]
+            s = SIG.GWSignal(wf, psd_path=psd_file(fwall), detector_shape=d['shape'], det_lat=d['lat'],
+                             det_long=d['long'], det_xax=d['xax'], verbose=False, is_ASD=False, useEarthMotion=earth,
+                             fmin=fwall)
+            z = np.zeros_like(ev['Mc'])
+            args = [f] + [ev[k] for k in ('Mc', 'eta', 'dL', 'theta', 'phi', 'iota', 'psi', 'tcoal', 'Phicoal',
+                                           'chi1z', 'chi2z')]
+            for r in ((0.,) if d['shape'] == 'L' else (0., 60., 120.)):
+                t = '%s_%s_r%d' % (tag, dname, int(r))
+                out[t + '_strain'] = s.GWstrain(*args, z, z, z, z, z, z, z, rot=r, is_chi1chi2=True)
+                ap, ac = s.GWAmplitudes(dict(ev), f, rot=r)
+                out[t + '_Ap'], out[t + '_Ac'] = np.asarray(ap), np.asarray(ac)
+            if not wf.is_HigherModes:
+                out[tag + '_GWPhase'] = np.asarray(s.GWPhase(dict(ev), f))
+    np.savez_compressed(os.path.join(OUT, 'strain_caller.npz'), **out)
+    print('wrote strain_caller', len(out), 'arrays')
+
+
 def main():
     only = sys.argv[2:]
     if only:   # regenerate only the named parts: make_<part>()
@@ -603,6 +639,7 @@ def main():
     make_overlap()
     make_snr_derivs()
     make_derivs()
+    make_strain_caller()
     # KAT from the reference tutorial: GW170817-like TF2 Schwarzschild cut frequency 1590.1 Hz
     z = 0.00980
     ev = {'Mc': np.array([1.1859 * (1. + z)]), 'eta': np.array([0.24786618323504223])}

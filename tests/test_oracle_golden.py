@@ -317,3 +317,31 @@ def test_covariance_against_reference(tag):
     cr = np.moveaxis(g[tag + '_cov'], -1, 0)
     e2 = (np.abs(cov - cr) / (sr[:, :, None] * sr[:, None, :])).max(axis=(1, 2))
     assert np.all(e2 < np.maximum(1e-9, 1e-14 * cond)), (e2, cond)
+
+
+@pytest.mark.parametrize('tag,model,dets', [
+    ('phd', 'PhenomD', {'L1': (10., True), 'ETS': (5., True)}),
+    ('tf2', 'TF2', {'Virgo': (10., False)}),
+    ('phm', 'PhenomHM', {'ETS': (5., True)})])
+def test_strain_at_caller_frequencies(tag, model, dets):
+    """GWstrain, GWAmplitudes and GWPhase of gwfast at unsorted caller frequencies up to 1.3 times the
+    model's cut (tests/golden/make_golden.py, make_strain_caller) against the oracle: the models'
+    reference frequency is the lowest of each event's points. Strain to 1e-7 of its largest modulus (the
+    2 pi f tcoal term reaches ~1e9 rad, rounded differently in the two), amplitudes to 1e-10, GWPhase
+    within 1e-6 rad."""
+    g = np.load(os.path.join(GOLD, 'strain_caller.npz'))
+    ev = {k: g['%s_ev_%s' % (tag, k)] for k in O.PARAMS}
+    p = O.to_params(ev)
+    om = O.Model(model)
+    f = torch.as_tensor(np.ascontiguousarray(g[tag + '_f'].T), dtype=O.DT)   # (N, R)
+    for dn, (fw, earth) in dets.items():
+        det = det_of(dn, fw, earth)
+        for rot in ((0.,) if det.shape == 'L' else (0., 60., 120.)):
+            t = '%s_%s_r%d' % (tag, dn, int(rot))
+            h = O.strain(det, om, f, p, rot).numpy().T
+            assert rel(h, g[t + '_strain']) < 1e-7, t
+            ap, ac = (x.detach().numpy().T for x in O.amplitudes(det, om, f, p, rot))
+            assert rel(ap, g[t + '_Ap']) < 1e-10 and rel(ac, g[t + '_Ac']) < 1e-10, t
+    if tag + '_GWPhase' in g:
+        ph = (2. * np.pi * f * (p['tcoal'] * O.DAY_S) - p['Phicoal'] - om.phase(f, p)).detach().numpy().T
+        assert np.max(np.abs(ph - g[tag + '_GWPhase'])) < 1e-6
