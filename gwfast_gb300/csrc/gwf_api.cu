@@ -456,9 +456,28 @@ int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const
   int rc = ensure_aux(ctx, n_det);
   if (rc) return rc;
   GWF_CK(cudaMemsetAsync(ctx->mix_sovf.p, 0, (size_t)n_det * sizeof(int), st));
+  // network totals only: the L-shaped detectors that share the grid run as one FP64 group launch (the
+  // waveform once per point), on the first member's stream, its network total in that member's slice
+  std::vector<std::vector<int>> rg;
+  const bool rgroup = ctx->groups && !carm && !csda && !csdn && a.wf.model <= GWF_WF_PHENOMHM;
+  for (int i = 0; i < n_det; ++i) {
+    const gwf_det_desc& di = ctx->dets[det_ids[i]].desc;
+    bool placed = false;
+    for (auto& g : rg) {
+      const gwf_det_desc& d0 = ctx->dets[det_ids[g[0]]].desc;
+      if (rgroup && (int)g.size() < gwf::kMaxGroup && d0.shape == GWF_SHAPE_L && di.shape == GWF_SHAPE_L &&
+          d0.fmin == di.fmin && d0.fmax == di.fmax && d0.earth_rotation == di.earth_rotation) {
+        g.push_back(i);
+        placed = true;
+        break;
+      }
+    }
+    if (!placed) rg.push_back({i});
+  }
   GWF_CK(cudaEventRecord(ctx->fork, st));
   int slot = 0;
-  for (int i = 0; i < n_det; ++i) {
+  for (auto& grp : rg) {
+    const int i = grp[0];
     const DetRec& r = ctx->dets[det_ids[i]];
     gwf::LaunchArgs ai = a;
     ai.stream = ctx->aux[i];
@@ -482,12 +501,29 @@ int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const
     ai.out_sd_arm = csda ? csda + (size_t)slot * M * gwf::NP : nullptr;
     ai.out_sd_det = csdn ? csdn + (size_t)i * M * gwf::NP : nullptr;
     ai.accum = 0;
-    e = launch_fisher_any(ai.wf.model, ai);
+    if (grp.size() > 1) {
+      gwf::Group64 G;
+      G.nd = (int)grp.size();
+      for (int d = 0; d < G.nd; ++d) {
+        const int m = grp[d];
+        G.det[d] = dev_of(ctx->dets[det_ids[m]]);
+        G.same_psd[d] = d > 0 && ctx->dets[det_ids[m]].psd_class == ctx->dets[det_ids[grp[d - 1]]].psd_class;
+        G.scratch[d] = (unsigned char*)ctx->mix_scr.p + (size_t)m * chunk * stride;
+        G.rec_src[d] = recs[m];
+        G.patch[d] = patch[m];
+        if (recs[m]) ai.core_idx = idx;
+        if (d > 0) GWF_CK(cudaMemsetAsync(cnet + (size_t)m * M * per, 0, (size_t)M * per * sizeof(double), ai.stream));
+      }
+      e = ai.wf.model == 0 ? gwf::launch_group64_m0(ai, G)
+                           : (ai.wf.model == 1 ? gwf::launch_group64_m1(ai, G) : gwf::launch_group64_m2(ai, G));
+    } else {
+      e = launch_fisher_any(ai.wf.model, ai);
+    }
     if (e != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
     GWF_CK(cudaEventRecord(ctx->aux_done[i], ai.stream));
-    slot += r.desc.shape == GWF_SHAPE_T ? 3 : 1;
+    for (int m : grp) slot += ctx->dets[det_ids[m]].desc.shape == GWF_SHAPE_T ? 3 : 1;
   }
-  for (int i = 0; i < n_det; ++i) GWF_CK(cudaStreamWaitEvent(st, ctx->aux_done[i], 0));
+  for (auto& grp : rg) GWF_CK(cudaStreamWaitEvent(st, ctx->aux_done[grp[0]], 0));
   e = gwf::launch_sum_scatter(cnet, n_det, (long long)M * per, idx, (long long)M, (int)per, dnet, st);
   for (int s = 0; carm && s < slots && e == cudaSuccess; ++s)
     e = gwf::launch_scatter(carm + (size_t)s * M * per, idx, (long long)M, (int)per, darm + (size_t)s * N * per, st);
@@ -652,15 +688,18 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   // FP32 network totals: detectors with the same grid (fmin, fmax, Earth rotation) form groups
   // that one launch evaluates together (the waveform once per point for the whole group)
   std::vector<std::vector<int>> groups;
-  const bool grouping = fisher && ctx->groups && precision != GWF_PREC_FP64 && !darm && !dsda && !dsdn &&
-                        ctx->seg_points == 0;
+  // (FP64: the 11-parameter models, L-shaped detectors only)
+  const bool fp64_groups = precision == GWF_PREC_FP64;
+  const bool grouping = fisher && ctx->groups && !darm && !dsda && !dsdn && ctx->seg_points == 0 &&
+                        (!fp64_groups || wf->model <= GWF_WF_PHENOMHM);
   for (int i = 0; i < n_det; ++i) {
     const gwf_det_desc& di = ctx->dets[det_ids[i]].desc;
     bool placed = false;
     for (auto& g : groups) {
       const gwf_det_desc& d0 = ctx->dets[det_ids[g[0]]].desc;
       if (grouping && (int)g.size() < gwf::kMaxGroup && d0.fmin == di.fmin && d0.fmax == di.fmax &&
-          d0.earth_rotation == di.earth_rotation) {
+          d0.earth_rotation == di.earth_rotation &&
+          (!fp64_groups || (d0.shape == GWF_SHAPE_L && di.shape == GWF_SHAPE_L))) {
         g.push_back(i);
         placed = true;
         break;
@@ -750,6 +789,23 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
     first = false;
     ++gi;
     cudaError_t err;
+    if (grp.size() > 1 && fp64_groups) {   // FP64 network total of L-shaped detectors
+      gwf::Group64 G;
+      G.nd = (int)grp.size();
+      for (int d = 0; d < G.nd; ++d) {
+        G.det[d] = dev_of(ctx->dets[det_ids[grp[d]]]);
+        G.same_psd[d] = d > 0 && ctx->dets[det_ids[grp[d]]].psd_class == ctx->dets[det_ids[grp[d - 1]]].psd_class;
+        G.scratch[d] = a.scratch + (size_t)d * chunk * stride;
+      }
+      a.det = G.det[0];
+      a.out_arm = nullptr;
+      a.out_sd_arm = nullptr;
+      a.out_sd_det = nullptr;
+      err = wf->model == 0 ? gwf::launch_group64_m0(a, G) : (wf->model == 1 ? gwf::launch_group64_m1(a, G) : gwf::launch_group64_m2(a, G));
+      if (err != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(err));
+      if (side && gi > 1) GWF_CK(cudaEventRecord(ctx->aux_done[gi - 1], a.stream));
+      continue;
+    }
     if (grp.size() > 1) {   // (grouping implies: FP32 Fisher, network total only)
       gwf::GroupDev g;
       g.nd = (int)grp.size();

@@ -1221,7 +1221,10 @@ __device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32S
       else wave22_f32<MODEL, EARTH>(r.ef, r.pbf, r.tf, f, lnf, wc);
     }
     float sd = 0.0f, cd = 1.0f;   // the Earth-rotation angle is the same for every detector
-    if (EARTH && valid) rot_sc_tau(MODEL == 2 ? wv.tau : wc.tau, sd, cd);
+    if (EARTH && valid) {
+      if constexpr (MODEL == 2) rot_sc_tau(wv.tau, sd, cd);
+      else rot_sc_tau(wc.tau, sd, cd);
+    }
     for (int d = 0; d < nd; ++d) {
       const DetDev& det = g.det[d];
       if (!(d > 0 && g.same_psd[d]))   // (a detector sharing the previous one's table reuses its weight)
@@ -1301,6 +1304,165 @@ __global__ void __launch_bounds__(kThreads, group_min_blocks<MODEL>()) fisher_gr
   f32_item_group<MODEL, EARTH, TRI>(ev, g, S, gp, reinterpret_cast<int2*>(stage_raw), S.r.gf.R);
   write_gram<1>(S.gsum, S.r.scale, ColMix{2.0 * S.r.psi_sgn, S.r.chi_alpha}, n, ev.N, nullptr, out_det, nullptr, nullptr,
                 accum);
+}
+
+// ------------------------------------------------------------------ detector groups, FP64
+// The FP64 network total of L-shaped detectors that share the grid (same fmin, fmax, Earth-rotation
+// flag), as the FP32 group kernel: per point the waveform and its tangent once (the FP64 dual
+// evaluation, about two thirds of one detector's work), then each detector's Earth-rotation time,
+// pattern functions, derivative vectors and PSD weight, all accumulated into one Gram (the Gram of
+// the network is the Gram of all its detectors' vectors). The model record and the grid are detector
+// 0's; every detector's projection header comes from its own set-up record slice. The Gram entries
+// are summed in FP64 as in the per-detector kernel, only in another order across detectors.
+struct GroupDev64 {
+  DetDev det[kMaxGroup];
+  const unsigned char* rec[kMaxGroup];   // each detector's set-up records
+  int same_psd[kMaxGroup];               // detector d has detector d - 1's PSD table: the same weight
+  int nd;
+};
+
+template <int MODEL, bool EARTH>
+struct F64GroupState {
+  F64State<1, 1, np_of<MODEL>()> S;   // detector 0's record (model, grid) and the Gram
+  ProjEv pj[kMaxGroup];
+  ArmPat ap[kMaxGroup];                // without Earth rotation: each detector's pattern functions
+  TimeState ts[kMaxGroup];
+};
+
+template <int MODEL, bool EARTH>
+__device__ inline void f64g_prepare(const GroupDev64& g, long long rec, F64GroupState<MODEL, EARTH>& G) {
+  block_load<MODEL>(G.S.E, G.S.pj, G.S.g, g.rec[0], rec);
+  if ((int)threadIdx.x < g.nd) {
+    const int d = threadIdx.x;
+    G.pj[d] = reinterpret_cast<const SetupHdr*>(g.rec[d] + rec * rec_stride<MODEL>())->pj;
+    if (!EARTH) {
+      time_state(G.pj[d], G.pj[d].tc, G.ts[d]);
+      arm_pattern(G.pj[d], g.det[d].sin_zeta, G.ts[d].x, 0, G.ap[d]);
+    }
+  }
+  if (threadIdx.x == 0) G.S.rec = rec;
+  __syncthreads();
+}
+
+// Gram of points [k0, k1) of the group into G.S.gsum (summed over warps; no strain products)
+template <int MODEL, bool EARTH>
+__device__ inline void f64g_item(const EvBatch& ev, const GroupDev64& g, F64GroupState<MODEL, EARTH>& G, cd* stage,
+                                 int k0, int k1) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int NPM = np_of<MODEL>();
+  constexpr int NEM = ne_of(NPM), NEXM = nex_of(NPM);
+  constexpr int NPS = NPM + 1;
+  constexpr int NI = ndir_of<MODEL>();
+  constexpr int EPT = (NEM + 31) / 32;
+  double acc[EPT];
+  int ea[EPT], eb[EPT];
+  bool own[EPT];
+#pragma unroll
+  for (int i = 0; i < EPT; ++i) {
+    acc[i] = 0.0;
+    const int e = lane + 32 * i;
+    own[i] = e < NEM;
+    ea[i] = eb[i] = 0;
+    if (own[i]) pair_n(NPM, e, ea[i], eb[i]);
+  }
+  cd* my = stage + (size_t)warp * NPS * kSR64;
+  const int nd = g.nd;
+  double sw = 0.0;
+  for (int base = k0; base < k1; base += kThreads) {
+    const int k = base + tid;
+    const bool valid = k < k1;
+    double f = 0.0, lnf = 0.0, w = 0.0;
+    cd P, C, dP[NI], dC[NI], dPi, dCi;
+    DualOf<MODEL> tau(0.0);
+    double phi0, dtn[NI], dphl = 0.0, dphd = 0.0, dphe = 0.0;
+#pragma unroll
+    for (int q = 0; q < NI; ++q) dtn[q] = 0.0;
+    if (valid) {
+      grid_point(G.S.g, ev.spacing, k, f, lnf, w);
+      wave_point_dual<MODEL, EARTH>(G.S.E, G.S.pj, f, lnf, P, C, dP, dC, dPi, dCi, tau, phi0);
+      if (EARTH) {
+#pragma unroll
+        for (int q = 0; q < NI; ++q) dtn[q] = -tau.d[q] / kDay;
+      }
+      analytic_tangents<MODEL>(G.S.E, lnf, dphl, dphd, dphe);
+    }
+    for (int d = 0; d < nd; ++d) {
+      cd D[NPS];
+      if (valid) {
+        if (!(d > 0 && g.same_psd[d])) sw = sqrt(4.0 * w / psd_at(g.det[d], f, lnf));
+        TimeState ts;
+        if (EARTH) time_state(G.pj[d], G.S.pj.tc - tau.v / kDay, ts);
+        else ts = G.ts[d];
+        ArmPat ap;
+        if (EARTH) arm_pattern(G.pj[d], g.det[d].sin_zeta, ts.x, 0, ap);
+        else ap = G.ap[d];
+        arm_derivs<NI>(G.pj[d], ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D);
+        analytic_columns<MODEL>(cadd(cscale(P, ap.Fp), cscale(cmuli(C), ap.Fc)), dphl, dphd, dphe, D);
+      }
+#pragma unroll
+      for (int q = 0; q < NPM; ++q) my[q * kSR64 + lane] = valid ? cscale(D[q], sw) : cd{0.0, 0.0};
+      __syncwarp();
+#pragma unroll
+      for (int i = 0; i < EPT; ++i) {
+        if (own[i]) {
+          const cd* ra = my + ea[i] * kSR64;
+          const cd* rb = my + eb[i] * kSR64;
+          double s2 = 0.0;
+#pragma unroll 8
+          for (int j = 0; j < 32; ++j) s2 += ra[j].re * rb[j].re + ra[j].im * rb[j].im;
+          acc[i] += s2;
+        }
+      }
+      __syncwarp();
+    }
+  }
+  // cross-warp reduction through the staging area
+  __syncthreads();
+  double* red = reinterpret_cast<double*>(stage);   // [kWarps][NEM]
+#pragma unroll
+  for (int i = 0; i < EPT; ++i)
+    if (own[i]) red[warp * NEM + lane + 32 * i] = acc[i];
+  __syncthreads();
+  for (int e = tid; e < NEXM; e += kThreads) {
+    double s2 = 0.0;
+    if (e < NEM) {
+#pragma unroll
+      for (int wp = 0; wp < kWarps; ++wp) s2 += red[wp * NEM + e];
+    }
+    G.S.gsum[e] = s2;
+  }
+  __syncthreads();
+}
+
+template <int MODEL, bool EARTH>
+__global__ void __launch_bounds__(kThreads) fisher_group_kernel64(EvBatch ev, GroupDev64 g, double* out_det, int accum) {
+  extern __shared__ __align__(16) unsigned char stage_raw[];
+  __shared__ F64GroupState<MODEL, EARTH> G;
+  const long long n = ev.n0 + blockIdx.x;
+  if (n >= ev.N) return;
+  f64g_prepare<MODEL, EARTH>(g, blockIdx.x, G);
+  f64g_item<MODEL, EARTH>(ev, g, G, reinterpret_cast<cd*>(stage_raw), 0, G.S.g.ok ? G.S.g.R : 0);
+  write_gram<1, np_of<MODEL>()>(G.S.gsum, 1.0, ColMix{0.0, 0.0}, n, ev.N, nullptr, out_det, nullptr, nullptr, accum);
+}
+
+template <int MODEL, bool EARTH>
+__global__ void __launch_bounds__(kThreads) fisher_group_seg_kernel64(EvBatch ev, GroupDev64 g, long long count,
+                                                                      SegInfo si) {
+  static_assert(np_of<MODEL>() == NP, "segmented launches carry 11-parameter partial Grams");
+  extern __shared__ __align__(16) unsigned char stage_raw[];
+  __shared__ F64GroupState<MODEL, EARTH> G;
+  if (threadIdx.x == 0) G.S.rec = -1;
+  __syncthreads();
+  long long item, rec;
+  int k0;
+  while (next_item(si, count, item, rec, k0)) {
+    if (G.S.rec != rec) f64g_prepare<MODEL, EARTH>(g, rec, G);
+    const int R = G.S.g.ok ? G.S.g.R : 0;
+    const int k1 = k0 + si.seg < R ? k0 + si.seg : R;
+    f64g_item<MODEL, EARTH>(ev, g, G, reinterpret_cast<cd*>(stage_raw), k0, k1);
+    double* o = si.partial + item * NEX;
+    for (int e = threadIdx.x; e < NEX; e += blockDim.x) o[e] = G.S.gsum[e];
+  }
 }
 
 // ------------------------------------------------------------------ FP32 SNR

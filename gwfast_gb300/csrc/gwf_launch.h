@@ -150,6 +150,20 @@ cudaError_t launch_wave_m7(const LaunchArgs& a, const WaveOut& o);
 cudaError_t launch_group_m0(const LaunchArgs& a, const GroupDev& g);
 cudaError_t launch_group_m1(const LaunchArgs& a, const GroupDev& g);
 cudaError_t launch_group_m2(const LaunchArgs& a, const GroupDev& g);
+// FP64 network total of a group of L-shaped detectors sharing the grid (11-parameter models): per
+// detector its set-up record slice (a.cap_events records) and, for a gathered batch (a.core_idx),
+// where its records are copied from; a.seg > 0: segmented launch with a's segment buffers
+struct Group64 {
+  int nd = 0;
+  DetDev det[kMaxGroup];
+  int same_psd[kMaxGroup] = {};
+  unsigned char* scratch[kMaxGroup] = {};
+  const unsigned char* rec_src[kMaxGroup] = {};   // null: the set-up runs (detector 0) or only the header
+  int patch[kMaxGroup] = {};                       // rec_src is another detector's: recompute the header
+};
+cudaError_t launch_group64_m0(const LaunchArgs& a, const Group64& g);
+cudaError_t launch_group64_m1(const LaunchArgs& a, const Group64& g);
+cudaError_t launch_group64_m2(const LaunchArgs& a, const Group64& g);
 size_t setup_stride_m0();
 size_t core_bytes_m0();
 size_t core_bytes_m1();

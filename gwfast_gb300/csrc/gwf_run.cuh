@@ -282,6 +282,79 @@ cudaError_t group_dispatch(const LaunchArgs& a, const GroupDev& g) {
   }
 }
 
+// FP64 network total of a group of L-shaped detectors: per chunk each member's records (detector
+// 0: the set-up, or for a gathered batch a copy of the first pass's records; the others: their
+// projection header only, which is all the group kernel reads of them), then one launch over the
+// group, classic or segmented
+template <bool EARTH>
+cudaError_t group64_one(const LaunchArgs& a, const Group64& G) {
+  if constexpr (np_of<M>() != NP) {
+    return cudaErrorNotSupported;
+  } else {
+    const int smem = kWarps * (np_of<M>() + 1) * kSR64 * (int)sizeof(cd);
+    GroupDev64 g;
+    g.nd = G.nd;
+    for (int d = 0; d < G.nd; ++d) {
+      g.det[d] = G.det[d];
+      g.rec[d] = G.scratch[d];
+      g.same_psd[d] = G.same_psd[d];
+    }
+    auto kc = fisher_group_kernel64<M, EARTH>;
+    auto ks = fisher_group_seg_kernel64<M, EARTH>;
+    cudaError_t err = cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (err == cudaSuccess) err = cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int grid = 0;
+    if (err == cudaSuccess && a.seg > 0) err = persist_grid(ks, smem, &grid);
+    if (err != cudaSuccess) return err;
+    const long long chunk = a.cap_events;
+    for (long long n0 = 0; n0 < a.ev.N; n0 += chunk) {
+      EvBatch ev = a.ev;
+      ev.n0 = n0;
+      const long long cnt = (a.ev.N - n0) < chunk ? (a.ev.N - n0) : chunk;
+      const int epw = ev_lanes(cnt);
+      const unsigned nb = ev_blocks(cnt, epw);
+      if (a.timer && (err = a.timer->begin(a.stream, GWF_KT_SETUP)) != cudaSuccess) return err;
+      for (int d = 0; d < G.nd; ++d) {
+        unsigned char* sc = G.scratch[d];
+        if (G.rec_src[d] && a.core_idx) {
+          const long long words = cnt * (long long)(rec_stride<M>() / 16);
+          copy_records_kernel<<<(unsigned)((words + 255) / 256), 256, 0, a.stream>>>(
+              reinterpret_cast<const uint4*>(G.rec_src[d]), a.core_idx + n0, cnt, reinterpret_cast<uint4*>(sc));
+          if (G.patch[d]) proj_patch_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(ev, G.det[d], sc, cnt, epw);
+        } else if (d == 0) {
+          setup_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(ev, G.det[0], a.wf, a.qnm, a.nq, sc, cnt, a.core, a.core_mode,
+                                                         a.core_idx, epw);
+          if (a.core_done && a.core_mode == 1 && (err = cudaEventRecord(a.core_done, a.stream)) != cudaSuccess) return err;
+        } else {
+          proj_patch_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(ev, G.det[d], sc, cnt, epw);
+        }
+      }
+      if (a.timer && (err = a.timer->end(a.stream)) != cudaSuccess) return err;
+      if (a.seg > 0) {
+        if (a.timer && (err = a.timer->begin(a.stream, GWF_KT_SEGMENTED)) != cudaSuccess) return err;
+        seg_scan_kernel<M><<<1, 1024, 0, a.stream>>>(G.scratch[0], cnt, a.seg, a.seg_off);
+        if ((err = cudaMemsetAsync(a.seg_ctr, 0, sizeof(unsigned long long), a.stream)) != cudaSuccess) return err;
+        const SegInfo si = seg_info(a);
+        const int gr = (a.seg_cap > 0 && a.seg_cap < grid) ? (int)a.seg_cap : grid;
+        ks<<<gr, kThreads, smem, a.stream>>>(ev, g, cnt, si);
+        gram_reduce_kernel<1><<<(unsigned)cnt, kThreads, 0, a.stream>>>(ev.n0, ev.N, cnt, si, nullptr, 0, nullptr,
+                                                                        a.out_det, nullptr, nullptr, a.accum);
+      } else {
+        if (a.timer && (err = a.timer->begin(a.stream, GWF_KT_FISHER_F64)) != cudaSuccess) return err;
+        kc<<<(unsigned)cnt, kThreads, smem, a.stream>>>(ev, g, a.out_det, a.accum);
+      }
+      err = cudaGetLastError();
+      if (err == cudaSuccess && a.timer) err = a.timer->end(a.stream);
+      if (err != cudaSuccess) return err;
+    }
+    return cudaSuccess;
+  }
+}
+
+cudaError_t group64_dispatch(const LaunchArgs& a, const Group64& G) {
+  return a.det.earth ? group64_one<true>(a, G) : group64_one<false>(a, G);
+}
+
 template <bool EARTH, int NARM>
 cudaError_t wave_one(const LaunchArgs& a, const WaveOut& o) {
   EvBatch ev = a.ev;

@@ -285,3 +285,26 @@ def test_detector_groups_distinct_psds(gpu_lib):
     assert e.max() < 1e-5
     assert np.median(e64.max(axis=(1, 2))) < 1e-5
     assert np.median(sg.max(axis=1)) < 3 * np.median(ss.max(axis=1)) + 1e-6
+
+
+@pytest.mark.parametrize('model,dets,maker', [
+    ('IMRPhenomD', synthetic.NETWORK_LHET, synthetic.bbh_events),
+    ('IMRPhenomHM', (('L1', 10.), ('H1', 10.), ('Virgo', 10.)), synthetic.bbh_events),
+    ('TaylorF2_RestrictedPN', (('L1', 10.), ('Virgo', 10.)), synthetic.bns_events)])
+def test_fp64_detector_groups(gpu_lib, model, dets, maker):
+    """FP64 network total with the L-shaped detectors that share the grid in one launch (the waveform and
+    its tangent once per point) against one launch per detector: the same sums in another order."""
+    from gwfast_gb300 import _lib
+    ev = maker(64, seed=17)
+    net = synthetic.make_network(getattr(W, model)(), dets=dets, earth=True)
+    ctx = _lib.context(0)
+    try:
+        ctx.set_detector_groups(False)
+        Fs = np.moveaxis(net.FisherMatr(dict(ev), res=600), -1, 0)
+        ctx.set_detector_groups(True)
+        Fg = np.moveaxis(net.FisherMatr(dict(ev), res=600), -1, 0)
+    finally:
+        ctx.set_detector_groups(True)
+    e = entry_err(Fg, Fs).max()
+    print('%s FP64 groups vs per detector: max normalised |dF| %.2e' % (model, e))
+    assert e < 1e-12
