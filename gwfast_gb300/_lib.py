@@ -215,7 +215,8 @@ class Context:
         check(load().gwf_set_graphs(self.h, int(bool(on))))
 
     def set_detector_groups(self, on):
-        """FP32 network totals: evaluate detectors that share the grid in one launch (default on)."""
+        """Network totals: evaluate detectors that share the grid in one launch, the waveform once per
+        point (TaylorF2, IMRPhenomD, IMRPhenomHM; every precision; default on)."""
         check(load().gwf_set_detector_groups(self.h, int(bool(on))))
 
     KT_NAMES = {1: 'setup', 2: 'group_f32', 3: 'fisher_f32', 4: 'fisher_f64', 5: 'segmented'}

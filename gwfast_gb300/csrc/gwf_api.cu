@@ -456,8 +456,8 @@ int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const
   int rc = ensure_aux(ctx, n_det);
   if (rc) return rc;
   GWF_CK(cudaMemsetAsync(ctx->mix_sovf.p, 0, (size_t)n_det * sizeof(int), st));
-  // network totals only: the L-shaped detectors that share the grid run as one FP64 group launch (the
-  // waveform once per point), on the first member's stream, its network total in that member's slice
+  // network totals only: the detectors that share the grid run as one FP64 group launch (the waveform
+  // once per point), on the first member's stream, its network total in that member's slice
   std::vector<std::vector<int>> rg;
   const bool rgroup = ctx->groups && !carm && !csda && !csdn && a.wf.model <= GWF_WF_PHENOMHM;
   for (int i = 0; i < n_det; ++i) {
@@ -465,8 +465,8 @@ int refine(gwf_ctx* ctx, int n_det, const int* det_ids, gwf::LaunchArgs a, const
     bool placed = false;
     for (auto& g : rg) {
       const gwf_det_desc& d0 = ctx->dets[det_ids[g[0]]].desc;
-      if (rgroup && (int)g.size() < gwf::kMaxGroup && d0.shape == GWF_SHAPE_L && di.shape == GWF_SHAPE_L &&
-          d0.fmin == di.fmin && d0.fmax == di.fmax && d0.earth_rotation == di.earth_rotation) {
+      if (rgroup && (int)g.size() < gwf::kMaxGroup && d0.fmin == di.fmin && d0.fmax == di.fmax &&
+          d0.earth_rotation == di.earth_rotation) {
         g.push_back(i);
         placed = true;
         break;
@@ -688,7 +688,7 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   // FP32 network totals: detectors with the same grid (fmin, fmax, Earth rotation) form groups
   // that one launch evaluates together (the waveform once per point for the whole group)
   std::vector<std::vector<int>> groups;
-  // (FP64: the 11-parameter models, L-shaped detectors only)
+  // (FP64: the 11-parameter models)
   const bool fp64_groups = precision == GWF_PREC_FP64;
   const bool grouping = fisher && ctx->groups && !darm && !dsda && !dsdn && ctx->seg_points == 0 &&
                         (!fp64_groups || wf->model <= GWF_WF_PHENOMHM);
@@ -698,8 +698,7 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
     for (auto& g : groups) {
       const gwf_det_desc& d0 = ctx->dets[det_ids[g[0]]].desc;
       if (grouping && (int)g.size() < gwf::kMaxGroup && d0.fmin == di.fmin && d0.fmax == di.fmax &&
-          d0.earth_rotation == di.earth_rotation &&
-          (!fp64_groups || (d0.shape == GWF_SHAPE_L && di.shape == GWF_SHAPE_L))) {
+          d0.earth_rotation == di.earth_rotation) {
         g.push_back(i);
         placed = true;
         break;
@@ -789,7 +788,7 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
     first = false;
     ++gi;
     cudaError_t err;
-    if (grp.size() > 1 && fp64_groups) {   // FP64 network total of L-shaped detectors
+    if (grp.size() > 1 && fp64_groups) {   // FP64 network total of the group
       gwf::Group64 G;
       G.nd = (int)grp.size();
       for (int d = 0; d < G.nd; ++d) {

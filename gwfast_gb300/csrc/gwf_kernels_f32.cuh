@@ -1307,8 +1307,8 @@ __global__ void __launch_bounds__(kThreads, group_min_blocks<MODEL>()) fisher_gr
 }
 
 // ------------------------------------------------------------------ detector groups, FP64
-// The FP64 network total of L-shaped detectors that share the grid (same fmin, fmax, Earth-rotation
-// flag), as the FP32 group kernel: per point the waveform and its tangent once (the FP64 dual
+// The FP64 network total of detectors that share the grid (same fmin, fmax, Earth-rotation flag),
+// as the FP32 group kernel: per point the waveform and its tangent once (the FP64 dual
 // evaluation, about two thirds of one detector's work), then each detector's Earth-rotation time,
 // pattern functions, derivative vectors and PSD weight, all accumulated into one Gram (the Gram of
 // the network is the Gram of all its detectors' vectors). The model record and the grid are detector
@@ -1344,8 +1344,11 @@ __device__ inline void f64g_prepare(const GroupDev64& g, long long rec, F64Group
   __syncthreads();
 }
 
-// Gram of points [k0, k1) of the group into G.S.gsum (summed over warps; no strain products)
-template <int MODEL, bool EARTH>
+// Gram of points [k0, k1) of the group into G.S.gsum (summed over warps; no strain products).
+// TRI: the group holds a triangle, whose two combined vectors sqrt(3/2)(U + V) and sqrt(1/2)(U - V)
+// (its three arms' total, as in the per-detector kernel) both go into the Gram; the staging area
+// then has a second set of rows.
+template <int MODEL, bool EARTH, bool TRI>
 __device__ inline void f64g_item(const EvBatch& ev, const GroupDev64& g, F64GroupState<MODEL, EARTH>& G, cd* stage,
                                  int k0, int k1) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1365,9 +1368,25 @@ __device__ inline void f64g_item(const EvBatch& ev, const GroupDev64& g, F64Grou
     ea[i] = eb[i] = 0;
     if (own[i]) pair_n(NPM, e, ea[i], eb[i]);
   }
-  cd* my = stage + (size_t)warp * NPS * kSR64;
+  constexpr int NSET = TRI ? 2 : 1;
+  cd* my = stage + (size_t)warp * NSET * NPS * kSR64;
   const int nd = g.nd;
   double sw = 0.0;
+  // accumulate the rows of staging set gs into this lane's entries
+  auto gram = [&](int gs) {
+    const cd* base_s = my + gs * NPS * kSR64;
+#pragma unroll
+    for (int i = 0; i < EPT; ++i) {
+      if (own[i]) {
+        const cd* ra = base_s + ea[i] * kSR64;
+        const cd* rb = base_s + eb[i] * kSR64;
+        double s2 = 0.0;
+#pragma unroll 8
+        for (int j = 0; j < 32; ++j) s2 += ra[j].re * rb[j].re + ra[j].im * rb[j].im;
+        acc[i] += s2;
+      }
+    }
+  };
   for (int base = k0; base < k1; base += kThreads) {
     const int k = base + tid;
     const bool valid = k < k1;
@@ -1387,32 +1406,40 @@ __device__ inline void f64g_item(const EvBatch& ev, const GroupDev64& g, F64Grou
       analytic_tangents<MODEL>(G.S.E, lnf, dphl, dphd, dphe);
     }
     for (int d = 0; d < nd; ++d) {
-      cd D[NPS];
+      const bool tri = TRI && g.det[d].shape == 1;
+      TimeState ts;
       if (valid) {
         if (!(d > 0 && g.same_psd[d])) sw = sqrt(4.0 * w / psd_at(g.det[d], f, lnf));
-        TimeState ts;
         if (EARTH) time_state(G.pj[d], G.S.pj.tc - tau.v / kDay, ts);
         else ts = G.ts[d];
-        ArmPat ap;
-        if (EARTH) arm_pattern(G.pj[d], g.det[d].sin_zeta, ts.x, 0, ap);
-        else ap = G.ap[d];
-        arm_derivs<NI>(G.pj[d], ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D);
-        analytic_columns<MODEL>(cadd(cscale(P, ap.Fp), cscale(cmuli(C), ap.Fc)), dphl, dphd, dphe, D);
       }
+      for (int a = 0; a < (tri ? 2 : 1); ++a) {
+        cd D[NPS];
+        if (valid) {
+          ArmPat ap;
+          if (EARTH || a > 0) arm_pattern(G.pj[d], g.det[d].sin_zeta, ts.x, a, ap);
+          else ap = G.ap[d];
+          arm_derivs<NI>(G.pj[d], ap, ts, f, P, C, dP, dC, dPi, dCi, dtn, D);
+          analytic_columns<MODEL>(cadd(cscale(P, ap.Fp), cscale(cmuli(C), ap.Fc)), dphl, dphd, dphe, D);
+        }
+        if (!tri) {
 #pragma unroll
-      for (int q = 0; q < NPM; ++q) my[q * kSR64 + lane] = valid ? cscale(D[q], sw) : cd{0.0, 0.0};
-      __syncwarp();
+          for (int q = 0; q < NPM; ++q) my[q * kSR64 + lane] = valid ? cscale(D[q], sw) : cd{0.0, 0.0};
+        } else if (a == 0) {   // the first arm, weighted, waits in set 1's rows
 #pragma unroll
-      for (int i = 0; i < EPT; ++i) {
-        if (own[i]) {
-          const cd* ra = my + ea[i] * kSR64;
-          const cd* rb = my + eb[i] * kSR64;
-          double s2 = 0.0;
-#pragma unroll 8
-          for (int j = 0; j < 32; ++j) s2 += ra[j].re * rb[j].re + ra[j].im * rb[j].im;
-          acc[i] += s2;
+          for (int q = 0; q < NPM; ++q) my[(NPS + q) * kSR64 + lane] = valid ? cscale(D[q], sw) : cd{0.0, 0.0};
+        } else {               // U + V into set 0, U - V into set 1 (this lane's own slots)
+#pragma unroll
+          for (int q = 0; q < NPM; ++q) {
+            const cd u = my[(NPS + q) * kSR64 + lane], v = valid ? cscale(D[q], sw) : cd{0.0, 0.0};
+            my[q * kSR64 + lane] = cscale(cadd(u, v), 1.2247448713915890);
+            my[(NPS + q) * kSR64 + lane] = cscale(cadd(u, cscale(v, -1.0)), 0.70710678118654752);
+          }
         }
       }
+      __syncwarp();
+      gram(0);
+      if (tri) gram(1);
       __syncwarp();
     }
   }
@@ -1434,18 +1461,18 @@ __device__ inline void f64g_item(const EvBatch& ev, const GroupDev64& g, F64Grou
   __syncthreads();
 }
 
-template <int MODEL, bool EARTH>
+template <int MODEL, bool EARTH, bool TRI>
 __global__ void __launch_bounds__(kThreads) fisher_group_kernel64(EvBatch ev, GroupDev64 g, double* out_det, int accum) {
   extern __shared__ __align__(16) unsigned char stage_raw[];
   __shared__ F64GroupState<MODEL, EARTH> G;
   const long long n = ev.n0 + blockIdx.x;
   if (n >= ev.N) return;
   f64g_prepare<MODEL, EARTH>(g, blockIdx.x, G);
-  f64g_item<MODEL, EARTH>(ev, g, G, reinterpret_cast<cd*>(stage_raw), 0, G.S.g.ok ? G.S.g.R : 0);
+  f64g_item<MODEL, EARTH, TRI>(ev, g, G, reinterpret_cast<cd*>(stage_raw), 0, G.S.g.ok ? G.S.g.R : 0);
   write_gram<1, np_of<MODEL>()>(G.S.gsum, 1.0, ColMix{0.0, 0.0}, n, ev.N, nullptr, out_det, nullptr, nullptr, accum);
 }
 
-template <int MODEL, bool EARTH>
+template <int MODEL, bool EARTH, bool TRI>
 __global__ void __launch_bounds__(kThreads) fisher_group_seg_kernel64(EvBatch ev, GroupDev64 g, long long count,
                                                                       SegInfo si) {
   static_assert(np_of<MODEL>() == NP, "segmented launches carry 11-parameter partial Grams");
@@ -1459,7 +1486,7 @@ __global__ void __launch_bounds__(kThreads) fisher_group_seg_kernel64(EvBatch ev
     if (G.S.rec != rec) f64g_prepare<MODEL, EARTH>(g, rec, G);
     const int R = G.S.g.ok ? G.S.g.R : 0;
     const int k1 = k0 + si.seg < R ? k0 + si.seg : R;
-    f64g_item<MODEL, EARTH>(ev, g, G, reinterpret_cast<cd*>(stage_raw), k0, k1);
+    f64g_item<MODEL, EARTH, TRI>(ev, g, G, reinterpret_cast<cd*>(stage_raw), k0, k1);
     double* o = si.partial + item * NEX;
     for (int e = threadIdx.x; e < NEX; e += blockDim.x) o[e] = G.S.gsum[e];
   }

@@ -150,7 +150,7 @@ cudaError_t launch_wave_m7(const LaunchArgs& a, const WaveOut& o);
 cudaError_t launch_group_m0(const LaunchArgs& a, const GroupDev& g);
 cudaError_t launch_group_m1(const LaunchArgs& a, const GroupDev& g);
 cudaError_t launch_group_m2(const LaunchArgs& a, const GroupDev& g);
-// FP64 network total of a group of L-shaped detectors sharing the grid (11-parameter models): per
+// FP64 network total of a group of detectors sharing the grid (11-parameter models): per
 // detector its set-up record slice (a.cap_events records) and, for a gathered batch (a.core_idx),
 // where its records are copied from; a.seg > 0: segmented launch with a's segment buffers
 struct Group64 {

@@ -282,16 +282,16 @@ cudaError_t group_dispatch(const LaunchArgs& a, const GroupDev& g) {
   }
 }
 
-// FP64 network total of a group of L-shaped detectors: per chunk each member's records (detector
+// FP64 network total of a group of detectors on one grid: per chunk each member's records (detector
 // 0: the set-up, or for a gathered batch a copy of the first pass's records; the others: their
 // projection header only, which is all the group kernel reads of them), then one launch over the
-// group, classic or segmented
-template <bool EARTH>
+// group, classic or segmented. TRI: a member is a triangle (a second set of staging rows).
+template <bool EARTH, bool TRI>
 cudaError_t group64_one(const LaunchArgs& a, const Group64& G) {
   if constexpr (np_of<M>() != NP) {
     return cudaErrorNotSupported;
   } else {
-    const int smem = kWarps * (np_of<M>() + 1) * kSR64 * (int)sizeof(cd);
+    const int smem = kWarps * (TRI ? 2 : 1) * (np_of<M>() + 1) * kSR64 * (int)sizeof(cd);
     GroupDev64 g;
     g.nd = G.nd;
     for (int d = 0; d < G.nd; ++d) {
@@ -299,8 +299,8 @@ cudaError_t group64_one(const LaunchArgs& a, const Group64& G) {
       g.rec[d] = G.scratch[d];
       g.same_psd[d] = G.same_psd[d];
     }
-    auto kc = fisher_group_kernel64<M, EARTH>;
-    auto ks = fisher_group_seg_kernel64<M, EARTH>;
+    auto kc = fisher_group_kernel64<M, EARTH, TRI>;
+    auto ks = fisher_group_seg_kernel64<M, EARTH, TRI>;
     cudaError_t err = cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (err == cudaSuccess) err = cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     int grid = 0;
@@ -352,7 +352,10 @@ cudaError_t group64_one(const LaunchArgs& a, const Group64& G) {
 }
 
 cudaError_t group64_dispatch(const LaunchArgs& a, const Group64& G) {
-  return a.det.earth ? group64_one<true>(a, G) : group64_one<false>(a, G);
+  bool tri = false;
+  for (int d = 0; d < G.nd; ++d) tri |= G.det[d].shape == 1;
+  if (tri) return a.det.earth ? group64_one<true, true>(a, G) : group64_one<false, true>(a, G);
+  return a.det.earth ? group64_one<true, false>(a, G) : group64_one<false, false>(a, G);
 }
 
 template <bool EARTH, int NARM>

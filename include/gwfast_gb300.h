@@ -192,11 +192,13 @@ int gwf_overlap(gwf_ctx* ctx, int n_det, const int* det_ids, const gwf_wf_desc* 
                 int64_t ld1, const gwf_wf_desc* wf2, const double* params2, int64_t ld2, int64_t n_events, int32_t res,
                 int mem, double* out_ov, double* out_n1, double* out_n2, void* stream);
 
-/* Detector groups for FP32 network totals (no counterpart in gwfast: a launch-shape choice). on != 0
- * (the default): in gwf_fisher with precision GWF_PREC_FP32 or GWF_PREC_MIXED, per_arm = 0, no
- * SNR derivatives and no segments, detectors with the same fmin, fmax and Earth-rotation flag (up to
- * four) are evaluated by one launch that computes the waveform and its tangent once per frequency
- * point and accumulates all their derivative vectors into one Gram. on = 0: one launch per detector. */
+/* Detector groups for network totals (no counterpart in gwfast: a launch-shape choice). on != 0 (the
+ * default): in gwf_fisher with per_arm = 0, no SNR derivatives and no segments, detectors with the
+ * same fmin, fmax and Earth-rotation flag (up to four) are evaluated by one launch that computes the
+ * waveform and its tangent once per frequency point and accumulates all their derivative vectors into
+ * one Gram (TaylorF2, IMRPhenomD and IMRPhenomHM, every precision; in FP64 the same sums in another
+ * order; the mixed form's FP64 recomputation groups the same way). Detectors with identical PSD
+ * tables share the per-point weight. on = 0: one launch per detector. */
 int gwf_set_detector_groups(gwf_ctx* ctx, int on);
 
 /* Kernel timing (an extension for measurement; no counterpart in gwfast). on != 0: the following

@@ -289,11 +289,14 @@ def test_detector_groups_distinct_psds(gpu_lib):
 
 @pytest.mark.parametrize('model,dets,maker', [
     ('IMRPhenomD', synthetic.NETWORK_LHET, synthetic.bbh_events),
+    ('IMRPhenomD', (('ETS', 10.), ('L1', 10.), ('H1', 10.)), synthetic.bbh_events),
     ('IMRPhenomHM', (('L1', 10.), ('H1', 10.), ('Virgo', 10.)), synthetic.bbh_events),
+    ('IMRPhenomHM', synthetic.NETWORK_ET_CE, synthetic.bbh_events),
     ('TaylorF2_RestrictedPN', (('L1', 10.), ('Virgo', 10.)), synthetic.bns_events)])
 def test_fp64_detector_groups(gpu_lib, model, dets, maker):
-    """FP64 network total with the L-shaped detectors that share the grid in one launch (the waveform and
-    its tangent once per point) against one launch per detector: the same sums in another order."""
+    """FP64 network total with the detectors that share the grid in one launch (the waveform and its
+    tangent once per point; a triangle among them contributes its two combined vectors) against one
+    launch per detector: the same sums in another order."""
     from gwfast_gb300 import _lib
     ev = maker(64, seed=17)
     net = synthetic.make_network(getattr(W, model)(), dets=dets, earth=True)
