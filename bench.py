@@ -771,7 +771,7 @@ def main():
     if world == 1 and not args.headline_only:
         # the other workloads as keys of the same line (each its own synthetic catalogue; plain FP64
         # arms on samples of the same catalogue, as stated in each)
-        line['config4_north_star'] = measure_screen(1000000, args.train_events, args.train_epochs, 2, 1)
+        line['config4_screened_catalogue'] = measure_screen(1000000, args.train_events, args.train_epochs, 2, 1)
         line['config2_mixed_catalogue'] = measure_mixed_catalogue(100000, 2, 1, args.refine_cond)
         line['config3_phenomhm'] = measure_hm(100000, 2, 1, args.refine_cond)
     if not args.no_cpu_baseline:
