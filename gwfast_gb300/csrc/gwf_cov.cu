@@ -14,6 +14,49 @@
 
 namespace gwf {
 
+// cyclic Jacobi: B = A driven to diagonal form; V (if not null) accumulates the rotations. The
+// eigenvectors are only needed when the Cholesky factorisation fails, so the common path runs
+// without them (a third of each rotation's work) and the rare failure runs the sweeps again.
+template <int NC>
+__device__ void jacobi(const double* A, double* B, double* V) {
+  for (int i = 0; i < NC * NC; ++i) {
+    B[i] = A[i];
+    if (V) V[i] = (i % (NC + 1) == 0) ? 1.0 : 0.0;
+  }
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0.0, dia = 0.0;
+    for (int p = 0; p < NC; ++p) {
+      dia += B[p * NC + p] * B[p * NC + p];
+      for (int q = p + 1; q < NC; ++q) off += B[p * NC + q] * B[p * NC + q];
+    }
+    if (off <= 1e-34 * dia) break;
+    for (int p = 0; p < NC - 1; ++p)
+      for (int q = p + 1; q < NC; ++q) {
+        const double apq = B[p * NC + q];
+        if (apq == 0.0) continue;
+        const double th = (B[q * NC + q] - B[p * NC + p]) / (2.0 * apq);
+        const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+        const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+        for (int k = 0; k < NC; ++k) {  // B <- B G (columns p, q)
+          const double bkp = B[k * NC + p], bkq = B[k * NC + q];
+          B[k * NC + p] = cs * bkp - sn * bkq;
+          B[k * NC + q] = sn * bkp + cs * bkq;
+        }
+        for (int k = 0; k < NC; ++k) {  // B <- G^T B (rows p, q)
+          const double bpk = B[p * NC + k], bqk = B[q * NC + k];
+          B[p * NC + k] = cs * bpk - sn * bqk;
+          B[q * NC + k] = sn * bpk + cs * bqk;
+        }
+        if (V)
+          for (int k = 0; k < NC; ++k) {
+            const double vkp = V[k * NC + p], vkq = V[k * NC + q];
+            V[k * NC + p] = cs * vkp - sn * vkq;
+            V[k * NC + q] = sn * vkp + cs * vkq;
+          }
+      }
+  }
+}
+
 template <int NC>
 __global__ void cov_kernel(const double* __restrict__ F, long long N, double* __restrict__ cov,
                            double* __restrict__ eps, double* __restrict__ cond) {
@@ -40,40 +83,9 @@ __global__ void cov_kernel(const double* __restrict__ F, long long N, double* __
     if (cond) cond[n] = nan("");
     return;
   }
-  // ---- cyclic Jacobi on a copy: B -> diag, V accumulates rotations
+  // ---- cyclic Jacobi on a copy: B -> diag (the eigenvalues, for the condition number)
   double B[NC * NC];
-  for (int i = 0; i < NC * NC; ++i) { B[i] = A[i]; V[i] = (i % (NC + 1) == 0) ? 1.0 : 0.0; }
-  for (int sweep = 0; sweep < 60; ++sweep) {
-    double off = 0.0, dia = 0.0;
-    for (int p = 0; p < NC; ++p) {
-      dia += B[p * NC + p] * B[p * NC + p];
-      for (int q = p + 1; q < NC; ++q) off += B[p * NC + q] * B[p * NC + q];
-    }
-    if (off <= 1e-34 * dia) break;
-    for (int p = 0; p < NC - 1; ++p)
-      for (int q = p + 1; q < NC; ++q) {
-        const double apq = B[p * NC + q];
-        if (apq == 0.0) continue;
-        const double th = (B[q * NC + q] - B[p * NC + p]) / (2.0 * apq);
-        const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-        const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
-        for (int k = 0; k < NC; ++k) {  // B <- B G (columns p, q)
-          const double bkp = B[k * NC + p], bkq = B[k * NC + q];
-          B[k * NC + p] = cs * bkp - sn * bkq;
-          B[k * NC + q] = sn * bkp + cs * bkq;
-        }
-        for (int k = 0; k < NC; ++k) {  // B <- G^T B (rows p, q)
-          const double bpk = B[p * NC + k], bqk = B[q * NC + k];
-          B[p * NC + k] = cs * bpk - sn * bqk;
-          B[q * NC + k] = sn * bpk + cs * bqk;
-        }
-        for (int k = 0; k < NC; ++k) {
-          const double vkp = V[k * NC + p], vkq = V[k * NC + q];
-          V[k * NC + p] = cs * vkp - sn * vkq;
-          V[k * NC + q] = sn * vkp + cs * vkq;
-        }
-      }
-  }
+  jacobi<NC>(A, B, nullptr);
   double lmax = 0.0, lmin = INFINITY;
   bool negative = false;
   for (int i = 0; i < NC; ++i) {
@@ -117,7 +129,8 @@ __global__ void cov_kernel(const double* __restrict__ F, long long N, double* __
         for (int k = (i > j ? i : j); k < NC; ++k) s += M[k * NC + i] * M[k * NC + j];
         C[i * NC + j] = s;
       }
-  } else {
+  } else {   // (rare) the eigen-decomposition again, with its vectors: C' = V diag(1/l) V^T
+    jacobi<NC>(A, B, V);
     for (int i = 0; i < NC; ++i)
       for (int j = 0; j < NC; ++j) {
         double s = 0.0;
