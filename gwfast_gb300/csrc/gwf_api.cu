@@ -688,10 +688,15 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   // FP32 network totals: detectors with the same grid (fmin, fmax, Earth rotation) form groups
   // that one launch evaluates together (the waveform once per point for the whole group)
   std::vector<std::vector<int>> groups;
-  // (FP64: the 11-parameter models)
+  // (FP64: the 11-parameter models, Fisher network totals and SNRs; FP32: Fisher network totals)
   const bool fp64_groups = precision == GWF_PREC_FP64;
-  const bool grouping = fisher && ctx->groups && !darm && !dsda && !dsdn && ctx->seg_points == 0 &&
-                        (!fp64_groups || wf->model <= GWF_WF_PHENOMHM);
+  const bool grouping = ctx->groups && !dsda && !dsdn && ctx->seg_points == 0 &&
+                        (fisher ? (!darm && (!fp64_groups || wf->model <= GWF_WF_PHENOMHM))
+                                : (fp64_groups && wf->model <= GWF_WF_PHENOMHM));
+  // per-arm output slot of each detector, in the order of det_ids (groups may launch in another order)
+  std::vector<int> slot_of(n_det, 0);
+  for (int i = 1; i < n_det; ++i)
+    slot_of[i] = slot_of[i - 1] + (ctx->dets[det_ids[i - 1]].desc.shape == GWF_SHAPE_T ? 3 : 1);
   for (int i = 0; i < n_det; ++i) {
     const gwf_det_desc& di = ctx->dets[det_ids[i]].desc;
     bool placed = false;
@@ -760,7 +765,6 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   a.per_arm = per_arm || dsda;   // per-arm SNR derivatives need the per-arm Gram sets
   a.precision = precision == GWF_PREC_FP64 ? GWF_PREC_FP64 : GWF_PREC_FP32;
   a.stream = st;
-  int slot = 0;
   bool first = true;
   if (side) GWF_CK(cudaEventRecord(ctx->fork, st));
   // the mixed form's second stage reuses the FP64 set-up records of this pass when they all stay in
@@ -800,7 +804,14 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
       a.out_arm = nullptr;
       a.out_sd_arm = nullptr;
       a.out_sd_det = nullptr;
-      err = wf->model == 0 ? gwf::launch_group64_m0(a, G) : (wf->model == 1 ? gwf::launch_group64_m1(a, G) : gwf::launch_group64_m2(a, G));
+      if (fisher) {
+        err = wf->model == 0 ? gwf::launch_group64_m0(a, G)
+                             : (wf->model == 1 ? gwf::launch_group64_m1(a, G) : gwf::launch_group64_m2(a, G));
+      } else {
+        for (int d = 0; d < G.nd; ++d) G.out_arm[d] = darm ? darm + (size_t)slot_of[grp[d]] * N : nullptr;
+        err = wf->model == 0 ? gwf::launch_snr_group64_m0(a, G)
+                             : (wf->model == 1 ? gwf::launch_snr_group64_m1(a, G) : gwf::launch_snr_group64_m2(a, G));
+      }
       if (err != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(err));
       if (side && gi > 1) GWF_CK(cudaEventRecord(ctx->aux_done[gi - 1], a.stream));
       continue;
@@ -833,13 +844,12 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
     const DetRec& r = ctx->dets[det_ids[grp[0]]];
     if (keep_recs) recs[grp[0]] = a.scratch;
     a.det = dev_of(r);
-    a.out_arm = darm ? darm + (size_t)slot * N * per : nullptr;
-    a.out_sd_arm = dsda ? dsda + (size_t)slot * N * npar : nullptr;
+    a.out_arm = darm ? darm + (size_t)slot_of[grp[0]] * N * per : nullptr;
+    a.out_sd_arm = dsda ? dsda + (size_t)slot_of[grp[0]] * N * npar : nullptr;
     a.out_sd_det = dsdn;
     err = fisher ? launch_fisher_any(wf->model, a) : launch_snr_any(wf->model, a);
     if (err != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(err));
     if (side && gi > 1) GWF_CK(cudaEventRecord(ctx->aux_done[gi - 1], a.stream));
-    slot += r.desc.shape == GWF_SHAPE_T ? 3 : 1;
   }
   if (side) {   // join the groups and add their network totals
     for (int g = 1; g < ngr; ++g) GWF_CK(cudaStreamWaitEvent(st, ctx->aux_done[g], 0));

@@ -1492,6 +1492,103 @@ __global__ void __launch_bounds__(kThreads) fisher_group_seg_kernel64(EvBatch ev
   }
 }
 
+// FP64 SNR of a group of detectors on one grid (gwfast/signal.py:658-777 per detector): the waveform
+// value and the time to coalescence once per point for the group, then each detector's pattern
+// functions and PSD weight. Outputs per detector as snr_kernel: its arms' sums at out_arm[d] (slot a at
+// out_arm[d] + a N, when not null) and the network total 4 sum over all arms into out_det.
+struct GroupSNR64 {
+  DetDev det[kMaxGroup];
+  const unsigned char* rec[kMaxGroup];   // each detector's set-up records (d > 0: the header is read)
+  double* out_arm[kMaxGroup];
+  int same_psd[kMaxGroup];
+  int nd;
+};
+
+template <int MODEL, bool EARTH, bool TRI>
+__global__ void __launch_bounds__(kThreads) snr_group_kernel64(EvBatch ev, GroupSNR64 g, double* out_det, int accum) {
+  __shared__ EvUnion E;
+  __shared__ GridEv gr;
+  __shared__ ProjEv pj[kMaxGroup];
+  __shared__ ArmPat apc[kMaxGroup][2];
+  __shared__ double red[kWarps][kMaxGroup * 3];
+  const long long n = ev.n0 + blockIdx.x;
+  if (n >= ev.N) return;
+  block_load<MODEL>(E, pj[0], gr, g.rec[0], blockIdx.x);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nd = g.nd;
+  if (tid < nd) {
+    const int d = tid;
+    if (d > 0) pj[d] = reinterpret_cast<const SetupHdr*>(g.rec[d] + (size_t)blockIdx.x * rec_stride<MODEL>())->pj;
+    if (!EARTH) {
+      TimeState ts;
+      time_state(pj[d], pj[d].tc, ts);
+      for (int a = 0; a < (g.det[d].shape == 1 ? 2 : 1); ++a) arm_pattern(pj[d], g.det[d].sin_zeta, ts.x, a, apc[d][a]);
+    }
+  }
+  __syncthreads();
+  double s[kMaxGroup][3];
+#pragma unroll
+  for (int d = 0; d < kMaxGroup; ++d) s[d][0] = s[d][1] = s[d][2] = 0.0;
+  const int R = gr.ok ? gr.R : 0;
+  for (int k = tid; k < R; k += kThreads) {
+    double f, lnf, w;
+    grid_point(gr, ev.spacing, k, f, lnf, w);
+    double ap, ac, tau = 0.0;
+    wave_point_val<MODEL, EARTH>(E, pj[0], f, lnf, ap, ac, tau);
+    double ws = 0.0;
+#pragma unroll
+    for (int d = 0; d < kMaxGroup; ++d) {
+      if (d >= nd) break;
+      if (!(d > 0 && g.same_psd[d])) ws = w / psd_at(g.det[d], f, lnf);
+      const bool tri = TRI && g.det[d].shape == 1;
+      double Fp[2], Fc[2];
+      if (EARTH) {
+        TimeState ts;
+        time_state(pj[d], pj[0].tc - tau / kDay, ts);
+        for (int a = 0; a < (tri ? 2 : 1); ++a) {
+          ArmPat p;
+          arm_pattern(pj[d], g.det[d].sin_zeta, ts.x, a, p);
+          Fp[a] = p.Fp;
+          Fc[a] = p.Fc;
+        }
+      } else {
+        for (int a = 0; a < (tri ? 2 : 1); ++a) { Fp[a] = apc[d][a].Fp; Fc[a] = apc[d][a].Fc; }
+      }
+      const double p1 = ap * Fp[0], c1 = ac * Fc[0];
+      s[d][0] += ws * (p1 * p1 + c1 * c1);
+      if (tri) {
+        const double p2 = ap * Fp[1], c2 = ac * Fc[1];
+        s[d][1] += ws * (p2 * p2 + c2 * c2);
+        const double p3 = p1 + p2, c3 = c1 + c2;
+        s[d][2] += ws * (p3 * p3 + c3 * c3);
+      }
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < kMaxGroup; ++d)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      double v = s[d][a];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[warp][d * 3 + a] = v;
+    }
+  __syncthreads();
+  if (tid == 0) {
+    double tot = 0.0;
+    for (int d = 0; d < nd; ++d) {
+      const int na = g.det[d].shape == 1 ? 3 : 1;
+      for (int a = 0; a < na; ++a) {
+        double v = 0.0;
+        for (int wp = 0; wp < kWarps; ++wp) v += red[wp][d * 3 + a];
+        if (g.out_arm[d]) g.out_arm[d][(size_t)a * ev.N + n] = v;
+        tot += 4.0 * v;
+      }
+    }
+    if (out_det) out_det[n] = accum ? out_det[n] + tot : tot;
+  }
+}
+
 // ------------------------------------------------------------------ FP32 SNR
 // Per arm: scale * sum_k w_k / S_k (|h+|^2 F+^2 + |hx|^2 Fx^2) with the amplitudes, the pattern
 // functions and the Earth-rotation time in FP32; each thread sums its points with Kahan compensation,

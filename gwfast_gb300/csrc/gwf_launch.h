@@ -160,10 +160,15 @@ struct Group64 {
   unsigned char* scratch[kMaxGroup] = {};
   const unsigned char* rec_src[kMaxGroup] = {};   // null: the set-up runs (detector 0) or only the header
   int patch[kMaxGroup] = {};                       // rec_src is another detector's: recompute the header
+  double* out_arm[kMaxGroup] = {};                 // SNR: each detector's per-arm slots (or null)
 };
 cudaError_t launch_group64_m0(const LaunchArgs& a, const Group64& g);
 cudaError_t launch_group64_m1(const LaunchArgs& a, const Group64& g);
 cudaError_t launch_group64_m2(const LaunchArgs& a, const Group64& g);
+// FP64 SNR of such a group (network total into a.out_det, per-arm slots into g.out_arm)
+cudaError_t launch_snr_group64_m0(const LaunchArgs& a, const Group64& g);
+cudaError_t launch_snr_group64_m1(const LaunchArgs& a, const Group64& g);
+cudaError_t launch_snr_group64_m2(const LaunchArgs& a, const Group64& g);
 size_t setup_stride_m0();
 size_t core_bytes_m0();
 size_t core_bytes_m1();

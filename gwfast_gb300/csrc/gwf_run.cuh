@@ -282,6 +282,32 @@ cudaError_t group_dispatch(const LaunchArgs& a, const GroupDev& g) {
   }
 }
 
+// records of events [ev.n0, ev.n0 + cnt) for each member of an FP64 group: detector 0 runs the set-up
+// (or, for a gathered batch, copies the first pass's records), the others get their projection header
+// only, which is all the group kernels read of them
+cudaError_t group64_records(const LaunchArgs& a, const Group64& G, const EvBatch& ev, long long cnt, int epw,
+                            unsigned nb) {
+  for (int d = 0; d < G.nd; ++d) {
+    unsigned char* sc = G.scratch[d];
+    if (G.rec_src[d] && a.core_idx) {
+      const long long words = cnt * (long long)(rec_stride<M>() / 16);
+      copy_records_kernel<<<(unsigned)((words + 255) / 256), 256, 0, a.stream>>>(
+          reinterpret_cast<const uint4*>(G.rec_src[d]), a.core_idx + ev.n0, cnt, reinterpret_cast<uint4*>(sc));
+      if (G.patch[d]) proj_patch_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(ev, G.det[d], sc, cnt, epw);
+    } else if (d == 0) {
+      setup_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(ev, G.det[0], a.wf, a.qnm, a.nq, sc, cnt, a.core, a.core_mode,
+                                                     a.core_idx, epw);
+      if (a.core_done && a.core_mode == 1) {
+        const cudaError_t err = cudaEventRecord(a.core_done, a.stream);
+        if (err != cudaSuccess) return err;
+      }
+    } else {
+      proj_patch_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(ev, G.det[d], sc, cnt, epw);
+    }
+  }
+  return cudaGetLastError();
+}
+
 // FP64 network total of a group of detectors on one grid: per chunk each member's records (detector
 // 0: the set-up, or for a gathered batch a copy of the first pass's records; the others: their
 // projection header only, which is all the group kernel reads of them), then one launch over the
@@ -314,21 +340,7 @@ cudaError_t group64_one(const LaunchArgs& a, const Group64& G) {
       const int epw = ev_lanes(cnt);
       const unsigned nb = ev_blocks(cnt, epw);
       if (a.timer && (err = a.timer->begin(a.stream, GWF_KT_SETUP)) != cudaSuccess) return err;
-      for (int d = 0; d < G.nd; ++d) {
-        unsigned char* sc = G.scratch[d];
-        if (G.rec_src[d] && a.core_idx) {
-          const long long words = cnt * (long long)(rec_stride<M>() / 16);
-          copy_records_kernel<<<(unsigned)((words + 255) / 256), 256, 0, a.stream>>>(
-              reinterpret_cast<const uint4*>(G.rec_src[d]), a.core_idx + n0, cnt, reinterpret_cast<uint4*>(sc));
-          if (G.patch[d]) proj_patch_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(ev, G.det[d], sc, cnt, epw);
-        } else if (d == 0) {
-          setup_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(ev, G.det[0], a.wf, a.qnm, a.nq, sc, cnt, a.core, a.core_mode,
-                                                         a.core_idx, epw);
-          if (a.core_done && a.core_mode == 1 && (err = cudaEventRecord(a.core_done, a.stream)) != cudaSuccess) return err;
-        } else {
-          proj_patch_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(ev, G.det[d], sc, cnt, epw);
-        }
-      }
+      if ((err = group64_records(a, G, ev, cnt, epw, nb)) != cudaSuccess) return err;
       if (a.timer && (err = a.timer->end(a.stream)) != cudaSuccess) return err;
       if (a.seg > 0) {
         if (a.timer && (err = a.timer->begin(a.stream, GWF_KT_SEGMENTED)) != cudaSuccess) return err;
@@ -349,6 +361,42 @@ cudaError_t group64_one(const LaunchArgs& a, const Group64& G) {
     }
     return cudaSuccess;
   }
+}
+
+// FP64 SNR of a group of detectors on one grid: per chunk the members' records, then one launch
+template <bool EARTH, bool TRI>
+cudaError_t snr_group64_one(const LaunchArgs& a, const Group64& G) {
+  if constexpr (np_of<M>() != NP) {
+    return cudaErrorNotSupported;
+  } else {
+    GroupSNR64 g;
+    g.nd = G.nd;
+    for (int d = 0; d < G.nd; ++d) {
+      g.det[d] = G.det[d];
+      g.rec[d] = G.scratch[d];
+      g.out_arm[d] = G.out_arm[d];
+      g.same_psd[d] = G.same_psd[d];
+    }
+    const long long chunk = a.cap_events;
+    for (long long n0 = 0; n0 < a.ev.N; n0 += chunk) {
+      EvBatch ev = a.ev;
+      ev.n0 = n0;
+      const long long cnt = (a.ev.N - n0) < chunk ? (a.ev.N - n0) : chunk;
+      const int epw = ev_lanes(cnt);
+      cudaError_t err = group64_records(a, G, ev, cnt, epw, ev_blocks(cnt, epw));
+      if (err != cudaSuccess) return err;
+      snr_group_kernel64<M, EARTH, TRI><<<(unsigned)cnt, kThreads, 0, a.stream>>>(ev, g, a.out_det, a.accum);
+      if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    }
+    return cudaSuccess;
+  }
+}
+
+cudaError_t snr_group64_dispatch(const LaunchArgs& a, const Group64& G) {
+  bool tri = false;
+  for (int d = 0; d < G.nd; ++d) tri |= G.det[d].shape == 1;
+  if (tri) return a.det.earth ? snr_group64_one<true, true>(a, G) : snr_group64_one<false, true>(a, G);
+  return a.det.earth ? snr_group64_one<true, false>(a, G) : snr_group64_one<false, false>(a, G);
 }
 
 cudaError_t group64_dispatch(const LaunchArgs& a, const Group64& G) {
