@@ -688,11 +688,10 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
   // FP32 network totals: detectors with the same grid (fmin, fmax, Earth rotation) form groups
   // that one launch evaluates together (the waveform once per point for the whole group)
   std::vector<std::vector<int>> groups;
-  // (FP64: the 11-parameter models, Fisher network totals and SNRs; FP32: Fisher network totals)
+  // (the 11-parameter models: Fisher network totals and SNRs, every precision)
   const bool fp64_groups = precision == GWF_PREC_FP64;
-  const bool grouping = ctx->groups && !dsda && !dsdn && ctx->seg_points == 0 &&
-                        (fisher ? (!darm && (!fp64_groups || wf->model <= GWF_WF_PHENOMHM))
-                                : (fp64_groups && wf->model <= GWF_WF_PHENOMHM));
+  const bool grouping = ctx->groups && !dsda && !dsdn && ctx->seg_points == 0 && wf->model <= GWF_WF_PHENOMHM &&
+                        (!fisher || !darm);
   // per-arm output slot of each detector, in the order of det_ids (groups may launch in another order)
   std::vector<int> slot_of(n_det, 0);
   for (int i = 1; i < n_det; ++i)
@@ -816,7 +815,23 @@ int run_body(gwf_ctx* ctx, bool fisher, int n_det, const int* det_ids, const gwf
       if (side && gi > 1) GWF_CK(cudaEventRecord(ctx->aux_done[gi - 1], a.stream));
       continue;
     }
-    if (grp.size() > 1) {   // (grouping implies: FP32 Fisher, network total only)
+    if (grp.size() > 1 && !fisher) {   // FP32 SNR of the group
+      gwf::Group64 G;
+      G.nd = (int)grp.size();
+      for (int d = 0; d < G.nd; ++d) {
+        G.det[d] = dev_of(ctx->dets[det_ids[grp[d]]]);
+        G.same_psd[d] = d > 0 && ctx->dets[det_ids[grp[d]]].psd_class == ctx->dets[det_ids[grp[d - 1]]].psd_class;
+        G.out_arm[d] = darm ? darm + (size_t)slot_of[grp[d]] * N : nullptr;
+      }
+      a.det = G.det[0];
+      a.out_arm = nullptr;
+      err = wf->model == 0 ? gwf::launch_snr_group_f32_m0(a, G)
+                           : (wf->model == 1 ? gwf::launch_snr_group_f32_m1(a, G) : gwf::launch_snr_group_f32_m2(a, G));
+      if (err != cudaSuccess) return fail(GWF_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(err));
+      if (side && gi > 1) GWF_CK(cudaEventRecord(ctx->aux_done[gi - 1], a.stream));
+      continue;
+    }
+    if (grp.size() > 1) {   // (grouping implies here: FP32 Fisher, network total only)
       gwf::GroupDev g;
       g.nd = (int)grp.size();
       for (int d = 0; d < g.nd; ++d) {

@@ -1690,4 +1690,138 @@ __global__ void __launch_bounds__(kThreads) snr_kernel_f32(EvBatch ev, DetDev de
   }
 }
 
+// FP32 SNR of a group of detectors on one grid: the waveform value and the time to coalescence (and
+// the Earth-rotation angle) once per point for the group, then each detector's pattern functions and
+// PSD weight, as snr_kernel_f32 per detector. Detector d's projection comes from its FP32 record slot;
+// its sums are scaled by its own amplitude^2 / PSD normalisation (detector 0's times sr[d]).
+struct GroupSNR32 {
+  DetDev det[kMaxGroup];
+  double* out_arm[kMaxGroup];
+  double sr[kMaxGroup];      // psd_scale of detector 0 / psd_scale of detector d
+  int same_psd[kMaxGroup];
+  int nd;
+  long long slice;           // bytes between the FP32 record areas of consecutive detectors
+};
+
+template <int MODEL, bool EARTH, bool TRI>
+__global__ void __launch_bounds__(kThreads) snr_group_kernel_f32(EvBatch ev, GroupSNR32 g, const unsigned char* scratch32,
+                                                                 double* out_det, int accum) {
+  __shared__ F32Rec<MODEL> r;
+  __shared__ GroupProj gp;
+  __shared__ double red[kWarps][kMaxGroup * 3];
+  const long long n = ev.n0 + blockIdx.x;
+  if (n >= ev.N) return;
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(scratch32 + (size_t)blockIdx.x * f32_stride<MODEL>());
+    uint4* dst = reinterpret_cast<uint4*>(&r);
+    for (int i = threadIdx.x; i < (int)(sizeof(F32Rec<MODEL>) / 16); i += blockDim.x) dst[i] = src[i];
+  }
+  const int nd = g.nd;
+  if ((int)threadIdx.x < nd) {
+    const int d = threadIdx.x;
+    const F32Rec<MODEL>& rd =
+        *reinterpret_cast<const F32Rec<MODEL>*>(scratch32 + d * g.slice + (size_t)blockIdx.x * f32_stride<MODEL>());
+    gp.pf[d] = rd.pf;
+    gp.apc[d][0] = rd.apc[0];
+    gp.apc[d][1] = rd.apc[1];
+    gp.tsc[d] = rd.tsc;
+  }
+  __syncthreads();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  float sum[kMaxGroup][3], cmp[kMaxGroup][3];
+#pragma unroll
+  for (int d = 0; d < kMaxGroup; ++d)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) sum[d][a] = cmp[d][a] = 0.0f;
+  const int R = r.gf.R;
+  GridIterF grid;
+  for (int base = 0; base < R; base += kThreads) {
+    const int k = base + tid;
+    grid.step(r, ev.spacing, base, lane, warp);
+    if (k >= R) continue;
+    float f, lnf, w;
+    grid.point(r, ev.spacing, k, lane, f, lnf, w);
+    float ap, ac, tau = 0.0f;
+    if constexpr (MODEL == 2) {
+      WaveF wv;
+      wave_f32_hm<EARTH>(r.ef, r.pf, r.tf, f, lnf, wv);
+      ap = sqrtf(wv.P.re * wv.P.re + wv.P.im * wv.P.im);
+      ac = sqrtf(wv.C.re * wv.C.re + wv.C.im * wv.C.im);
+      tau = wv.tau;
+    } else {
+      float A;
+      if (MODEL == 0) {
+        const float f13 = cbrtf(f);
+        A = r.ef.tf2.ampK.v * (1.0f / (f * sqrtf(f13)));
+        if (EARTH) tau = tau_star_point<float>(r.ef.tf2.Ms, r.ef.tf2.vM, r.ef.tf2.eta, f13);
+      } else {
+        A = phd_amp_point<float>(r.ef.phd, f);
+        if (EARTH) tau = tau_star_point<float>(r.ef.phd.Ms, r.ef.phd.vM, r.ef.phd.eta, cbrtf(f));
+      }
+      ap = A * r.pf.cp;
+      ac = A * r.pf.ci;
+    }
+    float sd = 0.0f, cd = 1.0f;   // the Earth-rotation angle is the same for every detector
+    if (EARTH) rot_sc_tau(tau, sd, cd);
+    float ws = 0.0f;
+#pragma unroll
+    for (int d = 0; d < kMaxGroup; ++d) {
+      if (d >= nd) break;
+      const DetDev& det = g.det[d];
+      if (!(d > 0 && g.same_psd[d])) ws = w / psd_at_f(det, f, lnf, (float)det.acc_l0, (float)det.acc_idl);
+      const bool tri = TRI && det.shape == 1;
+      TimeF ts;
+      if (EARTH) time_f_rot(gp.pf[d], sd, cd, ts);
+      float p[2], c[2];
+      for (int a = 0; a < (tri ? 2 : 1); ++a) {
+        ArmF pat;
+        if (EARTH) arm_f(gp.pf[d], ts, a, pat);
+        else pat = gp.apc[d][a];
+        p[a] = ap * pat.Fp;
+        c[a] = ac * pat.Fc;
+      }
+      float term[3];
+      term[0] = ws * (p[0] * p[0] + c[0] * c[0]);
+      term[1] = term[2] = 0.0f;
+      if (tri) {
+        term[1] = ws * (p[1] * p[1] + c[1] * c[1]);
+        const float p3 = p[0] + p[1], c3 = c[0] + c[1];
+        term[2] = ws * (p3 * p3 + c3 * c3);
+      }
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {   // Kahan
+        const float y = term[a] - cmp[d][a];
+        const float t = sum[d][a] + y;
+        cmp[d][a] = (t - sum[d][a]) - y;
+        sum[d][a] = t;
+      }
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < kMaxGroup; ++d)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      double v = (double)sum[d][a] - (double)cmp[d][a];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[warp][d * 3 + a] = v;
+    }
+  __syncthreads();
+  if (tid == 0) {
+    double tot = 0.0;
+    for (int d = 0; d < nd; ++d) {
+      const int na = g.det[d].shape == 1 ? 3 : 1;
+      const double sc = r.scale * g.sr[d];
+      for (int a = 0; a < na; ++a) {
+        double v = 0.0;
+        for (int wp = 0; wp < kWarps; ++wp) v += red[wp][d * 3 + a];
+        v *= sc;
+        if (g.out_arm[d]) g.out_arm[d][(size_t)a * ev.N + n] = v;
+        tot += 4.0 * v;
+      }
+    }
+    if (out_det) out_det[n] = accum ? out_det[n] + tot : tot;
+  }
+}
+
 }  // namespace gwf

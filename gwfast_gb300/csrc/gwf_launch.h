@@ -169,6 +169,10 @@ cudaError_t launch_group64_m2(const LaunchArgs& a, const Group64& g);
 cudaError_t launch_snr_group64_m0(const LaunchArgs& a, const Group64& g);
 cudaError_t launch_snr_group64_m1(const LaunchArgs& a, const Group64& g);
 cudaError_t launch_snr_group64_m2(const LaunchArgs& a, const Group64& g);
+// FP32 SNR of a group (a.scratch holds g.nd slices of a.cap_events set-up records; g.scratch unused)
+cudaError_t launch_snr_group_f32_m0(const LaunchArgs& a, const Group64& g);
+cudaError_t launch_snr_group_f32_m1(const LaunchArgs& a, const Group64& g);
+cudaError_t launch_snr_group_f32_m2(const LaunchArgs& a, const Group64& g);
 size_t setup_stride_m0();
 size_t core_bytes_m0();
 size_t core_bytes_m1();

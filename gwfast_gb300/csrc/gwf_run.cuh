@@ -272,6 +272,62 @@ cudaError_t group_one(const LaunchArgs& a, GroupDev g) {
   return cudaSuccess;
 }
 
+// FP32 SNR of a group of detectors on one grid (the set-up as group_one: detector 0's FP64 and FP32
+// records, the others' projection only), then one launch over the group
+template <bool EARTH, bool TRI>
+cudaError_t snr_group_one_f32(const LaunchArgs& a, const Group64& G) {
+  if constexpr (M >= 3) {
+    return cudaErrorNotSupported;
+  } else {
+    const long long chunk = a.cap_events;
+    const size_t stride = rec_stride<M>() + f32_stride<M>();
+    GroupSNR32 g;
+    g.nd = G.nd;
+    g.slice = (long long)(chunk * stride);
+    for (int d = 0; d < G.nd; ++d) {
+      g.det[d] = G.det[d];
+      g.out_arm[d] = G.out_arm[d];
+      g.sr[d] = G.det[0].psd_scale / G.det[d].psd_scale;
+      g.same_psd[d] = G.same_psd[d];
+    }
+    for (long long n0 = 0; n0 < a.ev.N; n0 += chunk) {
+      EvBatch ev = a.ev;
+      ev.n0 = n0;
+      const long long cnt = (a.ev.N - n0) < chunk ? (a.ev.N - n0) : chunk;
+      const int epw = ev_lanes(cnt);
+      const unsigned nb = ev_blocks(cnt, epw);
+      for (int d = 0; d < G.nd; ++d) {
+        unsigned char* sc = a.scratch + (size_t)d * chunk * stride;
+        unsigned char* s32 = sc + (size_t)chunk * rec_stride<M>();
+        const int narm = G.det[d].shape == 1 ? 2 : 1;
+        if (d > 0) {
+          proj_f32_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(ev, G.det[d], s32, cnt, narm, G.det[d].earth, epw);
+          continue;
+        }
+        setup_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(ev, G.det[0], a.wf, a.qnm, a.nq, sc, cnt, a.core, a.core_mode,
+                                                       nullptr, epw);
+        if (a.core_done && a.core_mode == 1) {
+          const cudaError_t e = cudaEventRecord(a.core_done, a.stream);
+          if (e != cudaSuccess) return e;
+        }
+        setup_f32_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(G.det[0], sc, s32, cnt, narm, G.det[0].earth, epw);
+      }
+      snr_group_kernel_f32<M, EARTH, TRI><<<(unsigned)cnt, kThreads, 0, a.stream>>>(
+          ev, g, a.scratch + (size_t)chunk * rec_stride<M>(), a.out_det, a.accum);
+      const cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
+}
+
+cudaError_t snr_group_f32_dispatch(const LaunchArgs& a, const Group64& G) {
+  bool tri = false;
+  for (int d = 0; d < G.nd; ++d) tri |= G.det[d].shape == 1;
+  if (tri) return a.det.earth ? snr_group_one_f32<true, true>(a, G) : snr_group_one_f32<false, true>(a, G);
+  return a.det.earth ? snr_group_one_f32<true, false>(a, G) : snr_group_one_f32<false, false>(a, G);
+}
+
 cudaError_t group_dispatch(const LaunchArgs& a, const GroupDev& g) {
   if constexpr (M >= 3) return cudaErrorNotSupported;
   else {

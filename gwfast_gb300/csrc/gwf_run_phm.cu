@@ -12,5 +12,6 @@ cudaError_t launch_wave_m2(const LaunchArgs& a, const WaveOut& o) { return wave_
 cudaError_t launch_group_m2(const LaunchArgs& a, const GroupDev& g) { return group_dispatch(a, g); }
 cudaError_t launch_group64_m2(const LaunchArgs& a, const Group64& g) { return group64_dispatch(a, g); }
 cudaError_t launch_snr_group64_m2(const LaunchArgs& a, const Group64& g) { return snr_group64_dispatch(a, g); }
+cudaError_t launch_snr_group_f32_m2(const LaunchArgs& a, const Group64& g) { return snr_group_f32_dispatch(a, g); }
 
 }  // namespace gwf

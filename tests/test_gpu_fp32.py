@@ -317,22 +317,24 @@ def test_fp64_detector_groups(gpu_lib, model, dets, maker):
     ('IMRPhenomD', (('L1', 10.), ('ETS', 5.), ('H1', 10.))),
     ('IMRPhenomD', (('ETS', 10.), ('L1', 10.), ('Virgo', 10.))),
     ('IMRPhenomHM', synthetic.NETWORK_ET_CE)])
-def test_fp64_snr_groups(gpu_lib, model, dets):
-    """FP64 SNRs with the detectors that share the grid in one launch (the waveform value once per point)
-    against one launch per detector, every arm and the network: the same sums in another order. The
-    first network launches its L1 + H1 group before the triangle between them, so the per-arm slots
-    are checked against the detectors' order."""
+@pytest.mark.parametrize('precision,tol', [('fp64', 1e-12), ('fp32', 1e-6)])
+def test_snr_groups(gpu_lib, model, dets, precision, tol):
+    """SNRs with the detectors that share the grid in one launch (the waveform value once per point)
+    against one launch per detector, every arm and the network (FP64: the same sums in another order;
+    FP32: the same Kahan sums, each detector's scale formed from detector 0's). The first network
+    launches its L1 + H1 group before the triangle between them, so the per-arm slots are checked
+    against the detectors' order."""
     from gwfast_gb300 import _lib
     ev = synthetic.bbh_events(64, seed=19)
     net = synthetic.make_network(getattr(W, model)(), dets=dets, earth=True)
     ctx = _lib.context(0)
     try:
         ctx.set_detector_groups(False)
-        s1 = net.SNR(dict(ev), res=600, return_all=True)
+        s1 = net.SNR(dict(ev), res=600, return_all=True, precision=precision)
         ctx.set_detector_groups(True)
-        sg = net.SNR(dict(ev), res=600, return_all=True)
+        sg = net.SNR(dict(ev), res=600, return_all=True, precision=precision)
     finally:
         ctx.set_detector_groups(True)
     worst = max(np.max(np.abs(np.asarray(sg[k]) - np.asarray(s1[k])) / np.asarray(s1[k])) for k in s1)
-    print('%s FP64 SNR groups vs per detector (%s): max rel diff %.2e' % (model, ', '.join(s1), worst))
-    assert worst < 1e-12
+    print('%s %s SNR groups vs per detector (%s): max rel diff %.2e' % (model, precision, ', '.join(s1), worst))
+    assert worst < tol
