@@ -728,9 +728,10 @@ def main():
         'snr_per_s_fp32': world * N / (ms_snr32 / 1e3),
         # first pass: 2 set-up + 2 FP32-record launches (L1, ETS), H1's projection launch, the L1+H1
         # group kernel, the ET kernel and the join of the two groups' totals; the condition estimate
-        # and selection; with refined events: gather, 3 x (set-up record copy, segment scan, segmented
-        # FP64 kernel, reduction), H1's projection patch, sum-scatter
-        'gpu_launches': 8 + 2 + (15 if refined > 0 else 0),
+        # and selection; with refined events: gather; L1 + H1 as one FP64 group (2 set-up record
+        # copies, H1's projection patch, segment scan, segmented group kernel, reduction); ETS (record
+        # copy, segment scan, segmented FP64 kernel, reduction); sum-scatter
+        'gpu_launches': 8 + 2 + (12 if refined > 0 else 0),
         'e2e': {'value': world * N / e2e_s, 'unit': 'Fisher/s', 'h2d_bytes_per_step': int(p_host.nbytes),
                 'd2h_bytes_per_step': int(F_host.nbytes),
                 'ms_per_step_each': [round(1e3 * t, 3) for t in e2e_iter],
