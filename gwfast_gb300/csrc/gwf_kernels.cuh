@@ -595,6 +595,24 @@ __device__ __forceinline__ const PhaseBasis* rec_basis(const unsigned char* scra
   return reinterpret_cast<const PhaseBasis*>(scratch + i * rec_stride<MODEL>() + sizeof(SetupHdr) + wave_bytes<MODEL>());
 }
 
+// copy N 8-byte words, 32 at a time: every load of a batch is issued before any of its stores. The
+// source and destination are different records, but the compiler cannot tell, so a plain loop
+// waits for each load in turn (one L2 round trip per word).
+template <int N>
+__device__ __forceinline__ void copy_words(unsigned long long* dst, const unsigned long long* src) {
+  constexpr int B = 32;
+#pragma unroll 1
+  for (int w0 = 0; w0 < N; w0 += B) {
+    unsigned long long v[B];
+#pragma unroll
+    for (int k = 0; k < B; ++k)
+      if (w0 + k < N) v[k] = src[w0 + k];
+#pragma unroll
+    for (int k = 0; k < B; ++k)
+      if (w0 + k < N) dst[w0 + k] = v[k];
+  }
+}
+
 // core: optional per-call cache of the source-dependent model record, indexed by event (or by
 // core_idx[event] for a gathered batch); core_mode 1 computes the record and stores it there, 2 loads
 // it and recomputes only the detector-dependent part (the per-event set-up is FP64-bound, and a
@@ -625,7 +643,7 @@ __global__ void __launch_bounds__(kEvBlock) setup_kernel(EvBatch ev, DetDev det_
     unsigned long long* cw = core ? reinterpret_cast<unsigned long long*>(core + (size_t)crow * wave_bytes<MODEL>()) : nullptr;
     unsigned long long* ew = reinterpret_cast<unsigned long long*>(&E);
     if (core_mode == 2 && cw) {
-      for (int w = 0; w < nw; ++w) ew[w] = cw[w];
+      copy_words<nw>(ew, cw);
       if (MODEL == 1) phd_ref(E.phd, det.fmin);
       if (MODEL == 2) hm_ref(E.hm, det.fmin);
       if (MODEL == 4) nrt_ref(E.nrt, det.fmin);
@@ -637,7 +655,7 @@ __global__ void __launch_bounds__(kEvBlock) setup_kernel(EvBatch ev, DetDev det_
         for (int mode = 0; mode < 6; ++mode)
           hm_setup_mode(E.hm, mode, D4::seed(eta, P_ETA), D4::seed(c1, P_CHI1), D4::seed(c2, P_CHI2), io);
       if (core_mode == 1 && cw)
-        for (int w = 0; w < nw; ++w) cw[w] = ew[w];
+        copy_words<nw>(cw, ew);
     }
     PhaseBasis* pb = reinterpret_cast<PhaseBasis*>(rec + sizeof(SetupHdr) + wave_bytes<MODEL>());
     if (MODEL == 0) tf2_phase_basis(E.tf2, *pb);

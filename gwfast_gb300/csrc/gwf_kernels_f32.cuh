@@ -178,15 +178,28 @@ struct PBF {
   float u1, u0, k4, mg, fmrd;
 };
 
+// (the 22 basis duals are read 11 at a time, every load of a batch before any store: see round_struct)
 __device__ inline void pbf_fill(const PhaseBasis& src, PBF& b, double alpha) {
   auto tan = [&](const D4& d, int q) { return q == P_CHI1 ? d.d[P_CHI1] - alpha * d.d[P_CHI2] : d.d[q]; };
-  for (int i = 0; i < 22 * 4; ++i) {
-    const int c = i >> 2, q = i & 3;
-    const D4& d = c < 13 ? src.ins[c] : (c < 17 ? src.itm[c - 13] : src.mrd[c - 17]);
-    const double v = tan(d, q);
-    const float h = (float)v;
-    b.hi[c][q] = h;
-    b.lo[c][q] = (float)(v - (double)h);
+  static_assert(offsetof(PhaseBasis, itm) == 13 * sizeof(D4) && offsetof(PhaseBasis, mrd) == 17 * sizeof(D4),
+                "the basis duals are one array");
+  const D4* bas = src.ins;
+#pragma unroll 1
+  for (int c0 = 0; c0 < 22; c0 += 11) {
+    double t[11][4];
+#pragma unroll
+    for (int k = 0; k < 11; ++k)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) t[k][q] = bas[c0 + k].d[q];
+#pragma unroll
+    for (int k = 0; k < 11; ++k)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const double v = q == P_CHI1 ? t[k][P_CHI1] - alpha * t[k][P_CHI2] : t[k][q];
+        const float h = (float)v;
+        b.hi[c0 + k][q] = h;
+        b.lo[c0 + k][q] = (float)(v - (double)h);
+      }
   }
   for (int q = 0; q < 4; ++q) {
     b.du1[q] = (float)tan(src.U1, q);
@@ -272,10 +285,24 @@ __device__ inline void round_struct(const SRC& s, DST& d, const D4* amp_member, 
   float* b = reinterpret_cast<float*>(&d);
   const int lo = (int)(reinterpret_cast<const double*>(amp_member) - a);
   const double inv = 1.0 / amp;
-  for (int i = 0; i < (int)(sizeof(DST) / sizeof(float)); ++i) {
-    double v = a[i];
-    if (i % 5 == 1 + P_CHI1) v -= alpha * a[i + 1];
-    b[i] = (float)((i >= lo && i < lo + 5) ? v * inv : v);
+  // five duals at a time, every load of a batch issued before any of its stores: the two records
+  // do not overlap, but the compiler cannot tell, and a plain loop waits for each load in turn
+  constexpr int n = (int)(sizeof(DST) / sizeof(float)), B = 25;
+#pragma unroll 1
+  for (int i0 = 0; i0 < n; i0 += B) {
+    double v[B];
+#pragma unroll
+    for (int k = 0; k < B; ++k)
+      if (i0 + k < n) v[k] = a[i0 + k];
+#pragma unroll
+    for (int k = 0; k < B; ++k) {
+      const int i = i0 + k;
+      if (i < n) {
+        double x = v[k];
+        if (k % 5 == 1 + P_CHI1) x -= alpha * v[k + 1];   // i0 is a multiple of 5: i % 5 == k % 5
+        b[i] = (float)((i >= lo && i < lo + 5) ? x * inv : x);
+      }
+    }
   }
 }
 
@@ -569,6 +596,24 @@ __device__ inline DF4 to_df4(const D4& d, double alpha, double scale) {
 
 constexpr int kHMModeDuals = 20;   // leading dual members of HMModeT (rho ... hi4)
 
+// src[0..n) -> FP32 duals f32[] and FP64 values f64[], dual `scaled` multiplied by scale; five duals at
+// a time, every load of a batch before any store (see round_struct)
+__device__ inline void conv_duals(const D4* src, DF4* f32, double* f64, int n, double alpha, int scaled, double scale) {
+#pragma unroll 1
+  for (int i0 = 0; i0 < n; i0 += 5) {
+    D4 t[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+      if (i0 + k < n) t[k] = src[i0 + k];
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+      if (i0 + k < n) {
+        f32[i0 + k] = to_df4(t[k], alpha, i0 + k == scaled ? scale : 1.0);
+        f64[i0 + k] = t[k].v;
+      }
+  }
+}
+
 __device__ inline void hm_round(const HMEv& s, HMF32& d, double amp, double alpha) {
   static_assert(sizeof(PhdCoreT<D4>) % sizeof(D4) == 0, "core holds only duals");
   static_assert(sizeof(PhdCoreT<D4>) / sizeof(D4) == sizeof(PhdCoreT<DF4>) / sizeof(DF4) &&
@@ -581,10 +626,7 @@ __device__ inline void hm_round(const HMEv& s, HMF32& d, double amp, double alph
   DF4* b = reinterpret_cast<DF4*>(&d.e32.k);
   double* c = reinterpret_cast<double*>(&d.e64.k);
   const D4* ampm = &s.k.ampPref;
-  for (int i = 0; i < n; ++i) {
-    b[i] = to_df4(a[i], alpha, a + i == ampm ? 1.0 / amp : 1.0);
-    c[i] = a[i].v;
-  }
+  conv_duals(a, b, c, n, alpha, (int)(ampm - a), 1.0 / amp);
   d.e32.phi0 = to_df4(s.phi0, alpha, 1.0);
   d.e64.phi0 = s.phi0.v;
   for (int m = 0; m < 6; ++m) {
@@ -594,10 +636,7 @@ __device__ inline void hm_round(const HMEv& s, HMF32& d, double amp, double alph
     const D4* sa = reinterpret_cast<const D4*>(&sm);
     DF4* fa = reinterpret_cast<DF4*>(&fm);
     double* va = reinterpret_cast<double*>(&vm);
-    for (int i = 0; i < kHMModeDuals; ++i) {
-      fa[i] = to_df4(sa[i], alpha, 1.0);
-      va[i] = sa[i].v;
-    }
+    conv_duals(sa, fa, va, kHMModeDuals, alpha, -1, 1.0);
     fm.yp = vm.yp = sm.yp; fm.yc = vm.yc = sm.yc; fm.dyp = vm.dyp = sm.dyp; fm.dyc = vm.dyc = sm.dyc;
     fm.ysp = vm.ysp = sm.ysp; fm.ysm = vm.ysm = sm.ysm; fm.shift = vm.shift = sm.shift;
     fm.l = vm.l = sm.l; fm.m = vm.m = sm.m;
