@@ -277,6 +277,7 @@ gwf::DetDev dev_of(const DetRec& r) {
   d.psd_f32_lo = r.n > 0 ? (float)r.h_f.front() : 0.0f;
   d.psd_f32_hi = r.n > 0 ? (float)r.h_f.back() : 0.0f;
   d.psd_scale = r.scale;
+  gwf::det_trig(d);
   return d;
 }
 

@@ -73,7 +73,24 @@ struct DetDev {
   const float4* psd_seg;
   float psd_f32_lo, psd_f32_hi;   // first and last table frequency (FP32)
   double psd_scale;
+  // sines and cosines of the latitude, twice the latitude and twice the angle of each arm (the arms
+  // at xax and xax + 60 degrees), set on the host by det_trig: constants of the detector, which the
+  // per-event projection set-up would otherwise evaluate for every event
+  double sl, cl, s2l, c2l;
+  double s2g[2], c2g[2];
 };
+
+__host__ inline void det_trig(DetDev& d) {
+  d.sl = sin(d.lat);
+  d.cl = cos(d.lat);
+  d.s2l = sin(2.0 * d.lat);
+  d.c2l = cos(2.0 * d.lat);
+  for (int a = 0; a < 2; ++a) {
+    const double g = d.xax + a * (3.14159265358979323846 / 3.0);
+    d.s2g[a] = sin(2.0 * g);
+    d.c2g[a] = cos(2.0 * g);
+  }
+}
 
 struct EvBatch {
   const double* p;       // parameters, [11][ld] (Fisher order)
@@ -159,17 +176,15 @@ struct TimeState {
 __device__ __forceinline__ void proj_setup(ProjEv& pj, const DetDev& d, double theta, double phi, double iota,
                                            double psi, double tc, double dL) {
   const double dec = 0.5 * kPi - theta;
-  double sd, cdd, s2d, c2d, s2ps, c2ps, si, ci;
+  double sd, cdd, s2ps, c2ps, si, ci;
   sincos(dec, &sd, &cdd);
-  sincos(2.0 * dec, &s2d, &c2d);
+  const double s2d = 2.0 * sd * cdd, c2d = (cdd - sd) * (cdd + sd);   // (double angle)
   sincos(2.0 * psi, &s2ps, &c2ps);
   sincos(iota, &si, &ci);
   pj.c2p = c2ps; pj.s2p = s2ps;
   pj.cp = 0.5 * (1.0 + ci * ci); pj.ci = ci;
   pj.dcp = -ci * si; pj.dci = -si;
-  double sl, cl, s2l, c2l;
-  sincos(d.lat, &sl, &cl);
-  sincos(2.0 * d.lat, &s2l, &c2l);
+  const double sl = d.sl, cl = d.cl, s2l = d.s2l, c2l = d.c2l;
   // a = s2g*A1 + c2g*A2 ; b = c2g*B1 + s2g*B2 with
   // A1 = KA1[0] cos2x + KA1[1] cos x + KA1[2];  A2 = KA2[0] sin2x + KA2[1] sin x
   // B1 = KB1[0] cos2x + KB1[1] cos x;           B2 = KB2[0] sin2x + KB2[1] sin x
@@ -182,9 +197,9 @@ __device__ __forceinline__ void proj_setup(ProjEv& pj, const DetDev& d, double t
   pj.KB1[1] = cl * cdd;                            pj.dKB1[1] = -cl * sd;
   pj.KB2[0] = 0.25 * (3.0 - c2l) * sd;             pj.dKB2[0] = 0.25 * (3.0 - c2l) * cdd;
   pj.KB2[1] = 0.5 * s2l * cdd;                     pj.dKB2[1] = -0.5 * s2l * sd;
-  for (int a = 0; a < 2; ++a) {
-    const double g = d.xax + a * (kPi / 3.0);      // arms rotated by 0 and 60 degrees
-    sincos(2.0 * g, &pj.s2g[a], &pj.c2g[a]);
+  for (int a = 0; a < 2; ++a) {   // arms rotated by 0 and 60 degrees
+    pj.s2g[a] = d.s2g[a];
+    pj.c2g[a] = d.c2g[a];
   }
   pj.Rc = kREarth / kClight;
   pj.cdcl = cdd * cl; pj.sdsl = sd * sl; pj.sdcl = sd * cl; pj.cdsl = cdd * sl;

@@ -339,9 +339,10 @@ __device__ inline void tau_setup(TauF& t, const D4& Ms, const D4& vM, const D4& 
   t.lnv0 = (float)lnv0;
   t.lg0 = (float)(log(16.0) + 2.0 * lnv0);
   auto tan = [&](const D4& d, int q) { return q == P_CHI1 ? d.d[P_CHI1] - alpha * d.d[P_CHI2] : d.d[q]; };
+  const double ims = 1.0 / Ms.v, ieta = 1.0 / eta, ivm = 1.0 / vM.v;
   for (int q = 0; q < 4; ++q) {
-    t.dlnT0[q] = (float)(tan(Ms, q) / Ms.v - tan(eta_, q) / eta);
-    t.dlnv[q] = (float)(tan(vM, q) / vM.v);
+    t.dlnT0[q] = (float)(tan(Ms, q) * ims - tan(eta_, q) * ieta);
+    t.dlnv[q] = (float)(tan(vM, q) * ivm);
     t.deta[q] = (float)tan(eta_, q);
   }
 }

@@ -312,6 +312,25 @@ __device__ __forceinline__ D fit11(int k, const D& eta, const D& xi) {
                               + (c[8] + c[9] * eta + c[10] * e2) * xi * xi) * xi;
 }
 
+// The same fit on duals. It depends on the parameters only through eta and xi, so the value and
+// the two partial derivatives are formed in plain arithmetic and the N tangents by the chain rule
+// at the end: ~30 FP64 operations instead of ~110 of dual arithmetic. The per-event set-up is bound
+// by the FP64 pipe and evaluates 19 of these fits per event.
+template <class T, int N>
+__device__ __forceinline__ Dual<T, N> fit11(int k, const Dual<T, N>& eta, const Dual<T, N>& xi) {
+  const double* c = kFits[k];
+  const T e = eta.v, x = xi.v, e2 = e * e;
+  const T A = c[2] + c[3] * e + c[4] * e2, B = c[5] + c[6] * e + c[7] * e2, C = c[8] + c[9] * e + c[10] * e2;
+  Dual<T, N> r;
+  r.v = c[0] + c[1] * e + (A + B * x + C * x * x) * x;
+  // d/deta and d/dxi of c0 + c1 e + (A + B x + C x^2) x
+  const T fe = c[1] + ((c[3] + 2.0 * c[4] * e) + ((c[6] + 2.0 * c[7] * e) + (c[9] + 2.0 * c[10] * e) * x) * x) * x;
+  const T fx = A + (2.0 * B + 3.0 * C * x) * x;
+#pragma unroll
+  for (int q = 0; q < N; ++q) r.d[q] = fe * eta.d[q] + fx * xi.d[q];
+  return r;
+}
+
 // final spin (gwfast/waveforms.py:1256-1276) and radiated energy (:1278-1297)
 template <class D>
 __device__ inline D final_spin(const D& eta, const D& chi1, const D& chi2) {

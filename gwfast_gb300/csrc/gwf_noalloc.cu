@@ -220,6 +220,7 @@ extern "C" int gwf_fisher_noalloc(const gwf_det_desc* det, const double* psd_f, 
   a.det.psd_seg = nullptr;
   a.det.psd_f32_lo = a.det.psd_f32_hi = 0.0f;
   a.det.psd_scale = 1.0;
+  gwf::det_trig(a.det);
   a.wf.model = wf->model;
   a.wf.spin_ho = wf->spin_ho;
   a.wf.fcut_par = wf->fcut_par;
