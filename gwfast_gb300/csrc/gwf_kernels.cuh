@@ -666,9 +666,12 @@ __global__ void __launch_bounds__(kEvBlock) setup_kernel(EvBatch ev, DetDev det_
       if (MODEL == 7) nsbh_ref(E.nsbh, det.fmin, h.g.fcut);
     } else {
       event_setup<MODEL>(E, det, wf, qnm, nq, Mc, eta, c1, c2, dL, lt, dlt, ecc, h.g.fcut);
-      if (MODEL == 2)
-        for (int mode = 0; mode < 6; ++mode)
-          hm_setup_mode(E.hm, mode, D4::seed(eta, P_ETA), D4::seed(c1, P_CHI1), D4::seed(c2, P_CHI2), io);
+      if (MODEL == 2) {
+        const D4 et = D4::seed(eta, P_ETA), k1 = D4::seed(c1, P_CHI1), k2 = D4::seed(c2, P_CHI2);
+        const D4 af = final_spin(et, k1, k2);
+        const D4 finmass = 1.0 - radiated_energy(et, k1, k2);
+        for (int mode = 0; mode < 6; ++mode) hm_setup_mode(E.hm, mode, et, k1, k2, io, af, finmass);
+      }
       if (core_mode == 1 && cw)
         copy_words<nw>(cw, ew);
     }

@@ -24,6 +24,7 @@
 #include <type_traits>
 
 #include "gwf_kernels.cuh"
+#include "gwf_f32conv.cuh"
 
 namespace gwf {
 
@@ -53,17 +54,18 @@ struct TimeF { float D, D_th, D_ph, D_t, sx, cx; };
 struct ArmF { float Fp, Fc, Fp_x, Fc_x, Fp_d, Fc_d, Fp_s, Fc_s; };
 struct GridF { float lnfmin, delta, fac_w, w0, wl, fmin, fcut, df, acc_l0, acc_idl; int R; };
 
+// (the FP32 copies by f32_rn: the same values as casts, off the FP64 pipe)
 __device__ inline void projf_setup(ProjF& q, const ProjEv& p, double sz) {
-  q.c2p = (float)p.c2p; q.s2p = (float)p.s2p; q.cp = (float)p.cp; q.ci = (float)p.ci;
-  q.dcp = (float)p.dcp; q.dci = (float)p.dci;
-  for (int i = 0; i < 3; ++i) { q.KA1[i] = (float)p.KA1[i]; q.dKA1[i] = (float)p.dKA1[i]; }
+  q.c2p = f32_rn(p.c2p); q.s2p = f32_rn(p.s2p); q.cp = f32_rn(p.cp); q.ci = f32_rn(p.ci);
+  q.dcp = f32_rn(p.dcp); q.dci = f32_rn(p.dci);
+  for (int i = 0; i < 3; ++i) { q.KA1[i] = f32_rn(p.KA1[i]); q.dKA1[i] = f32_rn(p.dKA1[i]); }
   for (int i = 0; i < 2; ++i) {
-    q.KA2[i] = (float)p.KA2[i]; q.dKA2[i] = (float)p.dKA2[i];
-    q.KB1[i] = (float)p.KB1[i]; q.dKB1[i] = (float)p.dKB1[i];
-    q.KB2[i] = (float)p.KB2[i]; q.dKB2[i] = (float)p.dKB2[i];
-    q.s2g[i] = (float)p.s2g[i]; q.c2g[i] = (float)p.c2g[i];
+    q.KA2[i] = f32_rn(p.KA2[i]); q.dKA2[i] = f32_rn(p.dKA2[i]);
+    q.KB1[i] = f32_rn(p.KB1[i]); q.dKB1[i] = f32_rn(p.dKB1[i]);
+    q.KB2[i] = f32_rn(p.KB2[i]); q.dKB2[i] = f32_rn(p.dKB2[i]);
+    q.s2g[i] = f32_rn(p.s2g[i]); q.c2g[i] = f32_rn(p.c2g[i]);
   }
-  q.Rc = (float)p.Rc; q.cdcl = (float)p.cdcl; q.sdsl = (float)p.sdsl; q.sdcl = (float)p.sdcl; q.cdsl = (float)p.cdsl;
+  q.Rc = f32_rn(p.Rc); q.cdcl = f32_rn(p.cdcl); q.sdsl = f32_rn(p.sdsl); q.sdcl = f32_rn(p.sdcl); q.cdsl = f32_rn(p.cdsl);
   double s, c;
   sincos(p.u0 + kTwoPi * p.tc, &s, &c);
   q.sU0 = (float)s; q.cU0 = (float)c;
@@ -196,9 +198,7 @@ __device__ inline void pbf_fill(const PhaseBasis& src, PBF& b, double alpha) {
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const double v = q == P_CHI1 ? t[k][P_CHI1] - alpha * t[k][P_CHI2] : t[k][q];
-        const float h = (float)v;
-        b.hi[c0 + k][q] = h;
-        b.lo[c0 + k][q] = (float)(v - (double)h);
+        f32_split(v, b.hi[c0 + k][q], b.lo[c0 + k][q]);
       }
   }
   for (int q = 0; q < 4; ++q) {
@@ -300,7 +300,7 @@ __device__ inline void round_struct(const SRC& s, DST& d, const D4* amp_member, 
       if (i < n) {
         double x = v[k];
         if (k % 5 == 1 + P_CHI1) x -= alpha * v[k + 1];   // i0 is a multiple of 5: i % 5 == k % 5
-        b[i] = (float)((i >= lo && i < lo + 5) ? x * inv : x);
+        b[i] = f32_rn((i >= lo && i < lo + 5) ? x * inv : x);
       }
     }
   }
@@ -586,11 +586,11 @@ struct NoRec {};
 // setup_f32_kernel) and value and tangents multiplied by scale
 __device__ inline DF4 to_df4(const D4& d, double alpha, double scale) {
   DF4 r;
-  r.v = (float)(d.v * scale);
+  r.v = f32_rn(d.v * scale);
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const double t = q == P_CHI1 ? d.d[P_CHI1] - alpha * d.d[P_CHI2] : d.d[q];
-    r.d[q] = (float)(t * scale);
+    r.d[q] = f32_rn(t * scale);
   }
   return r;
 }

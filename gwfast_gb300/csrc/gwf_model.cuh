@@ -588,7 +588,7 @@ __device__ inline void phd_setup(PhdEv& e, const D4& Mc, const D4& eta, const D4
   phenom_core_setup(k, Mc, eta, chi1, chi2, fr, fd);
   phd_ref(e, fmin_hz);
   // 2 sqrt(5/(64 pi)) M G/c^2[Gpc] M G/c^3 / dL * sqrt(2 eta/3) pi^(-1/6)  (gwfast/waveforms.py:1204, :1248)
-  const D4 M = Mc / dpowc(eta, 0.6);
+  const D4 M = k.MG * (1.0 / kG3);   // total mass Mc / eta^(3/5) (MG = M G/c^3)
   k.ampPref = (2.0 * sqrt(5.0 / (64.0 * kPi)) * kG2Gpc * kG3 / dL * pow(kPi, -1.0 / 6.0)) * M * M * dsqrt(eta * (2.0 / 3.0));
 }
 
@@ -670,7 +670,8 @@ __device__ inline void phd_phase_basis(const PhdCore& k, PhaseBasis& b) {
   const D4 pm13_2 = pm13 * pm13;
   const PNC& c = k.pn;
   const D4 lin = k.t0 * k.fRef - k.phiRef;           // constant part of -t0 (Mf - MfRef) - phiRef
-  const D4 m13 = dexp(dlog(MG) * (1.0 / 3.0));
+  const D4 m13 = pm13 * 0.68278406325529573;          // MG^(1/3) = (pi MG)^(1/3) / pi^(1/3)
+  const D4 lmg = lpm - 1.1447298858494002;            // ln MG = ln(pi MG) - ln pi
   // inspiral (gwfast/waveforms.py:1145)
   b.ins[0] = c.A * pm_53;
   b.ins[1] = c.A * c.c2 * pm_53 * pm13_2;
@@ -689,7 +690,7 @@ __device__ inline void phd_phase_basis(const PhdCore& k, PhaseBasis& b) {
   b.itm[0] = (k.bet[0] / eta + k.C2Int - k.t0) * MG;
   b.itm[1] = -k.bet[2] / (3.0 * eta * MG * MG * MG);
   b.itm[2] = k.bet[1] / eta;
-  b.itm[3] = k.bet[1] / eta * dlog(MG) + k.C1Int + lin;
+  b.itm[3] = k.bet[1] / eta * lmg + k.C1Int + lin;
   // merger-ringdown: (-a2/x + 4/3 a3 x^3/4 + a1 x + a4 atan((x - a5 fring)/fdamp))/eta + C1MRD + C2MRD x
   const D4 m14 = dsqrt(dsqrt(MG));
   b.mrd[0] = -k.alp[1] / (eta * MG);
@@ -1257,20 +1258,20 @@ __device__ inline void hm_setup_core(HMEv& e, const D4& Mc, const D4& eta, const
   rd_fit(1, finmass, af, fr, fd);
   phenom_core_setup(k, Mc, eta, chi1, chi2, fr, fd);
   hm_ref(e, fmin_hz);
-  const D4 M = Mc / dpowc(eta, 0.6);
+  const D4 M = k.MG * (1.0 / kG3);   // total mass Mc / eta^(3/5) (MG = M G/c^3)
   // M G/c^2[Gpc] M G/c^3 / dL * sqrt(2 eta/3) pi^(-1/6)   (gwfast/waveforms.py:2444, :2489)
   k.ampPref = (kG2Gpc * kG3 / dL * pow(kPi, -1.0 / 6.0)) * M * M * dsqrt(eta * (2.0 / 3.0));
 }
 
-__device__ inline void hm_setup_mode(HMEv& e, int mode, const D4& eta, const D4& chi1, const D4& chi2, double iota) {
+// af, finmass: the remnant's spin and mass (final_spin, 1 - radiated_energy), the same for every mode
+__device__ inline void hm_setup_mode(HMEv& e, int mode, const D4& eta, const D4& chi1, const D4& chi2, double iota,
+                                     const D4& af, const D4& finmass) {
   PhdCore& k = e.k;
   HMMode& md = e.md[mode];
   const int l = kModeL[mode], m = kModeM[mode];
   md.l = l; md.m = m;
   const double shifts[5] = {0.0, 0.5 * kPi, 0.0, -0.5 * kPi, kPi};
   md.shift = shifts[m];
-  const D4 af = final_spin(eta, chi1, chi2);
-  const D4 finmass = 1.0 - radiated_energy(eta, chi1, chi2);
   D4 frlm, fdlm;
   rd_fit(mode, finmass, af, frlm, fdlm);
   md.frlm = frlm;

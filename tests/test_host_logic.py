@@ -292,3 +292,22 @@ def test_batch_files_roundtrip(tmp_path):
     none = dict(out, detected=np.zeros(4, bool), fisher=None)
     pipeline.batch_to_file(none, 0, str(tmp_path))
     assert set(pipeline.batch_from_file(str(tmp_path), 0, 4)) == {'snrs'}
+
+
+def test_f32_rounding_matches_casts(tmp_path):
+    """The integer FP64 -> FP32 rounding of the FP32 record set-up (gwfast_gb300/csrc/gwf_f32conv.cuh,
+    compiled here as host C++) gives the bit patterns of the casts it replaces on 12 M values: random
+    bit patterns, normal values across and beyond the FP32 range, round-to-nearest-even ties and
+    near-ties, mantissa carries into the exponent, and the special values."""
+    import shutil
+    import subprocess
+    gxx = shutil.which('g++')
+    if gxx is None:
+        pytest.skip('g++ not found')
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = str(tmp_path / 'f32conv_check')
+    subprocess.run([gxx, '-O2', '-std=c++17', '-I', os.path.join(root, 'gwfast_gb300', 'csrc'),
+                    os.path.join(root, 'tests', 'f32conv_check.cpp'), '-o', exe], check=True)
+    r = subprocess.run([exe, '4000000'], capture_output=True, text=True)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout
