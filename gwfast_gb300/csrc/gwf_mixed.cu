@@ -52,18 +52,14 @@ __global__ void __launch_bounds__(kEvBlock) cond_kernel(const double* __restrict
     }
   }
   double x[K], y[K];
-  // largest eigenvalue: power iteration on A = L L^T
+  // largest eigenvalue: power iteration on A = L L^T. The equilibrated matrix has trace 11, so
+  // |A x| <= 11 |x| and twelve steps from |x| ~ 3.5 stay far from overflow: the iterate is not
+  // renormalised (a square root, a division and 22 FP64 operations per step on the FP64-bound
+  // path); the Rayleigh quotient |L^T x|^2 / |x|^2 of the last iterate is the estimate
 #pragma unroll
   for (int i = 0; i < K; ++i) x[i] = 1.0 + 0.1 * i;
-  double lmax = 0.0;
 #pragma unroll 1
   for (int it = 0; it < 12; ++it) {
-    double nx = 0.0;
-#pragma unroll
-    for (int i = 0; i < K; ++i) nx += x[i] * x[i];
-    nx = 1.0 / sqrt(nx);
-#pragma unroll
-    for (int i = 0; i < K; ++i) x[i] *= nx;
 #pragma unroll
     for (int i = 0; i < K; ++i) {   // y = L^T x
       double s = 0.0;
@@ -71,29 +67,36 @@ __global__ void __launch_bounds__(kEvBlock) cond_kernel(const double* __restrict
       for (int k = i; k < K; ++k) s += L[T(k, i)] * x[k];
       y[i] = s;
     }
-    double q = 0.0;
+    if (it == 11) break;
 #pragma unroll
-    for (int i = 0; i < K; ++i) {   // x = L y, Rayleigh quotient |L^T x|^2
-      q += y[i] * y[i];
+    for (int i = 0; i < K; ++i) {   // x = L y
       double s = 0.0;
 #pragma unroll
       for (int k = 0; k <= i; ++k) s += L[T(i, k)] * y[k];
       x[i] = s;
     }
-    lmax = q;
   }
-  // smallest eigenvalue: inverse iteration, x <- A^{-1} x by forward and back substitution
+  double nx = 0.0, q = 0.0;
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    nx += x[i] * x[i];
+    q += y[i] * y[i];
+  }
+  const double lmax = q / nx;
+  // smallest eigenvalue: inverse iteration, x <- A^{-1} x by forward and back substitution; each
+  // step grows |x| by up to 1 / lambda_min, so the iterate is renormalised every other step
 #pragma unroll
   for (int i = 0; i < K; ++i) x[i] = (i & 1) ? -1.0 : 1.0 + 0.05 * i;
-  double lmin = INFINITY;
 #pragma unroll 1
   for (int it = 0; it < 8; ++it) {
-    double nx = 0.0;
+    if ((it & 1) == 0) {
+      double s2 = 0.0;
 #pragma unroll
-    for (int i = 0; i < K; ++i) nx += x[i] * x[i];
-    nx = 1.0 / sqrt(nx);
+      for (int i = 0; i < K; ++i) s2 += x[i] * x[i];
+      const double r = rsqrt(s2);
 #pragma unroll
-    for (int i = 0; i < K; ++i) x[i] *= nx;
+      for (int i = 0; i < K; ++i) x[i] *= r;
+    }
 #pragma unroll
     for (int i = 0; i < K; ++i) {   // L y = x
       double s = x[i];
@@ -101,9 +104,7 @@ __global__ void __launch_bounds__(kEvBlock) cond_kernel(const double* __restrict
       for (int k = 0; k < i; ++k) s -= L[T(i, k)] * y[k];
       y[i] = s * il[i];
     }
-    double q = 0.0;                 // x^T A^{-1} x = |y|^2
-#pragma unroll
-    for (int i = 0; i < K; ++i) q += y[i] * y[i];
+    if (it == 7) break;
 #pragma unroll
     for (int i = K - 1; i >= 0; --i) {   // L^T x = y
       double s = y[i];
@@ -111,8 +112,15 @@ __global__ void __launch_bounds__(kEvBlock) cond_kernel(const double* __restrict
       for (int k = i + 1; k < K; ++k) s -= L[T(k, i)] * x[k];
       x[i] = s * il[i];
     }
-    lmin = 1.0 / q;
   }
+  nx = 0.0;
+  q = 0.0;   // x^T A^{-1} x / |x|^2 = |y|^2 / |x|^2
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    nx += x[i] * x[i];
+    q += y[i] * y[i];
+  }
+  const double lmin = nx / q;
   cond[n] = lmax / lmin;
 }
 
