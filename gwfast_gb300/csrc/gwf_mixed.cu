@@ -11,8 +11,8 @@ namespace gwf {
 namespace {
 
 // Condition-number estimate of the diagonally equilibrated Fisher (the quantity fisherTools
-// reports), one thread per event: Cholesky factor, then power iteration for the largest
-// eigenvalue and inverse iteration (two triangular solves per step) for the smallest, each
+// reports), one thread per event: Cholesky factor, then inverse iteration (two triangular solves
+// per step, FP64) for the smallest eigenvalue and power iteration (FP32) for the largest, each
 // closed by a Rayleigh quotient. Not positive definite -> infinity. Far cheaper than the Jacobi
 // eigen-decomposition of the covariance kernel; only used to pick events for FP64, where a
 // factor of a few does not matter: the largest eigenvalue of an equilibrated 11 x 11 matrix lies
@@ -52,39 +52,8 @@ __global__ void __launch_bounds__(kEvBlock) cond_kernel(const double* __restrict
     }
   }
   double x[K], y[K];
-  // largest eigenvalue: power iteration on A = L L^T. The equilibrated matrix has trace 11, so
-  // |A x| <= 11 |x| and twelve steps from |x| ~ 3.5 stay far from overflow: the iterate is not
-  // renormalised (a square root, a division and 22 FP64 operations per step on the FP64-bound
-  // path); the Rayleigh quotient |L^T x|^2 / |x|^2 of the last iterate is the estimate
-#pragma unroll
-  for (int i = 0; i < K; ++i) x[i] = 1.0 + 0.1 * i;
-#pragma unroll 1
-  for (int it = 0; it < 12; ++it) {
-#pragma unroll
-    for (int i = 0; i < K; ++i) {   // y = L^T x
-      double s = 0.0;
-#pragma unroll
-      for (int k = i; k < K; ++k) s += L[T(k, i)] * x[k];
-      y[i] = s;
-    }
-    if (it == 11) break;
-#pragma unroll
-    for (int i = 0; i < K; ++i) {   // x = L y
-      double s = 0.0;
-#pragma unroll
-      for (int k = 0; k <= i; ++k) s += L[T(i, k)] * y[k];
-      x[i] = s;
-    }
-  }
-  double nx = 0.0, q = 0.0;
-#pragma unroll
-  for (int i = 0; i < K; ++i) {
-    nx += x[i] * x[i];
-    q += y[i] * y[i];
-  }
-  const double lmax = q / nx;
-  // smallest eigenvalue: inverse iteration, x <- A^{-1} x by forward and back substitution; each
-  // step grows |x| by up to 1 / lambda_min, so the iterate is renormalised every other step
+  // smallest eigenvalue: inverse iteration in FP64, x <- A^{-1} x by forward and back substitution;
+  // each step grows |x| by up to 1 / lambda_min, so the iterate is renormalised every other step
 #pragma unroll
   for (int i = 0; i < K; ++i) x[i] = (i & 1) ? -1.0 : 1.0 + 0.05 * i;
 #pragma unroll 1
@@ -113,14 +82,48 @@ __global__ void __launch_bounds__(kEvBlock) cond_kernel(const double* __restrict
       x[i] = s * il[i];
     }
   }
-  nx = 0.0;
-  q = 0.0;   // x^T A^{-1} x / |x|^2 = |y|^2 / |x|^2
+  double nx = 0.0, q = 0.0;   // x^T A^{-1} x / |x|^2 = |y|^2 / |x|^2
 #pragma unroll
   for (int i = 0; i < K; ++i) {
     nx += x[i] * x[i];
     q += y[i] * y[i];
   }
   const double lmin = nx / q;
+  // largest eigenvalue: power iteration on A = L L^T in FP32 (on the FP32 pipe; the FP64 pipe sets
+  // this kernel's time). lambda_max lies in [1, 11] and is only needed to a few per cent; rounding L
+  // to FP32 moves it by ~1e-7 relative. |A x| <= 11 |x|, so twelve steps from |x| ~ 3.5 stay below
+  // 1e13 without renormalisation; the Rayleigh quotient |L^T x|^2 / |x|^2 of the last iterate is
+  // the estimate.
+  float Lf[K * (K + 1) / 2], xf[K], yf[K];
+#pragma unroll
+  for (int i = 0; i < K * (K + 1) / 2; ++i) Lf[i] = f32_rn(L[i]);   // (integer rounding, off the FP64 pipe)
+#pragma unroll
+  for (int i = 0; i < K; ++i) xf[i] = 1.0f + 0.1f * i;
+#pragma unroll 1
+  for (int it = 0; it < 12; ++it) {
+#pragma unroll
+    for (int i = 0; i < K; ++i) {   // y = L^T x
+      float s = 0.0f;
+#pragma unroll
+      for (int k = i; k < K; ++k) s = fmaf(Lf[T(k, i)], xf[k], s);
+      yf[i] = s;
+    }
+    if (it == 11) break;
+#pragma unroll
+    for (int i = 0; i < K; ++i) {   // x = L y
+      float s = 0.0f;
+#pragma unroll
+      for (int k = 0; k <= i; ++k) s = fmaf(Lf[T(i, k)], yf[k], s);
+      xf[i] = s;
+    }
+  }
+  float nxf = 0.0f, qf = 0.0f;
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    nxf = fmaf(xf[i], xf[i], nxf);
+    qf = fmaf(yf[i], yf[i], qf);
+  }
+  const double lmax = (double)qf / (double)nxf;
   cond[n] = lmax / lmin;
 }
 
