@@ -54,8 +54,10 @@ cudaError_t chunked(const LaunchArgs& a, bool f32, MAIN main) {
       if (er != cudaSuccess) return er;
     }
     if constexpr (M < 3) {   // (the tidal models have no FP32 form)
-      if (f32) setup_f32_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(a.det, a.scratch, scratch32_of(a), cnt,
-                                                                  a.det.shape == 1 ? 2 : 1, a.det.earth, epw);
+      const int repw = ev_lanes(cnt, kRecWarpsPerSM);
+      if (f32)
+        setup_f32_kernel<M><<<ev_blocks(cnt, repw), kEvBlock, 0, a.stream>>>(a.det, a.scratch, scratch32_of(a), cnt,
+                                                                             a.det.shape == 1 ? 2 : 1, a.det.earth, repw);
     }
     if (a.timer) {
       const cudaError_t et = a.timer->end(a.stream);
@@ -256,8 +258,9 @@ cudaError_t group_one(const LaunchArgs& a, GroupDev g) {
         err = cudaEventRecord(a.core_done, a.stream);
         if (err != cudaSuccess) return err;
       }
-      setup_f32_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(g.det[d], sc, s32, cnt, g.det[d].shape == 1 ? 2 : 1,
-                                                         g.det[d].earth, epw);
+      const int repw = ev_lanes(cnt, kRecWarpsPerSM);
+      setup_f32_kernel<M><<<ev_blocks(cnt, repw), kEvBlock, 0, a.stream>>>(g.det[d], sc, s32, cnt,
+                                                                           g.det[d].shape == 1 ? 2 : 1, g.det[d].earth, repw);
     }
     if (a.timer) {
       err = a.timer->end(a.stream);
@@ -310,7 +313,9 @@ cudaError_t snr_group_one_f32(const LaunchArgs& a, const Group64& G) {
           const cudaError_t e = cudaEventRecord(a.core_done, a.stream);
           if (e != cudaSuccess) return e;
         }
-        setup_f32_kernel<M><<<nb, kEvBlock, 0, a.stream>>>(G.det[0], sc, s32, cnt, narm, G.det[0].earth, epw);
+        const int repw = ev_lanes(cnt, kRecWarpsPerSM);
+        setup_f32_kernel<M><<<ev_blocks(cnt, repw), kEvBlock, 0, a.stream>>>(G.det[0], sc, s32, cnt, narm, G.det[0].earth,
+                                                                             repw);
       }
       snr_group_kernel_f32<M, EARTH, TRI><<<(unsigned)cnt, kThreads, 0, a.stream>>>(
           ev, g, a.scratch + (size_t)chunk * rec_stride<M>(), a.out_det, a.accum);
