@@ -47,7 +47,10 @@ GWF_CONV_HD float f32_rn(double v) {
   const uint64_t u = conv_bits(v);
   const uint32_t hi = (uint32_t)(u >> 32), lo = (uint32_t)u;
   const uint32_t e = (hi >> 20) & 0x7FFu;
-  if (e - 897u > 253u) return (float)v;   // e outside [897, 1150] (e < 897 wraps round)
+  if (e - 897u > 253u) {   // e outside [897, 1150] (e < 897 wraps round)
+    if (((hi & 0x7FFFFFFFu) | lo) == 0u) return conv_float(hi);   // +-0
+    return (float)v;
+  }
   // exponent and the top 23 mantissa bits, rebased from bias 1023 to 127; 29 bits dropped
   uint32_t f = ((((hi & 0x7FFFFFFFu) << 3) | (lo >> 29)) - (896u << 23));
   const uint32_t r = lo & 0x1FFFFFFFu;
@@ -66,6 +69,11 @@ GWF_CONV_HD void f32_split(double v, float& h, float& l) {
   const uint32_t e = (hi >> 20) & 0x7FFu;
   // e - 52 - 1023 + 127 >= 1 keeps 2^(E - 52) a normal float; e <= 1149 keeps h finite
   if (e - 949u > 200u) {
+    if (((hi & 0x7FFFFFFFu) | lo) == 0u) {   // +-0: (+-0, +0)
+      h = conv_float(hi);
+      l = 0.0f;
+      return;
+    }
     h = (float)v;
     l = (float)(v - (double)h);
     return;

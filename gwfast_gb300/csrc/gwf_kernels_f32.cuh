@@ -296,13 +296,20 @@ __device__ inline void round_struct(const SRC& s, DST& d, const D4* amp_member, 
       if (i0 + k < n) v[k] = a[i0 + k];
 #pragma unroll
     for (int k = 0; k < B; ++k) {
-      const int i = i0 + k;
-      if (i < n) {
+      if (i0 + k < n) {
         double x = v[k];
         if (k % 5 == 1 + P_CHI1) x -= alpha * v[k + 1];   // i0 is a multiple of 5: i % 5 == k % 5
-        b[i] = f32_rn((i >= lo && i < lo + 5) ? x * inv : x);
+        b[i0 + k] = f32_rn(x);
       }
     }
+  }
+  // the amplitude dual again, divided by amp (a select inside the loop above would have made the
+  // compiler multiply every word)
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    double x = a[lo + k];
+    if (k == 1 + P_CHI1) x -= alpha * a[lo + k + 1];
+    b[lo + k] = f32_rn(x * inv);
   }
 }
 
@@ -609,10 +616,12 @@ __device__ inline void conv_duals(const D4* src, DF4* f32, double* f64, int n, d
 #pragma unroll
     for (int k = 0; k < 5; ++k)
       if (i0 + k < n) {
-        f32[i0 + k] = to_df4(t[k], alpha, i0 + k == scaled ? scale : 1.0);
+        f32[i0 + k] = to_df4(t[k], alpha, 1.0);
         f64[i0 + k] = t[k].v;
       }
   }
+  // the scaled dual again (a select of the scale inside the loop would multiply every word)
+  if (scaled >= 0 && scaled < n) f32[scaled] = to_df4(src[scaled], alpha, scale);
 }
 
 __device__ inline void hm_round(const HMEv& s, HMF32& d, double amp, double alpha) {
