@@ -426,10 +426,12 @@ __device__ __forceinline__ void tf2_any_point(const EvUnion& E, double f, double
 
 // waveform at one point: P, C (hp = P, hc = i C) with tangents, iota derivatives, and tau_star tangent.
 // phi0: the waveform phase left out of P and C (22-mode models: Phi(f); HM: 0, the mode phases are in P, C)
+// pb (TaylorF2 and IMRPhenomD, Fisher kernels): the event's phase basis; the phase tangent is then
+// the basis sum (phase_tangent_d) instead of the dual evaluation of the phase, and phi0 is not formed
 template <int MODEL, bool EARTH>
 __device__ __forceinline__ void wave_point_dual(const EvUnion& E, const ProjEv& pj, double f, double lnf,
                                                 cd& P, cd& C, cd* dP, cd* dC, cd& dPi, cd& dCi, DualOf<MODEL>& tau,
-                                                double& phi0) {
+                                                double& phi0, const PhaseBasis* pb = nullptr) {
   constexpr int NI = ndir_of<MODEL>();
   phi0 = 0.0;
   if constexpr (MODEL == 2) {
@@ -460,22 +462,40 @@ __device__ __forceinline__ void wave_point_dual(const EvUnion& E, const ProjEv& 
     dCi = {pj.dci * A.v, 0.0};
   } else {
     D4 A, Phi;
-    if (is_tf2<MODEL>()) {
-      const TF2Ev& t = tf2_base<MODEL>(E);
-      const double f13 = exp(lnf / 3.0);
-      tf2_any_point<MODEL, D4>(E, f, f13, lnf, A, Phi);
-      if (EARTH) tau = tau_star_point<D4>(t.Ms, t.vM, t.eta, f13);
+    double dphi[4];
+    bool basis = false;
+    if constexpr (MODEL == 0 || MODEL == 1) basis = pb != nullptr;
+    if (basis) {
+      if constexpr (MODEL == 0) {
+        const TF2Ev& t = E.tf2;
+        A = t.ampK * exp(lnf * (-7.0 / 6.0));
+        if (EARTH) tau = tau_star_point<D4>(t.Ms, t.vM, t.eta, exp(lnf / 3.0));
+      } else if constexpr (MODEL == 1) {
+        A = phd_amp_point<D4>(E.phd.k, f);
+        if (EARTH) tau = tau_star_point<D4>(E.phd.k.Ms, E.phd.k.vM, E.phd.k.eta, exp(lnf / 3.0));
+      }
+      phase_tangent_d(*pb, f, lnf, dphi);
+      phi0 = 0.0;
     } else {
-      phd_point<D4>(E.phd.k, f, A, Phi);
-      if (EARTH) tau = tau_star_point<D4>(E.phd.k.Ms, E.phd.k.vM, E.phd.k.eta, exp(lnf / 3.0));
+      if (is_tf2<MODEL>()) {
+        const TF2Ev& t = tf2_base<MODEL>(E);
+        const double f13 = exp(lnf / 3.0);
+        tf2_any_point<MODEL, D4>(E, f, f13, lnf, A, Phi);
+        if (EARTH) tau = tau_star_point<D4>(t.Ms, t.vM, t.eta, f13);
+      } else {
+        phd_point<D4>(E.phd.k, f, A, Phi);
+        if (EARTH) tau = tau_star_point<D4>(E.phd.k.Ms, E.phd.k.vM, E.phd.k.eta, exp(lnf / 3.0));
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) dphi[k] = Phi.d[k];
+      phi0 = Phi.v + (is_tf2<MODEL>() ? kTF2PhaseConst : 0.0);
     }
     // W = A e^{-i Phi} with the common phase dropped: value A, tangent dA - i A dPhi
-    phi0 = Phi.v + (is_tf2<MODEL>() ? kTF2PhaseConst : 0.0);
     P = {pj.cp * A.v, 0.0};
     C = {pj.ci * A.v, 0.0};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      const cd dW = {A.d[k], -A.v * Phi.d[k]};
+      const cd dW = {A.d[k], -A.v * dphi[k]};
       dP[k] = cscale(dW, pj.cp);
       dC[k] = cscale(dW, pj.ci);
     }
@@ -683,20 +703,27 @@ __global__ void __launch_bounds__(kEvBlock) setup_kernel(EvBatch ev, DetDev det_
 }
 
 // cooperative copy of one event record into shared memory (all pieces are multiples of 8 bytes)
+// (pb: also the phase basis that follows the model record, for TaylorF2 and IMRPhenomD)
 template <int MODEL>
-__device__ inline void block_load(EvUnion& E, ProjEv& pj, GridEv& g, const unsigned char* scratch, long long i) {
+__device__ inline void block_load(EvUnion& E, ProjEv& pj, GridEv& g, const unsigned char* scratch, long long i,
+                                  PhaseBasis* pb = nullptr) {
   const unsigned char* rec = scratch + i * rec_stride<MODEL>();
   const unsigned long long* src = reinterpret_cast<const unsigned long long*>(rec);
   unsigned long long* dg = reinterpret_cast<unsigned long long*>(&g);
   unsigned long long* dp = reinterpret_cast<unsigned long long*>(&pj);
   unsigned long long* de = reinterpret_cast<unsigned long long*>(&E);
+  unsigned long long* db = reinterpret_cast<unsigned long long*>(pb);
   constexpr int ng = sizeof(GridEv) / 8, np = sizeof(ProjEv) / 8, ne = wave_bytes<MODEL>() / 8;
+  constexpr int nb = basis_bytes<MODEL>() / 8;
   static_assert(sizeof(SetupHdr) == sizeof(GridEv) + sizeof(ProjEv), "packed header");
-  for (int w = threadIdx.x; w < ng + np + ne; w += blockDim.x) {
+  static_assert(basis_bytes<MODEL>() % 8 == 0, "basis in 8-byte words");
+  const int nw = ng + np + ne + (pb ? nb : 0);
+  for (int w = threadIdx.x; w < nw; w += blockDim.x) {
     const unsigned long long v = src[w];
     if (w < ng) dg[w] = v;
     else if (w < ng + np) dp[w - ng] = v;
-    else de[w - ng - np] = v;
+    else if (w < ng + np + ne) de[w - ng - np] = v;
+    else db[w - ng - np - ne] = v;
   }
   __syncthreads();
 }
@@ -789,6 +816,7 @@ __device__ void write_gram(const double* gsum, double scale, ColMix mix, long lo
 template <int NARM, int NG, int NPR = NP>
 struct F64State {
   EvUnion E;
+  PhaseBasis pb;   // TaylorF2 and IMRPhenomD: the phase tangent's basis
   ProjEv pj;
   GridEv g;
   ArmPat apc[NARM];
@@ -800,7 +828,7 @@ struct F64State {
 template <int MODEL, bool EARTH, int NARM, int NG>
 __device__ inline void f64_prepare(const DetDev& det, const unsigned char* scratch, long long rec,
                                    F64State<NARM, NG, np_of<MODEL>()>& S) {
-  block_load<MODEL>(S.E, S.pj, S.g, scratch, rec);
+  block_load<MODEL>(S.E, S.pj, S.g, scratch, rec, (MODEL == 0 || MODEL == 1) ? &S.pb : nullptr);
   if (!EARTH) {
     if (threadIdx.x == 0) {
       time_state(S.pj, S.pj.tc, S.tsc);
@@ -854,7 +882,8 @@ __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<N
       cd P, C, dP[NI], dC[NI], dPi, dCi;
       DualOf<MODEL> tau(0.0);
       double phi0;
-      wave_point_dual<MODEL, EARTH>(S.E, S.pj, f, lnf, P, C, dP, dC, dPi, dCi, tau, phi0);
+      wave_point_dual<MODEL, EARTH>(S.E, S.pj, f, lnf, P, C, dP, dC, dPi, dCi, tau, phi0,
+                                    (MODEL == 0 || MODEL == 1) ? &S.pb : nullptr);
       double dtn[NI];
 #pragma unroll
       for (int q = 0; q < NI; ++q) dtn[q] = 0.0;

@@ -1380,7 +1380,7 @@ struct F64GroupState {
 
 template <int MODEL, bool EARTH>
 __device__ inline void f64g_prepare(const GroupDev64& g, long long rec, F64GroupState<MODEL, EARTH>& G) {
-  block_load<MODEL>(G.S.E, G.S.pj, G.S.g, g.rec[0], rec);
+  block_load<MODEL>(G.S.E, G.S.pj, G.S.g, g.rec[0], rec, (MODEL == 0 || MODEL == 1) ? &G.S.pb : nullptr);
   if ((int)threadIdx.x < g.nd) {
     const int d = threadIdx.x;
     G.pj[d] = reinterpret_cast<const SetupHdr*>(g.rec[d] + rec * rec_stride<MODEL>())->pj;
@@ -1447,7 +1447,8 @@ __device__ inline void f64g_item(const EvBatch& ev, const GroupDev64& g, F64Grou
     for (int q = 0; q < NI; ++q) dtn[q] = 0.0;
     if (valid) {
       grid_point(G.S.g, ev.spacing, k, f, lnf, w);
-      wave_point_dual<MODEL, EARTH>(G.S.E, G.S.pj, f, lnf, P, C, dP, dC, dPi, dCi, tau, phi0);
+      wave_point_dual<MODEL, EARTH>(G.S.E, G.S.pj, f, lnf, P, C, dP, dC, dPi, dCi, tau, phi0,
+                                    (MODEL == 0 || MODEL == 1) ? &G.S.pb : nullptr);
       if (EARTH) {
 #pragma unroll
         for (int q = 0; q < NI; ++q) dtn[q] = -tau.d[q] / kDay;

@@ -705,6 +705,45 @@ __device__ inline void phd_phase_basis(const PhdCore& k, PhaseBasis& b) {
   b.pad = 0.0;
 }
 
+// d Phi / d(Mc, eta, chi1z, chi2z) at physical frequency f (Hz) from the basis, in FP64: the FP64
+// Fisher kernels' phase tangent for TaylorF2 and IMRPhenomD (a basis sum of at most 13 terms per
+// direction in place of the dual evaluation of the phase at every point). The region tests are those
+// of complete_phase, on MG f; beyond Mf = 0.2 the phase and its tangent are zero. In the
+// merger-ringdown term k4 atan(U1 f - U0) the argument depends on the parameters as well.
+__device__ __forceinline__ void phase_tangent_d(const PhaseBasis& b, double f, double lnf, double (&dphi)[4]) {
+  const double x = b.MG.v * f;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) dphi[q] = 0.0;
+  if (x < kPhiFJoin) {
+    const double f13 = cbrt(f), i13 = 1.0 / f13, i23 = i13 * i13;
+    // f^-5/3 f^-1 f^-2/3 f^-1/3 1 ln f f^1/3 f^1/3 ln f f^2/3 f f^4/3 f^5/3 f^2
+    const double bas[13] = {i23 * i23 * i13, i23 * i13, i23, i13, 1.0, lnf, f13, f13 * lnf, f13 * f13,
+                            f, f * f13, f * f13 * f13, f * f};
+#pragma unroll
+    for (int j = 0; j < 13; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dphi[q] = fma(b.ins[j].d[q], bas[j], dphi[q]);
+  } else if (x < b.fMRD) {
+    const double i1 = 1.0 / f;
+    const double bas[4] = {f, i1 * i1 * i1, lnf, 1.0};
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dphi[q] = fma(b.itm[j].d[q], bas[j], dphi[q]);
+  } else if (x < kMfCut) {
+    const double u = b.U1.v * f - b.U0.v;
+    const double f14 = sqrt(sqrt(f));
+    const double bas[5] = {1.0 / f, f14 * f14 * f14, f, 1.0, atan(u)};
+#pragma unroll
+    for (int j = 0; j < 5; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dphi[q] = fma(b.mrd[j].d[q], bas[j], dphi[q]);
+    const double kd = b.mrd[4].v / (1.0 + u * u);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) dphi[q] = fma(kd, fma(b.U1.d[q], f, -b.U0.d[q]), dphi[q]);
+  }
+}
+
 // ------------------------------------------------------------------ IMRPhenomD_NRTidalv2 (gwfast/waveforms.py:1339-1836)
 // IMRPhenomD with the spin-induced quadrupole (from the tidal deformabilities) in its 2PN and 3PN
 // spin-spin phase terms, the NRTidalv2 tidal phase (Pade approximant, arXiv:1905.06011 eq. 17), the

@@ -37,10 +37,14 @@ def test_compute_errs_fixed_params(gpu_lib):
                                params_fix=('psi', 'Phicoal'))
     assert fx['cov'].shape == (9, 9, 64)
     keep = [0, 1, 2, 3, 4, 5, 7, 9, 10]
-    F = full['fisher'][np.ix_(keep, keep)]
-    C = np.moveaxis(np.linalg.inv(np.moveaxis(F, -1, 0)), 0, -1)
+    # reference: numpy's inverse of the reduced Fisher with its diagonal scaled out first (the raw 9x9
+    # matrices reach condition numbers near 1e15, their equilibrated forms 1e11, and the unscaled
+    # inverse then differs from either by ~1e-6 from rounding alone)
+    F = np.moveaxis(full['fisher'][np.ix_(keep, keep)], -1, 0)
+    d = 1.0 / np.sqrt(np.einsum('nii->ni', F))
+    C = d[:, :, None] * np.linalg.inv(d[:, :, None] * F * d[:, None, :]) * d[:, None, :]
     ok = full['cond'] < 1e12
-    rel = np.abs(np.sqrt(np.einsum('iin->in', C)) - fx['errors']) / fx['errors']
+    rel = np.abs(np.sqrt(np.einsum('nii->in', C)) - fx['errors']) / fx['errors']
     assert np.max(rel[:, ok]) < 1e-6
 
 
