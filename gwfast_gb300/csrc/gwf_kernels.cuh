@@ -431,7 +431,7 @@ __device__ __forceinline__ void tf2_any_point(const EvUnion& E, double f, double
 template <int MODEL, bool EARTH>
 __device__ __forceinline__ void wave_point_dual(const EvUnion& E, const ProjEv& pj, double f, double lnf,
                                                 cd& P, cd& C, cd* dP, cd* dC, cd& dPi, cd& dCi, DualOf<MODEL>& tau,
-                                                double& phi0, const PhaseBasis* pb = nullptr) {
+                                                double& phi0, const PhaseBasis* pb = nullptr, const TauD* td = nullptr) {
   constexpr int NI = ndir_of<MODEL>();
   phi0 = 0.0;
   if constexpr (MODEL == 2) {
@@ -469,10 +469,12 @@ __device__ __forceinline__ void wave_point_dual(const EvUnion& E, const ProjEv& 
       if constexpr (MODEL == 0) {
         const TF2Ev& t = E.tf2;
         A = t.ampK * exp(lnf * (-7.0 / 6.0));
-        if (EARTH) tau = tau_star_point<D4>(t.Ms, t.vM, t.eta, exp(lnf / 3.0));
+        if (EARTH) tau = td ? tau_point_d(*td, exp(lnf / 3.0), lnf) : tau_star_point<D4>(t.Ms, t.vM, t.eta, exp(lnf / 3.0));
       } else if constexpr (MODEL == 1) {
         A = phd_amp_point<D4>(E.phd.k, f);
-        if (EARTH) tau = tau_star_point<D4>(E.phd.k.Ms, E.phd.k.vM, E.phd.k.eta, exp(lnf / 3.0));
+        if (EARTH)
+          tau = td ? tau_point_d(*td, exp(lnf / 3.0), lnf)
+                   : tau_star_point<D4>(E.phd.k.Ms, E.phd.k.vM, E.phd.k.eta, exp(lnf / 3.0));
       }
       phase_tangent_d(*pb, f, lnf, dphi);
       phi0 = 0.0;
@@ -817,6 +819,7 @@ template <int NARM, int NG, int NPR = NP>
 struct F64State {
   EvUnion E;
   PhaseBasis pb;   // TaylorF2 and IMRPhenomD: the phase tangent's basis
+  TauD td;         // and the coefficients of tau_star (Earth rotation)
   ProjEv pj;
   GridEv g;
   ArmPat apc[NARM];
@@ -833,6 +836,12 @@ __device__ inline void f64_prepare(const DetDev& det, const unsigned char* scrat
     if (threadIdx.x == 0) {
       time_state(S.pj, S.pj.tc, S.tsc);
       for (int a = 0; a < NARM; ++a) arm_pattern(S.pj, det.sin_zeta, S.tsc.x, a, S.apc[a]);
+    }
+  }
+  if constexpr (EARTH && (MODEL == 0 || MODEL == 1)) {
+    if (threadIdx.x == 32 && S.g.ok) {
+      if constexpr (MODEL == 0) tau_setup_d(S.td, S.E.tf2.Ms, S.E.tf2.vM, S.E.tf2.eta);
+      else tau_setup_d(S.td, S.E.phd.k.Ms, S.E.phd.k.vM, S.E.phd.k.eta);
     }
   }
   if (threadIdx.x == 0) S.rec = rec;
@@ -883,7 +892,8 @@ __device__ inline void f64_item(const EvBatch& ev, const DetDev& det, F64State<N
       DualOf<MODEL> tau(0.0);
       double phi0;
       wave_point_dual<MODEL, EARTH>(S.E, S.pj, f, lnf, P, C, dP, dC, dPi, dCi, tau, phi0,
-                                    (MODEL == 0 || MODEL == 1) ? &S.pb : nullptr);
+                                    (MODEL == 0 || MODEL == 1) ? &S.pb : nullptr,
+                                    (MODEL == 0 || MODEL == 1) ? &S.td : nullptr);
       double dtn[NI];
 #pragma unroll
       for (int q = 0; q < NI; ++q) dtn[q] = 0.0;

@@ -1381,6 +1381,12 @@ struct F64GroupState {
 template <int MODEL, bool EARTH>
 __device__ inline void f64g_prepare(const GroupDev64& g, long long rec, F64GroupState<MODEL, EARTH>& G) {
   block_load<MODEL>(G.S.E, G.S.pj, G.S.g, g.rec[0], rec, (MODEL == 0 || MODEL == 1) ? &G.S.pb : nullptr);
+  if constexpr (EARTH && (MODEL == 0 || MODEL == 1)) {
+    if (threadIdx.x == 32 && G.S.g.ok) {
+      if constexpr (MODEL == 0) tau_setup_d(G.S.td, G.S.E.tf2.Ms, G.S.E.tf2.vM, G.S.E.tf2.eta);
+      else tau_setup_d(G.S.td, G.S.E.phd.k.Ms, G.S.E.phd.k.vM, G.S.E.phd.k.eta);
+    }
+  }
   if ((int)threadIdx.x < g.nd) {
     const int d = threadIdx.x;
     G.pj[d] = reinterpret_cast<const SetupHdr*>(g.rec[d] + rec * rec_stride<MODEL>())->pj;
@@ -1448,7 +1454,8 @@ __device__ inline void f64g_item(const EvBatch& ev, const GroupDev64& g, F64Grou
     if (valid) {
       grid_point(G.S.g, ev.spacing, k, f, lnf, w);
       wave_point_dual<MODEL, EARTH>(G.S.E, G.S.pj, f, lnf, P, C, dP, dC, dPi, dCi, tau, phi0,
-                                    (MODEL == 0 || MODEL == 1) ? &G.S.pb : nullptr);
+                                    (MODEL == 0 || MODEL == 1) ? &G.S.pb : nullptr,
+                                    (MODEL == 0 || MODEL == 1) ? &G.S.td : nullptr);
       if (EARTH) {
 #pragma unroll
         for (int q = 0; q < NI; ++q) dtn[q] = -tau.d[q] / kDay;
