@@ -471,7 +471,7 @@ __device__ __forceinline__ void wave_point_dual(const EvUnion& E, const ProjEv& 
         A = t.ampK * exp(lnf * (-7.0 / 6.0));
         if (EARTH) tau = td ? tau_point_d(*td, exp(lnf / 3.0), lnf) : tau_star_point<D4>(t.Ms, t.vM, t.eta, exp(lnf / 3.0));
       } else if constexpr (MODEL == 1) {
-        A = phd_amp_point<D4>(E.phd.k, f);
+        A = td ? phd_amp_d(E.phd.k, *td, f) : phd_amp_point<D4>(E.phd.k, f);
         if (EARTH)
           tau = td ? tau_point_d(*td, exp(lnf / 3.0), lnf)
                    : tau_star_point<D4>(E.phd.k.Ms, E.phd.k.vM, E.phd.k.eta, exp(lnf / 3.0));
@@ -838,10 +838,13 @@ __device__ inline void f64_prepare(const DetDev& det, const unsigned char* scrat
       for (int a = 0; a < NARM; ++a) arm_pattern(S.pj, det.sin_zeta, S.tsc.x, a, S.apc[a]);
     }
   }
-  if constexpr (EARTH && (MODEL == 0 || MODEL == 1)) {
+  if constexpr (MODEL == 0 || MODEL == 1) {
     if (threadIdx.x == 32 && S.g.ok) {
       if constexpr (MODEL == 0) tau_setup_d(S.td, S.E.tf2.Ms, S.E.tf2.vM, S.E.tf2.eta);
-      else tau_setup_d(S.td, S.E.phd.k.Ms, S.E.phd.k.vM, S.E.phd.k.eta);
+      else {
+        tau_setup_d(S.td, S.E.phd.k.Ms, S.E.phd.k.vM, S.E.phd.k.eta);
+        amp_setup_d(S.td, S.E.phd.k.ampPref, S.E.phd.k.MG);
+      }
     }
   }
   if (threadIdx.x == 0) S.rec = rec;

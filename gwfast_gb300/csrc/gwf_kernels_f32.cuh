@@ -1381,10 +1381,13 @@ struct F64GroupState {
 template <int MODEL, bool EARTH>
 __device__ inline void f64g_prepare(const GroupDev64& g, long long rec, F64GroupState<MODEL, EARTH>& G) {
   block_load<MODEL>(G.S.E, G.S.pj, G.S.g, g.rec[0], rec, (MODEL == 0 || MODEL == 1) ? &G.S.pb : nullptr);
-  if constexpr (EARTH && (MODEL == 0 || MODEL == 1)) {
+  if constexpr (MODEL == 0 || MODEL == 1) {
     if (threadIdx.x == 32 && G.S.g.ok) {
       if constexpr (MODEL == 0) tau_setup_d(G.S.td, G.S.E.tf2.Ms, G.S.E.tf2.vM, G.S.E.tf2.eta);
-      else tau_setup_d(G.S.td, G.S.E.phd.k.Ms, G.S.E.phd.k.vM, G.S.E.phd.k.eta);
+      else {
+        tau_setup_d(G.S.td, G.S.E.phd.k.Ms, G.S.E.phd.k.vM, G.S.E.phd.k.eta);
+        amp_setup_d(G.S.td, G.S.E.phd.k.ampPref, G.S.E.phd.k.MG);
+      }
     }
   }
   if ((int)threadIdx.x < g.nd) {

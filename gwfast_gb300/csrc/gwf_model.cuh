@@ -287,16 +287,19 @@ __device__ __forceinline__ S tau_star_point(const C& Ms, const C& vM, const C& e
   return pre * (t05 + t6 + t7);
 }
 
-// tau_star in the FP64 Fisher kernels (TaylorF2, IMRPhenomD): the polynomial above with per-event
-// coefficients, so that a point costs a few FMAs instead of the four-direction dual evaluation.
-// tau = T0 v^-8 P(v), T0 = (5/256) Ms / eta, v = vM f^(1/3), P(v) = 1 + sum_{k=2..7} a_k v^k (a_6 with
-// its a6l ln(16 v^2) part); the parameters enter only through Ms, eta and vM, and v's tangent is
-// v d ln vM, so d tau = tau d ln T0 + T0 v^-8 [(v P' - 8 P) d ln vM + (dP/deta) d eta].
+// Per-event coefficients of the FP64 Fisher kernels' point evaluation (TaylorF2, IMRPhenomD), formed
+// in the CTA prologue so that a point costs a few FMAs instead of four-direction dual arithmetic.
+// tau_star: the polynomial above, tau = T0 v^-8 P(v), T0 = (5/256) Ms / eta, v = vM f^(1/3),
+// P(v) = 1 + sum_{k=2..7} a_k v^k (a_6 with its a6l ln(16 v^2) part); the parameters enter only
+// through Ms, eta and vM, and v's tangent is v d ln vM, so
+//   d tau = tau d ln T0 + T0 v^-8 [(v P' - 8 P) d ln vM + (dP/deta) d eta].
+// IMRPhenomD's inspiral amplitude (phd_amp_d): the log-derivatives of its prefactor and of MG.
 struct TauD {
   double T0, lg0;        // (5/256) Ms / eta; ln 16 + 2 ln vM (ln(16 v^2) = lg0 + 2/3 ln f)
   double vM;
   double a[6], b[6];     // a_2..a_7 (a_6 without its log term) and their eta derivatives
   double dlnT0[4], dlnv[4], deta[4];
+  double dlnP[4], dlnMG[4];   // d ln ampPref, d ln MG (IMRPhenomD)
 };
 constexpr double kTauA6ld = 3424.0 / 105.0;
 
@@ -323,6 +326,15 @@ __device__ inline void tau_setup_d(TauD& t, const D4& Ms, const D4& vM, const D4
     t.dlnT0[q] = Ms.d[q] * ims - eta_.d[q] * ieta;
     t.dlnv[q] = vM.d[q] * ivm;
     t.deta[q] = eta_.d[q];
+  }
+}
+
+// the amplitude part of TauD (IMRPhenomD)
+__device__ inline void amp_setup_d(TauD& t, const D4& ampPref, const D4& MG) {
+  const double ip = 1.0 / ampPref.v, img = 1.0 / MG.v;
+  for (int q = 0; q < 4; ++q) {
+    t.dlnP[q] = ampPref.d[q] * ip;
+    t.dlnMG[q] = MG.d[q] * img;
   }
 }
 
@@ -675,6 +687,35 @@ __device__ __forceinline__ S phd_amp_point(const PhdCoreT<C>& k, typename Real<S
   typedef typename Real<S>::T T;
   const S x = co<S>(k.MG) * f;
   return co<S>(k.ampPref) * (T(1) / (x * dsqrt(dcbrt(x)))) * complete_amp_shape(k, x);
+}
+
+// IMRPhenomD amplitude with its tangent in FP64 (the FP64 Fisher kernels). In the inspiral region
+// A = ampPref x^(-7/6) S(x), S = 1 + sum_k c_k x^(k/3) (k = 2..9; c_k = a23, a1, a43, a53, a2, r1, r2,
+// r3), x = MG f with tangent x d ln MG, so
+//   d ln A = d ln ampPref + (-7/6 + x S'(x) / S) d ln MG + (sum_k d c_k x^(k/3)) / S
+// (t: the event's log-derivatives of ampPref and MG); elsewhere the dual evaluation.
+__device__ __forceinline__ D4 phd_amp_d(const PhdCore& k, const TauD& t, double f) {
+  const double xv = k.MG.v * f;
+  if (!(xv < kAmpFJoin)) return phd_amp_point<D4>(k, f);
+  const double x13 = cbrt(xv), x23 = x13 * x13, x2 = xv * xv;
+  const double bas[8] = {x23, xv, xv * x13, xv * x23, x2, x2 * x13, x2 * x23, x2 * xv};
+  const D4* c[8] = {&k.a23, &k.a1, &k.a43, &k.a53, &k.a2, &k.r1, &k.r2, &k.r3};
+  double S = 1.0, xS = 0.0, T[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const double cb = c[j]->v * bas[j];
+    S += cb;
+    xS = fma((double)(j + 2) * (1.0 / 3.0), cb, xS);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) T[q] = fma(c[j]->d[q], bas[j], T[q]);
+  }
+  const double iS = 1.0 / S;
+  D4 A;
+  A.v = k.ampPref.v * S / (xv * sqrt(x13));
+  const double gx = -7.0 / 6.0 + xS * iS;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) A.d[q] = A.v * (t.dlnP[q] + gx * t.dlnMG[q] + T[q] * iS);
+  return A;
 }
 
 // ------------------------------------------------------------------ phase tangent in a frequency basis
