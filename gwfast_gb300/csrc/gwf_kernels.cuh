@@ -587,15 +587,15 @@ __device__ __forceinline__ void wave_point_val(const EvUnion& E, const ProjEv& p
       if (MODEL == 4) nrt_point<double>(E.nrt, f, A, Phi);
       else nsbh_point<double>(E.nsbh, f, A, Phi);
       if (EARTH) tau = tau_star_point<double>(kc.Ms, kc.vM, kc.eta, exp(lnf / 3.0));
-    } else if (is_tf2<MODEL>()) {
+    } else if (is_tf2<MODEL>()) {   // (the phase does not enter |h|: amplitudes only)
       const TF2Ev& t = tf2_base<MODEL>(E);
-      const double f13 = exp(lnf / 3.0);
-      tf2_point<double>(t, f, f13, lnf, exp(lnf * (-7.0 / 6.0)), A, Phi);
-      if (EARTH) tau = tau_star_point<double>(t.Ms, t.vM, t.eta, f13);
+      A = t.ampK.v * exp(lnf * (-7.0 / 6.0));
+      if (EARTH) tau = tau_star_point<double>(t.Ms, t.vM, t.eta, exp(lnf / 3.0));
     } else {
-      phd_point<double>(E.phd.k, f, A, Phi);
+      A = phd_amp_point<double>(E.phd.k, f);
       if (EARTH) tau = tau_star_point<double>(E.phd.k.Ms, E.phd.k.vM, E.phd.k.eta, exp(lnf / 3.0));
     }
+    (void)Phi;
     ap = A * pj.cp;
     ac = A * pj.ci;
   }
