@@ -30,10 +30,10 @@ inline int device_sms() {
 // (2 per SM), 0.416 ms at 4 warps per SM, 0.61 ms at 8 and 1.43 ms at 32.
 constexpr int kEvWarpsPerSM = 4;
 constexpr int kEvMinLanes = 4;
-// the FP32 record kernel (setup_f32_kernel) does less FP64 work per event (its conversions run on
-// the integer pipe) and moves ~3 KB per event, but its remaining FP64 work still sets its time: the
-// L1 + H1 set-up section (10^4 events) took 0.341 ms at 4 warps per SM, 0.359 at 8, 0.404 at 16
-// and 0.470 at 32
+// the FP32 record kernel (setup_f32_kernel) does little FP64 work per event (its conversions run on
+// the integer pipe; FP64 pipe 23 % busy) and moves ~3 KB per event; more warps per SM still do not
+// pay: the L1 + H1 set-up section (10^4 events) took 0.326 ms at 4 warps per SM, 0.330 at 8 and
+// 0.341 at 16
 constexpr int kRecWarpsPerSM = 4;
 inline int ev_lanes(long long cnt, int warps_per_sm = kEvWarpsPerSM) {
   const long long warps = (long long)warps_per_sm * device_sms();
