@@ -660,22 +660,24 @@ __device__ inline void hm_round(const HMEv& s, HMF32& d, double amp, double alph
 // short polynomial instead of its own cube root and logarithm.
 struct InsShared { double x13, ix13, lx, ixp; };
 
-__device__ __forceinline__ double ins_phase_scaled(const PhdCoreT<double>& k, const InsShared& b, double x, int m) {
+// (1 / ai = m / 2 exactly; ieta = 1 / eta, formed once per point: the FP64 pipe sets this kernel's
+// speed, and each FP64 division is a dozen of its instructions)
+__device__ __forceinline__ double ins_phase_scaled(const PhdCoreT<double>& k, const InsShared& b, double x, int m,
+                                                   double ieta) {
   // cbrt(ai), 1 / cbrt(ai), log(ai) for ai = 2 / m, m = 1..4
   constexpr double kCb[5] = {0.0, 1.2599210498948731648, 1.0, 0.87358046473629886905, 0.79370052598409973738};
   constexpr double kICb[5] = {0.0, 0.79370052598409973738, 1.0, 1.1447142425533318678, 1.2599210498948731648};
   constexpr double kLg[5] = {0.0, 0.69314718055994530942, 0.0, -0.40546510810816438198, -0.69314718055994530942};
-  const double ai = 2.0 / m;
   const double x13 = b.x13 * kCb[m];
   const double ix13 = b.ix13 * kICb[m];
   const double ix23 = ix13 * ix13;
-  const double ixp = b.ixp / ai;
+  const double ixp = b.ixp * (0.5 * m);
   const double lx = (b.lx + kLg[m]) * (1.0 / 3.0);
   const double tf2 = ix23 * ixp + k.pn.c2 * ixp + k.pn.c3 * ix23 + k.pn.c4 * ix13 + k.pn.c5 + k.pn.c5l * lx
                      + (k.pn.c6 + k.pn.c6l * lx) * x13 + k.pn.c7 * x13 * x13;
   const double m13 = x13 * 0.68278406325529573;
   return k.pn.A * tf2 + (k.sig[0] * x + 0.75 * k.sig[1] * x * m13 + 0.6 * k.sig[2] * x * m13 * m13
-                         + 0.5 * k.sig[3] * x * x) / k.eta;
+                         + 0.5 * k.sig[3] * x * x) * ieta;
 }
 
 // IMRPhenomHM at one point, FP32 form: the detector-independent part (as wave_f32). Q = P - s C is
@@ -690,6 +692,8 @@ __device__ __forceinline__ void wave_f32_hm(const HMF32& H, const ProjF& pf, con
   const double lin64 = v.k.t0 * (x64 - v.k.fRef);
   const DF4 lin = e.k.t0 * (x - e.k.fRef);
   const bool spos = pf.sgn > 0.0f;
+  constexpr double kAi[5] = {0.0, 2.0, 1.0, 2.0 / 3.0, 0.5};   // ai = 2 / m
+  const double ieta = 1.0 / v.k.eta;
   InsShared ins;
   if (x64 < 2.0 * kPhiFJoin) {   // some mode argument x * 2 / m lies in the inspiral region
     const double xp = kPi * x64;
@@ -707,7 +711,7 @@ __device__ __forceinline__ void wave_f32_hm(const HMF32& H, const ProjF& pf, con
   for (int mode = 0; mode < 6; ++mode) {
     const HMModeT<DF4>& m = e.md[mode];
     const HMModeT<double>& mv = v.md[mode];
-    const double ai64 = 2.0 / mv.m;
+    const double ai64 = kAi[mv.m];
     const float ai = 2.0f / (float)m.m;
     // amplitude: frequency map chosen on the FP64 argument, as the FP64 kernel does
     DF4 fs;
@@ -724,8 +728,8 @@ __device__ __forceinline__ void wave_f32_hm(const HMF32& H, const ProjF& pf, con
     DF4 ph;
     if (x64 < mv.fip) {
       const double xa = x64 * ai64;
-      ph64 = (xa < kPhiFJoin ? ins_phase_scaled(v.k, ins, xa, mv.m)
-                             : complete_phase<double>(v.k, xa, mv.C1, mv.C2, mv.rho, mv.tau)) / ai64;
+      ph64 = (xa < kPhiFJoin ? ins_phase_scaled(v.k, ins, xa, mv.m, ieta)
+                             : complete_phase<double>(v.k, xa, mv.C1, mv.C2, mv.rho, mv.tau)) * (0.5 * mv.m);
       ph = complete_phase<DF4>(e.k, x * ai, m.C1, m.C2, m.rho, m.tau) / ai;
     } else if (x64 < mv.frlm) {
       ph64 = mv.PhDBA - mv.PhDB + complete_phase<double>(v.k, x64 * mv.amp_ + mv.bmp, mv.C1, mv.C2, mv.rho, mv.tau) / mv.amp_;
@@ -738,7 +742,7 @@ __device__ __forceinline__ void wave_f32_hm(const HMF32& H, const ProjF& pf, con
     ph = ph - lin - (float)m.m * e.phi0;   // its value is not used
     const double red = ph64 - kTwoPi * rint(ph64 * (1.0 / kTwoPi));
     float sn, cs;
-    sincosf((float)red, &sn, &cs);
+    sincosf(f32_rn(red), &sn, &cs);
     // mode term amp e^{-i phase} and its tangent (d amp - i amp d phase) e^{-i phase}
     const float a = amp.v;
     const cf M = {a * cs, -a * sn};
