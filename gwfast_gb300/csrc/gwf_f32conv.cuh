@@ -1,10 +1,11 @@
 // FP64 -> FP32 rounding with integer instructions.
 //
-// The per-event FP32 record kernel is bound by the FP64 pipe (one warp per scheduler), and the
-// double -> float conversion instruction issues on that pipe. These functions do the same IEEE
-// round-to-nearest-even on the bit patterns with 32-bit integer operations (ALU pipe) for results
-// in the normal FP32 range, and hand every other case (zero, FP32 subnormal or overflow, infinity,
-// NaN) to the conversion instruction, so the result is the same bit pattern as a plain cast.
+// The double -> float conversion instruction issues on the FP64 pipe, which bounds the kernels that
+// use it most (the per-event FP32 records, the condition estimate's FP32 factor, the FP32 form of
+// IMRPhenomHM with its FP64 mode phases). These functions do the same IEEE round-to-nearest-even on
+// the bit patterns with 32-bit integer operations (ALU pipe) for results in the normal FP32 range,
+// and hand every other case (FP32 subnormal or overflow, infinity, NaN) to the conversion
+// instruction; signed zeros stay on the integer path. The result is the bit pattern of a plain cast.
 //
 // Bit layout: double = sign | 11-bit exponent e (bias 1023) | 52-bit mantissa; float = sign |
 // 8-bit exponent (bias 127) | 23-bit mantissa. A double with e in [897, 1150] rounds to a normal
