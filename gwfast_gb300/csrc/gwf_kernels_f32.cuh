@@ -586,6 +586,9 @@ __device__ __forceinline__ void point_f32(const EvUnionF& EF, const PBF& pbf, co
 struct HMF32 {
   HMEvT<DF4> e32;
   HMEvT<double> e64;
+  // per mode: 1 / amp_, 1 / rho and 1 / (fdamp rho tau), so that the FP64 mode phases divide only by
+  // the frequency (complete_phase_hm64)
+  double inv_amp[6], inv_rho[6], iden[6];
 };
 struct NoRec {};
 
@@ -650,6 +653,9 @@ __device__ inline void hm_round(const HMEv& s, HMF32& d, double amp, double alph
     fm.yp = vm.yp = sm.yp; fm.yc = vm.yc = sm.yc; fm.dyp = vm.dyp = sm.dyp; fm.dyc = vm.dyc = sm.dyc;
     fm.ysp = vm.ysp = sm.ysp; fm.ysm = vm.ysm = sm.ysm; fm.shift = vm.shift = sm.shift;
     fm.l = vm.l = sm.l; fm.m = vm.m = sm.m;
+    d.inv_amp[m] = 1.0 / sm.amp_.v;
+    d.inv_rho[m] = 1.0 / sm.rho.v;
+    d.iden[m] = 1.0 / (s.k.fdamp.v * sm.rho.v * sm.tau.v);
   }
 }
 
@@ -678,6 +684,23 @@ __device__ __forceinline__ double ins_phase_scaled(const PhdCoreT<double>& k, co
   const double m13 = x13 * 0.68278406325529573;
   return k.pn.A * tf2 + (k.sig[0] * x + 0.75 * k.sig[1] * x * m13 + 0.6 * k.sig[2] * x * m13 * m13
                          + 0.5 * k.sig[3] * x * x) * ieta;
+}
+
+// complete_phase<double> for the FP32 form's mode phases with the event's reciprocals (ieta = 1 / eta,
+// iden = 1 / (fdamp rho tau)): the intermediate and merger-ringdown pieces then divide only by x
+__device__ __forceinline__ double complete_phase_hm64(const PhdCoreT<double>& k, double x, double C1, double C2,
+                                                      double rho, double iden, double ieta) {
+  if (x < kPhiFJoin) return ins_phase<double>(k, x);
+  if (x < k.fMRD) {
+    const double ix = 1.0 / x;
+    return (k.bet[0] * x - k.bet[2] * (1.0 / 3.0) * ix * ix * ix + k.bet[1] * log(x)) * ieta + k.C1Int + k.C2Int * x;
+  }
+  if (x < kMfCut) {
+    const double x14 = sqrt(sqrt(x));
+    return (-k.alp[1] / x + (4.0 / 3.0) * k.alp[2] * x14 * x14 * x14 + k.alp[0] * x
+            + k.alp[3] * rho * atan((x - k.alp[4] * k.fring) * iden)) * ieta + C1 + C2 * x;
+  }
+  return 0.0;
 }
 
 // IMRPhenomHM at one point, FP32 form: the detector-independent part (as wave_f32). Q = P - s C is
@@ -729,13 +752,15 @@ __device__ __forceinline__ void wave_f32_hm(const HMF32& H, const ProjF& pf, con
     if (x64 < mv.fip) {
       const double xa = x64 * ai64;
       ph64 = (xa < kPhiFJoin ? ins_phase_scaled(v.k, ins, xa, mv.m, ieta)
-                             : complete_phase<double>(v.k, xa, mv.C1, mv.C2, mv.rho, mv.tau)) * (0.5 * mv.m);
+                             : complete_phase_hm64(v.k, xa, mv.C1, mv.C2, mv.rho, H.iden[mode], ieta)) * (0.5 * mv.m);
       ph = complete_phase<DF4>(e.k, x * ai, m.C1, m.C2, m.rho, m.tau) / ai;
     } else if (x64 < mv.frlm) {
-      ph64 = mv.PhDBA - mv.PhDB + complete_phase<double>(v.k, x64 * mv.amp_ + mv.bmp, mv.C1, mv.C2, mv.rho, mv.tau) / mv.amp_;
+      ph64 = mv.PhDBA - mv.PhDB
+             + complete_phase_hm64(v.k, x64 * mv.amp_ + mv.bmp, mv.C1, mv.C2, mv.rho, H.iden[mode], ieta) * H.inv_amp[mode];
       ph = m.PhDBA - m.PhDB + complete_phase<DF4>(e.k, x * m.amp_ + m.bmp, m.C1, m.C2, m.rho, m.tau) / m.amp_;
     } else {
-      ph64 = mv.phC - mv.PhDC + complete_phase<double>(v.k, x64 * mv.rho, mv.C1, mv.C2, mv.rho, mv.tau) / mv.rho;
+      ph64 = mv.phC - mv.PhDC
+             + complete_phase_hm64(v.k, x64 * mv.rho, mv.C1, mv.C2, mv.rho, H.iden[mode], ieta) * H.inv_rho[mode];
       ph = m.phC - m.PhDC + complete_phase<DF4>(e.k, x * m.rho, m.C1, m.C2, m.rho, m.tau) / m.rho;
     }
     ph64 = ph64 - lin64 - (double)mv.m * v.phi0 + mv.shift;
