@@ -1355,10 +1355,12 @@ __device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32S
 // Six blocks per SM (80 registers) for the 22-mode models: the fixed-latency FP32 chains are its top
 // stall and two more warps per SM outweigh the extra spills (IMRPhenomD, L1 + H1, 10^4 events:
 // 2.688 ms against 2.729 ms at five blocks and 96 registers; seven blocks, 72 registers, 2.45 ms
-// against 2.39 ms once the compact waveform cut the spills); IMRPhenomHM, with its FP64 mode phases,
-// keeps five. (The triangle kernel was slower at six: 2.390 against 2.305 ms.)
+// against 2.39 ms once the compact waveform cut the spills). IMRPhenomHM as well, since its FP64 mode
+// phases lost their divisions (ETS + CE1Id + CE2NM, 2 * 10^4 events: FP32 form 178.7 k Fisher/s at
+// six blocks, 175.4 k at five, 168.9 k at four). (The triangle kernel was slower at six: 2.390
+// against 2.305 ms.)
 template <int MODEL>
-__host__ __device__ constexpr int group_min_blocks() { return MODEL == 2 ? 5 : 6; }
+__host__ __device__ constexpr int group_min_blocks() { return 6; }
 
 template <int MODEL, bool EARTH, bool TRI>
 __global__ void __launch_bounds__(kThreads, group_min_blocks<MODEL>()) fisher_group_kernel_f32(EvBatch ev, GroupDev g,
