@@ -1357,8 +1357,8 @@ __device__ inline void f32_item_group(const EvBatch& ev, const GroupDev& g, F32S
 // 2.688 ms against 2.729 ms at five blocks and 96 registers; seven blocks, 72 registers, 2.45 ms
 // against 2.39 ms once the compact waveform cut the spills). IMRPhenomHM as well, since its FP64 mode
 // phases lost their divisions (ETS + CE1Id + CE2NM, 2 * 10^4 events: FP32 form 178.7 k Fisher/s at
-// six blocks, 175.4 k at five, 168.9 k at four). (The triangle kernel was slower at six: 2.390
-// against 2.305 ms.)
+// six blocks, 175.4 k at five, 168.9 k at four; 174.5 k at seven against 178.4 k at six in another
+// run). (The triangle kernel was slower at six: 2.390 against 2.305 ms.)
 template <int MODEL>
 __host__ __device__ constexpr int group_min_blocks() { return 6; }
 
